@@ -1,0 +1,152 @@
+/* ngbem_gb300: C-ABI of the GB300-native boundary-element operator path.
+ *
+ * Drop-in boundary for ngbem's operator construction and H-matrix application
+ * (Weggler/ngbem).  Each entry point names the reference interface it replaces.
+ * Conventions:
+ *   - every function returns an int status (BEM_OK = 0); bem_last_error() gives a
+ *     thread-local message for the last failure; no C++ exception crosses this ABI;
+ *   - handles are opaque; host arrays are caller-owned; vectors are float64 (real
+ *     operators) or interleaved complex128 (complex operators);
+ *   - device pointers and cudaStream_t are passed as void*.
+ */
+#ifndef NGBEM_GB300_H
+#define NGBEM_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define BEM_OK 0
+#define BEM_ERR_ARG 1      /* invalid argument */
+#define BEM_ERR_CUDA 2     /* CUDA runtime failure or no device */
+#define BEM_ERR_ALLOC 3    /* device or host allocation failed */
+#define BEM_ERR_STATE 4    /* call not valid for this object */
+#define BEM_ERR_INTERNAL 5 /* device-side check failed (capacity, rank cap, ...) */
+
+/* kernel ids: reference src/ngbem.hpp:226-434 (LaplaceSL/DL/HS, HelmholtzSL/DL/HS,
+ * CombinedField, MaxwellSL) */
+enum {
+  BEM_LAPLACE_SL = 0, BEM_LAPLACE_DL = 1, BEM_LAPLACE_HS = 2,
+  BEM_HELMHOLTZ_SL = 3, BEM_HELMHOLTZ_DL = 4, BEM_HELMHOLTZ_HS = 5,
+  BEM_HELMHOLTZ_CF = 6, BEM_MAXWELL_SL = 7
+};
+/* trace spaces: SurfaceL2 order 0 (P0), H1 order 1 trace (P1), HDivSurface order 0 (RT0) */
+enum { BEM_P0 = 0, BEM_P1 = 1, BEM_RT0 = 2 };
+/* trace evaluators: GetEvaluator(BND) (ID), DiffOpBoundaryRot (ROT), DiffOpHelmholtz (HELM),
+ * DiffOpMaxwellNew (MAXWELL); reference src/diffops.hpp:12-338 */
+enum { BEM_EV_ID = 0, BEM_EV_ROT = 1, BEM_EV_HELM = 2, BEM_EV_MAXWELL = 3 };
+/* precision modes: plain FP64 on the GPU, or mixed (FP64 singular pairs, FP32 regular
+ * near field, ACA and factors) */
+enum { BEM_FP64 = 0, BEM_MIXED = 1 };
+/* assembly methods (reference python_bem.cpp:30-33: "dense" = one root block) */
+enum { BEM_METHOD_ACA = 0, BEM_METHOD_DENSE = 1 };
+
+typedef struct bem_mesh_s* bem_mesh_t;
+typedef struct bem_space_s* bem_space_t;
+typedef struct bem_operator_s* bem_operator_t;
+
+/* BEMParameters (reference src/ngbem.hpp:13-27) plus the GB300 extensions. */
+typedef struct {
+  int intorder;           /* reference intorder: both rules unless overridden */
+  int intorder_singular;  /* <= 0: intorder.  Sauter-Schwab rules */
+  int intorder_regular;   /* <= 0: intorder.  disjoint tensor rule and far-field points */
+  int leafsize;           /* minimal cluster size (reference default 40) */
+  double eta;             /* admissibility parameter (default 2) */
+  double eps;             /* ACA tolerance (default 1e-6) */
+  int method;             /* BEM_METHOD_ACA or BEM_METHOD_DENSE */
+  int precision;          /* BEM_FP64 or BEM_MIXED */
+  int max_rank;           /* ACA rank cap per block; a block reaching it is assembled densely (0: 128) */
+  double aca_eps_floor;   /* mixed precision: ACA tolerance floor (0: 2e-7) */
+  long long scratch_bytes;/* ACA scratch budget in bytes (0: 4 GiB) */
+} bem_params_t;
+
+/* Assembly and storage summary (reference HMatrix::NZE, src/hmat.cpp:623-630). */
+typedef struct {
+  int is_complex;
+  int height, width;           /* test ndof, trial ndof */
+  int nblocks, nnear, nfar, nfallback;
+  long long nze;               /* sum m*n (dense) + r*(m+n) (low rank) */
+  int max_rank;
+  long long sum_rank;
+  long long bytes_dense, bytes_lowrank;  /* device storage */
+  int n_singular_pairs;        /* Sauter-Schwab element pairs assembled */
+  long long n_regular_pairs;   /* disjoint element pairs assembled (tensor rule) */
+  double ms_setup, ms_aca, ms_nearfield, ms_projection, ms_total;  /* assembly phases */
+} bem_operator_info_t;
+
+/* Fill *p with the reference defaults (intorder 3, leafsize 40, eta 2, eps 1e-6, aca). */
+int bem_params_default(bem_params_t* p);
+
+/* Mesh of flat triangles; vertex order per triangle defines the outward normal.
+ * Replaces NGSolve MeshAccess for the surface (reference src/ngbem.cpp:33-34). */
+int bem_mesh_create(int nv, const double* xyz, int nt, const int* tri, bem_mesh_t* out);
+int bem_mesh_num_edges(bem_mesh_t mesh, int* ne);
+int bem_mesh_destroy(bem_mesh_t mesh);
+
+/* Trace space on a mesh (replaces the NGSolve FESpace argument of the factories,
+ * reference src/python_bem.cpp:27-173).  RT0 dofs are edges numbered by first
+ * appearance (element order, local edges (0,1),(1,2),(2,0)). */
+int bem_space_create(bem_mesh_t mesh, int kind, int dual_mapping, bem_space_t* out);
+int bem_space_ndof(bem_space_t space, int* ndof);
+int bem_space_destroy(bem_space_t space);
+
+/* Cluster tree of a space (reference ClusterTree ctor, src/hmat.cpp:409-453); host only.
+ * perm: ndof ints (mapcluster2glob).  ci: 7 longs per cluster (Level, Parent, Child1,
+ * Child2, Number, PermuPos, BasisElement).  cd: 23 doubles per cluster (Radius, EVec[9],
+ * EVal[3], XMin[3], XMax[3], Centre[3], DiagLength). */
+int bem_cluster_tree(bem_space_t space, int leafsize, int* perm, int max_clusters,
+                     int* nclusters, long* ci, double* cd);
+
+/* Block partition (reference HMatrix ctor / HMatrix_help, src/hmat.cpp:587-621); host only.
+ * Returns blocks in the reference order: row (test) cluster, col (trial) cluster, near flag. */
+int bem_partition(bem_space_t trial, bem_space_t test, int leafsize, double eta, int max_blocks,
+                  int* nblocks, int* rowcl, int* colcl, int* near);
+
+/* Operator construction = assembly on the GPU (reference GenericIntegralOperator ctor,
+ * src/ngbem.cpp:314-330, and CalcHMatrix :118-157; factories src/python_bem.cpp:27-173).
+ * test may equal trial.  Synchronous: returns when the H-matrix is resident in HBM. */
+int bem_operator_create(int kernel, double kappa, bem_space_t trial, bem_space_t test,
+                        int trial_eval, int test_eval, const bem_params_t* params,
+                        bem_operator_t* out);
+
+/* Galerkin mass matrix <u, v> of identity traces as a sparse operator (replaces the NGSolve
+ * BilinearForm(u*v*ds) used beside the BEM operators, e.g. reference tests/test_Laplace.py:50).
+ * complex_vectors: 1 if it acts on complex128 vectors. */
+int bem_mass_create(bem_space_t trial, bem_space_t test, int complex_vectors, bem_operator_t* out);
+
+int bem_operator_info(bem_operator_t op, bem_operator_info_t* info);
+
+/* Block list after assembly: row/col cluster, near flag, rank (-1 dense), dense fallback. */
+int bem_operator_blocks(bem_operator_t op, int* rowcl, int* colcl, int* near, int* rank,
+                        int* fallback);
+
+/* y = alpha * op(A) x + beta * y on the device (reference HMatrix::Mult / MultAdd /
+ * MultTrans / MultTransAdd, src/hmat.cpp:632-666).  trans=1 is the plain transpose (no
+ * conjugation).  alpha/beta point to (re, im) pairs.  nrhs column-major right-hand sides
+ * (leading dimension = vector length).  Stream-ordered, asynchronous. */
+int bem_operator_mult(bem_operator_t op, int trans, const double* alpha, const void* x,
+                      const double* beta, void* y, int nrhs, void* stream);
+
+/* Same with HOST buffers: copies x up, applies, copies y back (synchronous). */
+int bem_operator_mult_host(bem_operator_t op, int trans, const double* alpha, const void* x,
+                           const double* beta, void* y, int nrhs);
+
+/* Dense height x width matrix of the operator (row-major, host), for small cases. */
+int bem_operator_to_dense(bem_operator_t op, void* out);
+
+int bem_operator_destroy(bem_operator_t op);
+
+/* Restarted GMRES on A = sum_k coef[k] * ops[k] (ngsolve.krylovspace.GMRes as used by the
+ * reference tests, e.g. tests/test_Laplace.py:60).  b, x: device vectors; x holds the
+ * initial guess.  FP64 Arnoldi with classical Gram-Schmidt and re-orthogonalisation; the
+ * operator application is replayed from a CUDA graph.  coef: 2*nterms doubles (re, im).
+ * iters/resid: iterations done and final relative residual. */
+int bem_gmres(int nterms, const bem_operator_t* ops, const double* coef, const void* b, void* x,
+              int maxiter, int restart, double tol, int* iters, double* resid, void* stream);
+
+const char* bem_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

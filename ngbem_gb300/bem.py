@@ -1,0 +1,555 @@
+"""Python mirror of ngbem's operator API (reference src/python_bem.cpp:11-194).
+
+Factories keep the reference names, argument order, keyword names and defaults
+(intorder=3, leafsize=40, eta=2., eps=1e-6, method="aca", testhmatrix=False).  The NGSolve
+FESpace argument becomes a trace space on a flat triangle mesh (SurfaceL2 order 0 = P0,
+H1 order 1 = P1, HDivSurface order 0 = RT0).  ``.mat`` is an H-matrix resident in GPU
+memory with the BaseMatrix surface the reference's callers use: Mult, MultAdd, MultTrans,
+MultTransAdd, ``*``, ``.T``, ``nze``, CreateRowVector, CreateColVector, and sums/scalings
+of matrices (``0.5 * M.mat + K.mat``).
+
+GB300 extensions (keyword-only): precision ("fp64" plain path or "mixed"),
+intorder_singular / intorder_regular (separate Sauter-Schwab and regular orders),
+max_rank (ACA rank cap; capped blocks are assembled densely), aca_eps_floor.
+
+Vectors are torch tensors on the GPU (float64 or complex128); numpy arrays are accepted and
+go through the host-buffer entry point (copies inside the call).
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _lib
+from ._lib import KERNELS, KINDS, EVALS, check, cplx2, lib
+from .meshes import Mesh
+
+__all__ = ["SurfaceL2", "H1", "HDivSurface", "TraceSpace", "BaseMatrix", "HMatrix", "MassMatrix",
+           "IntegralOperator", "IntegralOperatorC",
+           "SingleLayerPotentialOperator", "DoubleLayerPotentialOperator", "HypersingularOperator",
+           "HelmholtzSingleLayerPotentialOperator", "HelmholtzDoubleLayerPotentialOperator",
+           "HelmholtzCombinedFieldOperator", "HelmholtzHypersingularOperator",
+           "MaxwellSingleLayerPotentialOperator", "MaxwellSingleLayerPotentialOperatorCurl",
+           "MaxwellDoubleLayerPotentialOperator", "MassOperator", "GMRes", "cluster_tree", "partition"]
+
+
+def _torch():
+    import torch
+    return torch
+
+
+# ----------------------------------------------------------------------------------------
+# meshes and spaces
+# ----------------------------------------------------------------------------------------
+class _MeshHandle:
+    _cache: dict = {}
+
+    def __init__(self, mesh: Mesh):
+        self.mesh = mesh
+        self.h = C.c_void_p()
+        X = np.ascontiguousarray(mesh.vertices, dtype=np.float64)
+        T = np.ascontiguousarray(mesh.triangles, dtype=np.int32)
+        check(lib.bem_mesh_create(mesh.nv, X.ctypes.data_as(_lib._dp), mesh.nt, T.ctypes.data_as(_lib._ip),
+                                  C.byref(self.h)))
+        ne = C.c_int()
+        check(lib.bem_mesh_num_edges(self.h, C.byref(ne)))
+        self.ne = ne.value
+
+    @classmethod
+    def of(cls, mesh: Mesh):
+        key = id(mesh)
+        h = cls._cache.get(key)
+        if h is None or h.mesh is not mesh:
+            h = cls(mesh)
+            cls._cache[key] = h
+        return h
+
+    def __del__(self):
+        if getattr(self, "h", None) and self.h.value:
+            lib.bem_mesh_destroy(self.h)
+            self.h = C.c_void_p()
+
+
+class TraceSpace:
+    """Surface trace space: kind "P0" (SurfaceL2 order 0), "P1" (H1 order 1), "RT0" (HDivSurface order 0)."""
+
+    def __init__(self, mesh: Mesh, kind: str, dual_mapping: bool = False, complex: bool = False):
+        if kind not in KINDS:
+            raise ValueError(f"unknown space kind {kind!r}")
+        self.mesh = mesh
+        self.kind = kind
+        self.dual_mapping = bool(dual_mapping)
+        self.is_complex = bool(complex)
+        self._mh = _MeshHandle.of(mesh)
+        self.h = C.c_void_p()
+        check(lib.bem_space_create(self._mh.h, KINDS[kind], int(self.dual_mapping), C.byref(self.h)))
+        n = C.c_int()
+        check(lib.bem_space_ndof(self.h, C.byref(n)))
+        self.ndof = n.value
+
+    def __repr__(self):
+        return f"TraceSpace({self.kind}, ndof={self.ndof})"
+
+    def __del__(self):
+        if getattr(self, "h", None) and self.h.value:
+            lib.bem_space_destroy(self.h)
+            self.h = C.c_void_p()
+
+
+def SurfaceL2(mesh: Mesh, order: int = 0, dual_mapping: bool = False, complex: bool = False) -> TraceSpace:
+    """Piecewise constants on the surface (the reference uses NGSolve SurfaceL2; order 0 here)."""
+    if order != 0:
+        raise NotImplementedError("SurfaceL2: only order 0 (piecewise constants) is supported")
+    return TraceSpace(mesh, "P0", dual_mapping, complex)
+
+
+def H1(mesh: Mesh, order: int = 1, complex: bool = False) -> TraceSpace:
+    """Continuous piecewise linears on the surface (trace of NGSolve H1, order 1)."""
+    if order != 1:
+        raise NotImplementedError("H1: only order 1 is supported")
+    return TraceSpace(mesh, "P1", False, complex)
+
+
+def HDivSurface(mesh: Mesh, order: int = 0, complex: bool = False) -> TraceSpace:
+    """Lowest-order Raviart-Thomas on the surface (NGSolve HDivSurface order 0)."""
+    if order != 0:
+        raise NotImplementedError("HDivSurface: only order 0 (RT0) is supported")
+    return TraceSpace(mesh, "RT0", False, complex)
+
+
+def cluster_tree(space: TraceSpace, leafsize: int = 40):
+    """Cluster tree of a space (host): (perm, int fields [nc,7], float fields [nc,23])."""
+    maxc = 4 * space.ndof + 8
+    perm = np.zeros(space.ndof, dtype=np.int32)
+    ci = np.zeros(7 * maxc, dtype=np.int64)
+    cd = np.zeros(23 * maxc, dtype=np.float64)
+    nc = C.c_int()
+    check(lib.bem_cluster_tree(space.h, leafsize, perm.ctypes.data_as(_lib._ip), maxc, C.byref(nc),
+                               ci.ctypes.data_as(_lib._lp), cd.ctypes.data_as(_lib._dp)))
+    n = nc.value
+    return perm, ci[: 7 * n].reshape(n, 7), cd[: 23 * n].reshape(n, 23)
+
+
+def partition(trial: TraceSpace, test: TraceSpace | None = None, leafsize: int = 40, eta: float = 2.0):
+    """Block partition (host): dict of rowcl, colcl, near arrays in the reference order."""
+    test = trial if test is None else test
+    maxb = 64 * max(trial.ndof, test.ndof) + 64
+    arrs = [np.zeros(maxb, dtype=np.int32) for _ in range(3)]
+    nb = C.c_int()
+    check(lib.bem_partition(trial.h, test.h, leafsize, float(eta), maxb, C.byref(nb),
+                            *[a.ctypes.data_as(_lib._ip) for a in arrs]))
+    n = nb.value
+    return dict(rowcl=arrs[0][:n], colcl=arrs[1][:n], near=arrs[2][:n])
+
+
+# ----------------------------------------------------------------------------------------
+# matrices
+# ----------------------------------------------------------------------------------------
+def _as_device(x, dtype):
+    torch = _torch()
+    if isinstance(x, torch.Tensor):
+        if not x.is_cuda:
+            raise ValueError("torch vectors must live on the GPU")
+        if x.dtype != dtype:
+            x = x.to(dtype)
+        return x.contiguous()
+    raise TypeError("expected a torch CUDA tensor")
+
+
+class BaseMatrix:
+    """Linear operator algebra (sums, scalings, transposes) over GPU vectors."""
+
+    height: int
+    width: int
+    is_complex: bool
+
+    # y = s * A x + y
+    def MultAdd(self, s, x, y):
+        self._apply(False, s, x, 1.0, y)
+
+    def MultTransAdd(self, s, x, y):
+        self._apply(True, s, x, 1.0, y)
+
+    def Mult(self, x, y):
+        self._apply(False, 1.0, x, 0.0, y)
+
+    def MultTrans(self, x, y):
+        self._apply(True, 1.0, x, 0.0, y)
+
+    @property
+    def T(self):
+        return _Transposed(self)
+
+    def CreateRowVector(self):
+        return self._vec(self.width)
+
+    def CreateColVector(self):
+        return self._vec(self.height)
+
+    def _vec(self, n):
+        torch = _torch()
+        return torch.zeros(n, dtype=torch.complex128 if self.is_complex else torch.float64, device="cuda")
+
+    def __mul__(self, x):
+        if isinstance(x, BaseMatrix):
+            raise NotImplementedError("matrix products are not supported")
+        if isinstance(x, np.ndarray):
+            return self._apply_host(False, x)
+        y = self.CreateColVector() if not (x.is_complex() and not self.is_complex) else None
+        if y is None:
+            raise TypeError("complex vector on a real operator")
+        self.Mult(x, y)
+        return y
+
+    def __rmul__(self, s):
+        return _Scaled(self, s)
+
+    def __add__(self, other):
+        return _Sum([(1.0, self), (1.0, other)])
+
+    def __sub__(self, other):
+        return _Sum([(1.0, self), (-1.0, other)])
+
+    def __neg__(self):
+        return _Scaled(self, -1.0)
+
+    def _terms(self):
+        return [(1.0, self)]
+
+    def _apply_host(self, trans, x):
+        torch = _torch()
+        xd = torch.from_numpy(np.ascontiguousarray(x)).cuda()
+        y = self._vec(self.width if trans else self.height)
+        self._apply(trans, 1.0, xd, 0.0, y)
+        return y.cpu().numpy()
+
+
+class _Scaled(BaseMatrix):
+    def __init__(self, A, s):
+        self.A, self.s = A, s
+        self.height, self.width = A.height, A.width
+        self.is_complex = A.is_complex or isinstance(s, complex)
+
+    def _apply(self, trans, alpha, x, beta, y):
+        self.A._apply(trans, alpha * self.s, x, beta, y)
+
+    def _terms(self):
+        return [(self.s * c, M) for c, M in self.A._terms()]
+
+
+class _Sum(BaseMatrix):
+    def __init__(self, terms):
+        self.parts = terms
+        self.height, self.width = terms[0][1].height, terms[0][1].width
+        for _, M in terms:
+            if (M.height, M.width) != (self.height, self.width):
+                raise ValueError("matrix sizes differ")
+        self.is_complex = any(M.is_complex or isinstance(c, complex) for c, M in terms)
+
+    def _apply(self, trans, alpha, x, beta, y):
+        b = beta
+        for c, M in self.parts:
+            M._apply(trans, alpha * c, x, b, y)
+            b = 1.0
+
+    def _terms(self):
+        out = []
+        for c, M in self.parts:
+            out += [(c * c2, M2) for c2, M2 in M._terms()]
+        return out
+
+
+class _Transposed(BaseMatrix):
+    def __init__(self, A):
+        self.A = A
+        self.height, self.width = A.width, A.height
+        self.is_complex = A.is_complex
+
+    def _apply(self, trans, alpha, x, beta, y):
+        self.A._apply(not trans, alpha, x, beta, y)
+
+    @property
+    def T(self):
+        return self.A
+
+
+class _NativeMatrix(BaseMatrix):
+    """A matrix owned by the C library (H-matrix or sparse mass matrix)."""
+
+    def __init__(self, handle):
+        self.h = handle
+        info = _lib.OperatorInfo()
+        check(lib.bem_operator_info(self.h, C.byref(info)))
+        self.info = {k: getattr(info, k) for k, _ in _lib.OperatorInfo._fields_}
+        self.height, self.width = info.height, info.width
+        self.is_complex = bool(info.is_complex)
+
+    @property
+    def nze(self):
+        return int(self.info["nze"])
+
+    def _apply(self, trans, alpha, x, beta, y):
+        torch = _torch()
+        dt = torch.complex128 if self.is_complex else torch.float64
+        nin, nout = (self.height, self.width) if trans else (self.width, self.height)
+        if not (isinstance(y, torch.Tensor) and y.is_cuda and y.dtype == dt and y.is_contiguous()):
+            raise TypeError(f"y must be a contiguous CUDA tensor of dtype {dt}")
+        xd = _as_device(x, dt)
+        if xd.shape[0] != nin or y.shape[0] != nout:
+            raise ValueError("vector length does not match the matrix")
+        nrhs = 1 if xd.dim() == 1 else xd.shape[1]
+        if xd.dim() == 2:
+            # column-major right-hand sides: each column contiguous
+            xd = xd.t().contiguous()
+            yt = y.t().contiguous() if beta != 0 else torch.empty((nrhs, nout), dtype=dt, device=y.device)
+        else:
+            yt = y
+        stream = torch.cuda.current_stream().cuda_stream
+        check(lib.bem_operator_mult(self.h, int(trans), cplx2(alpha), C.c_void_p(xd.data_ptr()), cplx2(beta),
+                                    C.c_void_p(yt.data_ptr()), nrhs, C.c_void_p(stream)))
+        if xd.dim() == 2:
+            y.copy_(yt.t())
+
+    def mult_host(self, x: np.ndarray, trans=False, alpha=1.0, beta=0.0, y: np.ndarray | None = None):
+        """Apply with host buffers through bem_operator_mult_host (copies inside the call)."""
+        dt = np.complex128 if self.is_complex else np.float64
+        x = np.ascontiguousarray(x, dtype=dt)
+        nrhs = 1 if x.ndim == 1 else x.shape[1]
+        xc = x if x.ndim == 1 else np.asfortranarray(x)
+        nout = self.width if trans else self.height
+        if y is None:
+            y = np.zeros((nout,) if x.ndim == 1 else (nout, nrhs), dtype=dt, order="F")
+        check(lib.bem_operator_mult_host(self.h, int(trans), cplx2(alpha), C.c_void_p(xc.ctypes.data),
+                                         cplx2(beta), C.c_void_p(y.ctypes.data), nrhs))
+        return y
+
+    def __del__(self):
+        if getattr(self, "h", None) and self.h.value:
+            lib.bem_operator_destroy(self.h)
+            self.h = C.c_void_p()
+
+
+class HMatrix(_NativeMatrix):
+    """H-matrix (reference HMatrix<T>, src/hmat.hpp:162-201) resident in GPU memory."""
+
+    def blocks(self):
+        n = self.info["nblocks"]
+        arrs = [np.zeros(n, dtype=np.int32) for _ in range(5)]
+        check(lib.bem_operator_blocks(self.h, *[a.ctypes.data_as(_lib._ip) for a in arrs]))
+        return dict(zip(["rowcl", "colcl", "near", "rank", "fallback"], arrs))
+
+    def to_dense(self) -> np.ndarray:
+        dt = np.complex128 if self.is_complex else np.float64
+        out = np.zeros((self.height, self.width), dtype=dt)
+        check(lib.bem_operator_to_dense(self.h, C.c_void_p(out.ctypes.data)))
+        return out
+
+
+class MassMatrix(_NativeMatrix):
+    """Sparse Galerkin mass matrix <u, v> of identity traces (rows = test dofs)."""
+
+
+def MassOperator(trial_space: TraceSpace, test_space: TraceSpace | None = None, complex: bool = False) -> MassMatrix:
+    test_space = trial_space if test_space is None else test_space
+    h = C.c_void_p()
+    check(lib.bem_mass_create(trial_space.h, test_space.h, int(bool(complex)), C.byref(h)))
+    return MassMatrix(h)
+
+
+# ----------------------------------------------------------------------------------------
+# integral operators
+# ----------------------------------------------------------------------------------------
+class IntegralOperator:
+    """Assembled layer-potential operator (reference IntegralOperator<T>, src/ngbem.hpp:32-87)."""
+
+    def __init__(self, kernel, kappa, trial, test, trial_eval, test_eval, intorder, leafsize, eta, eps, method,
+                 testhmatrix, precision="fp64", intorder_singular=None, intorder_regular=None, max_rank=None,
+                 aca_eps_floor=None):
+        test = trial if test is None else test
+        p = _lib.Params()
+        check(lib.bem_params_default(C.byref(p)))
+        p.intorder = int(intorder)
+        p.intorder_singular = int(intorder_singular or 0)
+        p.intorder_regular = int(intorder_regular or 0)
+        p.leafsize = int(leafsize)
+        p.eta = float(eta)
+        p.eps = float(eps)
+        p.method = _lib.METHODS[method]
+        p.precision = _lib.PRECISIONS[precision]
+        p.max_rank = int(max_rank or 0)
+        p.aca_eps_floor = float(aca_eps_floor or 0.0)
+        self.params = p
+        self.kernel, self.kappa = kernel, kappa
+        self.trial_space, self.test_space = trial, test
+        self._evals = (trial_eval, test_eval)
+        h = C.c_void_p()
+        check(lib.bem_operator_create(KERNELS[kernel], float(kappa), trial.h, test.h, EVALS[trial_eval],
+                                      EVALS[test_eval], C.byref(p), C.byref(h)))
+        self.mat = HMatrix(h)
+        if testhmatrix:
+            self._test_hmatrix()
+
+    @property
+    def info(self):
+        return self.mat.info
+
+    def GetPotential(self, gf):
+        raise NotImplementedError("potential evaluation (PotentialCF) is not part of this build")
+
+    def _test_hmatrix(self):
+        """Reference testhmatrix diagnostic (src/ngbem.cpp:332-369): dense assembly plus 30
+        power iterations of (D - H)^H (D - H); prints compression rate and 2-norm error."""
+        torch = _torch()
+        p = self.params
+        dense = IntegralOperator(self.kernel, self.kappa, self.trial_space, self.test_space, *self._evals,
+                                 p.intorder, p.leafsize, p.eta, p.eps, "dense", False,
+                                 precision="fp64", intorder_singular=p.intorder_singular or None,
+                                 intorder_regular=p.intorder_regular or None)
+        print(f"dense: {self.mat.height} x {self.mat.width}")
+        D, H = dense.mat, self.mat
+        x = H.CreateRowVector()
+        x.fill_(1.0)
+        y = H.CreateColVector()
+        for _ in range(30):
+            x /= torch.linalg.vector_norm(x)
+            D.Mult(x, y)
+            H.MultAdd(-1.0, x, y)
+            y = y.conj()
+            D.MultTrans(y, x)
+            H.MultTransAdd(-1.0, y, x)
+            x = x.conj()
+        rate = self.mat.nze / (float(self.mat.height) * self.mat.width)
+        err = float(torch.sqrt(torch.linalg.vector_norm(x)))
+        print(f"compression rate {rate}  2-norm error {err}")
+        self.testhmatrix_result = (rate, err)
+
+
+IntegralOperatorC = IntegralOperator
+
+
+def _dense_args(method, leafsize, eta):
+    # reference python_bem.cpp:30-33: method "dense" means one root block
+    return method, leafsize, eta
+
+
+def _no_regions(*regions):
+    if any(r is not None for r in regions):
+        raise NotImplementedError("definedon region masks are not supported")
+
+
+def SingleLayerPotentialOperator(space, intorder=3, leafsize=40, eta=2., eps=1e-6, method="aca",
+                                 testhmatrix=False, **gb):
+    """Laplace single layer V (reference python_bem.cpp:27-38)."""
+    return IntegralOperator("laplace_sl", 0.0, space, space, "id", "id", intorder, leafsize, eta, eps, method,
+                            testhmatrix, **gb)
+
+
+def DoubleLayerPotentialOperator(trial_space, test_space, trial_definedon=None, test_definedon=None, intorder=3,
+                                 leafsize=40, eta=2., eps=1e-6, method="aca", testhmatrix=False, **gb):
+    """Laplace double layer K (reference python_bem.cpp:41-60)."""
+    _no_regions(trial_definedon, test_definedon)
+    return IntegralOperator("laplace_dl", 0.0, trial_space, test_space, "id", "id", intorder, leafsize, eta, eps,
+                            method, testhmatrix, **gb)
+
+
+def HypersingularOperator(space, definedon=None, intorder=3, leafsize=40, eta=2., eps=1e-6, method="aca",
+                          testhmatrix=False, **gb):
+    """Laplace hypersingular W with surface-curl traces (reference python_bem.cpp:63-75).
+    As in the reference, method is not consulted (always an ACA H-matrix)."""
+    _no_regions(definedon)
+    return IntegralOperator("laplace_hs", 0.0, space, space, "rot", "rot", intorder, leafsize, eta, eps, "aca",
+                            testhmatrix, **gb)
+
+
+def _kappa(kappa):
+    if kappa is None:
+        raise TypeError("kappa is required")
+    return float(kappa)
+
+
+def HelmholtzSingleLayerPotentialOperator(trial_space, test_space=None, kappa=None, intorder=3, leafsize=40, eta=2.,
+                                          eps=1e-6, method="aca", testhmatrix=False, **gb):
+    """Helmholtz single layer (reference python_bem.cpp:79-87).  test_space=None uses the
+    trial space (the reference dereferences the null test space there)."""
+    return IntegralOperator("helmholtz_sl", _kappa(kappa), trial_space, test_space, "id", "id", intorder, leafsize,
+                            eta, eps, "aca", testhmatrix, **gb)
+
+
+def HelmholtzDoubleLayerPotentialOperator(trial_space, test_space=None, kappa=None, intorder=3, leafsize=40,
+                                          eta=2., eps=1e-6, method="aca", testhmatrix=False, **gb):
+    """Helmholtz double layer (reference python_bem.cpp:91-99)."""
+    return IntegralOperator("helmholtz_dl", _kappa(kappa), trial_space, test_space, "id", "id", intorder, leafsize,
+                            eta, eps, "aca", testhmatrix, **gb)
+
+
+def HelmholtzCombinedFieldOperator(trial_space, test_space=None, kappa=None, intorder=3, leafsize=40, eta=2.,
+                                   eps=1e-6, method="aca", testhmatrix=False, **gb):
+    """Helmholtz combined field DL - i kappa SL (reference python_bem.cpp:102-110)."""
+    return IntegralOperator("helmholtz_cf", _kappa(kappa), trial_space, test_space, "id", "id", intorder, leafsize,
+                            eta, eps, "aca", testhmatrix, **gb)
+
+
+def HelmholtzHypersingularOperator(trial_space, test_space=None, kappa=None, intorder=3, leafsize=40, eta=2.,
+                                   eps=1e-6, method="aca", testhmatrix=False, **gb):
+    """Helmholtz hypersingular with [n x grad u; u] traces (reference python_bem.cpp:113-119)."""
+    return IntegralOperator("helmholtz_hs", _kappa(kappa), trial_space, test_space, "helm", "helm", intorder,
+                            leafsize, eta, eps, "aca", testhmatrix, **gb)
+
+
+def MaxwellSingleLayerPotentialOperator(space, kappa, definedon=None, intorder=3, leafsize=40, eta=2., eps=1e-6,
+                                        method="aca", testhmatrix=False, **gb):
+    """Maxwell single layer on HDivSurface with [Piola u; div u] traces (reference
+    python_bem.cpp:122-134): kappa <u,v> - 1/kappa <div u, div v> weighted by G."""
+    _no_regions(definedon)
+    return IntegralOperator("maxwell_sl", _kappa(kappa), space, space, "maxwell", "maxwell", intorder, leafsize,
+                            eta, eps, "aca", testhmatrix, **gb)
+
+
+def MaxwellSingleLayerPotentialOperatorCurl(space, kappa, definedon=None, **kw):
+    raise NotImplementedError("MaxwellSingleLayerPotentialOperatorCurl (HCurl traces) is not part of this build")
+
+
+def MaxwellDoubleLayerPotentialOperator(trial_space, test_space, kappa, **kw):
+    raise NotImplementedError("MaxwellDoubleLayerPotentialOperator (HCurl rotated traces) is not part of this build")
+
+
+# ----------------------------------------------------------------------------------------
+# GMRES
+# ----------------------------------------------------------------------------------------
+def GMRes(A, b, pre=None, freedofs=None, x=None, maxsteps=100, tol=1e-7, innerproduct=None, callback=None,
+          restart=None, startiteration=0, printrates=False, reltol=None):
+    """Restarted GMRES on the GPU for sums of native matrices (the role of
+    ngsolve.krylovspace.GMRes in the reference tests).  Returns the solution vector; the
+    iteration count and final relative residual are in GMRes.last."""
+    torch = _torch()
+    if pre is not None or freedofs is not None or innerproduct is not None:
+        raise NotImplementedError("GMRes: preconditioners, freedofs and inner products are not supported")
+    terms = A._terms() if isinstance(A, BaseMatrix) else [(1.0, A)]
+    for _, M in terms:
+        if not isinstance(M, _NativeMatrix):
+            raise TypeError("GMRes needs sums of H-matrices and mass matrices")
+    cplx = any(M.is_complex or isinstance(c, complex) for c, M in terms)
+    dt = torch.complex128 if cplx else torch.float64
+    bd = _as_device(b, dt)
+    xd = torch.zeros_like(bd) if x is None else _as_device(x, dt).clone()
+    ops = (C.c_void_p * len(terms))(*[M.h for _, M in terms])
+    coef = (C.c_double * (2 * len(terms)))()
+    for k, (c, _) in enumerate(terms):
+        z = complex(c)
+        coef[2 * k], coef[2 * k + 1] = z.real, z.imag
+    it, res = C.c_int(), C.c_double()
+    stream = torch.cuda.current_stream().cuda_stream
+    check(lib.bem_gmres(len(terms), ops, coef, C.c_void_p(bd.data_ptr()), C.c_void_p(xd.data_ptr()), int(maxsteps),
+                        int(restart or min(maxsteps, 200)), float(reltol if reltol is not None else tol),
+                        C.byref(it), C.byref(res), C.c_void_p(stream)))
+    GMRes.last = dict(iterations=it.value, residual=res.value)
+    if printrates:
+        print(f"GMRes iteration {it.value}, residual = {res.value}")
+    if x is not None:
+        x.copy_(xd)
+        return x
+    return xd
+
+
+GMRes.last = {}

@@ -1,0 +1,306 @@
+// Device-side building blocks: complex arithmetic, Green's functions with their term
+// tables, trace evaluators and warp/block reductions.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "bem_shared.h"
+
+namespace bem {
+
+// ----------------------------------------------------------------------------------------
+// complex numbers
+// ----------------------------------------------------------------------------------------
+template <class R>
+struct cpx {
+  R x, y;
+};
+template <class R> __host__ __device__ __forceinline__ cpx<R> mkc(R a, R b) { return cpx<R>{a, b}; }
+template <class R> __host__ __device__ __forceinline__ cpx<R> operator+(cpx<R> a, cpx<R> b) { return {a.x + b.x, a.y + b.y}; }
+template <class R> __host__ __device__ __forceinline__ cpx<R> operator-(cpx<R> a, cpx<R> b) { return {a.x - b.x, a.y - b.y}; }
+template <class R> __host__ __device__ __forceinline__ cpx<R> operator*(cpx<R> a, cpx<R> b) { return {a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x}; }
+template <class R> __host__ __device__ __forceinline__ cpx<R> operator*(R s, cpx<R> a) { return {s * a.x, s * a.y}; }
+template <class R> __host__ __device__ __forceinline__ cpx<R> operator*(cpx<R> a, R s) { return {s * a.x, s * a.y}; }
+template <class R> __host__ __device__ __forceinline__ cpx<R>& operator+=(cpx<R>& a, cpx<R> b) { a.x += b.x; a.y += b.y; return a; }
+template <class R> __host__ __device__ __forceinline__ cpx<R>& operator-=(cpx<R>& a, cpx<R> b) { a.x -= b.x; a.y -= b.y; return a; }
+template <class R> __host__ __device__ __forceinline__ cpx<R>& operator*=(cpx<R>& a, cpx<R> b) { a = a * b; return a; }
+template <class R> __host__ __device__ __forceinline__ cpx<R>& operator*=(cpx<R>& a, R s) { a.x *= s; a.y *= s; return a; }
+
+template <class V> struct scal;
+template <> struct scal<float> { using R = float; static constexpr bool cplx = false; };
+template <> struct scal<double> { using R = double; static constexpr bool cplx = false; };
+template <> struct scal<cpx<float>> { using R = float; static constexpr bool cplx = true; };
+template <> struct scal<cpx<double>> { using R = double; static constexpr bool cplx = true; };
+
+template <bool C, class R> struct VT_ { using type = R; };
+template <class R> struct VT_<true, R> { using type = cpx<R>; };
+template <bool C, class R> using VT = typename VT_<C, R>::type;
+
+__device__ __forceinline__ float zero_of(float) { return 0.f; }
+__device__ __forceinline__ double zero_of(double) { return 0.0; }
+template <class R> __device__ __forceinline__ cpx<R> zero_of(cpx<R>) { return {R(0), R(0)}; }
+template <class V> __device__ __forceinline__ V vzero() { return zero_of(V()); }
+
+__device__ __forceinline__ float conjv(float a) { return a; }
+__device__ __forceinline__ double conjv(double a) { return a; }
+template <class R> __device__ __forceinline__ cpx<R> conjv(cpx<R> a) { return {a.x, -a.y}; }
+__device__ __forceinline__ float absv(float a) { return fabsf(a); }
+__device__ __forceinline__ double absv(double a) { return fabs(a); }
+__device__ __forceinline__ float absv(cpx<float> a) { return sqrtf(a.x * a.x + a.y * a.y); }
+__device__ __forceinline__ double absv(cpx<double> a) { return sqrt(a.x * a.x + a.y * a.y); }
+__device__ __forceinline__ float norm2v(float a) { return a * a; }
+__device__ __forceinline__ double norm2v(double a) { return a * a; }
+template <class R> __device__ __forceinline__ R norm2v(cpx<R> a) { return a.x * a.x + a.y * a.y; }
+__device__ __forceinline__ float realv(float a) { return a; }
+__device__ __forceinline__ double realv(double a) { return a; }
+template <class R> __device__ __forceinline__ R realv(cpx<R> a) { return a.x; }
+// 1/a for real or complex a
+__device__ __forceinline__ float invv(float a) { return 1.f / a; }
+__device__ __forceinline__ double invv(double a) { return 1.0 / a; }
+template <class R> __device__ __forceinline__ cpx<R> invv(cpx<R> a) { R d = a.x * a.x + a.y * a.y; return {a.x / d, -a.y / d}; }
+
+// conversions between storage and accumulation types
+__device__ __forceinline__ void cvt(float& d, double s) { d = (float)s; }
+__device__ __forceinline__ void cvt(double& d, double s) { d = s; }
+__device__ __forceinline__ void cvt(double& d, float s) { d = (double)s; }
+__device__ __forceinline__ void cvt(float& d, float s) { d = s; }
+template <class A, class B> __device__ __forceinline__ void cvt(cpx<A>& d, cpx<B> s) { cvt(d.x, s.x); cvt(d.y, s.y); }
+template <class A> __device__ __forceinline__ void cvt(cpx<A>& d, double s) { cvt(d.x, s); d.y = A(0); }
+template <class A> __device__ __forceinline__ void cvt(cpx<A>& d, float s) { cvt(d.x, s); d.y = A(0); }
+
+__device__ __forceinline__ void atomic_add(float* p, float v) { atomicAdd(p, v); }
+__device__ __forceinline__ void atomic_add(double* p, double v) { atomicAdd(p, v); }
+template <class R> __device__ __forceinline__ void atomic_add(cpx<R>* p, cpx<R> v) {
+  atomicAdd(&p->x, v.x);
+  atomicAdd(&p->y, v.y);
+}
+
+__device__ __forceinline__ float rsqrt_(float a) { return rsqrtf(a); }
+__device__ __forceinline__ double rsqrt_(double a) { return 1.0 / sqrt(a); }
+__device__ __forceinline__ void sincos_(float a, float* s, float* c) { sincosf(a, s, c); }
+__device__ __forceinline__ void sincos_(double a, double* s, double* c) { sincos(a, s, c); }
+__device__ __forceinline__ float sqrt_(float a) { return sqrtf(a); }
+__device__ __forceinline__ double sqrt_(double a) { return sqrt(a); }
+
+// ----------------------------------------------------------------------------------------
+// Green's functions (reference src/ngbem.hpp:226-468).  eval() takes d = x - y, the normals
+// and kappa and returns the NC kernel components.  Term tables (fac, kernel comp, trial comp,
+// test comp): fac kind 0 = 1, 1 = kappa, 2 = -1/kappa.
+// ----------------------------------------------------------------------------------------
+#define BEM_INV4PI 0.079577471545947667884441881686257181
+
+template <int KID> struct Green;
+
+template <> struct Green<K_LAPLACE_SL> {
+  static constexpr bool CPLX = false; static constexpr int NC = 1; static constexpr int NT = 1;
+  static constexpr bool NEEDS_NX = false, NEEDS_NY = false;
+  __host__ __device__ static constexpr int kc(int) { return 0; }
+  __host__ __device__ static constexpr int trc(int) { return 0; }
+  __host__ __device__ static constexpr int tec(int) { return 0; }
+  __host__ __device__ static constexpr int fk(int) { return 0; }
+  template <class R>
+  __device__ static __forceinline__ void eval(R dx, R dy, R dz, const R*, const R*, R, R* out) {
+    R ir = rsqrt_(dx * dx + dy * dy + dz * dz);
+    out[0] = ir * R(BEM_INV4PI);
+  }
+};
+
+template <> struct Green<K_LAPLACE_DL> {
+  static constexpr bool CPLX = false; static constexpr int NC = 1; static constexpr int NT = 1;
+  static constexpr bool NEEDS_NX = false, NEEDS_NY = true;
+  __host__ __device__ static constexpr int kc(int) { return 0; }
+  __host__ __device__ static constexpr int trc(int) { return 0; }
+  __host__ __device__ static constexpr int tec(int) { return 0; }
+  __host__ __device__ static constexpr int fk(int) { return 0; }
+  template <class R>
+  __device__ static __forceinline__ void eval(R dx, R dy, R dz, const R*, const R* ny, R, R* out) {
+    R ir = rsqrt_(dx * dx + dy * dy + dz * dz);
+    R nxy = ny[0] * dx + ny[1] * dy + ny[2] * dz;
+    out[0] = nxy * (ir * ir * ir) * R(BEM_INV4PI);
+  }
+};
+
+template <> struct Green<K_LAPLACE_HS> {
+  static constexpr bool CPLX = false; static constexpr int NC = 1; static constexpr int NT = 3;
+  static constexpr bool NEEDS_NX = false, NEEDS_NY = false;
+  __host__ __device__ static constexpr int kc(int) { return 0; }
+  __host__ __device__ static constexpr int trc(int t) { return t; }
+  __host__ __device__ static constexpr int tec(int t) { return t; }
+  __host__ __device__ static constexpr int fk(int) { return 0; }
+  template <class R>
+  __device__ static __forceinline__ void eval(R dx, R dy, R dz, const R*, const R*, R, R* out) {
+    R ir = rsqrt_(dx * dx + dy * dy + dz * dz);
+    out[0] = ir * R(BEM_INV4PI);
+  }
+};
+
+template <> struct Green<K_HELMHOLTZ_SL> {
+  static constexpr bool CPLX = true; static constexpr int NC = 1; static constexpr int NT = 1;
+  static constexpr bool NEEDS_NX = false, NEEDS_NY = false;
+  __host__ __device__ static constexpr int kc(int) { return 0; }
+  __host__ __device__ static constexpr int trc(int) { return 0; }
+  __host__ __device__ static constexpr int tec(int) { return 0; }
+  __host__ __device__ static constexpr int fk(int) { return 0; }
+  template <class R>
+  __device__ static __forceinline__ void eval(R dx, R dy, R dz, const R*, const R*, R kappa, cpx<R>* out) {
+    R r2 = dx * dx + dy * dy + dz * dz;
+    R ir = rsqrt_(r2);
+    R s, c;
+    sincos_(kappa * (r2 * ir), &s, &c);
+    R f = ir * R(BEM_INV4PI);
+    out[0] = mkc(c * f, s * f);
+  }
+};
+
+template <> struct Green<K_MAXWELL_SL> {
+  static constexpr bool CPLX = true; static constexpr int NC = 1; static constexpr int NT = 4;
+  static constexpr bool NEEDS_NX = false, NEEDS_NY = false;
+  __host__ __device__ static constexpr int kc(int) { return 0; }
+  __host__ __device__ static constexpr int trc(int t) { return t; }
+  __host__ __device__ static constexpr int tec(int t) { return t; }
+  __host__ __device__ static constexpr int fk(int t) { return t < 3 ? 1 : 2; }
+  template <class R>
+  __device__ static __forceinline__ void eval(R dx, R dy, R dz, const R* nx, const R* ny, R kappa, cpx<R>* out) {
+    Green<K_HELMHOLTZ_SL>::eval(dx, dy, dz, nx, ny, kappa, out);
+  }
+};
+
+template <> struct Green<K_HELMHOLTZ_DL> {
+  static constexpr bool CPLX = true; static constexpr int NC = 1; static constexpr int NT = 1;
+  static constexpr bool NEEDS_NX = false, NEEDS_NY = true;
+  __host__ __device__ static constexpr int kc(int) { return 0; }
+  __host__ __device__ static constexpr int trc(int) { return 0; }
+  __host__ __device__ static constexpr int tec(int) { return 0; }
+  __host__ __device__ static constexpr int fk(int) { return 0; }
+  template <class R>
+  __device__ static __forceinline__ void eval(R dx, R dy, R dz, const R*, const R* ny, R kappa, cpx<R>* out) {
+    R r2 = dx * dx + dy * dy + dz * dz;
+    R ir = rsqrt_(r2);
+    R r = r2 * ir;
+    R s, c;
+    sincos_(kappa * r, &s, &c);
+    R nxy = ny[0] * dx + ny[1] * dy + ny[2] * dz;
+    R f = nxy * (ir * ir * ir) * R(BEM_INV4PI);
+    // e^{ikr} * f * (1 - i kappa r)
+    cpx<R> e = mkc(c * f, s * f);
+    out[0] = e * mkc(R(1), -kappa * r);
+  }
+};
+
+template <> struct Green<K_HELMHOLTZ_CF> {
+  static constexpr bool CPLX = true; static constexpr int NC = 1; static constexpr int NT = 1;
+  static constexpr bool NEEDS_NX = false, NEEDS_NY = true;
+  __host__ __device__ static constexpr int kc(int) { return 0; }
+  __host__ __device__ static constexpr int trc(int) { return 0; }
+  __host__ __device__ static constexpr int tec(int) { return 0; }
+  __host__ __device__ static constexpr int fk(int) { return 0; }
+  template <class R>
+  __device__ static __forceinline__ void eval(R dx, R dy, R dz, const R*, const R* ny, R kappa, cpx<R>* out) {
+    R r2 = dx * dx + dy * dy + dz * dz;
+    R ir = rsqrt_(r2);
+    R r = r2 * ir;
+    R s, c;
+    sincos_(kappa * r, &s, &c);
+    R nxy = ny[0] * dx + ny[1] * dy + ny[2] * dz;
+    R f = (ir * ir * ir) * R(BEM_INV4PI);
+    // e^{ikr}/(4 pi r^3) * (nxy (1 - i kappa r) - i kappa r^2)
+    cpx<R> e = mkc(c * f, s * f);
+    out[0] = e * mkc(nxy, -kappa * r * nxy - kappa * r2);
+  }
+};
+
+template <> struct Green<K_HELMHOLTZ_HS> {
+  static constexpr bool CPLX = true; static constexpr int NC = 2; static constexpr int NT = 4;
+  static constexpr bool NEEDS_NX = true, NEEDS_NY = true;
+  __host__ __device__ static constexpr int kc(int t) { return t < 3 ? 0 : 1; }
+  __host__ __device__ static constexpr int trc(int t) { return t; }
+  __host__ __device__ static constexpr int tec(int t) { return t; }
+  __host__ __device__ static constexpr int fk(int) { return 0; }
+  template <class R>
+  __device__ static __forceinline__ void eval(R dx, R dy, R dz, const R* nx, const R* ny, R kappa, cpx<R>* out) {
+    R r2 = dx * dx + dy * dy + dz * dz;
+    R ir = rsqrt_(r2);
+    R s, c;
+    sincos_(kappa * (r2 * ir), &s, &c);
+    R f = ir * R(BEM_INV4PI);
+    cpx<R> kern = mkc(c * f, s * f);
+    R nxny = nx[0] * ny[0] + nx[1] * ny[1] + nx[2] * ny[2];
+    out[0] = kern;
+    out[1] = kern * (-kappa * kappa * nxny);
+  }
+};
+
+template <class G, class R>
+__device__ __forceinline__ R term_fac(int t, R kappa) {
+  int k = G::fk(t);
+  return k == 0 ? R(1) : (k == 1 ? kappa : R(-1) / kappa);
+}
+
+// ----------------------------------------------------------------------------------------
+// Trace evaluators.  ND local dofs, DIM components.  Values at a point with reference
+// coordinates (xi, eta) and physical offsets xp[k][c] = x - p_k (vertex k):
+//   P0   : 1 (or 1/|J| with dual mapping)
+//   P1   : lambda_a = (xi, eta, 1 - xi - eta)
+//   ROT  : n x grad lambda_a                       (DiffOpBoundaryRot)
+//   HELM : [n x grad lambda_a ; lambda_a]          (DiffOpHelmholtz)
+//   MAX  : [sigma_a (x - p_opp(a)) / |J| ; 2 sigma_a / |J|]  (DiffOpMaxwellNew, RT0)
+//   RT0ID: sigma_a (x - p_opp(a)) / |J|           (HDivSurface identity trace)
+// Local RT0 edge a joins vertices (a, a+1 mod 3); its opposite vertex is (a+2) mod 3.
+// ----------------------------------------------------------------------------------------
+template <int TR> struct TraceInfo;
+template <> struct TraceInfo<TR_P0> { static constexpr int ND = 1, DIM = 1; };
+template <> struct TraceInfo<TR_P1> { static constexpr int ND = 3, DIM = 1; };
+template <> struct TraceInfo<TR_ROT> { static constexpr int ND = 3, DIM = 3; };
+template <> struct TraceInfo<TR_HELM> { static constexpr int ND = 3, DIM = 4; };
+template <> struct TraceInfo<TR_MAX> { static constexpr int ND = 3, DIM = 4; };
+template <> struct TraceInfo<TR_RT0ID> { static constexpr int ND = 3, DIM = 3; };
+
+// value of trace component c of local dof a
+template <int TR, class R>
+__device__ __forceinline__ R trace_val(int a, int c, R xi, R eta, const R (*xp)[3], R invdetJ,
+                                       const R (*rot)[3], int sgn, bool dual) {
+  if (TR == TR_P0) return dual ? invdetJ : R(1);
+  if (TR == TR_P1) return a == 0 ? xi : (a == 1 ? eta : R(1) - xi - eta);
+  if (TR == TR_ROT) return rot[a][c];
+  if (TR == TR_HELM) {
+    if (c < 3) return rot[a][c];
+    return a == 0 ? xi : (a == 1 ? eta : R(1) - xi - eta);
+  }
+  // MAX and RT0ID
+  if (c < 3) {
+    int o = (a + 2) % 3;
+    return R(sgn) * xp[o][c] * invdetJ;
+  }
+  return R(2 * sgn) * invdetJ;
+}
+
+// ----------------------------------------------------------------------------------------
+// reductions
+// ----------------------------------------------------------------------------------------
+__device__ __forceinline__ float shfl_xor(float v, int m) { return __shfl_xor_sync(0xffffffffu, v, m); }
+__device__ __forceinline__ double shfl_xor(double v, int m) { return __shfl_xor_sync(0xffffffffu, v, m); }
+template <class R> __device__ __forceinline__ cpx<R> shfl_xor(cpx<R> v, int m) { return {shfl_xor(v.x, m), shfl_xor(v.y, m)}; }
+
+template <class V>
+__device__ __forceinline__ V warp_sum(V v) {
+#pragma unroll
+  for (int m = 16; m > 0; m >>= 1) v += shfl_xor(v, m);
+  return v;
+}
+
+// argmax with lowest-index tie-break; idx < 0 means "none".
+template <class R>
+__device__ __forceinline__ void argmax_combine(R& v, int& i, R v2, int i2) {
+  if (i2 >= 0 && (i < 0 || v2 > v || (v2 == v && i2 < i))) { v = v2; i = i2; }
+}
+template <class R>
+__device__ __forceinline__ void warp_argmax(R& v, int& i) {
+#pragma unroll
+  for (int m = 16; m > 0; m >>= 1) {
+    R v2 = shfl_xor(v, m);
+    int i2 = __shfl_xor_sync(0xffffffffu, i, m);
+    argmax_combine(v, i, v2, i2);
+  }
+}
+
+}  // namespace bem

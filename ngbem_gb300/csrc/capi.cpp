@@ -1,0 +1,273 @@
+// extern "C" entry points of libngbem_gb300 (declared in include/ngbem_gb300.h).
+// Every call catches C++ exceptions and converts them to an int status plus a
+// thread-local message (bem_last_error).
+#include <cstring>
+
+#include "host.hpp"
+
+using namespace bem;
+
+static thread_local std::string g_last_error;
+
+template <class F>
+static int guarded(F&& f) {
+  try {
+    f();
+    return BEM_OK;
+  } catch (const Error& e) {
+    g_last_error = e.what();
+    return e.code;
+  } catch (const std::bad_alloc&) {
+    g_last_error = "host allocation failed";
+    return BEM_ERR_ALLOC;
+  } catch (const std::exception& e) {
+    g_last_error = e.what();
+    return BEM_ERR_INTERNAL;
+  } catch (...) {
+    g_last_error = "unknown error";
+    return BEM_ERR_INTERNAL;
+  }
+}
+
+#define REQUIRE(cond, msg) \
+  if (!(cond)) throw Error(BEM_ERR_ARG, msg)
+
+extern "C" {
+
+const char* bem_last_error(void) { return g_last_error.c_str(); }
+
+int bem_params_default(bem_params_t* p) {
+  return guarded([&] {
+    REQUIRE(p, "null params");
+    std::memset(p, 0, sizeof(*p));
+    p->intorder = 3;
+    p->leafsize = 40;
+    p->eta = 2.0;
+    p->eps = 1e-6;
+    p->method = BEM_METHOD_ACA;
+    p->precision = BEM_FP64;
+  });
+}
+
+int bem_mesh_create(int nv, const double* xyz, int nt, const int* tri, bem_mesh_t* out) {
+  return guarded([&] {
+    REQUIRE(out && xyz && tri, "null argument");
+    auto m = std::make_unique<bem_mesh_s>();
+    m->m.build(nv, xyz, nt, tri);
+    *out = m.release();
+  });
+}
+
+int bem_mesh_num_edges(bem_mesh_t mesh, int* ne) {
+  return guarded([&] {
+    REQUIRE(mesh && ne, "null argument");
+    *ne = mesh->m.ne;
+  });
+}
+
+int bem_mesh_destroy(bem_mesh_t mesh) {
+  return guarded([&] { delete mesh; });
+}
+
+int bem_space_create(bem_mesh_t mesh, int kind, int dual_mapping, bem_space_t* out) {
+  return guarded([&] {
+    REQUIRE(mesh && out, "null argument");
+    REQUIRE(kind == BEM_P0 || kind == BEM_P1 || kind == BEM_RT0, "unknown space kind");
+    REQUIRE(!dual_mapping || kind == BEM_P0, "dual mapping is defined for P0 only");
+    auto s = std::make_unique<bem_space_s>();
+    s->s.build(&mesh->m, kind, dual_mapping);
+    *out = s.release();
+  });
+}
+
+int bem_space_ndof(bem_space_t space, int* ndof) {
+  return guarded([&] {
+    REQUIRE(space && ndof, "null argument");
+    *ndof = space->s.ndof;
+  });
+}
+
+int bem_space_destroy(bem_space_t space) {
+  return guarded([&] { delete space; });
+}
+
+int bem_cluster_tree(bem_space_t space, int leafsize, int* perm, int max_clusters, int* nclusters, long* ci,
+                     double* cd) {
+  return guarded([&] {
+    REQUIRE(space && perm && nclusters, "null argument");
+    REQUIRE(leafsize >= 1, "leafsize must be positive");
+    ClusterTreeH t;
+    t.build(space->s, leafsize);
+    const int nc = (int)t.cl.size();
+    *nclusters = nc;
+    std::memcpy(perm, t.perm.data(), t.perm.size() * sizeof(int));
+    if (nc > max_clusters) throw Error(BEM_ERR_ARG, "max_clusters too small");
+    for (int c = 0; c < nc; ++c) {
+      const ClusterH& C = t.cl[c];
+      if (ci) {
+        long* I = ci + 7 * (size_t)c;
+        I[0] = C.Level; I[1] = C.Parent; I[2] = C.Child1; I[3] = C.Child2;
+        I[4] = C.Number; I[5] = C.PermuPos; I[6] = C.BasisElement;
+      }
+      if (cd) {
+        double* D = cd + 23 * (size_t)c;
+        D[0] = C.Radius;
+        for (int k = 0; k < 9; ++k) D[1 + k] = C.EVec[k];
+        for (int k = 0; k < 3; ++k) {
+          D[10 + k] = C.EVal[k];
+          D[13 + k] = C.XMin[k];
+          D[16 + k] = C.XMax[k];
+          D[19 + k] = C.Centre[k];
+        }
+        D[22] = C.DiagLength;
+      }
+    }
+  });
+}
+
+int bem_partition(bem_space_t trial, bem_space_t test, int leafsize, double eta, int max_blocks, int* nblocks,
+                  int* rowcl, int* colcl, int* near) {
+  return guarded([&] {
+    REQUIRE(trial && test && nblocks, "null argument");
+    ClusterTreeH tt, ts;
+    tt.build(trial->s, leafsize);
+    const ClusterTreeH* row = &tt;
+    if (test != trial) {
+      ts.build(test->s, leafsize);
+      row = &ts;
+    }
+    std::vector<BlockH> bl;
+    partition_blocks(*row, tt, eta, bl);
+    *nblocks = (int)bl.size();
+    if ((int)bl.size() > max_blocks) throw Error(BEM_ERR_ARG, "max_blocks too small");
+    for (size_t k = 0; k < bl.size(); ++k) {
+      if (rowcl) rowcl[k] = bl[k].rowcl;
+      if (colcl) colcl[k] = bl[k].colcl;
+      if (near) near[k] = bl[k].near ? 1 : 0;
+    }
+  });
+}
+
+int bem_operator_create(int kernel, double kappa, bem_space_t trial, bem_space_t test, int trial_eval, int test_eval,
+                        const bem_params_t* params, bem_operator_t* out) {
+  return guarded([&] {
+    REQUIRE(trial && out && params, "null argument");
+    REQUIRE(kernel >= 0 && kernel < K_NUM, "unknown kernel id");
+    if (!test) test = trial;
+    if (kernel == BEM_MAXWELL_SL) REQUIRE(kappa != 0.0, "Maxwell single layer needs kappa != 0");
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) throw Error(BEM_ERR_CUDA, "no CUDA device");
+    auto op = std::make_unique<HOperator>();
+    op->kid = kernel;
+    op->kappa = kappa;
+    op->trial = &trial->s;
+    op->test = &test->s;
+    op->trial_ev = trial_eval;
+    op->test_ev = test_eval;
+    op->prm = *params;
+    op->assemble();
+    auto h = std::make_unique<bem_operator_s>();
+    h->op = std::move(op);
+    *out = h.release();
+  });
+}
+
+int bem_mass_create(bem_space_t trial, bem_space_t test, int complex_vectors, bem_operator_t* out) {
+  return guarded([&] {
+    REQUIRE(trial && test && out, "null argument");
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) throw Error(BEM_ERR_CUDA, "no CUDA device");
+    auto op = std::make_unique<MassOperator>();
+    op->build(&trial->s, &test->s, complex_vectors != 0);
+    auto h = std::make_unique<bem_operator_s>();
+    h->op = std::move(op);
+    *out = h.release();
+  });
+}
+
+int bem_operator_info(bem_operator_t op, bem_operator_info_t* info) {
+  return guarded([&] {
+    REQUIRE(op && info, "null argument");
+    auto* h = dynamic_cast<HOperator*>(op->op.get());
+    if (h) {
+      *info = h->info;
+    } else {
+      std::memset(info, 0, sizeof(*info));
+      info->is_complex = op->op->cplx;
+      info->height = op->op->height;
+      info->width = op->op->width;
+      auto* m = dynamic_cast<MassOperator*>(op->op.get());
+      if (m) info->nze = (long long)m->h_val.size();
+    }
+  });
+}
+
+int bem_operator_blocks(bem_operator_t op, int* rowcl, int* colcl, int* near, int* rank, int* fallback) {
+  return guarded([&] {
+    REQUIRE(op, "null argument");
+    auto* h = dynamic_cast<HOperator*>(op->op.get());
+    if (!h) throw Error(BEM_ERR_STATE, "not an H-matrix operator");
+    for (size_t k = 0; k < h->blocks.size(); ++k) {
+      if (rowcl) rowcl[k] = h->blocks[k].rowcl;
+      if (colcl) colcl[k] = h->blocks[k].colcl;
+      if (near) near[k] = h->blocks[k].near ? 1 : 0;
+      if (rank) rank[k] = h->block_rank[k];
+      if (fallback) fallback[k] = h->block_fallback[k];
+    }
+  });
+}
+
+int bem_operator_mult(bem_operator_t op, int trans, const double* alpha, const void* x, const double* beta, void* y,
+                      int nrhs, void* stream) {
+  return guarded([&] {
+    REQUIRE(op && alpha && beta && x && y, "null argument");
+    REQUIRE(nrhs >= 1, "nrhs must be >= 1");
+    op->op->mult(trans, alpha, x, beta, y, nrhs, (cudaStream_t)stream);
+  });
+}
+
+int bem_operator_mult_host(bem_operator_t op, int trans, const double* alpha, const void* x, const double* beta,
+                           void* y, int nrhs) {
+  return guarded([&] {
+    REQUIRE(op && alpha && beta && x && y, "null argument");
+    OperatorBase* o = op->op.get();
+    const size_t esz = o->cplx ? 16 : 8;
+    const size_t nin = (size_t)(trans ? o->height : o->width) * nrhs;
+    const size_t nout = (size_t)(trans ? o->width : o->height) * nrhs;
+    DevBuf dx, dy;
+    dx.alloc(nin * esz);
+    dy.alloc(nout * esz);
+    BEM_CUDA(cudaMemcpy(dx.p, x, nin * esz, cudaMemcpyHostToDevice));
+    if (beta[0] != 0.0 || beta[1] != 0.0) BEM_CUDA(cudaMemcpy(dy.p, y, nout * esz, cudaMemcpyHostToDevice));
+    o->mult(trans, alpha, dx.p, beta, dy.p, nrhs, 0);
+    BEM_CUDA(cudaMemcpy(y, dy.p, nout * esz, cudaMemcpyDeviceToHost));
+  });
+}
+
+int bem_operator_to_dense(bem_operator_t op, void* out) {
+  return guarded([&] {
+    REQUIRE(op && out, "null argument");
+    auto* h = dynamic_cast<HOperator*>(op->op.get());
+    if (!h) throw Error(BEM_ERR_STATE, "not an H-matrix operator");
+    h->to_dense(out);
+  });
+}
+
+int bem_operator_destroy(bem_operator_t op) {
+  return guarded([&] { delete op; });
+}
+
+int bem_gmres(int nterms, const bem_operator_t* ops, const double* coef, const void* b, void* x, int maxiter,
+              int restart, double tol, int* iters, double* resid, void* stream) {
+  return guarded([&] {
+    REQUIRE(ops && coef && b && x && nterms >= 1, "null argument");
+    std::vector<OperatorBase*> v;
+    for (int k = 0; k < nterms; ++k) {
+      REQUIRE(ops[k], "null operator");
+      v.push_back(ops[k]->op.get());
+    }
+    gmres_solve(nterms, v.data(), coef, b, x, maxiter, restart, tol, iters, resid, (cudaStream_t)stream);
+  });
+}
+
+}  // extern "C"

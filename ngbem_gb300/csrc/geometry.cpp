@@ -1,0 +1,484 @@
+// Mesh, trace spaces, cluster trees and the block partition.
+//
+// The cluster tree restates the reference's Rjasanow PCA bisection bit for bit
+// (ComputeClusterData src/hmat.cpp:13-150, Rja_DivideCluster :155-374, Rja_ClusterTree
+// :379-407, ClusterTree ctor :409-453) with a documented 3x3 eigen solver in place of LAPACK
+// dsyev; the partition restates Rja_AdmissiblePair (:457-471) and HMatrix_help (:587-612).
+#include <algorithm>
+#include <cmath>
+#include <numeric>
+#include <unordered_map>
+
+#include "host.hpp"
+
+namespace bem {
+
+// ------------------------------------------------------------------------------------------
+// mesh
+// ------------------------------------------------------------------------------------------
+void MeshH::build(int nv_, const double* xyz, int nt_, const int* tri) {
+  if (nv_ <= 0 || nt_ <= 0) throw Error(BEM_ERR_ARG, "mesh needs vertices and triangles");
+  nv = nv_;
+  nt = nt_;
+  X.assign(xyz, xyz + 3 * (size_t)nv);
+  T.assign(tri, tri + 3 * (size_t)nt);
+  for (int k = 0; k < 3 * nt; ++k)
+    if (T[k] < 0 || T[k] >= nv) throw Error(BEM_ERR_ARG, "triangle vertex index out of range");
+  // edges by first appearance: elements in order, local edges (0,1),(1,2),(2,0)
+  std::unordered_map<long long, int> ids;
+  ids.reserve((size_t)nt * 2);
+  TE.resize(3 * (size_t)nt);
+  E.clear();
+  for (int e = 0; e < nt; ++e)
+    for (int k = 0; k < 3; ++k) {
+      int a = T[3 * e + k], b = T[3 * e + (k + 1) % 3];
+      int lo = std::min(a, b), hi = std::max(a, b);
+      long long key = (long long)lo * nv + hi;
+      auto it = ids.find(key);
+      int id;
+      if (it == ids.end()) {
+        id = (int)(E.size() / 2);
+        ids.emplace(key, id);
+        E.push_back(lo);
+        E.push_back(hi);
+      } else {
+        id = it->second;
+      }
+      TE[3 * e + k] = id;
+    }
+  ne = (int)(E.size() / 2);
+  rec.resize(nt);
+  for (int e = 0; e < nt; ++e) {
+    ElemRec64& r = rec[e];
+    for (int k = 0; k < 3; ++k)
+      for (int c = 0; c < 3; ++c) r.p[k][c] = X[3 * (size_t)T[3 * e + k] + c];
+    double J0[3], J1[3];
+    for (int c = 0; c < 3; ++c) {
+      J0[c] = r.p[0][c] - r.p[2][c];
+      J1[c] = r.p[1][c] - r.p[2][c];
+    }
+    const double cr[3] = {J0[1] * J1[2] - J0[2] * J1[1], J0[2] * J1[0] - J0[0] * J1[2], J0[0] * J1[1] - J0[1] * J1[0]};
+    r.detJ = std::sqrt(cr[0] * cr[0] + cr[1] * cr[1] + cr[2] * cr[2]);
+    if (!(r.detJ > 0.0)) throw Error(BEM_ERR_ARG, "degenerate triangle " + std::to_string(e));
+    r.invdetJ = 1.0 / r.detJ;
+    for (int c = 0; c < 3; ++c) r.n[c] = cr[c] / r.detJ;
+    // surface gradients of the hat functions: J (J^T J)^{-1} grad_ref, rotated by n x .
+    const double g00 = J0[0] * J0[0] + J0[1] * J0[1] + J0[2] * J0[2];
+    const double g01 = J0[0] * J1[0] + J0[1] * J1[1] + J0[2] * J1[2];
+    const double g11 = J1[0] * J1[0] + J1[1] * J1[1] + J1[2] * J1[2];
+    const double det = g00 * g11 - g01 * g01;
+    const double gh[3][2] = {{1.0, 0.0}, {0.0, 1.0}, {-1.0, -1.0}};
+    for (int a = 0; a < 3; ++a) {
+      const double c0 = (g11 * gh[a][0] - g01 * gh[a][1]) / det;
+      const double c1 = (-g01 * gh[a][0] + g00 * gh[a][1]) / det;
+      double g[3];
+      for (int c = 0; c < 3; ++c) g[c] = J0[c] * c0 + J1[c] * c1;
+      r.rot[a][0] = r.n[1] * g[2] - r.n[2] * g[1];
+      r.rot[a][1] = r.n[2] * g[0] - r.n[0] * g[2];
+      r.rot[a][2] = r.n[0] * g[1] - r.n[1] * g[0];
+    }
+    r.pad[0] = 0.0;
+  }
+}
+
+void MeshH::map(int e, double xi, double eta, double* x) const {
+  const ElemRec64& r = rec[e];
+  const double l2 = 1.0 - xi - eta;
+  for (int c = 0; c < 3; ++c) x[c] = xi * r.p[0][c] + eta * r.p[1][c] + l2 * r.p[2][c];
+}
+
+void MeshH::ensure_device() {
+  std::lock_guard<std::mutex> lk(mu);
+  if (dev_ready) return;
+  std::vector<int4> t4(nt);
+  for (int e = 0; e < nt; ++e) t4[e] = make_int4(T[3 * e], T[3 * e + 1], T[3 * e + 2], 0);
+  d_tri.upload(t4);
+  d_rec64.upload(rec);
+  BEM_CUDA(cudaDeviceSynchronize());
+  dev_ready = true;
+}
+
+template <class P>
+static void build_tables(const MeshH& m, const TrigRule& r, std::vector<ElemRecP<P>>& recs,
+                         std::vector<QPt<P>>& qoff, std::vector<APt<P>>& apts, std::vector<P>& rq) {
+  const int nq = (int)r.w.size();
+  recs.resize(m.nt);
+  qoff.resize((size_t)m.nt * nq);
+  apts.resize((size_t)m.nt * nq);
+  rq.resize(2 * nq);
+  for (int q = 0; q < nq; ++q) {
+    rq[2 * q] = (P)r.xi[q];
+    rq[2 * q + 1] = (P)r.eta[q];
+  }
+  for (int e = 0; e < m.nt; ++e) {
+    const ElemRec64& s = m.rec[e];
+    ElemRecP<P>& d = recs[e];
+    double c[3];
+    for (int k = 0; k < 3; ++k) c[k] = (s.p[0][k] + s.p[1][k] + s.p[2][k]) / 3.0;
+    for (int k = 0; k < 3; ++k) {
+      d.chi[k] = (P)c[k];
+      d.clo[k] = (P)(c[k] - (double)d.chi[k]);
+      d.n[k] = (P)s.n[k];
+    }
+    d.detJ = (P)s.detJ;
+    d.invdetJ = (P)s.invdetJ;
+    for (int a = 0; a < 3; ++a)
+      for (int k = 0; k < 3; ++k) {
+        d.o[a][k] = (P)(s.p[a][k] - c[k]);
+        d.rot[a][k] = (P)s.rot[a][k];
+      }
+    d.pad[0] = d.pad[1] = d.pad[2] = (P)0;
+    for (int q = 0; q < nq; ++q) {
+      double x[3];
+      m.map(e, r.xi[q], r.eta[q], x);
+      const double w = r.w[q] * s.detJ;
+      QPt<P>& qo = qoff[(size_t)e * nq + q];
+      qo.x = (P)(x[0] - c[0]);
+      qo.y = (P)(x[1] - c[1]);
+      qo.z = (P)(x[2] - c[2]);
+      qo.w = (P)w;
+      APt<P>& ap = apts[(size_t)e * nq + q];
+      ap.hx = (P)x[0];
+      ap.hy = (P)x[1];
+      ap.hz = (P)x[2];
+      ap.lx = (P)(x[0] - (double)ap.hx);
+      ap.ly = (P)(x[1] - (double)ap.hy);
+      ap.lz = (P)(x[2] - (double)ap.hz);
+      ap.w = (P)w;
+      ap.pad = (P)0;
+    }
+  }
+}
+
+MeshH::RuleTables& MeshH::rule_tables(int order) {
+  ensure_device();
+  std::lock_guard<std::mutex> lk(mu);
+  auto it = tables.find(order);
+  if (it != tables.end()) return *it->second;
+  auto t = std::make_unique<RuleTables>();
+  TrigRule r = make_trig_rule(order);
+  t->nq = (int)r.w.size();
+  {
+    std::vector<ElemRecP<double>> recs;
+    std::vector<QPt<double>> qo;
+    std::vector<APt<double>> ap;
+    std::vector<double> rq;
+    build_tables<double>(*this, r, recs, qo, ap, rq);
+    t->rec[0].upload(recs);
+    t->qoff[0].upload(qo);
+    t->apts[0].upload(ap);
+    t->rq[0].upload(rq);
+    BEM_CUDA(cudaDeviceSynchronize());
+  }
+  {
+    std::vector<ElemRecP<float>> recs;
+    std::vector<QPt<float>> qo;
+    std::vector<APt<float>> ap;
+    std::vector<float> rq;
+    build_tables<float>(*this, r, recs, qo, ap, rq);
+    t->rec[1].upload(recs);
+    t->qoff[1].upload(qo);
+    t->apts[1].upload(ap);
+    t->rq[1].upload(rq);
+    BEM_CUDA(cudaDeviceSynchronize());
+  }
+  auto& ref = *t;
+  tables[order] = std::move(t);
+  return ref;
+}
+
+// ------------------------------------------------------------------------------------------
+// trace spaces
+// ------------------------------------------------------------------------------------------
+void SpaceH::build(MeshH* m, int kind_, int dual_) {
+  mesh = m;
+  kind = kind_;
+  dual = dual_ ? 1 : 0;
+  dofs.assign(3 * (size_t)m->nt, 0);
+  sign.assign(3 * (size_t)m->nt, 1);
+  if (kind == BEM_P0) {
+    nd = 1;
+    ndof = m->nt;
+    for (int e = 0; e < m->nt; ++e) dofs[3 * e] = dofs[3 * e + 1] = dofs[3 * e + 2] = e;
+  } else if (kind == BEM_P1) {
+    nd = 3;
+    ndof = m->nv;
+    dofs = m->T;
+  } else if (kind == BEM_RT0) {
+    nd = 3;
+    ndof = m->ne;
+    dofs = m->TE;
+    for (int e = 0; e < m->nt; ++e)
+      for (int k = 0; k < 3; ++k) sign[3 * e + k] = m->T[3 * e + k] < m->T[3 * e + (k + 1) % 3] ? 1 : -1;
+  } else {
+    throw Error(BEM_ERR_ARG, "unknown space kind");
+  }
+  // dof -> elements (CSR, ascending element ids)
+  e4d_ptr.assign(ndof + 1, 0);
+  for (int e = 0; e < m->nt; ++e)
+    for (int a = 0; a < nd; ++a) e4d_ptr[dofs[3 * e + a] + 1]++;
+  for (int d = 0; d < ndof; ++d) e4d_ptr[d + 1] += e4d_ptr[d];
+  e4d.assign(e4d_ptr[ndof], 0);
+  std::vector<int> fill(e4d_ptr.begin(), e4d_ptr.end() - 1);
+  for (int e = 0; e < m->nt; ++e)
+    for (int a = 0; a < nd; ++a) e4d[fill[dofs[3 * e + a]]++] = e;
+  for (int d = 0; d < ndof; ++d)
+    if (e4d_ptr[d + 1] == e4d_ptr[d]) throw Error(BEM_ERR_ARG, "space has a dof without elements");
+}
+
+void SpaceH::ensure_device() {
+  if (d_dofs.p) return;
+  std::vector<int4> d4(mesh->nt), s4(mesh->nt);
+  for (int e = 0; e < mesh->nt; ++e) {
+    d4[e] = make_int4(dofs[3 * e], dofs[3 * e + 1], dofs[3 * e + 2], 0);
+    s4[e] = make_int4(sign[3 * e], sign[3 * e + 1], sign[3 * e + 2], 0);
+  }
+  d_dofs.upload(d4);
+  d_sign.upload(s4);
+  BEM_CUDA(cudaDeviceSynchronize());
+}
+
+int trace_kind(int space_kind, int ev) {
+  if (space_kind == BEM_P0) return ev == BEM_EV_ID ? TR_P0 : -1;
+  if (space_kind == BEM_P1) {
+    if (ev == BEM_EV_ID) return TR_P1;
+    if (ev == BEM_EV_ROT) return TR_ROT;
+    if (ev == BEM_EV_HELM) return TR_HELM;
+    return -1;
+  }
+  if (space_kind == BEM_RT0) {
+    if (ev == BEM_EV_MAXWELL) return TR_MAX;
+    if (ev == BEM_EV_ID) return TR_RT0ID;
+    return -1;
+  }
+  return -1;
+}
+
+// ------------------------------------------------------------------------------------------
+// cluster tree
+// ------------------------------------------------------------------------------------------
+// ComputeClusterData: dof weights (mean adjacent area) and points (vertex if the dof has more
+// than two elements, edge midpoint if two, centroid if one); the last element wins.
+static void cluster_data(const SpaceH& sp, std::vector<double>& G, std::vector<std::array<double, 3>>& X) {
+  const MeshH& m = *sp.mesh;
+  const int ndof = sp.ndof;
+  G.assign(ndof, 0.0);
+  X.assign(ndof, {0.0, 0.0, 0.0});
+  std::vector<int> cnt(ndof, 0);
+  for (int e = 0; e < m.nt; ++e)
+    for (int a = 0; a < sp.nd; ++a) {
+      const int d = sp.el_dofs(e)[a];
+      G[d] += m.area(e);
+      cnt[d] += 1;
+    }
+  static const double xhat[7][2] = {{1, 0}, {0, 1}, {0, 0}, {0.5, 0.5}, {0, 0.5}, {0.5, 0}, {1. / 3, 1. / 3}};
+  for (int e = 0; e < m.nt; ++e) {
+    double pt[7][3];
+    for (int j = 0; j < 7; ++j) m.map(e, xhat[j][0], xhat[j][1], pt[j]);
+    const int* dn = sp.el_dofs(e);
+    int nvert = 0, nedge = 0;
+    for (int a = 0; a < sp.nd; ++a) {
+      const int c = cnt[dn[a]];
+      if (c > 2) { X[dn[a]] = {pt[nvert][0], pt[nvert][1], pt[nvert][2]}; ++nvert; }
+      if (c == 2) ++nedge;
+      if (c == 1) X[dn[a]] = {pt[6][0], pt[6][1], pt[6][2]};
+    }
+    const int per_edge = nedge / 3;
+    int ie = 0;
+    for (int a = 0; a < sp.nd; ++a) {
+      if (cnt[dn[a]] != 2) continue;
+      for (int o = 0; o < per_edge; ++o) X[dn[a + o]] = {pt[3 + ie][0], pt[3 + ie][1], pt[3 + ie][2]};
+      ++ie;
+      a += per_edge - 1;
+    }
+  }
+  for (int i = 0; i < ndof; ++i) G[i] /= (double)cnt[i];
+}
+
+void ClusterTreeH::build(const SpaceH& sp, int leafsize) {
+  std::vector<double> G;
+  std::vector<std::array<double, 3>> X;
+  cluster_data(sp, G, X);
+  const int n = sp.ndof;
+  perm.resize(n);
+  std::iota(perm.begin(), perm.end(), 0);
+  cl.clear();
+  ClusterH root;
+  root.Number = n;
+  cl.push_back(root);
+  for (size_t ic = 0; ic < cl.size(); ++ic) {
+    const int cnum = (int)cl[ic].Number;
+    const int b = (int)cl[ic].PermuPos;
+    const int e = b + cnum - 1;
+    double mom[10] = {0.};
+    for (int i = b; i <= e; ++i) {
+      const int j = perm[i];
+      mom[0] += G[j];
+      mom[1] += G[j] * X[j][0];
+      mom[2] += G[j] * X[j][1];
+      mom[3] += G[j] * X[j][2];
+      mom[4] += G[j] * X[j][0] * X[j][0];
+      mom[5] += G[j] * X[j][0] * X[j][1];
+      mom[6] += G[j] * X[j][0] * X[j][2];
+      mom[7] += G[j] * X[j][1] * X[j][1];
+      mom[8] += G[j] * X[j][1] * X[j][2];
+      mom[9] += G[j] * X[j][2] * X[j][2];
+    }
+    const double ctr[3] = {mom[1] / mom[0], mom[2] / mom[0], mom[3] / mom[0]};
+    std::vector<double> cov(9);
+    cov[0] = mom[4] - ctr[0] * mom[1];
+    cov[1] = mom[5] - ctr[0] * mom[2];
+    cov[2] = mom[6] - ctr[0] * mom[3];
+    cov[3] = cov[1];
+    cov[4] = mom[7] - ctr[1] * mom[2];
+    cov[5] = mom[8] - ctr[1] * mom[3];
+    cov[6] = cov[2];
+    cov[7] = cov[5];
+    cov[8] = mom[9] - ctr[2] * mom[3];
+    std::vector<double> W, A;
+    sym_eigen(3, cov, W, A);
+
+    int jmin = 0;
+    double xmin[3] = {0, 0, 0}, xmax[3] = {0, 0, 0};
+    double radius = 0.0, dmin = 0.0;
+    for (int i = b; i <= e; ++i) {
+      const int j = perm[i];
+      const double df[3] = {X[j][0] - ctr[0], X[j][1] - ctr[1], X[j][2] - ctr[2]};
+      const double dist = std::sqrt(df[0] * df[0] + df[1] * df[1] + df[2] * df[2]);
+      if (i == b || dist < dmin) { jmin = j; dmin = dist; }
+      double xt[3];
+      for (int r = 0; r < 3; ++r) xt[r] = A[3 * r] * df[0] + A[3 * r + 1] * df[1] + A[3 * r + 2] * df[2];
+      radius = std::fmax(radius, std::sqrt(xt[0] * xt[0] + xt[1] * xt[1] + xt[2] * xt[2]));
+      if (i == b) {
+        for (int r = 0; r < 3; ++r) xmin[r] = xmax[r] = xt[r];
+      } else {
+        for (int r = 0; r < 3; ++r) {
+          xmin[r] = std::fmin(xmin[r], xt[r]);
+          xmax[r] = std::fmax(xmax[r], xt[r]);
+        }
+      }
+    }
+    const double dg[3] = {xmax[0] - xmin[0], xmax[1] - xmin[1], xmax[2] - xmin[2]};
+    {
+      ClusterH& C = cl[ic];
+      C.BasisElement = jmin;
+      C.Radius = radius;
+      C.DiagLength = std::sqrt(dg[0] * dg[0] + dg[1] * dg[1] + dg[2] * dg[2]);
+      for (int k = 0; k < 3; ++k) {
+        C.EVal[k] = W[k];
+        C.XMin[k] = xmin[k];
+        C.XMax[k] = xmax[k];
+        C.Centre[k] = ctr[k];
+      }
+      for (int k = 0; k < 9; ++k) C.EVec[k] = A[k];
+      C.Child1 = C.Child2 = -1;
+    }
+    if (cnum <= leafsize) continue;
+    // split on the principal axis by an in-place swap partition
+    int n1 = 0, n2 = 0, chk = b, end = e;
+    const double crit = ctr[0] * A[6] + ctr[1] * A[7] + ctr[2] * A[8];
+    for (int i = 0; i < cnum; ++i) {
+      const int j = perm[chk];
+      if (X[j][0] * A[6] + X[j][1] * A[7] + X[j][2] * A[8] >= crit) {
+        ++n1;
+        ++chk;
+      } else {
+        ++n2;
+        perm[chk] = perm[end];
+        perm[end] = j;
+        --end;
+      }
+    }
+    if (n1 == 0 || n2 == 0) continue;
+    ClusterH c1, c2;
+    c1.Level = c2.Level = cl[ic].Level + 1;
+    c1.Parent = c2.Parent = (long)ic;
+    c1.Number = n1;
+    c1.PermuPos = b;
+    c2.Number = n2;
+    c2.PermuPos = b + n1;
+    cl[ic].Child1 = (long)cl.size();
+    cl[ic].Child2 = (long)cl.size() + 1;
+    cl.push_back(c1);
+    cl.push_back(c2);
+  }
+  pinv.assign(n, 0);
+  for (int k = 0; k < n; ++k) pinv[perm[k]] = k;
+}
+
+void ClusterTreeH::build_patches(const SpaceH& sp) {
+  const int nc = (int)cl.size();
+  std::vector<std::vector<int>> pl(nc);
+  for (int c = nc - 1; c >= 0; --c) {
+    const ClusterH& C = cl[c];
+    std::vector<int>& out = pl[c];
+    if (sp.kind == BEM_P0) {
+      out.assign(perm.begin() + C.PermuPos, perm.begin() + C.PermuPos + C.Number);
+      continue;
+    }
+    if (C.Child1 >= 0) {
+      const auto& a = pl[C.Child1];
+      const auto& b = pl[C.Child2];
+      out.reserve(a.size() + b.size());
+      std::set_union(a.begin(), a.end(), b.begin(), b.end(), std::back_inserter(out));
+    } else {
+      for (long k = C.PermuPos; k < C.PermuPos + C.Number; ++k) {
+        const int d = perm[k];
+        out.insert(out.end(), sp.e4d.begin() + sp.e4d_ptr[d], sp.e4d.begin() + sp.e4d_ptr[d + 1]);
+      }
+      std::sort(out.begin(), out.end());
+      out.erase(std::unique(out.begin(), out.end()), out.end());
+    }
+  }
+  patch_ptr.assign(nc + 1, 0);
+  for (int c = 0; c < nc; ++c) patch_ptr[c + 1] = patch_ptr[c] + (int)pl[c].size();
+  patch.resize(patch_ptr[nc]);
+  patch_rad.assign(nc, 0.0);
+  const MeshH& m = *sp.mesh;
+  for (int c = 0; c < nc; ++c) {
+    std::copy(pl[c].begin(), pl[c].end(), patch.begin() + patch_ptr[c]);
+    double r2 = 0.0;
+    for (int e : pl[c])
+      for (int k = 0; k < 3; ++k) {
+        const double* v = &m.X[3 * (size_t)m.T[3 * e + k]];
+        const double dx = v[0] - cl[c].Centre[0], dy = v[1] - cl[c].Centre[1], dz = v[2] - cl[c].Centre[2];
+        r2 = std::max(r2, dx * dx + dy * dy + dz * dz);
+      }
+    patch_rad[c] = std::sqrt(r2);
+  }
+}
+
+// ------------------------------------------------------------------------------------------
+// partition
+// ------------------------------------------------------------------------------------------
+static bool admissible(const ClusterH& a, const ClusterH& b, double eta) {
+  const double df[3] = {a.Centre[0] - b.Centre[0], a.Centre[1] - b.Centre[1], a.Centre[2] - b.Centre[2]};
+  double dist = std::sqrt(df[0] * df[0] + df[1] * df[1] + df[2] * df[2]);
+  dist = std::fmax(0., dist - a.Radius - b.Radius);
+  return std::fmin(a.Radius, b.Radius) < eta * dist;
+}
+
+void partition_blocks(const ClusterTreeH& row, const ClusterTreeH& col, double eta, std::vector<BlockH>& out) {
+  out.clear();
+  // depth-first, children in the order (1,1), (1,2), (2,1), (2,2)
+  std::vector<std::pair<long, long>> stack;
+  stack.push_back({0, 0});
+  while (!stack.empty()) {
+    auto [i, j] = stack.back();
+    stack.pop_back();
+    const ClusterH& rc = row.cl[i];
+    const ClusterH& cc = col.cl[j];
+    if (rc.Child1 == -1 || cc.Child1 == -1) {
+      out.push_back({(int)i, (int)j, true});
+    } else if (admissible(rc, cc, eta)) {
+      out.push_back({(int)i, (int)j, false});
+    } else {
+      stack.push_back({rc.Child2, cc.Child2});
+      stack.push_back({rc.Child2, cc.Child1});
+      stack.push_back({rc.Child1, cc.Child2});
+      stack.push_back({rc.Child1, cc.Child1});
+    }
+  }
+}
+
+}  // namespace bem

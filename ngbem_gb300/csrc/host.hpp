@@ -1,0 +1,202 @@
+// Host-side structures of the operator path: quadrature rules, mesh, trace spaces, cluster
+// trees, the block partition and the assembled H-matrix.  Compiled with -ffp-contract=off so
+// that the cluster tree is bit-identical across hosts (it must match the oracle bit for bit).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <array>
+#include <climits>
+#include <cstdint>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/ngbem_gb300.h"
+#include "bem_shared.h"
+#include "kernels.h"
+
+namespace bem {
+
+struct Error : std::runtime_error {
+  int code;
+  Error(int c, const std::string& m) : std::runtime_error(m), code(c) {}
+};
+
+#define BEM_CUDA(call)                                                                          \
+  do {                                                                                          \
+    cudaError_t e_ = (call);                                                                    \
+    if (e_ != cudaSuccess)                                                                      \
+      throw ::bem::Error(BEM_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_));     \
+  } while (0)
+
+// Device buffer owned by RAII.
+struct DevBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+  DevBuf() = default;
+  DevBuf(const DevBuf&) = delete;
+  DevBuf& operator=(const DevBuf&) = delete;
+  ~DevBuf() { release(); }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+  }
+  void alloc(size_t n) {
+    release();
+    if (n == 0) n = 16;
+    cudaError_t e = cudaMalloc(&p, n);
+    if (e != cudaSuccess) {
+      p = nullptr;
+      throw Error(BEM_ERR_ALLOC, std::string("cudaMalloc(") + std::to_string(n) + "): " + cudaGetErrorString(e));
+    }
+    bytes = n;
+  }
+  template <class T>
+  void upload(const std::vector<T>& v, cudaStream_t s = 0) {
+    alloc(v.size() * sizeof(T));
+    if (!v.empty()) BEM_CUDA(cudaMemcpyAsync(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, s));
+  }
+  template <class T> T* as() const { return (T*)p; }
+};
+
+// ---- quadrature (quadrature.cpp) -------------------------------------------------------
+void sym_eigen(int n, std::vector<double> A, std::vector<double>& evals, std::vector<double>& evecs);
+struct TrigRule { std::vector<double> xi, eta, w; };
+TrigRule make_trig_rule(int order);
+struct SSRule { std::vector<double> x0, x1, y0, y1, w; };
+SSRule make_ss_rule(int cls, int order);
+
+// ---- mesh and spaces (geometry.cpp) -----------------------------------------------------
+struct MeshH {
+  int nv = 0, nt = 0, ne = 0;
+  std::vector<double> X;      // 3*nv
+  std::vector<int> T;         // 3*nt
+  std::vector<int> E;         // 2*ne
+  std::vector<int> TE;        // 3*nt
+  std::vector<ElemRec64> rec;
+  // device tables, built on first use
+  std::mutex mu;
+  bool dev_ready = false;
+  DevBuf d_tri, d_rec64;
+  struct RuleTables {
+    int nq = 0;
+    DevBuf rec[2], qoff[2], apts[2], rq[2];  // [0] fp64, [1] fp32
+  };
+  std::map<int, std::unique_ptr<RuleTables>> tables;  // by regular order
+  void build(int nv_, const double* xyz, int nt_, const int* tri);
+  void map(int e, double xi, double eta, double* x) const;
+  double area(int e) const { return 0.5 * rec[e].detJ; }
+  void ensure_device();
+  RuleTables& rule_tables(int order);
+};
+
+struct SpaceH {
+  MeshH* mesh = nullptr;
+  int kind = BEM_P0, nd = 1, ndof = 0, dual = 0;
+  std::vector<int> dofs;      // 3*nt (unused entries = dof 0 for P0)
+  std::vector<int> sign;      // 3*nt
+  std::vector<int> e4d_ptr, e4d;  // dof -> elements (CSR, element order)
+  DevBuf d_dofs, d_sign;
+  void build(MeshH* m, int kind_, int dual_);
+  const int* el_dofs(int e) const { return &dofs[3 * e]; }
+  void ensure_device();
+};
+
+// ---- cluster tree and partition (geometry.cpp) -----------------------------------------
+struct ClusterH {
+  long Level = 0, Parent = -1, Child1 = -1, Child2 = -1, Number = 0, PermuPos = 0, BasisElement = 0;
+  double Radius = 0, EVec[9] = {0}, EVal[3] = {0}, XMin[3] = {0}, XMax[3] = {0}, Centre[3] = {0};
+  double DiagLength = 0;
+};
+
+struct ClusterTreeH {
+  std::vector<int> perm;      // cluster position -> dof (mapcluster2glob)
+  std::vector<int> pinv;      // dof -> cluster position
+  std::vector<ClusterH> cl;
+  // element patches per cluster (elements touching a dof of the cluster)
+  std::vector<int> patch_ptr, patch;
+  std::vector<double> patch_rad;  // radius of the patch vertices around Centre
+  void build(const SpaceH& sp, int leafsize);
+  void build_patches(const SpaceH& sp);
+};
+
+struct BlockH {
+  int rowcl, colcl;
+  bool near;
+};
+void partition_blocks(const ClusterTreeH& row, const ClusterTreeH& col, double eta, std::vector<BlockH>& out);
+
+// ---- operators (operator.cpp) ------------------------------------------------------------
+struct OperatorBase {
+  virtual ~OperatorBase() = default;
+  bool cplx = false;
+  int height = 0, width = 0;
+  virtual void mult(int trans, const double* alpha, const void* x, const double* beta, void* y, int nrhs,
+                    cudaStream_t s) = 0;
+};
+
+struct HOperator : OperatorBase {
+  int kid = 0;
+  double kappa = 0.0;
+  SpaceH* trial = nullptr;
+  SpaceH* test = nullptr;
+  int trial_ev = 0, test_ev = 0, trt = 0, tet = 0;
+  bem_params_t prm{};
+  int prec = 0;           // 0 fp64, 1 mixed
+  size_t vsize = 8;       // bytes of one stored value
+  std::unique_ptr<ClusterTreeH> own_trial, own_test;
+  ClusterTreeH* ttrial = nullptr;
+  ClusterTreeH* ttest = nullptr;
+  std::vector<BlockH> blocks;
+  std::vector<int> block_rank, block_fallback;
+
+  // device data
+  DevBuf d_perm_trial, d_perm_test, d_pinv_trial, d_pinv_test;
+  std::vector<std::unique_ptr<DevBuf>> pools;  // dense and factor pools
+  DevBuf d_mvdense, d_mvlr;
+  DevBuf d_items_s1, d_items_ap, d_items_s1t, d_items_apt;
+  int n_items_s1 = 0, n_items_ap = 0, n_items_s1t = 0, n_items_apt = 0;
+  int t_len = 0;
+  DevBuf d_t, d_xp, d_yp;
+  int ws_nrhs = 0;
+  std::vector<MVDense> mvdense;
+  std::vector<MVLowRank> mvlr;
+  bem_operator_info_t info{};
+
+  void assemble();
+  void mult(int trans, const double* alpha, const void* x, const double* beta, void* y, int nrhs,
+            cudaStream_t s) override;
+  void to_dense(void* out);
+};
+
+struct MassOperator : OperatorBase {
+  // cplx (from OperatorBase) = the vectors it acts on are complex128
+  DevBuf rowptr, col, val;
+  int nrows = 0, ncols = 0;
+  std::vector<int> h_rowptr, h_col;
+  std::vector<double> h_val;
+  void build(SpaceH* trial, SpaceH* test, bool complex_vectors);
+  void mult(int trans, const double* alpha, const void* x, const double* beta, void* y, int nrhs,
+            cudaStream_t s) override;
+};
+
+int trace_kind(int space_kind, int ev);
+bool pairs_overflow(size_t ntiles);
+int gmres_solve(int nterms, OperatorBase* const* ops, const double* coef, const void* b, void* x, int maxiter,
+                int restart, double tol, int* iters, double* resid, cudaStream_t s);
+
+}  // namespace bem
+
+struct bem_mesh_s {
+  bem::MeshH m;
+};
+struct bem_space_s {
+  bem::SpaceH s;
+};
+struct bem_operator_s {
+  std::unique_ptr<bem::OperatorBase> op;
+};

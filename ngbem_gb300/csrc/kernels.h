@@ -1,0 +1,136 @@
+// Host-side declarations of the CUDA kernel launchers and their argument blocks.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "bem_shared.h"
+
+namespace bem {
+
+struct SpaceDev {
+  int tr;              // TraceKind
+  int nd;              // local dofs per element
+  int dual;            // P0 dual mapping (1/|J| scaling)
+  const int4* dofs;    // element -> dofs
+  const int4* sign;    // RT0 edge orientation per element (+1/-1)
+  const int* pinv;     // dof -> position in the cluster permutation
+};
+
+// Points of the regular triangle rule on element e: offsets from the centroid and the
+// weight w_q*|J| (QPt), or absolute position as a hi+lo pair (APt) for ACA.
+template <class P> struct QPt { P x, y, z, w; };
+template <class P> struct APt { P hx, hy, hz, lx, ly, lz, w, pad; };
+
+struct NFArgs {
+  const NFTile* tiles;
+  int ntiles;
+  const DenseDesc* blocks;
+  const int* patch_test;
+  const int* patch_trial;
+  const int4* tri;
+  SpaceDev test, trial;
+  const void* erecP;      // ElemRecP<P>[nt]
+  const void* qoff;       // QPt<P>[nt*nq]
+  const void* rq;         // reference points (xi, eta) of the regular rule, P2[nq]
+  int nq;
+  double kappa;
+  void* pool;             // dense pool, value type of the operator in storage precision
+  int atomic_scatter;     // 0: every dense entry is owned by one element pair (P0 x P0)
+  SingItem* sing;
+  int* sing_count;
+  int sing_cap;
+  int* err;
+  // singular kernel
+  const ElemRec64* erec64;
+  const double* ss[3];    // Sauter-Schwab tables: x0[n], x1[n], y0[n], y1[n], w[n]
+  int ss_n[3];
+  int ss_smem_bytes;      // > 0: stage all three tables in shared memory
+  int sing_grid;
+};
+
+struct AcaArgs {
+  const FarDesc* far;
+  int nfar;
+  const int* patch_test;
+  const int* patch_trial;
+  const void* apts;       // APt<P>[nt*nq]
+  const void* erecP;      // normals
+  int nq;
+  double kappa;
+  double eps;
+  void* U;                // scratch, value type in precision P
+  void* V;
+  int* ranks;             // [nfar][NC]
+  int* status;            // [nfar] 1 = rank cap reached
+};
+
+struct ProjArgs {
+  const FarDesc* far;
+  const LRDesc* lr;
+  int nfar;
+  const int* ranks;
+  const int* patch_test;
+  const int* patch_trial;
+  const void* erecP;
+  const void* qoff;
+  const void* rq;
+  int nq;
+  double kappa;
+  SpaceDev test, trial;
+  const void* U;          // ACA scratch
+  const void* V;
+};
+
+// kid: KernelId; prec: 0 fp64, 1 mixed; trt/tet: TraceKind of trial/test side.
+bool nf_combo_supported(int kid, int trt, int tet);
+void launch_nf_regular(int kid, int prec, int trt, int tet, const NFArgs& a, cudaStream_t s);
+void launch_nf_singular(int kid, int prec, int trt, int tet, const NFArgs& a, cudaStream_t s);
+void launch_aca(int kid, int prec, const AcaArgs& a, cudaStream_t s);
+void launch_projection(int kid, int prec, int trt, int tet, const ProjArgs& a, cudaStream_t s);
+int kernel_ncomp(int kid);
+bool kernel_complex(int kid);
+
+// ---- matvec -----------------------------------------------------------------------------
+struct MVItem {
+  int kind;    // 0 dense, 1 low rank
+  int idx;     // block index in its list
+  int start;   // first row (or column for the transposed/stage-1 passes)
+  int count;   // rows/cols in this item
+};
+
+struct MVArgs {
+  const MVDense* dense;
+  const MVLowRank* lr;
+  void* t;                 // R-vectors (storage precision), zeroed before stage 1
+  const void* xp;          // permuted input (storage precision), layout [k][nrhs]
+  void* yp;                // permuted output accumulator (fp64 or complex128), layout [k][nrhs]
+  const MVItem* items;
+  int nitems;
+  int nrhs;
+};
+
+// prec 0: fp64 storage, 1: fp32 storage.  cplx: complex operator.
+void launch_mv_stage1(int prec, bool cplx, bool trans, const MVArgs& a, cudaStream_t s);
+void launch_mv_apply(int prec, bool cplx, bool trans, const MVArgs& a, cudaStream_t s);
+// xp[k*nrhs + r] = (storage) x[r*ld + perm[k]]
+void launch_permute_in(int prec, bool cplx, const int* perm, int n, int nrhs, int ld,
+                       const void* x, void* xp, cudaStream_t s);
+// y[r*ld + perm[k]] = alpha * yp[k*nrhs + r] + beta * y[...]   (fp64 / complex128)
+void launch_permute_out(bool cplx, const int* perm, int n, int nrhs, int ld, const double* alpha,
+                        const double* beta, const void* yp, void* y, cudaStream_t s);
+// CSR SpMV in fp64: y = alpha*A x + beta*y (A real; vectors real or complex; nrhs columns)
+void launch_spmv(bool cplx, bool trans, int nrows, int ncols, const int* rowptr, const int* col,
+                 const double* val, const double* alpha, const double* beta, const void* x,
+                 void* y, int nrhs, cudaStream_t s);
+
+// ---- BLAS-1/2 helpers for GMRES (fp64 / complex128), column-major basis Q (ld = n) -------
+void launch_gemv_ct(bool cplx, int n, int k, const void* Q, const void* w, void* h, cudaStream_t s);
+void launch_gemv_sub(bool cplx, int n, int k, const void* Q, const void* h, void* w, cudaStream_t s);
+void launch_nrm2(bool cplx, int n, const void* w, double* out, cudaStream_t s);
+void launch_scale_copy(bool cplx, int n, const void* w, double inv, void* q, cudaStream_t s);
+// x += Q y  (y on device, complex or real)
+void launch_axpy_basis(bool cplx, int n, int k, const void* Q, const void* y, void* x, cudaStream_t s);
+// r = b - r  (r holds A x on input)
+void launch_residual(bool cplx, int n, const void* b, void* r, cudaStream_t s);
+
+}  // namespace bem

@@ -1,0 +1,798 @@
+// Assembly and application of the H-matrix on the GPU (reference GenericIntegralOperator
+// ctor src/ngbem.cpp:314-330, CalcHMatrix :118-157, HMatrix src/hmat.cpp:614-681).
+//
+// Assembly pipeline (one operator, two CUDA streams):
+//   host : cluster trees, element patches per cluster, partition, far blocks whose patches
+//          share a vertex are re-binned to dense (the reference throws and falls back,
+//          src/ngbem.cpp:839-842 / :143-153)
+//   sA   : batched ACA over the admissible blocks, then projection onto the dofs
+//   sN   : regular near-field kernel over all dense blocks (bins singular pairs), then the
+//          persistent FP64 Sauter-Schwab kernel over the binned singular pairs
+//   host : blocks whose ACA hit the rank cap are assembled densely in a second near pass
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <complex>
+#include <cstring>
+
+#include "host.hpp"
+
+namespace bem {
+
+using clk = std::chrono::steady_clock;
+static double ms_since(clk::time_point t0) {
+  return std::chrono::duration<double, std::milli>(clk::now() - t0).count();
+}
+
+struct StreamPair {
+  cudaStream_t a = nullptr, n = nullptr;
+  StreamPair() {
+    BEM_CUDA(cudaStreamCreateWithFlags(&a, cudaStreamNonBlocking));
+    BEM_CUDA(cudaStreamCreateWithFlags(&n, cudaStreamNonBlocking));
+  }
+  ~StreamPair() {
+    if (a) cudaStreamDestroy(a);
+    if (n) cudaStreamDestroy(n);
+  }
+};
+
+static SpaceDev space_dev(const SpaceH& s, int tr, const DevBuf& pinv) {
+  SpaceDev d;
+  d.tr = tr;
+  d.nd = s.nd;
+  d.dual = s.dual;
+  d.dofs = s.d_dofs.as<int4>();
+  d.sign = s.d_sign.as<int4>();
+  d.pinv = pinv.as<int>();
+  return d;
+}
+
+// Dense near-field pass over a list of blocks (pool owned by the caller).
+struct NearPass {
+  std::vector<DenseDesc> desc;
+  std::vector<int> block_ids;  // index into HOperator::blocks
+  DevBuf d_desc, d_tiles, d_sing, d_count, d_err;
+  long long npairs = 0;
+  int ntiles = 0;
+  int sing_cap = 0;
+};
+
+void HOperator::assemble() {
+  const auto t_start = clk::now();
+  trt = trace_kind(trial->kind, trial_ev);
+  tet = trace_kind(test->kind, test_ev);
+  if (trt < 0 || tet < 0) throw Error(BEM_ERR_ARG, "evaluator not available for this space");
+  if (!nf_combo_supported(kid, trt, tet)) throw Error(BEM_ERR_ARG, "kernel / trace combination not supported");
+  if (trial->mesh != test->mesh) throw Error(BEM_ERR_ARG, "trial and test spaces must live on one mesh");
+  cplx = kernel_complex(kid);
+  const int NC = kernel_ncomp(kid);
+  prec = prm.precision == BEM_MIXED ? 1 : 0;
+  const size_t rsz = prec == 0 ? 8 : 4;
+  vsize = rsz * (cplx ? 2 : 1);
+  const int order_s = prm.intorder_singular > 0 ? prm.intorder_singular : prm.intorder;
+  const int order_r = prm.intorder_regular > 0 ? prm.intorder_regular : prm.intorder;
+  if (order_s < 0 || order_r < 0 || order_s > 40 || order_r > 40) throw Error(BEM_ERR_ARG, "intorder out of range");
+  const bool dense_method = prm.method == BEM_METHOD_DENSE;
+  const int leaf = dense_method ? INT_MAX : prm.leafsize;
+  const double eta = dense_method ? 0.0 : prm.eta;
+  if (leaf < 1) throw Error(BEM_ERR_ARG, "leafsize must be positive");
+  int kcap = prm.max_rank > 0 ? prm.max_rank : 128;
+  kcap = std::min(kcap, 256);
+  double eps = prm.eps;
+  if (prec == 1) eps = std::max(eps, prm.aca_eps_floor > 0 ? prm.aca_eps_floor : 2e-7);
+  const long long budget = prm.scratch_bytes > 0 ? prm.scratch_bytes : (4LL << 30);
+  MeshH& mesh = *trial->mesh;
+  height = test->ndof;
+  width = trial->ndof;
+
+  // ---- trees, patches, partition (host) ------------------------------------------------
+  own_trial = std::make_unique<ClusterTreeH>();
+  own_trial->build(*trial, leaf);
+  own_trial->build_patches(*trial);
+  ttrial = own_trial.get();
+  if (test == trial) {
+    ttest = ttrial;
+  } else {
+    own_test = std::make_unique<ClusterTreeH>();
+    own_test->build(*test, leaf);
+    own_test->build_patches(*test);
+    ttest = own_test.get();
+  }
+  partition_blocks(*ttest, *ttrial, eta, blocks);
+  const int nb = (int)blocks.size();
+  block_rank.assign(nb, -1);
+  block_fallback.assign(nb, 0);
+
+  // far blocks whose patches share a vertex -> dense (reference fallback)
+  std::vector<int> stamp(mesh.nv, -1);
+  std::vector<int> far_ids, dense_ids;
+  for (int b = 0; b < nb; ++b) {
+    const BlockH& B = blocks[b];
+    if (B.near) { dense_ids.push_back(b); continue; }
+    const ClusterH& ci = ttest->cl[B.rowcl];
+    const ClusterH& cj = ttrial->cl[B.colcl];
+    const double dx = ci.Centre[0] - cj.Centre[0], dy = ci.Centre[1] - cj.Centre[1], dz = ci.Centre[2] - cj.Centre[2];
+    const double dist = std::sqrt(dx * dx + dy * dy + dz * dz);
+    bool shared = false;
+    if (dist <= ttest->patch_rad[B.rowcl] + ttrial->patch_rad[B.colcl] + 1e-12 * (1.0 + dist)) {
+      for (int k = ttest->patch_ptr[B.rowcl]; k < ttest->patch_ptr[B.rowcl + 1]; ++k) {
+        const int e = ttest->patch[k];
+        for (int v = 0; v < 3; ++v) stamp[mesh.T[3 * e + v]] = b;
+      }
+      for (int k = ttrial->patch_ptr[B.colcl]; k < ttrial->patch_ptr[B.colcl + 1] && !shared; ++k) {
+        const int e = ttrial->patch[k];
+        for (int v = 0; v < 3; ++v)
+          if (stamp[mesh.T[3 * e + v]] == b) shared = true;
+      }
+    }
+    if (shared) { block_fallback[b] = 1; dense_ids.push_back(b); }
+    else far_ids.push_back(b);
+  }
+
+  // ---- device tables ---------------------------------------------------------------------
+  mesh.ensure_device();
+  trial->ensure_device();
+  test->ensure_device();
+  MeshH::RuleTables& rt = mesh.rule_tables(order_r);
+  const int nq = rt.nq;
+  d_perm_trial.upload(ttrial->perm);
+  d_pinv_trial.upload(ttrial->pinv);
+  DevBuf d_patch_trial, d_patch_test;
+  d_patch_trial.upload(ttrial->patch);
+  if (ttest != ttrial) {
+    d_perm_test.upload(ttest->perm);
+    d_pinv_test.upload(ttest->pinv);
+    d_patch_test.upload(ttest->patch);
+  }
+  const DevBuf& pinv_test = ttest != ttrial ? d_pinv_test : d_pinv_trial;
+  const int* patch_test_dev = ttest != ttrial ? d_patch_test.as<int>() : d_patch_trial.as<int>();
+  SpaceDev sd_trial = space_dev(*trial, trt, d_pinv_trial);
+  SpaceDev sd_test = space_dev(*test, tet, pinv_test);
+  // Sauter-Schwab tables
+  DevBuf d_ss[3];
+  int ss_n[3];
+  long long ss_bytes = 0;
+  for (int c = 0; c < 3; ++c) {
+    SSRule r = make_ss_rule(c, order_s);
+    ss_n[c] = (int)r.w.size();
+    std::vector<double> tab;
+    tab.reserve(5 * r.w.size());
+    tab.insert(tab.end(), r.x0.begin(), r.x0.end());
+    tab.insert(tab.end(), r.x1.begin(), r.x1.end());
+    tab.insert(tab.end(), r.y0.begin(), r.y0.end());
+    tab.insert(tab.end(), r.y1.begin(), r.y1.end());
+    tab.insert(tab.end(), r.w.begin(), r.w.end());
+    d_ss[c].upload(tab);
+    ss_bytes += (long long)tab.size() * 8;
+  }
+  // max number of elements sharing a vertex with one element (bound for singular pairs)
+  std::vector<int> valence(mesh.nv, 0);
+  for (int k = 0; k < 3 * mesh.nt; ++k) valence[mesh.T[k]]++;
+  int maxnb = 1;
+  for (int e = 0; e < mesh.nt; ++e)
+    maxnb = std::max(maxnb, valence[mesh.T[3 * e]] + valence[mesh.T[3 * e + 1]] + valence[mesh.T[3 * e + 2]]);
+  BEM_CUDA(cudaDeviceSynchronize());
+  info.ms_setup = ms_since(t_start);
+
+  StreamPair sp;
+  cudaEvent_t evA0, evA1, evN0, evN1, evP0, evP1;
+  BEM_CUDA(cudaEventCreate(&evA0)); BEM_CUDA(cudaEventCreate(&evA1));
+  BEM_CUDA(cudaEventCreate(&evN0)); BEM_CUDA(cudaEventCreate(&evN1));
+  BEM_CUDA(cudaEventCreate(&evP0)); BEM_CUDA(cudaEventCreate(&evP1));
+  struct EvGuard {
+    cudaEvent_t* e; int n;
+    ~EvGuard() { for (int i = 0; i < n; ++i) cudaEventDestroy(e[i]); }
+  };
+  cudaEvent_t evs[6] = {evA0, evA1, evN0, evN1, evP0, evP1};
+  EvGuard eg{evs, 6};
+
+  // ---- near field (dense blocks) ----------------------------------------------------------
+  auto run_near = [&](NearPass& np, const std::vector<int>& ids, cudaStream_t s) {
+    np.block_ids = ids;
+    np.desc.clear();
+    long long off = 0;
+    std::vector<NFTile> tiles;
+    long long cap = 0;
+    for (int b : ids) {
+      const BlockH& B = blocks[b];
+      const ClusterH& ci = ttest->cl[B.rowcl];
+      const ClusterH& cj = ttrial->cl[B.colcl];
+      DenseDesc d;
+      d.off = off;
+      d.r0 = (int)ci.PermuPos;
+      d.m = (int)ci.Number;
+      d.c0 = (int)cj.PermuPos;
+      d.n = (int)cj.Number;
+      d.pi0 = ttest->patch_ptr[B.rowcl];
+      d.ni = ttest->patch_ptr[B.rowcl + 1] - d.pi0;
+      d.pj0 = ttrial->patch_ptr[B.colcl];
+      d.nj = ttrial->patch_ptr[B.colcl + 1] - d.pj0;
+      off += (long long)d.m * d.n;
+      const long long pairs = (long long)d.ni * d.nj;
+      np.npairs += pairs;
+      const int bi = (int)np.desc.size();
+      for (long long k0 = 0; k0 < pairs; k0 += 128) tiles.push_back(NFTile{bi, (int)k0});
+      // bound on singular pairs of this block
+      const double dx = ci.Centre[0] - cj.Centre[0], dy = ci.Centre[1] - cj.Centre[1], dz = ci.Centre[2] - cj.Centre[2];
+      const double dist = std::sqrt(dx * dx + dy * dy + dz * dz);
+      if (dist <= ttest->patch_rad[B.rowcl] + ttrial->patch_rad[B.colcl] + 1e-12 * (1.0 + dist))
+        cap += std::min(pairs, (long long)std::min(d.ni, d.nj) * maxnb);
+      np.desc.push_back(d);
+    }
+    if (np.desc.empty()) return std::unique_ptr<DevBuf>();
+    if (np.npairs > (long long)INT_MAX || pairs_overflow(tiles.size())) throw Error(BEM_ERR_ARG, "too many near-field tiles");
+    if (cap > (1LL << 31) - 1) throw Error(BEM_ERR_ALLOC, "singular pair list too large");
+    np.ntiles = (int)tiles.size();
+    np.sing_cap = (int)std::max<long long>(cap, 1);
+    auto pool = std::make_unique<DevBuf>();
+    pool->alloc((size_t)off * vsize);
+    BEM_CUDA(cudaMemsetAsync(pool->p, 0, (size_t)off * vsize, s));
+    np.d_desc.upload(np.desc, s);
+    np.d_tiles.upload(tiles, s);
+    np.d_sing.alloc((size_t)np.sing_cap * sizeof(SingItem));
+    np.d_count.alloc(sizeof(int));
+    np.d_err.alloc(sizeof(int));
+    BEM_CUDA(cudaMemsetAsync(np.d_count.p, 0, sizeof(int), s));
+    BEM_CUDA(cudaMemsetAsync(np.d_err.p, 0, sizeof(int), s));
+    NFArgs a{};
+    a.tiles = np.d_tiles.as<NFTile>();
+    a.ntiles = np.ntiles;
+    a.blocks = np.d_desc.as<DenseDesc>();
+    a.patch_test = patch_test_dev;
+    a.patch_trial = d_patch_trial.as<int>();
+    a.tri = mesh.d_tri.as<int4>();
+    a.test = sd_test;
+    a.trial = sd_trial;
+    a.erecP = rt.rec[prec].p;
+    a.qoff = rt.qoff[prec].p;
+    a.rq = rt.rq[prec].p;
+    a.nq = nq;
+    a.kappa = kappa;
+    a.pool = pool->p;
+    a.atomic_scatter = (trt == TR_P0 && tet == TR_P0) ? 0 : 1;
+    a.sing = np.d_sing.as<SingItem>();
+    a.sing_count = np.d_count.as<int>();
+    a.sing_cap = np.sing_cap;
+    a.err = np.d_err.as<int>();
+    a.erec64 = mesh.d_rec64.as<ElemRec64>();
+    for (int c = 0; c < 3; ++c) { a.ss[c] = d_ss[c].as<double>(); a.ss_n[c] = ss_n[c]; }
+    a.ss_smem_bytes = ss_bytes <= 160 * 1024 ? (int)ss_bytes : 0;
+    a.sing_grid = 152 * 4;
+    launch_nf_regular(kid, prec, trt, tet, a, s);
+    BEM_CUDA(cudaGetLastError());
+    launch_nf_singular(kid, prec, trt, tet, a, s);
+    BEM_CUDA(cudaGetLastError());
+    return pool;
+  };
+
+  NearPass np1;
+  BEM_CUDA(cudaEventRecord(evN0, sp.n));
+  auto pool1 = run_near(np1, dense_ids, sp.n);
+  BEM_CUDA(cudaEventRecord(evN1, sp.n));
+
+  // ---- ACA (batched by scratch budget) + projection ----------------------------------------
+  const size_t psz = rsz * (cplx ? 2 : 1);  // ACA value size (compute precision = storage precision)
+  std::vector<int> overflow_ids;
+  std::vector<LRDesc> lr_all;
+  std::vector<int> lr_block;
+  float ms_aca = 0.f, ms_proj = 0.f;
+  // plan the batches first so that the scratch is allocated once: cudaFree would
+  // synchronise the device and serialise the near-field stream with the ACA stream
+  std::vector<std::vector<FarDesc>> batches;
+  std::vector<size_t> batch_first;
+  long long max_su = 0, max_sv = 0;
+  {
+    size_t f0 = 0;
+    while (f0 < far_ids.size()) {
+    std::vector<FarDesc> fd;
+    long long su = 0, sv = 0;
+    size_t f1 = f0;
+    while (f1 < far_ids.size()) {
+      const BlockH& B = blocks[far_ids[f1]];
+      FarDesc d;
+      const ClusterH& ci = ttest->cl[B.rowcl];
+      const ClusterH& cj = ttrial->cl[B.colcl];
+      d.r0 = (int)ci.PermuPos; d.m = (int)ci.Number; d.c0 = (int)cj.PermuPos; d.n = (int)cj.Number;
+      d.pi0 = ttest->patch_ptr[B.rowcl];
+      d.ni = ttest->patch_ptr[B.rowcl + 1] - d.pi0;
+      d.pj0 = ttrial->patch_ptr[B.colcl];
+      d.nj = ttrial->patch_ptr[B.colcl + 1] - d.pj0;
+      const long long M = (long long)d.ni * nq, N = (long long)d.nj * nq;
+      d.kcap = (int)std::min<long long>(kcap, std::min(M, N));
+      d.pad = 0;
+      const long long need = (long long)NC * d.kcap * (M + N) * (long long)psz;
+      if (f1 > f0 && (su + sv) * (long long)psz + need > budget) break;
+      d.su = su;
+      d.sv = sv;
+      su += (long long)NC * d.kcap * M;
+      sv += (long long)NC * d.kcap * N;
+      fd.push_back(d);
+      ++f1;
+    }
+    max_su = std::max(max_su, su);
+    max_sv = std::max(max_sv, sv);
+    batches.push_back(std::move(fd));
+    batch_first.push_back(f0);
+    f0 = f1;
+    }
+  }
+  DevBuf d_U, d_V;
+  if (!batches.empty()) {
+    d_U.alloc((size_t)max_su * psz);
+    d_V.alloc((size_t)max_sv * psz);
+  }
+  std::vector<std::unique_ptr<DevBuf>> keep;
+  auto newbuf = [&]() { keep.push_back(std::make_unique<DevBuf>()); return keep.back().get(); };
+  for (size_t bi = 0; bi < batches.size(); ++bi) {
+    const std::vector<FarDesc>& fd = batches[bi];
+    const size_t f0 = batch_first[bi];
+    const int nf = (int)fd.size();
+    DevBuf& d_fd = *newbuf();
+    DevBuf& d_ranks = *newbuf();
+    DevBuf& d_status = *newbuf();
+    d_fd.upload(fd, sp.a);
+    d_ranks.alloc((size_t)nf * NC * sizeof(int));
+    d_status.alloc((size_t)nf * sizeof(int));
+    AcaArgs aa{};
+    aa.far = d_fd.as<FarDesc>();
+    aa.nfar = nf;
+    aa.patch_test = patch_test_dev;
+    aa.patch_trial = d_patch_trial.as<int>();
+    aa.apts = rt.apts[prec].p;
+    aa.erecP = rt.rec[prec].p;
+    aa.nq = nq;
+    aa.kappa = kappa;
+    aa.eps = eps;
+    aa.U = d_U.p;
+    aa.V = d_V.p;
+    aa.ranks = d_ranks.as<int>();
+    aa.status = d_status.as<int>();
+    BEM_CUDA(cudaEventRecord(evA0, sp.a));
+    launch_aca(kid, prec, aa, sp.a);
+    BEM_CUDA(cudaGetLastError());
+    BEM_CUDA(cudaEventRecord(evA1, sp.a));
+    std::vector<int> ranks((size_t)nf * NC), status(nf);
+    BEM_CUDA(cudaMemcpyAsync(ranks.data(), d_ranks.p, ranks.size() * sizeof(int), cudaMemcpyDeviceToHost, sp.a));
+    BEM_CUDA(cudaMemcpyAsync(status.data(), d_status.p, status.size() * sizeof(int), cudaMemcpyDeviceToHost, sp.a));
+    BEM_CUDA(cudaStreamSynchronize(sp.a));
+    float t;
+    BEM_CUDA(cudaEventElapsedTime(&t, evA0, evA1));
+    ms_aca += t;
+    // factor pool for this batch
+    std::vector<LRDesc> lr(nf);
+    std::vector<int> pranks((size_t)nf * NC, 0);
+    long long usz = 0, vsz = 0;
+    for (int f = 0; f < nf; ++f) {
+      const int b = far_ids[f0 + f];
+      LRDesc& L = lr[f];
+      L.r0 = fd[f].r0; L.m = fd[f].m; L.c0 = fd[f].c0; L.n = fd[f].n;
+      L.R = 0; L.toff = 0; L.u = 0; L.v = 0;
+      if (status[f]) { overflow_ids.push_back(b); block_fallback[b] = 2; continue; }
+      int R = 0;
+      const int nt = (kid == K_LAPLACE_HS) ? 3 : ((kid == K_HELMHOLTZ_HS || kid == K_MAXWELL_SL) ? 4 : 1);
+      for (int tt = 0; tt < nt; ++tt) {
+        const int kc = (kid == K_HELMHOLTZ_HS && tt == 3) ? 1 : 0;
+        R += ranks[(size_t)f * NC + kc];
+      }
+      for (int c = 0; c < NC; ++c) pranks[(size_t)f * NC + c] = ranks[(size_t)f * NC + c];
+      L.R = R;
+      L.u = (unsigned long long)usz;  // offsets for now
+      L.v = (unsigned long long)vsz;
+      usz += (long long)L.m * R;
+      vsz += (long long)R * L.n;
+    }
+    auto upool = std::make_unique<DevBuf>(), vpool = std::make_unique<DevBuf>();
+    upool->alloc((size_t)std::max<long long>(usz, 1) * vsize);
+    vpool->alloc((size_t)std::max<long long>(vsz, 1) * vsize);
+    BEM_CUDA(cudaMemsetAsync(upool->p, 0, upool->bytes, sp.a));
+    BEM_CUDA(cudaMemsetAsync(vpool->p, 0, vpool->bytes, sp.a));
+    for (int f = 0; f < nf; ++f) {
+      if (status[f]) continue;
+      lr[f].u = (unsigned long long)((char*)upool->p + lr[f].u * vsize);
+      lr[f].v = (unsigned long long)((char*)vpool->p + lr[f].v * vsize);
+    }
+    DevBuf& d_lr = *newbuf();
+    DevBuf& d_pr = *newbuf();
+    d_lr.upload(lr, sp.a);
+    d_pr.upload(pranks, sp.a);
+    ProjArgs pa{};
+    pa.far = d_fd.as<FarDesc>();
+    pa.lr = d_lr.as<LRDesc>();
+    pa.nfar = nf;
+    pa.ranks = d_pr.as<int>();
+    pa.patch_test = patch_test_dev;
+    pa.patch_trial = d_patch_trial.as<int>();
+    pa.erecP = rt.rec[prec].p;
+    pa.qoff = rt.qoff[prec].p;
+    pa.rq = rt.rq[prec].p;
+    pa.nq = nq;
+    pa.kappa = kappa;
+    pa.test = sd_test;
+    pa.trial = sd_trial;
+    pa.U = d_U.p;
+    pa.V = d_V.p;
+    BEM_CUDA(cudaEventRecord(evP0, sp.a));
+    launch_projection(kid, prec, trt, tet, pa, sp.a);
+    BEM_CUDA(cudaGetLastError());
+    BEM_CUDA(cudaEventRecord(evP1, sp.a));
+    BEM_CUDA(cudaStreamSynchronize(sp.a));
+    BEM_CUDA(cudaEventElapsedTime(&t, evP0, evP1));
+    ms_proj += t;
+    for (int f = 0; f < nf; ++f) {
+      if (status[f]) continue;
+      const int b = far_ids[f0 + f];
+      block_rank[b] = lr[f].R;
+      lr_all.push_back(lr[f]);
+      lr_block.push_back(b);
+    }
+    pools.push_back(std::move(upool));
+    pools.push_back(std::move(vpool));
+  }
+
+  // ---- near-field pass 1 done; pass 2 for ACA rank-cap blocks ------------------------------
+  BEM_CUDA(cudaStreamSynchronize(sp.n));
+  float ms_near = 0.f;
+  if (!np1.desc.empty()) BEM_CUDA(cudaEventElapsedTime(&ms_near, evN0, evN1));
+  auto check_pass = [&](NearPass& np) {
+    if (np.desc.empty()) return;
+    int err = 0, cnt = 0;
+    BEM_CUDA(cudaMemcpy(&err, np.d_err.p, sizeof(int), cudaMemcpyDeviceToHost));
+    BEM_CUDA(cudaMemcpy(&cnt, np.d_count.p, sizeof(int), cudaMemcpyDeviceToHost));
+    if (err || cnt > np.sing_cap) throw Error(BEM_ERR_INTERNAL, "singular pair list overflow");
+    info.n_singular_pairs += cnt;
+    info.n_regular_pairs += np.npairs - cnt;
+  };
+  check_pass(np1);
+  NearPass np2;
+  std::unique_ptr<DevBuf> pool2;
+  if (!overflow_ids.empty()) {
+    BEM_CUDA(cudaEventRecord(evN0, sp.n));
+    pool2 = run_near(np2, overflow_ids, sp.n);
+    BEM_CUDA(cudaEventRecord(evN1, sp.n));
+    BEM_CUDA(cudaStreamSynchronize(sp.n));
+    float t2 = 0.f;
+    BEM_CUDA(cudaEventElapsedTime(&t2, evN0, evN1));
+    ms_near += t2;
+    check_pass(np2);
+  }
+
+  // ---- matvec descriptors -------------------------------------------------------------------
+  mvdense.clear();
+  auto add_dense = [&](NearPass& np, DevBuf* pool) {
+    for (size_t k = 0; k < np.desc.size(); ++k) {
+      const DenseDesc& d = np.desc[k];
+      MVDense m;
+      m.ptr = (unsigned long long)((char*)pool->p + (size_t)d.off * vsize);
+      m.r0 = d.r0; m.m = d.m; m.c0 = d.c0; m.n = d.n;
+      mvdense.push_back(m);
+      info.bytes_dense += (long long)d.m * d.n * (long long)vsize;
+    }
+  };
+  if (pool1) add_dense(np1, pool1.get());
+  if (pool2) add_dense(np2, pool2.get());
+  if (pool1) pools.push_back(std::move(pool1));
+  if (pool2) pools.push_back(std::move(pool2));
+  mvlr = lr_all;
+  t_len = 0;
+  for (auto& L : mvlr) {
+    L.toff = t_len;
+    t_len += L.R;
+    info.bytes_lowrank += (long long)L.R * (L.m + L.n) * (long long)vsize;
+  }
+  std::vector<MVItem> s1, ap, s1t, apt;
+  for (int f = 0; f < (int)mvlr.size(); ++f) {
+    const LRDesc& L = mvlr[f];
+    if (L.R == 0) continue;
+    for (int j = 0; j < L.n; j += 256) s1.push_back({1, f, j, std::min(256, L.n - j)});
+    for (int i = 0; i < L.m; i += 256) ap.push_back({1, f, i, std::min(256, L.m - i)});
+    for (int i = 0; i < L.m; i += 256) s1t.push_back({1, f, i, std::min(256, L.m - i)});
+    for (int j = 0; j < L.n; j += 256) apt.push_back({1, f, j, std::min(256, L.n - j)});
+  }
+  for (int k = 0; k < (int)mvdense.size(); ++k) {
+    const MVDense& D = mvdense[k];
+    for (int i = 0; i < D.m; i += 32) ap.push_back({0, k, i, std::min(32, D.m - i)});
+    for (int j = 0; j < D.n; j += 256) apt.push_back({0, k, j, std::min(256, D.n - j)});
+  }
+  d_mvdense.upload(mvdense);
+  d_mvlr.upload(mvlr);
+  d_items_s1.upload(s1); n_items_s1 = (int)s1.size();
+  d_items_ap.upload(ap); n_items_ap = (int)ap.size();
+  d_items_s1t.upload(s1t); n_items_s1t = (int)s1t.size();
+  d_items_apt.upload(apt); n_items_apt = (int)apt.size();
+  BEM_CUDA(cudaDeviceSynchronize());
+  keep.clear();
+  d_U.release();
+  d_V.release();
+
+  // ---- info -----------------------------------------------------------------------------------
+  info.is_complex = cplx ? 1 : 0;
+  info.height = height;
+  info.width = width;
+  info.nblocks = nb;
+  info.nnear = 0;
+  info.nfar = (int)mvlr.size();
+  info.nfallback = 0;
+  info.nze = 0;
+  info.max_rank = 0;
+  info.sum_rank = 0;
+  for (int b = 0; b < nb; ++b) {
+    const ClusterH& ci = ttest->cl[blocks[b].rowcl];
+    const ClusterH& cj = ttrial->cl[blocks[b].colcl];
+    if (blocks[b].near) info.nnear++;
+    if (block_fallback[b]) info.nfallback++;
+    if (block_rank[b] >= 0) {
+      info.nze += (long long)block_rank[b] * (ci.Number + cj.Number);
+      info.max_rank = std::max(info.max_rank, block_rank[b]);
+      info.sum_rank += block_rank[b];
+    } else {
+      info.nze += (long long)ci.Number * cj.Number;
+    }
+  }
+  info.ms_aca = ms_aca;
+  info.ms_projection = ms_proj;
+  info.ms_nearfield = ms_near;
+  info.ms_total = ms_since(t_start);
+}
+
+bool pairs_overflow(size_t ntiles) { return ntiles > (size_t)INT_MAX; }
+
+// ---------------------------------------------------------------------------------------------
+void HOperator::mult(int trans, const double* alpha, const void* x, const double* beta, void* y, int nrhs,
+                     cudaStream_t s) {
+  if (nrhs < 1) throw Error(BEM_ERR_ARG, "nrhs must be >= 1");
+  const int in_n = trans ? height : width;
+  const int out_n = trans ? width : height;
+  const int nmax = std::max(height, width);
+  const size_t accsz = cplx ? 16 : 8;
+  if (ws_nrhs < nrhs) {
+    d_xp.alloc((size_t)nmax * nrhs * vsize);
+    d_yp.alloc((size_t)nmax * nrhs * accsz);
+    d_t.alloc((size_t)std::max(t_len, 1) * nrhs * vsize);
+    ws_nrhs = nrhs;
+  }
+  const int* pin = trans ? (ttest == ttrial ? d_perm_trial.as<int>() : d_perm_test.as<int>()) : d_perm_trial.as<int>();
+  const int* pout = trans ? d_perm_trial.as<int>() : (ttest == ttrial ? d_perm_trial.as<int>() : d_perm_test.as<int>());
+  launch_permute_in(prec, cplx, pin, in_n, nrhs, in_n, x, d_xp.p, s);
+  BEM_CUDA(cudaMemsetAsync(d_yp.p, 0, (size_t)out_n * nrhs * accsz, s));
+  MVArgs a{};
+  a.dense = d_mvdense.as<MVDense>();
+  a.lr = d_mvlr.as<MVLowRank>();
+  a.t = d_t.p;
+  a.xp = d_xp.p;
+  a.yp = d_yp.p;
+  a.nrhs = nrhs;
+  if (t_len > 0) {
+    BEM_CUDA(cudaMemsetAsync(d_t.p, 0, (size_t)t_len * nrhs * vsize, s));
+    a.items = trans ? d_items_s1t.as<MVItem>() : d_items_s1.as<MVItem>();
+    a.nitems = trans ? n_items_s1t : n_items_s1;
+    launch_mv_stage1(prec, cplx, trans != 0, a, s);
+  }
+  a.items = trans ? d_items_apt.as<MVItem>() : d_items_ap.as<MVItem>();
+  a.nitems = trans ? n_items_apt : n_items_ap;
+  launch_mv_apply(prec, cplx, trans != 0, a, s);
+  launch_permute_out(cplx, pout, out_n, nrhs, out_n, alpha, beta, d_yp.p, y, s);
+  BEM_CUDA(cudaGetLastError());
+}
+
+void HOperator::to_dense(void* out) {
+  const size_t esz = cplx ? 16 : 8;
+  const int chunk = std::min(width, 32);
+  DevBuf X, Y;
+  X.alloc((size_t)width * chunk * esz);
+  Y.alloc((size_t)height * chunk * esz);
+  std::vector<char> hx((size_t)width * chunk * esz), hy((size_t)height * chunk * esz);
+  const double one[2] = {1.0, 0.0}, zero[2] = {0.0, 0.0};
+  for (int c0 = 0; c0 < width; c0 += chunk) {
+    const int nc = std::min(chunk, width - c0);
+    std::fill(hx.begin(), hx.end(), 0);
+    for (int c = 0; c < nc; ++c) {
+      double* col = (double*)(hx.data() + (size_t)c * width * esz);
+      col[(size_t)(c0 + c) * (cplx ? 2 : 1)] = 1.0;
+    }
+    BEM_CUDA(cudaMemcpy(X.p, hx.data(), (size_t)width * nc * esz, cudaMemcpyHostToDevice));
+    mult(0, one, X.p, zero, Y.p, nc, 0);
+    BEM_CUDA(cudaMemcpy(hy.data(), Y.p, (size_t)height * nc * esz, cudaMemcpyDeviceToHost));
+    for (int c = 0; c < nc; ++c)
+      for (int r = 0; r < height; ++r)
+        std::memcpy((char*)out + ((size_t)r * width + c0 + c) * esz, hy.data() + ((size_t)c * height + r) * esz, esz);
+  }
+}
+
+// ---------------------------------------------------------------------------------------------
+// mass matrix <u, v> of identity traces, CSR in fp64 (rows = test dofs)
+void MassOperator::build(SpaceH* trial, SpaceH* test, bool complex_vectors) {
+  if (trial->mesh != test->mesh) throw Error(BEM_ERR_ARG, "mass matrix needs one mesh");
+  MeshH& m = *trial->mesh;
+  cplx = complex_vectors;
+  nrows = test->ndof;
+  ncols = trial->ndof;
+  height = nrows;
+  width = ncols;
+  TrigRule r = make_trig_rule(4);
+  const int nq = (int)r.w.size();
+  std::vector<std::vector<std::pair<int, double>>> rows(nrows);
+  auto shape = [&](const SpaceH& sp, int e, double xi, double eta, double S[3][3], int& dim) {
+    const ElemRec64& g = m.rec[e];
+    if (sp.kind == BEM_P0) { S[0][0] = sp.dual ? g.invdetJ : 1.0; dim = 1; return; }
+    if (sp.kind == BEM_P1) { S[0][0] = xi; S[1][0] = eta; S[2][0] = 1.0 - xi - eta; dim = 1; return; }
+    double x[3];
+    m.map(e, xi, eta, x);
+    for (int a = 0; a < 3; ++a) {
+      const int o = (a + 2) % 3;
+      for (int c = 0; c < 3; ++c) S[a][c] = sp.sign[3 * e + a] * (x[c] - g.p[o][c]) * g.invdetJ;
+    }
+    dim = 3;
+  };
+  for (int e = 0; e < m.nt; ++e)
+    for (int q = 0; q < nq; ++q) {
+      double Si[3][3], Sj[3][3];
+      int di, dj;
+      shape(*test, e, r.xi[q], r.eta[q], Si, di);
+      shape(*trial, e, r.xi[q], r.eta[q], Sj, dj);
+      if (di != dj) throw Error(BEM_ERR_ARG, "mass matrix of scalar and vector spaces");
+      const double w = r.w[q] * m.rec[e].detJ;
+      for (int a = 0; a < test->nd; ++a)
+        for (int b = 0; b < trial->nd; ++b) {
+          double s = 0.0;
+          for (int c = 0; c < di; ++c) s += Si[a][c] * Sj[b][c];
+          rows[test->el_dofs(e)[a]].push_back({trial->el_dofs(e)[b], w * s});
+        }
+    }
+  h_rowptr.assign(nrows + 1, 0);
+  h_col.clear();
+  h_val.clear();
+  for (int i = 0; i < nrows; ++i) {
+    auto& rw = rows[i];
+    std::sort(rw.begin(), rw.end(), [](auto& a, auto& b) { return a.first < b.first; });
+    for (size_t k = 0; k < rw.size();) {
+      size_t l = k;
+      double s = 0.0;
+      while (l < rw.size() && rw[l].first == rw[k].first) s += rw[l++].second;
+      h_col.push_back(rw[k].first);
+      h_val.push_back(s);
+      k = l;
+    }
+    h_rowptr[i + 1] = (int)h_col.size();
+  }
+  rowptr.upload(h_rowptr);
+  col.upload(h_col);
+  val.upload(h_val);
+  BEM_CUDA(cudaDeviceSynchronize());
+}
+
+void MassOperator::mult(int trans, const double* alpha, const void* x, const double* beta, void* y, int nrhs,
+                        cudaStream_t s) {
+  launch_spmv(cplx, trans != 0, nrows, ncols, rowptr.as<int>(), col.as<int>(), val.as<double>(), alpha, beta,
+              x, y, nrhs, s);
+  BEM_CUDA(cudaGetLastError());
+}
+
+// ---------------------------------------------------------------------------------------------
+// GMRES(restart) with CGS2 Arnoldi in fp64; the operator application is a CUDA graph.
+int gmres_solve(int nterms, OperatorBase* const* ops, const double* coef, const void* b, void* x, int maxiter,
+                int restart, double tol, int* iters, double* resid, cudaStream_t s) {
+  if (nterms < 1) throw Error(BEM_ERR_ARG, "gmres needs at least one operator");
+  const int n = ops[0]->height;
+  bool cplx = false;
+  for (int k = 0; k < nterms; ++k) {
+    if (ops[k]->height != n || ops[k]->width != n) throw Error(BEM_ERR_ARG, "gmres operators must be square and equal-sized");
+    cplx = cplx || ops[k]->cplx || coef[2 * k + 1] != 0.0;
+  }
+  for (int k = 0; k < nterms; ++k)
+    if (ops[k]->cplx != cplx)
+      throw Error(BEM_ERR_ARG, "gmres operators must all act on real or all on complex vectors");
+  restart = std::max(1, std::min(restart, maxiter > 0 ? maxiter : restart));
+  const size_t esz = cplx ? 16 : 8;
+  using C = std::complex<double>;
+  DevBuf Q, gin, gout, hdev, nrm;
+  Q.alloc((size_t)n * (restart + 1) * esz);
+  gin.alloc((size_t)n * esz);
+  gout.alloc((size_t)n * esz);
+  hdev.alloc((size_t)(restart + 2) * esz);
+  nrm.alloc(sizeof(double));
+  const double zero[2] = {0.0, 0.0}, one[2] = {1.0, 0.0};
+  auto apply_ops = [&](cudaStream_t st) {
+    for (int k = 0; k < nterms; ++k) ops[k]->mult(0, coef + 2 * k, gin.p, k == 0 ? zero : one, gout.p, 1, st);
+  };
+  // warm-up (allocates operator workspaces), then capture
+  apply_ops(s);
+  BEM_CUDA(cudaStreamSynchronize(s));
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  BEM_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+  apply_ops(s);
+  BEM_CUDA(cudaStreamEndCapture(s, &graph));
+  BEM_CUDA(cudaGraphInstantiate(&exec, graph, 0));
+  struct GraphGuard {
+    cudaGraph_t g; cudaGraphExec_t e;
+    ~GraphGuard() { if (e) cudaGraphExecDestroy(e); if (g) cudaGraphDestroy(g); }
+  } gg{graph, exec};
+
+  auto dnorm = [&](const void* v) {
+    launch_nrm2(cplx, n, v, nrm.as<double>(), s);
+    double h;
+    BEM_CUDA(cudaMemcpyAsync(&h, nrm.p, sizeof(double), cudaMemcpyDeviceToHost, s));
+    BEM_CUDA(cudaStreamSynchronize(s));
+    return h;
+  };
+  const double bnorm = dnorm(b);
+  const double bscale = bnorm > 0.0 ? bnorm : 1.0;
+  int it = 0;
+  double rel = 0.0;
+  char* Qp = (char*)Q.p;
+  for (;;) {
+    // r = b - A x
+    BEM_CUDA(cudaMemcpyAsync(gin.p, x, (size_t)n * esz, cudaMemcpyDeviceToDevice, s));
+    BEM_CUDA(cudaGraphLaunch(exec, s));
+    launch_residual(cplx, n, b, gout.p, s);
+    const double beta = dnorm(gout.p);
+    rel = beta / bscale;
+    if (rel <= tol || it >= maxiter || beta == 0.0) break;
+    launch_scale_copy(cplx, n, gout.p, 1.0 / beta, Qp, s);
+    std::vector<C> H((size_t)(restart + 1) * restart, C(0)), cs(restart), sn(restart), g(restart + 1, C(0));
+    g[0] = beta;
+    int j = 0;
+    for (; j < restart && it < maxiter; ++j, ++it) {
+      BEM_CUDA(cudaMemcpyAsync(gin.p, Qp + (size_t)j * n * esz, (size_t)n * esz, cudaMemcpyDeviceToDevice, s));
+      BEM_CUDA(cudaGraphLaunch(exec, s));
+      std::vector<C> h(j + 1, C(0));
+      for (int pass = 0; pass < 2; ++pass) {
+        launch_gemv_ct(cplx, n, j + 1, Q.p, gout.p, hdev.p, s);
+        launch_gemv_sub(cplx, n, j + 1, Q.p, hdev.p, gout.p, s);
+        std::vector<double> hh((size_t)(j + 1) * (cplx ? 2 : 1));
+        BEM_CUDA(cudaMemcpyAsync(hh.data(), hdev.p, hh.size() * 8, cudaMemcpyDeviceToHost, s));
+        BEM_CUDA(cudaStreamSynchronize(s));
+        for (int i = 0; i <= j; ++i) h[i] += cplx ? C(hh[2 * i], hh[2 * i + 1]) : C(hh[i], 0.0);
+      }
+      const double hn = dnorm(gout.p);
+      if (hn > 0.0) launch_scale_copy(cplx, n, gout.p, 1.0 / hn, Qp + (size_t)(j + 1) * n * esz, s);
+      for (int i = 0; i <= j; ++i) H[(size_t)i * restart + j] = h[i];
+      H[(size_t)(j + 1) * restart + j] = hn;
+      // apply previous rotations
+      for (int i = 0; i < j; ++i) {
+        C a = H[(size_t)i * restart + j], c2 = H[(size_t)(i + 1) * restart + j];
+        H[(size_t)i * restart + j] = std::conj(cs[i]) * a + std::conj(sn[i]) * c2;
+        H[(size_t)(i + 1) * restart + j] = -sn[i] * a + cs[i] * c2;
+      }
+      C a = H[(size_t)j * restart + j], c2 = H[(size_t)(j + 1) * restart + j];
+      double den = std::sqrt(std::norm(a) + std::norm(c2));
+      if (den == 0.0) { cs[j] = 1.0; sn[j] = 0.0; }
+      else { cs[j] = a / den; sn[j] = c2 / den; }
+      H[(size_t)j * restart + j] = std::conj(cs[j]) * a + std::conj(sn[j]) * c2;
+      H[(size_t)(j + 1) * restart + j] = 0.0;
+      g[j + 1] = -sn[j] * g[j];
+      g[j] = std::conj(cs[j]) * g[j];
+      rel = std::abs(g[j + 1]) / bscale;
+      if (rel <= tol || hn == 0.0) { ++j; ++it; break; }
+    }
+    // solve the triangular system and update x
+    const int k = j;
+    std::vector<C> yv(k, C(0));
+    for (int i = k - 1; i >= 0; --i) {
+      C sacc = g[i];
+      for (int l = i + 1; l < k; ++l) sacc -= H[(size_t)i * restart + l] * yv[l];
+      yv[i] = sacc / H[(size_t)i * restart + i];
+    }
+    std::vector<double> yh((size_t)k * (cplx ? 2 : 1));
+    for (int i = 0; i < k; ++i) {
+      if (cplx) { yh[2 * i] = yv[i].real(); yh[2 * i + 1] = yv[i].imag(); }
+      else yh[i] = yv[i].real();
+    }
+    BEM_CUDA(cudaMemcpyAsync(hdev.p, yh.data(), yh.size() * 8, cudaMemcpyHostToDevice, s));
+    launch_axpy_basis(cplx, n, k, Q.p, hdev.p, x, s);
+    BEM_CUDA(cudaStreamSynchronize(s));
+    if (rel <= tol || it >= maxiter) {
+      // final true residual
+      BEM_CUDA(cudaMemcpyAsync(gin.p, x, (size_t)n * esz, cudaMemcpyDeviceToDevice, s));
+      BEM_CUDA(cudaGraphLaunch(exec, s));
+      launch_residual(cplx, n, b, gout.p, s);
+      rel = dnorm(gout.p) / bscale;
+      break;
+    }
+  }
+  if (iters) *iters = it;
+  if (resid) *resid = rel;
+  return BEM_OK;
+}
+
+}  // namespace bem

@@ -1,0 +1,129 @@
+"""Flat triangle surface meshes used as operator inputs.
+
+NGSolve/Netgen meshes (OCC spheres, boxes) are not available here, so the operator path
+works on plain triangle meshes given as vertex coordinates and vertex triples.  The
+generators below build deterministic, consistently outward-oriented meshes:
+
+* ``icosphere(level)``: the icosahedron subdivided ``level`` times (each triangle split in
+  four at its edge midpoints) with every vertex projected to the unit sphere:
+  20*4**level triangles, 10*4**level + 2 vertices.
+* ``ellipsoid(level, axes)``: the icosphere scaled by the semi-axes.
+* ``perturbed_icosphere(level, sigma, seed)``: vertices moved radially by sigma*N(0,1).
+
+Consistent orientation matters: the common-edge Sauter-Schwab permutation assumes that
+two triangles sharing an edge traverse it in opposite directions (reference
+src/ngbem.cpp:583-586).
+"""
+from __future__ import annotations
+
+import numpy as np
+
+__all__ = ["Mesh", "icosphere", "ellipsoid", "perturbed_icosphere"]
+
+
+class Mesh:
+    """A triangle surface mesh: ``vertices`` (nv x 3 float64), ``triangles`` (nt x 3 int32)."""
+
+    def __init__(self, vertices, triangles):
+        self.vertices = np.ascontiguousarray(vertices, dtype=np.float64)
+        self.triangles = np.ascontiguousarray(triangles, dtype=np.int32)
+        if self.vertices.ndim != 2 or self.vertices.shape[1] != 3:
+            raise ValueError("vertices must be (nv, 3)")
+        if self.triangles.ndim != 2 or self.triangles.shape[1] != 3:
+            raise ValueError("triangles must be (nt, 3)")
+        if self.triangles.size and (self.triangles.min() < 0 or self.triangles.max() >= len(self.vertices)):
+            raise ValueError("triangle vertex index out of range")
+
+    @property
+    def nv(self) -> int:
+        return int(self.vertices.shape[0])
+
+    @property
+    def ne(self) -> int:
+        return int(self.triangles.shape[0])
+
+    nt = ne
+
+    def areas(self) -> np.ndarray:
+        p = self.vertices[self.triangles]
+        return 0.5 * np.linalg.norm(np.cross(p[:, 0] - p[:, 2], p[:, 1] - p[:, 2]), axis=1)
+
+    def normals(self) -> np.ndarray:
+        p = self.vertices[self.triangles]
+        c = np.cross(p[:, 0] - p[:, 2], p[:, 1] - p[:, 2])
+        return c / np.linalg.norm(c, axis=1)[:, None]
+
+    def centroids(self) -> np.ndarray:
+        return self.vertices[self.triangles].mean(axis=1)
+
+    def __repr__(self):
+        return f"Mesh(nv={self.nv}, nt={self.nt})"
+
+
+def _icosahedron():
+    t = (1.0 + np.sqrt(5.0)) / 2.0
+    v = np.array([[-1, t, 0], [1, t, 0], [-1, -t, 0], [1, -t, 0],
+                  [0, -1, t], [0, 1, t], [0, -1, -t], [0, 1, -t],
+                  [t, 0, -1], [t, 0, 1], [-t, 0, -1], [-t, 0, 1]], dtype=np.float64)
+    f = [[0, 11, 5], [0, 5, 1], [0, 1, 7], [0, 7, 10], [0, 10, 11],
+         [1, 5, 9], [5, 11, 4], [11, 10, 2], [10, 7, 6], [7, 1, 8],
+         [3, 9, 4], [3, 4, 2], [3, 2, 6], [3, 6, 8], [3, 8, 9],
+         [4, 9, 5], [2, 4, 11], [6, 2, 10], [8, 6, 7], [9, 8, 1]]
+    v = v / np.linalg.norm(v, axis=1)[:, None]
+    f = np.array(f, dtype=np.int64)
+    # orient every face outward
+    p = v[f]
+    n = np.cross(p[:, 1] - p[:, 0], p[:, 2] - p[:, 0])
+    flip = np.einsum("ij,ij->i", n, p.mean(axis=1)) < 0
+    f[flip] = f[flip][:, [0, 2, 1]]
+    return v, f
+
+
+def _subdivide(v, f):
+    verts = [tuple(x) for x in v]
+    cache = {}
+    out = np.empty((4 * len(f), 3), dtype=np.int64)
+
+    def mid(a, b):
+        key = (a, b) if a < b else (b, a)
+        idx = cache.get(key)
+        if idx is None:
+            pa, pb = verts[a], verts[b]
+            m = np.array([(pa[0] + pb[0]) * 0.5, (pa[1] + pb[1]) * 0.5, (pa[2] + pb[2]) * 0.5])
+            m = m / np.sqrt(m[0] * m[0] + m[1] * m[1] + m[2] * m[2])
+            idx = len(verts)
+            verts.append((m[0], m[1], m[2]))
+            cache[key] = idx
+        return idx
+
+    for k, (a, b, c) in enumerate(f.tolist()):
+        ab, bc, ca = mid(a, b), mid(b, c), mid(c, a)
+        out[4 * k + 0] = (a, ab, ca)
+        out[4 * k + 1] = (b, bc, ab)
+        out[4 * k + 2] = (c, ca, bc)
+        out[4 * k + 3] = (ab, bc, ca)
+    return np.array(verts, dtype=np.float64), out
+
+
+def icosphere(level: int, radius: float = 1.0) -> Mesh:
+    """Unit icosphere with 20*4**level triangles (outward normals)."""
+    if level < 0:
+        raise ValueError("level must be >= 0")
+    v, f = _icosahedron()
+    for _ in range(level):
+        v, f = _subdivide(v, f)
+    return Mesh(v * radius, f.astype(np.int32))
+
+
+def ellipsoid(level: int, axes=(1.0, 0.7, 0.5)) -> Mesh:
+    """Icosphere scaled by semi-axes ``axes``."""
+    m = icosphere(level)
+    return Mesh(m.vertices * np.asarray(axes, dtype=np.float64)[None, :], m.triangles)
+
+
+def perturbed_icosphere(level: int, sigma: float = 0.05, seed: int = 0) -> Mesh:
+    """Icosphere with vertices moved radially: r = 1 + sigma * N(0,1) (seeded)."""
+    m = icosphere(level)
+    rng = np.random.default_rng(seed)
+    r = 1.0 + sigma * rng.standard_normal(m.nv)
+    return Mesh(m.vertices * r[:, None], m.triangles)
