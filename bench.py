@@ -1,0 +1,351 @@
+#!/usr/bin/env python
+"""Benchmark of the operator path on the Laplace Dirichlet-to-Neumann workload.
+
+Workload (the reference's headline config for this metric): unit icosphere at subdivision
+level 5 (20480 triangles), Laplace single layer V on P0 (20480 dofs) and double layer K from
+P1 (10242 dofs) to P0, H-matrices with leaf size 20, eta = 2, ACA eps = 1e-8, intorder 3,
+mixed precision (FP64 Sauter-Schwab pairs, FP32 regular near field, ACA and factors),
+Dirichlet data x^2 - y^2, GMRES to 1e-8 with the matvec replayed from a CUDA graph.
+Synthetic data: the mesh is generated, the density of the timed steps is N(0,1) (seeded).
+
+A step is one H-matrix application y = V x (the per-iteration cost of the DtN solve) with
+x resident in HBM; L2 is flushed (a 512 MiB write) before every step and each step is timed
+with CUDA events on the launch stream.  value = H-matvec/s over all ranks.  The assembly
+time (metric's first half) is reported as assembly_s.  e2e = the same step through the
+host-buffer C-ABI entry point (H2D of x, D2H of y inside the timed region).
+
+--impl reference times the reference algorithm's CPU implementation (the FP64 C++ oracle,
+all host threads) on the same workload and prints the same JSON line with impl=reference.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "assembly s + H-matvec/s at 1e-6 rel.err vs FP64 plain path, 1 GB300"
+SEED = 20261203 + 2
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--level", type=int, default=5)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 plain-path comparison")
+    return ap.parse_args()
+
+
+def workload(level):
+    return {"workload": f"laplace_dtn_icosphere_L{level}", "mesh": f"unit icosphere level {level}",
+            "triangles": 20 * 4 ** level, "V": "laplace SL P0->P0", "K": "laplace DL P1->P0",
+            "leafsize": 20, "eta": 2.0, "eps": 1e-8, "intorder": 3, "precision": "mixed",
+            "step": "one H-matvec y = V x", "l2": "flushed (512 MiB write) before every step",
+            "gmres": "V u = (M/2 + K) g, g = x^2 - y^2, tol 1e-8, CUDA graph"}
+
+
+class ClockSampler:
+    """nvidia-smi clocks sampled every 200 ms while the timed region runs."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.idx = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                                          "-i", str(self.idx), "-lms", "200"], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (FileNotFoundError, OSError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.t.join(timeout=2)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_setup(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+# ---------------------------------------------------------------------------------------------
+def cpu_reference(level, nthreads=0, steps=20, warmup=2):
+    """Oracle (FP64 C++ restatement of the reference, all host threads): assembly of V and
+    matvec throughput on the same workload."""
+    import numpy as np
+    from ngbem_gb300.meshes import icosphere
+    from oracle import pyoracle as O
+    O.build()
+    m = icosphere(level)
+    t0 = time.perf_counter()
+    V = O.OracleOperator("laplace_sl", m, "P0", intorder=3, leafsize=20, eta=2.0, eps=1e-8, nthreads=nthreads)
+    t_asm = time.perf_counter() - t0
+    x = np.random.default_rng(SEED).standard_normal(V.width)
+    for _ in range(warmup):
+        V.mult(x)
+    times = []
+    for _ in range(steps):
+        t = time.perf_counter()
+        V.mult(x)
+        times.append(time.perf_counter() - t)
+    cores = nthreads or os.cpu_count()
+    return {"matvec_per_s": steps / sum(times), "assembly_s": t_asm, "cores": cores, "nze": V.nze,
+            "ms_per_step": 1e3 * sum(times) / steps, "oracle": V, "x": x}
+
+
+def run_reference(args):
+    world, rank, _ = dist_setup(args)
+    if rank != 0:
+        return
+    r = cpu_reference(args.level, 0, steps=args.steps, warmup=args.warmup)
+    v = r["matvec_per_s"]
+    line = {"metric": METRIC, "impl": "reference", "value": v, "unit": "matvec/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": r["ms_per_step"],
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "config": workload(args.level),
+            "assembly_s": r["assembly_s"], "nze": r["nze"],
+            "cpu_baseline": {"value": v, "unit": "matvec/s", "cores": r["cores"], "kind": "port",
+                             "sample": f"full workload: oracle assembly of V ({r['assembly_s']:.2f} s) then "
+                                       f"{args.steps} timed matvecs"},
+            "e2e": {"value": v, "unit": "matvec/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------------------------
+def run_ours(args):
+    import numpy as np
+    import torch
+
+    import ngbem_gb300 as nb
+
+    world, rank, local = dist_setup(args)
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    dev = torch.device("cuda", local)
+    L = args.level
+    mesh = nb.icosphere(L)
+    P0 = nb.SurfaceL2(mesh, order=0)
+    P1 = nb.H1(mesh, order=1)
+    opts = dict(intorder=3, leafsize=20, eta=2.0, eps=1e-8)
+
+    # ---- assembly (mixed precision): one warm-up construction, then timed constructions
+    def assemble(prec):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        V = nb.SingleLayerPotentialOperator(P0, precision=prec, **opts)
+        K = nb.DoubleLayerPotentialOperator(P1, P0, precision=prec, **opts)
+        torch.cuda.synchronize()
+        return V, K, time.perf_counter() - t0
+
+    V, K, _ = assemble("mixed")
+    del V, K
+    asm = []
+    for _ in range(2):
+        V, K, t = assemble("mixed")
+        asm.append(t)
+    assembly_s = min(asm)
+    info_V, info_K = V.mat.info, K.mat.info
+
+    rng = np.random.default_rng(SEED)
+    x_h = rng.standard_normal(P0.ndof)
+    x = torch.from_numpy(x_h).to(dev)
+    acc = {}
+    if not args.no_fp64:
+        V64, K64, t64 = assemble("fp64")
+        acc["assembly_s_fp64"] = t64
+        y32 = V.mat * x
+        y64 = V64.mat * x
+        acc["V_matvec_rel_err_vs_fp64"] = float(torch.linalg.vector_norm(y32 - y64) / torch.linalg.vector_norm(y64))
+        xk = torch.from_numpy(rng.standard_normal(P1.ndof)).to(dev)
+        k32, k64 = K.mat * xk, K64.mat * xk
+        acc["K_matvec_rel_err_vs_fp64"] = float(torch.linalg.vector_norm(k32 - k64) / torch.linalg.vector_norm(k64))
+
+    # ---- DtN solve: V u = (M/2 + K) g
+    M = nb.MassOperator(P1, P0)
+    vt = mesh.vertices
+    g = torch.from_numpy(vt[:, 0] ** 2 - vt[:, 1] ** 2).to(dev)
+    rhs = (0.5 * M + K.mat) * g
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    u = nb.GMRes(V.mat, rhs, maxsteps=500, tol=1e-8, restart=500)
+    torch.cuda.synchronize()
+    t_solve = time.perf_counter() - t0
+    gm = dict(nb.GMRes.last)
+    c = mesh.centroids()
+    c = c / np.linalg.norm(c, axis=1)[:, None]
+    exact = 2.0 * (c[:, 0] ** 2 - c[:, 1] ** 2)
+    areas = mesh.areas()
+    uh = u.cpu().numpy()
+    gm["solve_s"] = t_solve
+    gm["l2_err_vs_exact"] = float(np.sqrt(np.sum(areas * (uh - exact) ** 2) / np.sum(areas * exact ** 2)))
+    if not args.no_fp64:
+        rhs64 = (0.5 * M + K64.mat) * g
+        u64 = nb.GMRes(V64.mat, rhs64, maxsteps=500, tol=1e-8, restart=500)
+        acc["solution_rel_err_vs_fp64"] = float(torch.linalg.vector_norm(u - u64) / torch.linalg.vector_norm(u64))
+        gm["iterations_fp64"] = nb.GMRes.last["iterations"]
+        del V64, K64
+
+    # ---- timed steps: y = V x, L2 flushed before each step, CUDA events on the stream
+    y = V.mat.CreateColVector()
+    flush = torch.empty(512 * 2 ** 20 // 4, dtype=torch.float32, device=dev)
+    stream = torch.cuda.current_stream()
+    for _ in range(args.warmup):
+        flush.fill_(1.0)
+        V.mat.Mult(x, y)
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    sampler = ClockSampler(local)
+    sampler.start()
+    time.sleep(0.3)
+    V.mat.set_profiling(True)
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    t_wall0 = time.perf_counter()
+    for k in range(args.steps):
+        flush.fill_(1.0)
+        evs[k][0].record(stream)
+        V.mat.Mult(x, y)
+        evs[k][1].record(stream)
+    torch.cuda.synchronize()
+    t_wall = time.perf_counter() - t_wall0
+    kms, kcount = V.mat.kernel_times()
+    V.mat.set_profiling(False)
+    step_ms = [a.elapsed_time(b) for a, b in evs]
+    dev_ms = sum(step_ms)
+
+    # ---- e2e: host pinned buffers through bem_operator_mult_host
+    xh = torch.from_numpy(x_h).pin_memory()
+    yh = torch.zeros(P0.ndof, dtype=torch.float64).pin_memory()
+    xh_np, yh_np = xh.numpy(), yh.numpy()
+    for _ in range(args.warmup):
+        V.mat.mult_host(xh_np, y=yh_np)
+    e2e_t = []
+    for _ in range(args.steps):
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        V.mat.mult_host(xh_np, y=yh_np)
+        e2e_t.append(time.perf_counter() - t)
+    clocks = sampler.stop()
+    e2e_check = float(np.linalg.norm(yh_np - y.cpu().numpy()) / np.linalg.norm(y.cpu().numpy()))
+
+    if world > 1:
+        tt = torch.tensor([dev_ms, sum(e2e_t)], dtype=torch.float64, device=dev)
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        dev_ms, e2e_sum = float(tt[0]), float(tt[1])
+    else:
+        e2e_sum = sum(e2e_t)
+    value = world * args.steps / (dev_ms / 1e3)
+    e2e_value = world * args.steps / e2e_sum
+
+    # ---- roofline of the dominant kernel (apply: dense near field + U2 t)
+    import json as _j
+    peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    peak, peak_src = 6800.0, "fallback"
+    if os.path.exists(peaks_path):
+        peak, peak_src = float(_j.load(open(peaks_path))["hbm_gbs"]), "measured"
+    iv = info_V
+    vs = 4  # fp32 storage
+    n, m = V.mat.width, V.mat.height
+    apply_bytes = iv["bytes_dense"] + iv["bytes_lowrank_u"] + n * vs + iv["sum_rank"] * vs + m * 8
+    stage1_bytes = (iv["bytes_lowrank"] - iv["bytes_lowrank_u"]) + n * vs + iv["sum_rank"] * vs
+    apply_ms = kms[2] / max(kcount[2], 1)
+    stage1_ms = kms[1] / max(kcount[1], 1)
+    achieved = apply_bytes / (apply_ms * 1e-3) / 1e9
+    matvec_bytes = iv["bytes_dense"] + iv["bytes_lowrank"] + 2 * n * 8 + 2 * m * 8
+    roofline = {"bound": "hbm", "kernel": "mv_apply_kernel", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "peak_source": peak_src, "traffic": None,
+                "algorithmic_bytes": apply_bytes, "avg_launch_ms": apply_ms,
+                "stage1_GBps": stage1_bytes / (stage1_ms * 1e-3) / 1e9, "stage1_avg_ms": stage1_ms,
+                "matvec_GBps": matvec_bytes / (dev_ms / args.steps * 1e-3) / 1e9}
+    launches = int(sum(kcount))
+
+    line = {"metric": METRIC, "value": value, "unit": "matvec/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": dev_ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": workload(L), "assembly_s": assembly_s,
+            "assembly_breakdown_ms": {"V": {k: iv[k] for k in ("ms_setup", "ms_aca", "ms_nearfield", "ms_projection", "ms_total")},
+                                      "K": {k: info_K[k] for k in ("ms_setup", "ms_aca", "ms_nearfield", "ms_projection", "ms_total")}},
+            "hmatrix": {"V": {k: iv[k] for k in ("nblocks", "nnear", "nfar", "nfallback", "nze", "max_rank",
+                                                 "bytes_dense", "bytes_lowrank", "n_singular_pairs", "n_regular_pairs")},
+                        "K": {k: info_K[k] for k in ("nblocks", "nfar", "nfallback", "nze", "max_rank")}},
+            "accuracy": acc, "gmres": gm, "roofline": roofline, "gpu_launches": launches,
+            "wall_s_timed_region": t_wall, "clocks": clocks,
+            "e2e": {"value": e2e_value, "unit": "matvec/s", "h2d_bytes_per_step": P0.ndof * 8,
+                    "d2h_bytes_per_step": P0.ndof * 8, "check_rel_err": e2e_check}}
+
+    if rank == 0 and not args.no_cpu_baseline:
+        r = cpu_reference(L, 0, steps=10, warmup=1)
+        # the oracle's matvec on the same x, against our FP64-accumulated mixed result
+        yo = r["oracle"].mult(x_h)
+        line["accuracy"]["V_matvec_rel_err_vs_oracle"] = float(np.linalg.norm(y.cpu().numpy() - yo) / np.linalg.norm(yo))
+        line["cpu_baseline"] = {"value": r["matvec_per_s"], "unit": "matvec/s", "cores": r["cores"], "kind": "port",
+                                "assembly_s": r["assembly_s"],
+                                "sample": f"full workload: oracle FP64 assembly of V ({r['assembly_s']:.2f} s, "
+                                          f"{r['cores']} threads) then 10 timed matvecs"}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -69,6 +69,7 @@ typedef struct {
   int max_rank;
   long long sum_rank;
   long long bytes_dense, bytes_lowrank;  /* device storage */
+  long long bytes_lowrank_u;             /* of which U factors (m x R per block) */
   int n_singular_pairs;        /* Sauter-Schwab element pairs assembled */
   long long n_regular_pairs;   /* disjoint element pairs assembled (tensor rule) */
   double ms_setup, ms_aca, ms_nearfield, ms_projection, ms_total;  /* assembly phases */
@@ -135,6 +136,14 @@ int bem_operator_mult_host(bem_operator_t op, int trans, const double* alpha, co
 int bem_operator_to_dense(bem_operator_t op, void* out);
 
 int bem_operator_destroy(bem_operator_t op);
+
+/* Diagnostics (no counterpart in the reference, whose Timer/RegionTimer instrumentation at
+ * src/hmat.cpp:650 plays this role): when enabled, every bem_operator_mult records CUDA
+ * events on its stream around its four launches; bem_operator_kernel_times returns the
+ * accumulated milliseconds and launch counts of [permute-in, low-rank stage 1, apply,
+ * permute-out].  Enabling resets the counters. */
+int bem_operator_set_profiling(bem_operator_t op, int enable);
+int bem_operator_kernel_times(bem_operator_t op, double* ms, long long* launches);
 
 /* Restarted GMRES on A = sum_k coef[k] * ops[k] (ngsolve.krylovspace.GMRes as used by the
  * reference tests, e.g. tests/test_Laplace.py:60).  b, x: device vectors; x holds the

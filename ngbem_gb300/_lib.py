@@ -38,7 +38,7 @@ class OperatorInfo(C.Structure):
     _fields_ = [("is_complex", C.c_int), ("height", C.c_int), ("width", C.c_int), ("nblocks", C.c_int),
                 ("nnear", C.c_int), ("nfar", C.c_int), ("nfallback", C.c_int), ("nze", C.c_longlong),
                 ("max_rank", C.c_int), ("sum_rank", C.c_longlong), ("bytes_dense", C.c_longlong),
-                ("bytes_lowrank", C.c_longlong), ("n_singular_pairs", C.c_int),
+                ("bytes_lowrank", C.c_longlong), ("bytes_lowrank_u", C.c_longlong), ("n_singular_pairs", C.c_int),
                 ("n_regular_pairs", C.c_longlong), ("ms_setup", C.c_double), ("ms_aca", C.c_double),
                 ("ms_nearfield", C.c_double), ("ms_projection", C.c_double), ("ms_total", C.c_double)]
 
@@ -65,6 +65,8 @@ SIGNATURES = {
     "bem_operator_mult_host": ([_vp, C.c_int, _dp, _vp, _dp, _vp, C.c_int], C.c_int),
     "bem_operator_to_dense": ([_vp, _vp], C.c_int),
     "bem_operator_destroy": ([_vp], C.c_int),
+    "bem_operator_set_profiling": ([_vp, C.c_int], C.c_int),
+    "bem_operator_kernel_times": ([_vp, _dp, C.POINTER(C.c_longlong)], C.c_int),
     "bem_gmres": ([C.c_int, C.POINTER(_vp), _dp, _vp, _vp, C.c_int, C.c_int, C.c_double, _ip, _dp, _vp],
                   C.c_int),
 }

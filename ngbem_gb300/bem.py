@@ -339,6 +339,16 @@ class HMatrix(_NativeMatrix):
         check(lib.bem_operator_blocks(self.h, *[a.ctypes.data_as(_lib._ip) for a in arrs]))
         return dict(zip(["rowcl", "colcl", "near", "rank", "fallback"], arrs))
 
+    def set_profiling(self, enable: bool = True):
+        check(lib.bem_operator_set_profiling(self.h, int(bool(enable))))
+
+    def kernel_times(self):
+        """Accumulated (ms, launches) of [permute_in, stage1, apply, permute_out]."""
+        ms = (C.c_double * 4)()
+        n = (C.c_longlong * 4)()
+        check(lib.bem_operator_kernel_times(self.h, ms, n))
+        return list(ms), list(n)
+
     def to_dense(self) -> np.ndarray:
         dt = np.complex128 if self.is_complex else np.float64
         out = np.zeros((self.height, self.width), dtype=dt)

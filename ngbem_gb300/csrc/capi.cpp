@@ -234,13 +234,14 @@ int bem_operator_mult_host(bem_operator_t op, int trans, const double* alpha, co
     const size_t esz = o->cplx ? 16 : 8;
     const size_t nin = (size_t)(trans ? o->height : o->width) * nrhs;
     const size_t nout = (size_t)(trans ? o->width : o->height) * nrhs;
-    DevBuf dx, dy;
-    dx.alloc(nin * esz);
-    dy.alloc(nout * esz);
-    BEM_CUDA(cudaMemcpy(dx.p, x, nin * esz, cudaMemcpyHostToDevice));
-    if (beta[0] != 0.0 || beta[1] != 0.0) BEM_CUDA(cudaMemcpy(dy.p, y, nout * esz, cudaMemcpyHostToDevice));
-    o->mult(trans, alpha, dx.p, beta, dy.p, nrhs, 0);
-    BEM_CUDA(cudaMemcpy(y, dy.p, nout * esz, cudaMemcpyDeviceToHost));
+    if (o->stage_x.bytes < nin * esz) o->stage_x.alloc(nin * esz);
+    if (o->stage_y.bytes < nout * esz) o->stage_y.alloc(nout * esz);
+    BEM_CUDA(cudaMemcpyAsync(o->stage_x.p, x, nin * esz, cudaMemcpyHostToDevice, 0));
+    if (beta[0] != 0.0 || beta[1] != 0.0)
+      BEM_CUDA(cudaMemcpyAsync(o->stage_y.p, y, nout * esz, cudaMemcpyHostToDevice, 0));
+    o->mult(trans, alpha, o->stage_x.p, beta, o->stage_y.p, nrhs, 0);
+    BEM_CUDA(cudaMemcpyAsync(y, o->stage_y.p, nout * esz, cudaMemcpyDeviceToHost, 0));
+    BEM_CUDA(cudaStreamSynchronize(0));
   });
 }
 
@@ -250,6 +251,30 @@ int bem_operator_to_dense(bem_operator_t op, void* out) {
     auto* h = dynamic_cast<HOperator*>(op->op.get());
     if (!h) throw Error(BEM_ERR_STATE, "not an H-matrix operator");
     h->to_dense(out);
+  });
+}
+
+int bem_operator_set_profiling(bem_operator_t op, int enable) {
+  return guarded([&] {
+    REQUIRE(op, "null argument");
+    auto* h = dynamic_cast<HOperator*>(op->op.get());
+    if (!h) throw Error(BEM_ERR_STATE, "not an H-matrix operator");
+    h->collect_profile();
+    h->profiling = enable != 0;
+    for (int k = 0; k < 4; ++k) { h->kms[k] = 0.0; h->kcount[k] = 0; }
+  });
+}
+
+int bem_operator_kernel_times(bem_operator_t op, double* ms, long long* launches) {
+  return guarded([&] {
+    REQUIRE(op && ms, "null argument");
+    auto* h = dynamic_cast<HOperator*>(op->op.get());
+    if (!h) throw Error(BEM_ERR_STATE, "not an H-matrix operator");
+    h->collect_profile();
+    for (int k = 0; k < 4; ++k) {
+      ms[k] = h->kms[k];
+      if (launches) launches[k] = h->kcount[k];
+    }
   });
 }
 

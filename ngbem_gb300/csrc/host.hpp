@@ -135,6 +135,7 @@ struct OperatorBase {
   virtual ~OperatorBase() = default;
   bool cplx = false;
   int height = 0, width = 0;
+  DevBuf stage_x, stage_y;  // device staging for the host-buffer entry point
   virtual void mult(int trans, const double* alpha, const void* x, const double* beta, void* y, int nrhs,
                     cudaStream_t s) = 0;
 };
@@ -166,6 +167,14 @@ struct HOperator : OperatorBase {
   std::vector<MVDense> mvdense;
   std::vector<MVLowRank> mvlr;
   bem_operator_info_t info{};
+  // optional per-kernel timing of mult (CUDA events on the launch stream)
+  bool profiling = false;
+  cudaEvent_t pev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+  std::vector<std::array<cudaEvent_t, 5>> pending;  // recorded, not yet read
+  double kms[4] = {0, 0, 0, 0};                     // permute_in, stage1, apply, permute_out
+  long long kcount[4] = {0, 0, 0, 0};
+  void collect_profile();
+  ~HOperator() override;
 
   void assemble();
   void mult(int trans, const double* alpha, const void* x, const double* beta, void* y, int nrhs,

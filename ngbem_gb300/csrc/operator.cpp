@@ -478,6 +478,7 @@ void HOperator::assemble() {
     L.toff = t_len;
     t_len += L.R;
     info.bytes_lowrank += (long long)L.R * (L.m + L.n) * (long long)vsize;
+    info.bytes_lowrank_u += (long long)L.R * L.m * (long long)vsize;
   }
   std::vector<MVItem> s1, ap, s1t, apt;
   for (int f = 0; f < (int)mvlr.size(); ++f) {
@@ -552,8 +553,14 @@ void HOperator::mult(int trans, const double* alpha, const void* x, const double
   }
   const int* pin = trans ? (ttest == ttrial ? d_perm_trial.as<int>() : d_perm_test.as<int>()) : d_perm_trial.as<int>();
   const int* pout = trans ? d_perm_trial.as<int>() : (ttest == ttrial ? d_perm_trial.as<int>() : d_perm_test.as<int>());
+  std::array<cudaEvent_t, 5> ev{};
+  if (profiling) {
+    for (auto& e : ev) BEM_CUDA(cudaEventCreate(&e));
+    BEM_CUDA(cudaEventRecord(ev[0], s));
+  }
   launch_permute_in(prec, cplx, pin, in_n, nrhs, in_n, x, d_xp.p, s);
   BEM_CUDA(cudaMemsetAsync(d_yp.p, 0, (size_t)out_n * nrhs * accsz, s));
+  if (profiling) BEM_CUDA(cudaEventRecord(ev[1], s));
   MVArgs a{};
   a.dense = d_mvdense.as<MVDense>();
   a.lr = d_mvlr.as<MVLowRank>();
@@ -567,11 +574,36 @@ void HOperator::mult(int trans, const double* alpha, const void* x, const double
     a.nitems = trans ? n_items_s1t : n_items_s1;
     launch_mv_stage1(prec, cplx, trans != 0, a, s);
   }
+  if (profiling) BEM_CUDA(cudaEventRecord(ev[2], s));
   a.items = trans ? d_items_apt.as<MVItem>() : d_items_ap.as<MVItem>();
   a.nitems = trans ? n_items_apt : n_items_ap;
   launch_mv_apply(prec, cplx, trans != 0, a, s);
+  if (profiling) BEM_CUDA(cudaEventRecord(ev[3], s));
   launch_permute_out(cplx, pout, out_n, nrhs, out_n, alpha, beta, d_yp.p, y, s);
+  if (profiling) {
+    BEM_CUDA(cudaEventRecord(ev[4], s));
+    pending.push_back(ev);
+  }
   BEM_CUDA(cudaGetLastError());
+}
+
+void HOperator::collect_profile() {
+  for (auto& ev : pending) {
+    BEM_CUDA(cudaEventSynchronize(ev[4]));
+    for (int k = 0; k < 4; ++k) {
+      float t = 0.f;
+      BEM_CUDA(cudaEventElapsedTime(&t, ev[k], ev[k + 1]));
+      kms[k] += t;
+      kcount[k] += 1;
+    }
+    for (auto& e : ev) cudaEventDestroy(e);
+  }
+  pending.clear();
+}
+
+HOperator::~HOperator() {
+  for (auto& ev : pending)
+    for (auto& e : ev) cudaEventDestroy(e);
 }
 
 void HOperator::to_dense(void* out) {
@@ -669,8 +701,33 @@ void MassOperator::mult(int trans, const double* alpha, const void* x, const dou
 
 // ---------------------------------------------------------------------------------------------
 // GMRES(restart) with CGS2 Arnoldi in fp64; the operator application is a CUDA graph.
+static int gmres_impl(int nterms, OperatorBase* const* ops, const double* coef, const void* b, void* x, int maxiter,
+                      int restart, double tol, int* iters, double* resid, cudaStream_t s);
+
+// GMRES runs on a private stream (the legacy default stream cannot be captured into a graph),
+// ordered after the caller's stream on entry and before it on exit.
 int gmres_solve(int nterms, OperatorBase* const* ops, const double* coef, const void* b, void* x, int maxiter,
-                int restart, double tol, int* iters, double* resid, cudaStream_t s) {
+                int restart, double tol, int* iters, double* resid, cudaStream_t caller) {
+  cudaStream_t s = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  BEM_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+  struct Guard {
+    cudaStream_t& s; cudaEvent_t& a; cudaEvent_t& b;
+    ~Guard() { if (a) cudaEventDestroy(a); if (b) cudaEventDestroy(b); if (s) cudaStreamDestroy(s); }
+  } guard{s, e0, e1};
+  BEM_CUDA(cudaEventCreateWithFlags(&e0, cudaEventDisableTiming));
+  BEM_CUDA(cudaEventCreateWithFlags(&e1, cudaEventDisableTiming));
+  BEM_CUDA(cudaEventRecord(e0, caller));
+  BEM_CUDA(cudaStreamWaitEvent(s, e0, 0));
+  int rc = gmres_impl(nterms, ops, coef, b, x, maxiter, restart, tol, iters, resid, s);
+  BEM_CUDA(cudaEventRecord(e1, s));
+  BEM_CUDA(cudaStreamWaitEvent(caller, e1, 0));
+  BEM_CUDA(cudaStreamSynchronize(s));
+  return rc;
+}
+
+static int gmres_impl(int nterms, OperatorBase* const* ops, const double* coef, const void* b, void* x, int maxiter,
+                      int restart, double tol, int* iters, double* resid, cudaStream_t s) {
   if (nterms < 1) throw Error(BEM_ERR_ARG, "gmres needs at least one operator");
   const int n = ops[0]->height;
   bool cplx = false;

@@ -1,0 +1,102 @@
+"""Host-side logic on the CPU: the C-ABI library loads and exports every declared symbol,
+the cluster tree and block partition are bit-exact with the oracle, and invalid arguments
+come back as status codes (no GPU compute is called here)."""
+import ctypes as C
+import os
+import re
+
+import numpy as np
+import pytest
+
+import ngbem_gb300 as nb
+from ngbem_gb300 import _lib
+from ngbem_gb300.meshes import icosphere, ellipsoid, perturbed_icosphere
+
+HEADER = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include", "ngbem_gb300.h")
+
+
+def test_library_exports_header_symbols():
+    src = open(HEADER).read()
+    names = set(re.findall(r"^\s*(?:int|const char\*)\s+(bem_\w+)\s*\(", src, re.M))
+    assert len(names) >= 20
+    for n in names:
+        assert hasattr(_lib.lib, n), n
+    assert set(_lib.SIGNATURES) >= names
+
+
+@pytest.mark.parametrize("mesh_fn,kind,leaf", [
+    (lambda: icosphere(2), "P0", 20), (lambda: icosphere(3), "P0", 20), (lambda: icosphere(3), "P1", 20),
+    (lambda: icosphere(3), "RT0", 40), (lambda: ellipsoid(3), "P0", 40), (lambda: ellipsoid(3), "P1", 10),
+    (lambda: perturbed_icosphere(3, 0.05, 7), "P0", 20), (lambda: icosphere(4), "P0", 40),
+    (lambda: icosphere(2), "P0", 2 ** 31 - 1)])
+def test_cluster_tree_bit_exact(oracle, mesh_fn, kind, leaf):
+    m = mesh_fn()
+    sp = nb.TraceSpace(m, kind)
+    p1, ci1, cd1 = nb.cluster_tree(sp, leaf)
+    p2, ci2, cd2 = oracle.cluster_tree(m, kind, leaf)
+    assert np.array_equal(p1, p2)
+    assert np.array_equal(ci1, ci2)
+    assert np.array_equal(cd1.view(np.int64), cd2.view(np.int64))  # bit for bit
+    # a valid binary tree: children partition the parent's dof range
+    for c in range(len(ci1)):
+        lvl, par, c1, c2, num, pos, _ = ci1[c]
+        if c1 >= 0:
+            assert ci1[c1][5] == pos and ci1[c2][5] == pos + ci1[c1][4] and ci1[c1][4] + ci1[c2][4] == num
+    assert sorted(p1.tolist()) == list(range(sp.ndof))
+
+
+@pytest.mark.parametrize("trial,test,leaf,eta", [("P0", "P0", 20, 2.0), ("P1", "P0", 20, 2.0),
+                                                 ("P1", "P1", 10, 3.0), ("RT0", "RT0", 40, 2.0),
+                                                 ("P0", "P0", 20, 0.0)])
+def test_partition_matches_oracle_blocks(oracle, trial, test, leaf, eta):
+    m = icosphere(3)
+    tr = nb.TraceSpace(m, trial)
+    te = tr if test == trial else nb.TraceSpace(m, test)
+    part = nb.partition(tr, te, leaf, eta)
+    # the oracle builds the same partition inside its operator (blocks in assembly order)
+    H = oracle.OracleOperator("laplace_sl", m, trial, test, intorder=2, leafsize=leaf, eta=eta, eps=1e-3)
+    ob = H.blocks()
+    assert np.array_equal(part["rowcl"], ob["rowcl"])
+    assert np.array_equal(part["colcl"], ob["colcl"])
+    assert np.array_equal(part["near"], ob["near"])
+    if eta == 0.0:
+        assert part["near"].all()
+
+
+def test_argument_errors_are_status_codes():
+    m = icosphere(1)
+    h = C.c_void_p()
+    X = np.ascontiguousarray(m.vertices)
+    T = np.ascontiguousarray(m.triangles).copy()
+    T[0, 0] = 10 ** 6
+    st = _lib.lib.bem_mesh_create(m.nv, X.ctypes.data_as(_lib._dp), m.nt, T.ctypes.data_as(_lib._ip), C.byref(h))
+    assert st == _lib.BEM_ERR_ARG and b"out of range" in _lib.lib.bem_last_error()
+    with pytest.raises(_lib.BemError):
+        nb.TraceSpace(m, "P1", dual_mapping=True)
+    with pytest.raises(ValueError):
+        nb.TraceSpace(m, "P2")
+    with pytest.raises(NotImplementedError):
+        nb.SurfaceL2(m, order=2)
+    sp = nb.SurfaceL2(m)
+    with pytest.raises(_lib.BemError):
+        nb.cluster_tree(sp, 0)
+
+
+def test_mesh_generators():
+    for L in range(4):
+        m = icosphere(L)
+        assert m.nt == 20 * 4 ** L and m.nv == 10 * 4 ** L + 2
+        # outward orientation and closed surface (each edge shared by two triangles, opposite directions)
+        assert (np.einsum("ij,ij->i", m.normals(), m.centroids()) > 0).all()
+        e = np.concatenate([m.triangles[:, [0, 1]], m.triangles[:, [1, 2]], m.triangles[:, [2, 0]]])
+        fwd = set(map(tuple, e.tolist()))
+        assert all((b, a) in fwd for a, b in fwd)
+    el = ellipsoid(2)
+    assert np.allclose(np.abs(el.vertices).max(axis=0), [1.0, 0.7, 0.5], atol=0.02)
+
+
+def test_edge_numbering_matches_oracle(oracle):
+    m = icosphere(2)
+    sp = nb.HDivSurface(m)
+    edges, te = oracle.mesh_edges(m)
+    assert sp.ndof == len(edges) == 3 * m.nt // 2

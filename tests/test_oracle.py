@@ -1,0 +1,117 @@
+"""Known-answer tests that pin the FP64 oracle (the restatement of the reference algorithms).
+
+The reference's own tests build NGSolve/OCC meshes that cannot be regenerated here, so the
+oracle is pinned by the patterns those tests use, re-run on synthetic meshes:
+  - quadrature rules integrate polynomials / the constant exactly (intrules.cpp);
+  - Laplace SL/DL spectra on the sphere approach 1/(2l+1) and -1/(2(2l+1));
+  - the Dirichlet-to-Neumann map of the harmonic x^2-y^2 is 2(x^2-y^2) on the unit sphere
+    (pattern of tests/test_Laplace.py);
+  - ACA matvec error against the dense operator stays below eps (tests/test_aca.py:21-28);
+  - convergence of the dense operator in intorder (tests/test_SLIntegration.py:27-39).
+"""
+import math
+
+import numpy as np
+import pytest
+
+from ngbem_gb300.meshes import icosphere, ellipsoid
+
+
+@pytest.mark.parametrize("order", [1, 2, 3, 4, 5, 6, 8, 10])
+def test_trig_rule_exactness(oracle, order):
+    xi, eta, w = oracle.trig_rule(order)
+    assert len(w) == (order // 2 + 1) ** 2
+    for a in range(order + 1):
+        for b in range(order + 1 - a):
+            exact = math.factorial(a) * math.factorial(b) / math.factorial(a + b + 2)
+            assert abs((w * xi ** a * eta ** b).sum() - exact) < 1e-14
+
+
+@pytest.mark.parametrize("cls,npts", [(0, 6), (1, 5), (2, 2)])
+@pytest.mark.parametrize("order", [2, 4, 6])
+def test_sauter_schwab_rules(oracle, cls, npts, order):
+    x0, x1, y0, y1, w = oracle.ss_rule(cls, order)
+    ns = order // 2 + 1
+    assert len(w) == npts * ns ** 4
+    # integral of 1 over T x T = 1/4; all points inside the reference triangle
+    assert abs(w.sum() - 0.25) < 1e-13
+    for a, b in [(x0, x1), (y0, y1)]:
+        assert (a >= -1e-15).all() and (b >= -1e-15).all() and (a + b <= 1 + 1e-15).all()
+    # integral of x0 * y1 over T x T = (1/6)*(1/6): exact once the Duffy Jacobian times the
+    # integrand (degree 5 in xi) is integrated exactly, i.e. from order 4 on
+    if order >= 4:
+        assert abs((w * x0 * y1).sum() - 1.0 / 36.0) < 1e-12
+
+
+def test_laplace_sl_spectrum_on_sphere(oracle):
+    m = icosphere(3)
+    V = oracle.dense_matrix("laplace_sl", m, "P0", intorder=4)
+    A = m.areas()
+    ev = np.sort(np.linalg.eigvalsh(0.5 * (V + V.T) / np.sqrt(np.outer(A, A))))[::-1]
+    assert abs(ev[0] - 1.0) < 5e-3            # l = 0
+    assert np.allclose(ev[1:4], 1.0 / 3.0, atol=5e-3)   # l = 1 (three-fold)
+    assert np.allclose(ev[4:9], 1.0 / 5.0, atol=5e-3)   # l = 2 (five-fold)
+
+
+def test_laplace_dl_constant_and_dtn(oracle):
+    """K 1 = -1/2 M 1 on a closed surface (interior), and the DtN answer for x^2 - y^2."""
+    m = icosphere(3)
+    K = oracle.dense_matrix("laplace_dl", m, "P1", "P0", intorder=4)
+    M = oracle.mass_matrix(m, "P1", "P0")
+    one = np.ones(m.nv)
+    assert np.linalg.norm(K @ one + 0.5 * M @ one) / np.linalg.norm(M @ one) < 5e-3
+    V = oracle.dense_matrix("laplace_sl", m, "P0", intorder=4)
+    g = m.vertices[:, 0] ** 2 - m.vertices[:, 1] ** 2
+    u = np.linalg.solve(V, (0.5 * M + K) @ g)
+    c = m.centroids()
+    c /= np.linalg.norm(c, axis=1)[:, None]
+    exact = 2 * (c[:, 0] ** 2 - c[:, 1] ** 2)
+    A = m.areas()
+    err = np.sqrt(np.sum(A * (u - exact) ** 2) / np.sum(A * exact ** 2))
+    assert err < 0.02
+
+
+def test_sl_intorder_convergence(oracle):
+    """Pattern of tests/test_SLIntegration.py: error vs a high-order reference decreases."""
+    m = icosphere(1)
+    ref = oracle.dense_matrix("laplace_sl", m, "P0", intorder=20)
+    errs = [np.linalg.norm(oracle.dense_matrix("laplace_sl", m, "P0", intorder=p) - ref, 2) for p in (2, 4, 6, 8)]
+    assert errs[0] > errs[1] > errs[2] > errs[3]
+    assert errs[3] < 1e-6 * np.linalg.norm(ref, 2)
+
+
+@pytest.mark.parametrize("kernel,kind,kappa", [("laplace_sl", "P0", 0.0), ("helmholtz_sl", "P0", 4.0),
+                                               ("laplace_dl", "P1", 0.0)])
+def test_aca_against_dense(oracle, kernel, kind, kappa):
+    """Pattern of tests/test_aca.py: ||(Vdense - V) x|| small at eps."""
+    m = ellipsoid(3)
+    eps = 1e-6
+    H = oracle.OracleOperator(kernel, m, kind, "P0" if kernel == "laplace_dl" else kind, kappa=kappa,
+                              intorder=3, leafsize=20, eta=2.0, eps=eps)
+    D = oracle.dense_matrix(kernel, m, kind, "P0" if kernel == "laplace_dl" else kind, kappa=kappa, intorder=3)
+    assert H.nfar > 0
+    x = np.random.default_rng(4711).standard_normal(H.width)
+    err = np.linalg.norm(D @ x - H.mult(x)) / np.linalg.norm(D @ x)
+    assert err < 10 * eps
+    if kind == "P0":
+        assert H.nze < D.size   # compression pays already at 1280 dofs for P0
+
+
+def test_hmatrix_transpose_consistency(oracle):
+    m = icosphere(3)
+    H = oracle.OracleOperator("laplace_dl", m, "P1", "P0", intorder=3, leafsize=20, eta=2.0, eps=1e-8)
+    Hd = H.to_dense()
+    rng = np.random.default_rng(3)
+    x, z = rng.standard_normal(H.width), rng.standard_normal(H.height)
+    assert np.allclose(H.mult(x), Hd @ x, rtol=1e-12, atol=1e-14)
+    assert np.allclose(H.mult(z, trans=True), Hd.T @ z, rtol=1e-12, atol=1e-14)
+
+
+def test_rt0_mass_and_maxwell_symmetry(oracle):
+    m = icosphere(1)
+    Mm = oracle.mass_matrix(m, "RT0", "RT0")
+    assert np.allclose(Mm, Mm.T, atol=1e-14)
+    assert np.linalg.eigvalsh(Mm).min() > 0
+    W = oracle.dense_matrix("maxwell_sl", m, "RT0", kappa=2.0, trial_eval="maxwell", intorder=6)
+    # the Maxwell single-layer Galerkin matrix is complex symmetric up to quadrature error
+    assert np.linalg.norm(W - W.T) / np.linalg.norm(W) < 1e-3
