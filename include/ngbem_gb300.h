@@ -73,6 +73,9 @@ typedef struct {
   int n_singular_pairs;        /* Sauter-Schwab element pairs assembled */
   long long n_regular_pairs;   /* disjoint element pairs assembled (tensor rule) */
   double ms_setup, ms_aca, ms_nearfield, ms_projection, ms_total;  /* assembly phases */
+  int mv_items[4];             /* matvec work items per pass (t=V2x, y+=Dx+U2t, t=U2^Tx, y+=D^Tx+V2^Tt) */
+  int mv_segments;             /* matvec segments (block pieces) */
+  int mv_ranges[4];            /* staged input ranges per pass */
 } bem_operator_info_t;
 
 /* Fill *p with the reference defaults (intorder 3, leafsize 40, eta 2, eps 1e-6, aca). */
@@ -136,6 +139,14 @@ int bem_operator_mult_host(bem_operator_t op, int trans, const double* alpha, co
 int bem_operator_to_dense(bem_operator_t op, void* out);
 
 int bem_operator_destroy(bem_operator_t op);
+
+/* Arithmetic of the matvec for FP32-stored operators (no counterpart in the reference, which is
+ * FP64 throughout): compensated = 1 (default) forms every product and sum error-free (x split
+ * into FP32 hi+lo, TwoProd/TwoSum), so the only rounding is that of the stored entries;
+ * compensated = 0 uses plain FP32 FMAs (about 1e-7 relative rounding, faster).  FP64-stored
+ * operators ignore it.  bem_gmres uses the plain form inside its Krylov iterations and the
+ * compensated form for its residuals (iterative refinement). */
+int bem_operator_set_accuracy(bem_operator_t op, int compensated);
 
 /* Diagnostics (no counterpart in the reference, whose Timer/RegionTimer instrumentation at
  * src/hmat.cpp:650 plays this role): when enabled, every bem_operator_mult records CUDA

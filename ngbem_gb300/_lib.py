@@ -40,7 +40,8 @@ class OperatorInfo(C.Structure):
                 ("max_rank", C.c_int), ("sum_rank", C.c_longlong), ("bytes_dense", C.c_longlong),
                 ("bytes_lowrank", C.c_longlong), ("bytes_lowrank_u", C.c_longlong), ("n_singular_pairs", C.c_int),
                 ("n_regular_pairs", C.c_longlong), ("ms_setup", C.c_double), ("ms_aca", C.c_double),
-                ("ms_nearfield", C.c_double), ("ms_projection", C.c_double), ("ms_total", C.c_double)]
+                ("ms_nearfield", C.c_double), ("ms_projection", C.c_double), ("ms_total", C.c_double),
+                ("mv_items", C.c_int * 4), ("mv_segments", C.c_int), ("mv_ranges", C.c_int * 4)]
 
 
 _vp, _dp, _ip, _lp = C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_int), C.POINTER(C.c_long)
@@ -66,6 +67,7 @@ SIGNATURES = {
     "bem_operator_to_dense": ([_vp, _vp], C.c_int),
     "bem_operator_destroy": ([_vp], C.c_int),
     "bem_operator_set_profiling": ([_vp, C.c_int], C.c_int),
+    "bem_operator_set_accuracy": ([_vp, C.c_int], C.c_int),
     "bem_operator_kernel_times": ([_vp, _dp, C.POINTER(C.c_longlong)], C.c_int),
     "bem_gmres": ([C.c_int, C.POINTER(_vp), _dp, _vp, _vp, C.c_int, C.c_int, C.c_double, _ip, _dp, _vp],
                   C.c_int),

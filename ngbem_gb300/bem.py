@@ -281,7 +281,8 @@ class _NativeMatrix(BaseMatrix):
         self.h = handle
         info = _lib.OperatorInfo()
         check(lib.bem_operator_info(self.h, C.byref(info)))
-        self.info = {k: getattr(info, k) for k, _ in _lib.OperatorInfo._fields_}
+        self.info = {k: (list(getattr(info, k)) if k in ("mv_items", "mv_ranges") else getattr(info, k))
+                     for k, _ in _lib.OperatorInfo._fields_}
         self.height, self.width = info.height, info.width
         self.is_complex = bool(info.is_complex)
 
@@ -338,6 +339,10 @@ class HMatrix(_NativeMatrix):
         arrs = [np.zeros(n, dtype=np.int32) for _ in range(5)]
         check(lib.bem_operator_blocks(self.h, *[a.ctypes.data_as(_lib._ip) for a in arrs]))
         return dict(zip(["rowcl", "colcl", "near", "rank", "fallback"], arrs))
+
+    def set_accuracy(self, compensated: bool = True):
+        """FP32-stored operators: error-free (True, default) or plain FP32 (False) matvec arithmetic."""
+        check(lib.bem_operator_set_accuracy(self.h, int(bool(compensated))))
 
     def set_profiling(self, enable: bool = True):
         check(lib.bem_operator_set_profiling(self.h, int(bool(enable))))

@@ -257,7 +257,7 @@ __global__ void __launch_bounds__(256) aca_project_kernel(ProjArgs a) {
 #pragma unroll
       for (int x = 0; x < NDI; ++x) {
         const int li = a.test.pinv[i4c_(dn, x)] - L.r0;
-        if (li >= 0 && li < L.m) atomic_add(&U2[(size_t)(off + kk) * L.m + li], acc[x] * fac);
+        if (li >= 0 && li < L.m) atomic_add(&U2[lr_u_index(L, li, off + kk)], acc[x] * fac);
       }
     }
     for (int idx = threadIdx.x; idx < d.nj * r; idx += blockDim.x) {
@@ -286,7 +286,7 @@ __global__ void __launch_bounds__(256) aca_project_kernel(ProjArgs a) {
 #pragma unroll
       for (int x = 0; x < NDJ; ++x) {
         const int lj = a.trial.pinv[i4c_(dn, x)] - L.c0;
-        if (lj >= 0 && lj < L.n) atomic_add(&V2[(size_t)(off + kk) * L.n + lj], acc[x]);
+        if (lj >= 0 && lj < L.n) atomic_add(&V2[lr_v_index(L, off + kk, lj)], acc[x]);
       }
     }
     off += r;

@@ -39,7 +39,7 @@ struct ElemRecP {
 
 // A dense (near-field or fallback) block of the H-matrix.
 struct DenseDesc {
-  long long off;      // offset of the m x n row-major block in the dense pool (elements)
+  long long off;      // offset of the m x n column-major block in the dense pool (elements, 16-byte aligned)
   int r0, m;          // rows [r0, r0+m) in the test cluster permutation
   int c0, n;          // cols [c0, c0+n) in the trial cluster permutation
   int pi0, ni;        // test patch: patch_elems[pi0 .. pi0+ni)
@@ -66,19 +66,62 @@ struct FarDesc {
   int pad;
 };
 
-// Low-rank factors after projection: U2 (m x R, column-major) and V2 (R x n, row-major),
-// addressed by absolute device pointers (factor pools may be allocated per ACA batch).
+// Low-rank factors after projection, addressed by absolute device pointers (factor pools may
+// be allocated per ACA batch).  Chunked layouts so that every chunk is one contiguous,
+// 16-byte aligned copy:
+//   U2 (m x R): row chunks of cu rows;   U2(i, r) at u + (i/cu)*cu*R + r*cu + i%cu
+//   V2 (R x n): column chunks of cv cols; V2(r, j) at v + (j/cv)*cv*R + (j%cv)*R + r
 struct LRDesc {
   unsigned long long u, v;
   int r0, m, c0, n;
   int R;
   int toff;              // offset of the R-vector of V2*x in the temporary pool
+  int cu, cv;
 };
+__host__ __device__ inline long long lr_u_index(const LRDesc& L, int i, int r) {
+  return (long long)(i / L.cu) * L.cu * L.R + (long long)r * L.cu + (i % L.cu);
+}
+__host__ __device__ inline long long lr_v_index(const LRDesc& L, int r, int j) {
+  return (long long)(j / L.cv) * L.cv * L.R + (long long)(j % L.cv) * L.R + r;
+}
 
-// matvec descriptors (absolute device pointers)
+// matvec descriptors (absolute device pointers); dense blocks are column-major
 struct MVDense {
   unsigned long long ptr;
   int r0, m, c0, n;
+};
+
+// A segment of a matvec work item: a (part of a) block whose payload sits at byte offset
+// soff of the item.  kind 0: dense columns [k0, k0+cnt); 1: U2 row chunk [k0, k0+cnt);
+// 2: V2 column chunk [k0, k0+cnt).
+struct MVSeg {
+  int kind, blk, k0, cnt, soff, pad;
+};
+// A work item: one contiguous copy of `bytes` bytes from src (bytes == 0: read in place),
+// its pieces [seg0, seg0+nseg) and the input ranges [rng0, rng0+nrng) copied next to it
+// (inbytes in total).
+struct MVTItem {
+  unsigned long long src;
+  int bytes, seg0, nseg, rng0, nrng, inbytes;
+  int r[8];  // the first two input ranges inline (src, elem, bytes, dst each); others in the range list
+  int pad;
+};
+
+// A piece of an item as one pass applies it: out[out_off + o] += sum_k A[o*so + k*sk] *
+// in[in_off + k] for o < O, k < Kc, with A at byte soff of the item payload.  flags bit 0:
+// the input is the R-vector pool t (else the permuted x); bit 1: the output is t (else y).
+// in_soff: byte offset of in[in_off] in the item's staged input area.
+struct MVPiece {
+  int soff, so, sk, O, Kc, in_off, out_off, flags, in_soff;
+  int ow;      // lanes per group: min(O, 32)
+  int groups;  // 32 / ow lane groups splitting k
+  float inv_ow;  // 1/ow (exact lane -> group mapping for lane < 32)
+};
+
+// An input range staged with an item: `bytes` bytes from element `elem` (16-byte aligned
+// start) of x (src 0) or t (src 1), to byte `dst` of the input area.
+struct MVRange {
+  int src, elem, bytes, dst;
 };
 typedef LRDesc MVLowRank;
 

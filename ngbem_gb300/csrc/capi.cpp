@@ -254,6 +254,15 @@ int bem_operator_to_dense(bem_operator_t op, void* out) {
   });
 }
 
+int bem_operator_set_accuracy(bem_operator_t op, int compensated) {
+  return guarded([&] {
+    REQUIRE(op, "null argument");
+    auto* h = dynamic_cast<HOperator*>(op->op.get());
+    if (!h) throw Error(BEM_ERR_STATE, "not an H-matrix operator");
+    h->mv_compensated = compensated != 0;
+  });
+}
+
 int bem_operator_set_profiling(bem_operator_t op, int enable) {
   return guarded([&] {
     REQUIRE(op, "null argument");

@@ -158,11 +158,13 @@ struct HOperator : OperatorBase {
   // device data
   DevBuf d_perm_trial, d_perm_test, d_pinv_trial, d_pinv_test;
   std::vector<std::unique_ptr<DevBuf>> pools;  // dense and factor pools
-  DevBuf d_mvdense, d_mvlr;
-  DevBuf d_items_s1, d_items_ap, d_items_s1t, d_items_apt;
-  int n_items_s1 = 0, n_items_ap = 0, n_items_s1t = 0, n_items_apt = 0;
+  DevBuf d_mvdense, d_mvlr, d_err, d_sched;
+  DevBuf d_items[4], d_pieces[4], d_ranges[4];  // per pass: 0 t=V2 x, 1 y+=Dx+U2 t, 2 t=U2^T x, 3 y+=D^T x+V2^T t
+  int n_items[4] = {0, 0, 0, 0};
+  int mv_grid = 152;
+  int mv_compensated = 1;  // fp32 storage: error-free products/sums (1) or plain FP32 (0)
   int t_len = 0;
-  DevBuf d_t, d_xp, d_yp;
+  DevBuf d_t, d_tx, d_xp, d_yp;
   int ws_nrhs = 0;
   std::vector<MVDense> mvdense;
   std::vector<MVLowRank> mvlr;
@@ -177,6 +179,8 @@ struct HOperator : OperatorBase {
   ~HOperator() override;
 
   void assemble();
+  void build_mv_items();
+  int device_status();   // matvec pipeline error flags (0 = ok)
   void mult(int trans, const double* alpha, const void* x, const double* beta, void* y, int nrhs,
             cudaStream_t s) override;
   void to_dense(void* out);

@@ -91,28 +91,35 @@ int kernel_ncomp(int kid);
 bool kernel_complex(int kid);
 
 // ---- matvec -----------------------------------------------------------------------------
-struct MVItem {
-  int kind;    // 0 dense, 1 low rank
-  int idx;     // block index in its list
-  int start;   // first row (or column for the transposed/stage-1 passes)
-  int count;   // rows/cols in this item
-};
-
-struct MVArgs {
-  const MVDense* dense;
-  const MVLowRank* lr;
-  void* t;                 // R-vectors (storage precision), zeroed before stage 1
-  const void* xp;          // permuted input (storage precision), layout [k][nrhs]
-  void* yp;                // permuted output accumulator (fp64 or complex128), layout [k][nrhs]
-  const MVItem* items;
+// Item-based matvec pass (see matvec.cu).  pass 0: t = V2 x, 1: y += D x + U2 t,
+// 2: t = U2^T x, 3: y += D^T x + V2^T t.  xp holds the permuted input in the pass's
+// input form (FP32 hi+lo pairs for fp32 storage), t and yp are FP64 accumulators.
+struct MVArgs2 {
+  const MVTItem* items;   // seg0/nseg index `pieces`, rng0/nrng index `ranges`
   int nitems;
+  const MVPiece* pieces;
+  const MVRange* ranges;
+  const void* xp;
+  void* t;
+  const void* tx;    // t converted to the input form (fp32 hi+lo), read by passes 1 and 3
+  void* yp;
+  int pass;
   int nrhs;
+  int compensated;   // fp32 storage: 1 error-free products and sums, 0 plain FP32 FMA
+  int in_esz;        // bytes of one staged input value (x or t entry: 8 real, 16 complex)
+  int* err;
+  int* sched;        // two zeroed counters (items claimed, CTAs finished); left zero after a pass
 };
-
 // prec 0: fp64 storage, 1: fp32 storage.  cplx: complex operator.
-void launch_mv_stage1(int prec, bool cplx, bool trans, const MVArgs& a, cudaStream_t s);
-void launch_mv_apply(int prec, bool cplx, bool trans, const MVArgs& a, cudaStream_t s);
-// xp[k*nrhs + r] = (storage) x[r*ld + perm[k]]
+void launch_mv_pass(int prec, bool cplx, const MVArgs2& a, int grid, cudaStream_t s);
+int mv_stage_bytes();
+// tx = t in the input form (no-op for fp64 storage, where tx aliases t)
+void launch_t_to_x(int prec, bool cplx, const void* t, void* tx, long long n, cudaStream_t s);
+int mv_max_pieces();   // pieces per work item (descriptors staged with the payload)
+int mv_in_bytes();     // staged input bytes per work item
+// bytes of one permuted input value (X type) for a storage precision
+inline int mv_x_bytes(int prec, bool cplx) { return (prec == 0 ? 8 : 8) * (cplx ? 2 : 1); }
+// xp[k*nrhs + r] = (input form) x[r*ld + perm[k]]
 void launch_permute_in(int prec, bool cplx, const int* perm, int n, int nrhs, int ld,
                        const void* x, void* xp, cudaStream_t s);
 // y[r*ld + perm[k]] = alpha * yp[k*nrhs + r] + beta * y[...]   (fp64 / complex128)

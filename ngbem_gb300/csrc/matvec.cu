@@ -8,6 +8,8 @@
 // accumulating into an FP64 (complex128) permuted vector with atomics; a final kernel
 // un-permutes and applies alpha/beta.  Storage precision S is fp64 or fp32; products are
 // formed in S and block partial sums are added in FP64.
+#include <algorithm>
+
 #include "bem_device.cuh"
 #include "kernels.h"
 
@@ -25,18 +27,7 @@ __device__ __forceinline__ cpx<double> to_acc(cpx<float> v) { return {(double)v.
 __device__ __forceinline__ cpx<double> to_acc(cpx<double> v) { return v; }
 
 // ---------------------------------------------------------------------------------------
-template <class VS>
-__global__ void permute_in_kernel(const int* perm, int n, int nrhs, int ld, const void* xv, VS* xp) {
-  using VD = typename acc_of<VS>::type;
-  const VD* x = (const VD*)xv;
-  const long long total = (long long)n * nrhs;
-  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total; t += (long long)gridDim.x * blockDim.x) {
-    const int k = (int)(t / nrhs), r = (int)(t - (long long)k * nrhs);
-    VS v;
-    cvt(v, x[(size_t)r * ld + perm[k]]);
-    xp[t] = v;
-  }
-}
+
 
 template <class VD>
 __global__ void permute_out_kernel(const int* perm, int n, int nrhs, int ld, VD alpha, VD beta, int use_beta,
@@ -54,136 +45,541 @@ __global__ void permute_out_kernel(const int* perm, int n, int nrhs, int ld, VD 
 __device__ __forceinline__ double scal_mul(double a, double b) { return a * b; }
 
 // ---------------------------------------------------------------------------------------
-// stage 1: t = V2 x (non-transposed) over column chunks; transposed: t = U2^T x over row chunks
-template <class VS>
-__global__ void __launch_bounds__(256) mv_stage1_kernel(MVArgs a, int trans) {
-  const MVItem it = a.items[blockIdx.x];
-  const LRDesc L = a.lr[it.idx];
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  const VS* xp = (const VS*)a.xp;
-  VS* t = (VS*)a.t;
-  const int nrhs = a.nrhs;
-  if (!trans) {
-    const VS* V2 = (const VS*)L.v;
-    for (int r = w; r < L.R; r += nw) {
-      const VS* row = V2 + (size_t)r * L.n;
-      if (nrhs == 1) {
-        VS s = vzero<VS>();
-        for (int j = it.start + lane; j < it.start + it.count; j += 32) s += row[j] * xp[L.c0 + j];
-        s = warp_sum(s);
-        if (lane == 0) atomic_add(&t[L.toff + r], s);
-      } else {
-        for (int g = 0; g < nrhs; g += 32) {
-          const int rh = g + lane;
-          if (rh >= nrhs) continue;
-          VS s = vzero<VS>();
-          for (int j = it.start; j < it.start + it.count; ++j) s += row[j] * xp[(size_t)(L.c0 + j) * nrhs + rh];
-          atomic_add(&t[(size_t)(L.toff + r) * nrhs + rh], s);
-        }
-      }
-    }
-  } else {
-    const VS* U2 = (const VS*)L.u;
-    for (int r = w; r < L.R; r += nw) {
-      const VS* col = U2 + (size_t)r * L.m;
-      if (nrhs == 1) {
-        VS s = vzero<VS>();
-        for (int i = it.start + lane; i < it.start + it.count; i += 32) s += col[i] * xp[L.r0 + i];
-        s = warp_sum(s);
-        if (lane == 0) atomic_add(&t[L.toff + r], s);
-      } else {
-        for (int g = 0; g < nrhs; g += 32) {
-          const int rh = g + lane;
-          if (rh >= nrhs) continue;
-          VS s = vzero<VS>();
-          for (int i = it.start; i < it.start + it.count; ++i) s += col[i] * xp[(size_t)(L.r0 + i) * nrhs + rh];
-          atomic_add(&t[(size_t)(L.toff + r) * nrhs + rh], s);
-        }
-      }
-    }
-  }
-}
-
+// Item-based passes.  The H-matrix payload (dense blocks column-major, U2 row chunks, V2
+// column chunks) is grouped into work items of at most MV_STAGE bytes; a pass streams its
+// items through shared memory with cp.async.bulk (TMA bulk copies completing on mbarriers,
+// MV_NSTAGE-deep pipeline, persistent grid) and each warp applies the segments of an item.
+// Pass 0: t = V2 x; 1: y += D x + U2 t; 2: t = U2^T x; 3: y += D^T x + V2^T t.
+//
+// FP32 storage uses error-free transformations: x is split into hi + lo FP32 parts and every
+// product a*x_hi is formed exactly (a*x_hi = p + e with an FMA) and summed with TwoSum, so the
+// only rounding of the mixed matvec is the FP32 rounding of the stored entries: the operator
+// it applies is linear and consistent to ~1e-13, which GMRES needs to reach 1e-8.
 // ---------------------------------------------------------------------------------------
-// apply: y += D x (dense) and y += U2 t (low rank), row chunks; transposed over column chunks
-template <class VS>
-__global__ void __launch_bounds__(256) mv_apply_kernel(MVArgs a, int trans) {
-  using VD = typename acc_of<VS>::type;
-  const MVItem it = a.items[blockIdx.x];
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  const VS* xp = (const VS*)a.xp;
-  const VS* t = (const VS*)a.t;
-  VD* yp = (VD*)a.yp;
-  const int nrhs = a.nrhs;
-  if (it.kind == 0) {
-    const MVDense D = a.dense[it.idx];
-    const VS* M = (const VS*)D.ptr;
-    if (!trans) {
-      for (int i = it.start + w; i < it.start + it.count; i += nw) {
-        const VS* row = M + (size_t)i * D.n;
-        if (nrhs == 1) {
-          VS s = vzero<VS>();
-          for (int j = lane; j < D.n; j += 32) s += row[j] * xp[D.c0 + j];
-          s = warp_sum(s);
-          if (lane == 0) atomic_add(&yp[D.r0 + i], to_acc(s));
-        } else {
-          for (int g = 0; g < nrhs; g += 32) {
-            const int rh = g + lane;
-            if (rh >= nrhs) continue;
-            VS s = vzero<VS>();
-            for (int j = 0; j < D.n; ++j) s += row[j] * xp[(size_t)(D.c0 + j) * nrhs + rh];
-            atomic_add(&yp[(size_t)(D.r0 + i) * nrhs + rh], to_acc(s));
-          }
+template <class VS> struct MT;
+template <> struct MT<float> { using X = float2; using D = double; };
+template <> struct MT<double> { using X = double; using D = double; };
+template <> struct MT<cpx<float>> { using X = float4; using D = cpx<double>; };
+template <> struct MT<cpx<double>> { using X = cpx<double>; using D = cpx<double>; };
+
+__device__ __forceinline__ float2 split_x(double v) {
+  float h = __double2float_rn(v);
+  return make_float2(h, __double2float_rn(v - (double)h));
+}
+__device__ __forceinline__ float4 split_x(cpx<double> v) {
+  float2 a = split_x(v.x), b = split_x(v.y);
+  return make_float4(a.x, a.y, b.x, b.y);
+}
+__device__ __forceinline__ double split_x_d(double v) { return v; }
+
+template <class VS> __device__ __forceinline__ typename MT<VS>::X to_x(typename MT<VS>::D v);
+template <> __device__ __forceinline__ float2 to_x<float>(double v) { return split_x(v); }
+template <> __device__ __forceinline__ double to_x<double>(double v) { return v; }
+template <> __device__ __forceinline__ float4 to_x<cpx<float>>(cpx<double> v) { return split_x(v); }
+template <> __device__ __forceinline__ cpx<double> to_x<cpx<double>>(cpx<double> v) { return v; }
+
+// compensated FP32 accumulator
+struct CAcc { float h, l; };
+__device__ __forceinline__ void cadd(CAcc& s, float a, float xh, float xl) {
+  const float p = __fmul_rn(a, xh);
+  const float e = fmaf(a, xh, -p);
+  const float t = __fadd_rn(s.h, p);
+  const float bb = __fsub_rn(t, s.h);
+  const float err = __fadd_rn(__fsub_rn(s.h, __fsub_rn(t, bb)), __fsub_rn(p, bb));
+  s.h = t;
+  s.l = __fadd_rn(s.l, __fadd_rn(err, fmaf(a, xl, e)));
+}
+__device__ __forceinline__ void cmerge(CAcc& s, float oh, float ol) {
+  const float t = __fadd_rn(s.h, oh);
+  const float bb = __fsub_rn(t, s.h);
+  const float err = __fadd_rn(__fsub_rn(s.h, __fsub_rn(t, bb)), __fsub_rn(oh, bb));
+  s.h = t;
+  s.l = __fadd_rn(s.l, __fadd_rn(ol, err));
+}
+
+template <class VS> struct Acc;
+template <> struct Acc<float> {
+  CAcc a{0.f, 0.f};
+  __device__ __forceinline__ void add(float m, float2 x) { cadd(a, m, x.x, x.y); }
+  __device__ __forceinline__ Acc from_lane(int src) const {
+    Acc r;
+    r.a.h = __shfl_sync(0xffffffffu, a.h, src);
+    r.a.l = __shfl_sync(0xffffffffu, a.l, src);
+    return r;
+  }
+  __device__ __forceinline__ void merge(const Acc& o) { cmerge(a, o.a.h, o.a.l); }
+  __device__ __forceinline__ void merge_xor(int mask) {
+    float oh = __shfl_xor_sync(0xffffffffu, a.h, mask), ol = __shfl_xor_sync(0xffffffffu, a.l, mask);
+    cmerge(a, oh, ol);
+  }
+  __device__ __forceinline__ double val() const { return (double)a.h + (double)a.l; }
+};
+template <> struct Acc<cpx<float>> {
+  CAcc re{0.f, 0.f}, im{0.f, 0.f};
+  __device__ __forceinline__ Acc from_lane(int src) const {
+    Acc r;
+    r.re.h = __shfl_sync(0xffffffffu, re.h, src);
+    r.re.l = __shfl_sync(0xffffffffu, re.l, src);
+    r.im.h = __shfl_sync(0xffffffffu, im.h, src);
+    r.im.l = __shfl_sync(0xffffffffu, im.l, src);
+    return r;
+  }
+  __device__ __forceinline__ void merge(const Acc& o) { cmerge(re, o.re.h, o.re.l); cmerge(im, o.im.h, o.im.l); }
+  __device__ __forceinline__ void add(cpx<float> m, float4 x) {
+    cadd(re, m.x, x.x, x.y);
+    cadd(re, -m.y, x.z, x.w);
+    cadd(im, m.x, x.z, x.w);
+    cadd(im, m.y, x.x, x.y);
+  }
+  __device__ __forceinline__ void merge_xor(int mask) {
+    float a = __shfl_xor_sync(0xffffffffu, re.h, mask), b = __shfl_xor_sync(0xffffffffu, re.l, mask);
+    float c = __shfl_xor_sync(0xffffffffu, im.h, mask), d = __shfl_xor_sync(0xffffffffu, im.l, mask);
+    cmerge(re, a, b);
+    cmerge(im, c, d);
+  }
+  __device__ __forceinline__ cpx<double> val() const { return {(double)re.h + (double)re.l, (double)im.h + (double)im.l}; }
+};
+// plain FP32 accumulation (x_hi only): one FMA per product
+struct AccF {
+  float a = 0.f;
+  __device__ __forceinline__ void add(float m, float2 x) { a = fmaf(m, x.x, a); }
+  __device__ __forceinline__ AccF from_lane(int src) const { AccF r; r.a = __shfl_sync(0xffffffffu, a, src); return r; }
+  __device__ __forceinline__ void merge(const AccF& o) { a += o.a; }
+  __device__ __forceinline__ double val() const { return (double)a; }
+};
+struct AccCF {
+  float re = 0.f, im = 0.f;
+  __device__ __forceinline__ void add(cpx<float> m, float4 x) {
+    re = fmaf(m.x, x.x, re);
+    re = fmaf(-m.y, x.z, re);
+    im = fmaf(m.x, x.z, im);
+    im = fmaf(m.y, x.x, im);
+  }
+  __device__ __forceinline__ AccCF from_lane(int src) const {
+    AccCF r;
+    r.re = __shfl_sync(0xffffffffu, re, src);
+    r.im = __shfl_sync(0xffffffffu, im, src);
+    return r;
+  }
+  __device__ __forceinline__ void merge(const AccCF& o) { re += o.re; im += o.im; }
+  __device__ __forceinline__ cpx<double> val() const { return {(double)re, (double)im}; }
+};
+template <class VS, bool COMP> struct AccSel { using type = Acc<VS>; };
+template <> struct AccSel<float, false> { using type = AccF; };
+template <> struct AccSel<cpx<float>, false> { using type = AccCF; };
+
+template <> struct Acc<double> {
+  double a = 0.0;
+  __device__ __forceinline__ Acc from_lane(int src) const { Acc r; r.a = __shfl_sync(0xffffffffu, a, src); return r; }
+  __device__ __forceinline__ void merge(const Acc& o) { a += o.a; }
+  __device__ __forceinline__ void add(double m, double x) { a = fma(m, x, a); }
+  __device__ __forceinline__ void merge_xor(int mask) { a += __shfl_xor_sync(0xffffffffu, a, mask); }
+  __device__ __forceinline__ double val() const { return a; }
+};
+template <> struct Acc<cpx<double>> {
+  cpx<double> a{0.0, 0.0};
+  __device__ __forceinline__ Acc from_lane(int src) const {
+    Acc r;
+    r.a.x = __shfl_sync(0xffffffffu, a.x, src);
+    r.a.y = __shfl_sync(0xffffffffu, a.y, src);
+    return r;
+  }
+  __device__ __forceinline__ void merge(const Acc& o) { a += o.a; }
+  __device__ __forceinline__ void add(cpx<double> m, cpx<double> x) { a += m * x; }
+  __device__ __forceinline__ void merge_xor(int mask) { a += shfl_xor(a, mask); }
+  __device__ __forceinline__ cpx<double> val() const { return a; }
+};
+
+#define MV_STAGE 32768
+#define MV_NSTAGE 4
+#define MV_THREADS 1024
+#define MV_CONSUMERS (MV_THREADS / 32 - 1)
+#define MV_INBUF 128
+#define MV_MAXPC 128
+#define MV_INAREA 16384
+#define MV_HDR 256
+
+// what the producer tells the consumers about the item in a stage (nseg < 0: no more items)
+struct MVStageHdr {
+  int nseg, bytes, inbytes, pad;
+  unsigned long long src;
+  unsigned long long pad2;
+};
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void mbar_init(uint64_t* bar, int count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+__device__ __forceinline__ void bulk_load(void* dst, const void* src, int bytes, uint64_t* bar) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes) : "memory");
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(smem_u32(dst)),
+      "l"(src), "r"(bytes), "r"(smem_u32(bar))
+      : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// bounded wait: false after ~1<<22 polls (the phase never completed)
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+  for (int i = 0; i < (1 << 22); ++i)
+    if (mbar_try_wait(bar, parity)) return true;
+  return false;
+}
+// bounded wait with a short sleep between polls, for the many consumer warps (leaves the
+// issue slots to the producer warp and to warps with work)
+__device__ __forceinline__ bool mbar_wait_sleep(uint64_t* bar, uint32_t parity) {
+  for (int i = 0; i < (1 << 20); ++i) {
+    if (mbar_try_wait(bar, parity)) return true;
+    __nanosleep(64);
+  }
+  return false;
+}
+
+// out[o] += sum_k A[o*so + k*sk] * in[k] for o < O, one warp.  When O < 32 the lanes form
+// G = 32/O groups (lane = o + g*O) that split k and are combined by shuffles, so G*O lanes
+// work; with so = 1 and sk = O consecutive lanes read consecutive shared-memory words.
+template <class VS, bool COMP, class InF, class OutF>
+__device__ __forceinline__ void warp_gemv(const VS* A, int so, int sk, int O, int Kc, InF in, OutF out,
+                                          typename MT<VS>::X* buf, int lane, bool first_staged = false) {
+  using AccT = typename AccSel<VS, COMP>::type;
+  using X = typename MT<VS>::X;
+  const int Ow = O < 32 ? O : 32;
+  const int G = 32 / Ow;
+  const int g = lane / Ow, ol = lane - g * Ow;
+  const bool active = g < G;
+  for (int kc0 = 0; kc0 < Kc; kc0 += MV_INBUF) {
+    const int kn = min(MV_INBUF, Kc - kc0);
+    if (!(first_staged && kc0 == 0)) {
+      __syncwarp();
+      for (int k = lane; k < kn; k += 32) buf[k] = in(kc0 + k);
+    }
+    __syncwarp();
+    for (int o0 = 0; o0 < O; o0 += Ow) {
+      const int o = o0 + ol;
+      AccT acc;
+      if (active && o < O) {
+        const VS* Ap = A + o * so + (kc0 + g) * sk;
+        const X* bp = buf + g;
+        const int astep = G * sk;
+        int k = g;
+#pragma unroll 4
+        for (; k < kn; k += G) {
+          acc.add(*Ap, *bp);
+          Ap += astep;
+          bp += G;
         }
       }
-    } else {
-      // columns [start, start+count) of the block; thread per (column, rhs)
-      for (int jj = threadIdx.x; jj < it.count * nrhs; jj += blockDim.x) {
-        const int j = it.start + jj / nrhs, rh = jj - (jj / nrhs) * nrhs;
-        VS s = vzero<VS>();
-        for (int i = 0; i < D.m; ++i) s += M[(size_t)i * D.n + j] * xp[(size_t)(D.r0 + i) * nrhs + rh];
-        atomic_add(&yp[(size_t)(D.c0 + j) * nrhs + rh], to_acc(s));
+      // combine the G groups into group 0 (source lanes o + j*Ow)
+      for (int j = 1; j < G; ++j) {
+        AccT other = acc.from_lane(ol + j * Ow);
+        if (g == 0) acc.merge(other);
       }
-    }
-  } else {
-    const LRDesc L = a.lr[it.idx];
-    if (!trans) {
-      const VS* U2 = (const VS*)L.u;
-      for (int ii = threadIdx.x; ii < it.count * nrhs; ii += blockDim.x) {
-        const int i = it.start + ii / nrhs, rh = ii - (ii / nrhs) * nrhs;
-        VS s = vzero<VS>();
-        for (int r = 0; r < L.R; ++r) s += U2[(size_t)r * L.m + i] * t[(size_t)(L.toff + r) * nrhs + rh];
-        atomic_add(&yp[(size_t)(L.r0 + i) * nrhs + rh], to_acc(s));
-      }
-    } else {
-      const VS* V2 = (const VS*)L.v;
-      for (int jj = threadIdx.x; jj < it.count * nrhs; jj += blockDim.x) {
-        const int j = it.start + jj / nrhs, rh = jj - (jj / nrhs) * nrhs;
-        VS s = vzero<VS>();
-        for (int r = 0; r < L.R; ++r) s += V2[(size_t)r * L.n + j] * t[(size_t)(L.toff + r) * nrhs + rh];
-        atomic_add(&yp[(size_t)(L.c0 + j) * nrhs + rh], to_acc(s));
-      }
+      if (g == 0 && o < O) out(o, acc.val());
     }
   }
-  (void)lane;
+}
+
+// out[o] += sum_k A[o*so + k*sk] * in[k] for o < O, one warp, inputs already in shared
+// memory.  When O < 32 the lanes form G = 32/O groups (lane = o + g*O) that split k and are
+// combined by shuffles; with so = 1 and sk = O consecutive lanes read consecutive words.
+template <class VS, bool COMP, class InF, class OutF>
+__device__ __forceinline__ void warp_gemv_s(const VS* A, int so, int sk, int O, int Kc, int Ow, int G, float inv_ow,
+                                            InF in, OutF out, int lane) {
+  using AccT = typename AccSel<VS, COMP>::type;
+  const int g = __float2int_rz(((float)lane + 0.5f) * inv_ow);
+  const int ol = lane - g * Ow;
+  const bool active = g < G;
+  for (int o0 = 0; o0 < O; o0 += Ow) {
+    const int o = o0 + ol;
+    AccT acc;
+    if (active && o < O) {
+      const VS* Ap = A + o * so + g * sk;
+      const int astep = G * sk;
+#pragma unroll 4
+      for (int k = g; k < Kc; k += G) {
+        acc.add(*Ap, in(k));
+        Ap += astep;
+      }
+    }
+    for (int j = 1; j < G; ++j) {
+      AccT other = acc.from_lane(ol + j * Ow);
+      if (g == 0) acc.merge(other);
+    }
+    if (g == 0 && o < O) out(o, acc.val());
+  }
+}
+
+template <class VS, bool COMP>
+__device__ __forceinline__ void run_piece_s(const MVArgs2& a, const MVPiece& pc, const VS* A, const typename MT<VS>::X* xin,
+                                            int lane) {
+  using D = typename MT<VS>::D;
+  D* out = ((pc.flags & 2) ? (D*)a.t : (D*)a.yp) + pc.out_off;
+  warp_gemv_s<VS, COMP>(A, pc.so, pc.sk, pc.O, pc.Kc, pc.ow, pc.groups, pc.inv_ow, [&](int k) { return xin[k]; },
+                        [&](int o, D v) { atomic_add(&out[o], v); }, lane);
+}
+
+// Persistent single right-hand-side pass, warp specialised.  Warp 0 streams items into
+// MV_NSTAGE shared-memory stages with bulk copies: the payload, the item's piece descriptors
+// and the input ranges its pieces read (slices of the permuted x or of t), all counted on the
+// stage's full barrier.  The consumer warps take the pieces of each item round-robin --
+// reading only shared memory -- and release the stage on its empty barrier.
+//
+// Items are handed out on demand: a CTA starts with items blockIdx.x and blockIdx.x + G, then
+// claims the others from the counter a.sched[0] (index 2G + claim), so SMs whose copies land
+// later than others' do fewer items instead of setting the kernel time.  Claims are made one
+// item ahead, so their latency overlaps the copies of the current item.  The last CTA to
+// finish resets both counters, which leaves them zero for the next launch on the stream.
+// After its last item the producer pushes a stop marker (nseg < 0) through the next stage.
+template <class VS, bool COMP>
+__global__ void __launch_bounds__(MV_THREADS, 1) mv_tma_kernel(MVArgs2 a) {
+  extern __shared__ __align__(128) unsigned char smem[];
+  uint64_t* full = (uint64_t*)smem;                               // MV_NSTAGE barriers
+  uint64_t* empty = full + MV_NSTAGE;                             // MV_NSTAGE barriers
+  MVStageHdr* hdr = (MVStageHdr*)(smem + 16 * MV_NSTAGE);         // per stage: what the item holds
+  unsigned char* stage = smem + MV_HDR;
+  MVPiece* dstage = (MVPiece*)(stage + MV_NSTAGE * MV_STAGE);    // per stage: MV_MAXPC descriptors
+  unsigned char* istage = (unsigned char*)(dstage + MV_NSTAGE * MV_MAXPC);  // per stage: MV_INAREA bytes
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int G = gridDim.x;
+  const int nit = a.nitems;
+  if (tid == 0) {
+    for (int s = 0; s < MV_NSTAGE; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], MV_CONSUMERS);
+    }
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  }
+  __syncthreads();
+  if (warp == 0) {
+    uint32_t ephase = 0;
+    int it = 0;
+    int ok = 1;
+    // kc/dc: the item to issue now; kn/dn: the next one (descriptor load in flight);
+    // tok: lane 0's claim of the item after that (atomic in flight)
+    int kc = blockIdx.x;
+    int kn = blockIdx.x + G < nit ? blockIdx.x + G : nit;
+    MVTItem dc = a.items[kc], dn{};
+    if (kn < nit) dn = a.items[kn];
+    int tok = 0;
+    if (lane == 0 && kn < nit) tok = atomicAdd(a.sched, 1);
+    while (kc < nit) {
+      const int s = it % MV_NSTAGE;
+      // the first use of a stage passes at once (parity of the phase before the first)
+      if (lane == 0) ok = mbar_wait(&empty[s], ((ephase >> s) & 1u) ^ 1u) ? 1 : 0;
+      ok = __shfl_sync(0xffffffffu, ok, 0);
+      if (!ok) break;
+      ephase ^= 1u << s;
+      const int dbytes = dc.nseg * (int)sizeof(MVPiece);
+      if (lane == 0) {
+        hdr[s].nseg = dc.nseg;
+        hdr[s].bytes = dc.bytes;
+        hdr[s].inbytes = dc.inbytes;
+        hdr[s].src = dc.src;
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        // one arrival carries the transaction bytes of all copies of the item
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(&full[s])),
+                     "r"(dc.bytes + dbytes + (dc.inbytes > 0 ? dc.inbytes : 0)) : "memory");
+        if (dc.bytes > 0)
+          asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                       ::"r"(smem_u32(stage + s * MV_STAGE)), "l"((const void*)dc.src), "r"(dc.bytes),
+                       "r"(smem_u32(&full[s])) : "memory");
+        if (dbytes > 0)
+          asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                       ::"r"(smem_u32(dstage + s * MV_MAXPC)), "l"((const void*)(a.pieces + dc.seg0)),
+                       "r"(dbytes), "r"(smem_u32(&full[s])) : "memory");
+      }
+      __syncwarp();
+      unsigned char* ia = istage + s * MV_INAREA;
+      for (int r = lane; r < dc.nrng; r += 32) {
+        MVRange rg;
+        if (r < 2) rg = r == 0 ? MVRange{dc.r[0], dc.r[1], dc.r[2], dc.r[3]} : MVRange{dc.r[4], dc.r[5], dc.r[6], dc.r[7]};
+        else rg = a.ranges[dc.rng0 + r];
+        const unsigned char* gsrc = (const unsigned char*)(rg.src ? a.tx : a.xp) + (size_t)rg.elem * a.in_esz;
+        asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                     ::"r"(smem_u32(ia + rg.dst)), "l"((const void*)gsrc), "r"(rg.bytes),
+                     "r"(smem_u32(&full[s])) : "memory");
+      }
+      ++it;
+      // advance: the claim made one item ago names the item after next
+      kc = kn;
+      dc = dn;
+      if (kn < nit) {
+        const int k = 2 * G + __shfl_sync(0xffffffffu, tok, 0);
+        kn = k < nit ? k : nit;
+        if (kn < nit) {
+          dn = a.items[kn];
+          if (lane == 0) tok = atomicAdd(a.sched, 1);
+        }
+      }
+    }
+    if (lane == 0) {
+      if (!ok) atomicOr(a.err, 2);
+      // every issued copy must land before the stop marker reuses a stage
+      uint32_t fphase = 0;
+      for (int j = 0; j < it; ++j) {
+        const int s = j % MV_NSTAGE;
+        if (j >= it - MV_NSTAGE) mbar_wait(&full[s], (fphase >> s) & 1u);
+        fphase ^= 1u << s;
+      }
+      const int s = it % MV_NSTAGE;
+      if (ok && mbar_wait(&empty[s], ((ephase >> s) & 1u) ^ 1u)) {
+        hdr[s].nseg = -1;
+        mbar_arrive(&full[s]);
+      } else {
+        atomicOr(a.err, 2);
+      }
+      // the claims of this CTA are done; the last CTA out resets the counters
+      __threadfence();
+      if (atomicAdd(a.sched + 1, 1) == G - 1) {
+        atomicExch(a.sched, 0);
+        atomicExch(a.sched + 1, 0);
+      }
+    }
+    return;
+  }
+  const int cw = warp - 1;
+  uint32_t fphase = 0;
+  int pbase = 0;  // pieces of this CTA's earlier items: warp cw takes pieces with (pbase + q) % C == cw
+  for (int it = 0;; ++it) {
+    const int s = it % MV_NSTAGE;
+    if (!mbar_wait_sleep(&full[s], (fphase >> s) & 1u)) {
+      if (lane == 0) atomicOr(a.err, 2);
+      break;
+    }
+    fphase ^= 1u << s;
+    const int nseg = hdr[s].nseg;
+    if (nseg < 0) break;
+    const bool sa = hdr[s].bytes > 0, si = hdr[s].inbytes >= 0;
+    int q0 = cw - pbase % MV_CONSUMERS;
+    if (q0 < 0) q0 += MV_CONSUMERS;
+    pbase += nseg;
+    const MVPiece* pcs = dstage + s * MV_MAXPC;
+    // separate paths so that staged operands are read with shared-memory loads
+    using X = typename MT<VS>::X;
+    const unsigned char* sbase = stage + s * MV_STAGE;
+    const unsigned char* ia = istage + s * MV_INAREA;
+    if (sa && si) {
+      for (int q = q0; q < nseg; q += MV_CONSUMERS) {
+        const MVPiece pc = pcs[q];
+        run_piece_s<VS, COMP>(a, pc, (const VS*)(sbase + pc.soff), (const X*)(ia + pc.in_soff), lane);
+      }
+    } else {
+      const unsigned char* gbase = (const unsigned char*)hdr[s].src;
+      for (int q = q0; q < nseg; q += MV_CONSUMERS) {
+        const MVPiece pc = pcs[q];
+        const X* gin = (const X*)((const unsigned char*)((pc.flags & 1) ? a.tx : a.xp) + (size_t)pc.in_off * a.in_esz);
+        if (sa) run_piece_s<VS, COMP>(a, pc, (const VS*)(sbase + pc.soff), gin, lane);
+        else if (si) run_piece_s<VS, COMP>(a, pc, (const VS*)(gbase + pc.soff), (const X*)(ia + pc.in_soff), lane);
+        else run_piece_s<VS, COMP>(a, pc, (const VS*)(gbase + pc.soff), gin, lane);
+      }
+    }
+    __syncwarp();
+    if (lane == 0) mbar_arrive(&empty[s]);
+  }
+}
+
+// generic pass for several right-hand sides (payload read in place): lane = rhs
+template <class VS, bool COMP>
+__global__ void __launch_bounds__(256) mv_multi_kernel(MVArgs2 a) {
+  using AccT = typename AccSel<VS, COMP>::type;
+  using X = typename MT<VS>::X;
+  using D = typename MT<VS>::D;
+  const MVTItem item = a.items[blockIdx.x];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarp = blockDim.x >> 5;
+  const X* xp = (const X*)a.xp;
+  D* t = (D*)a.t;
+  D* yp = (D*)a.yp;
+  const int nr = a.nrhs;
+  for (int q = warp; q < item.nseg; q += nwarp) {
+    const MVPiece pc = a.pieces[item.seg0 + q];
+    const VS* A = (const VS*)((const unsigned char*)item.src + pc.soff);
+    const bool in_t = pc.flags & 1, out_t = pc.flags & 2;
+    for (int o = 0; o < pc.O; ++o)
+      for (int g = 0; g < nr; g += 32) {
+        const int rh = g + lane;
+        if (rh >= nr) continue;
+        AccT acc;
+        for (int k = 0; k < pc.Kc; ++k) {
+          const size_t idx = (size_t)(pc.in_off + k) * nr + rh;
+          const X xv = in_t ? ((const X*)a.tx)[idx] : xp[idx];
+          acc.add(A[(long long)o * pc.so + (long long)k * pc.sk], xv);
+        }
+        D* dst = (out_t ? t : yp) + (size_t)(pc.out_off + o) * nr + rh;
+        atomic_add(dst, acc.val());
+      }
+  }
+}
+
+int mv_smem_bytes() {
+  static_assert(16 * MV_NSTAGE + (int)sizeof(MVStageHdr) * MV_NSTAGE <= MV_HDR, "matvec header area");
+  return MV_HDR + MV_NSTAGE * (MV_STAGE + MV_MAXPC * (int)sizeof(MVPiece) + MV_INAREA);
+}
+int mv_in_bytes() { return MV_INAREA; }
+int mv_max_pieces() { return MV_MAXPC; }
+
+template <class VS, bool COMP>
+static void pass_t(const MVArgs2& a, int grid, cudaStream_t s) {
+  if (a.nitems <= 0) return;
+  if (a.nrhs == 1) {
+    const int smem = mv_smem_bytes();
+    static bool attr = false;
+    if (!attr) {
+      cudaFuncSetAttribute(mv_tma_kernel<VS, COMP>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+      attr = true;
+    }
+    mv_tma_kernel<VS, COMP><<<std::min(grid, a.nitems), MV_THREADS, smem, s>>>(a);
+  } else {
+    mv_multi_kernel<VS, COMP><<<a.nitems, 256, 0, s>>>(a);
+  }
+}
+
+void launch_mv_pass(int prec, bool cplx, const MVArgs2& a, int grid, cudaStream_t s) {
+  if (prec == 0) {
+    if (cplx) pass_t<cpx<double>, true>(a, grid, s);
+    else pass_t<double, true>(a, grid, s);
+  } else if (a.compensated) {
+    if (cplx) pass_t<cpx<float>, true>(a, grid, s);
+    else pass_t<float, true>(a, grid, s);
+  } else {
+    if (cplx) pass_t<cpx<float>, false>(a, grid, s);
+    else pass_t<float, false>(a, grid, s);
+  }
+}
+
+int mv_stage_bytes() { return MV_STAGE; }
+
+template <class VS>
+__global__ void permute_in_kernel(const int* perm, int n, int nrhs, int ld, const void* xv, void* xpv) {
+  using D = typename MT<VS>::D;
+  using X = typename MT<VS>::X;
+  const D* x = (const D*)xv;
+  X* xp = (X*)xpv;
+  const long long total = (long long)n * nrhs;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total; t += (long long)gridDim.x * blockDim.x) {
+    const int k = (int)(t / nrhs), r = (int)(t - (long long)k * nrhs);
+    xp[t] = to_x<VS>(x[(size_t)r * ld + perm[k]]);
+  }
 }
 
 template <class VS>
-static void stage1_t(const MVArgs& a, bool trans, cudaStream_t s) {
-  if (a.nitems > 0) mv_stage1_kernel<VS><<<a.nitems, 256, 0, s>>>(a, trans ? 1 : 0);
-}
-template <class VS>
-static void apply_t(const MVArgs& a, bool trans, cudaStream_t s) {
-  if (a.nitems > 0) mv_apply_kernel<VS><<<a.nitems, 256, 0, s>>>(a, trans ? 1 : 0);
-}
-
-void launch_mv_stage1(int prec, bool cplx, bool trans, const MVArgs& a, cudaStream_t s) {
-  if (prec == 0) { if (cplx) stage1_t<cpx<double>>(a, trans, s); else stage1_t<double>(a, trans, s); }
-  else { if (cplx) stage1_t<cpx<float>>(a, trans, s); else stage1_t<float>(a, trans, s); }
-}
-void launch_mv_apply(int prec, bool cplx, bool trans, const MVArgs& a, cudaStream_t s) {
-  if (prec == 0) { if (cplx) apply_t<cpx<double>>(a, trans, s); else apply_t<double>(a, trans, s); }
-  else { if (cplx) apply_t<cpx<float>>(a, trans, s); else apply_t<float>(a, trans, s); }
+__global__ void t_to_x_kernel(const void* tv, void* txv, long long n) {
+  using D = typename MT<VS>::D;
+  using X = typename MT<VS>::X;
+  const D* t = (const D*)tv;
+  X* tx = (X*)txv;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    tx[i] = to_x<VS>(t[i]);
 }
 
 static int grid_for(long long total) {
@@ -197,11 +593,11 @@ void launch_permute_in(int prec, bool cplx, const int* perm, int n, int nrhs, in
                        cudaStream_t s) {
   int g = grid_for((long long)n * nrhs);
   if (prec == 0) {
-    if (cplx) permute_in_kernel<cpx<double>><<<g, 256, 0, s>>>(perm, n, nrhs, ld, x, (cpx<double>*)xp);
-    else permute_in_kernel<double><<<g, 256, 0, s>>>(perm, n, nrhs, ld, x, (double*)xp);
+    if (cplx) permute_in_kernel<cpx<double>><<<g, 256, 0, s>>>(perm, n, nrhs, ld, x, xp);
+    else permute_in_kernel<double><<<g, 256, 0, s>>>(perm, n, nrhs, ld, x, xp);
   } else {
-    if (cplx) permute_in_kernel<cpx<float>><<<g, 256, 0, s>>>(perm, n, nrhs, ld, x, (cpx<float>*)xp);
-    else permute_in_kernel<float><<<g, 256, 0, s>>>(perm, n, nrhs, ld, x, (float*)xp);
+    if (cplx) permute_in_kernel<cpx<float>><<<g, 256, 0, s>>>(perm, n, nrhs, ld, x, xp);
+    else permute_in_kernel<float><<<g, 256, 0, s>>>(perm, n, nrhs, ld, x, xp);
   }
 }
 
@@ -355,6 +751,13 @@ void launch_residual(bool cplx, int n, const void* b, void* r, cudaStream_t s) {
   int g = grid_for(n);
   if (cplx) residual_kernel<cpx<double>><<<g, 256, 0, s>>>(n, (const cpx<double>*)b, (cpx<double>*)r);
   else residual_kernel<double><<<g, 256, 0, s>>>(n, (const double*)b, (double*)r);
+}
+
+void launch_t_to_x(int prec, bool cplx, const void* t, void* tx, long long n, cudaStream_t s) {
+  if (n <= 0 || prec == 0) return;  // fp64 storage: t is already the input form
+  const int g = grid_for(n);
+  if (cplx) t_to_x_kernel<cpx<float>><<<g, 256, 0, s>>>(t, tx, n);
+  else t_to_x_kernel<float><<<g, 256, 0, s>>>(t, tx, n);
 }
 
 }  // namespace bem

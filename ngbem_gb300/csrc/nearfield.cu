@@ -162,7 +162,7 @@ __global__ void __launch_bounds__(128) nf_regular_kernel(NFArgs a) {
 #pragma unroll
     for (int c = 0; c < NDJ; ++c)
       if (rows[r] >= 0 && cols[c] >= 0) {
-        V* dst = pool + (size_t)rows[r] * d.n + cols[c];
+        V* dst = pool + (size_t)cols[c] * d.m + rows[r];  // column-major block
         if (a.atomic_scatter) atomic_add(dst, elmat[r][c]);
         else *dst = elmat[r][c];
       }
@@ -319,7 +319,7 @@ __global__ void __launch_bounds__(256) nf_singular_kernel(NFArgs a) {
           if (col < 0 || col >= d.n) continue;
           VS v;
           cvt(v, acc[r][c]);
-          VS* dst = pool + (size_t)row * d.n + col;
+          VS* dst = pool + (size_t)col * d.m + row;  // column-major block
           if (a.atomic_scatter) atomic_add(dst, v);
           else *dst = v;
         }

@@ -187,6 +187,7 @@ void HOperator::assemble() {
   EvGuard eg{evs, 6};
 
   // ---- near field (dense blocks) ----------------------------------------------------------
+  const long long align_el = (long long)std::max<size_t>(1, 16 / vsize);
   auto run_near = [&](NearPass& np, const std::vector<int>& ids, cudaStream_t s) {
     np.block_ids = ids;
     np.desc.clear();
@@ -207,7 +208,7 @@ void HOperator::assemble() {
       d.ni = ttest->patch_ptr[B.rowcl + 1] - d.pi0;
       d.pj0 = ttrial->patch_ptr[B.colcl];
       d.nj = ttrial->patch_ptr[B.colcl + 1] - d.pj0;
-      off += (long long)d.m * d.n;
+      off += ((long long)d.m * d.n + align_el - 1) / align_el * align_el;  // 16-byte aligned blocks
       const long long pairs = (long long)d.ni * d.nj;
       np.npairs += pairs;
       const int bi = (int)np.desc.size();
@@ -225,8 +226,8 @@ void HOperator::assemble() {
     np.ntiles = (int)tiles.size();
     np.sing_cap = (int)std::max<long long>(cap, 1);
     auto pool = std::make_unique<DevBuf>();
-    pool->alloc((size_t)off * vsize);
-    BEM_CUDA(cudaMemsetAsync(pool->p, 0, (size_t)off * vsize, s));
+    pool->alloc((size_t)(off + align_el) * vsize);
+    BEM_CUDA(cudaMemsetAsync(pool->p, 0, pool->bytes, s));
     np.d_desc.upload(np.desc, s);
     np.d_tiles.upload(tiles, s);
     np.d_sing.alloc((size_t)np.sing_cap * sizeof(SingItem));
@@ -276,6 +277,14 @@ void HOperator::assemble() {
   std::vector<LRDesc> lr_all;
   std::vector<int> lr_block;
   float ms_aca = 0.f, ms_proj = 0.f;
+  // rows (cols) per U2 (V2) chunk: a multiple of 4, one chunk at most one matvec stage
+  auto chunk_len = [&](int dim, int R) {
+    const int full = (dim + 3) / 4 * 4;
+    if (R <= 0) return 4;
+    const int maxc = (int)(mv_stage_bytes() / ((size_t)R * vsize)) / 4 * 4;
+    if (maxc < 4) return full;  // too wide for a stage: one chunk, read in place
+    return std::min(full, maxc);
+  };
   // plan the batches first so that the scratch is allocated once: cudaFree would
   // synchronise the device and serialise the near-field stream with the ACA stream
   std::vector<std::vector<FarDesc>> batches;
@@ -366,7 +375,7 @@ void HOperator::assemble() {
       const int b = far_ids[f0 + f];
       LRDesc& L = lr[f];
       L.r0 = fd[f].r0; L.m = fd[f].m; L.c0 = fd[f].c0; L.n = fd[f].n;
-      L.R = 0; L.toff = 0; L.u = 0; L.v = 0;
+      L.R = 0; L.toff = 0; L.u = 0; L.v = 0; L.cu = 4; L.cv = 4;
       if (status[f]) { overflow_ids.push_back(b); block_fallback[b] = 2; continue; }
       int R = 0;
       const int nt = (kid == K_LAPLACE_HS) ? 3 : ((kid == K_HELMHOLTZ_HS || kid == K_MAXWELL_SL) ? 4 : 1);
@@ -376,10 +385,12 @@ void HOperator::assemble() {
       }
       for (int c = 0; c < NC; ++c) pranks[(size_t)f * NC + c] = ranks[(size_t)f * NC + c];
       L.R = R;
+      L.cu = chunk_len(L.m, R);
+      L.cv = chunk_len(L.n, R);
       L.u = (unsigned long long)usz;  // offsets for now
       L.v = (unsigned long long)vsz;
-      usz += (long long)L.m * R;
-      vsz += (long long)R * L.n;
+      usz += (long long)((L.m + L.cu - 1) / L.cu) * L.cu * R;
+      vsz += (long long)((L.n + L.cv - 1) / L.cv) * L.cv * R;
     }
     auto upool = std::make_unique<DevBuf>(), vpool = std::make_unique<DevBuf>();
     upool->alloc((size_t)std::max<long long>(usz, 1) * vsize);
@@ -480,26 +491,7 @@ void HOperator::assemble() {
     info.bytes_lowrank += (long long)L.R * (L.m + L.n) * (long long)vsize;
     info.bytes_lowrank_u += (long long)L.R * L.m * (long long)vsize;
   }
-  std::vector<MVItem> s1, ap, s1t, apt;
-  for (int f = 0; f < (int)mvlr.size(); ++f) {
-    const LRDesc& L = mvlr[f];
-    if (L.R == 0) continue;
-    for (int j = 0; j < L.n; j += 256) s1.push_back({1, f, j, std::min(256, L.n - j)});
-    for (int i = 0; i < L.m; i += 256) ap.push_back({1, f, i, std::min(256, L.m - i)});
-    for (int i = 0; i < L.m; i += 256) s1t.push_back({1, f, i, std::min(256, L.m - i)});
-    for (int j = 0; j < L.n; j += 256) apt.push_back({1, f, j, std::min(256, L.n - j)});
-  }
-  for (int k = 0; k < (int)mvdense.size(); ++k) {
-    const MVDense& D = mvdense[k];
-    for (int i = 0; i < D.m; i += 32) ap.push_back({0, k, i, std::min(32, D.m - i)});
-    for (int j = 0; j < D.n; j += 256) apt.push_back({0, k, j, std::min(256, D.n - j)});
-  }
-  d_mvdense.upload(mvdense);
-  d_mvlr.upload(mvlr);
-  d_items_s1.upload(s1); n_items_s1 = (int)s1.size();
-  d_items_ap.upload(ap); n_items_ap = (int)ap.size();
-  d_items_s1t.upload(s1t); n_items_s1t = (int)s1t.size();
-  d_items_apt.upload(apt); n_items_apt = (int)apt.size();
+  build_mv_items();
   BEM_CUDA(cudaDeviceSynchronize());
   keep.clear();
   d_U.release();
@@ -538,17 +530,218 @@ void HOperator::assemble() {
 bool pairs_overflow(size_t ntiles) { return ntiles > (size_t)INT_MAX; }
 
 // ---------------------------------------------------------------------------------------------
+// Groups the payload (dense blocks, U2 chunks, V2 chunks) into work items of at most one
+// matvec stage: consecutive segments whose bytes are contiguous share one bulk copy.
+void HOperator::build_mv_items() {
+  const size_t stage = (size_t)mv_stage_bytes();
+  const int piece = 512;  // target elements per piece (one consumer warp's task)
+  // A span is one contiguous payload range (a block, or a chunk of one) with its generic
+  // pieces (kind, block, first row/col, count, byte offset from the span start).
+  struct GPiece { int kind, blk, k0, cnt, soff; };
+  struct Span { unsigned long long src; size_t bytes; bool direct; std::vector<GPiece> pcs; };
+  struct GItem { unsigned long long src; int bytes; std::vector<GPiece> pcs; };
+  auto group = [&](const std::vector<Span>& spans, std::vector<GItem>& items) {
+    GItem cur{0, 0, {}};
+    bool open = false;
+    for (const Span& sp : spans) {
+      if (sp.direct) {
+        if (open) { items.push_back(std::move(cur)); open = false; }
+        items.push_back(GItem{sp.src, 0, sp.pcs});
+        continue;
+      }
+      if (!(open && sp.src == cur.src + (unsigned long long)cur.bytes && cur.bytes + sp.bytes <= stage &&
+            cur.pcs.size() + sp.pcs.size() <= (size_t)mv_max_pieces())) {
+        if (open) items.push_back(std::move(cur));
+        cur = GItem{sp.src, 0, {}};
+        open = true;
+      }
+      for (GPiece g : sp.pcs) {
+        g.soff += cur.bytes;
+        cur.pcs.push_back(g);
+      }
+      cur.bytes += (int)sp.bytes;
+    }
+    if (open) items.push_back(std::move(cur));
+  };
+  auto pad16 = [](size_t b) { return (b + 15) / 16 * 16; };
+  auto pieces = [&](int kind, int blk, int k0, int cnt, int per, size_t step) {
+    std::vector<GPiece> out;
+    int pc = std::max(1, piece / std::max(1, per));
+    const int cap = mv_max_pieces();
+    if ((cnt + pc - 1) / pc > cap) pc = (cnt + cap - 1) / cap;
+    for (int a = 0; a < cnt; a += pc) out.push_back(GPiece{kind, blk, k0 + a, std::min(pc, cnt - a), (int)(a * step)});
+    return out;
+  };
+  // dense blocks (column-major): column chunks with 16-byte aligned starts
+  std::vector<Span> sd;
+  for (int k = 0; k < (int)mvdense.size(); ++k) {
+    const MVDense& D = mvdense[k];
+    const size_t colb = (size_t)D.m * vsize;
+    const size_t total = pad16(colb * D.n);
+    if (total <= stage) {
+      sd.push_back({D.ptr, total, false, pieces(0, k, 0, D.n, D.m, colb)});
+      continue;
+    }
+    size_t q = 1;
+    while ((colb * q) % 16) ++q;
+    const size_t cc = stage / colb / q * q;
+    if (cc == 0) {  // one column exceeds a stage: read in place
+      sd.push_back({D.ptr, 0, true, pieces(0, k, 0, D.n, D.m, colb)});
+      continue;
+    }
+    for (int j0 = 0; j0 < D.n; j0 += (int)cc) {
+      const int cnt = std::min((int)cc, D.n - j0);
+      const size_t b0 = (size_t)j0 * colb;
+      const size_t b1 = (j0 + cnt == D.n) ? total : (size_t)(j0 + cnt) * colb;
+      sd.push_back({D.ptr + b0, b1 - b0, false, pieces(0, k, j0, cnt, D.m, colb)});
+    }
+  }
+  // low-rank factors: U2 row chunks (pieces of rows), V2 column chunks (pieces of columns)
+  std::vector<Span> su, sv;
+  for (int f = 0; f < (int)mvlr.size(); ++f) {
+    const LRDesc& L = mvlr[f];
+    if (L.R == 0) continue;
+    const size_t cub = (size_t)L.cu * L.R * vsize, cvb = (size_t)L.cv * L.R * vsize;
+    for (int i0 = 0, c = 0; i0 < L.m; i0 += L.cu, ++c)
+      su.push_back({L.u + c * cub, cub, cub > stage, pieces(1, f, i0, std::min(L.cu, L.m - i0), L.R, vsize)});
+    for (int j0 = 0, c = 0; j0 < L.n; j0 += L.cv, ++c)
+      sv.push_back({L.v + c * cvb, cvb, cvb > stage,
+                    pieces(2, f, j0, std::min(L.cv, L.n - j0), L.R, (size_t)L.R * vsize)});
+  }
+  std::vector<GItem> id, iu, iv;
+  group(sd, id);
+  group(su, iu);
+  group(sv, iv);
+  // per pass: 0 t = V2 x, 1 y += D x + U2 t, 2 t = U2^T x, 3 y += D^T x + V2^T t
+  auto piece_raw = [&](int pass, const GPiece& g) {
+    MVPiece p{};
+    p.soff = g.soff;
+    if (g.kind == 0) {
+      const MVDense& D = mvdense[g.blk];
+      if (pass == 1) p = MVPiece{g.soff, 1, D.m, D.m, g.cnt, D.c0 + g.k0, D.r0, 0};
+      else p = MVPiece{g.soff, D.m, 1, g.cnt, D.m, D.r0, D.c0 + g.k0, 0};
+    } else if (g.kind == 1) {
+      const LRDesc& L = mvlr[g.blk];
+      if (pass == 1) p = MVPiece{g.soff, 1, L.cu, g.cnt, L.R, L.toff, L.r0 + g.k0, 1};
+      else p = MVPiece{g.soff, L.cu, 1, L.R, g.cnt, L.r0 + g.k0, L.toff, 2};
+    } else {
+      const LRDesc& L = mvlr[g.blk];
+      if (pass == 0) p = MVPiece{g.soff, 1, L.R, L.R, g.cnt, L.c0 + g.k0, L.toff, 2};
+      else p = MVPiece{g.soff, L.R, 1, g.cnt, L.R, L.toff, L.c0 + g.k0, 1};
+    }
+    return p;
+  };
+  auto piece_for = [&](int pass, const GPiece& g) {
+    MVPiece p = piece_raw(pass, g);
+    p.ow = std::min(p.O, 32);
+    p.groups = 32 / p.ow;
+    p.inv_ow = 1.0f / (float)p.ow;
+    return p;
+  };
+  const std::vector<GItem>* lists[4][2] = {{&iv, nullptr}, {&id, &iu}, {&iu, nullptr}, {&id, &iv}};
+  long long npieces = 0;
+  const int esz = cplx ? 16 : 8;          // one x or t entry as staged (x: FP32 hi+lo or FP64)
+  const int per16 = 16 / esz;             // entries per 16 bytes
+  const int inarea = mv_in_bytes();
+  for (int pass = 0; pass < 4; ++pass) {
+    std::vector<MVTItem> items;
+    std::vector<MVPiece> pcs;
+    std::vector<MVRange> rngs;
+    for (auto* L : lists[pass]) {
+      if (!L) continue;
+      for (const GItem& gi : *L) {
+        MVTItem it{};
+        it.src = gi.src;
+        it.bytes = gi.bytes;
+        it.seg0 = (int)pcs.size();
+        it.nseg = (int)gi.pcs.size();
+        it.rng0 = (int)rngs.size();
+        // input intervals of the pieces, merged into 16-byte aligned ranges of x or t
+        struct Iv { int src, e0, e1; };
+        std::vector<Iv> ivs;
+        std::vector<int> piv;  // range index of each piece
+        for (const GPiece& g : gi.pcs) {
+          const MVPiece p = piece_for(pass, g);
+          const int src = p.flags & 1;
+          const int e0 = p.in_off, e1 = p.in_off + p.Kc;
+          if (!ivs.empty() && ivs.back().src == src && e0 <= ivs.back().e1 + per16 && e1 >= ivs.back().e0 - per16) {
+            ivs.back().e0 = std::min(ivs.back().e0, e0);
+            ivs.back().e1 = std::max(ivs.back().e1, e1);
+          } else {
+            ivs.push_back({src, e0, e1});
+          }
+          piv.push_back((int)ivs.size() - 1);
+          pcs.push_back(p);
+        }
+        std::vector<int> dst(ivs.size());
+        int total = 0;
+        for (size_t r = 0; r < ivs.size(); ++r) {
+          const int a0 = ivs[r].e0 / per16 * per16;
+          const int a1 = (ivs[r].e1 + per16 - 1) / per16 * per16;
+          ivs[r].e0 = a0;
+          ivs[r].e1 = a1;
+          dst[r] = total;
+          total += (a1 - a0) * esz;
+        }
+        if (total <= inarea) {
+          for (size_t r = 0; r < ivs.size(); ++r) {
+            const MVRange rg{ivs[r].src, ivs[r].e0, (ivs[r].e1 - ivs[r].e0) * esz, dst[r]};
+            rngs.push_back(rg);
+            if (r < 2) {
+              it.r[4 * r + 0] = rg.src;
+              it.r[4 * r + 1] = rg.elem;
+              it.r[4 * r + 2] = rg.bytes;
+              it.r[4 * r + 3] = rg.dst;
+            }
+          }
+          for (size_t q = 0; q < gi.pcs.size(); ++q) {
+            MVPiece& p = pcs[it.seg0 + q];
+            const Iv& v = ivs[piv[q]];
+            p.in_soff = dst[piv[q]] + (p.in_off - v.e0) * esz;
+          }
+          it.nrng = (int)ivs.size();
+          it.inbytes = total;
+        } else {
+          it.nrng = 0;
+          it.inbytes = -1;  // inputs read in place
+        }
+        items.push_back(it);
+      }
+    }
+    d_items[pass].upload(items);
+    d_pieces[pass].upload(pcs);
+    d_ranges[pass].upload(rngs);
+    info.mv_ranges[pass] = (int)rngs.size();
+    n_items[pass] = (int)items.size();
+    info.mv_items[pass] = n_items[pass];
+    npieces += (long long)pcs.size();
+  }
+  info.mv_segments = (int)npieces;
+  d_mvdense.upload(mvdense);
+  d_mvlr.upload(mvlr);
+  d_err.alloc(sizeof(int));
+  BEM_CUDA(cudaMemset(d_err.p, 0, sizeof(int)));
+  d_sched.alloc(2 * sizeof(int));
+  BEM_CUDA(cudaMemset(d_sched.p, 0, 2 * sizeof(int)));
+  int dev = 0, nsm = 152;
+  BEM_CUDA(cudaGetDevice(&dev));
+  BEM_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+  mv_grid = nsm;
+}
+
 void HOperator::mult(int trans, const double* alpha, const void* x, const double* beta, void* y, int nrhs,
                      cudaStream_t s) {
   if (nrhs < 1) throw Error(BEM_ERR_ARG, "nrhs must be >= 1");
   const int in_n = trans ? height : width;
   const int out_n = trans ? width : height;
   const int nmax = std::max(height, width);
-  const size_t accsz = cplx ? 16 : 8;
+  const size_t dsz = cplx ? 16 : 8;                 // FP64 accumulators
+  const size_t xsz = (size_t)mv_x_bytes(prec, cplx);  // permuted input values
   if (ws_nrhs < nrhs) {
-    d_xp.alloc((size_t)nmax * nrhs * vsize);
-    d_yp.alloc((size_t)nmax * nrhs * accsz);
-    d_t.alloc((size_t)std::max(t_len, 1) * nrhs * vsize);
+    d_xp.alloc((size_t)nmax * nrhs * xsz + 32);
+    d_yp.alloc((size_t)nmax * nrhs * dsz + 32);
+    d_t.alloc((size_t)std::max(t_len, 1) * nrhs * dsz + 32);
+    d_tx.alloc((size_t)std::max(t_len, 1) * nrhs * xsz + 32);
     ws_nrhs = nrhs;
   }
   const int* pin = trans ? (ttest == ttrial ? d_perm_trial.as<int>() : d_perm_test.as<int>()) : d_perm_trial.as<int>();
@@ -559,25 +752,35 @@ void HOperator::mult(int trans, const double* alpha, const void* x, const double
     BEM_CUDA(cudaEventRecord(ev[0], s));
   }
   launch_permute_in(prec, cplx, pin, in_n, nrhs, in_n, x, d_xp.p, s);
-  BEM_CUDA(cudaMemsetAsync(d_yp.p, 0, (size_t)out_n * nrhs * accsz, s));
+  BEM_CUDA(cudaMemsetAsync(d_yp.p, 0, (size_t)out_n * nrhs * dsz, s));
   if (profiling) BEM_CUDA(cudaEventRecord(ev[1], s));
-  MVArgs a{};
-  a.dense = d_mvdense.as<MVDense>();
-  a.lr = d_mvlr.as<MVLowRank>();
-  a.t = d_t.p;
+  MVArgs2 a{};
   a.xp = d_xp.p;
+  a.t = d_t.p;
+  a.tx = prec == 0 ? d_t.p : d_tx.p;
   a.yp = d_yp.p;
   a.nrhs = nrhs;
+  a.compensated = mv_compensated;
+  a.in_esz = cplx ? 16 : 8;
+  a.err = d_err.as<int>();
+  a.sched = d_sched.as<int>();
   if (t_len > 0) {
-    BEM_CUDA(cudaMemsetAsync(d_t.p, 0, (size_t)t_len * nrhs * vsize, s));
-    a.items = trans ? d_items_s1t.as<MVItem>() : d_items_s1.as<MVItem>();
-    a.nitems = trans ? n_items_s1t : n_items_s1;
-    launch_mv_stage1(prec, cplx, trans != 0, a, s);
+    BEM_CUDA(cudaMemsetAsync(d_t.p, 0, (size_t)t_len * nrhs * dsz, s));
+    a.pass = trans ? 2 : 0;
+    a.items = d_items[a.pass].as<MVTItem>();
+    a.pieces = d_pieces[a.pass].as<MVPiece>();
+    a.ranges = d_ranges[a.pass].as<MVRange>();
+    a.nitems = n_items[a.pass];
+    launch_mv_pass(prec, cplx, a, mv_grid, s);
+    launch_t_to_x(prec, cplx, d_t.p, d_tx.p, (long long)t_len * nrhs, s);
   }
   if (profiling) BEM_CUDA(cudaEventRecord(ev[2], s));
-  a.items = trans ? d_items_apt.as<MVItem>() : d_items_ap.as<MVItem>();
-  a.nitems = trans ? n_items_apt : n_items_ap;
-  launch_mv_apply(prec, cplx, trans != 0, a, s);
+  a.pass = trans ? 3 : 1;
+  a.items = d_items[a.pass].as<MVTItem>();
+  a.pieces = d_pieces[a.pass].as<MVPiece>();
+  a.ranges = d_ranges[a.pass].as<MVRange>();
+  a.nitems = n_items[a.pass];
+  launch_mv_pass(prec, cplx, a, mv_grid, s);
   if (profiling) BEM_CUDA(cudaEventRecord(ev[3], s));
   launch_permute_out(cplx, pout, out_n, nrhs, out_n, alpha, beta, d_yp.p, y, s);
   if (profiling) {
@@ -585,6 +788,12 @@ void HOperator::mult(int trans, const double* alpha, const void* x, const double
     pending.push_back(ev);
   }
   BEM_CUDA(cudaGetLastError());
+}
+
+int HOperator::device_status() {
+  int e = 0;
+  BEM_CUDA(cudaMemcpy(&e, d_err.p, sizeof(int), cudaMemcpyDeviceToHost));
+  return e;
 }
 
 void HOperator::collect_profile() {
@@ -726,103 +935,80 @@ int gmres_solve(int nterms, OperatorBase* const* ops, const double* coef, const 
   return rc;
 }
 
-static int gmres_impl(int nterms, OperatorBase* const* ops, const double* coef, const void* b, void* x, int maxiter,
-                      int restart, double tol, int* iters, double* resid, cudaStream_t s) {
-  if (nterms < 1) throw Error(BEM_ERR_ARG, "gmres needs at least one operator");
-  const int n = ops[0]->height;
+// One restarted GMRES(restart) run on the operator replayed by `exec` (input gin, output
+// gout): x is the initial guess and the result; stops at ||b - A x|| <= tol * scale.
+struct GmresWS {
   bool cplx = false;
-  for (int k = 0; k < nterms; ++k) {
-    if (ops[k]->height != n || ops[k]->width != n) throw Error(BEM_ERR_ARG, "gmres operators must be square and equal-sized");
-    cplx = cplx || ops[k]->cplx || coef[2 * k + 1] != 0.0;
-  }
-  for (int k = 0; k < nterms; ++k)
-    if (ops[k]->cplx != cplx)
-      throw Error(BEM_ERR_ARG, "gmres operators must all act on real or all on complex vectors");
-  restart = std::max(1, std::min(restart, maxiter > 0 ? maxiter : restart));
-  const size_t esz = cplx ? 16 : 8;
-  using C = std::complex<double>;
-  DevBuf Q, gin, gout, hdev, nrm;
-  Q.alloc((size_t)n * (restart + 1) * esz);
-  gin.alloc((size_t)n * esz);
-  gout.alloc((size_t)n * esz);
-  hdev.alloc((size_t)(restart + 2) * esz);
-  nrm.alloc(sizeof(double));
-  const double zero[2] = {0.0, 0.0}, one[2] = {1.0, 0.0};
-  auto apply_ops = [&](cudaStream_t st) {
-    for (int k = 0; k < nterms; ++k) ops[k]->mult(0, coef + 2 * k, gin.p, k == 0 ? zero : one, gout.p, 1, st);
-  };
-  // warm-up (allocates operator workspaces), then capture
-  apply_ops(s);
-  BEM_CUDA(cudaStreamSynchronize(s));
-  cudaGraph_t graph = nullptr;
-  cudaGraphExec_t exec = nullptr;
-  BEM_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-  apply_ops(s);
-  BEM_CUDA(cudaStreamEndCapture(s, &graph));
-  BEM_CUDA(cudaGraphInstantiate(&exec, graph, 0));
-  struct GraphGuard {
-    cudaGraph_t g; cudaGraphExec_t e;
-    ~GraphGuard() { if (e) cudaGraphExecDestroy(e); if (g) cudaGraphDestroy(g); }
-  } gg{graph, exec};
-
-  auto dnorm = [&](const void* v) {
+  int n = 0, restart = 0;
+  size_t esz = 8;
+  DevBuf Q, gin, gout, hdev, nrm, one;
+  cudaStream_t s = nullptr;
+  double dnorm(const void* v) {
     launch_nrm2(cplx, n, v, nrm.as<double>(), s);
     double h;
     BEM_CUDA(cudaMemcpyAsync(&h, nrm.p, sizeof(double), cudaMemcpyDeviceToHost, s));
     BEM_CUDA(cudaStreamSynchronize(s));
     return h;
-  };
-  const double bnorm = dnorm(b);
-  const double bscale = bnorm > 0.0 ? bnorm : 1.0;
-  int it = 0;
-  double rel = 0.0;
-  char* Qp = (char*)Q.p;
-  for (;;) {
-    // r = b - A x
+  }
+  // r = b - A x into gout; returns ||r||
+  double residual(cudaGraphExec_t exec, const void* b, const void* x) {
     BEM_CUDA(cudaMemcpyAsync(gin.p, x, (size_t)n * esz, cudaMemcpyDeviceToDevice, s));
     BEM_CUDA(cudaGraphLaunch(exec, s));
     launch_residual(cplx, n, b, gout.p, s);
-    const double beta = dnorm(gout.p);
-    rel = beta / bscale;
+    return dnorm(gout.p);
+  }
+};
+
+static void gmres_run(GmresWS& w, cudaGraphExec_t exec, const void* b, void* x, int maxiter, double tol, double scale,
+                      int& it, double& rel) {
+  using C = std::complex<double>;
+  const int n = w.n, restart = w.restart;
+  const size_t esz = w.esz;
+  const bool cplx = w.cplx;
+  cudaStream_t s = w.s;
+  char* Qp = (char*)w.Q.p;
+  it = 0;
+  rel = 0.0;
+  for (;;) {
+    const double beta = w.residual(exec, b, x);
+    rel = beta / scale;
     if (rel <= tol || it >= maxiter || beta == 0.0) break;
-    launch_scale_copy(cplx, n, gout.p, 1.0 / beta, Qp, s);
+    launch_scale_copy(cplx, n, w.gout.p, 1.0 / beta, Qp, s);
     std::vector<C> H((size_t)(restart + 1) * restart, C(0)), cs(restart), sn(restart), g(restart + 1, C(0));
     g[0] = beta;
     int j = 0;
     for (; j < restart && it < maxiter; ++j, ++it) {
-      BEM_CUDA(cudaMemcpyAsync(gin.p, Qp + (size_t)j * n * esz, (size_t)n * esz, cudaMemcpyDeviceToDevice, s));
+      BEM_CUDA(cudaMemcpyAsync(w.gin.p, Qp + (size_t)j * n * esz, (size_t)n * esz, cudaMemcpyDeviceToDevice, s));
       BEM_CUDA(cudaGraphLaunch(exec, s));
       std::vector<C> h(j + 1, C(0));
       for (int pass = 0; pass < 2; ++pass) {
-        launch_gemv_ct(cplx, n, j + 1, Q.p, gout.p, hdev.p, s);
-        launch_gemv_sub(cplx, n, j + 1, Q.p, hdev.p, gout.p, s);
+        launch_gemv_ct(cplx, n, j + 1, w.Q.p, w.gout.p, w.hdev.p, s);
+        launch_gemv_sub(cplx, n, j + 1, w.Q.p, w.hdev.p, w.gout.p, s);
         std::vector<double> hh((size_t)(j + 1) * (cplx ? 2 : 1));
-        BEM_CUDA(cudaMemcpyAsync(hh.data(), hdev.p, hh.size() * 8, cudaMemcpyDeviceToHost, s));
+        BEM_CUDA(cudaMemcpyAsync(hh.data(), w.hdev.p, hh.size() * 8, cudaMemcpyDeviceToHost, s));
         BEM_CUDA(cudaStreamSynchronize(s));
         for (int i = 0; i <= j; ++i) h[i] += cplx ? C(hh[2 * i], hh[2 * i + 1]) : C(hh[i], 0.0);
       }
-      const double hn = dnorm(gout.p);
-      if (hn > 0.0) launch_scale_copy(cplx, n, gout.p, 1.0 / hn, Qp + (size_t)(j + 1) * n * esz, s);
+      const double hn = w.dnorm(w.gout.p);
+      if (hn > 0.0) launch_scale_copy(cplx, n, w.gout.p, 1.0 / hn, Qp + (size_t)(j + 1) * n * esz, s);
       for (int i = 0; i <= j; ++i) H[(size_t)i * restart + j] = h[i];
       H[(size_t)(j + 1) * restart + j] = hn;
-      // apply previous rotations
       for (int i = 0; i < j; ++i) {
         C a = H[(size_t)i * restart + j], c2 = H[(size_t)(i + 1) * restart + j];
         H[(size_t)i * restart + j] = std::conj(cs[i]) * a + std::conj(sn[i]) * c2;
         H[(size_t)(i + 1) * restart + j] = -sn[i] * a + cs[i] * c2;
       }
       C a = H[(size_t)j * restart + j], c2 = H[(size_t)(j + 1) * restart + j];
-      double den = std::sqrt(std::norm(a) + std::norm(c2));
+      const double den = std::sqrt(std::norm(a) + std::norm(c2));
       if (den == 0.0) { cs[j] = 1.0; sn[j] = 0.0; }
       else { cs[j] = a / den; sn[j] = c2 / den; }
       H[(size_t)j * restart + j] = std::conj(cs[j]) * a + std::conj(sn[j]) * c2;
       H[(size_t)(j + 1) * restart + j] = 0.0;
       g[j + 1] = -sn[j] * g[j];
       g[j] = std::conj(cs[j]) * g[j];
-      rel = std::abs(g[j + 1]) / bscale;
+      rel = std::abs(g[j + 1]) / scale;
       if (rel <= tol || hn == 0.0) { ++j; ++it; break; }
     }
-    // solve the triangular system and update x
     const int k = j;
     std::vector<C> yv(k, C(0));
     for (int i = k - 1; i >= 0; --i) {
@@ -835,18 +1021,105 @@ static int gmres_impl(int nterms, OperatorBase* const* ops, const double* coef, 
       if (cplx) { yh[2 * i] = yv[i].real(); yh[2 * i + 1] = yv[i].imag(); }
       else yh[i] = yv[i].real();
     }
-    BEM_CUDA(cudaMemcpyAsync(hdev.p, yh.data(), yh.size() * 8, cudaMemcpyHostToDevice, s));
-    launch_axpy_basis(cplx, n, k, Q.p, hdev.p, x, s);
+    BEM_CUDA(cudaMemcpyAsync(w.hdev.p, yh.data(), yh.size() * 8, cudaMemcpyHostToDevice, s));
+    launch_axpy_basis(cplx, n, k, w.Q.p, w.hdev.p, x, s);
     BEM_CUDA(cudaStreamSynchronize(s));
     if (rel <= tol || it >= maxiter) {
-      // final true residual
-      BEM_CUDA(cudaMemcpyAsync(gin.p, x, (size_t)n * esz, cudaMemcpyDeviceToDevice, s));
-      BEM_CUDA(cudaGraphLaunch(exec, s));
-      launch_residual(cplx, n, b, gout.p, s);
-      rel = dnorm(gout.p) / bscale;
+      rel = w.residual(exec, b, x) / scale;
       break;
     }
   }
+}
+
+// GMRES for sum_k coef[k] ops[k].  When an operator stores its blocks in FP32, the solve is a
+// GMRES-based iterative refinement: the Krylov iterations apply the plain FP32 matvec, each
+// outer step recomputes the residual with the error-free (compensated) matvec and corrects x,
+// so the final residual reaches the tolerance for the stored operator.
+static int gmres_impl(int nterms, OperatorBase* const* ops, const double* coef, const void* b, void* x, int maxiter,
+                      int restart, double tol, int* iters, double* resid, cudaStream_t s) {
+  if (nterms < 1) throw Error(BEM_ERR_ARG, "gmres needs at least one operator");
+  const int n = ops[0]->height;
+  bool cplx = false, mixed = false;
+  std::vector<HOperator*> hops;
+  for (int k = 0; k < nterms; ++k) {
+    if (ops[k]->height != n || ops[k]->width != n) throw Error(BEM_ERR_ARG, "gmres operators must be square and equal-sized");
+    cplx = cplx || ops[k]->cplx || coef[2 * k + 1] != 0.0;
+    if (auto* h = dynamic_cast<HOperator*>(ops[k])) {
+      hops.push_back(h);
+      mixed = mixed || h->prec == 1;
+    }
+  }
+  for (int k = 0; k < nterms; ++k)
+    if (ops[k]->cplx != cplx)
+      throw Error(BEM_ERR_ARG, "gmres operators must all act on real or all on complex vectors");
+  restart = std::max(1, std::min(restart, maxiter > 0 ? maxiter : restart));
+  GmresWS w;
+  w.cplx = cplx;
+  w.n = n;
+  w.restart = restart;
+  w.esz = cplx ? 16 : 8;
+  w.s = s;
+  w.Q.alloc((size_t)n * (restart + 1) * w.esz);
+  w.gin.alloc((size_t)n * w.esz);
+  w.gout.alloc((size_t)n * w.esz);
+  w.hdev.alloc((size_t)(restart + 2) * w.esz);
+  w.nrm.alloc(sizeof(double));
+  const double onev[2] = {1.0, 0.0};
+  w.one.alloc(16);
+  BEM_CUDA(cudaMemcpy(w.one.p, onev, 16, cudaMemcpyHostToDevice));
+  const double zero[2] = {0.0, 0.0}, one[2] = {1.0, 0.0};
+  std::vector<int> saved;
+  for (auto* h : hops) saved.push_back(h->mv_compensated);
+  struct Restore {
+    std::vector<HOperator*>& h;
+    std::vector<int>& v;
+    ~Restore() { for (size_t i = 0; i < h.size(); ++i) h[i]->mv_compensated = v[i]; }
+  } restore{hops, saved};
+  auto capture = [&](int compensated, cudaGraph_t& g, cudaGraphExec_t& e) {
+    for (auto* h : hops) h->mv_compensated = compensated;
+    auto apply = [&]() {
+      for (int k = 0; k < nterms; ++k) ops[k]->mult(0, coef + 2 * k, w.gin.p, k == 0 ? zero : one, w.gout.p, 1, s);
+    };
+    apply();  // allocates the operators' workspaces outside the capture
+    BEM_CUDA(cudaStreamSynchronize(s));
+    BEM_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    apply();
+    BEM_CUDA(cudaStreamEndCapture(s, &g));
+    BEM_CUDA(cudaGraphInstantiate(&e, g, 0));
+  };
+  struct GraphGuard {
+    cudaGraph_t g = nullptr;
+    cudaGraphExec_t e = nullptr;
+    ~GraphGuard() { if (e) cudaGraphExecDestroy(e); if (g) cudaGraphDestroy(g); }
+  } acc, fast;
+  capture(1, acc.g, acc.e);
+  const double bnorm = w.dnorm(b);
+  const double scale = bnorm > 0.0 ? bnorm : 1.0;
+  int it = 0;
+  double rel = 0.0;
+  if (!mixed) {
+    gmres_run(w, acc.e, b, x, maxiter, tol, scale, it, rel);
+  } else {
+    capture(0, fast.g, fast.e);
+    DevBuf r, e;
+    r.alloc((size_t)n * w.esz);
+    e.alloc((size_t)n * w.esz);
+    for (int outer = 0; outer < 50; ++outer) {
+      rel = w.residual(acc.e, b, x) / scale;
+      if (rel <= tol || it >= maxiter) break;
+      BEM_CUDA(cudaMemcpyAsync(r.p, w.gout.p, (size_t)n * w.esz, cudaMemcpyDeviceToDevice, s));
+      BEM_CUDA(cudaMemsetAsync(e.p, 0, (size_t)n * w.esz, s));
+      // the inner solve reduces the residual to what the outer step still needs, but not
+      // below the rounding level of the FP32 matvec
+      const double inner_tol = std::max(0.5 * tol / rel, 1e-6);
+      int iit = 0;
+      double irel = 0.0;
+      gmres_run(w, fast.e, r.p, e.p, maxiter - it, inner_tol, rel * scale, iit, irel);
+      it += std::max(iit, 1);
+      launch_axpy_basis(cplx, n, 1, e.p, w.one.p, x, s);  // x += e
+    }
+  }
+  BEM_CUDA(cudaStreamSynchronize(s));
   if (iters) *iters = it;
   if (resid) *resid = rel;
   return BEM_OK;
