@@ -131,6 +131,23 @@ int bem_operator_blocks(bem_operator_t op, int* rowcl, int* colcl, int* near, in
 int bem_operator_mult(bem_operator_t op, int trans, const double* alpha, const void* x,
                       const double* beta, void* y, int nrhs, void* stream);
 
+/* Bytes of the fixed device scratch area used by bem_operator_mult_noalloc (one per device). */
+#define BEM_NOALLOC_SCRATCH_BYTES (16u << 20)
+
+/* bem_operator_mult for callers that must not have device memory allocated on their behalf
+ * (no counterpart in the reference).  bem_operator_mult grows operator-owned scratch on first
+ * use and when nrhs grows (cudaFree + cudaMalloc; cudaFree waits for the whole device).  This
+ * entry point allocates nothing: its scratch is a fixed file-scope device array of
+ * BEM_NOALLOC_SCRATCH_BYTES.  Same arguments, same result (up to the order of FP64 atomic
+ * additions).  H-matrix operators only (BEM_ERR_STATE for a mass operator).  A call whose
+ * scratch would exceed the area -- about 2 * (height + width + sum of block ranks) * nrhs
+ * values -- returns BEM_ERR_ARG before launching anything.  The first call on a device looks
+ * the array up (and may load device code): make it before any stream capture.  The area is
+ * shared by every call on a device, so overlapping calls (several streams or host threads)
+ * race: serialise them. */
+int bem_operator_mult_noalloc(bem_operator_t op, int trans, const double* alpha, const void* x,
+                              const double* beta, void* y, int nrhs, void* stream);
+
 /* Same with HOST buffers: copies x up, applies, copies y back (synchronous). */
 int bem_operator_mult_host(bem_operator_t op, int trans, const double* alpha, const void* x,
                            const double* beta, void* y, int nrhs);

@@ -19,6 +19,7 @@ if not os.path.exists(LIB_PATH):
 lib = C.CDLL(LIB_PATH)
 
 BEM_OK, BEM_ERR_ARG, BEM_ERR_CUDA, BEM_ERR_ALLOC, BEM_ERR_STATE, BEM_ERR_INTERNAL = range(6)
+NOALLOC_SCRATCH_BYTES = 16 << 20  # BEM_NOALLOC_SCRATCH_BYTES of include/ngbem_gb300.h
 KERNELS = {"laplace_sl": 0, "laplace_dl": 1, "laplace_hs": 2, "helmholtz_sl": 3, "helmholtz_dl": 4,
            "helmholtz_hs": 5, "helmholtz_cf": 6, "maxwell_sl": 7}
 KINDS = {"P0": 0, "P1": 1, "RT0": 2}
@@ -63,6 +64,7 @@ SIGNATURES = {
     "bem_operator_info": ([_vp, C.POINTER(OperatorInfo)], C.c_int),
     "bem_operator_blocks": ([_vp, _ip, _ip, _ip, _ip, _ip], C.c_int),
     "bem_operator_mult": ([_vp, C.c_int, _dp, _vp, _dp, _vp, C.c_int, _vp], C.c_int),
+    "bem_operator_mult_noalloc": ([_vp, C.c_int, _dp, _vp, _dp, _vp, C.c_int, _vp], C.c_int),
     "bem_operator_mult_host": ([_vp, C.c_int, _dp, _vp, _dp, _vp, C.c_int], C.c_int),
     "bem_operator_to_dense": ([_vp, _vp], C.c_int),
     "bem_operator_destroy": ([_vp], C.c_int),

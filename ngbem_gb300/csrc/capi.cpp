@@ -226,6 +226,16 @@ int bem_operator_mult(bem_operator_t op, int trans, const double* alpha, const v
   });
 }
 
+int bem_operator_mult_noalloc(bem_operator_t op, int trans, const double* alpha, const void* x, const double* beta,
+                              void* y, int nrhs, void* stream) {
+  return guarded([&] {
+    REQUIRE(op && alpha && beta && x && y, "null argument");
+    auto* h = dynamic_cast<HOperator*>(op->op.get());
+    if (!h) throw Error(BEM_ERR_STATE, "not an H-matrix operator");
+    mult_noalloc(*h, trans, alpha, x, beta, y, nrhs, (cudaStream_t)stream);
+  });
+}
+
 int bem_operator_mult_host(bem_operator_t op, int trans, const double* alpha, const void* x, const double* beta,
                            void* y, int nrhs) {
   return guarded([&] {

@@ -197,6 +197,11 @@ struct MassOperator : OperatorBase {
             cudaStream_t s) override;
 };
 
+// op.mult with the scratch taken from a fixed device array instead of operator buffers
+// (mult_noalloc.cu); allocates nothing.
+void mult_noalloc(HOperator& op, int trans, const double* alpha, const void* x, const double* beta, void* y,
+                  int nrhs, cudaStream_t s);
+
 int trace_kind(int space_kind, int ev);
 bool pairs_overflow(size_t ntiles);
 int gmres_solve(int nterms, OperatorBase* const* ops, const double* coef, const void* b, void* x, int maxiter,
