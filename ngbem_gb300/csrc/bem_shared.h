@@ -104,8 +104,9 @@ struct MVTItem {
   unsigned long long src;
   int bytes, seg0, nseg, rng0, nrng, inbytes;
   int r[8];  // the first two input ranges inline (src, elem, bytes, dst each); others in the range list
-  int pad;
+  int pad[4];  // 80 bytes: runs of descriptors are bulk-copied (16-byte multiples)
 };
+static_assert(sizeof(MVTItem) % 16 == 0, "MVTItem is bulk-copied");
 
 // A piece of an item as one pass applies it: out[out_off + o] += sum_k A[o*so + k*sk] *
 // in[in_off + k] for o < O, k < Kc, with A at byte soff of the item payload.  flags bit 0:

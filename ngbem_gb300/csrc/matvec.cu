@@ -197,7 +197,8 @@ template <> struct Acc<cpx<double>> {
 #define MV_INBUF 128
 #define MV_MAXPC 128
 #define MV_INAREA 16384
-#define MV_HDR 256
+#define MV_CHMAX 8   // items per claimed chunk, at most
+#define MV_HDR (128 + MV_NSTAGE * 32 + 2 * MV_CHMAX * 80)
 
 // what the producer tells the consumers about the item in a stage (nseg < 0: no more items)
 struct MVStageHdr {
@@ -334,10 +335,12 @@ __device__ __forceinline__ void run_piece_s(const MVArgs2& a, const MVPiece& pc,
 // stage's full barrier.  The consumer warps take the pieces of each item round-robin --
 // reading only shared memory -- and release the stage on its empty barrier.
 //
-// Items are handed out on demand: a CTA starts with items blockIdx.x and blockIdx.x + G, then
-// claims the others from the counter a.sched[0] (index 2G + claim), so SMs whose copies land
-// later than others' do fewer items instead of setting the kernel time.  Claims are made one
-// item ahead, so their latency overlaps the copies of the current item.  The last CTA to
+// Items are handed out in chunks of consecutive items.  A CTA's first chunk is fixed
+// (blockIdx.x * w0 ...); later chunks are claimed from the counter a.sched[0], with sizes that
+// shrink as the items run out (guided scheduling), so SMs whose copies land later do fewer
+// items instead of setting the kernel time.  The descriptors of a chunk are bulk-copied into
+// one of two shared-memory buffers while the previous chunk is issued, and each claim is
+// made one chunk ahead, so the issue loop never waits on a global load.  The last CTA to
 // finish resets both counters, which leaves them zero for the next launch on the stream.
 // After its last item the producer pushes a stop marker (nseg < 0) through the next stage.
 template <class VS, bool COMP>
@@ -345,7 +348,9 @@ __global__ void __launch_bounds__(MV_THREADS, 1) mv_tma_kernel(MVArgs2 a) {
   extern __shared__ __align__(128) unsigned char smem[];
   uint64_t* full = (uint64_t*)smem;                               // MV_NSTAGE barriers
   uint64_t* empty = full + MV_NSTAGE;                             // MV_NSTAGE barriers
-  MVStageHdr* hdr = (MVStageHdr*)(smem + 16 * MV_NSTAGE);         // per stage: what the item holds
+  uint64_t* dbar = empty + MV_NSTAGE;                             // 2 barriers: descriptor buffers
+  MVStageHdr* hdr = (MVStageHdr*)(smem + 128);                    // per stage: what the item holds
+  MVTItem* dring = (MVTItem*)(smem + 128 + MV_NSTAGE * sizeof(MVStageHdr));  // 2 x MV_CHMAX descriptors
   unsigned char* stage = smem + MV_HDR;
   MVPiece* dstage = (MVPiece*)(stage + MV_NSTAGE * MV_STAGE);    // per stage: MV_MAXPC descriptors
   unsigned char* istage = (unsigned char*)(dstage + MV_NSTAGE * MV_MAXPC);  // per stage: MV_INAREA bytes
@@ -357,70 +362,109 @@ __global__ void __launch_bounds__(MV_THREADS, 1) mv_tma_kernel(MVArgs2 a) {
       mbar_init(&full[s], 1);
       mbar_init(&empty[s], MV_CONSUMERS);
     }
+    mbar_init(&dbar[0], 1);
+    mbar_init(&dbar[1], 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
   }
   __syncthreads();
   if (warp == 0) {
-    uint32_t ephase = 0;
+    uint32_t ephase = 0, dphase = 0;
     int it = 0;
     int ok = 1;
-    // kc/dc: the item to issue now; kn/dn: the next one (descriptor load in flight);
-    // tok: lane 0's claim of the item after that (atomic in flight)
-    int kc = blockIdx.x;
-    int kn = blockIdx.x + G < nit ? blockIdx.x + G : nit;
-    MVTItem dc = a.items[kc], dn{};
-    if (kn < nit) dn = a.items[kn];
-    int tok = 0;
-    if (lane == 0 && kn < nit) tok = atomicAdd(a.sched, 1);
-    while (kc < nit) {
-      const int s = it % MV_NSTAGE;
-      // the first use of a stage passes at once (parity of the phase before the first)
-      if (lane == 0) ok = mbar_wait(&empty[s], ((ephase >> s) & 1u) ^ 1u) ? 1 : 0;
+    auto chunk_size = [&](int remaining) {
+      const int w = remaining / (4 * G);
+      return w < 2 ? 2 : (w > MV_CHMAX ? MV_CHMAX : w);
+    };
+    auto fetch_descs = [&](int buf, int c0, int cn) {  // lane 0
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      bulk_load(dring + buf * MV_CHMAX, a.items + c0, cn * (int)sizeof(MVTItem), &dbar[buf]);
+    };
+    // fixed first chunk, then claims at w0 * G + counter
+    const int w0 = chunk_size(nit);
+    const int base = w0 * G;
+    int c0 = blockIdx.x * w0;
+    int cn = c0 < nit ? min(w0, nit - c0) : 0;
+    int sc = 0;
+    int dpend = -1;  // descriptor buffer with a copy in flight that nobody has waited for
+    if (cn > 0) {
+      if (lane == 0) fetch_descs(0, c0, cn);
+      dpend = 0;
+    }
+    int want = chunk_size(nit - base), tok = 0;
+    bool pend = base < nit;
+    if (pend && lane == 0) tok = atomicAdd(a.sched, want);
+    while (cn > 0) {
+      ok = mbar_wait(&dbar[sc], (dphase >> sc) & 1u) ? 1 : 0;
       ok = __shfl_sync(0xffffffffu, ok, 0);
       if (!ok) break;
-      ephase ^= 1u << s;
-      const int dbytes = dc.nseg * (int)sizeof(MVPiece);
-      if (lane == 0) {
-        hdr[s].nseg = dc.nseg;
-        hdr[s].bytes = dc.bytes;
-        hdr[s].inbytes = dc.inbytes;
-        hdr[s].src = dc.src;
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-        // one arrival carries the transaction bytes of all copies of the item
-        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(&full[s])),
-                     "r"(dc.bytes + dbytes + (dc.inbytes > 0 ? dc.inbytes : 0)) : "memory");
-        if (dc.bytes > 0)
-          asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
-                       ::"r"(smem_u32(stage + s * MV_STAGE)), "l"((const void*)dc.src), "r"(dc.bytes),
-                       "r"(smem_u32(&full[s])) : "memory");
-        if (dbytes > 0)
-          asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
-                       ::"r"(smem_u32(dstage + s * MV_MAXPC)), "l"((const void*)(a.pieces + dc.seg0)),
-                       "r"(dbytes), "r"(smem_u32(&full[s])) : "memory");
-      }
-      __syncwarp();
-      unsigned char* ia = istage + s * MV_INAREA;
-      for (int r = lane; r < dc.nrng; r += 32) {
-        MVRange rg;
-        if (r < 2) rg = r == 0 ? MVRange{dc.r[0], dc.r[1], dc.r[2], dc.r[3]} : MVRange{dc.r[4], dc.r[5], dc.r[6], dc.r[7]};
-        else rg = a.ranges[dc.rng0 + r];
-        const unsigned char* gsrc = (const unsigned char*)(rg.src ? a.tx : a.xp) + (size_t)rg.elem * a.in_esz;
-        asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
-                     ::"r"(smem_u32(ia + rg.dst)), "l"((const void*)gsrc), "r"(rg.bytes),
-                     "r"(smem_u32(&full[s])) : "memory");
-      }
-      ++it;
-      // advance: the claim made one item ago names the item after next
-      kc = kn;
-      dc = dn;
-      if (kn < nit) {
-        const int k = 2 * G + __shfl_sync(0xffffffffu, tok, 0);
-        kn = k < nit ? k : nit;
-        if (kn < nit) {
-          dn = a.items[kn];
-          if (lane == 0) tok = atomicAdd(a.sched, 1);
+      dphase ^= 1u << sc;
+      dpend = -1;
+      int n0 = 0, nn = 0, wnext = 0;
+      for (int j = 0; j < cn && ok; ++j) {
+        const MVTItem* d = dring + sc * MV_CHMAX + j;
+        const unsigned long long src = d->src;
+        const int bytes = d->bytes, seg0 = d->seg0, nseg = d->nseg, rng0 = d->rng0, nrng = d->nrng;
+        const int inbytes = d->inbytes;
+        const int s = it % MV_NSTAGE;
+        // the first use of a stage passes at once (parity of the phase before the first)
+        if (lane == 0) ok = mbar_wait(&empty[s], ((ephase >> s) & 1u) ^ 1u) ? 1 : 0;
+        ok = __shfl_sync(0xffffffffu, ok, 0);
+        if (!ok) break;
+        ephase ^= 1u << s;
+        const int dbytes = nseg * (int)sizeof(MVPiece);
+        if (lane == 0) {
+          hdr[s].nseg = nseg;
+          hdr[s].bytes = bytes;
+          hdr[s].inbytes = inbytes;
+          hdr[s].src = src;
+          asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+          // one arrival carries the transaction bytes of all copies of the item
+          asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(&full[s])),
+                       "r"(bytes + dbytes + (inbytes > 0 ? inbytes : 0)) : "memory");
+          if (bytes > 0)
+            asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                         ::"r"(smem_u32(stage + s * MV_STAGE)), "l"((const void*)src), "r"(bytes),
+                         "r"(smem_u32(&full[s])) : "memory");
+          if (dbytes > 0)
+            asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                         ::"r"(smem_u32(dstage + s * MV_MAXPC)), "l"((const void*)(a.pieces + seg0)),
+                         "r"(dbytes), "r"(smem_u32(&full[s])) : "memory");
         }
+        unsigned char* ia = istage + s * MV_INAREA;
+        for (int r = lane; r < nrng; r += 32) {
+          MVRange rg;
+          if (r < 2) rg = MVRange{d->r[4 * r], d->r[4 * r + 1], d->r[4 * r + 2], d->r[4 * r + 3]};
+          else rg = a.ranges[rng0 + r];
+          const unsigned char* gsrc = (const unsigned char*)(rg.src ? a.tx : a.xp) + (size_t)rg.elem * a.in_esz;
+          asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                       ::"r"(smem_u32(ia + rg.dst)), "l"((const void*)gsrc), "r"(rg.bytes),
+                       "r"(smem_u32(&full[s])) : "memory");
+        }
+        __syncwarp();
+        ++it;
+        if (pend) {
+          // the claim made a chunk ago: start copying the descriptors of the next chunk
+          pend = false;
+          const int k = base + __shfl_sync(0xffffffffu, tok, 0);
+          n0 = k;
+          nn = k < nit ? min(want, nit - k) : 0;
+          wnext = nit - (k + want);
+          if (nn > 0) {
+            if (lane == 0) fetch_descs(sc ^ 1, n0, nn);
+            dpend = sc ^ 1;
+          }
+        }
+      }
+      if (!ok) break;
+      __syncwarp();
+      sc ^= 1;
+      c0 = n0;
+      cn = nn;
+      if (cn > 0 && wnext > 0) {
+        want = chunk_size(wnext);
+        pend = true;
+        if (lane == 0) tok = atomicAdd(a.sched, want);
       }
     }
     if (lane == 0) {
@@ -432,6 +476,8 @@ __global__ void __launch_bounds__(MV_THREADS, 1) mv_tma_kernel(MVArgs2 a) {
         if (j >= it - MV_NSTAGE) mbar_wait(&full[s], (fphase >> s) & 1u);
         fphase ^= 1u << s;
       }
+      // a descriptor copy still in flight (error path) must land too
+      if (dpend >= 0) mbar_wait(&dbar[dpend], (dphase >> dpend) & 1u);
       const int s = it % MV_NSTAGE;
       if (ok && mbar_wait(&empty[s], ((ephase >> s) & 1u) ^ 1u)) {
         hdr[s].nseg = -1;
@@ -522,7 +568,8 @@ __global__ void __launch_bounds__(256) mv_multi_kernel(MVArgs2 a) {
 }
 
 int mv_smem_bytes() {
-  static_assert(16 * MV_NSTAGE + (int)sizeof(MVStageHdr) * MV_NSTAGE <= MV_HDR, "matvec header area");
+  static_assert(16 * MV_NSTAGE + 16 <= 128 && sizeof(MVStageHdr) == 32 && sizeof(MVTItem) == 80,
+                "matvec header area");
   return MV_HDR + MV_NSTAGE * (MV_STAGE + MV_MAXPC * (int)sizeof(MVPiece) + MV_INAREA);
 }
 int mv_in_bytes() { return MV_INAREA; }
