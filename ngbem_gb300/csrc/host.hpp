@@ -159,8 +159,11 @@ struct HOperator : OperatorBase {
   DevBuf d_perm_trial, d_perm_test, d_pinv_trial, d_pinv_test;
   std::vector<std::unique_ptr<DevBuf>> pools;  // dense and factor pools
   DevBuf d_mvdense, d_mvlr, d_err, d_sched;
-  DevBuf d_items[4], d_pieces[4], d_ranges[4];  // per pass: 0 t=V2 x, 1 y+=Dx+U2 t, 2 t=U2^T x, 3 y+=D^T x+V2^T t
-  int n_items[4] = {0, 0, 0, 0};
+  // per pass: 0 t=V2 x, 1 y+=Dx+U2 t, 2 t=U2^T x, 3 y+=D^T x+V2^T t; 4-7 the two phases of the
+  // single-launch matvec (4: t=V2 x and y+=Dx, 5: y+=U2 t; 6, 7 the same for the transpose)
+  DevBuf d_items[MV_NPASS], d_pieces[MV_NPASS], d_ranges[MV_NPASS];
+  int n_items[MV_NPASS] = {};
+  bool mv_fused = true;  // one cooperative launch per single-RHS matvec (else the 4-pass pipeline)
   int mv_grid = 152;
   int mv_compensated = 1;  // fp32 storage: error-free products/sums (1) or plain FP32 (0)
   int t_len = 0;
@@ -173,6 +176,7 @@ struct HOperator : OperatorBase {
   bool profiling = false;
   cudaEvent_t pev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
   std::vector<std::array<cudaEvent_t, 5>> pending;  // recorded, not yet read
+  std::vector<bool> pending_fused;                   // ... by a single-launch matvec
   double kms[4] = {0, 0, 0, 0};                     // permute_in, stage1, apply, permute_out
   long long kcount[4] = {0, 0, 0, 0};
   void collect_profile();

@@ -110,6 +110,35 @@ struct MVArgs2 {
   int* err;
   int* sched;        // two zeroed counters (items claimed, CTAs finished); left zero after a pass
 };
+// passes per operator: 0-3 the four-pass pipeline, 4-7 the phases of the single-launch matvec
+#define MV_NPASS 8
+
+// Single-launch matvec (one right-hand side): permute x, phase A items (t = V2 x and y += D x),
+// t -> input form, phase B items (y += U2 t), un-permute y with alpha/beta; grid barriers
+// between the phases (cooperative launch).  a: the shared arguments of the passes (items,
+// pieces, ranges, nitems are set per phase from the fields below).
+struct MVFusedArgs {
+  MVArgs2 a;
+  const MVTItem* items[2];
+  const MVPiece* pieces[2];
+  const MVRange* ranges[2];
+  int nitems[2];
+  int* ctr[2];          // chunk-claim counters of the two phases (zeroed in the prologue)
+  unsigned* bar;        // grid barrier: [0] arrivals (zero between barriers), [1] generation
+  const int* perm_in;   // xp[k] = x[perm_in[k]], k < n_in
+  int n_in;
+  const void* x;        // FP64 / complex128 input
+  const int* perm_out;  // y[perm_out[k]] = alpha yp[k] + beta y[perm_out[k]], k < n_out
+  int n_out;
+  void* y;
+  double alpha[2], beta[2];
+  int use_beta;
+  long long t_len;
+};
+// false if the device cannot run it (no cooperative launch or the pipeline does not fit an SM)
+bool mv_fused_supported();
+cudaError_t launch_mv_fused(int prec, bool cplx, const MVFusedArgs& f, cudaStream_t s);
+
 // prec 0: fp64 storage, 1: fp32 storage.  cplx: complex operator.
 void launch_mv_pass(int prec, bool cplx, const MVArgs2& a, int grid, cudaStream_t s);
 int mv_stage_bytes();

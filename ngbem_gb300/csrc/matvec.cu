@@ -9,6 +9,7 @@
 // un-permutes and applies alpha/beta.  Storage precision S is fp64 or fp32; products are
 // formed in S and block partial sums are added in FP64.
 #include <algorithm>
+#include <type_traits>
 
 #include "bem_device.cuh"
 #include "kernels.h"
@@ -43,6 +44,10 @@ __global__ void permute_out_kernel(const int* perm, int n, int nrhs, int ld, VD 
 }
 
 __device__ __forceinline__ double scal_mul(double a, double b) { return a * b; }
+
+template <class D> __device__ __forceinline__ D mk_d(double re, double im);
+template <> __device__ __forceinline__ double mk_d<double>(double re, double) { return re; }
+template <> __device__ __forceinline__ cpx<double> mk_d<cpx<double>>(double re, double im) { return mkc(re, im); }
 
 // ---------------------------------------------------------------------------------------
 // Item-based passes.  The H-matrix payload (dense blocks column-major, U2 row chunks, V2
@@ -329,199 +334,227 @@ __device__ __forceinline__ void run_piece_s(const MVArgs2& a, const MVPiece& pc,
                         [&](int o, D v) { atomic_add(&out[o], v); }, lane);
 }
 
-// Persistent single right-hand-side pass, warp specialised.  Warp 0 streams items into
-// MV_NSTAGE shared-memory stages with bulk copies: the payload, the item's piece descriptors
-// and the input ranges its pieces read (slices of the permuted x or of t), all counted on the
-// stage's full barrier.  The consumer warps take the pieces of each item round-robin --
-// reading only shared memory -- and release the stage on its empty barrier.
+// Persistent single right-hand-side pass, warp specialised.  Warp 0 (the producer) streams
+// items into MV_NSTAGE shared-memory stages with bulk copies: the payload, the item's piece
+// descriptors and the input ranges its pieces read (slices of the permuted x or of t), all
+// counted on the stage's full barrier.  The consumer warps take the pieces of each item
+// round-robin -- reading only shared memory -- and release the stage on its empty barrier.
 //
 // Items are handed out in chunks of consecutive items.  A CTA's first chunk is fixed
-// (blockIdx.x * w0 ...); later chunks are claimed from the counter a.sched[0], with sizes that
-// shrink as the items run out (guided scheduling), so SMs whose copies land later do fewer
-// items instead of setting the kernel time.  The descriptors of a chunk are bulk-copied into
-// one of two shared-memory buffers while the previous chunk is issued, and each claim is
-// made one chunk ahead, so the issue loop never waits on a global load.  The last CTA to
-// finish resets both counters, which leaves them zero for the next launch on the stream.
-// After its last item the producer pushes a stop marker (nseg < 0) through the next stage.
-template <class VS, bool COMP>
-__global__ void __launch_bounds__(MV_THREADS, 1) mv_tma_kernel(MVArgs2 a) {
-  extern __shared__ __align__(128) unsigned char smem[];
-  uint64_t* full = (uint64_t*)smem;                               // MV_NSTAGE barriers
-  uint64_t* empty = full + MV_NSTAGE;                             // MV_NSTAGE barriers
-  uint64_t* dbar = empty + MV_NSTAGE;                             // 2 barriers: descriptor buffers
-  MVStageHdr* hdr = (MVStageHdr*)(smem + 128);                    // per stage: what the item holds
-  MVTItem* dring = (MVTItem*)(smem + 128 + MV_NSTAGE * sizeof(MVStageHdr));  // 2 x MV_CHMAX descriptors
-  unsigned char* stage = smem + MV_HDR;
-  MVPiece* dstage = (MVPiece*)(stage + MV_NSTAGE * MV_STAGE);    // per stage: MV_MAXPC descriptors
-  unsigned char* istage = (unsigned char*)(dstage + MV_NSTAGE * MV_MAXPC);  // per stage: MV_INAREA bytes
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int G = gridDim.x;
-  const int nit = a.nitems;
-  if (tid == 0) {
+// (blockIdx.x * w0 ...); later chunks are claimed from a counter, with sizes that shrink as
+// the items run out (guided scheduling), so SMs whose copies land later do fewer items
+// instead of setting the kernel time.  The descriptors of a chunk are bulk-copied into one of
+// two shared-memory buffers while the previous chunk is issued, and each claim is made one
+// chunk ahead, so the issue loop never waits on a global load.  After its last item the
+// producer pushes a stop marker (nseg < 0) through the next stage; the consumers release it
+// like an item, so a second pass can run through the same pipeline.
+struct MVSmem {
+  uint64_t* full;        // MV_NSTAGE barriers: stage filled
+  uint64_t* empty;       // MV_NSTAGE barriers: stage released by all consumer warps
+  uint64_t* dbar;        // 2 barriers: descriptor buffers filled
+  MVStageHdr* hdr;       // per stage: what the item holds
+  MVTItem* dring;        // 2 x MV_CHMAX item descriptors
+  unsigned char* stage;  // per stage: MV_STAGE payload bytes
+  MVPiece* dstage;       // per stage: MV_MAXPC piece descriptors
+  unsigned char* istage; // per stage: MV_INAREA staged input bytes
+};
+
+__device__ __forceinline__ MVSmem mv_smem(unsigned char* smem) {
+  MVSmem m;
+  m.full = (uint64_t*)smem;
+  m.empty = m.full + MV_NSTAGE;
+  m.dbar = m.empty + MV_NSTAGE;
+  m.hdr = (MVStageHdr*)(smem + 128);
+  m.dring = (MVTItem*)(smem + 128 + MV_NSTAGE * sizeof(MVStageHdr));
+  m.stage = smem + MV_HDR;
+  m.dstage = (MVPiece*)(m.stage + MV_NSTAGE * MV_STAGE);
+  m.istage = (unsigned char*)(m.dstage + MV_NSTAGE * MV_MAXPC);
+  return m;
+}
+
+__device__ __forceinline__ void mv_init_barriers(const MVSmem& m) {
+  if (threadIdx.x == 0) {
     for (int s = 0; s < MV_NSTAGE; ++s) {
-      mbar_init(&full[s], 1);
-      mbar_init(&empty[s], MV_CONSUMERS);
+      mbar_init(&m.full[s], 1);
+      mbar_init(&m.empty[s], MV_CONSUMERS);
     }
-    mbar_init(&dbar[0], 1);
-    mbar_init(&dbar[1], 1);
+    mbar_init(&m.dbar[0], 1);
+    mbar_init(&m.dbar[1], 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
   }
   __syncthreads();
-  if (warp == 0) {
-    uint32_t ephase = 0, dphase = 0;
-    int it = 0;
-    int ok = 1;
-    auto chunk_size = [&](int remaining) {
-      const int w = remaining / (4 * G);
-      return w < 2 ? 2 : (w > MV_CHMAX ? MV_CHMAX : w);
-    };
-    auto fetch_descs = [&](int buf, int c0, int cn) {  // lane 0
-      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-      bulk_load(dring + buf * MV_CHMAX, a.items + c0, cn * (int)sizeof(MVTItem), &dbar[buf]);
-    };
-    // fixed first chunk, then claims at w0 * G + counter
-    const int w0 = chunk_size(nit);
-    const int base = w0 * G;
-    int c0 = blockIdx.x * w0;
-    int cn = c0 < nit ? min(w0, nit - c0) : 0;
-    int sc = 0;
-    int dpend = -1;  // descriptor buffer with a copy in flight that nobody has waited for
-    if (cn > 0) {
-      if (lane == 0) fetch_descs(0, c0, cn);
-      dpend = 0;
-    }
-    int want = chunk_size(nit - base), tok = 0;
-    bool pend = base < nit;
-    if (pend && lane == 0) tok = atomicAdd(a.sched, want);
-    while (cn > 0) {
-      ok = mbar_wait(&dbar[sc], (dphase >> sc) & 1u) ? 1 : 0;
+}
+
+// pipeline position of the producer warp / of one consumer warp (carried across passes)
+struct MVProd { uint32_t ephase = 0, dphase = 0; int it = 0; };
+struct MVCons { uint32_t fphase = 0; int it = 0; int pbase = 0; };
+
+// Producer warp: streams items [0, nit) (first chunk fixed, the rest claimed from *ctr), then
+// the stop marker.  Returns false if a wait timed out (error flag set; copies drained).
+__device__ bool mv_produce(const MVArgs2& a, const MVTItem* items, int nit, int* ctr, const MVSmem& m, MVProd& p,
+                           int lane) {
+  const int G = gridDim.x;
+  int ok = 1;
+  const int it0 = p.it;
+  // global data written before this pass by ordinary stores (x, t) is read by bulk copies
+  asm volatile("fence.proxy.async.global;" ::: "memory");
+  auto chunk_size = [&](int remaining) {
+    const int w = remaining / (4 * G);
+    return w < 2 ? 2 : (w > MV_CHMAX ? MV_CHMAX : w);
+  };
+  auto fetch_descs = [&](int buf, int c0, int cn) {  // lane 0
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    bulk_load(m.dring + buf * MV_CHMAX, items + c0, cn * (int)sizeof(MVTItem), &m.dbar[buf]);
+  };
+  // fixed first chunk, then claims at w0 * G + counter
+  const int w0 = chunk_size(nit);
+  const int base = w0 * G;
+  int c0 = blockIdx.x * w0;
+  int cn = c0 < nit ? min(w0, nit - c0) : 0;
+  int sc = 0;
+  int dpend = -1;  // descriptor buffer with a copy in flight that nobody has waited for
+  if (cn > 0) {
+    if (lane == 0) fetch_descs(0, c0, cn);
+    dpend = 0;
+  }
+  int want = chunk_size(nit - base), tok = 0;
+  bool pend = base < nit;
+  if (pend && lane == 0) tok = atomicAdd(ctr, want);
+  while (cn > 0) {
+    ok = mbar_wait(&m.dbar[sc], (p.dphase >> sc) & 1u) ? 1 : 0;
+    ok = __shfl_sync(0xffffffffu, ok, 0);
+    if (!ok) break;
+    p.dphase ^= 1u << sc;
+    dpend = -1;
+    int n0 = 0, nn = 0, wnext = 0;
+    for (int j = 0; j < cn; ++j) {
+      const MVTItem* d = m.dring + sc * MV_CHMAX + j;
+      const unsigned long long src = d->src;
+      const int bytes = d->bytes, seg0 = d->seg0, nseg = d->nseg, rng0 = d->rng0, nrng = d->nrng;
+      const int inbytes = d->inbytes;
+      const int s = p.it % MV_NSTAGE;
+      // the first use of a stage passes at once (parity of the phase before the first)
+      if (lane == 0) ok = mbar_wait(&m.empty[s], ((p.ephase >> s) & 1u) ^ 1u) ? 1 : 0;
       ok = __shfl_sync(0xffffffffu, ok, 0);
       if (!ok) break;
-      dphase ^= 1u << sc;
-      dpend = -1;
-      int n0 = 0, nn = 0, wnext = 0;
-      for (int j = 0; j < cn && ok; ++j) {
-        const MVTItem* d = dring + sc * MV_CHMAX + j;
-        const unsigned long long src = d->src;
-        const int bytes = d->bytes, seg0 = d->seg0, nseg = d->nseg, rng0 = d->rng0, nrng = d->nrng;
-        const int inbytes = d->inbytes;
-        const int s = it % MV_NSTAGE;
-        // the first use of a stage passes at once (parity of the phase before the first)
-        if (lane == 0) ok = mbar_wait(&empty[s], ((ephase >> s) & 1u) ^ 1u) ? 1 : 0;
-        ok = __shfl_sync(0xffffffffu, ok, 0);
-        if (!ok) break;
-        ephase ^= 1u << s;
-        const int dbytes = nseg * (int)sizeof(MVPiece);
-        if (lane == 0) {
-          hdr[s].nseg = nseg;
-          hdr[s].bytes = bytes;
-          hdr[s].inbytes = inbytes;
-          hdr[s].src = src;
-          asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-          // one arrival carries the transaction bytes of all copies of the item
-          asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(&full[s])),
-                       "r"(bytes + dbytes + (inbytes > 0 ? inbytes : 0)) : "memory");
-          if (bytes > 0)
-            asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
-                         ::"r"(smem_u32(stage + s * MV_STAGE)), "l"((const void*)src), "r"(bytes),
-                         "r"(smem_u32(&full[s])) : "memory");
-          if (dbytes > 0)
-            asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
-                         ::"r"(smem_u32(dstage + s * MV_MAXPC)), "l"((const void*)(a.pieces + seg0)),
-                         "r"(dbytes), "r"(smem_u32(&full[s])) : "memory");
-        }
-        unsigned char* ia = istage + s * MV_INAREA;
-        for (int r = lane; r < nrng; r += 32) {
-          MVRange rg;
-          if (r < 2) rg = MVRange{d->r[4 * r], d->r[4 * r + 1], d->r[4 * r + 2], d->r[4 * r + 3]};
-          else rg = a.ranges[rng0 + r];
-          const unsigned char* gsrc = (const unsigned char*)(rg.src ? a.tx : a.xp) + (size_t)rg.elem * a.in_esz;
+      p.ephase ^= 1u << s;
+      const int dbytes = nseg * (int)sizeof(MVPiece);
+      if (lane == 0) {
+        m.hdr[s].nseg = nseg;
+        m.hdr[s].bytes = bytes;
+        m.hdr[s].inbytes = inbytes;
+        m.hdr[s].src = src;
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        // one arrival carries the transaction bytes of all copies of the item
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(&m.full[s])),
+                     "r"(bytes + dbytes + (inbytes > 0 ? inbytes : 0)) : "memory");
+        if (bytes > 0)
           asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
-                       ::"r"(smem_u32(ia + rg.dst)), "l"((const void*)gsrc), "r"(rg.bytes),
-                       "r"(smem_u32(&full[s])) : "memory");
-        }
-        __syncwarp();
-        ++it;
-        if (pend) {
-          // the claim made a chunk ago: start copying the descriptors of the next chunk
-          pend = false;
-          const int k = base + __shfl_sync(0xffffffffu, tok, 0);
-          n0 = k;
-          nn = k < nit ? min(want, nit - k) : 0;
-          wnext = nit - (k + want);
-          if (nn > 0) {
-            if (lane == 0) fetch_descs(sc ^ 1, n0, nn);
-            dpend = sc ^ 1;
-          }
-        }
+                       ::"r"(smem_u32(m.stage + s * MV_STAGE)), "l"((const void*)src), "r"(bytes),
+                       "r"(smem_u32(&m.full[s])) : "memory");
+        if (dbytes > 0)
+          asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                       ::"r"(smem_u32(m.dstage + s * MV_MAXPC)), "l"((const void*)(a.pieces + seg0)),
+                       "r"(dbytes), "r"(smem_u32(&m.full[s])) : "memory");
       }
-      if (!ok) break;
+      unsigned char* ia = m.istage + s * MV_INAREA;
+      for (int r = lane; r < nrng; r += 32) {
+        MVRange rg;
+        if (r < 2) rg = MVRange{d->r[4 * r], d->r[4 * r + 1], d->r[4 * r + 2], d->r[4 * r + 3]};
+        else rg = a.ranges[rng0 + r];
+        const unsigned char* gsrc = (const unsigned char*)(rg.src ? a.tx : a.xp) + (size_t)rg.elem * a.in_esz;
+        asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                     ::"r"(smem_u32(ia + rg.dst)), "l"((const void*)gsrc), "r"(rg.bytes),
+                     "r"(smem_u32(&m.full[s])) : "memory");
+      }
       __syncwarp();
-      sc ^= 1;
-      c0 = n0;
-      cn = nn;
-      if (cn > 0 && wnext > 0) {
-        want = chunk_size(wnext);
-        pend = true;
-        if (lane == 0) tok = atomicAdd(a.sched, want);
+      ++p.it;
+      if (pend) {
+        // the claim made a chunk ago: start copying the descriptors of the next chunk
+        pend = false;
+        const int k = base + __shfl_sync(0xffffffffu, tok, 0);
+        n0 = k;
+        nn = k < nit ? min(want, nit - k) : 0;
+        wnext = nit - (k + want);
+        if (nn > 0) {
+          if (lane == 0) fetch_descs(sc ^ 1, n0, nn);
+          dpend = sc ^ 1;
+        }
       }
     }
-    if (lane == 0) {
-      if (!ok) atomicOr(a.err, 2);
-      // every issued copy must land before the stop marker reuses a stage
-      uint32_t fphase = 0;
-      for (int j = 0; j < it; ++j) {
-        const int s = j % MV_NSTAGE;
-        if (j >= it - MV_NSTAGE) mbar_wait(&full[s], (fphase >> s) & 1u);
-        fphase ^= 1u << s;
-      }
-      // a descriptor copy still in flight (error path) must land too
-      if (dpend >= 0) mbar_wait(&dbar[dpend], (dphase >> dpend) & 1u);
-      const int s = it % MV_NSTAGE;
-      if (ok && mbar_wait(&empty[s], ((ephase >> s) & 1u) ^ 1u)) {
-        hdr[s].nseg = -1;
-        mbar_arrive(&full[s]);
-      } else {
-        atomicOr(a.err, 2);
-      }
-      // the claims of this CTA are done; the last CTA out resets the counters
-      __threadfence();
-      if (atomicAdd(a.sched + 1, 1) == G - 1) {
-        atomicExch(a.sched, 0);
-        atomicExch(a.sched + 1, 0);
-      }
+    if (!ok) break;
+    __syncwarp();
+    sc ^= 1;
+    c0 = n0;
+    cn = nn;
+    if (cn > 0 && wnext > 0) {
+      want = chunk_size(wnext);
+      pend = true;
+      if (lane == 0) tok = atomicAdd(ctr, want);
     }
-    return;
   }
-  const int cw = warp - 1;
-  uint32_t fphase = 0;
-  int pbase = 0;  // pieces of this CTA's earlier items: warp cw takes pieces with (pbase + q) % C == cw
-  for (int it = 0;; ++it) {
-    const int s = it % MV_NSTAGE;
-    if (!mbar_wait_sleep(&full[s], (fphase >> s) & 1u)) {
-      if (lane == 0) atomicOr(a.err, 2);
-      break;
+  if (lane == 0) {
+    if (!ok) {
+      atomicOr(a.err, 2);
+      // every issued copy must land before shared memory is reused or the CTA exits
+      for (int j = max(it0, p.it - MV_NSTAGE); j < p.it; ++j) {
+        const int s = j % MV_NSTAGE;
+        const uint32_t par = (uint32_t)((j / MV_NSTAGE) & 1);
+        mbar_wait(&m.full[s], par);
+      }
+      if (dpend >= 0) mbar_wait(&m.dbar[dpend], (p.dphase >> dpend) & 1u);
     }
-    fphase ^= 1u << s;
-    const int nseg = hdr[s].nseg;
-    if (nseg < 0) break;
-    const bool sa = hdr[s].bytes > 0, si = hdr[s].inbytes >= 0;
-    int q0 = cw - pbase % MV_CONSUMERS;
+    // stop marker (a wait that times out leaves the consumers to time out on their own)
+    const int s = p.it % MV_NSTAGE;
+    if (mbar_wait(&m.empty[s], ((p.ephase >> s) & 1u) ^ 1u)) {
+      m.hdr[s].nseg = -1;
+      mbar_arrive(&m.full[s]);
+    } else {
+      ok = 0;
+      atomicOr(a.err, 2);
+    }
+  }
+  ++p.it;
+  p.ephase ^= 1u << ((p.it - 1) % MV_NSTAGE);
+  return __shfl_sync(0xffffffffu, ok, 0) != 0;
+}
+
+// One consumer warp (cw = 0 .. MV_CONSUMERS-1): applies its pieces of every item until the
+// stop marker.
+template <class VS, bool COMP>
+__device__ void mv_consume(const MVArgs2& a, const MVSmem& m, MVCons& c, int cw, int lane) {
+  for (;; ++c.it) {
+    const int s = c.it % MV_NSTAGE;
+    if (!mbar_wait_sleep(&m.full[s], (c.fphase >> s) & 1u)) {
+      if (lane == 0) atomicOr(a.err, 2);
+      ++c.it;
+      return;
+    }
+    c.fphase ^= 1u << s;
+    const int nseg = m.hdr[s].nseg;
+    if (nseg < 0) {
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&m.empty[s]);
+      ++c.it;
+      return;
+    }
+    const bool sa = m.hdr[s].bytes > 0, si = m.hdr[s].inbytes >= 0;
+    int q0 = cw - c.pbase % MV_CONSUMERS;  // warp cw takes pieces with (pbase + q) % C == cw
     if (q0 < 0) q0 += MV_CONSUMERS;
-    pbase += nseg;
-    const MVPiece* pcs = dstage + s * MV_MAXPC;
+    c.pbase += nseg;
+    const MVPiece* pcs = m.dstage + s * MV_MAXPC;
     // separate paths so that staged operands are read with shared-memory loads
     using X = typename MT<VS>::X;
-    const unsigned char* sbase = stage + s * MV_STAGE;
-    const unsigned char* ia = istage + s * MV_INAREA;
+    const unsigned char* sbase = m.stage + s * MV_STAGE;
+    const unsigned char* ia = m.istage + s * MV_INAREA;
     if (sa && si) {
       for (int q = q0; q < nseg; q += MV_CONSUMERS) {
         const MVPiece pc = pcs[q];
         run_piece_s<VS, COMP>(a, pc, (const VS*)(sbase + pc.soff), (const X*)(ia + pc.in_soff), lane);
       }
     } else {
-      const unsigned char* gbase = (const unsigned char*)hdr[s].src;
+      const unsigned char* gbase = (const unsigned char*)m.hdr[s].src;
       for (int q = q0; q < nseg; q += MV_CONSUMERS) {
         const MVPiece pc = pcs[q];
         const X* gin = (const X*)((const unsigned char*)((pc.flags & 1) ? a.tx : a.xp) + (size_t)pc.in_off * a.in_esz);
@@ -531,7 +564,125 @@ __global__ void __launch_bounds__(MV_THREADS, 1) mv_tma_kernel(MVArgs2 a) {
       }
     }
     __syncwarp();
-    if (lane == 0) mbar_arrive(&empty[s]);
+    if (lane == 0) mbar_arrive(&m.empty[s]);
+  }
+}
+
+// One pass as its own launch.  The chunk-claim counter a.sched[0] is reset by the last CTA to
+// finish (counter a.sched[1]), which leaves both zero for the next launch on the stream.
+template <class VS, bool COMP>
+__global__ void __launch_bounds__(MV_THREADS, 1) mv_tma_kernel(MVArgs2 a) {
+  extern __shared__ __align__(128) unsigned char smem[];
+  const MVSmem m = mv_smem(smem);
+  mv_init_barriers(m);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (warp == 0) {
+    MVProd p;
+    mv_produce(a, a.items, a.nitems, a.sched, m, p, lane);
+    if (lane == 0) {
+      __threadfence();
+      if (atomicAdd(a.sched + 1, 1) == (int)gridDim.x - 1) {
+        atomicExch(a.sched, 0);
+        atomicExch(a.sched + 1, 0);
+      }
+    }
+    return;
+  }
+  MVCons c;
+  mv_consume<VS, COMP>(a, m, c, warp - 1, lane);
+}
+
+// Grid-wide barrier of a cooperative launch (all CTAs resident).  bar[0] counts arrivals and
+// is zero between barriers; bar[1] is the generation.  A wait that runs past its limit sets
+// the error flag and returns false instead of hanging.
+__device__ bool mv_grid_sync(unsigned* bar, int* err, int* flag) {
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int ok = 1;
+    volatile unsigned* gen = bar + 1;
+    const unsigned g0 = *gen;
+    __threadfence();
+    if (atomicAdd(bar, 1u) == gridDim.x - 1) {
+      atomicExch(bar, 0u);
+      __threadfence();
+      atomicAdd(bar + 1, 1u);
+    } else {
+      int i = 0;
+      while (*gen == g0) {
+        if (++i > (1 << 24)) {
+          ok = 0;
+          atomicOr(err, 4);
+          break;
+        }
+        __nanosleep(32);
+      }
+    }
+    __threadfence();
+    *flag = ok;
+  }
+  __syncthreads();
+  return *flag != 0;
+}
+
+template <class VS, bool COMP>
+__global__ void __launch_bounds__(MV_THREADS, 1) mv_fused_kernel(MVFusedArgs f) {
+  using D = typename MT<VS>::D;
+  using X = typename MT<VS>::X;
+  extern __shared__ __align__(128) unsigned char smem[];
+  __shared__ int bflag;
+  const MVSmem m = mv_smem(smem);
+  mv_init_barriers(m);
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const long long gtid = (long long)blockIdx.x * blockDim.x + tid, gstride = (long long)gridDim.x * blockDim.x;
+  MVArgs2 a = f.a;
+  // prologue: permuted input, zeroed accumulators, zeroed claim counters
+  {
+    const D* x = (const D*)f.x;
+    X* xp = (X*)a.xp;
+    for (long long k = gtid; k < f.n_in; k += gstride) xp[k] = to_x<VS>(x[f.perm_in[k]]);
+    D* yp = (D*)a.yp;
+    for (long long k = gtid; k < f.n_out; k += gstride) yp[k] = D{};
+    D* t = (D*)a.t;
+    for (long long k = gtid; k < f.t_len; k += gstride) t[k] = D{};
+    if (gtid == 0) {
+      *f.ctr[0] = 0;
+      *f.ctr[1] = 0;
+    }
+  }
+  mv_grid_sync(f.bar, a.err, &bflag);
+  MVProd p;
+  MVCons c;
+  for (int ph = 0; ph < 2; ++ph) {
+    if (ph == 1) {
+      // t is complete: its input form for phase B
+      if constexpr (!std::is_same<VS, double>::value && !std::is_same<VS, cpx<double>>::value) {
+        const D* t = (const D*)a.t;
+        X* tx = (X*)a.tx;
+        for (long long k = gtid; k < f.t_len; k += gstride) tx[k] = to_x<VS>(t[k]);
+        mv_grid_sync(f.bar, a.err, &bflag);
+      }
+    }
+    a.items = f.items[ph];
+    a.pieces = f.pieces[ph];
+    a.ranges = f.ranges[ph];
+    a.nitems = f.nitems[ph];
+    if (a.nitems > 0) {
+      if (warp == 0) mv_produce(a, a.items, a.nitems, f.ctr[ph], m, p, lane);
+      else mv_consume<VS, COMP>(a, m, c, warp - 1, lane);
+    }
+    mv_grid_sync(f.bar, a.err, &bflag);
+  }
+  // epilogue: y = alpha yp + beta y in the caller's numbering
+  {
+    const D* yp = (const D*)a.yp;
+    D* y = (D*)f.y;
+    const D al = mk_d<D>(f.alpha[0], f.alpha[1]), be = mk_d<D>(f.beta[0], f.beta[1]);
+    for (long long k = gtid; k < f.n_out; k += gstride) {
+      D* dst = y + f.perm_out[k];
+      D v = al * yp[k];
+      if (f.use_beta) v += be * (*dst);
+      *dst = v;
+    }
   }
 }
 
@@ -605,6 +756,49 @@ void launch_mv_pass(int prec, bool cplx, const MVArgs2& a, int grid, cudaStream_
 }
 
 int mv_stage_bytes() { return MV_STAGE; }
+
+template <class VS, bool COMP>
+static cudaError_t fused_t(const MVFusedArgs& f, cudaStream_t s) {
+  const int smem = mv_smem_bytes();
+  static bool attr = false;
+  if (!attr) {
+    cudaError_t e = cudaFuncSetAttribute(mv_fused_kernel<VS, COMP>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (e != cudaSuccess) return e;
+    attr = true;
+  }
+  int dev = 0, nsm = 0, nb = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, mv_fused_kernel<VS, COMP>, MV_THREADS, smem);
+  if (e != cudaSuccess) return e;
+  if (nb < 1) return cudaErrorCooperativeLaunchTooLarge;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(nsm);  // one CTA per SM, all resident: the grid barriers rely on it
+  cfg.blockDim = dim3(MV_THREADS);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeCooperative;
+  at[0].val.cooperative = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, mv_fused_kernel<VS, COMP>, f);
+}
+
+bool mv_fused_supported() {
+  int dev = 0, coop = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return false;
+  if (cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev) != cudaSuccess || !coop) return false;
+  int optin = 0;
+  cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  return optin >= mv_smem_bytes();
+}
+
+cudaError_t launch_mv_fused(int prec, bool cplx, const MVFusedArgs& f, cudaStream_t s) {
+  if (prec == 0) return cplx ? fused_t<cpx<double>, true>(f, s) : fused_t<double, true>(f, s);
+  if (f.a.compensated) return cplx ? fused_t<cpx<float>, true>(f, s) : fused_t<float, true>(f, s);
+  return cplx ? fused_t<cpx<float>, false>(f, s) : fused_t<float, false>(f, s);
+}
 
 template <class VS>
 __global__ void permute_in_kernel(const int* perm, int n, int nrhs, int ld, const void* xv, void* xpv) {

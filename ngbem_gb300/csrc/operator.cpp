@@ -638,18 +638,23 @@ void HOperator::build_mv_items() {
     p.inv_ow = 1.0f / (float)p.ow;
     return p;
   };
-  const std::vector<GItem>* lists[4][2] = {{&iv, nullptr}, {&id, &iu}, {&iu, nullptr}, {&id, &iv}};
+  // passes 0-3 as above; 4-7 are the phases of the single-launch matvec: 4 = t = V2 x with
+  // y += D x (no dependence on t), 5 = y += U2 t; 6 = t = U2^T x with y += D^T x, 7 = y += V2^T t.
+  // Each list is applied with the piece semantics of pass `sem`.
+  struct LS { const std::vector<GItem>* L; int sem; };
+  const std::vector<LS> lists[MV_NPASS] = {{{&iv, 0}},          {{&id, 1}, {&iu, 1}}, {{&iu, 2}}, {{&id, 3}, {&iv, 3}},
+                                           {{&iv, 0}, {&id, 1}}, {{&iu, 1}},           {{&iu, 2}, {&id, 3}}, {{&iv, 3}}};
   long long npieces = 0;
   const int esz = cplx ? 16 : 8;          // one x or t entry as staged (x: FP32 hi+lo or FP64)
   const int per16 = 16 / esz;             // entries per 16 bytes
   const int inarea = mv_in_bytes();
-  for (int pass = 0; pass < 4; ++pass) {
+  for (int pass = 0; pass < MV_NPASS; ++pass) {
     std::vector<MVTItem> items;
     std::vector<MVPiece> pcs;
     std::vector<MVRange> rngs;
-    for (auto* L : lists[pass]) {
-      if (!L) continue;
-      for (const GItem& gi : *L) {
+    for (const LS& ls : lists[pass]) {
+      const int sem = ls.sem;
+      for (const GItem& gi : *ls.L) {
         MVTItem it{};
         it.src = gi.src;
         it.bytes = gi.bytes;
@@ -661,7 +666,7 @@ void HOperator::build_mv_items() {
         std::vector<Iv> ivs;
         std::vector<int> piv;  // range index of each piece
         for (const GPiece& g : gi.pcs) {
-          const MVPiece p = piece_for(pass, g);
+          const MVPiece p = piece_for(sem, g);
           const int src = p.flags & 1;
           const int e0 = p.in_off, e1 = p.in_off + p.Kc;
           if (!ivs.empty() && ivs.back().src == src && e0 <= ivs.back().e1 + per16 && e1 >= ivs.back().e0 - per16) {
@@ -711,18 +716,23 @@ void HOperator::build_mv_items() {
     d_items[pass].upload(items);
     d_pieces[pass].upload(pcs);
     d_ranges[pass].upload(rngs);
-    info.mv_ranges[pass] = (int)rngs.size();
     n_items[pass] = (int)items.size();
-    info.mv_items[pass] = n_items[pass];
-    npieces += (long long)pcs.size();
+    if (pass < 4) {
+      info.mv_ranges[pass] = (int)rngs.size();
+      info.mv_items[pass] = n_items[pass];
+      npieces += (long long)pcs.size();
+    }
   }
   info.mv_segments = (int)npieces;
   d_mvdense.upload(mvdense);
   d_mvlr.upload(mvlr);
   d_err.alloc(sizeof(int));
   BEM_CUDA(cudaMemset(d_err.p, 0, sizeof(int)));
-  d_sched.alloc(2 * sizeof(int));
-  BEM_CUDA(cudaMemset(d_sched.p, 0, 2 * sizeof(int)));
+  // [0, 1] claim / finish counters of the pass kernels, [2, 3] claim counters of the two phases
+  // of the single-launch matvec, [4, 5] its grid barrier (arrivals, generation)
+  d_sched.alloc(8 * sizeof(int));
+  BEM_CUDA(cudaMemset(d_sched.p, 0, 8 * sizeof(int)));
+  mv_fused = mv_fused_supported();
   int dev = 0, nsm = 152;
   BEM_CUDA(cudaGetDevice(&dev));
   BEM_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
@@ -750,6 +760,51 @@ void HOperator::mult(int trans, const double* alpha, const void* x, const double
   if (profiling) {
     for (auto& e : ev) BEM_CUDA(cudaEventCreate(&e));
     BEM_CUDA(cudaEventRecord(ev[0], s));
+  }
+  if (mv_fused && nrhs == 1) {
+    // one cooperative launch: permute, phase A, t -> input form, phase B, un-permute
+    MVFusedArgs f{};
+    f.a.xp = d_xp.p;
+    f.a.t = d_t.p;
+    f.a.tx = prec == 0 ? d_t.p : d_tx.p;
+    f.a.yp = d_yp.p;
+    f.a.nrhs = 1;
+    f.a.compensated = mv_compensated;
+    f.a.in_esz = cplx ? 16 : 8;
+    f.a.err = d_err.as<int>();
+    const int p0 = trans ? 6 : 4;
+    for (int ph = 0; ph < 2; ++ph) {
+      f.items[ph] = d_items[p0 + ph].as<MVTItem>();
+      f.pieces[ph] = d_pieces[p0 + ph].as<MVPiece>();
+      f.ranges[ph] = d_ranges[p0 + ph].as<MVRange>();
+      f.nitems[ph] = n_items[p0 + ph];
+      f.ctr[ph] = d_sched.as<int>() + 2 + ph;
+    }
+    f.bar = (unsigned*)(d_sched.as<int>() + 4);
+    f.perm_in = pin;
+    f.n_in = in_n;
+    f.x = x;
+    f.perm_out = pout;
+    f.n_out = out_n;
+    f.y = y;
+    f.alpha[0] = alpha[0];
+    f.alpha[1] = alpha[1];
+    f.beta[0] = beta[0];
+    f.beta[1] = beta[1];
+    f.use_beta = (beta[0] != 0.0 || beta[1] != 0.0) ? 1 : 0;
+    f.t_len = t_len;
+    if (profiling) {
+      BEM_CUDA(cudaEventRecord(ev[1], s));
+      BEM_CUDA(cudaEventRecord(ev[2], s));
+    }
+    BEM_CUDA(launch_mv_fused(prec, cplx, f, s));
+    if (profiling) {
+      BEM_CUDA(cudaEventRecord(ev[3], s));
+      BEM_CUDA(cudaEventRecord(ev[4], s));
+      pending.push_back(ev);
+      pending_fused.push_back(true);
+    }
+    return;
   }
   launch_permute_in(prec, cplx, pin, in_n, nrhs, in_n, x, d_xp.p, s);
   BEM_CUDA(cudaMemsetAsync(d_yp.p, 0, (size_t)out_n * nrhs * dsz, s));
@@ -786,6 +841,7 @@ void HOperator::mult(int trans, const double* alpha, const void* x, const double
   if (profiling) {
     BEM_CUDA(cudaEventRecord(ev[4], s));
     pending.push_back(ev);
+    pending_fused.push_back(false);
   }
   BEM_CUDA(cudaGetLastError());
 }
@@ -797,9 +853,11 @@ int HOperator::device_status() {
 }
 
 void HOperator::collect_profile() {
-  for (auto& ev : pending) {
+  for (size_t i = 0; i < pending.size(); ++i) {
+    auto& ev = pending[i];
     BEM_CUDA(cudaEventSynchronize(ev[4]));
     for (int k = 0; k < 4; ++k) {
+      if (pending_fused[i] && k != 2) continue;  // one launch: its time is the apply slot
       float t = 0.f;
       BEM_CUDA(cudaEventElapsedTime(&t, ev[k], ev[k + 1]));
       kms[k] += t;
@@ -808,6 +866,7 @@ void HOperator::collect_profile() {
     for (auto& e : ev) cudaEventDestroy(e);
   }
   pending.clear();
+  pending_fused.clear();
 }
 
 HOperator::~HOperator() {
