@@ -142,6 +142,7 @@ cudaError_t launch_mv_fused(int prec, bool cplx, const MVFusedArgs& f, cudaStrea
 // prec 0: fp64 storage, 1: fp32 storage.  cplx: complex operator.
 void launch_mv_pass(int prec, bool cplx, const MVArgs2& a, int grid, cudaStream_t s);
 int mv_stage_bytes();
+int mv_piece_elems();  // target stored elements per piece
 // tx = t in the input form (no-op for fp64 storage, where tx aliases t)
 void launch_t_to_x(int prec, bool cplx, const void* t, void* tx, long long n, cudaStream_t s);
 int mv_max_pieces();   // pieces per work item (descriptors staged with the payload)

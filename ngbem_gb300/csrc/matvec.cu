@@ -195,13 +195,26 @@ template <> struct Acc<cpx<double>> {
   __device__ __forceinline__ cpx<double> val() const { return a; }
 };
 
+// pipeline shape: MV_NSTAGE stages, each with MV_STAGE payload bytes, MV_MAXPC piece
+// descriptors and MV_INAREA bytes of staged inputs (all within one SM's shared memory)
+#ifndef MV_STAGE
 #define MV_STAGE 32768
-#define MV_NSTAGE 4
+#endif
+#ifndef MV_PIECE
+#define MV_PIECE 512  // target stored elements per piece (one consumer warp's task)
+#endif
+#ifndef MV_NSTAGE
+#define MV_NSTAGE 5
+#endif
 #define MV_THREADS 1024
 #define MV_CONSUMERS (MV_THREADS / 32 - 1)
 #define MV_INBUF 128
-#define MV_MAXPC 128
-#define MV_INAREA 16384
+#ifndef MV_MAXPC
+#define MV_MAXPC 32
+#endif
+#ifndef MV_INAREA
+#define MV_INAREA 8192
+#endif
 #define MV_CHMAX 8   // items per claimed chunk, at most
 #define MV_HDR (128 + MV_NSTAGE * 32 + 2 * MV_CHMAX * 80)
 
@@ -756,6 +769,7 @@ void launch_mv_pass(int prec, bool cplx, const MVArgs2& a, int grid, cudaStream_
 }
 
 int mv_stage_bytes() { return MV_STAGE; }
+int mv_piece_elems() { return MV_PIECE; }
 
 template <class VS, bool COMP>
 static cudaError_t fused_t(const MVFusedArgs& f, cudaStream_t s) {

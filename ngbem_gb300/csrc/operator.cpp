@@ -534,7 +534,7 @@ bool pairs_overflow(size_t ntiles) { return ntiles > (size_t)INT_MAX; }
 // matvec stage: consecutive segments whose bytes are contiguous share one bulk copy.
 void HOperator::build_mv_items() {
   const size_t stage = (size_t)mv_stage_bytes();
-  const int piece = 512;  // target elements per piece (one consumer warp's task)
+  const int piece = mv_piece_elems();  // target elements per piece (one consumer warp's task)
   // A span is one contiguous payload range (a block, or a chunk of one) with its generic
   // pieces (kind, block, first row/col, count, byte offset from the span start).
   struct GPiece { int kind, blk, k0, cnt, soff; };
@@ -661,32 +661,66 @@ void HOperator::build_mv_items() {
         it.seg0 = (int)pcs.size();
         it.nseg = (int)gi.pcs.size();
         it.rng0 = (int)rngs.size();
-        // input intervals of the pieces, merged into 16-byte aligned ranges of x or t
+        // input intervals of the pieces, merged into 16-byte aligned ranges of x or t.  Nearby
+        // ranges are merged further (smallest gap first) while the staged bytes still fit the
+        // input area: the producer issues the first two ranges from the descriptor and has to
+        // load the others, so staging a few unused entries of x or t (L2 resident) is cheaper.
         struct Iv { int src, e0, e1; };
-        std::vector<Iv> ivs;
-        std::vector<int> piv;  // range index of each piece
+        std::vector<Iv> raw;
         for (const GPiece& g : gi.pcs) {
           const MVPiece p = piece_for(sem, g);
-          const int src = p.flags & 1;
-          const int e0 = p.in_off, e1 = p.in_off + p.Kc;
-          if (!ivs.empty() && ivs.back().src == src && e0 <= ivs.back().e1 + per16 && e1 >= ivs.back().e0 - per16) {
-            ivs.back().e0 = std::min(ivs.back().e0, e0);
-            ivs.back().e1 = std::max(ivs.back().e1, e1);
-          } else {
-            ivs.push_back({src, e0, e1});
-          }
-          piv.push_back((int)ivs.size() - 1);
+          raw.push_back({p.flags & 1, p.in_off, p.in_off + p.Kc});
           pcs.push_back(p);
+        }
+        std::vector<Iv> ivs = raw;
+        for (Iv& v : ivs) {
+          v.e0 = v.e0 / per16 * per16;
+          v.e1 = (v.e1 + per16 - 1) / per16 * per16;
+        }
+        std::sort(ivs.begin(), ivs.end(), [](const Iv& x, const Iv& y) {
+          return x.src != y.src ? x.src < y.src : x.e0 < y.e0;
+        });
+        {
+          std::vector<Iv> m;
+          for (const Iv& v : ivs) {
+            if (!m.empty() && m.back().src == v.src && v.e0 <= m.back().e1) m.back().e1 = std::max(m.back().e1, v.e1);
+            else m.push_back(v);
+          }
+          ivs.swap(m);
+        }
+        auto staged = [&]() {
+          long long b = 0;
+          for (const Iv& v : ivs) b += (long long)(v.e1 - v.e0) * esz;
+          return b;
+        };
+        long long tot = staged();
+        while (ivs.size() > 2) {
+          int best = -1;
+          long long gap = 0;
+          for (size_t r = 0; r + 1 < ivs.size(); ++r) {
+            if (ivs[r].src != ivs[r + 1].src) continue;
+            const long long g2 = (long long)(ivs[r + 1].e0 - ivs[r].e1) * esz;
+            if (best < 0 || g2 < gap) {
+              best = (int)r;
+              gap = g2;
+            }
+          }
+          if (best < 0 || tot + gap > inarea) break;
+          ivs[best].e1 = ivs[best + 1].e1;
+          ivs.erase(ivs.begin() + best + 1);
+          tot += gap;
+        }
+        std::vector<int> piv;  // range index of each piece
+        for (const Iv& v : raw) {
+          int r = 0;
+          while (!(ivs[r].src == v.src && ivs[r].e0 <= v.e0 && v.e1 <= ivs[r].e1)) ++r;
+          piv.push_back(r);
         }
         std::vector<int> dst(ivs.size());
         int total = 0;
         for (size_t r = 0; r < ivs.size(); ++r) {
-          const int a0 = ivs[r].e0 / per16 * per16;
-          const int a1 = (ivs[r].e1 + per16 - 1) / per16 * per16;
-          ivs[r].e0 = a0;
-          ivs[r].e1 = a1;
           dst[r] = total;
-          total += (a1 - a0) * esz;
+          total += (ivs[r].e1 - ivs[r].e0) * esz;
         }
         if (total <= inarea) {
           for (size_t r = 0; r < ivs.size(); ++r) {
