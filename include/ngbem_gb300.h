@@ -44,6 +44,7 @@ enum { BEM_METHOD_ACA = 0, BEM_METHOD_DENSE = 1 };
 typedef struct bem_mesh_s* bem_mesh_t;
 typedef struct bem_space_s* bem_space_t;
 typedef struct bem_operator_s* bem_operator_t;
+typedef struct bem_slbatch_s* bem_slbatch_t;
 
 /* BEMParameters (reference src/ngbem.hpp:13-27) plus the GB300 extensions. */
 typedef struct {
@@ -156,6 +157,31 @@ int bem_operator_mult_host(bem_operator_t op, int trans, const double* alpha, co
 int bem_operator_to_dense(bem_operator_t op, void* out);
 
 int bem_operator_destroy(bem_operator_t op);
+
+/* ---- Batched single-layer energy and shape gradient (no counterpart in the reference, which
+ * has no derivatives; the energy u^T V(X) u is what u^T (SingleLayerPotentialOperator(...).mat
+ * * u) gives for a P0 space, src/python_bem.cpp:27-40 and src/ngbem.cpp:373-738).
+ * Topology of nprob closed triangle meshes: nverts[b], ntris[b], tris = concatenated triangles
+ * (3 vertex ids local to their mesh).  Quadrature: tensor triangle rule of order
+ * intorder_regular (0..5) on pairs sharing no vertex, Sauter-Schwab rules of order
+ * intorder_singular on the others, as the dense near-field assembly uses them.
+ * precision: BEM_FP64 (all FP64) or BEM_MIXED (regular pairs in FP32 with hi+lo centroid
+ * differences, singular pairs FP64).  dual_mapping: the P0 basis 1/|J|. */
+int bem_sl_batch_create(int nprob, const int* nverts, const int* ntris, const int* tris, int intorder_regular,
+                        int intorder_singular, int precision, int dual_mapping, bem_slbatch_t* out);
+
+/* One evaluation on the device (stream-ordered).  X: 3 * sum(nverts) coordinates (problems
+ * concatenated), u: sum(ntris) densities.  Outputs (device, overwritten; any may be NULL):
+ * energy[nprob] = u_b^T V(X_b) u_b, vu[sum ntris] = V(X_b) u_b, grad[3 * sum nverts] =
+ * weights[b] * dE_b/dX (weights NULL: 1).  grad = NULL skips the derivative kernels.  The
+ * derivative is exact for the discrete energy (the rule moves with the mesh). */
+int bem_sl_batch_eval(bem_slbatch_t batch, const double* X, const double* u, const double* weights,
+                      double* energy, double* vu, double* grad, void* stream);
+
+/* nunits: regular work units, nsing: singular element pairs, npairs_regular: regular pairs. */
+int bem_sl_batch_info(bem_slbatch_t batch, int* nunits, int* nsing, long long* npairs_regular);
+
+int bem_sl_batch_destroy(bem_slbatch_t batch);
 
 /* Arithmetic of the matvec for FP32-stored operators (no counterpart in the reference, which is
  * FP64 throughout): compensated = 1 (default) forms every product and sum error-free (x split

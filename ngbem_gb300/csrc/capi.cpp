@@ -301,6 +301,39 @@ int bem_operator_destroy(bem_operator_t op) {
   return guarded([&] { delete op; });
 }
 
+int bem_sl_batch_create(int nprob, const int* nverts, const int* ntris, const int* tris, int intorder_regular,
+                        int intorder_singular, int precision, int dual_mapping, bem_slbatch_t* out) {
+  return guarded([&] {
+    REQUIRE(nverts && ntris && tris && out, "null argument");
+    REQUIRE(precision == BEM_FP64 || precision == BEM_MIXED, "unknown precision");
+    auto b = std::make_unique<bem_slbatch_s>();
+    b->b.build(nprob, nverts, ntris, tris, intorder_regular, intorder_singular, precision == BEM_FP64 ? 0 : 1,
+               dual_mapping ? 1 : 0);
+    *out = b.release();
+  });
+}
+
+int bem_sl_batch_eval(bem_slbatch_t batch, const double* X, const double* u, const double* weights, double* energy,
+                      double* vu, double* grad, void* stream) {
+  return guarded([&] {
+    REQUIRE(batch && X && u, "null argument");
+    batch->b.eval(X, u, weights, energy, vu, grad, (cudaStream_t)stream);
+  });
+}
+
+int bem_sl_batch_info(bem_slbatch_t batch, int* nunits, int* nsing, long long* npairs_regular) {
+  return guarded([&] {
+    REQUIRE(batch, "null argument");
+    if (nunits) *nunits = batch->b.nunits;
+    if (nsing) *nsing = batch->b.nsing;
+    if (npairs_regular) *npairs_regular = batch->b.npairs_regular;
+  });
+}
+
+int bem_sl_batch_destroy(bem_slbatch_t batch) {
+  return guarded([&] { delete batch; });
+}
+
 int bem_gmres(int nterms, const bem_operator_t* ops, const double* coef, const void* b, void* x, int maxiter,
               int restart, double tol, int* iters, double* resid, void* stream) {
   return guarded([&] {

@@ -201,6 +201,22 @@ struct MassOperator : OperatorBase {
             cudaStream_t s) override;
 };
 
+// Batched single-layer energy (energy_host.cpp / energy.cu): element topology of a batch of
+// closed meshes, built once; eval() takes new coordinates and densities each call.
+struct SLBatch {
+  int nprob = 0, ntri = 0, nvert = 0, nq = 0, prec = 0, dual = 0;
+  int nunits = 0, nsing = 0;
+  long long npairs_regular = 0;
+  double rxi[16] = {}, reta[16] = {}, rw[16] = {};
+  int ss_n[3] = {0, 0, 0};
+  DevBuf d_tri, d_tprob, d_t0, d_nt, d_units, d_sing, d_ss[3];
+  DevBuf d_D, d_dD, d_cf, d_off, d_q64, scratch_out;
+  void build(int nprob, const int* nverts, const int* ntris, const int* tris, int order_reg, int order_sing, int prec,
+             int dual);
+  void eval(const double* X, const double* u, const double* wprob, double* energy, double* vu, double* grad,
+            cudaStream_t s);
+};
+
 // op.mult with the scratch taken from a fixed device array instead of operator buffers
 // (mult_noalloc.cu); allocates nothing.
 void mult_noalloc(HOperator& op, int trans, const double* alpha, const void* x, const double* beta, void* y,
@@ -221,4 +237,7 @@ struct bem_space_s {
 };
 struct bem_operator_s {
   std::unique_ptr<bem::OperatorBase> op;
+};
+struct bem_slbatch_s {
+  bem::SLBatch b;
 };

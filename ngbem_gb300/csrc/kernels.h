@@ -139,6 +139,37 @@ struct MVFusedArgs {
 bool mv_fused_supported();
 cudaError_t launch_mv_fused(int prec, bool cplx, const MVFusedArgs& f, cudaStream_t s);
 
+// Batched single-layer energy E_b = u_b^T V(X_b) u_b, V u and dE/dX (energy.cu)
+struct SLEArgs {
+  const double* X;        // 3 * nv_total vertex coordinates
+  const int4* tri;        // global vertex ids per element
+  const double* u;        // P0 densities, one per element
+  const double* wprob;    // per-problem factor of the gradient (or null: 1)
+  const int* tprob;       // problem of each element
+  const int* t0;          // first element of each problem
+  const int* nt;          // elements of each problem
+  int ntri, dual, nq;
+  double rxi[16], reta[16], rw[16];  // regular triangle rule (reference vertices (1,0),(0,1),(0,0))
+  // per-element scratch written by the prep kernel
+  double* D;              // |J| (1 with the dual mapping)
+  double* dD;             // 9 per element: dD/dP_a
+  float* cf;              // 6 per element: centroid hi, lo
+  float* off;             // nq*3 per element: quadrature points - centroid (float)
+  double* q64;            // nq*3 per element: quadrature points
+  const int4* units;      // (problem, first test element, first trial element, -)
+  int nunits;
+  const int2* sing;       // ordered element pairs sharing a vertex (global element ids)
+  int nsing;
+  const double* ss[3];    // Sauter-Schwab tables x0, x1, y0, y1, w (identical, edge, vertex)
+  int ss_n[3];
+  double* energy;         // nprob (accumulated)
+  double* vu;             // ntri (accumulated)
+  double* grad;           // 3 * nv_total (accumulated; only with the gradient)
+};
+int sle_tile_test();
+int sle_tile_trial(bool fp64, int nq);
+void launch_sle(const SLEArgs& a, bool fp64, bool grad, cudaStream_t s);
+
 // prec 0: fp64 storage, 1: fp32 storage.  cplx: complex operator.
 void launch_mv_pass(int prec, bool cplx, const MVArgs2& a, int grid, cudaStream_t s);
 int mv_stage_bytes();
