@@ -94,6 +94,15 @@ __global__ void sle_prep_kernel(SLEArgs a) {
   }
 }
 
+// 1/sqrt(x) for x > 0 in FP64: the FP32 hardware estimate refined by one Newton-Raphson step
+// for f(y) = 1/y^2 - x (y <- y (3 - x y^2) / 2), which squares the relative error of the
+// estimate (about 1e-7) to about 1e-14 -- far below the quadrature error -- for a handful of
+// FP64 operations instead of a full-precision FP64 reciprocal square root.
+__device__ __forceinline__ double rsqrt_nr(double x) {
+  const double y = (double)rsqrtf((float)x);
+  return y * fma(-0.5 * x, y * y, 1.5);
+}
+
 template <class R> __device__ __forceinline__ R rsq(R x);
 template <> __device__ __forceinline__ float rsq<float>(float x) { return rsqrtf(x); }
 template <> __device__ __forceinline__ double rsq<double>(double x) { return rsqrt(x); }
@@ -238,9 +247,33 @@ __global__ void __launch_bounds__(SLE_TI) sle_regular_kernel(SLEArgs a) {
 }
 
 // Singular pairs (sharing a vertex, an edge or identical): one warp per ordered pair, FP64
-// Sauter-Schwab rules with the vertex permutations of the near-field kernel.
+// Sauter-Schwab rules.  The tables hold one point per Duffy direction (xi = 1): 1/|d| is
+// homogeneous of degree -1 and the points of a direction are xi times its xi = 1 point, so the
+// radial sum is ss_c2 times the direction's term (ss_c1 for the degree -2 gradient moment M,
+// ss_c2 for the moments that carry one more factor xi through s_k or t_k).  The vertices are permuted once per pair so that the rule's barycentric
+// coordinates (1 - s0 - s1, s0, s1) belong to (P'0, P'1, P'2) -- the same assignment as the
+// near-field kernel's vertex permutations -- and P'0 is the common vertex (identical pairs:
+// P'0 = P2).  Then d = x - y = s0 E1 + s1 E2 - t0 F1 - t1 F2 with edge vectors from P'0, and the
+// position derivative needs only the moments M = sum w h d, sum s_k w h d, sum t_k w h d
+// (h = 1/|d|^3), mapped back to the three vertices once per pair.
 template <bool GRAD>
 __global__ void __launch_bounds__(256) sle_singular_kernel(SLEArgs a) {
+  extern __shared__ double s_tab[];
+  const double* tab[3];
+  {
+    int off = 0;
+    for (int c = 0; c < 3; ++c) {
+      const int n5 = 5 * a.ss_n[c];
+      if (a.ss_smem) {
+        for (int t = threadIdx.x; t < n5; t += blockDim.x) s_tab[off + t] = a.ss[c][t];
+        tab[c] = s_tab + off;
+      } else {
+        tab[c] = a.ss[c];
+      }
+      off += n5;
+    }
+    __syncthreads();
+  }
   const int lane = threadIdx.x & 31;
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int nwarps = (gridDim.x * blockDim.x) >> 5;
@@ -255,8 +288,9 @@ __global__ void __launch_bounds__(256) sle_singular_kernel(SLEArgs a) {
 #pragma unroll
       for (int q = 0; q < 3; ++q) ncommon += (vi[p] == vj[q]);
     const int cls = ncommon == 3 ? 0 : (ncommon == 2 ? 1 : 2);
-    int px[3] = {0, 1, 2}, py[3] = {0, 1, 2};
+    int px[3] = {2, 0, 1}, py[3] = {2, 0, 1};
     if (cls == 1) {
+      // edge table (0,1) | (1,2) | (2,0); the common edge comes first, reversed in y
       int cex = 0, cey = 0;
       for (int cx = 0; cx < 3; ++cx)
         for (int cy = 0; cy < 3; ++cy) {
@@ -273,80 +307,95 @@ __global__ void __launch_bounds__(256) sle_singular_kernel(SLEArgs a) {
       px[0] = cvx; px[1] = (cvx + 1) % 3; px[2] = (cvx + 2) % 3;
       py[0] = cvy; py[1] = (cvy + 1) % 3; py[2] = (cvy + 2) % 3;
     }
-    double Pi[3][3], Pj[3][3];
+    int gi[3], gj[3];  // global vertex ids in permuted order
 #pragma unroll
-    for (int v = 0; v < 3; ++v)
+    for (int k = 0; k < 3; ++k) {
+      gi[k] = px[k] == 0 ? vi[0] : (px[k] == 1 ? vi[1] : vi[2]);
+      gj[k] = py[k] == 0 ? vj[0] : (py[k] == 1 ? vj[1] : vj[2]);
+    }
+    double E1[3], E2[3], F1[3], F2[3];
 #pragma unroll
-      for (int c = 0; c < 3; ++c) {
-        Pi[v][c] = a.X[3 * vi[v] + c];
-        Pj[v][c] = a.X[3 * vj[v] + c];
-      }
+    for (int c = 0; c < 3; ++c) {
+      const double pi0 = a.X[3 * gi[0] + c], pj0 = a.X[3 * gj[0] + c];
+      E1[c] = a.X[3 * gi[1] + c] - pi0;
+      E2[c] = a.X[3 * gi[2] + c] - pi0;
+      F1[c] = a.X[3 * gj[1] + c] - pj0;
+      F2[c] = a.X[3 * gj[2] + c] - pj0;
+    }
     const int npts = a.ss_n[cls];
-    const double* T = a.ss[cls];
-    double S = 0.0, Bx[3][3], By[3][3];
-#pragma unroll
-    for (int v = 0; v < 3; ++v)
-#pragma unroll
-      for (int c = 0; c < 3; ++c) Bx[v][c] = By[v][c] = 0.0;
+    const double* T = tab[cls];
+    double S = 0.0, M[3] = {0, 0, 0}, Ms0[3] = {0, 0, 0}, Ms1[3] = {0, 0, 0}, Mt0[3] = {0, 0, 0},
+           Mt1[3] = {0, 0, 0};
     for (int k = lane; k < npts; k += 32) {
-      const double x0 = T[k], x1 = T[npts + k], y0 = T[2 * npts + k], y1 = T[3 * npts + k], w = T[4 * npts + k];
-      double lx[3], ly[3];
-      if (cls == 0) {
-        lx[0] = x0; lx[1] = x1; lx[2] = 1.0 - x0 - x1;
-        ly[0] = y0; ly[1] = y1; ly[2] = 1.0 - y0 - y1;
-      } else {
-        const double bx[3] = {1.0 - x0 - x1, x0, x1}, by[3] = {1.0 - y0 - y1, y0, y1};
-#pragma unroll
-        for (int q = 0; q < 3; ++q) { lx[px[q]] = bx[q]; ly[py[q]] = by[q]; }
-        lx[2] = 1.0 - lx[0] - lx[1];
-        ly[2] = 1.0 - ly[0] - ly[1];
-      }
+      const double s0 = T[k], s1 = T[npts + k], t0 = T[2 * npts + k], t1 = T[3 * npts + k], w = T[4 * npts + k];
       double d[3];
+      if (cls == 0) {
+        const double u0 = s0 - t0, u1 = s1 - t1;
 #pragma unroll
-      for (int c = 0; c < 3; ++c)
-        d[c] = (lx[0] * Pi[0][c] + lx[1] * Pi[1][c] + lx[2] * Pi[2][c]) -
-               (ly[0] * Pj[0][c] + ly[1] * Pj[1][c] + ly[2] * Pj[2][c]);
-      const double rinv = rsqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+        for (int c = 0; c < 3; ++c) d[c] = u0 * E1[c] + u1 * E2[c];
+      } else {
+#pragma unroll
+        for (int c = 0; c < 3; ++c) d[c] = (s0 * E1[c] + s1 * E2[c]) - (t0 * F1[c] + t1 * F2[c]);
+      }
+      const double rinv = rsqrt_nr(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
       const double g = w * rinv;
       S += g;
       if (GRAD) {
         const double h = g * rinv * rinv;
 #pragma unroll
-        for (int v = 0; v < 3; ++v)
-#pragma unroll
-          for (int c = 0; c < 3; ++c) {
-            Bx[v][c] += lx[v] * h * d[c];
-            By[v][c] += ly[v] * h * d[c];
-          }
+        for (int c = 0; c < 3; ++c) {
+          const double hd = h * d[c];
+          M[c] += hd;
+          Ms0[c] += s0 * hd;
+          Ms1[c] += s1 * hd;
+          Mt0[c] += t0 * hd;
+          Mt1[c] += t1 * hd;
+        }
       }
     }
     S = warp_sum(S);
     if (GRAD) {
 #pragma unroll
-      for (int v = 0; v < 3; ++v)
-#pragma unroll
-        for (int c = 0; c < 3; ++c) {
-          Bx[v][c] = warp_sum(Bx[v][c]);
-          By[v][c] = warp_sum(By[v][c]);
-        }
+      for (int c = 0; c < 3; ++c) {
+        M[c] = warp_sum(M[c]);
+        Ms0[c] = warp_sum(Ms0[c]);
+        Ms1[c] = warp_sum(Ms1[c]);
+        Mt0[c] = warp_sum(Mt0[c]);
+        Mt1[c] = warp_sum(Mt1[c]);
+      }
     }
     if (lane == 0) {
+      S *= a.ss_c2;
+      if (GRAD) {
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+          M[c] *= a.ss_c1;
+          Ms0[c] *= a.ss_c2;
+          Ms1[c] *= a.ss_c2;
+          Mt0[c] *= a.ss_c2;
+          Mt1[c] *= a.ss_c2;
+        }
+      }
       const int b = a.tprob[pr.x];
       const double Di = a.D[pr.x], Dj = a.D[pr.y], ui = a.u[pr.x], uj = a.u[pr.y];
       const double v = Di * Dj * S * inv4pi;
       atomicAdd(&a.vu[pr.x], uj * v);
       atomicAdd(&a.energy[b], ui * uj * v);
       if (GRAD) {
-        const double c0 = ui * uj * (a.wprob ? a.wprob[b] : 1.0) * inv4pi;
+        const double c0 = ui * uj * (a.wprob ? a.wprob[b] : 1.0) * inv4pi, DD = Di * Dj;
         const double* dDi = a.dD + 9 * (size_t)pr.x;
         const double* dDj = a.dD + 9 * (size_t)pr.y;
 #pragma unroll
-        for (int w = 0; w < 3; ++w)
+        for (int c = 0; c < 3; ++c) {
+          // sum w lambda'_k h d for the permuted vertices: lambda' = (1 - s0 - s1, s0, s1)
+          const double bx[3] = {M[c] - Ms0[c] - Ms1[c], Ms0[c], Ms1[c]};
+          const double by[3] = {M[c] - Mt0[c] - Mt1[c], Mt0[c], Mt1[c]};
 #pragma unroll
-          for (int c = 0; c < 3; ++c) {
-            atomicAdd(&a.grad[3 * (size_t)vi[w] + c], c0 * (Dj * dDi[3 * w + c] * S - Di * Dj * Bx[w][c]));
-            atomicAdd(&a.grad[3 * (size_t)vj[w] + c], c0 * (Di * dDj[3 * w + c] * S + Di * Dj * By[w][c]));
+          for (int k = 0; k < 3; ++k) {
+            atomicAdd(&a.grad[3 * (size_t)gi[k] + c], c0 * (Dj * dDi[3 * px[k] + c] * S - DD * bx[k]));
+            atomicAdd(&a.grad[3 * (size_t)gj[k] + c], c0 * (Di * dDj[3 * py[k] + c] * S + DD * by[k]));
           }
+        }
       }
     }
   }
@@ -381,9 +430,10 @@ void launch_sle(const SLEArgs& a, bool fp64, bool grad, cudaStream_t s) {
     }
   }
   if (a.nsing > 0) {
-    const int grid = std::min((a.nsing + 7) / 8, nsm * 16);
-    if (grad) sle_singular_kernel<true><<<grid, 256, 0, s>>>(a);
-    else sle_singular_kernel<false><<<grid, 256, 0, s>>>(a);
+    const int grid = std::min((a.nsing + 7) / 8, nsm * 8);
+    const int smem = a.ss_smem ? 40 * (a.ss_n[0] + a.ss_n[1] + a.ss_n[2]) : 0;
+    if (grad) sle_singular_kernel<true><<<grid, 256, smem, s>>>(a);
+    else sle_singular_kernel<false><<<grid, 256, smem, s>>>(a);
   }
 }
 

@@ -69,8 +69,11 @@ void SLBatch::build(int nprob_, const int* nverts, const int* ntris, const int* 
     rw[q] = r.w[q];
   }
   for (int c = 0; c < 3; ++c) {
-    SSRule s = make_ss_rule(c, order_sing);
+    // one point per direction (the Laplace kernel's homogeneity sums the radial points)
+    SSRule s = make_ss_rule(c, order_sing, true);
     ss_n[c] = (int)s.w.size();
+    ss_c1 = s.c1;
+    ss_c2 = s.c2;
     std::vector<double> tab;
     tab.insert(tab.end(), s.x0.begin(), s.x0.end());
     tab.insert(tab.end(), s.x1.begin(), s.x1.end());
@@ -139,6 +142,9 @@ void SLBatch::eval(const double* X, const double* u, const double* wprob, double
     a.ss[c] = d_ss[c].as<double>();
     a.ss_n[c] = ss_n[c];
   }
+  a.ss_smem = 40 * (ss_n[0] + ss_n[1] + ss_n[2]) <= 48 * 1024 ? 1 : 0;
+  a.ss_c1 = ss_c1;
+  a.ss_c2 = ss_c2;
   a.energy = energy;
   a.vu = vu;
   a.grad = grad;

@@ -67,8 +67,14 @@ struct DevBuf {
 void sym_eigen(int n, std::vector<double> A, std::vector<double>& evals, std::vector<double>& evecs);
 struct TrigRule { std::vector<double> xi, eta, w; };
 TrigRule make_trig_rule(int order);
-struct SSRule { std::vector<double> x0, x1, y0, y1, w; };
-SSRule make_ss_rule(int cls, int order);
+// Sauter-Schwab rule of a singularity class (0 identical, 1 common edge, 2 common vertex).
+// Every point is xi * (a, b, c, d) for a direction (a, b, c, d) and a Gauss point xi in (0, 1),
+// with weight xi^3 w_dir w_xi.  radial = true returns one point per direction at xi = 1 with
+// weight w_dir, and c1 = sum w_xi xi, c2 = sum w_xi xi^2: for an integrand homogeneous of
+// degree -1 in x - y (1/|x - y|) the sum over xi of a direction is c2 times the xi = 1 term,
+// and for degree -2 (grad 1/|x - y|) c1 times it.
+struct SSRule { std::vector<double> x0, x1, y0, y1, w; double c1 = 0.0, c2 = 0.0; };
+SSRule make_ss_rule(int cls, int order, bool radial = false);
 
 // ---- mesh and spaces (geometry.cpp) -----------------------------------------------------
 struct MeshH {
@@ -209,6 +215,7 @@ struct SLBatch {
   long long npairs_regular = 0;
   double rxi[16] = {}, reta[16] = {}, rw[16] = {};
   int ss_n[3] = {0, 0, 0};
+  double ss_c1 = 0.0, ss_c2 = 0.0;
   DevBuf d_tri, d_tprob, d_t0, d_nt, d_units, d_sing, d_ss[3];
   DevBuf d_D, d_dD, d_cf, d_off, d_q64, scratch_out;
   void build(int nprob, const int* nverts, const int* ntris, const int* tris, int order_reg, int order_sing, int prec,

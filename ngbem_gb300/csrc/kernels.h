@@ -160,8 +160,10 @@ struct SLEArgs {
   int nunits;
   const int2* sing;       // ordered element pairs sharing a vertex (global element ids)
   int nsing;
-  const double* ss[3];    // Sauter-Schwab tables x0, x1, y0, y1, w (identical, edge, vertex)
+  const double* ss[3];    // Sauter-Schwab directions x0, x1, y0, y1, w at xi = 1 (identical, edge, vertex)
   int ss_n[3];
+  double ss_c1, ss_c2;    // sum over the radial Gauss points of w_xi xi and w_xi xi^2
+  int ss_smem;            // 1: stage the three tables in shared memory (they fit 48 KB)
   double* energy;         // nprob (accumulated)
   double* vu;             // ntri (accumulated)
   double* grad;           // 3 * nv_total (accumulated; only with the gradient)

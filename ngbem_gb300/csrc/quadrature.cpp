@@ -117,11 +117,15 @@ TrigRule make_trig_rule(int order) {
   return r;
 }
 
-SSRule make_ss_rule(int cls, int order) {
+SSRule make_ss_rule(int cls, int order, bool radial) {
   std::vector<double> s, ws;
   gauss_jacobi_unit(order / 2 + 1, 0.0, 0.0, s, ws);
   const int n = (int)s.size();
   SSRule r;
+  for (int ix = 0; ix < n; ++ix) {
+    r.c1 += ws[ix] * s[ix];
+    r.c2 += ws[ix] * s[ix] * s[ix];
+  }
   auto add = [&](double xi, double a, double b, double c, double d, double w) {
     const double p0 = xi * a, p1 = xi * b, p2 = xi * c, p3 = xi * d;
     r.x0.push_back(p0 - p1);
@@ -135,9 +139,10 @@ SSRule make_ss_rule(int cls, int order) {
       for (int i3 = 0; i3 < n; ++i3) {
         const double e1 = s[i1], e2 = s[i2], e3 = s[i3];
         const double whex = ws[i1] * ws[i2] * ws[i3];
-        for (int ix = 0; ix < n; ++ix) {
-          const double xi = s[ix];
-          const double wb = whex * ws[ix];
+        for (int ix = 0; ix < (radial ? 1 : n); ++ix) {
+          // radial: one point per direction at xi = 1, weight without xi^3 and the xi weight
+          const double xi = radial ? 1.0 : s[ix];
+          const double wb = radial ? whex : whex * ws[ix];
           const double x3 = xi * xi * xi;
           if (cls == 0) {
             const double w = x3 * e1 * e1 * e2 * wb;
