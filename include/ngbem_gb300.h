@@ -207,6 +207,14 @@ int bem_operator_kernel_times(bem_operator_t op, double* ms, long long* launches
 int bem_gmres(int nterms, const bem_operator_t* ops, const double* coef, const void* b, void* x,
               int maxiter, int restart, double tol, int* iters, double* resid, void* stream);
 
+/* GMRES for nrhs right-hand sides at once (the reference calls GMRes once per right-hand
+ * side; here the nrhs independent solves advance in lockstep so that every Arnoldi step applies
+ * the operators once to all of them, streaming the H-matrix once per step).  b, x: nrhs
+ * column-major device vectors (leading dimension = n).  Per column: FP64 Arnoldi with CGS2,
+ * Givens rotations, own convergence; resid[nrhs] = final relative residuals; iters = steps. */
+int bem_gmres_batched(int nterms, const bem_operator_t* ops, const double* coef, int nrhs, const void* b,
+                      void* x, int maxiter, int restart, double tol, int* iters, double* resid, void* stream);
+
 const char* bem_last_error(void);
 
 #ifdef __cplusplus

@@ -75,6 +75,8 @@ SIGNATURES = {
     "bem_sl_batch_eval": ([_vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp], C.c_int),
     "bem_sl_batch_info": ([_vp, _ip, _ip, C.POINTER(C.c_longlong)], C.c_int),
     "bem_sl_batch_destroy": ([_vp], C.c_int),
+    "bem_gmres_batched": ([C.c_int, C.POINTER(_vp), _dp, C.c_int, _vp, _vp, C.c_int, C.c_int, C.c_double, _ip, _dp,
+                           _vp], C.c_int),
     "bem_gmres": ([C.c_int, C.POINTER(_vp), _dp, _vp, _vp, C.c_int, C.c_int, C.c_double, _ip, _dp, _vp],
                   C.c_int),
 }

@@ -555,9 +555,26 @@ def GMRes(A, b, pre=None, freedofs=None, x=None, maxsteps=100, tol=1e-7, innerpr
         coef[2 * k], coef[2 * k + 1] = z.real, z.imag
     it, res = C.c_int(), C.c_double()
     stream = torch.cuda.current_stream().cuda_stream
+    rtol = float(reltol if reltol is not None else tol)
+    if bd.dim() == 2:
+        # several right-hand sides (columns): solved together, one operator pass per step
+        nrhs = bd.shape[1]
+        bc = bd.t().contiguous()
+        xc = xd.t().contiguous()
+        resv = (C.c_double * nrhs)()
+        check(lib.bem_gmres_batched(len(terms), ops, coef, nrhs, C.c_void_p(bc.data_ptr()), C.c_void_p(xc.data_ptr()),
+                                    int(maxsteps), int(restart or min(maxsteps, 200)), rtol, C.byref(it), resv,
+                                    C.c_void_p(stream)))
+        GMRes.last = dict(iterations=it.value, residual=max(resv), residuals=list(resv))
+        if printrates:
+            print(f"GMRes iteration {it.value}, max residual = {max(resv)}")
+        xd = xc.t().contiguous()
+        if x is not None:
+            x.copy_(xd)
+            return x
+        return xd
     check(lib.bem_gmres(len(terms), ops, coef, C.c_void_p(bd.data_ptr()), C.c_void_p(xd.data_ptr()), int(maxsteps),
-                        int(restart or min(maxsteps, 200)), float(reltol if reltol is not None else tol),
-                        C.byref(it), C.byref(res), C.c_void_p(stream)))
+                        int(restart or min(maxsteps, 200)), rtol, C.byref(it), C.byref(res), C.c_void_p(stream)))
     GMRes.last = dict(iterations=it.value, residual=res.value)
     if printrates:
         print(f"GMRes iteration {it.value}, residual = {res.value}")

@@ -347,4 +347,19 @@ int bem_gmres(int nterms, const bem_operator_t* ops, const double* coef, const v
   });
 }
 
+int bem_gmres_batched(int nterms, const bem_operator_t* ops, const double* coef, int nrhs, const void* b, void* x,
+                      int maxiter, int restart, double tol, int* iters, double* resid, void* stream) {
+  return guarded([&] {
+    REQUIRE(ops && coef && b && x && nterms >= 1, "null argument");
+    REQUIRE(nrhs >= 1, "nrhs must be >= 1");
+    std::vector<OperatorBase*> v;
+    for (int k = 0; k < nterms; ++k) {
+      REQUIRE(ops[k], "null operator");
+      v.push_back(ops[k]->op.get());
+    }
+    gmres_batched_solve(nterms, v.data(), coef, nrhs, b, x, maxiter, restart, tol, iters, resid,
+                        (cudaStream_t)stream);
+  });
+}
+
 }  // extern "C"

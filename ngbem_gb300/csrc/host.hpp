@@ -233,6 +233,8 @@ int trace_kind(int space_kind, int ev);
 bool pairs_overflow(size_t ntiles);
 int gmres_solve(int nterms, OperatorBase* const* ops, const double* coef, const void* b, void* x, int maxiter,
                 int restart, double tol, int* iters, double* resid, cudaStream_t s);
+int gmres_batched_solve(int nterms, OperatorBase* const* ops, const double* coef, int nrhs, const void* b, void* x,
+                        int maxiter, int restart, double tol, int* iters, double* resid, cudaStream_t s);
 
 }  // namespace bem
 

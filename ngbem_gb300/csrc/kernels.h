@@ -201,6 +201,12 @@ void launch_scale_copy(bool cplx, int n, const void* w, double inv, void* q, cud
 // x += Q y  (y on device, complex or real)
 void launch_axpy_basis(bool cplx, int n, int k, const void* Q, const void* y, void* x, cudaStream_t s);
 // r = b - r  (r holds A x on input)
+// batched GMRES vectors (gmres_batch.cu): nrhs columns of length n, basis block i at i*nrhs*n
+void launch_bgemv_ct(bool cplx, int n, int k, int nrhs, const void* Q, const void* w, void* h, cudaStream_t s);
+void launch_bgemv_sub(bool cplx, int n, int k, int nrhs, const void* Q, const void* h, void* w, cudaStream_t s);
+void launch_baxpy_basis(bool cplx, int n, int k, int nrhs, const void* Q, const void* y, void* x, cudaStream_t s);
+void launch_bnrm2(bool cplx, int n, int nrhs, const void* w, double* out, cudaStream_t s);
+void launch_bscale(bool cplx, int n, int nrhs, const void* w, const double* inv, void* q, cudaStream_t s);
 void launch_residual(bool cplx, int n, const void* b, void* r, cudaStream_t s);
 
 }  // namespace bem

@@ -1,0 +1,84 @@
+"""Load vectors <f, v> on the trace spaces (the role of NGSolve's LinearForm(f*v*ds) beside the
+operators in the reference demos, e.g. demos/HelmholtzBurtonMiller.ipynb), host-side numpy.
+
+f is evaluated at the points of a collapsed Gauss triangle rule on every flat triangle; it is
+called as f(x, n) with x (nt, nq, 3) the points and n (nt, 3) the unit normals, and returns
+(nt, nq) values (or (nt, nq, m) for m right-hand sides at once).
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from .meshes import Mesh
+
+__all__ = ["triangle_rule", "p1_load_vector", "p0_load_vector", "plane_wave_bm_source", "random_directions"]
+
+
+def triangle_rule(order: int):
+    """Collapsed Gauss-Legendre rule on the reference triangle (1,0), (0,1), (0,0): with n =
+    order//2 + 2 points per direction, xi = u, eta = v (1 - u), weight w_u w_v (1 - u); exact for
+    polynomials of degree order on the triangle.  Weights sum to 1/2."""
+    n = order // 2 + 2
+    g, wg = np.polynomial.legendre.leggauss(n)
+    u, wu = (g + 1.0) / 2.0, wg / 2.0
+    xi = np.repeat(u, n)
+    eta = np.outer(1.0 - u, u).ravel()
+    wt = np.outer(wu * (1.0 - u), wu).ravel()
+    return xi, eta, wt
+
+
+def _geometry(mesh: Mesh, order: int):
+    X, T = mesh.vertices, mesh.triangles
+    p0, p1, p2 = X[T[:, 0]], X[T[:, 1]], X[T[:, 2]]
+    n = np.cross(p0 - p2, p1 - p2)
+    detj = np.linalg.norm(n, axis=1)
+    n = n / detj[:, None]
+    xi, eta, w = triangle_rule(order)
+    lam = np.stack([xi, eta, 1.0 - xi - eta], axis=1)            # (nq, 3) for (p0, p1, p2)
+    x = (lam[None, :, 0, None] * p0[:, None] + lam[None, :, 1, None] * p1[:, None]
+         + lam[None, :, 2, None] * p2[:, None])                    # (nt, nq, 3)
+    return x, n, detj, lam, w
+
+
+def p1_load_vector(mesh: Mesh, f, order: int = 6) -> np.ndarray:
+    """b_i = int_Gamma f phi_i for the continuous piecewise-linear basis (vertex dofs)."""
+    x, n, detj, lam, w = _geometry(mesh, order)
+    fv = np.asarray(f(x, n))
+    multi = fv.ndim == 3
+    if not multi:
+        fv = fv[..., None]
+    m = fv.shape[2]
+    out = np.zeros((mesh.nv, m), dtype=np.result_type(fv.dtype, np.float64))
+    for a in range(3):
+        contrib = np.einsum("q,tqm->tm", w * lam[:, a], fv) * detj[:, None]
+        np.add.at(out, mesh.triangles[:, a], contrib)
+    return out if multi else out[:, 0]
+
+
+def p0_load_vector(mesh: Mesh, f, order: int = 6) -> np.ndarray:
+    """b_e = int_{T_e} f for the piecewise-constant basis (element dofs)."""
+    x, n, detj, lam, w = _geometry(mesh, order)
+    fv = np.asarray(f(x, n))
+    if fv.ndim == 3:
+        return np.einsum("q,tqm->tm", w, fv) * detj[:, None]
+    return (fv @ w) * detj
+
+
+def plane_wave_bm_source(kappa: float, directions: np.ndarray):
+    """Burton-Miller data of incident plane waves exp(i kappa d.x), one per row of directions:
+    f = i kappa exp(i kappa d.x) (d.n - 1) (reference demos/HelmholtzBurtonMiller.ipynb, cell 8,
+    for d = e_x)."""
+    d = np.asarray(directions, dtype=np.float64)
+
+    def f(x, n):
+        ph = np.einsum("tqc,mc->tqm", x, d)
+        dn = np.einsum("tc,mc->tm", n, d)[:, None, :]
+        return 1j * kappa * np.exp(1j * kappa * ph) * (dn - 1.0)
+    return f
+
+
+def random_directions(m: int, seed: int) -> np.ndarray:
+    """m unit vectors, uniform on the sphere (normalised standard normal draws, seeded)."""
+    rng = np.random.default_rng(seed)
+    v = rng.standard_normal((m, 3))
+    return v / np.linalg.norm(v, axis=1)[:, None]
