@@ -77,6 +77,7 @@ typedef struct {
   int mv_items[4];             /* matvec work items per pass (t=V2x, y+=Dx+U2t, t=U2^Tx, y+=D^Tx+V2^Tt) */
   int mv_segments;             /* matvec segments (block pieces) */
   int mv_ranges[4];            /* staged input ranges per pass */
+  double ms_mvitems;           /* host time grouping the blocks into matvec work items */
 } bem_operator_info_t;
 
 /* Fill *p with the reference defaults (intorder 3, leafsize 40, eta 2, eps 1e-6, aca). */

@@ -481,4 +481,15 @@ void partition_blocks(const ClusterTreeH& row, const ClusterTreeH& col, double e
   }
 }
 
+std::shared_ptr<ClusterTreeH> SpaceH::tree(int leafsize) {
+  std::lock_guard<std::mutex> lk(tree_mu);
+  auto it = trees.find(leafsize);
+  if (it != trees.end()) return it->second;
+  auto t = std::make_shared<ClusterTreeH>();
+  t->build(*this, leafsize);
+  t->build_patches(*this);
+  trees[leafsize] = t;
+  return t;
+}
+
 }  // namespace bem

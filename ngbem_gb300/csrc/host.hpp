@@ -100,6 +100,8 @@ struct MeshH {
   RuleTables& rule_tables(int order);
 };
 
+struct ClusterTreeH;
+
 struct SpaceH {
   MeshH* mesh = nullptr;
   int kind = BEM_P0, nd = 1, ndof = 0, dual = 0;
@@ -110,6 +112,11 @@ struct SpaceH {
   void build(MeshH* m, int kind_, int dual_);
   const int* el_dofs(int e) const { return &dofs[3 * e]; }
   void ensure_device();
+  // cluster tree with element patches for a leaf size, built on first use and shared by the
+  // operators on this space (a tree depends only on the space and the leaf size)
+  std::shared_ptr<ClusterTreeH> tree(int leafsize);
+  std::mutex tree_mu;
+  std::map<int, std::shared_ptr<ClusterTreeH>> trees;
 };
 
 // ---- cluster tree and partition (geometry.cpp) -----------------------------------------
@@ -155,7 +162,7 @@ struct HOperator : OperatorBase {
   bem_params_t prm{};
   int prec = 0;           // 0 fp64, 1 mixed
   size_t vsize = 8;       // bytes of one stored value
-  std::unique_ptr<ClusterTreeH> own_trial, own_test;
+  std::shared_ptr<ClusterTreeH> own_trial, own_test;
   ClusterTreeH* ttrial = nullptr;
   ClusterTreeH* ttest = nullptr;
   std::vector<BlockH> blocks;

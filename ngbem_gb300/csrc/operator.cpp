@@ -10,7 +10,10 @@
 //          persistent FP64 Sauter-Schwab kernel over the binned singular pairs
 //   host : blocks whose ACA hit the rank cap are assembled densely in a second near pass
 #include <algorithm>
+#include <atomic>
 #include <chrono>
+#include <exception>
+#include <thread>
 #include <cmath>
 #include <complex>
 #include <cstring>
@@ -86,16 +89,12 @@ void HOperator::assemble() {
   width = trial->ndof;
 
   // ---- trees, patches, partition (host) ------------------------------------------------
-  own_trial = std::make_unique<ClusterTreeH>();
-  own_trial->build(*trial, leaf);
-  own_trial->build_patches(*trial);
+  own_trial = trial->tree(leaf);
   ttrial = own_trial.get();
   if (test == trial) {
     ttest = ttrial;
   } else {
-    own_test = std::make_unique<ClusterTreeH>();
-    own_test->build(*test, leaf);
-    own_test->build_patches(*test);
+    own_test = test->tree(leaf);
     ttest = own_test.get();
   }
   partition_blocks(*ttest, *ttrial, eta, blocks);
@@ -491,7 +490,9 @@ void HOperator::assemble() {
     info.bytes_lowrank += (long long)L.R * (L.m + L.n) * (long long)vsize;
     info.bytes_lowrank_u += (long long)L.R * L.m * (long long)vsize;
   }
+  const auto t_items = clk::now();
   build_mv_items();
+  info.ms_mvitems = ms_since(t_items);
   BEM_CUDA(cudaDeviceSynchronize());
   keep.clear();
   d_U.release();
@@ -538,80 +539,98 @@ void HOperator::build_mv_items() {
   // A span is one contiguous payload range (a block, or a chunk of one) with its generic
   // pieces (kind, block, first row/col, count, byte offset from the span start).
   struct GPiece { int kind, blk, k0, cnt, soff; };
-  struct Span { unsigned long long src; size_t bytes; bool direct; std::vector<GPiece> pcs; };
-  struct GItem { unsigned long long src; int bytes; std::vector<GPiece> pcs; };
-  auto group = [&](const std::vector<Span>& spans, std::vector<GItem>& items) {
-    GItem cur{0, 0, {}};
+  // spans and items keep their pieces in flat pools (first piece, count): no allocation per span
+  struct Span { unsigned long long src; size_t bytes; bool direct; int p0, np; };
+  struct GItem { unsigned long long src; int bytes; int p0, np; };
+  auto group = [&](const std::vector<Span>& spans, const std::vector<GPiece>& spool, std::vector<GItem>& items,
+                   std::vector<GPiece>& ipool) {
+    ipool.reserve(spool.size());
+    GItem cur{0, 0, 0, 0};
     bool open = false;
     for (const Span& sp : spans) {
       if (sp.direct) {
-        if (open) { items.push_back(std::move(cur)); open = false; }
-        items.push_back(GItem{sp.src, 0, sp.pcs});
+        if (open) { items.push_back(cur); open = false; }
+        items.push_back(GItem{sp.src, 0, (int)ipool.size(), sp.np});
+        ipool.insert(ipool.end(), spool.begin() + sp.p0, spool.begin() + sp.p0 + sp.np);
         continue;
       }
       if (!(open && sp.src == cur.src + (unsigned long long)cur.bytes && cur.bytes + sp.bytes <= stage &&
-            cur.pcs.size() + sp.pcs.size() <= (size_t)mv_max_pieces())) {
-        if (open) items.push_back(std::move(cur));
-        cur = GItem{sp.src, 0, {}};
+            (size_t)cur.np + sp.np <= (size_t)mv_max_pieces())) {
+        if (open) items.push_back(cur);
+        cur = GItem{sp.src, 0, (int)ipool.size(), 0};
         open = true;
       }
-      for (GPiece g : sp.pcs) {
+      for (int q = 0; q < sp.np; ++q) {
+        GPiece g = spool[sp.p0 + q];
         g.soff += cur.bytes;
-        cur.pcs.push_back(g);
+        ipool.push_back(g);
       }
+      cur.np += sp.np;
       cur.bytes += (int)sp.bytes;
     }
-    if (open) items.push_back(std::move(cur));
+    if (open) items.push_back(cur);
   };
   auto pad16 = [](size_t b) { return (b + 15) / 16 * 16; };
-  auto pieces = [&](int kind, int blk, int k0, int cnt, int per, size_t step) {
-    std::vector<GPiece> out;
+  // appends the pieces of one span to pool; returns the count
+  auto pieces = [&](std::vector<GPiece>& pool, int kind, int blk, int k0, int cnt, int per, size_t step) {
     int pc = std::max(1, piece / std::max(1, per));
     const int cap = mv_max_pieces();
     if ((cnt + pc - 1) / pc > cap) pc = (cnt + cap - 1) / cap;
-    for (int a = 0; a < cnt; a += pc) out.push_back(GPiece{kind, blk, k0 + a, std::min(pc, cnt - a), (int)(a * step)});
-    return out;
+    int np = 0;
+    for (int a = 0; a < cnt; a += pc, ++np) pool.push_back(GPiece{kind, blk, k0 + a, std::min(pc, cnt - a), (int)(a * step)});
+    return np;
   };
   // dense blocks (column-major): column chunks with 16-byte aligned starts
   std::vector<Span> sd;
+  std::vector<GPiece> pd;
+  sd.reserve(mvdense.size());
   for (int k = 0; k < (int)mvdense.size(); ++k) {
     const MVDense& D = mvdense[k];
     const size_t colb = (size_t)D.m * vsize;
     const size_t total = pad16(colb * D.n);
     if (total <= stage) {
-      sd.push_back({D.ptr, total, false, pieces(0, k, 0, D.n, D.m, colb)});
+      const int p0 = (int)pd.size();
+      sd.push_back({D.ptr, total, false, p0, pieces(pd, 0, k, 0, D.n, D.m, colb)});
       continue;
     }
     size_t q = 1;
     while ((colb * q) % 16) ++q;
     const size_t cc = stage / colb / q * q;
     if (cc == 0) {  // one column exceeds a stage: read in place
-      sd.push_back({D.ptr, 0, true, pieces(0, k, 0, D.n, D.m, colb)});
+      const int p0 = (int)pd.size();
+      sd.push_back({D.ptr, 0, true, p0, pieces(pd, 0, k, 0, D.n, D.m, colb)});
       continue;
     }
     for (int j0 = 0; j0 < D.n; j0 += (int)cc) {
       const int cnt = std::min((int)cc, D.n - j0);
       const size_t b0 = (size_t)j0 * colb;
       const size_t b1 = (j0 + cnt == D.n) ? total : (size_t)(j0 + cnt) * colb;
-      sd.push_back({D.ptr + b0, b1 - b0, false, pieces(0, k, j0, cnt, D.m, colb)});
+      const int p0 = (int)pd.size();
+      sd.push_back({D.ptr + b0, b1 - b0, false, p0, pieces(pd, 0, k, j0, cnt, D.m, colb)});
     }
   }
   // low-rank factors: U2 row chunks (pieces of rows), V2 column chunks (pieces of columns)
   std::vector<Span> su, sv;
+  std::vector<GPiece> pu, pv;
   for (int f = 0; f < (int)mvlr.size(); ++f) {
     const LRDesc& L = mvlr[f];
     if (L.R == 0) continue;
     const size_t cub = (size_t)L.cu * L.R * vsize, cvb = (size_t)L.cv * L.R * vsize;
-    for (int i0 = 0, c = 0; i0 < L.m; i0 += L.cu, ++c)
-      su.push_back({L.u + c * cub, cub, cub > stage, pieces(1, f, i0, std::min(L.cu, L.m - i0), L.R, vsize)});
-    for (int j0 = 0, c = 0; j0 < L.n; j0 += L.cv, ++c)
-      sv.push_back({L.v + c * cvb, cvb, cvb > stage,
-                    pieces(2, f, j0, std::min(L.cv, L.n - j0), L.R, (size_t)L.R * vsize)});
+    for (int i0 = 0, c = 0; i0 < L.m; i0 += L.cu, ++c) {
+      const int p0 = (int)pu.size();
+      su.push_back({L.u + c * cub, cub, cub > stage, p0, pieces(pu, 1, f, i0, std::min(L.cu, L.m - i0), L.R, vsize)});
+    }
+    for (int j0 = 0, c = 0; j0 < L.n; j0 += L.cv, ++c) {
+      const int p0 = (int)pv.size();
+      sv.push_back({L.v + c * cvb, cvb, cvb > stage, p0,
+                    pieces(pv, 2, f, j0, std::min(L.cv, L.n - j0), L.R, (size_t)L.R * vsize)});
+    }
   }
   std::vector<GItem> id, iu, iv;
-  group(sd, id);
-  group(su, iu);
-  group(sv, iv);
+  std::vector<GPiece> qd, qu, qv;
+  group(sd, pd, id, qd);
+  group(su, pu, iu, qu);
+  group(sv, pv, iv, qv);
   // per pass: 0 t = V2 x, 1 y += D x + U2 t, 2 t = U2^T x, 3 y += D^T x + V2^T t
   auto piece_raw = [&](int pass, const GPiece& g) {
     MVPiece p{};
@@ -641,38 +660,64 @@ void HOperator::build_mv_items() {
   // passes 0-3 as above; 4-7 are the phases of the single-launch matvec: 4 = t = V2 x with
   // y += D x (no dependence on t), 5 = y += U2 t; 6 = t = U2^T x with y += D^T x, 7 = y += V2^T t.
   // Each list is applied with the piece semantics of pass `sem`.
-  struct LS { const std::vector<GItem>* L; int sem; };
-  const std::vector<LS> lists[MV_NPASS] = {{{&iv, 0}},          {{&id, 1}, {&iu, 1}}, {{&iu, 2}}, {{&id, 3}, {&iv, 3}},
-                                           {{&iv, 0}, {&id, 1}}, {{&iu, 1}},           {{&iu, 2}, {&id, 3}}, {{&iv, 3}}};
+  struct LS { const std::vector<GItem>* L; const std::vector<GPiece>* P; int sem; };
+  const std::vector<LS> lists[MV_NPASS] = {
+      {{&iv, &qv, 0}},                   {{&id, &qd, 1}, {&iu, &qu, 1}}, {{&iu, &qu, 2}}, {{&id, &qd, 3}, {&iv, &qv, 3}},
+      {{&iv, &qv, 0}, {&id, &qd, 1}},   {{&iu, &qu, 1}},                {{&iu, &qu, 2}, {&id, &qd, 3}}, {{&iv, &qv, 3}}};
   long long npieces = 0;
   const int esz = cplx ? 16 : 8;          // one x or t entry as staged (x: FP32 hi+lo or FP64)
   const int per16 = 16 / esz;             // entries per 16 bytes
   const int inarea = mv_in_bytes();
-  for (int pass = 0; pass < MV_NPASS; ++pass) {
+  // the passes are independent: build their host tables on parallel threads, upload after
+  std::vector<MVTItem> pass_items[MV_NPASS];
+  std::vector<MVPiece> pass_pcs[MV_NPASS];
+  std::vector<MVRange> pass_rngs[MV_NPASS];
+  // tasks: a pass's item lists cut into chunks; each chunk builds its own tables with local
+  // offsets, and the chunks are concatenated in order afterwards
+  struct Task {
+    int pass;
+    const LS* ls;
+    size_t i0, i1;
     std::vector<MVTItem> items;
     std::vector<MVPiece> pcs;
     std::vector<MVRange> rngs;
+  };
+  std::vector<Task> tasks;
+  for (int pass = 0; pass < MV_NPASS; ++pass)
     for (const LS& ls : lists[pass]) {
+      const size_t n = ls.L->size(), chunk = std::max<size_t>(128, (n + 7) / 8);
+      for (size_t i0 = 0; i0 < n; i0 += chunk) tasks.push_back(Task{pass, &ls, i0, std::min(n, i0 + chunk), {}, {}, {}});
+    }
+  auto build_task = [&](Task& tk) {
+    std::vector<MVTItem>& items = tk.items;
+    std::vector<MVPiece>& pcs = tk.pcs;
+    std::vector<MVRange>& rngs = tk.rngs;
+    struct Iv { int src, e0, e1; };
+    std::vector<Iv> raw, ivs, merged;  // per-item scratch, reused
+    std::vector<int> piv, dst;
+    {
+      const LS& ls = *tk.ls;
       const int sem = ls.sem;
-      for (const GItem& gi : *ls.L) {
+      for (size_t ii = tk.i0; ii < tk.i1; ++ii) {
+        const GItem& gi = (*ls.L)[ii];
+        const GPiece* gp = ls.P->data() + gi.p0;
         MVTItem it{};
         it.src = gi.src;
         it.bytes = gi.bytes;
         it.seg0 = (int)pcs.size();
-        it.nseg = (int)gi.pcs.size();
+        it.nseg = gi.np;
         it.rng0 = (int)rngs.size();
         // input intervals of the pieces, merged into 16-byte aligned ranges of x or t.  Nearby
         // ranges are merged further (smallest gap first) while the staged bytes still fit the
         // input area: the producer issues the first two ranges from the descriptor and has to
         // load the others, so staging a few unused entries of x or t (L2 resident) is cheaper.
-        struct Iv { int src, e0, e1; };
-        std::vector<Iv> raw;
-        for (const GPiece& g : gi.pcs) {
-          const MVPiece p = piece_for(sem, g);
+        raw.clear();
+        for (int q = 0; q < gi.np; ++q) {
+          const MVPiece p = piece_for(sem, gp[q]);
           raw.push_back({p.flags & 1, p.in_off, p.in_off + p.Kc});
           pcs.push_back(p);
         }
-        std::vector<Iv> ivs = raw;
+        ivs.assign(raw.begin(), raw.end());
         for (Iv& v : ivs) {
           v.e0 = v.e0 / per16 * per16;
           v.e1 = (v.e1 + per16 - 1) / per16 * per16;
@@ -681,12 +726,14 @@ void HOperator::build_mv_items() {
           return x.src != y.src ? x.src < y.src : x.e0 < y.e0;
         });
         {
-          std::vector<Iv> m;
+          merged.clear();
           for (const Iv& v : ivs) {
-            if (!m.empty() && m.back().src == v.src && v.e0 <= m.back().e1) m.back().e1 = std::max(m.back().e1, v.e1);
-            else m.push_back(v);
+            if (!merged.empty() && merged.back().src == v.src && v.e0 <= merged.back().e1)
+              merged.back().e1 = std::max(merged.back().e1, v.e1);
+            else
+              merged.push_back(v);
           }
-          ivs.swap(m);
+          ivs.swap(merged);
         }
         auto staged = [&]() {
           long long b = 0;
@@ -710,13 +757,13 @@ void HOperator::build_mv_items() {
           ivs.erase(ivs.begin() + best + 1);
           tot += gap;
         }
-        std::vector<int> piv;  // range index of each piece
+        piv.clear();  // range index of each piece
         for (const Iv& v : raw) {
           int r = 0;
           while (!(ivs[r].src == v.src && ivs[r].e0 <= v.e0 && v.e1 <= ivs[r].e1)) ++r;
           piv.push_back(r);
         }
-        std::vector<int> dst(ivs.size());
+        dst.assign(ivs.size(), 0);
         int total = 0;
         for (size_t r = 0; r < ivs.size(); ++r) {
           dst[r] = total;
@@ -733,7 +780,7 @@ void HOperator::build_mv_items() {
               it.r[4 * r + 3] = rg.dst;
             }
           }
-          for (size_t q = 0; q < gi.pcs.size(); ++q) {
+          for (int q = 0; q < gi.np; ++q) {
             MVPiece& p = pcs[it.seg0 + q];
             const Iv& v = ivs[piv[q]];
             p.in_soff = dst[piv[q]] + (p.in_off - v.e0) * esz;
@@ -747,14 +794,55 @@ void HOperator::build_mv_items() {
         items.push_back(it);
       }
     }
-    d_items[pass].upload(items);
-    d_pieces[pass].upload(pcs);
-    d_ranges[pass].upload(rngs);
-    n_items[pass] = (int)items.size();
+  };
+  {
+    std::vector<std::thread> th;
+    std::exception_ptr failure;
+    std::mutex fmu;
+    std::atomic<size_t> next{0};
+    const int nth = (int)std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+    for (int w = 0; w < nth; ++w)
+      th.emplace_back([&] {
+        try {
+          for (size_t k = next++; k < tasks.size(); k = next++) build_task(tasks[k]);
+        } catch (...) {
+          std::lock_guard<std::mutex> lk(fmu);
+          failure = std::current_exception();
+        }
+      });
+    for (auto& t : th) t.join();
+    if (failure) std::rethrow_exception(failure);
+    size_t ni[MV_NPASS] = {}, np_[MV_NPASS] = {}, nr[MV_NPASS] = {};
+    for (const Task& tk : tasks) {
+      ni[tk.pass] += tk.items.size();
+      np_[tk.pass] += tk.pcs.size();
+      nr[tk.pass] += tk.rngs.size();
+    }
+    for (int pass = 0; pass < MV_NPASS; ++pass) {
+      pass_items[pass].reserve(ni[pass]);
+      pass_pcs[pass].reserve(np_[pass]);
+      pass_rngs[pass].reserve(nr[pass]);
+    }
+    for (Task& tk : tasks) {
+      const int seg_off = (int)pass_pcs[tk.pass].size(), rng_off = (int)pass_rngs[tk.pass].size();
+      for (MVTItem& it : tk.items) {
+        it.seg0 += seg_off;
+        it.rng0 += rng_off;
+      }
+      pass_items[tk.pass].insert(pass_items[tk.pass].end(), tk.items.begin(), tk.items.end());
+      pass_pcs[tk.pass].insert(pass_pcs[tk.pass].end(), tk.pcs.begin(), tk.pcs.end());
+      pass_rngs[tk.pass].insert(pass_rngs[tk.pass].end(), tk.rngs.begin(), tk.rngs.end());
+    }
+  }
+  for (int pass = 0; pass < MV_NPASS; ++pass) {
+    d_items[pass].upload(pass_items[pass]);
+    d_pieces[pass].upload(pass_pcs[pass]);
+    d_ranges[pass].upload(pass_rngs[pass]);
+    n_items[pass] = (int)pass_items[pass].size();
     if (pass < 4) {
-      info.mv_ranges[pass] = (int)rngs.size();
+      info.mv_ranges[pass] = (int)pass_rngs[pass].size();
       info.mv_items[pass] = n_items[pass];
-      npieces += (long long)pcs.size();
+      npieces += (long long)pass_pcs[pass].size();
     }
   }
   info.mv_segments = (int)npieces;
