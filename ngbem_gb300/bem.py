@@ -344,6 +344,13 @@ class HMatrix(_NativeMatrix):
         """FP32-stored operators: error-free (True, default) or plain FP32 (False) matvec arithmetic."""
         check(lib.bem_operator_set_accuracy(self.h, int(bool(compensated))))
 
+    def autotune(self, reps: int = 10) -> dict:
+        """Time the single-vector matvec for each piece size and schedule; keep the fastest."""
+        piece, fused, ms = C.c_int(), C.c_int(), C.c_double()
+        check(lib.bem_operator_autotune(self.h, int(reps), C.byref(piece), C.byref(fused), C.byref(ms)))
+        self.tuned = {"piece": piece.value, "fused": bool(fused.value), "ms": ms.value}
+        return self.tuned
+
     def set_profiling(self, enable: bool = True):
         check(lib.bem_operator_set_profiling(self.h, int(bool(enable))))
 

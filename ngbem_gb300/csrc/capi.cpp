@@ -273,6 +273,16 @@ int bem_operator_set_accuracy(bem_operator_t op, int compensated) {
   });
 }
 
+int bem_operator_autotune(bem_operator_t op, int reps, int* piece, int* fused, double* ms) {
+  return guarded([&] {
+    REQUIRE(op, "null argument");
+    auto* h = dynamic_cast<HOperator*>(op->op.get());
+    if (!h) throw Error(BEM_ERR_STATE, "not an H-matrix operator");
+    const double t = h->autotune(reps, piece, fused);
+    if (ms) *ms = t;
+  });
+}
+
 int bem_operator_set_profiling(bem_operator_t op, int enable) {
   return guarded([&] {
     REQUIRE(op, "null argument");

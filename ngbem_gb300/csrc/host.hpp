@@ -177,6 +177,8 @@ struct HOperator : OperatorBase {
   DevBuf d_items[MV_NPASS], d_pieces[MV_NPASS], d_ranges[MV_NPASS];
   int n_items[MV_NPASS] = {};
   bool mv_fused = true;  // one cooperative launch per single-RHS matvec (else the 4-pass pipeline)
+  int mv_piece = 0;      // stored elements per piece (0: the kernel's default); set by autotune
+  double autotune(int reps, int* best_piece, int* best_fused);
   int mv_grid = 152;
   int mv_compensated = 1;  // fp32 storage: error-free products/sums (1) or plain FP32 (0)
   int t_len = 0;

@@ -491,6 +491,7 @@ void HOperator::assemble() {
     info.bytes_lowrank_u += (long long)L.R * L.m * (long long)vsize;
   }
   const auto t_items = clk::now();
+  mv_fused = mv_fused_supported();
   build_mv_items();
   info.ms_mvitems = ms_since(t_items);
   BEM_CUDA(cudaDeviceSynchronize());
@@ -535,7 +536,7 @@ bool pairs_overflow(size_t ntiles) { return ntiles > (size_t)INT_MAX; }
 // matvec stage: consecutive segments whose bytes are contiguous share one bulk copy.
 void HOperator::build_mv_items() {
   const size_t stage = (size_t)mv_stage_bytes();
-  const int piece = mv_piece_elems();  // target elements per piece (one consumer warp's task)
+  const int piece = mv_piece > 0 ? mv_piece : mv_piece_elems();  // target elements per piece (one warp's task)
   // A span is one contiguous payload range (a block, or a chunk of one) with its generic
   // pieces (kind, block, first row/col, count, byte offset from the span start).
   struct GPiece { int kind, blk, k0, cnt, soff; };
@@ -854,7 +855,6 @@ void HOperator::build_mv_items() {
   // of the single-launch matvec, [4, 5] its grid barrier (arrivals, generation)
   d_sched.alloc(8 * sizeof(int));
   BEM_CUDA(cudaMemset(d_sched.p, 0, 8 * sizeof(int)));
-  mv_fused = mv_fused_supported();
   int dev = 0, nsm = 152;
   BEM_CUDA(cudaGetDevice(&dev));
   BEM_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
@@ -1558,6 +1558,67 @@ int gmres_batched_solve(int nterms, OperatorBase* const* ops, const double* coef
   if (resid)
     for (int q = 0; q < nrhs; ++q) resid[q] = rel[q];
   return BEM_OK;
+}
+
+}  // namespace bem
+
+namespace bem {
+
+// Picks the matvec work decomposition for this operator by timing it: the piece size (stored
+// elements per consumer-warp task, which also shapes the work items) and the schedule (one
+// cooperative launch, or the four-pass pipeline).  Each candidate is timed over `reps`
+// matvecs with CUDA events after a warm-up; the fastest is kept.
+double HOperator::autotune(int reps, int* best_piece, int* best_fused) {
+  if (reps < 1) reps = 1;
+  const int cand[] = {256, 384, 512, 768, 1024};
+  const size_t esz = cplx ? 16 : 8;
+  DevBuf x, y;
+  x.alloc((size_t)width * esz);
+  y.alloc((size_t)height * esz);
+  BEM_CUDA(cudaMemset(x.p, 0, (size_t)width * esz));
+  cudaStream_t s = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  BEM_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+  struct Guard {
+    cudaStream_t& s; cudaEvent_t& a; cudaEvent_t& b;
+    ~Guard() { if (a) cudaEventDestroy(a); if (b) cudaEventDestroy(b); if (s) cudaStreamDestroy(s); }
+  } guard{s, e0, e1};
+  BEM_CUDA(cudaEventCreate(&e0));
+  BEM_CUDA(cudaEventCreate(&e1));
+  const double one[2] = {1.0, 0.0}, zero[2] = {0.0, 0.0};
+  const bool fused_ok = mv_fused_supported();
+  const bool was_profiling = profiling;
+  profiling = false;
+  double best = 1e300;
+  int bp = mv_piece > 0 ? mv_piece : mv_piece_elems(), bf = mv_fused ? 1 : 0;
+  for (int pc : cand) {
+    mv_piece = pc;
+    build_mv_items();
+    for (int f = fused_ok ? 1 : 0; f >= 0; --f) {
+      mv_fused = f != 0;
+      for (int w = 0; w < 2; ++w) mult(0, one, x.p, zero, y.p, 1, s);
+      BEM_CUDA(cudaEventRecord(e0, s));
+      for (int r = 0; r < reps; ++r) mult(0, one, x.p, zero, y.p, 1, s);
+      BEM_CUDA(cudaEventRecord(e1, s));
+      BEM_CUDA(cudaEventSynchronize(e1));
+      float ms = 0.f;
+      BEM_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+      const double per = ms / reps;
+      if (per < best) {
+        best = per;
+        bp = pc;
+        bf = f;
+      }
+    }
+  }
+  mv_piece = bp;
+  mv_fused = bf != 0;
+  build_mv_items();
+  BEM_CUDA(cudaStreamSynchronize(s));
+  profiling = was_profiling;
+  if (best_piece) *best_piece = bp;
+  if (best_fused) *best_fused = bf;
+  return best;
 }
 
 }  // namespace bem
