@@ -46,7 +46,7 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 plain-path comparison")
     ap.add_argument("--no-gmres", action="store_true", help="skip the DtN GMRES solve (profiling runs)")
-    ap.add_argument("--workload", default="dtn", choices=["dtn", "shape", "bm"],
+    ap.add_argument("--workload", default="dtn", choices=["dtn", "shape", "bm", "maxwell"],
                     help="dtn: the headline H-matvec workload (default); shape: batched single-layer "
                          "energy + adjoint shape gradient over 64 perturbed icospheres (L2..L5); bm: "
                          "Helmholtz Burton-Miller kappa 8 on the L6 ellipsoid, 32 plane waves (batched GMRES)")
@@ -606,8 +606,82 @@ def run_bm(args):
         torch.distributed.destroy_process_group()
 
 
+def run_maxwell(args):
+    """Maxwell EFIE: single layer on RT0 of the unit icosphere at level args.level (default 5:
+    20480 triangles, 30720 edge dofs), kappa = 2, H-matrix leaf 20, eta 2, ACA eps 1e-6,
+    intorder 3.  Assembly and single-vector matvec time of the mixed path (complex64 far field,
+    complex128 singular pairs) and the plain FP64 GPU path, and the matvec error of the mixed
+    path against FP64 on a seeded random complex vector."""
+    import numpy as np
+    import torch
+
+    import ngbem_gb300 as nb
+
+    world, rank, local = dist_setup(args)
+    torch.cuda.set_device(local)
+    if world > 1:
+        torch.distributed.init_process_group("nccl")
+    L = args.level or 5
+    mesh = nb.icosphere(L)
+    # warm-up on a small sphere (module loading)
+    wR = nb.HDivSurface(nb.icosphere(2), complex=True)
+    for prec in ("mixed", "fp64"):
+        nb.MaxwellSingleLayerPotentialOperator(wR, kappa=2.0, leafsize=20, eps=1e-6, precision=prec)
+    rng = np.random.default_rng(SEED + 4)
+    out, ys = {}, {}
+    for prec in ("mixed", "fp64"):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        RT = nb.HDivSurface(mesh, complex=True)
+        op = nb.MaxwellSingleLayerPotentialOperator(RT, kappa=2.0, intorder=3, leafsize=20, eta=2.0, eps=1e-6,
+                                                    precision=prec)
+        torch.cuda.synchronize()
+        t_asm = time.perf_counter() - t0
+        if prec == "mixed":
+            xh = rng.standard_normal(RT.ndof) + 1j * rng.standard_normal(RT.ndof)
+            x = torch.from_numpy(xh).cuda()
+        tuned = op.mat.autotune(reps=5)
+        y = torch.empty_like(x)
+        for _ in range(args.warmup):
+            op.mat.Mult(x, y)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(args.steps):
+            op.mat.Mult(x, y)
+        e1.record()
+        torch.cuda.synchronize()
+        info = op.mat.info
+        ys[prec] = y.cpu().numpy()
+        out[prec] = {"assembly_s": t_asm, "matvec_ms": e0.elapsed_time(e1) / args.steps, "nze": info["nze"],
+                     "bytes": info["bytes_dense"] + info["bytes_lowrank"], "max_rank": info["max_rank"],
+                     "nfallback": info["nfallback"], "autotune": tuned}
+        del op
+        torch.cuda.empty_cache()
+    err = float(np.linalg.norm(ys["mixed"] - ys["fp64"]) / np.linalg.norm(ys["fp64"]))
+    line = {"metric": "Maxwell EFIE H-matvec/s (mixed) and assembly s", "value": 1e3 / out["mixed"]["matvec_ms"],
+            "unit": "matvec/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": out["mixed"]["matvec_ms"], "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "c64 far field / c128 singular pairs", "data": "synthetic",
+            "config": {"workload": f"maxwell_efie_rt0_icosphere_L{L}_kappa2", "triangles": mesh.nt,
+                       "dofs": int(3 * mesh.nt // 2), "kappa": 2.0, "leafsize": 20, "eta": 2.0, "eps": 1e-6,
+                       "intorder": 3, "l2": "not flushed (timed back to back)"},
+            "mixed": out["mixed"], "fp64": out["fp64"], "matvec_rel_err_mixed_vs_fp64": err,
+            "assembly_speedup": out["fp64"]["assembly_s"] / out["mixed"]["assembly_s"],
+            "matvec_speedup": out["fp64"]["matvec_ms"] / out["mixed"]["matvec_ms"]}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
 def main():
     args = parse()
+    if args.workload == "maxwell":
+        if args.impl == "reference":
+            print(json.dumps({"impl": "reference", "unavailable": "the dtn workload carries the CPU baseline"}))
+            return
+        run_maxwell(args)
+        return
     if args.workload == "bm":
         if args.impl == "reference":
             print(json.dumps({"impl": "reference", "unavailable": "the oracle's dense complex solve at 40962 dofs "
