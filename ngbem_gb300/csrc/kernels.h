@@ -124,7 +124,7 @@ struct MVFusedArgs {
   const MVRange* ranges[2];
   int nitems[2];
   int* ctr[2];          // chunk-claim counters of the two phases (zeroed in the prologue)
-  unsigned* bar;        // grid barrier: [0] arrivals (zero between barriers), [1] generation
+  unsigned long long* bar;  // grid barrier: arrival counter (only grows; a multiple of the grid between launches)
   const int* perm_in;   // xp[k] = x[perm_in[k]], k < n_in
   int n_in;
   const void* x;        // FP64 / complex128 input

@@ -361,6 +361,12 @@ __device__ __forceinline__ void run_piece_s(const MVArgs2& a, const MVPiece& pc,
 // chunk ahead, so the issue loop never waits on a global load.  After its last item the
 // producer pushes a stop marker (nseg < 0) through the next stage; the consumers release it
 // like an item, so a second pass can run through the same pipeline.
+// an item issued before its inputs were ready: its stage and input ranges
+struct MVPend {
+  int stage, rng0, nrng, pad;
+  int r[8];
+};
+
 struct MVSmem {
   uint64_t* full;        // MV_NSTAGE barriers: stage filled
   uint64_t* empty;       // MV_NSTAGE barriers: stage released by all consumer warps
@@ -370,6 +376,8 @@ struct MVSmem {
   unsigned char* stage;  // per stage: MV_STAGE payload bytes
   MVPiece* dstage;       // per stage: MV_MAXPC piece descriptors
   unsigned char* istage; // per stage: MV_INAREA staged input bytes
+  MVPend* pend;          // MV_NSTAGE items whose input ranges wait for the gate (producer only)
+  volatile int* gate;    // phase gate of the single-launch matvec (inputs of phase p ready: >= p + 1)
 };
 
 __device__ __forceinline__ MVSmem mv_smem(unsigned char* smem) {
@@ -382,6 +390,8 @@ __device__ __forceinline__ MVSmem mv_smem(unsigned char* smem) {
   m.stage = smem + MV_HDR;
   m.dstage = (MVPiece*)(m.stage + MV_NSTAGE * MV_STAGE);
   m.istage = (unsigned char*)(m.dstage + MV_NSTAGE * MV_MAXPC);
+  m.pend = (MVPend*)(m.istage + MV_NSTAGE * MV_INAREA);
+  m.gate = (volatile int*)(m.pend + MV_NSTAGE);
   return m;
 }
 
@@ -393,6 +403,7 @@ __device__ __forceinline__ void mv_init_barriers(const MVSmem& m) {
     }
     mbar_init(&m.dbar[0], 1);
     mbar_init(&m.dbar[1], 1);
+    *m.gate = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
   }
@@ -405,11 +416,52 @@ struct MVCons { uint32_t fphase = 0; int it = 0; int pbase = 0; };
 
 // Producer warp: streams items [0, nit) (first chunk fixed, the rest claimed from *ctr), then
 // the stop marker.  Returns false if a wait timed out (error flag set; copies drained).
+// need > 0: the inputs (x or t) of this pass are written by other CTAs; they are ready once the
+// gate reaches need.  Until then every item's payload and descriptors are issued at once and
+// its input-range copies are parked (the item's full barrier already expects their bytes, so no
+// consumer starts on it); the stage waits keep watching the gate, so the parked copies go out
+// as soon as it opens even while all stages are taken.
 __device__ bool mv_produce(const MVArgs2& a, const MVTItem* items, int nit, int* ctr, const MVSmem& m, MVProd& p,
-                           int lane) {
+                           int lane, int need = 0) {
   const int G = gridDim.x;
   int ok = 1;
   const int it0 = p.it;
+  bool open = need <= 0 || *m.gate >= need;
+  int npend = 0;
+  auto issue_ranges = [&](int s, int rng0, int nrng, const int* rin) {
+    unsigned char* ia = m.istage + s * MV_INAREA;
+    for (int r = lane; r < nrng; r += 32) {
+      MVRange rg;
+      if (r < 2) rg = MVRange{rin[4 * r], rin[4 * r + 1], rin[4 * r + 2], rin[4 * r + 3]};
+      else rg = a.ranges[rng0 + r];
+      const unsigned char* gsrc = (const unsigned char*)(rg.src ? a.tx : a.xp) + (size_t)rg.elem * a.in_esz;
+      asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+                   ::"r"(smem_u32(ia + rg.dst)), "l"((const void*)gsrc), "r"(rg.bytes),
+                   "r"(smem_u32(&m.full[s])) : "memory");
+    }
+  };
+  auto open_gate = [&]() {  // whole warp: the inputs are ready, issue the parked copies
+    __threadfence();
+    asm volatile("fence.proxy.async.global;" ::: "memory");
+    open = true;
+    for (int k = 0; k < npend; ++k) issue_ranges(m.pend[k].stage, m.pend[k].rng0, m.pend[k].nrng, m.pend[k].r);
+    __syncwarp();
+    npend = 0;
+  };
+  // wait for a free stage; meanwhile open the gate if it has become ready
+  auto wait_empty = [&](int s, uint32_t parity) -> int {
+    for (int i = 0; i < (1 << 22); ++i) {
+      int st = 0;
+      if (lane == 0) {
+        st = mbar_try_wait(&m.empty[s], parity) ? 1 : 0;
+        if (!open && *m.gate >= need) st |= 2;
+      }
+      st = __shfl_sync(0xffffffffu, st, 0);
+      if (st & 2) open_gate();
+      if (st & 1) return 1;
+    }
+    return 0;
+  };
   // global data written before this pass by ordinary stores (x, t) is read by bulk copies
   asm volatile("fence.proxy.async.global;" ::: "memory");
   auto chunk_size = [&](int remaining) {
@@ -447,9 +499,22 @@ __device__ bool mv_produce(const MVArgs2& a, const MVTItem* items, int nit, int*
       const int bytes = d->bytes, seg0 = d->seg0, nseg = d->nseg, rng0 = d->rng0, nrng = d->nrng;
       const int inbytes = d->inbytes;
       const int s = p.it % MV_NSTAGE;
+      if (!open && inbytes < 0) {
+        // inputs read in place: nothing may be issued for this item before they are ready
+        int st = 0;
+        for (int i = 0; i < (1 << 24) && !st; ++i) {
+          if (lane == 0) st = *m.gate >= need ? 1 : 0;
+          st = __shfl_sync(0xffffffffu, st, 0);
+          if (!st) __nanosleep(64);
+        }
+        if (!st) {
+          ok = 0;
+          break;
+        }
+        open_gate();
+      }
       // the first use of a stage passes at once (parity of the phase before the first)
-      if (lane == 0) ok = mbar_wait(&m.empty[s], ((p.ephase >> s) & 1u) ^ 1u) ? 1 : 0;
-      ok = __shfl_sync(0xffffffffu, ok, 0);
+      ok = wait_empty(s, ((p.ephase >> s) & 1u) ^ 1u);
       if (!ok) break;
       p.ephase ^= 1u << s;
       const int dbytes = nseg * (int)sizeof(MVPiece);
@@ -471,15 +536,18 @@ __device__ bool mv_produce(const MVArgs2& a, const MVTItem* items, int nit, int*
                        ::"r"(smem_u32(m.dstage + s * MV_MAXPC)), "l"((const void*)(a.pieces + seg0)),
                        "r"(dbytes), "r"(smem_u32(&m.full[s])) : "memory");
       }
-      unsigned char* ia = m.istage + s * MV_INAREA;
-      for (int r = lane; r < nrng; r += 32) {
-        MVRange rg;
-        if (r < 2) rg = MVRange{d->r[4 * r], d->r[4 * r + 1], d->r[4 * r + 2], d->r[4 * r + 3]};
-        else rg = a.ranges[rng0 + r];
-        const unsigned char* gsrc = (const unsigned char*)(rg.src ? a.tx : a.xp) + (size_t)rg.elem * a.in_esz;
-        asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
-                     ::"r"(smem_u32(ia + rg.dst)), "l"((const void*)gsrc), "r"(rg.bytes),
-                     "r"(smem_u32(&m.full[s])) : "memory");
+      if (open) {
+        issue_ranges(s, rng0, nrng, d->r);
+      } else if (nrng > 0) {
+        if (lane == 0) {
+          MVPend& e = m.pend[npend];
+          e.stage = s;
+          e.rng0 = rng0;
+          e.nrng = nrng;
+#pragma unroll
+          for (int k = 0; k < 8; ++k) e.r[k] = d->r[k];
+        }
+        ++npend;  // at most MV_NSTAGE: a parked item holds its stage until its inputs land
       }
       __syncwarp();
       ++p.it;
@@ -506,6 +574,17 @@ __device__ bool mv_produce(const MVArgs2& a, const MVTItem* items, int nit, int*
       pend = true;
       if (lane == 0) tok = atomicAdd(ctr, want);
     }
+  }
+  if (ok && !open) {
+    // all items issued before the inputs were ready: wait for the gate (bounded)
+    int st = 0;
+    for (int i = 0; i < (1 << 24) && !st; ++i) {
+      if (lane == 0) st = *m.gate >= need ? 1 : 0;
+      st = __shfl_sync(0xffffffffu, st, 0);
+      if (!st) __nanosleep(64);
+    }
+    if (st) open_gate();
+    else ok = 0;
   }
   if (lane == 0) {
     if (!ok) {
@@ -605,38 +684,55 @@ __global__ void __launch_bounds__(MV_THREADS, 1) mv_tma_kernel(MVArgs2 a) {
   mv_consume<VS, COMP>(a, m, c, warp - 1, lane);
 }
 
-// Grid-wide barrier of a cooperative launch (all CTAs resident).  bar[0] counts arrivals and
-// is zero between barriers; bar[1] is the generation.  A wait that runs past its limit sets
-// the error flag and returns false instead of hanging.
-__device__ bool mv_grid_sync(unsigned* bar, int* err, int* flag) {
-  __syncthreads();
-  if (threadIdx.x == 0) {
+// Grid-wide barrier of the consumer warps of a cooperative launch (all CTAs resident; the
+// producer warp of each CTA keeps streaming meanwhile): named barrier 1 over the consumer
+// threads, then thread 32 adds its arrival to the 64-bit counter *bar and waits until the
+// counter reaches this barrier's target.  The counter only grows: every launch passes the
+// same number of barriers with all CTAs, so it is a multiple of the grid size when a launch
+// starts, and barrier j of the launch completes at base + j * grid size.  One atomic and one
+// observation per CTA; nobody resets anything.  A wait that runs past its limit sets the
+// error flag and returns false instead of hanging.
+struct MVGridBar {
+  unsigned long long* ctr;
+  unsigned long long base;
+  int n;  // barriers passed in this launch
+};
+__device__ __forceinline__ unsigned long long ld_acquire_u64(const unsigned long long* p) {
+  unsigned long long v;
+  asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ bool mv_grid_sync_cons(MVGridBar& g, int* err, int* flag) {
+  asm volatile("bar.sync 1, %0;" ::"r"(MV_THREADS - 32) : "memory");
+  if (threadIdx.x == 32) {
     int ok = 1;
-    volatile unsigned* gen = bar + 1;
-    const unsigned g0 = *gen;
     __threadfence();
-    if (atomicAdd(bar, 1u) == gridDim.x - 1) {
-      atomicExch(bar, 0u);
-      __threadfence();
-      atomicAdd(bar + 1, 1u);
-    } else {
-      int i = 0;
-      while (*gen == g0) {
-        if (++i > (1 << 24)) {
-          ok = 0;
-          atomicOr(err, 4);
-          break;
-        }
-        __nanosleep(32);
+    asm volatile("red.release.gpu.global.add.u64 [%0], 1;" ::"l"(g.ctr) : "memory");
+    g.n += 1;
+    const unsigned long long target = g.base + (unsigned long long)g.n * gridDim.x;
+    int i = 0;
+    while (ld_acquire_u64(g.ctr) < target) {
+      if (++i > (1 << 24)) {
+        ok = 0;
+        atomicOr(err, 4);
+        break;
       }
+      __nanosleep(20);
     }
     __threadfence();
     *flag = ok;
   }
-  __syncthreads();
+  asm volatile("bar.sync 1, %0;" ::"r"(MV_THREADS - 32) : "memory");
   return *flag != 0;
 }
 
+// One whole matvec per launch.  Warp 0 of each CTA streams phase A from the start and phase B
+// right after it, issuing payloads and descriptors ahead of the grid barriers and parking the
+// input-range copies until the gate says the inputs are ready (gate 1: permuted x, after the
+// prologue barrier; gate 2: t in input form, after the phase-A barrier and the conversion).
+// The consumer warps do the prologue, the conversion and the epilogue with grid-stride loops
+// and hold the grid barriers.  The claim counters of the two phases are zero on entry (set at
+// operator build, reset again by the epilogue once every CTA has finished claiming).
 template <class VS, bool COMP>
 __global__ void __launch_bounds__(MV_THREADS, 1) mv_fused_kernel(MVFusedArgs f) {
   using D = typename MT<VS>::D;
@@ -646,51 +742,67 @@ __global__ void __launch_bounds__(MV_THREADS, 1) mv_fused_kernel(MVFusedArgs f) 
   const MVSmem m = mv_smem(smem);
   mv_init_barriers(m);
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const long long gtid = (long long)blockIdx.x * blockDim.x + tid, gstride = (long long)gridDim.x * blockDim.x;
   MVArgs2 a = f.a;
-  // prologue: permuted input, zeroed accumulators, zeroed claim counters
-  {
-    const D* x = (const D*)f.x;
-    X* xp = (X*)a.xp;
-    for (long long k = gtid; k < f.n_in; k += gstride) xp[k] = to_x<VS>(x[f.perm_in[k]]);
-    D* yp = (D*)a.yp;
-    for (long long k = gtid; k < f.n_out; k += gstride) yp[k] = D{};
-    D* t = (D*)a.t;
-    for (long long k = gtid; k < f.t_len; k += gstride) t[k] = D{};
-    if (gtid == 0) {
-      *f.ctr[0] = 0;
-      *f.ctr[1] = 0;
-    }
-  }
-  mv_grid_sync(f.bar, a.err, &bflag);
-  MVProd p;
-  MVCons c;
-  for (int ph = 0; ph < 2; ++ph) {
-    if (ph == 1) {
-      // t is complete: its input form for phase B
-      if constexpr (!std::is_same<VS, double>::value && !std::is_same<VS, cpx<double>>::value) {
-        const D* t = (const D*)a.t;
-        X* tx = (X*)a.tx;
-        for (long long k = gtid; k < f.t_len; k += gstride) tx[k] = to_x<VS>(t[k]);
-        mv_grid_sync(f.bar, a.err, &bflag);
-      }
-    }
+  auto set_phase = [&](int ph) {
     a.items = f.items[ph];
     a.pieces = f.pieces[ph];
     a.ranges = f.ranges[ph];
     a.nitems = f.nitems[ph];
-    if (a.nitems > 0) {
-      if (warp == 0) mv_produce(a, a.items, a.nitems, f.ctr[ph], m, p, lane);
-      else mv_consume<VS, COMP>(a, m, c, warp - 1, lane);
+  };
+  if (warp == 0) {
+    MVProd p;
+    for (int ph = 0; ph < 2; ++ph) {
+      set_phase(ph);
+      if (a.nitems > 0) mv_produce(a, a.items, a.nitems, f.ctr[ph], m, p, lane, ph + 1);
     }
-    mv_grid_sync(f.bar, a.err, &bflag);
+    return;
+  }
+  const long long ct = (long long)blockIdx.x * (MV_THREADS - 32) + (tid - 32);
+  const long long cs = (long long)gridDim.x * (MV_THREADS - 32);
+  MVGridBar gb{f.bar, 0ull, 0};
+  if (tid == 32) {
+    // no CTA of this launch can have passed its first barrier yet: round down to the launch's base
+    const unsigned long long c0 = ld_acquire_u64(f.bar);
+    gb.base = c0 - c0 % gridDim.x;
+  }
+  // prologue: permuted input, zeroed accumulators
+  {
+    const D* x = (const D*)f.x;
+    X* xp = (X*)a.xp;
+    for (long long k = ct; k < f.n_in; k += cs) xp[k] = to_x<VS>(x[f.perm_in[k]]);
+    D* yp = (D*)a.yp;
+    for (long long k = ct; k < f.n_out; k += cs) yp[k] = D{};
+    D* t = (D*)a.t;
+    for (long long k = ct; k < f.t_len; k += cs) t[k] = D{};
+  }
+  mv_grid_sync_cons(gb, a.err, &bflag);
+  if (tid == 32) *m.gate = 1;
+  MVCons c;
+  set_phase(0);
+  if (a.nitems > 0) mv_consume<VS, COMP>(a, m, c, warp - 1, lane);
+  mv_grid_sync_cons(gb, a.err, &bflag);
+  // t is complete: its input form for phase B
+  if constexpr (!std::is_same<VS, double>::value && !std::is_same<VS, cpx<double>>::value) {
+    const D* t = (const D*)a.t;
+    X* tx = (X*)a.tx;
+    for (long long k = ct; k < f.t_len; k += cs) tx[k] = to_x<VS>(t[k]);
+    mv_grid_sync_cons(gb, a.err, &bflag);
+  }
+  if (tid == 32) *m.gate = 2;
+  set_phase(1);
+  if (a.nitems > 0) mv_consume<VS, COMP>(a, m, c, warp - 1, lane);
+  mv_grid_sync_cons(gb, a.err, &bflag);
+  // every CTA has finished claiming: zero the claim counters for the next launch
+  if (blockIdx.x == 0 && tid == 32) {
+    *f.ctr[0] = 0;
+    *f.ctr[1] = 0;
   }
   // epilogue: y = alpha yp + beta y in the caller's numbering
   {
     const D* yp = (const D*)a.yp;
     D* y = (D*)f.y;
     const D al = mk_d<D>(f.alpha[0], f.alpha[1]), be = mk_d<D>(f.beta[0], f.beta[1]);
-    for (long long k = gtid; k < f.n_out; k += gstride) {
+    for (long long k = ct; k < f.n_out; k += cs) {
       D* dst = y + f.perm_out[k];
       D v = al * yp[k];
       if (f.use_beta) v += be * (*dst);
@@ -734,7 +846,8 @@ __global__ void __launch_bounds__(256) mv_multi_kernel(MVArgs2 a) {
 int mv_smem_bytes() {
   static_assert(16 * MV_NSTAGE + 16 <= 128 && sizeof(MVStageHdr) == 32 && sizeof(MVTItem) == 80,
                 "matvec header area");
-  return MV_HDR + MV_NSTAGE * (MV_STAGE + MV_MAXPC * (int)sizeof(MVPiece) + MV_INAREA);
+  return MV_HDR + MV_NSTAGE * (MV_STAGE + MV_MAXPC * (int)sizeof(MVPiece) + MV_INAREA) +
+         MV_NSTAGE * (int)sizeof(MVPend) + 16;
 }
 int mv_in_bytes() { return MV_INAREA; }
 int mv_max_pieces() { return MV_MAXPC; }

@@ -902,7 +902,7 @@ void HOperator::mult(int trans, const double* alpha, const void* x, const double
       f.nitems[ph] = n_items[p0 + ph];
       f.ctr[ph] = d_sched.as<int>() + 2 + ph;
     }
-    f.bar = (unsigned*)(d_sched.as<int>() + 4);
+    f.bar = (unsigned long long*)(d_sched.as<int>() + 4);
     f.perm_in = pin;
     f.n_in = in_n;
     f.x = x;
