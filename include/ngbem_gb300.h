@@ -194,7 +194,7 @@ int bem_operator_set_accuracy(bem_operator_t op, int compensated);
 
 /* Autotuner of the single right-hand-side matvec (no counterpart in the reference): times
  * `reps` applications for each candidate piece size (stored elements per warp task: 256, 384,
- * 512, 768, 1024) and schedule (one cooperative launch or the four-pass pipeline) and keeps the
+ * 512, 768, 1024, 1536, 2048) and schedule (one cooperative launch or the four-pass pipeline) and keeps the
  * fastest.  Outputs (may be NULL): the chosen piece size, 1 if the single launch won, and the
  * best time per matvec in milliseconds.  Synchronous; allocates two vectors. */
 int bem_operator_autotune(bem_operator_t op, int reps, int* piece, int* fused, double* ms);

@@ -81,7 +81,7 @@ __device__ __forceinline__ V kern_entry(const PtData<P>& x, const PtData<P>& y, 
 }
 
 template <int KID, class P>
-__global__ void __launch_bounds__(ACA_T) aca_kernel(AcaArgs a) {
+__global__ void __launch_bounds__(ACA_T, sizeof(P) == 4 ? 4 : 2) aca_kernel(AcaArgs a) {
   using G = Green<KID>;
   using V = VT<G::CPLX, P>;
   constexpr int NC = G::NC;

@@ -1570,7 +1570,7 @@ namespace bem {
 // matvecs with CUDA events after a warm-up; the fastest is kept.
 double HOperator::autotune(int reps, int* best_piece, int* best_fused) {
   if (reps < 1) reps = 1;
-  const int cand[] = {256, 384, 512, 768, 1024};
+  const int cand[] = {256, 384, 512, 768, 1024, 1536, 2048};
   const size_t esz = cplx ? 16 : 8;
   DevBuf x, y;
   x.alloc((size_t)width * esz);

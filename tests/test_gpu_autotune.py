@@ -18,6 +18,6 @@ def test_autotune_keeps_the_matvec(precision):
     x = torch.from_numpy(np.random.default_rng(5).standard_normal(m.nt)).cuda()
     y0 = (V.mat * x).cpu().numpy()
     t = V.mat.autotune(reps=3)
-    assert t["piece"] in (256, 384, 512, 768, 1024) and t["ms"] > 0
+    assert t["piece"] in (256, 384, 512, 768, 1024, 1536, 2048) and t["ms"] > 0
     y1 = (V.mat * x).cpu().numpy()
     assert np.linalg.norm(y1 - y0) / np.linalg.norm(y0) < 1e-12
