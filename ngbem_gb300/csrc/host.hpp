@@ -176,6 +176,9 @@ struct HOperator : OperatorBase {
   // single-launch matvec (4: t=V2 x and y+=Dx, 5: y+=U2 t; 6, 7 the same for the transpose)
   DevBuf d_items[MV_NPASS], d_pieces[MV_NPASS], d_ranges[MV_NPASS];
   int n_items[MV_NPASS] = {};
+  // several right-hand sides, not transposed: one piece per block (passes 0 and 1)
+  DevBuf d_mr_items[2], d_mr_pieces[2];
+  int n_mr_items[2] = {0, 0};
   bool mv_fused = true;  // one cooperative launch per single-RHS matvec (else the 4-pass pipeline)
   int mv_piece = 0;      // stored elements per piece (0: the kernel's default); set by autotune
   double autotune(int reps, int* best_piece, int* best_fused);

@@ -109,6 +109,7 @@ struct MVArgs2 {
   int in_esz;        // bytes of one staged input value (x or t entry: 8 real, 16 complex)
   int* err;
   int* sched;        // two zeroed counters (items claimed, CTAs finished); left zero after a pass
+  int chunked;       // several right-hand sides: items are single-piece chunks (chunk kernel)
 };
 // passes per operator: 0-3 the four-pass pipeline, 4-7 the phases of the single-launch matvec
 #define MV_NPASS 8

@@ -843,6 +843,74 @@ __global__ void __launch_bounds__(256) mv_multi_kernel(MVArgs2 a) {
   }
 }
 
+// Several right-hand sides over chunk items (one piece per chunk, lane = right-hand side).
+// Long reductions (Kc >= MV_MC_SPLIT: dense and V2 column chunks): the 8 warps split the
+// columns, each keeps partial sums for MV_MR rows in registers (one input load feeds MV_MR
+// products), and the partials are added across warps in shared memory before a single atomic
+// per output row and right-hand side.  Short reductions (U2 chunks, Kc = rank): the warps
+// split the rows and each row is reduced by one warp.
+#define MV_MR 8
+#define MV_MC_SPLIT 64
+template <class VS, bool COMP>
+__global__ void __launch_bounds__(256) mv_multi_chunk_kernel(MVArgs2 a) {
+  using AccT = typename AccSel<VS, COMP>::type;
+  using X = typename MT<VS>::X;
+  using D = typename MT<VS>::D;
+  __shared__ D part[8][MV_MR][32];
+  const MVTItem item = a.items[blockIdx.x];
+  const MVPiece pc = a.pieces[item.seg0];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const VS* A = (const VS*)((const unsigned char*)item.src + pc.soff);
+  const X* xin = (const X*)((pc.flags & 1) ? a.tx : a.xp);
+  D* out = ((pc.flags & 2) ? (D*)a.t : (D*)a.yp) + (size_t)pc.out_off * a.nrhs;
+  const int nr = a.nrhs;
+  if (pc.Kc < MV_MC_SPLIT) {
+    for (int o = warp; o < pc.O; o += 8)
+      for (int g = 0; g < nr; g += 32) {
+        const int rh = g + lane;
+        if (rh >= nr) continue;
+        AccT acc;
+        const X* xk = xin + (size_t)pc.in_off * nr + rh;
+        for (int k = 0; k < pc.Kc; ++k) acc.add(A[(long long)o * pc.so + (long long)k * pc.sk], xk[(size_t)k * nr]);
+        atomic_add(out + (size_t)o * nr + rh, acc.val());
+      }
+    return;
+  }
+  const int k0 = (int)(((long long)pc.Kc * warp) / 8), k1 = (int)(((long long)pc.Kc * (warp + 1)) / 8);
+  for (int o0 = 0; o0 < pc.O; o0 += MV_MR) {
+    const int no = min(MV_MR, pc.O - o0);
+    for (int g = 0; g < nr; g += 32) {
+      const int rh = g + lane;
+      AccT acc[MV_MR];
+      if (rh < nr) {
+        const X* xk = xin + (size_t)(pc.in_off + k0) * nr + rh;
+        const VS* Ak = A + (long long)o0 * pc.so + (long long)k0 * pc.sk;
+        for (int k = k0; k < k1; ++k) {
+          const X xv = *xk;
+#pragma unroll
+          for (int r = 0; r < MV_MR; ++r)
+            if (r < no) acc[r].add(Ak[(long long)r * pc.so], xv);
+          xk += nr;
+          Ak += pc.sk;
+        }
+      }
+#pragma unroll
+      for (int r = 0; r < MV_MR; ++r) part[warp][r][lane] = acc[r].val();
+      __syncthreads();
+      {
+        const int r = tid >> 5, l = tid & 31;  // 256 threads = MV_MR rows x 32 lanes
+        if (r < no && g + l < nr) {
+          D sum = part[0][r][l];
+#pragma unroll
+          for (int w = 1; w < 8; ++w) sum += part[w][r][l];
+          atomic_add(out + (size_t)(o0 + r) * nr + g + l, sum);
+        }
+      }
+      __syncthreads();
+    }
+  }
+}
+
 int mv_smem_bytes() {
   static_assert(16 * MV_NSTAGE + 16 <= 128 && sizeof(MVStageHdr) == 32 && sizeof(MVTItem) == 80,
                 "matvec header area");
@@ -863,6 +931,8 @@ static void pass_t(const MVArgs2& a, int grid, cudaStream_t s) {
       attr = true;
     }
     mv_tma_kernel<VS, COMP><<<std::min(grid, a.nitems), MV_THREADS, smem, s>>>(a);
+  } else if (a.chunked) {
+    mv_multi_chunk_kernel<VS, COMP><<<a.nitems, 256, 0, s>>>(a);
   } else {
     mv_multi_kernel<VS, COMP><<<a.nitems, 256, 0, s>>>(a);
   }

@@ -847,6 +847,41 @@ void HOperator::build_mv_items() {
     }
   }
   info.mv_segments = (int)npieces;
+  // lists for several right-hand sides (the pass kernel reads the blocks in place there): one
+  // piece per span (a dense column chunk, a V2 column chunk, a U2 row chunk, each at most one
+  // stage of bytes), so a piece reduces over the whole chunk and each output row receives one
+  // atomic per chunk instead of one per column slice; chunks keep the items balanced
+  {
+    std::vector<MVTItem> mi[2];
+    std::vector<MVPiece> mp[2];
+    auto add = [&](int ph, unsigned long long src, MVPiece pc) {
+      pc.ow = std::min(pc.O, 32);
+      pc.groups = 32 / pc.ow;
+      pc.inv_ow = 1.0f / (float)pc.ow;
+      MVTItem it{};
+      it.src = src;
+      it.seg0 = (int)mp[ph].size();
+      it.nseg = 1;
+      it.inbytes = -1;
+      mp[ph].push_back(pc);
+      mi[ph].push_back(it);
+    };
+    // first piece of a span gives (kind, block, first row/column); the count is the span's total
+    auto whole = [&](const Span& sp, const std::vector<GPiece>& pool, int sem) {
+      GPiece g = pool[sp.p0];
+      for (int q = 1; q < sp.np; ++q) g.cnt += pool[sp.p0 + q].cnt;
+      g.soff = 0;
+      return piece_raw(sem, g);
+    };
+    for (const Span& sp : sv) add(0, sp.src, whole(sp, pv, 0));
+    for (const Span& sp : sd) add(1, sp.src, whole(sp, pd, 1));
+    for (const Span& sp : su) add(1, sp.src, whole(sp, pu, 1));
+    for (int ph = 0; ph < 2; ++ph) {
+      d_mr_items[ph].upload(mi[ph]);
+      d_mr_pieces[ph].upload(mp[ph]);
+      n_mr_items[ph] = (int)mi[ph].size();
+    }
+  }
   d_mvdense.upload(mvdense);
   d_mvlr.upload(mvlr);
   d_err.alloc(sizeof(int));
@@ -948,6 +983,12 @@ void HOperator::mult(int trans, const double* alpha, const void* x, const double
     a.pieces = d_pieces[a.pass].as<MVPiece>();
     a.ranges = d_ranges[a.pass].as<MVRange>();
     a.nitems = n_items[a.pass];
+    if (nrhs > 1 && !trans) {
+      a.items = d_mr_items[0].as<MVTItem>();
+      a.pieces = d_mr_pieces[0].as<MVPiece>();
+      a.nitems = n_mr_items[0];
+      a.chunked = 1;
+    }
     launch_mv_pass(prec, cplx, a, mv_grid, s);
     launch_t_to_x(prec, cplx, d_t.p, d_tx.p, (long long)t_len * nrhs, s);
   }
@@ -957,6 +998,13 @@ void HOperator::mult(int trans, const double* alpha, const void* x, const double
   a.pieces = d_pieces[a.pass].as<MVPiece>();
   a.ranges = d_ranges[a.pass].as<MVRange>();
   a.nitems = n_items[a.pass];
+  a.chunked = 0;
+  if (nrhs > 1 && !trans) {
+    a.items = d_mr_items[1].as<MVTItem>();
+    a.pieces = d_mr_pieces[1].as<MVPiece>();
+    a.nitems = n_mr_items[1];
+    a.chunked = 1;
+  }
   launch_mv_pass(prec, cplx, a, mv_grid, s);
   if (profiling) BEM_CUDA(cudaEventRecord(ev[3], s));
   launch_permute_out(cplx, pout, out_n, nrhs, out_n, alpha, beta, d_yp.p, y, s);
