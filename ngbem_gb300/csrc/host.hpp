@@ -179,6 +179,8 @@ struct HOperator : OperatorBase {
   // several right-hand sides, not transposed: one piece per block (passes 0 and 1)
   DevBuf d_mr_items[2], d_mr_pieces[2];
   int n_mr_items[2] = {0, 0};
+  DevBuf d_ro_leaves, d_ro_ents;  // owner-computes lists of the second pass (several right-hand sides)
+  int n_ro_leaves = 0;
   bool mv_fused = true;  // one cooperative launch per single-RHS matvec (else the 4-pass pipeline)
   int mv_piece = 0;      // stored elements per piece (0: the kernel's default); set by autotune
   double autotune(int reps, int* best_piece, int* best_fused);

@@ -175,6 +175,23 @@ void launch_sle(const SLEArgs& a, bool fp64, bool grad, cudaStream_t s);
 
 // prec 0: fp64 storage, 1: fp32 storage.  cplx: complex operator.
 void launch_mv_pass(int prec, bool cplx, const MVArgs2& a, int grid, cudaStream_t s);
+// y += D x + U2 t for several right-hand sides, owner computes: one CTA per leaf row cluster
+// gathers every dense block and low-rank U2 row slice that touches its rows, adds them up in
+// shared memory and stores its rows of y (no global atomics).  entries: {kind (0 dense,
+// 1 low rank), block, first local row, rows}; leaves: {first row, end row, first entry, end}.
+struct MVRowArgs {
+  const int4* leaves;
+  int nleaves;
+  const int4* ents;
+  const MVDense* dense;
+  const LRDesc* lr;
+  const void* xp;   // permuted x (input form)
+  const void* tx;   // t (input form)
+  void* yp;         // permuted y (FP64 / complex128), written
+  int nrhs;
+  int compensated;
+};
+void launch_mv_rowowner(int prec, bool cplx, const MVRowArgs& a, cudaStream_t s);
 int mv_stage_bytes();
 int mv_piece_elems();  // target stored elements per piece
 // tx = t in the input form (no-op for fp64 storage, where tx aliases t)

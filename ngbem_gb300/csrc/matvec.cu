@@ -77,6 +77,13 @@ __device__ __forceinline__ float4 split_x(cpx<double> v) {
 }
 __device__ __forceinline__ double split_x_d(double v) { return v; }
 
+// FP64 additions into shared memory (several warps add to one row)
+__device__ __forceinline__ void shared_add(double* p, double v) { atomicAdd(p, v); }
+__device__ __forceinline__ void shared_add(cpx<double>* p, cpx<double> v) {
+  atomicAdd(&p->x, v.x);
+  atomicAdd(&p->y, v.y);
+}
+
 template <class VS> __device__ __forceinline__ typename MT<VS>::X to_x(typename MT<VS>::D v);
 template <> __device__ __forceinline__ float2 to_x<float>(double v) { return split_x(v); }
 template <> __device__ __forceinline__ double to_x<double>(double v) { return v; }
@@ -908,6 +915,98 @@ __global__ void __launch_bounds__(256) mv_multi_chunk_kernel(MVArgs2 a) {
       }
       __syncthreads();
     }
+  }
+}
+
+#define MV_RO_ROWS 64
+template <class VS, bool COMP>
+__global__ void __launch_bounds__(256) mv_rowowner_kernel(MVRowArgs a) {
+  using AccT = typename AccSel<VS, COMP>::type;
+  using X = typename MT<VS>::X;
+  using D = typename MT<VS>::D;
+  __shared__ D ysm[MV_RO_ROWS][32];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int4 L = a.leaves[blockIdx.x];  // rows [L.x, L.y), entries [L.z, L.w)
+  const int nr = a.nrhs;
+  const X* xp = (const X*)a.xp;
+  const X* tx = (const X*)a.tx;
+  D* yp = (D*)a.yp;
+  for (int t0 = L.x; t0 < L.y; t0 += MV_RO_ROWS) {
+    const int t1 = min(L.y, t0 + MV_RO_ROWS);
+    for (int g = 0; g < nr; g += 32) {
+      for (int q = tid; q < MV_RO_ROWS * 32; q += 256) ysm[q >> 5][q & 31] = D{};
+      __syncthreads();
+      const int rh = g + lane;
+      for (int e = L.z + warp; e < L.w; e += 8) {
+        const int4 E = a.ents[e];
+        // rows of this entry (global, permuted) inside the tile
+        int i0, i1, gr0;
+        if (E.x == 0) gr0 = a.dense[E.y].r0;
+        else gr0 = a.lr[E.y].r0;
+        i0 = max(t0, gr0 + E.z);
+        i1 = min(t1, gr0 + E.z + E.w);
+        if (rh >= nr) continue;
+        for (int ib = i0; ib < i1; ib += MV_MR) {
+          const int no = min(MV_MR, i1 - ib);
+          AccT acc[MV_MR];
+          if (E.x == 0) {
+            const MVDense Dd = a.dense[E.y];
+            const VS* A = (const VS*)Dd.ptr + (ib - Dd.r0);
+            const X* xk = xp + (size_t)Dd.c0 * nr + rh;
+            for (int k = 0; k < Dd.n; ++k) {
+              const X xv = xk[(size_t)k * nr];
+              const VS* Ak = A + (long long)k * Dd.m;
+#pragma unroll
+              for (int r = 0; r < MV_MR; ++r)
+                if (r < no) acc[r].add(Ak[r], xv);
+            }
+          } else {
+            const LRDesc Lr = a.lr[E.y];
+            const VS* U = (const VS*)Lr.u;
+            long long base[MV_MR];
+#pragma unroll
+            for (int r = 0; r < MV_MR; ++r) {
+              const int i = ib - Lr.r0 + (r < no ? r : 0);
+              base[r] = lr_u_index(Lr, i, 0);
+            }
+            const X* xk = tx + (size_t)Lr.toff * nr + rh;
+            for (int k = 0; k < Lr.R; ++k) {
+              const X xv = xk[(size_t)k * nr];
+#pragma unroll
+              for (int r = 0; r < MV_MR; ++r)
+                if (r < no) acc[r].add(U[base[r] + (long long)k * Lr.cu], xv);
+            }
+          }
+#pragma unroll
+          for (int r = 0; r < MV_MR; ++r)
+            if (r < no) shared_add(&ysm[ib + r - t0][lane], acc[r].val());
+        }
+      }
+      __syncthreads();
+      for (int q = tid; q < (t1 - t0) * 32; q += 256) {
+        const int i = q >> 5, l = q & 31;
+        if (g + l < nr) yp[(size_t)(t0 + i) * nr + g + l] = ysm[i][l];
+      }
+      __syncthreads();
+    }
+  }
+}
+
+template <class VS, bool COMP>
+static void rowowner_t(const MVRowArgs& a, cudaStream_t s) {
+  if (a.nleaves > 0) mv_rowowner_kernel<VS, COMP><<<a.nleaves, 256, 0, s>>>(a);
+}
+
+void launch_mv_rowowner(int prec, bool cplx, const MVRowArgs& a, cudaStream_t s) {
+  if (prec == 0) {
+    if (cplx) rowowner_t<cpx<double>, true>(a, s);
+    else rowowner_t<double, true>(a, s);
+  } else if (a.compensated) {
+    if (cplx) rowowner_t<cpx<float>, true>(a, s);
+    else rowowner_t<float, true>(a, s);
+  } else {
+    if (cplx) rowowner_t<cpx<float>, false>(a, s);
+    else rowowner_t<float, false>(a, s);
   }
 }
 

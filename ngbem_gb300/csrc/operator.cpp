@@ -876,6 +876,34 @@ void HOperator::build_mv_items() {
     for (const Span& sp : sv) add(0, sp.src, whole(sp, pv, 0));
     for (const Span& sp : sd) add(1, sp.src, whole(sp, pd, 1));
     for (const Span& sp : su) add(1, sp.src, whole(sp, pu, 1));
+    // owner-computes lists of y += D x + U2 t: per leaf row cluster, every dense block and
+    // low-rank U2 row slice that touches its rows (blocks split along the leaf boundaries)
+    {
+      std::vector<std::pair<int, int>> lv;  // leaf rows [first, end)
+      for (const ClusterH& C : ttest->cl)
+        if (C.Child1 < 0) lv.push_back({(int)C.PermuPos, (int)(C.PermuPos + C.Number)});
+      std::sort(lv.begin(), lv.end());
+      std::vector<std::vector<int4>> per(lv.size());
+      auto add_rows = [&](int kind, int blk, int r0, int m) {
+        int l = (int)(std::upper_bound(lv.begin(), lv.end(), std::make_pair(r0, INT_MAX)) - lv.begin()) - 1;
+        for (l = std::max(l, 0); l < (int)lv.size() && lv[l].first < r0 + m; ++l) {
+          const int a0 = std::max(r0, lv[l].first), a1 = std::min(r0 + m, lv[l].second);
+          if (a1 > a0) per[l].push_back(make_int4(kind, blk, a0 - r0, a1 - a0));
+        }
+      };
+      for (int k = 0; k < (int)mvdense.size(); ++k) add_rows(0, k, mvdense[k].r0, mvdense[k].m);
+      for (int f = 0; f < (int)mvlr.size(); ++f)
+        if (mvlr[f].R > 0) add_rows(1, f, mvlr[f].r0, mvlr[f].m);
+      std::vector<int4> leaves, ents;
+      for (size_t l = 0; l < lv.size(); ++l) {
+        const int e0 = (int)ents.size();
+        ents.insert(ents.end(), per[l].begin(), per[l].end());
+        leaves.push_back(make_int4(lv[l].first, lv[l].second, e0, (int)ents.size()));
+      }
+      d_ro_leaves.upload(leaves);
+      d_ro_ents.upload(ents);
+      n_ro_leaves = (int)leaves.size();
+    }
     for (int ph = 0; ph < 2; ++ph) {
       d_mr_items[ph].upload(mi[ph]);
       d_mr_pieces[ph].upload(mp[ph]);
@@ -999,13 +1027,30 @@ void HOperator::mult(int trans, const double* alpha, const void* x, const double
   a.ranges = d_ranges[a.pass].as<MVRange>();
   a.nitems = n_items[a.pass];
   a.chunked = 0;
-  if (nrhs > 1 && !trans) {
+  if (nrhs > 1 && !trans && prec == 0) {
     a.items = d_mr_items[1].as<MVTItem>();
     a.pieces = d_mr_pieces[1].as<MVPiece>();
     a.nitems = n_mr_items[1];
     a.chunked = 1;
+    launch_mv_pass(prec, cplx, a, mv_grid, s);
+  } else if (nrhs > 1 && !trans) {
+    // FP32 storage, owner computes: each leaf row cluster sums its dense and U2 contributions
+    // and stores y (FP64 storage keeps the chunk pass: its wider accumulators favour it)
+    MVRowArgs ra{};
+    ra.leaves = d_ro_leaves.as<int4>();
+    ra.nleaves = n_ro_leaves;
+    ra.ents = d_ro_ents.as<int4>();
+    ra.dense = d_mvdense.as<MVDense>();
+    ra.lr = d_mvlr.as<LRDesc>();
+    ra.xp = d_xp.p;
+    ra.tx = prec == 0 ? d_t.p : d_tx.p;
+    ra.yp = d_yp.p;
+    ra.nrhs = nrhs;
+    ra.compensated = mv_compensated;
+    launch_mv_rowowner(prec, cplx, ra, s);
+  } else {
+    launch_mv_pass(prec, cplx, a, mv_grid, s);
   }
-  launch_mv_pass(prec, cplx, a, mv_grid, s);
   if (profiling) BEM_CUDA(cudaEventRecord(ev[3], s));
   launch_permute_out(cplx, pout, out_n, nrhs, out_n, alpha, beta, d_yp.p, y, s);
   if (profiling) {
