@@ -5,6 +5,8 @@
 // :379-407, ClusterTree ctor :409-453) with a documented 3x3 eigen solver in place of LAPACK
 // dsyev; the partition restates Rja_AdmissiblePair (:457-471) and HMatrix_help (:587-612).
 #include <algorithm>
+#include <thread>
+#include <atomic>
 #include <cmath>
 #include <numeric>
 #include <unordered_map>
@@ -295,6 +297,28 @@ static void cluster_data(const SpaceH& sp, std::vector<double>& G, std::vector<s
   for (int i = 0; i < ndof; ++i) G[i] /= (double)cnt[i];
 }
 
+// Runs f(i) for i in [0, n) on up to 16 host threads (or inline when n is small).
+template <class F>
+static void parallel_for(int n, int min_per_thread, F&& f) {
+  const int nth = (int)std::min<unsigned>(16u, std::max(1u, std::thread::hardware_concurrency()));
+  const int use = std::min(nth, std::max(1, n / std::max(1, min_per_thread)));
+  if (use <= 1) {
+    for (int i = 0; i < n; ++i) f(i);
+    return;
+  }
+  std::atomic<int> next{0};
+  std::vector<std::thread> th;
+  for (int t = 0; t < use; ++t)
+    th.emplace_back([&] {
+      for (int i = next++; i < n; i = next++) f(i);
+    });
+  for (auto& t : th) t.join();
+}
+
+// PCA bisection tree (reference Rja_ClusterTree, src/hmat.cpp:155-407), breadth first.  The
+// clusters of one level own disjoint ranges of the permutation, so a level is split on parallel
+// threads; the children are then appended in cluster order, which gives the numbering of the
+// one-cluster-at-a-time traversal.  Each cluster's arithmetic is the serial one (bit-identical).
 void ClusterTreeH::build(const SpaceH& sp, int leafsize) {
   std::vector<double> G;
   std::vector<std::array<double, 3>> X;
@@ -306,7 +330,8 @@ void ClusterTreeH::build(const SpaceH& sp, int leafsize) {
   ClusterH root;
   root.Number = n;
   cl.push_back(root);
-  for (size_t ic = 0; ic < cl.size(); ++ic) {
+  struct Split { int n1 = 0, n2 = 0; bool split = false; };
+  auto process = [&](size_t ic, Split& out) {
     const int cnum = (int)cl[ic].Number;
     const int b = (int)cl[ic].PermuPos;
     const int e = b + cnum - 1;
@@ -373,7 +398,7 @@ void ClusterTreeH::build(const SpaceH& sp, int leafsize) {
       for (int k = 0; k < 9; ++k) C.EVec[k] = A[k];
       C.Child1 = C.Child2 = -1;
     }
-    if (cnum <= leafsize) continue;
+    if (cnum <= leafsize) return;
     // split on the principal axis by an in-place swap partition
     int n1 = 0, n2 = 0, chk = b, end = e;
     const double crit = ctr[0] * A[6] + ctr[1] * A[7] + ctr[2] * A[8];
@@ -389,18 +414,31 @@ void ClusterTreeH::build(const SpaceH& sp, int leafsize) {
         --end;
       }
     }
-    if (n1 == 0 || n2 == 0) continue;
-    ClusterH c1, c2;
-    c1.Level = c2.Level = cl[ic].Level + 1;
-    c1.Parent = c2.Parent = (long)ic;
-    c1.Number = n1;
-    c1.PermuPos = b;
-    c2.Number = n2;
-    c2.PermuPos = b + n1;
-    cl[ic].Child1 = (long)cl.size();
-    cl[ic].Child2 = (long)cl.size() + 1;
-    cl.push_back(c1);
-    cl.push_back(c2);
+    out.n1 = n1;
+    out.n2 = n2;
+    out.split = n1 > 0 && n2 > 0;
+  };
+  std::vector<Split> res;
+  for (size_t lo = 0; lo < cl.size();) {
+    const size_t hi = cl.size();
+    res.assign(hi - lo, Split{});
+    parallel_for((int)(hi - lo), 1, [&](int k) { process(lo + k, res[k]); });
+    for (size_t ic = lo; ic < hi; ++ic) {
+      const Split& sr = res[ic - lo];
+      if (!sr.split) continue;
+      ClusterH c1, c2;
+      c1.Level = c2.Level = cl[ic].Level + 1;
+      c1.Parent = c2.Parent = (long)ic;
+      c1.Number = sr.n1;
+      c1.PermuPos = cl[ic].PermuPos;
+      c2.Number = sr.n2;
+      c2.PermuPos = cl[ic].PermuPos + sr.n1;
+      cl[ic].Child1 = (long)cl.size();
+      cl[ic].Child2 = (long)cl.size() + 1;
+      cl.push_back(c1);
+      cl.push_back(c2);
+    }
+    lo = hi;
   }
   pinv.assign(n, 0);
   for (int k = 0; k < n; ++k) pinv[perm[k]] = k;
