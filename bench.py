@@ -569,22 +569,37 @@ def run_bm(args):
         torch.cuda.synchronize()
         mv_comp = e0.elapsed_time(e1) / 5
         mv_fast = mv_comp
-        if prec == "mixed":  # plain FP32 products (the GMRES inner iterations)
-            Cop.mat.set_accuracy(False)
-            Cop.mat.Mult(F, Y)
-            e0.record()
-            for _ in range(5):
+        extra = {}
+        if prec == "mixed":
+            # plain accuracy (the GMRES inner iterations): tensor-core low-rank products, then
+            # the CUDA-core products of the same operator for comparison
+            def timed_mult(reps=5):
                 Cop.mat.Mult(F, Y)
-            e1.record()
-            torch.cuda.synchronize()
-            mv_fast = e0.elapsed_time(e1) / 5
+                e0.record()
+                for _ in range(reps):
+                    Cop.mat.Mult(F, Y)
+                e1.record()
+                torch.cuda.synchronize()
+                return e0.elapsed_time(e1) / reps
+            Ycomp = Y.cpu().numpy()
+            Cop.mat.set_accuracy(False)
+            tc = Cop.mat.tensor_cores()
+            mv_fast = timed_mult()
+            Yt = Y.cpu().numpy()
+            Cop.mat.set_tensor_cores(False)
+            mv_cc = timed_mult()
+            Ycc = Y.cpu().numpy()
+            Cop.mat.set_tensor_cores(True)
             Cop.mat.set_accuracy(True)
+            extra = {"tensor_cores": tc, "matvec32_cuda_core_fast_ms": mv_cc,
+                     "matvec32_fast_rel_err_vs_compensated": float(np.linalg.norm(Yt - Ycomp) / np.linalg.norm(Ycomp)),
+                     "matvec32_cuda_core_fast_rel_err": float(np.linalg.norm(Ycc - Ycomp) / np.linalg.norm(Ycomp))}
         info = Cop.mat.info
         out[prec] = {"assembly_s": t1 - t0, "solve_s": t2 - t1, "total_s": t2 - t0,
                      "iterations": last["iterations"], "max_residual": last["residual"],
                      "matvec32_ms": mv_comp, "matvec32_fast_ms": mv_fast, "nze": info["nze"],
                      "max_rank": info["max_rank"],
-                     "bytes": info["bytes_dense"] + info["bytes_lowrank"], "nfallback": info["nfallback"]}
+                     "bytes": info["bytes_dense"] + info["bytes_lowrank"], "nfallback": info["nfallback"], **extra}
         sols[prec] = U.cpu().numpy()
         del Cop, U, Y
         torch.cuda.empty_cache()

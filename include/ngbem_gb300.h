@@ -199,6 +199,25 @@ int bem_operator_set_accuracy(bem_operator_t op, int compensated);
  * best time per matvec in milliseconds.  Synchronous; allocates two vectors. */
 int bem_operator_autotune(bem_operator_t op, int reps, int* piece, int* fused, double* ms);
 
+/* Tensor-core products for several right-hand sides (no counterpart in the reference, which
+ * applies HMatrix::MultAdd, src/hmat.cpp:647-655, one vector at a time).  For complex
+ * operators with FP32 storage, plain accuracy (bem_operator_set_accuracy(op, 0)) and 2..32
+ * right-hand sides, bem_operator_mult runs the low-rank products T = V2 X and Y += U2 T on the
+ * tcgen05 tensor cores with split-TF32 operands (high + low parts, FP32 accumulation; about
+ * 1e-6 relative) and the dense blocks on CUDA cores.  The packed operand panels (about twice
+ * the low-rank storage) are built on the first such call outside a stream capture, or here.
+ * enable = 1 (default) builds them now when the operator qualifies; 0 turns the path off and
+ * frees them.  bem_operator_tensor_cores reports the state (1 built, 0 not built, -1 the
+ * operator or device does not qualify), the device bytes of the panels, the work items of the
+ * two passes and the build time in ms (outputs may be NULL). */
+int bem_operator_set_tensor_cores(bem_operator_t op, int enable);
+int bem_operator_tensor_cores(bem_operator_t op, int* state, long long* bytes, int* items0, int* items1,
+                              double* ms_build);
+
+/* Known-answer check of the tensor-core encodings on the current device (one 128 x 32 x 16
+ * split-TF32 product of exactly representable values).  passed = 1 when every entry is exact. */
+int bem_tc_selftest(int* passed);
+
 /* Diagnostics (no counterpart in the reference, whose Timer/RegionTimer instrumentation at
  * src/hmat.cpp:650 plays this role): when enabled, every bem_operator_mult records CUDA
  * events on its stream around its four launches; bem_operator_kernel_times returns the

@@ -31,7 +31,8 @@ __all__ = ["SurfaceL2", "H1", "HDivSurface", "TraceSpace", "BaseMatrix", "HMatri
            "HelmholtzSingleLayerPotentialOperator", "HelmholtzDoubleLayerPotentialOperator",
            "HelmholtzCombinedFieldOperator", "HelmholtzHypersingularOperator",
            "MaxwellSingleLayerPotentialOperator", "MaxwellSingleLayerPotentialOperatorCurl",
-           "MaxwellDoubleLayerPotentialOperator", "MassOperator", "GMRes", "cluster_tree", "partition"]
+           "MaxwellDoubleLayerPotentialOperator", "MassOperator", "GMRes", "cluster_tree", "partition",
+           "tc_selftest"]
 
 
 def _torch():
@@ -129,6 +130,13 @@ def cluster_tree(space: TraceSpace, leafsize: int = 40):
                                ci.ctypes.data_as(_lib._lp), cd.ctypes.data_as(_lib._dp)))
     n = nc.value
     return perm, ci[: 7 * n].reshape(n, 7), cd[: 23 * n].reshape(n, 23)
+
+
+def tc_selftest() -> bool:
+    """Known-answer check of the tensor-core encodings on the current GPU (True: exact)."""
+    ok = C.c_int()
+    check(lib.bem_tc_selftest(C.byref(ok)))
+    return bool(ok.value)
 
 
 def partition(trial: TraceSpace, test: TraceSpace | None = None, leafsize: int = 40, eta: float = 2.0):
@@ -350,6 +358,18 @@ class HMatrix(_NativeMatrix):
         check(lib.bem_operator_autotune(self.h, int(reps), C.byref(piece), C.byref(fused), C.byref(ms)))
         self.tuned = {"piece": piece.value, "fused": bool(fused.value), "ms": ms.value}
         return self.tuned
+
+    def set_tensor_cores(self, enable: bool = True):
+        """Tensor-core products for 2..32 right-hand sides at plain accuracy (complex FP32 storage):
+        True builds the packed panels now when the operator qualifies, False turns them off."""
+        check(lib.bem_operator_set_tensor_cores(self.h, int(bool(enable))))
+
+    def tensor_cores(self) -> dict:
+        """State of the tensor-core path: 1 built, 0 not built, -1 not applicable."""
+        st, nb_, i0, i1, ms = C.c_int(), C.c_longlong(), C.c_int(), C.c_int(), C.c_double()
+        check(lib.bem_operator_tensor_cores(self.h, C.byref(st), C.byref(nb_), C.byref(i0), C.byref(i1),
+                                            C.byref(ms)))
+        return {"state": st.value, "bytes": nb_.value, "items": (i0.value, i1.value), "ms_build": ms.value}
 
     def set_profiling(self, enable: bool = True):
         check(lib.bem_operator_set_profiling(self.h, int(bool(enable))))

@@ -273,6 +273,42 @@ int bem_operator_set_accuracy(bem_operator_t op, int compensated) {
   });
 }
 
+int bem_operator_set_tensor_cores(bem_operator_t op, int enable) {
+  return guarded([&] {
+    REQUIRE(op, "null argument");
+    auto* h = dynamic_cast<HOperator*>(op->op.get());
+    if (!h) throw Error(BEM_ERR_STATE, "not an H-matrix operator");
+    if (!enable) {
+      h->release_tc();
+      h->tc_mode = 0;
+      return;
+    }
+    h->tc_mode = 1;
+    if (h->tc_state == 0) h->build_tc();
+  });
+}
+
+int bem_operator_tensor_cores(bem_operator_t op, int* state, long long* bytes, int* items0, int* items1,
+                              double* ms_build) {
+  return guarded([&] {
+    REQUIRE(op, "null argument");
+    auto* h = dynamic_cast<HOperator*>(op->op.get());
+    if (!h) throw Error(BEM_ERR_STATE, "not an H-matrix operator");
+    if (state) *state = h->tc_mode ? h->tc_state : 0;
+    if (bytes) *bytes = h->tc_bytes;
+    if (items0) *items0 = h->tc_items[0];
+    if (items1) *items1 = h->tc_items[1];
+    if (ms_build) *ms_build = h->tc_ms_build;
+  });
+}
+
+int bem_tc_selftest(int* passed) {
+  return guarded([&] {
+    REQUIRE(passed, "null argument");
+    *passed = tc_selftest();
+  });
+}
+
 int bem_operator_autotune(bem_operator_t op, int reps, int* piece, int* fused, double* ms) {
   return guarded([&] {
     REQUIRE(op, "null argument");

@@ -191,6 +191,20 @@ struct HOperator : OperatorBase {
   int ws_nrhs = 0;
   std::vector<MVDense> mvdense;
   std::vector<MVLowRank> mvlr;
+  // tensor-core products for 2..32 right-hand sides at plain accuracy (complex FP32 storage;
+  // tc_host.cpp, tc_matvec.cu): packed operand panels built on first use
+  int tc_mode = 1;   // 0: off (CUDA-core products)
+  int tc_state = 0;  // 0 not built, 1 built, -1 not applicable to this operator or device
+  DevBuf d_tc_xa, d_tc_ta, d_tc_vp, d_tc_up, d_tc_y;
+  DevBuf d_tc_items[2], d_tc_segs[2], d_tc_sched[2], d_tc_outs;
+  DevBuf d_ro_leaves_tc, d_ro_ents_tc;
+  int tc_grid[2] = {0, 0}, tc_items[2] = {0, 0}, tc_nkc_x = 0, n_ro_leaves_tc = 0;
+  long long tc_bytes = 0;
+  double tc_ms_build = 0.0;
+  bool tc_eligible(int trans, int nrhs, cudaStream_t s);
+  void build_tc();
+  void release_tc();
+  void mult_tc(const double* alpha, const void* x, const double* beta, void* y, int nrhs, cudaStream_t s);
   bem_operator_info_t info{};
   // optional per-kernel timing of mult (CUDA events on the launch stream)
   bool profiling = false;
@@ -240,6 +254,9 @@ struct SLBatch {
 
 // op.mult with the scratch taken from a fixed device array instead of operator buffers
 // (mult_noalloc.cu); allocates nothing.
+// 1 when the tensor-core encodings passed their known-answer product on this device (run once)
+int tc_selftest();
+
 void mult_noalloc(HOperator& op, int trans, const double* alpha, const void* x, const double* beta, void* y,
                   int nrhs, cudaStream_t s);
 

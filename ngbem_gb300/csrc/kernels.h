@@ -179,6 +179,8 @@ void launch_mv_pass(int prec, bool cplx, const MVArgs2& a, int grid, cudaStream_
 // gathers every dense block and low-rank U2 row slice that touches its rows, adds them up in
 // shared memory and stores its rows of y (no global atomics).  entries: {kind (0 dense,
 // 1 low rank), block, first local row, rows}; leaves: {first row, end row, first entry, end}.
+// Kind 2 (tensor-core products): {2, delta, first global row, rows} adds the complex64 rows
+// ypart[(i + delta) * 32 + rhs] of a row cluster's partial product.
 struct MVRowArgs {
   const int4* leaves;
   int nleaves;
@@ -190,6 +192,7 @@ struct MVRowArgs {
   void* yp;         // permuted y (FP64 / complex128), written
   int nrhs;
   int compensated;
+  const void* ypart;  // kind-2 partial rows (complex64, 32 right-hand sides per row)
 };
 void launch_mv_rowowner(int prec, bool cplx, const MVRowArgs& a, cudaStream_t s);
 int mv_stage_bytes();
@@ -226,5 +229,62 @@ void launch_baxpy_basis(bool cplx, int n, int k, int nrhs, const void* Q, const 
 void launch_bnrm2(bool cplx, int n, int nrhs, const void* w, double* out, cudaStream_t s);
 void launch_bscale(bool cplx, int n, int nrhs, const void* w, const double* inv, void* q, cudaStream_t s);
 void launch_residual(bool cplx, int n, const void* b, void* r, cudaStream_t s);
+
+// ---- tensor-core products for several right-hand sides (tc_matvec.cu) ---------------------
+// Operand panels are in the canonical K-major, no-swizzle layout of tcgen05 (core matrices of
+// 8 rows x 16 bytes), K counted in "cores" of 4 FP32 values:
+//   A panel, 128 rows: float4 index kc * 128 + row                     (2048 bytes per core)
+//   B panel, N rows, TF32 high and low parts: float4 (2 kc + h) * N + n   (32 N bytes per core)
+// Row 4 r + 2 a + h of an A panel is right-hand side r, real (a = 0) or imaginary part, high
+// (h = 0) or low TF32 part.
+struct TCSeg {
+  unsigned long long a, b;  // A and B panels (global addresses, 16-byte aligned)
+  int nkc;                  // K cores (even: one MMA takes K = 8)
+  int pad[3];
+};
+struct TCItem {
+  int seg0, nseg;  // segments accumulated into one TMEM accumulator
+  int N;           // MMA N: multiple of 16, 16..256
+  int out0, nout;  // pass 0: outputs [out0, out0+nout); pass 1: partial row offset, rows
+  int pad[3];
+};
+struct TCOut {            // pass 0: one low-rank block of a column tile
+  unsigned long long ta;  // its A panel for pass 1 (128 x 2 rpad)
+  int col, rpad;          // first accumulator column; rank padded to a multiple of 4
+};
+struct TCGemmArgs {
+  const TCItem* items;
+  const TCSeg* segs;
+  const TCOut* outs;
+  const int2* sched;  // per CTA: first item, item count
+  void* ypart;        // pass 1 output (complex64 rows of 32 right-hand sides)
+  int* err;
+};
+struct TCVJob {  // pack the V2 panel of a column tile
+  unsigned long long dst;
+  int kc0, nkc, N, cm0;  // first absolute K core, cores, N, column map offset
+};
+struct TCUJob {  // pack the U2 panel of (row tile, block)
+  unsigned long long dst;
+  int lr, i0, rows, N, nkc, pad;
+};
+#define TC_CAP (48 * 1024)  // bytes of one pipeline stage
+// K cores per stage for an MMA N (even, at least 2)
+__host__ __device__ inline int tc_kcs(int N) {
+  int k = (TC_CAP / (2048 + 32 * N)) & ~1;
+  return k < 2 ? 2 : k;
+}
+int tc_smem_bytes();
+// 1 when the running device executes the tcgen05 kernels (compute capability 10.x)
+int tc_supported();
+// xa (A panel, nkc cores) from x: x[r * ld + perm[j]] (complex128) for dof j, r < nrhs
+void launch_tc_xprep(const int* perm, int n, int nrhs, int ld, const void* x, void* xa, int nkc, cudaStream_t s);
+void launch_tc_pack_v(const TCVJob* jobs, int njobs, const int4* colmap, const LRDesc* lr, cudaStream_t s);
+void launch_tc_pack_u(const TCUJob* jobs, int njobs, const LRDesc* lr, cudaStream_t s);
+// pass 0 (pass = 0): T panels of every low-rank block; pass 1: partial rows of U2 T
+cudaError_t launch_tc_gemm(int pass, const TCGemmArgs& g, int grid, cudaStream_t s);
+// one 128 x N x (4 nkc) product D = A B^T on the tensor cores from ready panels (self-test):
+// d[row * N + n] (FP32); the B panel holds high and low parts, both are issued
+cudaError_t launch_tc_selftest(const void* a, const void* b, int N, int nkc, float* d, int* err, cudaStream_t s);
 
 }  // namespace bem

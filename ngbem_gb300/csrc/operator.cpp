@@ -946,6 +946,10 @@ void HOperator::mult(int trans, const double* alpha, const void* x, const double
     for (auto& e : ev) BEM_CUDA(cudaEventCreate(&e));
     BEM_CUDA(cudaEventRecord(ev[0], s));
   }
+  if (tc_eligible(trans, nrhs, s)) {
+    mult_tc(alpha, x, beta, y, nrhs, s);
+    return;
+  }
   if (mv_fused && nrhs == 1) {
     // one cooperative launch: permute, phase A, t -> input form, phase B, un-permute
     MVFusedArgs f{};

@@ -1,0 +1,380 @@
+// Host side of the tensor-core products for several right-hand sides (kernels in
+// tc_matvec.cu): tiles of the low-rank blocks, their packed operand panels, a balanced static
+// item list per CTA, the owner-computes lists that add the partial rows, and the application
+// Y = A X for 2..32 complex right-hand sides (reference HMatrix::MultAdd, src/hmat.cpp:647-655,
+// applied to many vectors at once).
+#include <algorithm>
+#include <chrono>
+#include <climits>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <queue>
+
+#include "host.hpp"
+
+namespace bem {
+
+namespace {
+
+using clk = std::chrono::steady_clock;
+
+// Known-answer check of the instruction and shared-memory descriptor encodings: one
+// 128 x 32 x 16 product of small integers and eighths (exact in TF32 and in FP32) against the
+// host product.  The tensor-core path is used only on a device where it passed.
+int tc_selftest_run() {
+  const int N = 32, nkc = 4, K = 16;
+  std::vector<float> A(128 * K), Bh(N * K), Bl(N * K);
+  for (int r = 0; r < 128; ++r)
+    for (int k = 0; k < K; ++k) A[r * K + k] = (float)((r * 7 + k * 3) % 11 - 5);
+  for (int n = 0; n < N; ++n)
+    for (int k = 0; k < K; ++k) {
+      Bh[n * K + k] = (float)((n * 5 + k) % 7 - 3);
+      Bl[n * K + k] = (float)((n + 2 * k) % 5 - 2) / 8.0f;
+    }
+  std::vector<float> pa((size_t)nkc * 128 * 4), pb((size_t)nkc * 2 * N * 4);
+  for (int kc = 0; kc < nkc; ++kc)
+    for (int r = 0; r < 128; ++r)
+      for (int k = 0; k < 4; ++k) pa[((size_t)kc * 128 + r) * 4 + k] = A[r * K + 4 * kc + k];
+  for (int kc = 0; kc < nkc; ++kc)
+    for (int h = 0; h < 2; ++h)
+      for (int n = 0; n < N; ++n)
+        for (int k = 0; k < 4; ++k)
+          pb[((size_t)(2 * kc + h) * N + n) * 4 + k] = (h ? Bl : Bh)[n * K + 4 * kc + k];
+  DevBuf da, db, dd, de;
+  da.upload(pa);
+  db.upload(pb);
+  dd.alloc((size_t)128 * N * sizeof(float));
+  de.alloc(sizeof(int));
+  BEM_CUDA(cudaMemset(dd.p, 0, dd.bytes));
+  BEM_CUDA(cudaMemset(de.p, 0, sizeof(int)));
+  BEM_CUDA(launch_tc_selftest(da.p, db.p, N, nkc, dd.as<float>(), de.as<int>(), 0));
+  BEM_CUDA(cudaDeviceSynchronize());
+  std::vector<float> d((size_t)128 * N);
+  int err = 0;
+  BEM_CUDA(cudaMemcpy(d.data(), dd.p, dd.bytes, cudaMemcpyDeviceToHost));
+  BEM_CUDA(cudaMemcpy(&err, de.p, sizeof(int), cudaMemcpyDeviceToHost));
+  if (err) return 0;
+  for (int r = 0; r < 128; ++r)
+    for (int n = 0; n < N; ++n) {
+      double e = 0.0;
+      for (int k = 0; k < K; ++k) e += (double)A[r * K + k] * ((double)Bh[n * K + k] + (double)Bl[n * K + k]);
+      if ((double)d[(size_t)r * N + n] != e) return 0;
+    }
+  return 1;
+}
+
+// longest-processing-time assignment of items to CTAs; items are reordered so that every
+// CTA's list is contiguous
+void balance(std::vector<TCItem>& items, const std::vector<double>& cost, int nsm, std::vector<int2>& sched) {
+  const int n = (int)items.size();
+  const int G = std::max(1, std::min(nsm, n));
+  std::vector<int> order(n);
+  for (int i = 0; i < n; ++i) order[i] = i;
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return cost[a] > cost[b]; });
+  using E = std::pair<double, int>;
+  std::priority_queue<E, std::vector<E>, std::greater<E>> q;
+  for (int c = 0; c < G; ++c) q.push({0.0, c});
+  std::vector<std::vector<int>> per(G);
+  for (int i : order) {
+    E e = q.top();
+    q.pop();
+    per[e.second].push_back(i);
+    q.push({e.first + cost[i], e.second});
+  }
+  std::vector<TCItem> out;
+  out.reserve(n);
+  sched.assign(G, make_int2(0, 0));
+  for (int c = 0; c < G; ++c) {
+    sched[c].x = (int)out.size();
+    for (int i : per[c]) out.push_back(items[i]);
+    sched[c].y = (int)per[c].size();
+  }
+  items.swap(out);
+}
+
+}  // namespace
+
+int tc_selftest() {
+  static std::mutex mu;
+  static int state = -2;
+  std::lock_guard<std::mutex> lock(mu);
+  if (state == -2) state = tc_supported() ? tc_selftest_run() : 0;
+  return state;
+}
+
+bool HOperator::tc_eligible(int trans, int nrhs, cudaStream_t s) {
+  if (!tc_mode || tc_state < 0 || trans || !cplx || prec != 1 || mv_compensated || nrhs < 2 || nrhs > 32 ||
+      t_len <= 0)
+    return false;
+  if (tc_state == 0) {
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    BEM_CUDA(cudaStreamIsCapturing(s, &cs));
+    if (cs != cudaStreamCaptureStatusNone) return false;  // built outside a capture only
+    build_tc();
+  }
+  return tc_state == 1;
+}
+
+void HOperator::build_tc() {
+  const auto t0 = clk::now();
+  tc_state = -1;
+  if (!cplx || prec != 1 || t_len <= 0 || !tc_selftest()) return;
+  for (const LRDesc& L : mvlr)
+    if (L.R > 128) return;  // a block's 2 x rank columns must fit one MMA (N <= 256)
+  const int nf = (int)mvlr.size();
+  std::vector<int> rpad(nf, 0);
+  std::vector<long long> taoff(nf, -1);
+  long long ta_bytes = 0;
+  for (int f = 0; f < nf; ++f)
+    if (mvlr[f].R > 0) {
+      rpad[f] = (mvlr[f].R + 3) & ~3;
+      taoff[f] = ta_bytes;
+      ta_bytes += (long long)rpad[f] * 1024;  // 128 rows x 2 rpad FP32
+    }
+  // pass 0: blocks grouped by column cluster, stacked into column tiles of N <= 256
+  std::map<std::pair<int, int>, std::vector<int>> cols, rows;
+  for (int f = 0; f < nf; ++f)
+    if (rpad[f] > 0) {
+      cols[{mvlr[f].c0, mvlr[f].n}].push_back(f);
+      rows[{mvlr[f].r0, mvlr[f].m}].push_back(f);
+    }
+  tc_nkc_x = (width + 3) / 4 + 2;
+  std::vector<TCItem> it0;
+  std::vector<double> cost0;
+  std::vector<TCSeg> sg0;
+  std::vector<TCOut> outs;
+  std::vector<TCVJob> vjobs;
+  std::vector<int4> colmap;
+  long long vp_bytes = 0;
+  struct OutRef { int f, col; };
+  for (auto& kv : cols) {
+    const int c0 = kv.first.first, n = kv.first.second;
+    const int kc0 = c0 / 4, kc1 = (c0 + n + 3) / 4;
+    const int nkc = (kc1 - kc0 + 1) & ~1;
+    const std::vector<int>& fs = kv.second;
+    for (size_t p = 0; p < fs.size();) {
+      std::vector<OutRef> tile;
+      int ncol = 0;
+      while (p < fs.size() && ncol + 2 * rpad[fs[p]] <= 256) {
+        tile.push_back({fs[p], ncol});
+        ncol += 2 * rpad[fs[p]];
+        ++p;
+      }
+      const int N = (ncol + 15) & ~15;
+      TCVJob J{};
+      J.dst = (unsigned long long)vp_bytes;  // offset; rebased after allocation
+      J.kc0 = kc0;
+      J.nkc = nkc;
+      J.N = N;
+      J.cm0 = (int)colmap.size();
+      for (int c = 0; c < N; ++c) colmap.push_back(make_int4(-1, 0, 0, 0));
+      TCItem I{};
+      I.seg0 = (int)sg0.size();
+      I.nseg = 1;
+      I.N = N;
+      I.out0 = (int)outs.size();
+      I.nout = (int)tile.size();
+      for (const OutRef& o : tile) {
+        for (int k = 0; k < mvlr[o.f].R; ++k)
+          for (int c = 0; c < 2; ++c) colmap[J.cm0 + o.col + 2 * k + c] = make_int4(o.f, k, c, 0);
+        TCOut O{};
+        O.ta = (unsigned long long)taoff[o.f];  // offset; rebased
+        O.col = o.col;
+        O.rpad = rpad[o.f];
+        outs.push_back(O);
+      }
+      TCSeg S{};
+      S.a = (unsigned long long)kc0 * 2048;  // offset into the X panel; rebased
+      S.b = J.dst;
+      S.nkc = nkc;
+      sg0.push_back(S);
+      vjobs.push_back(J);
+      it0.push_back(I);
+      cost0.push_back((double)nkc * (2048.0 + 32.0 * N) + 1024.0 * ncol / 2);
+      vp_bytes += (long long)nkc * 32 * N;
+    }
+  }
+  // pass 1: blocks grouped by row cluster; row tiles of <= 256 rows, one segment per block
+  std::vector<TCItem> it1;
+  std::vector<double> cost1;
+  std::vector<TCSeg> sg1;
+  std::vector<TCUJob> ujobs;
+  long long up_bytes = 0, yrows = 0;
+  struct RowGroup { int r0, m; long long yoff; };
+  std::vector<RowGroup> rgroups;
+  for (auto& kv : rows) {
+    const int r0 = kv.first.first, m = kv.first.second;
+    rgroups.push_back({r0, m, yrows});
+    for (int i0 = 0; i0 < m; i0 += 256) {
+      const int nr = std::min(256, m - i0);
+      const int N = (nr + 15) & ~15;
+      TCItem I{};
+      I.seg0 = (int)sg1.size();
+      I.nseg = (int)kv.second.size();
+      I.N = N;
+      I.out0 = (int)(yrows + i0);
+      I.nout = nr;
+      double c = 256.0 * N;
+      for (int f : kv.second) {
+        TCUJob J{};
+        J.dst = (unsigned long long)up_bytes;
+        J.lr = f;
+        J.i0 = i0;
+        J.rows = nr;
+        J.N = N;
+        J.nkc = rpad[f] / 2;
+        TCSeg S{};
+        S.a = (unsigned long long)taoff[f];
+        S.b = J.dst;
+        S.nkc = J.nkc;
+        sg1.push_back(S);
+        ujobs.push_back(J);
+        c += (double)J.nkc * (2048.0 + 32.0 * N);
+        up_bytes += (long long)J.nkc * 32 * N;
+      }
+      it1.push_back(I);
+      cost1.push_back(c);
+    }
+    yrows += m;
+  }
+  if (yrows > INT_MAX / 2) return;  // partial row offsets are ints
+  // device buffers: X panel, T panels, packed V2 and U2 panels, partial rows
+  d_tc_xa.alloc((size_t)tc_nkc_x * 2048);
+  d_tc_ta.alloc((size_t)std::max(ta_bytes, 16LL));
+  d_tc_vp.alloc((size_t)std::max(vp_bytes, 16LL));
+  d_tc_up.alloc((size_t)std::max(up_bytes, 16LL));
+  d_tc_y.alloc((size_t)std::max(yrows, 1LL) * 32 * 8);
+  const unsigned long long xa = (unsigned long long)d_tc_xa.p, ta = (unsigned long long)d_tc_ta.p;
+  const unsigned long long vp = (unsigned long long)d_tc_vp.p, up = (unsigned long long)d_tc_up.p;
+  for (TCVJob& J : vjobs) J.dst += vp;
+  for (TCSeg& S : sg0) {
+    S.a += xa;
+    S.b += vp;
+  }
+  for (TCOut& O : outs) O.ta += ta;
+  for (TCUJob& J : ujobs) J.dst += up;
+  for (TCSeg& S : sg1) {
+    S.a += ta;
+    S.b += up;
+  }
+  int dev = 0, nsm = 152;
+  BEM_CUDA(cudaGetDevice(&dev));
+  BEM_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+  std::vector<int2> sch0, sch1;
+  balance(it0, cost0, nsm, sch0);
+  balance(it1, cost1, nsm, sch1);
+  tc_grid[0] = it0.empty() ? 0 : (int)sch0.size();
+  tc_grid[1] = it1.empty() ? 0 : (int)sch1.size();
+  d_tc_items[0].upload(it0);
+  d_tc_items[1].upload(it1);
+  d_tc_segs[0].upload(sg0);
+  d_tc_segs[1].upload(sg1);
+  d_tc_sched[0].upload(sch0);
+  d_tc_sched[1].upload(sch1);
+  d_tc_outs.upload(outs);
+  // pack the factors (once)
+  {
+    DevBuf dv, du, dcm;
+    dv.upload(vjobs);
+    du.upload(ujobs);
+    dcm.upload(colmap);
+    launch_tc_pack_v(dv.as<TCVJob>(), (int)vjobs.size(), dcm.as<int4>(), d_mvlr.as<LRDesc>(), 0);
+    launch_tc_pack_u(du.as<TCUJob>(), (int)ujobs.size(), d_mvlr.as<LRDesc>(), 0);
+    BEM_CUDA(cudaGetLastError());
+    BEM_CUDA(cudaDeviceSynchronize());
+  }
+  // owner-computes lists: every dense block (kind 0) and every row cluster's partial rows
+  // (kind 2) that touch a leaf's rows
+  {
+    std::vector<std::pair<int, int>> lv;
+    for (const ClusterH& C : ttest->cl)
+      if (C.Child1 < 0) lv.push_back({(int)C.PermuPos, (int)(C.PermuPos + C.Number)});
+    std::sort(lv.begin(), lv.end());
+    std::vector<std::vector<int4>> per(lv.size());
+    auto for_leaves = [&](int r0, int m, auto&& fn) {
+      int l = (int)(std::upper_bound(lv.begin(), lv.end(), std::make_pair(r0, INT_MAX)) - lv.begin()) - 1;
+      for (l = std::max(l, 0); l < (int)lv.size() && lv[l].first < r0 + m; ++l) {
+        const int a0 = std::max(r0, lv[l].first), a1 = std::min(r0 + m, lv[l].second);
+        if (a1 > a0) fn(l, a0, a1);
+      }
+    };
+    for (int k = 0; k < (int)mvdense.size(); ++k)
+      for_leaves(mvdense[k].r0, mvdense[k].m,
+                 [&](int l, int a0, int a1) { per[l].push_back(make_int4(0, k, a0 - mvdense[k].r0, a1 - a0)); });
+    for (const RowGroup& g : rgroups)
+      for_leaves(g.r0, g.m, [&](int l, int a0, int a1) {
+        per[l].push_back(make_int4(2, (int)(g.yoff - g.r0), a0, a1 - a0));
+      });
+    std::vector<int4> leaves, ents;
+    for (size_t l = 0; l < lv.size(); ++l) {
+      const int e0 = (int)ents.size();
+      ents.insert(ents.end(), per[l].begin(), per[l].end());
+      leaves.push_back(make_int4(lv[l].first, lv[l].second, e0, (int)ents.size()));
+    }
+    d_ro_leaves_tc.upload(leaves);
+    d_ro_ents_tc.upload(ents);
+    n_ro_leaves_tc = (int)leaves.size();
+  }
+  BEM_CUDA(cudaDeviceSynchronize());
+  tc_bytes = (long long)(d_tc_xa.bytes + d_tc_ta.bytes + d_tc_vp.bytes + d_tc_up.bytes + d_tc_y.bytes);
+  tc_items[0] = (int)it0.size();
+  tc_items[1] = (int)it1.size();
+  tc_ms_build = std::chrono::duration<double, std::milli>(clk::now() - t0).count();
+  tc_state = 1;
+}
+
+void HOperator::release_tc() {
+  for (DevBuf* b : {&d_tc_xa, &d_tc_ta, &d_tc_vp, &d_tc_up, &d_tc_y, &d_tc_items[0], &d_tc_items[1], &d_tc_segs[0],
+                    &d_tc_segs[1], &d_tc_sched[0], &d_tc_sched[1], &d_tc_outs, &d_ro_leaves_tc, &d_ro_ents_tc})
+    b->release();
+  tc_state = 0;
+  tc_bytes = 0;
+}
+
+void HOperator::mult_tc(const double* alpha, const void* x, const double* beta, void* y, int nrhs, cudaStream_t s) {
+  const int* perm = d_perm_trial.as<int>();
+  const int* pout = ttest == ttrial ? d_perm_trial.as<int>() : d_perm_test.as<int>();
+  std::array<cudaEvent_t, 5> ev{};
+  if (profiling) {
+    for (auto& e : ev) BEM_CUDA(cudaEventCreate(&e));
+    BEM_CUDA(cudaEventRecord(ev[0], s));
+  }
+  launch_permute_in(prec, cplx, perm, width, nrhs, width, x, d_xp.p, s);  // dense blocks' input
+  launch_tc_xprep(perm, width, nrhs, width, x, d_tc_xa.p, tc_nkc_x, s);
+  if (profiling) BEM_CUDA(cudaEventRecord(ev[1], s));
+  for (int pass = 0; pass < 2; ++pass) {
+    TCGemmArgs g{};
+    g.items = d_tc_items[pass].as<TCItem>();
+    g.segs = d_tc_segs[pass].as<TCSeg>();
+    g.outs = d_tc_outs.as<TCOut>();
+    g.sched = d_tc_sched[pass].as<int2>();
+    g.ypart = d_tc_y.p;
+    g.err = d_err.as<int>();
+    BEM_CUDA(launch_tc_gemm(pass, g, tc_grid[pass], s));
+    if (profiling && pass == 0) BEM_CUDA(cudaEventRecord(ev[2], s));
+  }
+  MVRowArgs ra{};
+  ra.leaves = d_ro_leaves_tc.as<int4>();
+  ra.nleaves = n_ro_leaves_tc;
+  ra.ents = d_ro_ents_tc.as<int4>();
+  ra.dense = d_mvdense.as<MVDense>();
+  ra.lr = d_mvlr.as<LRDesc>();
+  ra.xp = d_xp.p;
+  ra.tx = d_tx.p;
+  ra.yp = d_yp.p;
+  ra.nrhs = nrhs;
+  ra.compensated = 0;
+  ra.ypart = d_tc_y.p;
+  launch_mv_rowowner(prec, cplx, ra, s);
+  if (profiling) BEM_CUDA(cudaEventRecord(ev[3], s));
+  launch_permute_out(cplx, pout, height, nrhs, height, alpha, beta, d_yp.p, y, s);
+  if (profiling) {
+    BEM_CUDA(cudaEventRecord(ev[4], s));
+    pending.push_back(ev);
+    pending_fused.push_back(false);
+  }
+  BEM_CUDA(cudaGetLastError());
+}
+
+}  // namespace bem

@@ -1,0 +1,542 @@
+// Several-right-hand-side products of the low-rank blocks on the tcgen05 tensor cores
+// (complex FP32 storage).  The reference applies each low-rank block as y += U2 (V2 x) one
+// vector at a time (LowRankMatrix::Mult / BEMBlock::MultAdd, src/hmat.cpp:473-565, summed by
+// HMatrix::MultAdd, :647-666); with 32 right-hand sides those products are GEMMs:
+//
+//   pass 0: T_b = V2_b X[cols b] for every low-rank block b.  The blocks of one column cluster
+//           are stacked along N (one X panel feeds all of them); every block's T is written
+//           once, as the A panel of pass 1.
+//   pass 1: Y_tau = sum_b U2_b T_b over the blocks of one row cluster tau; the tensor memory
+//           accumulates over all of them and the tile is stored once into a per-row-cluster
+//           partial buffer.  The owner-computes kernel (matvec.cu) adds, for each leaf, the
+//           partials of every row cluster that contains it to the leaf's dense products.
+//
+// Complex products run as real products.  Rows of the A side are (right-hand side r, real or
+// imaginary part a, TF32 high or low part h) at 4 r + 2 a + h, so M = 128 for 32 right-hand
+// sides; the B side holds the TF32 high and low parts of the stored factor and both are issued
+// into one accumulator.  Summing the two h rows gives (a_hi + a_lo)(b_hi + b_lo): a split-TF32
+// product about 2^-21 from the exact one, accumulated in FP32 (TMEM).
+//
+// Kernel roles (192 threads, one CTA per SM, persistent over a host-balanced item list):
+//   warp 0      bulk copies (cp.async.bulk + mbarrier complete_tx) of A and B K-ranges into a
+//               4-stage ring;
+//   warp 1      owns the tensor memory (512 columns: two 256-column accumulators) and one
+//               thread issues tcgen05.mma, releasing stages and accumulators by tcgen05.commit;
+//   warps 2-5   epilogue: tcgen05.ld of their TMEM lane quarter, combination of the real and
+//               imaginary and high and low rows with warp shuffles, global stores.
+// Every wait is bounded: a wait that runs out sets an error bit, the CTA drains what it
+// issued and frees its tensor memory.
+#include <cstdint>
+
+#include "bem_device.cuh"
+#include "kernels.h"
+
+namespace bem {
+
+#define TC_NST 4
+#define TC_THREADS 192
+#define TC_ACC_COLS 256
+#define TC_HDR 1024
+#define TC_ERR_WAIT 0x100
+
+namespace {
+
+__device__ __forceinline__ uint32_t su32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void bar_init(uint64_t* b, int count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(su32(b)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void bar_arrive(uint64_t* b) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(su32(b)) : "memory");
+}
+__device__ __forceinline__ bool bar_try(uint64_t* b, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+      : "=r"(ok)
+      : "r"(su32(b)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+// Bounded wait for the phase of `parity` to complete (non-blocking polls, a short sleep every
+// 256 of them: the limit is well under a second).  Returns false when the CTA is aborting or
+// when the limit ran out (then the error bit is set and the CTA aborts).
+__device__ bool bar_wait(uint64_t* b, uint32_t parity, volatile int* abort_flag, int* err) {
+  for (int i = 0; i < (1 << 22); ++i) {
+    if (bar_try(b, parity)) return true;
+    if ((i & 255) == 255) {
+      if (*abort_flag) return false;
+      __nanosleep(128);
+    }
+  }
+  atomicOr(err, TC_ERR_WAIT);
+  *abort_flag = 1;
+  return false;
+}
+__device__ __forceinline__ void expect_tx(uint64_t* b, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(su32(b)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* b) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                   su32(dst)),
+               "l"(src), "r"(bytes), "r"(su32(b))
+               : "memory");
+}
+
+// ---- tcgen05 --------------------------------------------------------------------------------
+__device__ __forceinline__ void tmem_alloc(uint32_t* dst, uint32_t ncols) {
+  asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(su32(dst)), "r"(ncols)
+               : "memory");
+  asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+}
+__device__ __forceinline__ void tmem_dealloc(uint32_t taddr, uint32_t ncols) {
+  asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(taddr), "r"(ncols) : "memory");
+}
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+// Shared-memory matrix descriptor, K-major without swizzle: start address, leading-dimension
+// byte offset (between core matrices adjacent in K), stride byte offset (between 8-row groups
+// adjacent in M or N), descriptor version 1 (bits 46-47), no base offset, no swizzle.
+__device__ __forceinline__ uint64_t sdesc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+  return (uint64_t)((saddr & 0x3FFFFu) >> 4) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
+         ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);
+}
+// Instruction descriptor of kind::tf32: D FP32 (bits 4-5 = 1), A and B TF32 (bits 7-9 and
+// 10-12 = 2), both K-major, N >> 3 at bit 17, M >> 4 at bit 24.
+__device__ __forceinline__ uint32_t idesc_tf32(int M, int N) {
+  return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+__device__ __forceinline__ void mma_tf32(uint32_t d, uint64_t a, uint64_t b, uint32_t idesc, uint32_t accumulate) {
+  asm volatile(
+      "{\n .reg .pred p;\n setp.ne.b32 p, %4, 0;\n tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n}\n" ::"r"(
+          d),
+      "l"(a), "l"(b), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+// the mbarrier gets one arrival when every MMA this thread issued so far has completed
+__device__ __forceinline__ void mma_commit(uint64_t* b) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(su32(b))
+               : "memory");
+}
+// 8 consecutive accumulator columns of this thread's TMEM lane; the values are defined after
+// tmem_wait (which takes them as operands so that no use moves above it)
+__device__ __forceinline__ void tmem_ld8(uint32_t taddr, float (&v)[8]) {
+  uint32_t r[8];
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+               : "r"(taddr)
+               : "memory");
+#pragma unroll
+  for (int k = 0; k < 8; ++k) v[k] = __uint_as_float(r[k]);
+}
+__device__ __forceinline__ void tmem_wait(float (&v)[8]) {
+  asm volatile("tcgen05.wait::ld.sync.aligned;"
+               : "+f"(v[0]), "+f"(v[1]), "+f"(v[2]), "+f"(v[3]), "+f"(v[4]), "+f"(v[5]), "+f"(v[6]), "+f"(v[7])
+               :
+               : "memory");
+}
+
+// round to TF32 (10 stored mantissa bits, nearest, ties away), low 13 bits cleared
+__device__ __forceinline__ float tf32_rn(float x) {
+  uint32_t r;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+  return __uint_as_float(r & 0xFFFFE000u);
+}
+// high (h = 0) or low (h = 1) TF32 part of v
+__device__ __forceinline__ float tf32_part(float v, int h) {
+  const float hi = tf32_rn(v);
+  return h ? tf32_rn(v - hi) : hi;
+}
+
+struct TCSmem {
+  uint64_t full[TC_NST], empty[TC_NST], accf[2], acce[2], fin;
+  uint32_t tmem;
+  int abort_flag;
+};
+
+}  // namespace
+
+// ---- the grouped GEMM -----------------------------------------------------------------------
+template <int PASS>
+__global__ void __launch_bounds__(TC_THREADS, 1) tc_gemm_kernel(TCGemmArgs g) {
+  extern __shared__ unsigned char tc_smem_raw[];
+  unsigned char* base = (unsigned char*)(((uintptr_t)tc_smem_raw + 1023) & ~(uintptr_t)1023);
+  TCSmem& S = *(TCSmem*)base;
+  unsigned char* stages = base + TC_HDR;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < TC_NST; ++s) {
+      bar_init(&S.full[s], 1);
+      bar_init(&S.empty[s], 1);
+    }
+    for (int a = 0; a < 2; ++a) {
+      bar_init(&S.accf[a], 1);
+      bar_init(&S.acce[a], 4);
+    }
+    bar_init(&S.fin, 1);
+    S.abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  }
+  if (warp == 1) tmem_alloc(&S.tmem, 2 * TC_ACC_COLS);
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = S.tmem;
+  volatile int* abort_flag = &S.abort_flag;
+  const int2 my = g.sched[blockIdx.x];
+
+  if (warp == 0) {
+    if (lane == 0) {
+      int it = 0;
+      bool ok = true;
+      for (int ii = my.x; ok && ii < my.x + my.y; ++ii) {
+        const TCItem I = g.items[ii];
+        const int kmax = tc_kcs(I.N);
+        for (int sg = I.seg0; ok && sg < I.seg0 + I.nseg; ++sg) {
+          const TCSeg Sg = g.segs[sg];
+          for (int kc = 0; kc < Sg.nkc; kc += kmax) {
+            const int kcs = min(kmax, Sg.nkc - kc);
+            const int s = it % TC_NST;
+            if (!bar_wait(&S.empty[s], ((it / TC_NST) & 1) ^ 1, abort_flag, g.err)) {
+              ok = false;
+              break;
+            }
+            unsigned char* st = stages + (size_t)s * TC_CAP;
+            const uint32_t ab = (uint32_t)kcs * 2048u, bb = (uint32_t)kcs * 32u * (uint32_t)I.N;
+            expect_tx(&S.full[s], ab + bb);
+            bulk_g2s(st, (const unsigned char*)Sg.a + (size_t)kc * 2048, ab, &S.full[s]);
+            bulk_g2s(st + ab, (const unsigned char*)Sg.b + (size_t)kc * 32 * I.N, bb, &S.full[s]);
+            ++it;
+          }
+        }
+      }
+      // drain: wait until the MMA thread released every stage still filled, so that no copy
+      // or commit arrival is in flight when the CTA ends
+      for (int j = it > TC_NST ? it - TC_NST : 0; j < it; ++j)
+        bar_wait(&S.empty[j % TC_NST], (j / TC_NST) & 1, abort_flag, g.err);
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      int it = 0, acc_it = 0;
+      bool ok = true, issued = false;
+      for (int ii = my.x; ok && ii < my.x + my.y; ++ii) {
+        const TCItem I = g.items[ii];
+        const int kmax = tc_kcs(I.N);
+        const int acc = acc_it & 1;
+        if (!bar_wait(&S.acce[acc], ((acc_it >> 1) & 1) ^ 1, abort_flag, g.err)) break;
+        tc_fence_after();
+        const uint32_t d = tmem + (uint32_t)(acc * TC_ACC_COLS);
+        const uint32_t idesc = idesc_tf32(128, I.N);
+        const uint32_t bstride = 32u * (uint32_t)I.N;
+        uint32_t accumulate = 0;
+        for (int sg = I.seg0; ok && sg < I.seg0 + I.nseg; ++sg) {
+          const int nkc = g.segs[sg].nkc;
+          for (int kc = 0; kc < nkc; kc += kmax) {
+            const int kcs = min(kmax, nkc - kc);
+            const int s = it % TC_NST;
+            if (!bar_wait(&S.full[s], (it / TC_NST) & 1, abort_flag, g.err)) {
+              ok = false;
+              break;
+            }
+            tc_fence_after();
+            const uint32_t sa = su32(stages + (size_t)s * TC_CAP);
+            const uint32_t sb = sa + (uint32_t)kcs * 2048u;
+            for (int k2 = 0; k2 < kcs; k2 += 2) {
+              const uint64_t ad = sdesc(sa + (uint32_t)k2 * 2048u, 2048u, 128u);
+              const uint64_t bh = sdesc(sb + (uint32_t)k2 * bstride, bstride, 128u);
+              const uint64_t bl = sdesc(sb + (uint32_t)k2 * bstride + 16u * (uint32_t)I.N, bstride, 128u);
+              mma_tf32(d, ad, bh, idesc, accumulate);
+              mma_tf32(d, ad, bl, idesc, 1u);
+              accumulate = 1;
+            }
+            issued = true;
+            mma_commit(&S.empty[s]);
+            ++it;
+          }
+        }
+        if (!ok) break;
+        mma_commit(&S.accf[acc]);
+        ++acc_it;
+      }
+      if (issued) {
+        mma_commit(&S.fin);
+        bar_wait(&S.fin, 0, abort_flag, g.err);
+      }
+    }
+  } else {
+    // epilogue: warp w reads TMEM lanes [32 (w % 4), +32): accumulator row 32 (w % 4) + lane
+    const int q4 = warp & 3;
+    const int row = 32 * q4 + lane;
+    const int rhs = row >> 2, a = (row >> 1) & 1, h = row & 1;
+    const unsigned FULL = 0xffffffffu;
+    int acc_it = 0;
+    for (int ii = my.x; ii < my.x + my.y; ++ii) {
+      const TCItem I = g.items[ii];
+      const int acc = acc_it & 1;
+      int ok = 1;
+      if (lane == 0) ok = bar_wait(&S.accf[acc], (acc_it >> 1) & 1, abort_flag, g.err) ? 1 : 0;
+      ok = __shfl_sync(FULL, ok, 0);
+      if (!ok) break;
+      tc_fence_after();
+      const uint32_t tb = tmem + ((uint32_t)(32 * q4) << 16) + (uint32_t)(acc * TC_ACC_COLS);
+      if (PASS == 0) {
+        // columns (rank k, real/imaginary c) of each block: T = V2 x combined from the four
+        // real products, written as the block's pass-1 A panel: row (r, a', h') holds, for
+        // K = (k, c), the h' part of  a' = 0: (Re T_k, -Im T_k);  a' = 1: (Im T_k, Re T_k)
+        for (int o = I.out0; o < I.out0 + I.nout; ++o) {
+          const TCOut O = g.outs[o];
+          float4* ta = (float4*)O.ta;
+          for (int c = 0; c < 2 * O.rpad; c += 8) {
+            float v[8], sm[8], pm[8], out[8];
+            tmem_ld8(tb + (uint32_t)(O.col + c), v);
+            tmem_wait(v);
+#pragma unroll
+            for (int k = 0; k < 8; ++k) sm[k] = v[k] + __shfl_xor_sync(FULL, v[k], 1);  // hi + lo rows
+#pragma unroll
+            for (int k = 0; k < 8; ++k) pm[k] = __shfl_xor_sync(FULL, sm[k], 2);        // other part a
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+              const float rr = a ? pm[2 * k] : sm[2 * k];          // sum_j Re x Re V
+              const float ri = a ? pm[2 * k + 1] : sm[2 * k + 1];  // sum_j Re x Im V
+              const float ir = a ? sm[2 * k] : pm[2 * k];          // sum_j Im x Re V
+              const float ii2 = a ? sm[2 * k + 1] : pm[2 * k + 1]; // sum_j Im x Im V
+              const float tr = rr - ii2, ti = ri + ir;
+              out[2 * k] = tf32_part(a ? ti : tr, h);
+              out[2 * k + 1] = tf32_part(a ? tr : -ti, h);
+            }
+            const int kc = c >> 2;
+            ta[(size_t)kc * 128 + row] = make_float4(out[0], out[1], out[2], out[3]);
+            ta[(size_t)(kc + 1) * 128 + row] = make_float4(out[4], out[5], out[6], out[7]);
+          }
+        }
+      } else {
+        // columns = rows i of the row tile; row (r, a, h) holds the h part of Re/Im (U2 T)_i
+        float2* yp = (float2*)g.ypart;
+        const int u = lane & 3;
+        for (int c = 0; c < I.nout; c += 8) {
+          float v[8], sm[8], pm[8];
+          tmem_ld8(tb + (uint32_t)c, v);
+          tmem_wait(v);
+#pragma unroll
+          for (int k = 0; k < 8; ++k) sm[k] = v[k] + __shfl_xor_sync(FULL, v[k], 1);
+#pragma unroll
+          for (int k = 0; k < 8; ++k) pm[k] = __shfl_xor_sync(FULL, sm[k], 2);
+#pragma unroll
+          for (int k = 0; k < 8; ++k) {
+            const int i = c + k;
+            if ((k >> 1) == u && i < I.nout)
+              yp[(size_t)(I.out0 + i) * 32 + rhs] = make_float2(a ? pm[k] : sm[k], a ? sm[k] : pm[k]);
+          }
+        }
+      }
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) bar_arrive(&S.acce[acc]);
+      ++acc_it;
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 1) {
+    tc_fence_after();
+    tmem_dealloc(tmem, 2 * TC_ACC_COLS);
+  }
+}
+
+int tc_smem_bytes() { return TC_HDR + TC_NST * TC_CAP + 1024; }
+
+int tc_supported() {
+  int dev = 0, major = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return 0;
+  if (cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, dev) != cudaSuccess) return 0;
+  return major == 10 ? 1 : 0;
+}
+
+template <int PASS>
+static cudaError_t tc_gemm_t(const TCGemmArgs& g, int grid, cudaStream_t s) {
+  static bool attr = false;
+  if (!attr) {
+    cudaError_t e = cudaFuncSetAttribute(tc_gemm_kernel<PASS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         tc_smem_bytes());
+    if (e != cudaSuccess) return e;
+    attr = true;
+  }
+  tc_gemm_kernel<PASS><<<grid, TC_THREADS, tc_smem_bytes(), s>>>(g);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_tc_gemm(int pass, const TCGemmArgs& g, int grid, cudaStream_t s) {
+  if (grid <= 0) return cudaSuccess;
+  return pass == 0 ? tc_gemm_t<0>(g, grid, s) : tc_gemm_t<1>(g, grid, s);
+}
+
+// ---- operand preparation ----------------------------------------------------------------------
+// A panel of X: row 4 r + 2 a + h, K core kc holds dofs 4 kc .. 4 kc + 3 (cluster order)
+__global__ void tc_xprep_kernel(const int* perm, int n, int nrhs, int ld, const double2* x, float4* xa, int nkc) {
+  const long long total = (long long)nkc * 128;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
+       t += (long long)gridDim.x * blockDim.x) {
+    const int kc = (int)(t >> 7), row = (int)(t & 127);
+    const int r = row >> 2, a = (row >> 1) & 1, h = row & 1;
+    float o[4];
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      const int j = 4 * kc + k;
+      double v = 0.0;
+      if (j < n && r < nrhs) {
+        const double2 z = x[(size_t)r * ld + perm[j]];
+        v = a ? z.y : z.x;
+      }
+      const float hi = tf32_rn((float)v);
+      o[k] = h ? tf32_rn((float)(v - (double)hi)) : hi;
+    }
+    xa[t] = make_float4(o[0], o[1], o[2], o[3]);
+  }
+}
+
+void launch_tc_xprep(const int* perm, int n, int nrhs, int ld, const void* x, void* xa, int nkc, cudaStream_t s) {
+  const long long total = (long long)nkc * 128;
+  const int grid = (int)std::min<long long>((total + 255) / 256, 152 * 8);
+  tc_xprep_kernel<<<grid, 256, 0, s>>>(perm, n, nrhs, ld, (const double2*)x, (float4*)xa, nkc);
+}
+
+// V2 panel of a column tile: column n = (block, rank k, part c) from the column map (x < 0:
+// zero column), K = dof; entries outside the block's columns are zero
+__global__ void tc_pack_v_kernel(const TCVJob* jobs, const int4* colmap, const LRDesc* lr) {
+  const TCVJob J = jobs[blockIdx.x];
+  float4* dst = (float4*)J.dst;
+  const long long total = (long long)J.nkc * 2 * J.N;
+  for (long long e = threadIdx.x; e < total; e += blockDim.x) {
+    const int n = (int)(e % J.N);
+    const int hk = (int)(e / J.N);
+    const int hl = hk & 1, kc = hk >> 1;
+    const int4 cm = colmap[J.cm0 + n];
+    float o[4] = {0.f, 0.f, 0.f, 0.f};
+    if (cm.x >= 0) {
+      const LRDesc L = lr[cm.x];
+      const float2* V = (const float2*)L.v;
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        const int j = 4 * (J.kc0 + kc) + k - L.c0;
+        if (j >= 0 && j < L.n) {
+          const float2 z = V[lr_v_index(L, cm.y, j)];
+          o[k] = tf32_part(cm.z ? z.y : z.x, hl);
+        }
+      }
+    }
+    dst[e] = make_float4(o[0], o[1], o[2], o[3]);
+  }
+}
+
+// U2 panel of (row tile, block): row n = block row i0 + n, K = (rank k, part c) at 2 k + c
+__global__ void tc_pack_u_kernel(const TCUJob* jobs, const LRDesc* lr) {
+  const TCUJob J = jobs[blockIdx.x];
+  const LRDesc L = lr[J.lr];
+  const float2* U = (const float2*)L.u;
+  float4* dst = (float4*)J.dst;
+  const long long total = (long long)J.nkc * 2 * J.N;
+  for (long long e = threadIdx.x; e < total; e += blockDim.x) {
+    const int n = (int)(e % J.N);
+    const int hk = (int)(e / J.N);
+    const int hl = hk & 1, kc = hk >> 1;
+    float o[4] = {0.f, 0.f, 0.f, 0.f};
+    if (n < J.rows) {
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        const int K = 4 * kc + k, rk = K >> 1;
+        if (rk < L.R) {
+          const float2 z = U[lr_u_index(L, J.i0 + n, rk)];
+          o[k] = tf32_part((K & 1) ? z.y : z.x, hl);
+        }
+      }
+    }
+    dst[e] = make_float4(o[0], o[1], o[2], o[3]);
+  }
+}
+
+void launch_tc_pack_v(const TCVJob* jobs, int njobs, const int4* colmap, const LRDesc* lr, cudaStream_t s) {
+  if (njobs > 0) tc_pack_v_kernel<<<njobs, 256, 0, s>>>(jobs, colmap, lr);
+}
+void launch_tc_pack_u(const TCUJob* jobs, int njobs, const LRDesc* lr, cudaStream_t s) {
+  if (njobs > 0) tc_pack_u_kernel<<<njobs, 256, 0, s>>>(jobs, lr);
+}
+
+// ---- self-test: one CTA, one 128 x N x (4 nkc) product ----------------------------------------
+// Shared memory leaves room beyond both panels, so that the descriptor reads stay inside the
+// allocation whatever the panel sizes of the test (N <= 64, nkc <= 4).
+#define TC_ST_A 40960
+#define TC_ST_B 16384
+__global__ void __launch_bounds__(128, 1) tc_selftest_kernel(const float4* a, const float4* b, int N, int nkc, float* d,
+                                                            int* err) {
+  extern __shared__ unsigned char tc_smem_raw[];
+  unsigned char* base = (unsigned char*)(((uintptr_t)tc_smem_raw + 1023) & ~(uintptr_t)1023);
+  TCSmem& S = *(TCSmem*)base;
+  unsigned char* sa = base + TC_HDR;
+  unsigned char* sb = sa + TC_ST_A;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (int i = threadIdx.x; i < (TC_ST_A + TC_ST_B) / 16; i += blockDim.x)
+    ((float4*)sa)[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+  if (threadIdx.x == 0) {
+    bar_init(&S.full[0], 1);
+    bar_init(&S.fin, 1);
+    S.abort_flag = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  if (warp == 0) tmem_alloc(&S.tmem, 64);
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = S.tmem;
+  volatile int* abort_flag = &S.abort_flag;
+  if (threadIdx.x == 0) {
+    const uint32_t ab = (uint32_t)nkc * 2048u, bb = (uint32_t)nkc * 32u * (uint32_t)N;
+    expect_tx(&S.full[0], ab + bb);
+    bulk_g2s(sa, a, ab, &S.full[0]);
+    bulk_g2s(sb, b, bb, &S.full[0]);
+    if (bar_wait(&S.full[0], 0, abort_flag, err)) {
+      tc_fence_after();
+      const uint32_t idesc = idesc_tf32(128, N), bstride = 32u * (uint32_t)N;
+      for (int k2 = 0; k2 < nkc; k2 += 2) {
+        const uint64_t ad = sdesc(su32(sa) + (uint32_t)k2 * 2048u, 2048u, 128u);
+        const uint64_t bh = sdesc(su32(sb) + (uint32_t)k2 * bstride, bstride, 128u);
+        const uint64_t bl = sdesc(su32(sb) + (uint32_t)k2 * bstride + 16u * (uint32_t)N, bstride, 128u);
+        mma_tf32(tmem, ad, bh, idesc, k2 > 0 ? 1u : 0u);
+        mma_tf32(tmem, ad, bl, idesc, 1u);
+      }
+      mma_commit(&S.fin);
+      bar_wait(&S.fin, 0, abort_flag, err);
+    }
+  }
+  __syncthreads();
+  tc_fence_after();
+  if (!*abort_flag) {
+    const int row = 32 * warp + lane;
+    for (int c = 0; c < N; c += 8) {
+      float v[8];
+      tmem_ld8(tmem + ((uint32_t)(32 * warp) << 16) + (uint32_t)c, v);
+      tmem_wait(v);
+#pragma unroll
+      for (int k = 0; k < 8; ++k) d[(size_t)row * N + c + k] = v[k];
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0) {
+    tc_fence_after();
+    tmem_dealloc(tmem, 64);
+  }
+}
+
+cudaError_t launch_tc_selftest(const void* a, const void* b, int N, int nkc, float* d, int* err, cudaStream_t s) {
+  if (N < 16 || N > 64 || N % 16 != 0 || nkc < 2 || nkc > 4 || nkc % 2 != 0) return cudaErrorInvalidValue;
+  const int smem = TC_HDR + TC_ST_A + TC_ST_B + 1024;
+  cudaError_t e = cudaFuncSetAttribute(tc_selftest_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  if (e != cudaSuccess) return e;
+  tc_selftest_kernel<<<1, 128, smem, s>>>((const float4*)a, (const float4*)b, N, nkc, d, err);
+  return cudaGetLastError();
+}
+
+}  // namespace bem
