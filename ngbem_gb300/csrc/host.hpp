@@ -195,10 +195,10 @@ struct HOperator : OperatorBase {
   // tc_host.cpp, tc_matvec.cu): packed operand panels built on first use
   int tc_mode = 1;   // 0: off (CUDA-core products)
   int tc_state = 0;  // 0 not built, 1 built, -1 not applicable to this operator or device
-  DevBuf d_tc_xa, d_tc_ta, d_tc_vp, d_tc_up, d_tc_y;
-  DevBuf d_tc_items[2], d_tc_segs[2], d_tc_sched[2], d_tc_outs;
-  DevBuf d_ro_leaves_tc, d_ro_ents_tc;
-  int tc_grid[2] = {0, 0}, tc_items[2] = {0, 0}, tc_nkc_x = 0, n_ro_leaves_tc = 0;
+  DevBuf d_tc_xa, d_tc_xa2, d_tc_ta, d_tc_vp, d_tc_up, d_tc_dp, d_tc_y;
+  DevBuf d_tc_items[2], d_tc_stages[2], d_tc_chunks[2], d_tc_sched[2], d_tc_outs;
+  DevBuf d_tc_leaves, d_tc_deltas;  // per leaf: the partial-row offsets of the row clusters holding it
+  int tc_grid[2] = {0, 0}, tc_items[2] = {0, 0}, tc_nkc_x = 0, tc_nkc_x2 = 0, n_tc_leaves = 0;
   long long tc_bytes = 0;
   double tc_ms_build = 0.0;
   bool tc_eligible(int trans, int nrhs, cudaStream_t s);

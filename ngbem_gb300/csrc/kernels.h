@@ -179,8 +179,6 @@ void launch_mv_pass(int prec, bool cplx, const MVArgs2& a, int grid, cudaStream_
 // gathers every dense block and low-rank U2 row slice that touches its rows, adds them up in
 // shared memory and stores its rows of y (no global atomics).  entries: {kind (0 dense,
 // 1 low rank), block, first local row, rows}; leaves: {first row, end row, first entry, end}.
-// Kind 2 (tensor-core products): {2, delta, first global row, rows} adds the complex64 rows
-// ypart[(i + delta) * 32 + rhs] of a row cluster's partial product.
 struct MVRowArgs {
   const int4* leaves;
   int nleaves;
@@ -192,7 +190,6 @@ struct MVRowArgs {
   void* yp;         // permuted y (FP64 / complex128), written
   int nrhs;
   int compensated;
-  const void* ypart;  // kind-2 partial rows (complex64, 32 right-hand sides per row)
 };
 void launch_mv_rowowner(int prec, bool cplx, const MVRowArgs& a, cudaStream_t s);
 int mv_stage_bytes();
@@ -252,12 +249,23 @@ struct TCOut {            // pass 0: one low-rank block of a column tile
   unsigned long long ta;  // its A panel for pass 1 (128 x 2 rpad)
   int col, rpad;          // first accumulator column; rank padded to a multiple of 4
 };
+// One K range of a segment in a pipeline stage (planned on the host): A at byte `off` of the
+// stage, B right after it.  flags: 1 first range of an item, 2 last range of an item, 4 last
+// range of the stage.
+struct TCChunk {
+  unsigned long long a, b;
+  unsigned int abytes, bbytes, off;
+  unsigned short N, flags;
+};
+static_assert(sizeof(TCChunk) == 32, "TCChunk is bulk-copied");
+#define TC_MAXCH 16  // ranges per stage
 struct TCGemmArgs {
   const TCItem* items;
-  const TCSeg* segs;
   const TCOut* outs;
-  const int2* sched;  // per CTA: first item, item count
-  void* ypart;        // pass 1 output (complex64 rows of 32 right-hand sides)
+  const int4* sched;     // per CTA: first item, items, first stage, stages
+  const int2* stages;    // per stage: first range, ranges
+  const TCChunk* chunks;
+  void* ypart;           // pass 1 output (complex64 rows of 32 right-hand sides)
   int* err;
 };
 struct TCVJob {  // pack the V2 panel of a column tile
@@ -268,19 +276,28 @@ struct TCUJob {  // pack the U2 panel of (row tile, block)
   unsigned long long dst;
   int lr, i0, rows, N, nkc, pad;
 };
-#define TC_CAP (48 * 1024)  // bytes of one pipeline stage
-// K cores per stage for an MMA N (even, at least 2)
-__host__ __device__ inline int tc_kcs(int N) {
-  int k = (TC_CAP / (2048 + 32 * N)) & ~1;
-  return k < 2 ? 2 : k;
-}
+struct TCDJob {  // pack the panel of (row tile, dense block): K = (column, real/imaginary)
+  unsigned long long dst;
+  int blk, i0, rows, N, kc0, nkc;
+};
+#define TC_CAP (48 * 1024)  // bytes of one pipeline stage (one MMA step of N = 256 takes 20 KB)
 int tc_smem_bytes();
 // 1 when the running device executes the tcgen05 kernels (compute capability 10.x)
 int tc_supported();
-// xa (A panel, nkc cores) from x: x[r * ld + perm[j]] (complex128) for dof j, r < nrhs
-void launch_tc_xprep(const int* perm, int n, int nrhs, int ld, const void* x, void* xa, int nkc, cudaStream_t s);
+// A panels of x = x[r * ld + perm[j]] (complex128), dof j in cluster order, r < nrhs:
+//   xa  (nkc cores): K = dof (4 per core), row (r, a, h) the h part of Re/Im x;
+//   xa2 (nkc2 cores): K = (dof, c) (2 dofs per core), row (r, a, h) the h part of
+//       a = 0: (Re x, -Im x), a = 1: (Im x, Re x), so that a real product with the
+//       (Re D, Im D) columns of a complex block gives Re and Im of D x.
+void launch_tc_xprep(const int* perm, int n, int nrhs, int ld, const void* x, void* xa, int nkc, void* xa2, int nkc2,
+                     cudaStream_t s);
 void launch_tc_pack_v(const TCVJob* jobs, int njobs, const int4* colmap, const LRDesc* lr, cudaStream_t s);
 void launch_tc_pack_u(const TCUJob* jobs, int njobs, const LRDesc* lr, cudaStream_t s);
+void launch_tc_pack_d(const TCDJob* jobs, int njobs, const MVDense* dense, cudaStream_t s);
+// y[r * ld + perm[i]] = alpha * sum_e ypart[(i + delta[e]) * 32 + r] + beta * y[...] over the
+// entries [L.z, L.w) of the leaf L = {first row, end row, first entry, end entry} holding row i
+void launch_tc_ysum_out(const int4* leaves, int nleaves, const int* deltas, const void* ypart, const int* perm,
+                        int nrhs, int ld, const double* alpha, const double* beta, void* y, cudaStream_t s);
 // pass 0 (pass = 0): T panels of every low-rank block; pass 1: partial rows of U2 T
 cudaError_t launch_tc_gemm(int pass, const TCGemmArgs& g, int grid, cudaStream_t s);
 // one 128 x N x (4 nkc) product D = A B^T on the tensor cores from ready panels (self-test):

@@ -942,20 +942,10 @@ __global__ void __launch_bounds__(256) mv_rowowner_kernel(MVRowArgs a) {
         // rows of this entry (global, permuted) inside the tile
         int i0, i1, gr0;
         if (E.x == 0) gr0 = a.dense[E.y].r0;
-        else if (E.x == 1) gr0 = a.lr[E.y].r0;
-        else gr0 = 0;
+        else gr0 = a.lr[E.y].r0;
         i0 = max(t0, gr0 + E.z);
         i1 = min(t1, gr0 + E.z + E.w);
         if (rh >= nr) continue;
-        if (E.x == 2) {
-          // partial rows of a row cluster's tensor-core product (complex64, 32 per row)
-          const float2* Yp = (const float2*)a.ypart;
-          for (int i = i0; i < i1; ++i) {
-            const float2 v = Yp[(size_t)(i + E.y) * 32 + rh];
-            shared_add(&ysm[i - t0][lane], mk_d<D>((double)v.x, (double)v.y));
-          }
-          continue;
-        }
         for (int ib = i0; ib < i1; ib += MV_MR) {
           const int no = min(MV_MR, i1 - ib);
           AccT acc[MV_MR];

@@ -1,8 +1,8 @@
 // Host side of the tensor-core products for several right-hand sides (kernels in
-// tc_matvec.cu): tiles of the low-rank blocks, their packed operand panels, a balanced static
-// item list per CTA, the owner-computes lists that add the partial rows, and the application
-// Y = A X for 2..32 complex right-hand sides (reference HMatrix::MultAdd, src/hmat.cpp:647-655,
-// applied to many vectors at once).
+// tc_matvec.cu): column and row tiles of the blocks, their packed operand panels, a balanced
+// static item list per CTA, the per-leaf lists of partial rows, and the application Y = A X for
+// 2..32 complex right-hand sides (reference HMatrix::MultAdd, src/hmat.cpp:647-655, applied to
+// many vectors at once).
 #include <algorithm>
 #include <chrono>
 #include <climits>
@@ -91,6 +91,57 @@ void balance(std::vector<TCItem>& items, const std::vector<double>& cost, int ns
     sched[c].y = (int)per[c].size();
   }
   items.swap(out);
+}
+
+// Stage plans of every CTA: the K ranges of its items' segments in order, packed into
+// pipeline stages of TC_CAP bytes (at most TC_MAXCH ranges, each at least one MMA step of
+// K = 8), so that the kernel reads one contiguous run of descriptors per stage.
+void plan_stages(const std::vector<TCItem>& items, const std::vector<TCSeg>& segs, const std::vector<int2>& sched,
+                 std::vector<int4>& sched4, std::vector<int2>& stages, std::vector<TCChunk>& chunks) {
+  sched4.assign(sched.size(), make_int4(0, 0, 0, 0));
+  for (size_t c = 0; c < sched.size(); ++c) {
+    const int s0 = (int)stages.size();
+    int used = 0, first = (int)chunks.size();
+    auto close = [&]() {
+      if ((int)chunks.size() > first) {
+        chunks.back().flags |= 4;
+        stages.push_back(make_int2(first, (int)chunks.size() - first));
+      }
+      first = (int)chunks.size();
+      used = 0;
+    };
+    for (int ii = sched[c].x; ii < sched[c].x + sched[c].y; ++ii) {
+      const TCItem& I = items[ii];
+      const int per = 2048 + 32 * I.N;
+      bool item_first = true;
+      for (int sg = I.seg0; sg < I.seg0 + I.nseg; ++sg) {
+        const TCSeg& S = segs[sg];
+        for (int kc = 0; kc < S.nkc;) {
+          const int fit = ((TC_CAP - used) / per) & ~1;
+          if (fit < 2 || (int)chunks.size() - first >= TC_MAXCH) {
+            close();
+            continue;
+          }
+          const int kcs = std::min(S.nkc - kc, fit);
+          TCChunk ch{};
+          ch.a = S.a + (unsigned long long)kc * 2048;
+          ch.b = S.b + (unsigned long long)kc * 32 * I.N;
+          ch.abytes = (unsigned)kcs * 2048;
+          ch.bbytes = (unsigned)kcs * 32 * I.N;
+          ch.off = (unsigned)used;
+          ch.N = (unsigned short)I.N;
+          ch.flags = item_first ? 1 : 0;
+          item_first = false;
+          used += kcs * per;
+          kc += kcs;
+          if (kc >= S.nkc && sg == I.seg0 + I.nseg - 1) ch.flags |= 2;
+          chunks.push_back(ch);
+        }
+      }
+    }
+    close();
+    sched4[c] = make_int4(sched[c].x, sched[c].y, s0, (int)stages.size() - s0);
+  }
 }
 
 }  // namespace
@@ -195,23 +246,35 @@ void HOperator::build_tc() {
       vp_bytes += (long long)nkc * 32 * N;
     }
   }
-  // pass 1: blocks grouped by row cluster; row tiles of <= 256 rows, one segment per block
+  // pass 1: low-rank and dense blocks grouped by row cluster; row tiles of <= 256 rows, one
+  // segment per block (U2 T for low rank, D X through the second X panel for dense)
+  tc_nkc_x2 = (width + 1) / 2 + 2;
+  std::map<std::pair<int, int>, std::vector<int>> drows;
+  for (int k = 0; k < (int)mvdense.size(); ++k) {
+    drows[{mvdense[k].r0, mvdense[k].m}].push_back(k);
+    rows[{mvdense[k].r0, mvdense[k].m}];  // make sure the row cluster has an entry
+  }
   std::vector<TCItem> it1;
   std::vector<double> cost1;
   std::vector<TCSeg> sg1;
+  std::vector<int> sg1_kind;  // 0: U2 segment (A = T panel), 1: dense segment (A = second X panel)
   std::vector<TCUJob> ujobs;
-  long long up_bytes = 0, yrows = 0;
+  std::vector<TCDJob> djobs;
+  long long up_bytes = 0, dp_bytes = 0, yrows = 0;
   struct RowGroup { int r0, m; long long yoff; };
   std::vector<RowGroup> rgroups;
+  const std::vector<int> none;
   for (auto& kv : rows) {
     const int r0 = kv.first.first, m = kv.first.second;
+    auto dit = drows.find(kv.first);
+    const std::vector<int>& dk = dit == drows.end() ? none : dit->second;
     rgroups.push_back({r0, m, yrows});
     for (int i0 = 0; i0 < m; i0 += 256) {
       const int nr = std::min(256, m - i0);
       const int N = (nr + 15) & ~15;
       TCItem I{};
       I.seg0 = (int)sg1.size();
-      I.nseg = (int)kv.second.size();
+      I.nseg = (int)(kv.second.size() + dk.size());
       I.N = N;
       I.out0 = (int)(yrows + i0);
       I.nout = nr;
@@ -229,9 +292,30 @@ void HOperator::build_tc() {
         S.b = J.dst;
         S.nkc = J.nkc;
         sg1.push_back(S);
+        sg1_kind.push_back(0);
         ujobs.push_back(J);
         c += (double)J.nkc * (2048.0 + 32.0 * N);
         up_bytes += (long long)J.nkc * 32 * N;
+      }
+      for (int k : dk) {
+        const MVDense& D = mvdense[k];
+        TCDJob J{};
+        J.dst = (unsigned long long)dp_bytes;
+        J.blk = k;
+        J.i0 = i0;
+        J.rows = nr;
+        J.N = N;
+        J.kc0 = D.c0 / 2;
+        J.nkc = ((D.c0 + D.n + 1) / 2 - J.kc0 + 1) & ~1;
+        TCSeg S{};
+        S.a = (unsigned long long)J.kc0 * 2048;
+        S.b = J.dst;
+        S.nkc = J.nkc;
+        sg1.push_back(S);
+        sg1_kind.push_back(1);
+        djobs.push_back(J);
+        c += (double)J.nkc * (2048.0 + 32.0 * N);
+        dp_bytes += (long long)J.nkc * 32 * N;
       }
       it1.push_back(I);
       cost1.push_back(c);
@@ -239,14 +323,17 @@ void HOperator::build_tc() {
     yrows += m;
   }
   if (yrows > INT_MAX / 2) return;  // partial row offsets are ints
-  // device buffers: X panel, T panels, packed V2 and U2 panels, partial rows
+  // device buffers: X panels, T panels, packed V2, U2 and dense panels, partial rows
   d_tc_xa.alloc((size_t)tc_nkc_x * 2048);
+  d_tc_xa2.alloc((size_t)tc_nkc_x2 * 2048);
   d_tc_ta.alloc((size_t)std::max(ta_bytes, 16LL));
   d_tc_vp.alloc((size_t)std::max(vp_bytes, 16LL));
   d_tc_up.alloc((size_t)std::max(up_bytes, 16LL));
+  d_tc_dp.alloc((size_t)std::max(dp_bytes, 16LL));
   d_tc_y.alloc((size_t)std::max(yrows, 1LL) * 32 * 8);
-  const unsigned long long xa = (unsigned long long)d_tc_xa.p, ta = (unsigned long long)d_tc_ta.p;
-  const unsigned long long vp = (unsigned long long)d_tc_vp.p, up = (unsigned long long)d_tc_up.p;
+  const unsigned long long xa = (unsigned long long)d_tc_xa.p, xa2 = (unsigned long long)d_tc_xa2.p;
+  const unsigned long long ta = (unsigned long long)d_tc_ta.p, vp = (unsigned long long)d_tc_vp.p;
+  const unsigned long long up = (unsigned long long)d_tc_up.p, dp = (unsigned long long)d_tc_dp.p;
   for (TCVJob& J : vjobs) J.dst += vp;
   for (TCSeg& S : sg0) {
     S.a += xa;
@@ -254,9 +341,10 @@ void HOperator::build_tc() {
   }
   for (TCOut& O : outs) O.ta += ta;
   for (TCUJob& J : ujobs) J.dst += up;
-  for (TCSeg& S : sg1) {
-    S.a += ta;
-    S.b += up;
+  for (TCDJob& J : djobs) J.dst += dp;
+  for (size_t q = 0; q < sg1.size(); ++q) {
+    sg1[q].a += sg1_kind[q] ? xa2 : ta;
+    sg1[q].b += sg1_kind[q] ? dp : up;
   }
   int dev = 0, nsm = 152;
   BEM_CUDA(cudaGetDevice(&dev));
@@ -266,58 +354,65 @@ void HOperator::build_tc() {
   balance(it1, cost1, nsm, sch1);
   tc_grid[0] = it0.empty() ? 0 : (int)sch0.size();
   tc_grid[1] = it1.empty() ? 0 : (int)sch1.size();
+  {
+    std::vector<int4> s4;
+    std::vector<int2> stg;
+    std::vector<TCChunk> chk;
+    plan_stages(it0, sg0, sch0, s4, stg, chk);
+    d_tc_sched[0].upload(s4);
+    d_tc_stages[0].upload(stg);
+    d_tc_chunks[0].upload(chk);
+    s4.clear();
+    stg.clear();
+    chk.clear();
+    plan_stages(it1, sg1, sch1, s4, stg, chk);
+    d_tc_sched[1].upload(s4);
+    d_tc_stages[1].upload(stg);
+    d_tc_chunks[1].upload(chk);
+  }
   d_tc_items[0].upload(it0);
   d_tc_items[1].upload(it1);
-  d_tc_segs[0].upload(sg0);
-  d_tc_segs[1].upload(sg1);
-  d_tc_sched[0].upload(sch0);
-  d_tc_sched[1].upload(sch1);
   d_tc_outs.upload(outs);
   // pack the factors (once)
   {
-    DevBuf dv, du, dcm;
+    DevBuf dv, du, dd, dcm;
     dv.upload(vjobs);
     du.upload(ujobs);
+    dd.upload(djobs);
     dcm.upload(colmap);
     launch_tc_pack_v(dv.as<TCVJob>(), (int)vjobs.size(), dcm.as<int4>(), d_mvlr.as<LRDesc>(), 0);
     launch_tc_pack_u(du.as<TCUJob>(), (int)ujobs.size(), d_mvlr.as<LRDesc>(), 0);
+    launch_tc_pack_d(dd.as<TCDJob>(), (int)djobs.size(), d_mvdense.as<MVDense>(), 0);
     BEM_CUDA(cudaGetLastError());
     BEM_CUDA(cudaDeviceSynchronize());
   }
-  // owner-computes lists: every dense block (kind 0) and every row cluster's partial rows
-  // (kind 2) that touch a leaf's rows
+  // per leaf: the partial-row offsets (row i of the leaf at i + delta) of every row cluster
+  // that holds it (row clusters nest, so each either holds the whole leaf or none of it)
   {
     std::vector<std::pair<int, int>> lv;
     for (const ClusterH& C : ttest->cl)
       if (C.Child1 < 0) lv.push_back({(int)C.PermuPos, (int)(C.PermuPos + C.Number)});
     std::sort(lv.begin(), lv.end());
-    std::vector<std::vector<int4>> per(lv.size());
-    auto for_leaves = [&](int r0, int m, auto&& fn) {
-      int l = (int)(std::upper_bound(lv.begin(), lv.end(), std::make_pair(r0, INT_MAX)) - lv.begin()) - 1;
-      for (l = std::max(l, 0); l < (int)lv.size() && lv[l].first < r0 + m; ++l) {
-        const int a0 = std::max(r0, lv[l].first), a1 = std::min(r0 + m, lv[l].second);
-        if (a1 > a0) fn(l, a0, a1);
-      }
-    };
-    for (int k = 0; k < (int)mvdense.size(); ++k)
-      for_leaves(mvdense[k].r0, mvdense[k].m,
-                 [&](int l, int a0, int a1) { per[l].push_back(make_int4(0, k, a0 - mvdense[k].r0, a1 - a0)); });
-    for (const RowGroup& g : rgroups)
-      for_leaves(g.r0, g.m, [&](int l, int a0, int a1) {
-        per[l].push_back(make_int4(2, (int)(g.yoff - g.r0), a0, a1 - a0));
-      });
-    std::vector<int4> leaves, ents;
-    for (size_t l = 0; l < lv.size(); ++l) {
-      const int e0 = (int)ents.size();
-      ents.insert(ents.end(), per[l].begin(), per[l].end());
-      leaves.push_back(make_int4(lv[l].first, lv[l].second, e0, (int)ents.size()));
+    std::vector<std::vector<int>> per(lv.size());
+    for (const RowGroup& g : rgroups) {
+      int l = (int)(std::upper_bound(lv.begin(), lv.end(), std::make_pair(g.r0, INT_MAX)) - lv.begin()) - 1;
+      for (l = std::max(l, 0); l < (int)lv.size() && lv[l].first < g.r0 + g.m; ++l)
+        if (lv[l].first >= g.r0 && lv[l].second <= g.r0 + g.m) per[l].push_back((int)(g.yoff - g.r0));
     }
-    d_ro_leaves_tc.upload(leaves);
-    d_ro_ents_tc.upload(ents);
-    n_ro_leaves_tc = (int)leaves.size();
+    std::vector<int4> leaves;
+    std::vector<int> deltas;
+    for (size_t l = 0; l < lv.size(); ++l) {
+      const int e0 = (int)deltas.size();
+      deltas.insert(deltas.end(), per[l].begin(), per[l].end());
+      leaves.push_back(make_int4(lv[l].first, lv[l].second, e0, (int)deltas.size()));
+    }
+    d_tc_leaves.upload(leaves);
+    d_tc_deltas.upload(deltas);
+    n_tc_leaves = (int)leaves.size();
   }
   BEM_CUDA(cudaDeviceSynchronize());
-  tc_bytes = (long long)(d_tc_xa.bytes + d_tc_ta.bytes + d_tc_vp.bytes + d_tc_up.bytes + d_tc_y.bytes);
+  tc_bytes = (long long)(d_tc_xa.bytes + d_tc_xa2.bytes + d_tc_ta.bytes + d_tc_vp.bytes + d_tc_up.bytes +
+                         d_tc_dp.bytes + d_tc_y.bytes);
   tc_items[0] = (int)it0.size();
   tc_items[1] = (int)it1.size();
   tc_ms_build = std::chrono::duration<double, std::milli>(clk::now() - t0).count();
@@ -325,8 +420,9 @@ void HOperator::build_tc() {
 }
 
 void HOperator::release_tc() {
-  for (DevBuf* b : {&d_tc_xa, &d_tc_ta, &d_tc_vp, &d_tc_up, &d_tc_y, &d_tc_items[0], &d_tc_items[1], &d_tc_segs[0],
-                    &d_tc_segs[1], &d_tc_sched[0], &d_tc_sched[1], &d_tc_outs, &d_ro_leaves_tc, &d_ro_ents_tc})
+  for (DevBuf* b : {&d_tc_xa, &d_tc_xa2, &d_tc_ta, &d_tc_vp, &d_tc_up, &d_tc_dp, &d_tc_y, &d_tc_items[0],
+                    &d_tc_items[1], &d_tc_stages[0], &d_tc_stages[1], &d_tc_chunks[0], &d_tc_chunks[1],
+                    &d_tc_sched[0], &d_tc_sched[1], &d_tc_outs, &d_tc_leaves, &d_tc_deltas})
     b->release();
   tc_state = 0;
   tc_bytes = 0;
@@ -340,35 +436,23 @@ void HOperator::mult_tc(const double* alpha, const void* x, const double* beta, 
     for (auto& e : ev) BEM_CUDA(cudaEventCreate(&e));
     BEM_CUDA(cudaEventRecord(ev[0], s));
   }
-  launch_permute_in(prec, cplx, perm, width, nrhs, width, x, d_xp.p, s);  // dense blocks' input
-  launch_tc_xprep(perm, width, nrhs, width, x, d_tc_xa.p, tc_nkc_x, s);
+  launch_tc_xprep(perm, width, nrhs, width, x, d_tc_xa.p, tc_nkc_x, d_tc_xa2.p, tc_nkc_x2, s);
   if (profiling) BEM_CUDA(cudaEventRecord(ev[1], s));
   for (int pass = 0; pass < 2; ++pass) {
     TCGemmArgs g{};
     g.items = d_tc_items[pass].as<TCItem>();
-    g.segs = d_tc_segs[pass].as<TCSeg>();
     g.outs = d_tc_outs.as<TCOut>();
-    g.sched = d_tc_sched[pass].as<int2>();
+    g.sched = d_tc_sched[pass].as<int4>();
+    g.stages = d_tc_stages[pass].as<int2>();
+    g.chunks = d_tc_chunks[pass].as<TCChunk>();
     g.ypart = d_tc_y.p;
     g.err = d_err.as<int>();
     BEM_CUDA(launch_tc_gemm(pass, g, tc_grid[pass], s));
     if (profiling && pass == 0) BEM_CUDA(cudaEventRecord(ev[2], s));
   }
-  MVRowArgs ra{};
-  ra.leaves = d_ro_leaves_tc.as<int4>();
-  ra.nleaves = n_ro_leaves_tc;
-  ra.ents = d_ro_ents_tc.as<int4>();
-  ra.dense = d_mvdense.as<MVDense>();
-  ra.lr = d_mvlr.as<LRDesc>();
-  ra.xp = d_xp.p;
-  ra.tx = d_tx.p;
-  ra.yp = d_yp.p;
-  ra.nrhs = nrhs;
-  ra.compensated = 0;
-  ra.ypart = d_tc_y.p;
-  launch_mv_rowowner(prec, cplx, ra, s);
   if (profiling) BEM_CUDA(cudaEventRecord(ev[3], s));
-  launch_permute_out(cplx, pout, height, nrhs, height, alpha, beta, d_yp.p, y, s);
+  launch_tc_ysum_out(d_tc_leaves.as<int4>(), n_tc_leaves, d_tc_deltas.as<int>(), d_tc_y.p, pout, nrhs, height, alpha,
+                     beta, y, s);
   if (profiling) {
     BEM_CUDA(cudaEventRecord(ev[4], s));
     pending.push_back(ev);

@@ -6,10 +6,11 @@
 //   pass 0: T_b = V2_b X[cols b] for every low-rank block b.  The blocks of one column cluster
 //           are stacked along N (one X panel feeds all of them); every block's T is written
 //           once, as the A panel of pass 1.
-//   pass 1: Y_tau = sum_b U2_b T_b over the blocks of one row cluster tau; the tensor memory
-//           accumulates over all of them and the tile is stored once into a per-row-cluster
-//           partial buffer.  The owner-computes kernel (matvec.cu) adds, for each leaf, the
-//           partials of every row cluster that contains it to the leaf's dense products.
+//   pass 1: Y_tau = sum_b U2_b T_b + sum_d D_d X[cols d] over the low-rank blocks b and the
+//           dense blocks d of one row cluster tau; the tensor memory accumulates over all of
+//           them and the tile is stored once into a per-row-cluster partial buffer.  A last
+//           kernel sums, for each row, the partials of every row cluster that holds it and
+//           writes y through the output permutation with alpha and beta.
 //
 // Complex products run as real products.  Rows of the A side are (right-hand side r, real or
 // imaginary part a, TF32 high or low part h) at 4 r + 2 a + h, so M = 128 for 32 right-hand
@@ -26,6 +27,7 @@
 //               imaginary and high and low rows with warp shuffles, global stores.
 // Every wait is bounded: a wait that runs out sets an error bit, the CTA drains what it
 // issued and frees its tensor memory.
+#include <algorithm>
 #include <cstdint>
 
 #include "bem_device.cuh"
@@ -36,7 +38,8 @@ namespace bem {
 #define TC_NST 4
 #define TC_THREADS 192
 #define TC_ACC_COLS 256
-#define TC_HDR 1024
+#define TC_HDR 4096  // barriers, then the range descriptors of each stage (TC_MAXCH x 32 bytes)
+#define TC_DESC 1024
 #define TC_ERR_WAIT 0x100
 
 namespace {
@@ -185,80 +188,98 @@ __global__ void __launch_bounds__(TC_THREADS, 1) tc_gemm_kernel(TCGemmArgs g) {
   tc_fence_after();
   const uint32_t tmem = S.tmem;
   volatile int* abort_flag = &S.abort_flag;
-  const int2 my = g.sched[blockIdx.x];
+  const int4 my = g.sched[blockIdx.x];
 
+  const int iend = my.x + my.y;
+  TCChunk* desc = (TCChunk*)(base + TC_DESC);  // [TC_NST][TC_MAXCH]
   if (warp == 0) {
-    if (lane == 0) {
-      int it = 0;
-      bool ok = true;
-      for (int ii = my.x; ok && ii < my.x + my.y; ++ii) {
-        const TCItem I = g.items[ii];
-        const int kmax = tc_kcs(I.N);
-        for (int sg = I.seg0; ok && sg < I.seg0 + I.nseg; ++sg) {
-          const TCSeg Sg = g.segs[sg];
-          for (int kc = 0; kc < Sg.nkc; kc += kmax) {
-            const int kcs = min(kmax, Sg.nkc - kc);
-            const int s = it % TC_NST;
-            if (!bar_wait(&S.empty[s], ((it / TC_NST) & 1) ^ 1, abort_flag, g.err)) {
-              ok = false;
-              break;
-            }
-            unsigned char* st = stages + (size_t)s * TC_CAP;
-            const uint32_t ab = (uint32_t)kcs * 2048u, bb = (uint32_t)kcs * 32u * (uint32_t)I.N;
-            expect_tx(&S.full[s], ab + bb);
-            bulk_g2s(st, (const unsigned char*)Sg.a + (size_t)kc * 2048, ab, &S.full[s]);
-            bulk_g2s(st + ab, (const unsigned char*)Sg.b + (size_t)kc * 32 * I.N, bb, &S.full[s]);
-            ++it;
-          }
-        }
+    // producer warp: lane c loads range c of the next stage while the current stage's slot is
+    // awaited, then every lane issues its own range's two bulk copies, and lane 0 copies the
+    // range descriptors next to the payload for the MMA thread
+    const int s_end = my.z + my.w;
+    int it = 0;
+    int2 st = my.w > 0 ? g.stages[my.z] : make_int2(0, 0);
+    TCChunk cd{};
+    if (my.w > 0 && lane < st.y) cd = g.chunks[st.x + lane];
+    for (int si = my.z; si < s_end; ++si, ++it) {
+      // prefetch the next stage's descriptors
+      int2 st_n = make_int2(0, 0);
+      TCChunk cd_n{};
+      if (si + 1 < s_end) {
+        st_n = g.stages[si + 1];
+        if (lane < st_n.y) cd_n = g.chunks[st_n.x + lane];
       }
-      // drain: wait until the MMA thread released every stage still filled, so that no copy
-      // or commit arrival is in flight when the CTA ends
+      uint32_t bytes = lane < st.y ? cd.abytes + cd.bbytes : 0u;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) bytes += __shfl_xor_sync(0xffffffffu, bytes, o);
+      const int slot = it % TC_NST;
+      int ok = 1;
+      if (lane == 0) {
+        ok = bar_wait(&S.empty[slot], ((it / TC_NST) & 1) ^ 1, abort_flag, g.err) ? 1 : 0;
+        if (ok) expect_tx(&S.full[slot], bytes + (uint32_t)st.y * (uint32_t)sizeof(TCChunk));
+      }
+      ok = __shfl_sync(0xffffffffu, ok, 0);
+      if (!ok) break;
+      unsigned char* sp = stages + (size_t)slot * TC_CAP;
+      if (lane < st.y) {
+        bulk_g2s(sp + cd.off, (const void*)cd.a, cd.abytes, &S.full[slot]);
+        bulk_g2s(sp + cd.off + cd.abytes, (const void*)cd.b, cd.bbytes, &S.full[slot]);
+      }
+      if (lane == 0)
+        bulk_g2s(desc + slot * TC_MAXCH, g.chunks + st.x, (uint32_t)st.y * (uint32_t)sizeof(TCChunk), &S.full[slot]);
+      st = st_n;
+      cd = cd_n;
+    }
+    // drain: wait until the MMA thread released every stage still filled, so that no copy
+    // or commit arrival is in flight when the CTA ends
+    if (lane == 0)
       for (int j = it > TC_NST ? it - TC_NST : 0; j < it; ++j)
         bar_wait(&S.empty[j % TC_NST], (j / TC_NST) & 1, abort_flag, g.err);
-    }
   } else if (warp == 1) {
     if (lane == 0) {
-      int it = 0, acc_it = 0;
+      int acc_it = 0, acc = 0;
+      uint32_t d = 0, idesc = 0, accumulate = 0;
       bool ok = true, issued = false;
-      for (int ii = my.x; ok && ii < my.x + my.y; ++ii) {
-        const TCItem I = g.items[ii];
-        const int kmax = tc_kcs(I.N);
-        const int acc = acc_it & 1;
-        if (!bar_wait(&S.acce[acc], ((acc_it >> 1) & 1) ^ 1, abort_flag, g.err)) break;
+      for (int it = 0; ok && it < my.w; ++it) {
+        const int slot = it % TC_NST;
+        if (!bar_wait(&S.full[slot], (it / TC_NST) & 1, abort_flag, g.err)) break;
         tc_fence_after();
-        const uint32_t d = tmem + (uint32_t)(acc * TC_ACC_COLS);
-        const uint32_t idesc = idesc_tf32(128, I.N);
-        const uint32_t bstride = 32u * (uint32_t)I.N;
-        uint32_t accumulate = 0;
-        for (int sg = I.seg0; ok && sg < I.seg0 + I.nseg; ++sg) {
-          const int nkc = g.segs[sg].nkc;
-          for (int kc = 0; kc < nkc; kc += kmax) {
-            const int kcs = min(kmax, nkc - kc);
-            const int s = it % TC_NST;
-            if (!bar_wait(&S.full[s], (it / TC_NST) & 1, abort_flag, g.err)) {
+        const uint32_t sp = su32(stages + (size_t)slot * TC_CAP);
+        const TCChunk* cds = desc + slot * TC_MAXCH;
+        for (int c = 0; c < TC_MAXCH; ++c) {
+          const TCChunk cd = cds[c];
+          if (cd.flags & 1) {
+            // first range of an item: take the accumulator the epilogue released
+            acc = acc_it & 1;
+            if (!bar_wait(&S.acce[acc], ((acc_it >> 1) & 1) ^ 1, abort_flag, g.err)) {
               ok = false;
               break;
             }
             tc_fence_after();
-            const uint32_t sa = su32(stages + (size_t)s * TC_CAP);
-            const uint32_t sb = sa + (uint32_t)kcs * 2048u;
-            for (int k2 = 0; k2 < kcs; k2 += 2) {
-              const uint64_t ad = sdesc(sa + (uint32_t)k2 * 2048u, 2048u, 128u);
-              const uint64_t bh = sdesc(sb + (uint32_t)k2 * bstride, bstride, 128u);
-              const uint64_t bl = sdesc(sb + (uint32_t)k2 * bstride + 16u * (uint32_t)I.N, bstride, 128u);
-              mma_tf32(d, ad, bh, idesc, accumulate);
-              mma_tf32(d, ad, bl, idesc, 1u);
-              accumulate = 1;
-            }
-            issued = true;
-            mma_commit(&S.empty[s]);
-            ++it;
+            d = tmem + (uint32_t)(acc * TC_ACC_COLS);
+            idesc = idesc_tf32(128, cd.N);
+            accumulate = 0;
           }
+          const uint32_t N = cd.N, bstride = 32u * N, kcs = cd.abytes / 2048u;
+          const uint32_t sa = sp + cd.off, sb = sa + cd.abytes;
+          for (uint32_t k2 = 0; k2 < kcs; k2 += 2) {
+            const uint64_t ad = sdesc(sa + k2 * 2048u, 2048u, 128u);
+            const uint64_t bh = sdesc(sb + k2 * bstride, bstride, 128u);
+            const uint64_t bl = sdesc(sb + k2 * bstride + 16u * N, bstride, 128u);
+            mma_tf32(d, ad, bh, idesc, accumulate);
+            mma_tf32(d, ad, bl, idesc, 1u);
+            accumulate = 1;
+          }
+          issued = true;
+          if (cd.flags & 2) {
+            // last range of the item: hand the accumulator to the epilogue
+            mma_commit(&S.accf[acc]);
+            ++acc_it;
+          }
+          if (cd.flags & 4) break;
         }
         if (!ok) break;
-        mma_commit(&S.accf[acc]);
-        ++acc_it;
+        mma_commit(&S.empty[slot]);
       }
       if (issued) {
         mma_commit(&S.fin);
@@ -272,7 +293,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) tc_gemm_kernel(TCGemmArgs g) {
     const int rhs = row >> 2, a = (row >> 1) & 1, h = row & 1;
     const unsigned FULL = 0xffffffffu;
     int acc_it = 0;
-    for (int ii = my.x; ii < my.x + my.y; ++ii) {
+    for (int ii = my.x; ii < iend; ++ii) {
       const TCItem I = g.items[ii];
       const int acc = acc_it & 1;
       int ok = 1;
@@ -373,33 +394,51 @@ cudaError_t launch_tc_gemm(int pass, const TCGemmArgs& g, int grid, cudaStream_t
 }
 
 // ---- operand preparation ----------------------------------------------------------------------
-// A panel of X: row 4 r + 2 a + h, K core kc holds dofs 4 kc .. 4 kc + 3 (cluster order)
-__global__ void tc_xprep_kernel(const int* perm, int n, int nrhs, int ld, const double2* x, float4* xa, int nkc) {
-  const long long total = (long long)nkc * 128;
-  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
-       t += (long long)gridDim.x * blockDim.x) {
-    const int kc = (int)(t >> 7), row = (int)(t & 127);
-    const int r = row >> 2, a = (row >> 1) & 1, h = row & 1;
+// A panels of x: xa with K = dof (core kc: dofs 4 kc .. 4 kc + 3), xa2 with K = (dof, c) (core
+// kc: dofs 2 kc, 2 kc + 1), row 4 r + 2 a + h
+// one CTA (128 threads) per K core of xa (4 dofs), which also fills cores 2 kc and 2 kc + 1 of
+// xa2: the 4 x 32 complex values are read once (through the permutation) and rounded to FP32
+// in shared memory (one FP64 conversion per value: the FP64 pipe is narrow on this part), then
+// thread = panel row splits them in FP32 and writes one 16-byte entry of each core
+__global__ void __launch_bounds__(128) tc_xprep_kernel(const int* perm, int n, int nrhs, int ld, const double2* x,
+                                                       float4* xa, int nkc, float4* xa2, int nkc2) {
+  __shared__ float2 z[32][4];
+  const int t = threadIdx.x;
+  const int r = t >> 2, a = (t >> 1) & 1, h = t & 1;
+  for (int kc = blockIdx.x; kc < nkc; kc += gridDim.x) {
+    {
+      const int j = 4 * kc + (t & 3);
+      float2 v = make_float2(0.f, 0.f);
+      if (j < n && (t >> 2) < nrhs) {
+        const double2 w = x[(size_t)(t >> 2) * ld + perm[j]];
+        v = make_float2((float)w.x, (float)w.y);
+      }
+      z[t >> 2][t & 3] = v;
+    }
+    __syncthreads();
     float o[4];
 #pragma unroll
-    for (int k = 0; k < 4; ++k) {
-      const int j = 4 * kc + k;
-      double v = 0.0;
-      if (j < n && r < nrhs) {
-        const double2 z = x[(size_t)r * ld + perm[j]];
-        v = a ? z.y : z.x;
+    for (int k = 0; k < 4; ++k) o[k] = tf32_part(a ? z[r][k].y : z[r][k].x, h);
+    xa[(size_t)kc * 128 + t] = make_float4(o[0], o[1], o[2], o[3]);
+#pragma unroll
+    for (int q = 0; q < 2; ++q) {
+      if (2 * kc + q >= nkc2) break;
+#pragma unroll
+      for (int k = 0; k < 2; ++k) {
+        const float2 v = z[r][2 * q + k];
+        o[2 * k] = tf32_part(a ? v.y : v.x, h);
+        o[2 * k + 1] = tf32_part(a ? v.x : -v.y, h);
       }
-      const float hi = tf32_rn((float)v);
-      o[k] = h ? tf32_rn((float)(v - (double)hi)) : hi;
+      xa2[(size_t)(2 * kc + q) * 128 + t] = make_float4(o[0], o[1], o[2], o[3]);
     }
-    xa[t] = make_float4(o[0], o[1], o[2], o[3]);
+    __syncthreads();
   }
 }
 
-void launch_tc_xprep(const int* perm, int n, int nrhs, int ld, const void* x, void* xa, int nkc, cudaStream_t s) {
-  const long long total = (long long)nkc * 128;
-  const int grid = (int)std::min<long long>((total + 255) / 256, 152 * 8);
-  tc_xprep_kernel<<<grid, 256, 0, s>>>(perm, n, nrhs, ld, (const double2*)x, (float4*)xa, nkc);
+void launch_tc_xprep(const int* perm, int n, int nrhs, int ld, const void* x, void* xa, int nkc, void* xa2, int nkc2,
+                     cudaStream_t s) {
+  const int grid = std::max(1, std::min(nkc, 152 * 16));
+  tc_xprep_kernel<<<grid, 128, 0, s>>>(perm, n, nrhs, ld, (const double2*)x, (float4*)xa, nkc, (float4*)xa2, nkc2);
 }
 
 // V2 panel of a column tile: column n = (block, rank k, part c) from the column map (x < 0:
@@ -454,6 +493,95 @@ __global__ void tc_pack_u_kernel(const TCUJob* jobs, const LRDesc* lr) {
     }
     dst[e] = make_float4(o[0], o[1], o[2], o[3]);
   }
+}
+
+// panel of (row tile, dense block): row n = block row i0 + n, K = (column j, part c) with the
+// columns of core kc at 2 kc, 2 kc + 1 (absolute, cluster order); the block is column-major
+__global__ void tc_pack_d_kernel(const TCDJob* jobs, const MVDense* dense) {
+  const TCDJob J = jobs[blockIdx.x];
+  const MVDense D = dense[J.blk];
+  const float2* A = (const float2*)D.ptr;
+  float4* dst = (float4*)J.dst;
+  const long long total = (long long)J.nkc * 2 * J.N;
+  for (long long e = threadIdx.x; e < total; e += blockDim.x) {
+    const int n = (int)(e % J.N);
+    const int hk = (int)(e / J.N);
+    const int hl = hk & 1, kc = hk >> 1;
+    float o[4] = {0.f, 0.f, 0.f, 0.f};
+    if (n < J.rows) {
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        const int j = 2 * (J.kc0 + kc) + (k >> 1) - D.c0;
+        if (j >= 0 && j < D.n) {
+          const float2 z = A[(size_t)(J.i0 + n) + (size_t)j * D.m];
+          o[k] = tf32_part((k & 1) ? z.y : z.x, hl);
+        }
+      }
+    }
+    dst[e] = make_float4(o[0], o[1], o[2], o[3]);
+  }
+}
+
+// y = alpha * (sum of the partial rows of every row cluster holding the row) + beta * y, written
+// through the output permutation; one CTA per leaf, thread per (row, right-hand side)
+#define TC_YS_MAXE 64
+// error-free sum of a float pair accumulator (s, c) and v (Knuth TwoSum, FP32)
+__device__ __forceinline__ void two_sum_acc(float& s, float& c, float v) {
+  const float t = s + v;
+  const float bp = t - s;
+  c += (s - (t - bp)) + (v - bp);
+  s = t;
+}
+// Partials are summed in FP32 with TwoSum compensation (the FP64 pipe is narrow on this part);
+// the FP64 result is hi + lo, formed once per component.
+__global__ void __launch_bounds__(256) tc_ysum_out_kernel(const int4* leaves, const int* deltas, const float2* ypart,
+                                                          const int* perm, int nrhs, int ld, double ar, double ai,
+                                                          double br, double bi, int use_alpha, int use_beta,
+                                                          double2* y) {
+  __shared__ int dl[TC_YS_MAXE];
+  const int4 L = leaves[blockIdx.x];
+  const int ne = L.w - L.z, ns = min(ne, TC_YS_MAXE);
+  for (int e = threadIdx.x; e < ns; e += blockDim.x) dl[e] = deltas[L.z + e];
+  __syncthreads();
+  const int total = (L.y - L.x) * 32;
+  for (int t = threadIdx.x; t < total; t += blockDim.x) {
+    const int i = L.x + (t >> 5), r = t & 31;
+    if (r >= nrhs) continue;
+    float sr = 0.f, cr = 0.f, si = 0.f, ci = 0.f;
+#pragma unroll 4
+    for (int e = 0; e < ns; ++e) {
+      const float2 v = ypart[(size_t)(i + dl[e]) * 32 + r];
+      two_sum_acc(sr, cr, v.x);
+      two_sum_acc(si, ci, v.y);
+    }
+    for (int e = ns; e < ne; ++e) {
+      const float2 v = ypart[(size_t)(i + deltas[L.z + e]) * 32 + r];
+      two_sum_acc(sr, cr, v.x);
+      two_sum_acc(si, ci, v.y);
+    }
+    double2 o = make_double2((double)sr + (double)cr, (double)si + (double)ci);
+    if (use_alpha) o = make_double2(ar * o.x - ai * o.y, ar * o.y + ai * o.x);
+    double2* yo = y + (size_t)r * ld + perm[i];
+    if (use_beta) {
+      const double2 w = *yo;
+      o.x += br * w.x - bi * w.y;
+      o.y += br * w.y + bi * w.x;
+    }
+    *yo = o;
+  }
+}
+
+void launch_tc_pack_d(const TCDJob* jobs, int njobs, const MVDense* dense, cudaStream_t s) {
+  if (njobs > 0) tc_pack_d_kernel<<<njobs, 256, 0, s>>>(jobs, dense);
+}
+
+void launch_tc_ysum_out(const int4* leaves, int nleaves, const int* deltas, const void* ypart, const int* perm,
+                        int nrhs, int ld, const double* alpha, const double* beta, void* y, cudaStream_t s) {
+  const int use_beta = (beta[0] != 0.0 || beta[1] != 0.0) ? 1 : 0;
+  const int use_alpha = (alpha[0] != 1.0 || alpha[1] != 0.0) ? 1 : 0;
+  if (nleaves > 0)
+    tc_ysum_out_kernel<<<nleaves, 256, 0, s>>>(leaves, deltas, (const float2*)ypart, perm, nrhs, ld, alpha[0], alpha[1],
+                                               beta[0], beta[1], use_alpha, use_beta, (double2*)y);
 }
 
 void launch_tc_pack_v(const TCVJob* jobs, int njobs, const int4* colmap, const LRDesc* lr, cudaStream_t s) {
