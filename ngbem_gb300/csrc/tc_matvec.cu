@@ -133,6 +133,27 @@ __device__ __forceinline__ void tmem_ld8(uint32_t taddr, float (&v)[8]) {
 #pragma unroll
   for (int k = 0; k < 8; ++k) v[k] = __uint_as_float(r[k]);
 }
+// 8 columns into v[8 J .. 8 J + 7] of a 32-value batch (tmem_wait32 completes the batch)
+template <int J>
+__device__ __forceinline__ void tmem_ld8_at(uint32_t taddr, float (&v)[32]) {
+  uint32_t r[8];
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
+               : "r"(taddr)
+               : "memory");
+#pragma unroll
+  for (int k = 0; k < 8; ++k) v[8 * J + k] = __uint_as_float(r[k]);
+}
+__device__ __forceinline__ void tmem_wait32(float (&v)[32]) {
+  asm volatile("tcgen05.wait::ld.sync.aligned;"
+               : "+f"(v[0]), "+f"(v[1]), "+f"(v[2]), "+f"(v[3]), "+f"(v[4]), "+f"(v[5]), "+f"(v[6]), "+f"(v[7]),
+                 "+f"(v[8]), "+f"(v[9]), "+f"(v[10]), "+f"(v[11]), "+f"(v[12]), "+f"(v[13]), "+f"(v[14]),
+                 "+f"(v[15]), "+f"(v[16]), "+f"(v[17]), "+f"(v[18]), "+f"(v[19]), "+f"(v[20]), "+f"(v[21]),
+                 "+f"(v[22]), "+f"(v[23]), "+f"(v[24]), "+f"(v[25]), "+f"(v[26]), "+f"(v[27]), "+f"(v[28]),
+                 "+f"(v[29]), "+f"(v[30]), "+f"(v[31])
+               :
+               : "memory");
+}
 __device__ __forceinline__ void tmem_wait(float (&v)[8]) {
   asm volatile("tcgen05.wait::ld.sync.aligned;"
                : "+f"(v[0]), "+f"(v[1]), "+f"(v[2]), "+f"(v[3]), "+f"(v[4]), "+f"(v[5]), "+f"(v[6]), "+f"(v[7])
@@ -293,8 +314,15 @@ __global__ void __launch_bounds__(TC_THREADS, 1) tc_gemm_kernel(TCGemmArgs g) {
     const int rhs = row >> 2, a = (row >> 1) & 1, h = row & 1;
     const unsigned FULL = 0xffffffffu;
     int acc_it = 0;
+    TCItem In{};
+    if (my.y > 0) In = g.items[my.x];
     for (int ii = my.x; ii < iend; ++ii) {
-      const TCItem I = g.items[ii];
+      const TCItem I = In;
+      if (ii + 1 < iend) In = g.items[ii + 1];  // next item's descriptor, loaded early
+      // pass 0: lane o holds the output descriptor of block o of the tile (at most 32 blocks:
+      // N <= 256 and a block takes at least 8 columns), loaded before the accumulator wait
+      TCOut oc{};
+      if (PASS == 0 && lane < I.nout) oc = g.outs[I.out0 + lane];
       const int acc = acc_it & 1;
       int ok = 1;
       if (lane == 0) ok = bar_wait(&S.accf[acc], (acc_it >> 1) & 1, abort_flag, g.err) ? 1 : 0;
@@ -306,49 +334,69 @@ __global__ void __launch_bounds__(TC_THREADS, 1) tc_gemm_kernel(TCGemmArgs g) {
         // columns (rank k, real/imaginary c) of each block: T = V2 x combined from the four
         // real products, written as the block's pass-1 A panel: row (r, a', h') holds, for
         // K = (k, c), the h' part of  a' = 0: (Re T_k, -Im T_k);  a' = 1: (Im T_k, Re T_k)
-        for (int o = I.out0; o < I.out0 + I.nout; ++o) {
-          const TCOut O = g.outs[o];
-          float4* ta = (float4*)O.ta;
-          for (int c = 0; c < 2 * O.rpad; c += 8) {
-            float v[8], sm[8], pm[8], out[8];
-            tmem_ld8(tb + (uint32_t)(O.col + c), v);
-            tmem_wait(v);
+        for (int o = 0; o < I.nout; ++o) {
+          float4* ta = (float4*)__shfl_sync(FULL, oc.ta, o);
+          const int col = __shfl_sync(FULL, oc.col, o), nc = 2 * __shfl_sync(FULL, oc.rpad, o);
+          for (int c = 0; c < nc; c += 32) {
+            const int ng = min(4, (nc - c) >> 3);  // 8-column groups in this batch (warp-uniform)
+            float v[32];
+            const uint32_t t0 = tb + (uint32_t)(col + c);
+            tmem_ld8_at<0>(t0, v);
+            if (ng > 1) tmem_ld8_at<1>(t0 + 8, v);
+            if (ng > 2) tmem_ld8_at<2>(t0 + 16, v);
+            if (ng > 3) tmem_ld8_at<3>(t0 + 24, v);
+            tmem_wait32(v);
 #pragma unroll
-            for (int k = 0; k < 8; ++k) sm[k] = v[k] + __shfl_xor_sync(FULL, v[k], 1);  // hi + lo rows
+            for (int j = 0; j < 4; ++j) {
+              if (j >= ng) break;
+              float sm[8], pm[8], out[8];
 #pragma unroll
-            for (int k = 0; k < 8; ++k) pm[k] = __shfl_xor_sync(FULL, sm[k], 2);        // other part a
+              for (int k = 0; k < 8; ++k) sm[k] = v[8 * j + k] + __shfl_xor_sync(FULL, v[8 * j + k], 1);  // hi + lo
 #pragma unroll
-            for (int k = 0; k < 4; ++k) {
-              const float rr = a ? pm[2 * k] : sm[2 * k];          // sum_j Re x Re V
-              const float ri = a ? pm[2 * k + 1] : sm[2 * k + 1];  // sum_j Re x Im V
-              const float ir = a ? sm[2 * k] : pm[2 * k];          // sum_j Im x Re V
-              const float ii2 = a ? sm[2 * k + 1] : pm[2 * k + 1]; // sum_j Im x Im V
-              const float tr = rr - ii2, ti = ri + ir;
-              out[2 * k] = tf32_part(a ? ti : tr, h);
-              out[2 * k + 1] = tf32_part(a ? tr : -ti, h);
+              for (int k = 0; k < 8; ++k) pm[k] = __shfl_xor_sync(FULL, sm[k], 2);  // the other part a
+#pragma unroll
+              for (int k = 0; k < 4; ++k) {
+                const float rr = a ? pm[2 * k] : sm[2 * k];          // sum_j Re x Re V
+                const float ri = a ? pm[2 * k + 1] : sm[2 * k + 1];  // sum_j Re x Im V
+                const float ir = a ? sm[2 * k] : pm[2 * k];          // sum_j Im x Re V
+                const float ii2 = a ? sm[2 * k + 1] : pm[2 * k + 1]; // sum_j Im x Im V
+                const float tr = rr - ii2, ti = ri + ir;
+                out[2 * k] = tf32_part(a ? ti : tr, h);
+                out[2 * k + 1] = tf32_part(a ? tr : -ti, h);
+              }
+              const int kc = (c + 8 * j) >> 2;
+              ta[(size_t)kc * 128 + row] = make_float4(out[0], out[1], out[2], out[3]);
+              ta[(size_t)(kc + 1) * 128 + row] = make_float4(out[4], out[5], out[6], out[7]);
             }
-            const int kc = c >> 2;
-            ta[(size_t)kc * 128 + row] = make_float4(out[0], out[1], out[2], out[3]);
-            ta[(size_t)(kc + 1) * 128 + row] = make_float4(out[4], out[5], out[6], out[7]);
           }
         }
       } else {
         // columns = rows i of the row tile; row (r, a, h) holds the h part of Re/Im (U2 T)_i
         float2* yp = (float2*)g.ypart;
         const int u = lane & 3;
-        for (int c = 0; c < I.nout; c += 8) {
-          float v[8], sm[8], pm[8];
-          tmem_ld8(tb + (uint32_t)c, v);
-          tmem_wait(v);
+        for (int c = 0; c < I.nout; c += 32) {
+          const int ng = min(4, (I.nout - c + 7) >> 3);
+          float v[32];
+          const uint32_t t0 = tb + (uint32_t)c;
+          tmem_ld8_at<0>(t0, v);
+          if (ng > 1) tmem_ld8_at<1>(t0 + 8, v);
+          if (ng > 2) tmem_ld8_at<2>(t0 + 16, v);
+          if (ng > 3) tmem_ld8_at<3>(t0 + 24, v);
+          tmem_wait32(v);
 #pragma unroll
-          for (int k = 0; k < 8; ++k) sm[k] = v[k] + __shfl_xor_sync(FULL, v[k], 1);
+          for (int j = 0; j < 4; ++j) {
+            if (j >= ng) break;
+            float sm[8], pm[8];
 #pragma unroll
-          for (int k = 0; k < 8; ++k) pm[k] = __shfl_xor_sync(FULL, sm[k], 2);
+            for (int k = 0; k < 8; ++k) sm[k] = v[8 * j + k] + __shfl_xor_sync(FULL, v[8 * j + k], 1);
 #pragma unroll
-          for (int k = 0; k < 8; ++k) {
-            const int i = c + k;
-            if ((k >> 1) == u && i < I.nout)
-              yp[(size_t)(I.out0 + i) * 32 + rhs] = make_float2(a ? pm[k] : sm[k], a ? sm[k] : pm[k]);
+            for (int k = 0; k < 8; ++k) pm[k] = __shfl_xor_sync(FULL, sm[k], 2);
+#pragma unroll
+            for (int k = 0; k < 8; ++k) {
+              const int i = c + 8 * j + k;
+              if ((k >> 1) == u && i < I.nout)
+                yp[(size_t)(I.out0 + i) * 32 + rhs] = make_float2(a ? pm[k] : sm[k], a ? sm[k] : pm[k]);
+            }
           }
         }
       }
