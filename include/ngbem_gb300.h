@@ -187,8 +187,9 @@ int bem_sl_batch_destroy(bem_slbatch_t batch);
 /* Arithmetic of the matvec for FP32-stored operators (no counterpart in the reference, which is
  * FP64 throughout): compensated = 1 (default) forms every product and sum error-free (x split
  * into FP32 hi+lo, TwoProd/TwoSum), so the only rounding is that of the stored entries;
- * compensated = 0 uses plain FP32 FMAs (about 1e-7 relative rounding, faster).  FP64-stored
- * operators ignore it.  bem_gmres uses the plain form inside its Krylov iterations and the
+ * compensated = 0 uses plain FP32 FMAs (about 1e-7 relative rounding, faster); complex
+ * operators applied to 2..32 right-hand sides then use the tensor cores (about 5e-6, see
+ * bem_operator_set_tensor_cores).  FP64-stored operators ignore it.  bem_gmres uses the plain form inside its Krylov iterations and the
  * compensated form for its residuals (iterative refinement). */
 int bem_operator_set_accuracy(bem_operator_t op, int compensated);
 
@@ -203,9 +204,10 @@ int bem_operator_autotune(bem_operator_t op, int reps, int* piece, int* fused, d
  * applies HMatrix::MultAdd, src/hmat.cpp:647-655, one vector at a time).  For complex
  * operators with FP32 storage, plain accuracy (bem_operator_set_accuracy(op, 0)) and 2..32
  * right-hand sides, bem_operator_mult runs the low-rank products T = V2 X and Y += U2 T on the
- * tcgen05 tensor cores with split-TF32 operands (high + low parts, FP32 accumulation; about
- * 1e-6 relative) and the dense blocks on CUDA cores.  The packed operand panels (about twice
- * the low-rank storage) are built on the first such call outside a stream capture, or here.
+ * tcgen05 tensor cores with split-TF32 operands (high + low parts, FP32 accumulation over a
+ * block row; about 5e-6 relative), the dense blocks included.  The packed operand panels
+ * (about 3x the low-rank storage) are built on the first such call outside a stream capture,
+ * or here.
  * enable = 1 (default) builds them now when the operator qualifies; 0 turns the path off and
  * frees them.  bem_operator_tensor_cores reports the state (1 built, 0 not built, -1 the
  * operator or device does not qualify), the device bytes of the panels, the work items of the
