@@ -24,11 +24,13 @@ extern "C" {
 #define BEM_ERR_INTERNAL 5 /* device-side check failed (capacity, rank cap, ...) */
 
 /* kernel ids: reference src/ngbem.hpp:226-434 (LaplaceSL/DL/HS, HelmholtzSL/DL/HS,
- * CombinedField, MaxwellSL) */
+ * CombinedField, MaxwellSL).  BEM_HELMHOLTZ_SL_DKAPPA (no counterpart in the reference) is the
+ * derivative of the Helmholtz single layer with respect to kappa, kernel i e^{i kappa r}/(4 pi):
+ * its operator is the kappa-derivative of the single-layer bilinear form. */
 enum {
   BEM_LAPLACE_SL = 0, BEM_LAPLACE_DL = 1, BEM_LAPLACE_HS = 2,
   BEM_HELMHOLTZ_SL = 3, BEM_HELMHOLTZ_DL = 4, BEM_HELMHOLTZ_HS = 5,
-  BEM_HELMHOLTZ_CF = 6, BEM_MAXWELL_SL = 7
+  BEM_HELMHOLTZ_CF = 6, BEM_MAXWELL_SL = 7, BEM_HELMHOLTZ_SL_DKAPPA = 8
 };
 /* trace spaces: SurfaceL2 order 0 (P0), H1 order 1 trace (P1), HDivSurface order 0 (RT0) */
 enum { BEM_P0 = 0, BEM_P1 = 1, BEM_RT0 = 2 };

@@ -30,6 +30,7 @@ __all__ = ["SurfaceL2", "H1", "HDivSurface", "TraceSpace", "BaseMatrix", "HMatri
            "SingleLayerPotentialOperator", "DoubleLayerPotentialOperator", "HypersingularOperator",
            "HelmholtzSingleLayerPotentialOperator", "HelmholtzDoubleLayerPotentialOperator",
            "HelmholtzCombinedFieldOperator", "HelmholtzHypersingularOperator",
+           "HelmholtzSingleLayerPotentialOperatorDKappa",
            "MaxwellSingleLayerPotentialOperator", "MaxwellSingleLayerPotentialOperatorCurl",
            "MaxwellDoubleLayerPotentialOperator", "MassOperator", "GMRes", "cluster_tree", "partition",
            "tc_selftest"]
@@ -516,6 +517,16 @@ def HelmholtzSingleLayerPotentialOperator(trial_space, test_space=None, kappa=No
     trial space (the reference dereferences the null test space there)."""
     return IntegralOperator("helmholtz_sl", _kappa(kappa), trial_space, test_space, "id", "id", intorder, leafsize,
                             eta, eps, "aca", testhmatrix, **gb)
+
+
+def HelmholtzSingleLayerPotentialOperatorDKappa(trial_space, test_space=None, kappa=None, intorder=3, leafsize=40,
+                                                eta=2., eps=1e-6, method="aca", testhmatrix=False, **gb):
+    """Derivative of the Helmholtz single layer with respect to kappa (no counterpart in the
+    reference): the operator of the bilinear form d/dkappa <V_kappa u, v>, kernel
+    i e^{i kappa |x-y|}/(4 pi).  Same arguments and assembly as
+    HelmholtzSingleLayerPotentialOperator."""
+    return IntegralOperator("helmholtz_sl_dkappa", _kappa(kappa), trial_space, test_space, "id", "id", intorder,
+                            leafsize, eta, eps, method, testhmatrix, **gb)
 
 
 def HelmholtzDoubleLayerPotentialOperator(trial_space, test_space=None, kappa=None, intorder=3, leafsize=40,

@@ -302,7 +302,7 @@ void launch_aca(int kid, int prec, const AcaArgs& a, cudaStream_t s) {
     return;                                                                    \
   }
   X(K_LAPLACE_SL) X(K_LAPLACE_DL) X(K_LAPLACE_HS) X(K_HELMHOLTZ_SL) X(K_HELMHOLTZ_DL)
-  X(K_HELMHOLTZ_HS) X(K_HELMHOLTZ_CF) X(K_MAXWELL_SL)
+  X(K_HELMHOLTZ_HS) X(K_HELMHOLTZ_CF) X(K_MAXWELL_SL) X(K_HELMHOLTZ_SL_DKAPPA)
 #undef X
 }
 
@@ -314,6 +314,8 @@ void launch_aca(int kid, int prec, const AcaArgs& a, cudaStream_t s) {
   X(K_LAPLACE_HS, TR_ROT, TR_ROT)                                                     \
   X(K_HELMHOLTZ_SL, TR_P0, TR_P0) X(K_HELMHOLTZ_SL, TR_P1, TR_P1)                     \
   X(K_HELMHOLTZ_SL, TR_P1, TR_P0) X(K_HELMHOLTZ_SL, TR_P0, TR_P1)                     \
+  X(K_HELMHOLTZ_SL_DKAPPA, TR_P0, TR_P0) X(K_HELMHOLTZ_SL_DKAPPA, TR_P1, TR_P1)       \
+  X(K_HELMHOLTZ_SL_DKAPPA, TR_P1, TR_P0) X(K_HELMHOLTZ_SL_DKAPPA, TR_P0, TR_P1)       \
   X(K_HELMHOLTZ_DL, TR_P0, TR_P0) X(K_HELMHOLTZ_DL, TR_P1, TR_P1)                     \
   X(K_HELMHOLTZ_DL, TR_P1, TR_P0) X(K_HELMHOLTZ_DL, TR_P0, TR_P1)                     \
   X(K_HELMHOLTZ_CF, TR_P0, TR_P0) X(K_HELMHOLTZ_CF, TR_P1, TR_P1)                     \

@@ -152,6 +152,24 @@ template <> struct Green<K_HELMHOLTZ_SL> {
   }
 };
 
+// d/dkappa of the Helmholtz single-layer kernel: d/dk e^{ikr}/(4 pi r) = i e^{ikr}/(4 pi), a
+// bounded kernel (the derivative of the bilinear form with respect to the wavenumber)
+template <> struct Green<K_HELMHOLTZ_SL_DKAPPA> {
+  static constexpr bool CPLX = true; static constexpr int NC = 1; static constexpr int NT = 1;
+  static constexpr bool NEEDS_NX = false, NEEDS_NY = false;
+  __host__ __device__ static constexpr int kc(int) { return 0; }
+  __host__ __device__ static constexpr int trc(int) { return 0; }
+  __host__ __device__ static constexpr int tec(int) { return 0; }
+  __host__ __device__ static constexpr int fk(int) { return 0; }
+  template <class R>
+  __device__ static __forceinline__ void eval(R dx, R dy, R dz, const R*, const R*, R kappa, cpx<R>* out) {
+    R r2 = dx * dx + dy * dy + dz * dz;
+    R s, c;
+    sincos_(kappa * sqrt_(r2), &s, &c);
+    out[0] = mkc(-s * R(BEM_INV4PI), c * R(BEM_INV4PI));
+  }
+};
+
 template <> struct Green<K_MAXWELL_SL> {
   static constexpr bool CPLX = true; static constexpr int NC = 1; static constexpr int NT = 4;
   static constexpr bool NEEDS_NX = false, NEEDS_NY = false;

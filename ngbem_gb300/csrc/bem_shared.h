@@ -7,7 +7,8 @@ namespace bem {
 enum KernelId {
   K_LAPLACE_SL = 0, K_LAPLACE_DL = 1, K_LAPLACE_HS = 2, K_HELMHOLTZ_SL = 3,
   K_HELMHOLTZ_DL = 4, K_HELMHOLTZ_HS = 5, K_HELMHOLTZ_CF = 6, K_MAXWELL_SL = 7,
-  K_NUM = 8
+  K_HELMHOLTZ_SL_DKAPPA = 8,  // d/dkappa of the Helmholtz single layer (no counterpart in the reference)
+  K_NUM = 9
 };
 
 // trace kinds = (space kind, evaluator) combinations the operators use

@@ -339,6 +339,8 @@ __global__ void __launch_bounds__(256) nf_singular_kernel(NFArgs a) {
   X(K_LAPLACE_HS, TR_ROT, TR_ROT)                                                     \
   X(K_HELMHOLTZ_SL, TR_P0, TR_P0) X(K_HELMHOLTZ_SL, TR_P1, TR_P1)                     \
   X(K_HELMHOLTZ_SL, TR_P1, TR_P0) X(K_HELMHOLTZ_SL, TR_P0, TR_P1)                     \
+  X(K_HELMHOLTZ_SL_DKAPPA, TR_P0, TR_P0) X(K_HELMHOLTZ_SL_DKAPPA, TR_P1, TR_P1)       \
+  X(K_HELMHOLTZ_SL_DKAPPA, TR_P1, TR_P0) X(K_HELMHOLTZ_SL_DKAPPA, TR_P0, TR_P1)       \
   X(K_HELMHOLTZ_DL, TR_P0, TR_P0) X(K_HELMHOLTZ_DL, TR_P1, TR_P1)                     \
   X(K_HELMHOLTZ_DL, TR_P1, TR_P0) X(K_HELMHOLTZ_DL, TR_P0, TR_P1)                     \
   X(K_HELMHOLTZ_CF, TR_P0, TR_P0) X(K_HELMHOLTZ_CF, TR_P1, TR_P1)                     \

@@ -18,7 +18,7 @@ from . import _lib
 from ._lib import check, lib
 from .meshes import Mesh
 
-__all__ = ["SingleLayerEnergyBatch", "SingleLayerEnergy"]
+__all__ = ["SingleLayerEnergyBatch", "SingleLayerEnergy", "HelmholtzEnergy"]
 
 
 def _torch():
@@ -138,3 +138,82 @@ def __getattr__(name):
     if name == "SingleLayerEnergy":
         return _function()
     raise AttributeError(name)
+
+
+class HelmholtzEnergy:
+    """E(kappa, u) = u^T V_kappa u for the Helmholtz single layer on a fixed trace space, as a
+    function of the wavenumber and of a real density, returned as (Re E, Im E).
+
+    ``energy(kappa, u)`` is differentiable (``torch.autograd``): the backward pass assembles the
+    kappa-derivative operator (kernel i e^{i kappa r}/(4 pi), the same quadrature and
+    H-matrix compression as V_kappa) and gives dE/dkappa = u^T (dV/dkappa) u and
+    dE/du = (V_kappa + V_kappa^T) u.  The reference has no derivatives; E is what
+    ``u^T (V.mat * u)`` gives for ``V = HelmholtzSingleLayerPotentialOperator(space, kappa=...)``.
+    Operators are reassembled when kappa changes.
+    """
+
+    def __init__(self, space, intorder=3, leafsize=40, eta=2.0, eps=1e-8, method="aca", precision="fp64"):
+        self.space = space
+        self.kw = dict(intorder=intorder, leafsize=leafsize, eta=eta, eps=eps, method=method, precision=precision)
+        self._ops = {}
+
+    def operator(self, kappa: float, derivative: bool = False):
+        from . import bem
+        key = (float(kappa), bool(derivative))
+        if key not in self._ops:
+            if len(self._ops) >= 4:
+                self._ops.clear()
+            f = bem.HelmholtzSingleLayerPotentialOperatorDKappa if derivative else \
+                bem.HelmholtzSingleLayerPotentialOperator
+            self._ops[key] = f(self.space, self.space, kappa=float(kappa), **self.kw)
+        return self._ops[key].mat
+
+    def __call__(self, kappa, u):
+        return _helmholtz_function().apply(kappa, u, self)
+
+
+def _make_helmholtz_function():
+    torch = _torch()
+
+    def apply_op(A, u, trans=False):
+        uc = u.to(torch.complex128)
+        y = torch.empty_like(uc)
+        (A.MultTrans if trans else A.Mult)(uc, y)
+        return y
+
+    class _HelmholtzEnergy(torch.autograd.Function):
+        @staticmethod
+        def forward(ctx, kappa, u, energy):
+            k = float(kappa)
+            V = energy.operator(k)
+            E = torch.dot(u.to(torch.complex128), apply_op(V, u))
+            ctx.save_for_backward(kappa, u)
+            ctx.energy = energy
+            return torch.stack([E.real, E.imag])
+
+        @staticmethod
+        def backward(ctx, gE):
+            kappa, u = ctx.saved_tensors
+            energy = ctx.energy
+            k = float(kappa)
+            gk = gu = None
+            if ctx.needs_input_grad[0]:
+                dE = torch.dot(u.to(torch.complex128), apply_op(energy.operator(k, derivative=True), u))
+                gk = (gE[0] * dE.real + gE[1] * dE.imag).to(kappa.dtype).reshape(kappa.shape)
+            if ctx.needs_input_grad[1]:
+                V = energy.operator(k)
+                w = apply_op(V, u) + apply_op(V, u, trans=True)
+                gu = (gE[0] * w.real + gE[1] * w.imag).to(u.dtype)
+            return gk, gu, None
+
+    return _HelmholtzEnergy
+
+
+class _LazyH:
+    fn = None
+
+
+def _helmholtz_function():
+    if _LazyH.fn is None:
+        _LazyH.fn = _make_helmholtz_function()
+    return _LazyH.fn

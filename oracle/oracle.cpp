@@ -380,6 +380,9 @@ void Kernel::eval<cplx>(const double* x, const double* y, const double* nx, cons
                (nxy * (cplx(1.0, 0.0) - cplx(0.0, kappa) * norm) - cplx(0.0, kappa) * norm * norm);
       break;
     }
+    case ORC_HELMHOLTZ_SL_DKAPPA:
+      out[0] = cplx(0.0, 1.0) * ex / (4 * PI);
+      break;
     default:  // HELMHOLTZ_SL, MAXWELL_SL
       out[0] = ex / (4 * PI * norm);
   }

@@ -31,7 +31,10 @@ extern "C" {
 enum {
   ORC_LAPLACE_SL = 0, ORC_LAPLACE_DL = 1, ORC_LAPLACE_HS = 2,
   ORC_HELMHOLTZ_SL = 3, ORC_HELMHOLTZ_DL = 4, ORC_HELMHOLTZ_HS = 5,
-  ORC_HELMHOLTZ_CF = 6, ORC_MAXWELL_SL = 7
+  ORC_HELMHOLTZ_CF = 6, ORC_MAXWELL_SL = 7,
+  // d/dkappa of the Helmholtz single layer, i e^{i kappa r}/(4 pi): no counterpart in the
+  // reference (which has no derivatives); pinned by central differences of ORC_HELMHOLTZ_SL
+  ORC_HELMHOLTZ_SL_DKAPPA = 8
 };
 // space kinds
 enum { ORC_P0 = 0, ORC_P1 = 1, ORC_RT0 = 2 };

@@ -15,7 +15,8 @@ _HERE = os.path.dirname(os.path.abspath(__file__))
 _LIB = None
 
 KERNELS = {"laplace_sl": 0, "laplace_dl": 1, "laplace_hs": 2, "helmholtz_sl": 3,
-           "helmholtz_dl": 4, "helmholtz_hs": 5, "helmholtz_cf": 6, "maxwell_sl": 7}
+           "helmholtz_dl": 4, "helmholtz_hs": 5, "helmholtz_cf": 6, "maxwell_sl": 7,
+           "helmholtz_sl_dkappa": 8}
 KINDS = {"P0": 0, "P1": 1, "RT0": 2}
 EVALS = {"id": 0, "rot": 1, "helm": 2, "maxwell": 3}
 

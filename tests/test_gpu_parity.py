@@ -26,6 +26,7 @@ CASES = [
     ("helmholtz_cf", "P1", "P1", "id", "id", 5.0),
     ("helmholtz_hs", "P1", "P1", "helm", "helm", 3.0),
     ("maxwell_sl", "RT0", "RT0", "maxwell", "maxwell", 2.0),
+    ("helmholtz_sl_dkappa", "P1", "P0", "id", "id", 3.0),
 ]
 
 

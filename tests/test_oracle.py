@@ -115,3 +115,19 @@ def test_rt0_mass_and_maxwell_symmetry(oracle):
     W = oracle.dense_matrix("maxwell_sl", m, "RT0", kappa=2.0, trial_eval="maxwell", intorder=6)
     # the Maxwell single-layer Galerkin matrix is complex symmetric up to quadrature error
     assert np.linalg.norm(W - W.T) / np.linalg.norm(W) < 1e-3
+
+
+@pytest.mark.parametrize("kind", ["P0", "P1"])
+def test_dkappa_kernel_is_the_kappa_derivative(oracle, kind):
+    """The kappa-derivative kernel i e^{i kappa r}/(4 pi) (no counterpart in the reference) gives
+    d/dkappa of the Helmholtz single-layer Galerkin matrix: against central differences of the
+    reference-pinned single layer with the same quadrature (h = 1e-4, O(h^2) = 1e-8)."""
+    m = icosphere(1)
+    kappa, h = 3.0, 1e-4
+    D = oracle.dense_matrix("helmholtz_sl_dkappa", m, kind, kappa=kappa, intorder=4)
+    Vp = oracle.dense_matrix("helmholtz_sl", m, kind, kappa=kappa + h, intorder=4)
+    Vm = oracle.dense_matrix("helmholtz_sl", m, kind, kappa=kappa - h, intorder=4)
+    fd = (Vp - Vm) / (2 * h)
+    assert np.linalg.norm(D - fd) / np.linalg.norm(fd) < 1e-7
+    # symmetric up to the quadrature (the Sauter-Schwab rules are not symmetric in the pair)
+    assert np.linalg.norm(D - D.T) / np.linalg.norm(D) < 1e-4

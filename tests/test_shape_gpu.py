@@ -6,12 +6,15 @@
   single coordinates and a random direction, relative to the gradient's scale, 1e-5.
 * The torch.autograd.Function: X.grad, u.grad = 2 V u and per-problem weights.
 * Mixed precision (FP32 regular pairs) against FP64: energy 1e-6, gradient 1e-5.
+* The wavenumber derivative of the Helmholtz single-layer energy (HelmholtzEnergy) against
+  central differences in kappa and in u, 1e-6.
 """
 import numpy as np
 import pytest
 import torch
 
-from ngbem_gb300.meshes import perturbed_icosphere
+import ngbem_gb300 as nb
+from ngbem_gb300.meshes import icosphere, perturbed_icosphere
 from ngbem_gb300.shape import SingleLayerEnergyBatch, SingleLayerEnergy
 
 pytestmark = pytest.mark.gpu
@@ -112,3 +115,31 @@ def test_batch_argument_errors():
         b.evaluate(X[:-1], u)
     with pytest.raises(TypeError):
         b.evaluate(X.float(), u)
+
+
+def test_helmholtz_energy_kappa_derivative():
+    """dE/dkappa and dE/du of E(kappa, u) = u^T V_kappa u (Helmholtz single layer, P0, L2) from
+    the kappa-derivative operator, against central differences (h = 1e-5) of the plain FP64
+    operator; the derivative operator against FD of the matrix itself is in the parity tests."""
+    from ngbem_gb300.shape import HelmholtzEnergy
+    m = icosphere(2)
+    P0 = nb.SurfaceL2(m)
+    en = HelmholtzEnergy(P0, intorder=4, method="dense")
+    g = torch.Generator().manual_seed(5)
+    u = torch.randn(P0.ndof, generator=g, dtype=torch.float64).cuda().requires_grad_(True)
+    kappa = torch.tensor(2.5, dtype=torch.float64, device="cuda", requires_grad=True)
+    E = en(kappa, u)
+    w = torch.tensor([0.7, -0.3], dtype=torch.float64, device="cuda")
+    (E * w).sum().backward()
+    h = 1e-5
+    with torch.no_grad():
+        Ep = en(torch.tensor(2.5 + h, dtype=torch.float64, device="cuda"), u)
+        Em = en(torch.tensor(2.5 - h, dtype=torch.float64, device="cuda"), u)
+    fd = float(((Ep - Em) / (2 * h) * w).sum())
+    assert abs(float(kappa.grad) - fd) <= 1e-6 * abs(fd)
+    d = torch.randn(P0.ndof, generator=g, dtype=torch.float64).cuda()
+    with torch.no_grad():
+        Up = en(kappa.detach(), u + h * d)
+        Um = en(kappa.detach(), u - h * d)
+    fdu = float(((Up - Um) / (2 * h) * w).sum())
+    assert abs(float(torch.dot(u.grad, d)) - fdu) <= 1e-6 * abs(fdu)
