@@ -188,6 +188,7 @@ struct HOperator : OperatorBase {
   int mv_compensated = 1;  // fp32 storage: error-free products/sums (1) or plain FP32 (0)
   int t_len = 0;
   DevBuf d_t, d_tx, d_xp, d_yp;
+
   int ws_nrhs = 0;
   std::vector<MVDense> mvdense;
   std::vector<MVLowRank> mvlr;

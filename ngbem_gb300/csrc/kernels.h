@@ -110,6 +110,8 @@ struct MVArgs2 {
   int* err;
   int* sched;        // two zeroed counters (items claimed, CTAs finished); left zero after a pass
   int chunked;       // several right-hand sides: items are single-piece chunks (chunk kernel)
+  int t_f32;         // plain FP32 arithmetic, single launch: t accumulates in FP32 straight into the
+                     // high parts of its input form tx (low parts stay zero), no conversion phase
 };
 // passes per operator: 0-3 the four-pass pipeline, 4-7 the phases of the single-launch matvec
 #define MV_NPASS 8

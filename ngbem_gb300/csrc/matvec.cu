@@ -176,6 +176,13 @@ struct AccCF {
   __device__ __forceinline__ void merge(const AccCF& o) { re += o.re; im += o.im; }
   __device__ __forceinline__ cpx<double> val() const { return {(double)re, (double)im}; }
 };
+// t in FP32: add a plain accumulator to the high part(s) of entry i of the input form (float2
+// hi/lo per real value, float4 re hi/lo, im hi/lo per complex value)
+__device__ __forceinline__ void add_hi(float* tx, long long i, const AccF& s) { atomicAdd(tx + 2 * i, s.a); }
+__device__ __forceinline__ void add_hi(float* tx, long long i, const AccCF& s) {
+  atomicAdd(tx + 4 * i, s.re);
+  atomicAdd(tx + 4 * i + 2, s.im);
+}
 template <class VS, bool COMP> struct AccSel { using type = Acc<VS>; };
 template <> struct AccSel<float, false> { using type = AccF; };
 template <> struct AccSel<cpx<float>, false> { using type = AccCF; };
@@ -341,7 +348,7 @@ __device__ __forceinline__ void warp_gemv_s(const VS* A, int so, int sk, int O, 
       AccT other = acc.from_lane(ol + j * Ow);
       if (g == 0) acc.merge(other);
     }
-    if (g == 0 && o < O) out(o, acc.val());
+    if (g == 0 && o < O) out(o, acc);
   }
 }
 
@@ -349,9 +356,17 @@ template <class VS, bool COMP>
 __device__ __forceinline__ void run_piece_s(const MVArgs2& a, const MVPiece& pc, const VS* A, const typename MT<VS>::X* xin,
                                             int lane) {
   using D = typename MT<VS>::D;
+  if constexpr (!COMP && (std::is_same<VS, float>::value || std::is_same<VS, cpx<float>>::value)) {
+    if ((pc.flags & 2) && a.t_f32) {
+      float* tx = (float*)a.tx;
+      warp_gemv_s<VS, COMP>(A, pc.so, pc.sk, pc.O, pc.Kc, pc.ow, pc.groups, pc.inv_ow, [&](int k) { return xin[k]; },
+                            [&](int o, const auto& s) { add_hi(tx, (long long)pc.out_off + o, s); }, lane);
+      return;
+    }
+  }
   D* out = ((pc.flags & 2) ? (D*)a.t : (D*)a.yp) + pc.out_off;
   warp_gemv_s<VS, COMP>(A, pc.so, pc.sk, pc.O, pc.Kc, pc.ow, pc.groups, pc.inv_ow, [&](int k) { return xin[k]; },
-                        [&](int o, D v) { atomic_add(&out[o], v); }, lane);
+                        [&](int o, const auto& s) { atomic_add(&out[o], s.val()); }, lane);
 }
 
 // Persistent single right-hand-side pass, warp specialised.  Warp 0 (the producer) streams
@@ -772,15 +787,25 @@ __global__ void __launch_bounds__(MV_THREADS, 1) mv_fused_kernel(MVFusedArgs f) 
     const unsigned long long c0 = ld_acquire_u64(f.bar);
     gb.base = c0 - c0 % gridDim.x;
   }
-  // prologue: permuted input, zeroed accumulators
+  // prologue: permuted input.  The accumulators yp, t and tx are zero on entry: every matvec
+  // of the operator leaves them zero (this kernel's epilogue, a memset after the multi-pass
+  // schedule); only after an error (a launch that may have stopped early) are they zeroed here.
+  constexpr bool FP32S = !std::is_same<VS, double>::value && !std::is_same<VS, cpx<double>>::value;
+  const bool t32 = a.t_f32 != 0;
   {
     const D* x = (const D*)f.x;
     X* xp = (X*)a.xp;
     for (long long k = ct; k < f.n_in; k += cs) xp[k] = to_x<VS>(x[f.perm_in[k]]);
-    D* yp = (D*)a.yp;
-    for (long long k = ct; k < f.n_out; k += cs) yp[k] = D{};
-    D* t = (D*)a.t;
-    for (long long k = ct; k < f.t_len; k += cs) t[k] = D{};
+    if (*(volatile int*)a.err != 0) {
+      D* yp = (D*)a.yp;
+      for (long long k = ct; k < f.n_out; k += cs) yp[k] = D{};
+      D* t = (D*)a.t;
+      for (long long k = ct; k < f.t_len; k += cs) t[k] = D{};
+      if (FP32S) {
+        X* tx = (X*)a.tx;
+        for (long long k = ct; k < f.t_len; k += cs) tx[k] = X{};
+      }
+    }
   }
   mv_grid_sync_cons(gb, a.err, &bflag);
   if (tid == 32) *m.gate = 1;
@@ -788,12 +813,14 @@ __global__ void __launch_bounds__(MV_THREADS, 1) mv_fused_kernel(MVFusedArgs f) 
   set_phase(0);
   if (a.nitems > 0) mv_consume<VS, COMP>(a, m, c, warp - 1, lane);
   mv_grid_sync_cons(gb, a.err, &bflag);
-  // t is complete: its input form for phase B
-  if constexpr (!std::is_same<VS, double>::value && !std::is_same<VS, cpx<double>>::value) {
-    const D* t = (const D*)a.t;
-    X* tx = (X*)a.tx;
-    for (long long k = ct; k < f.t_len; k += cs) tx[k] = to_x<VS>(t[k]);
-    mv_grid_sync_cons(gb, a.err, &bflag);
+  // t is complete: its input form for phase B (already in place when t accumulates in FP32)
+  if constexpr (FP32S) {
+    if (!t32) {
+      const D* t = (const D*)a.t;
+      X* tx = (X*)a.tx;
+      for (long long k = ct; k < f.t_len; k += cs) tx[k] = to_x<VS>(t[k]);
+      mv_grid_sync_cons(gb, a.err, &bflag);
+    }
   }
   if (tid == 32) *m.gate = 2;
   set_phase(1);
@@ -804,9 +831,11 @@ __global__ void __launch_bounds__(MV_THREADS, 1) mv_fused_kernel(MVFusedArgs f) 
     *f.ctr[0] = 0;
     *f.ctr[1] = 0;
   }
-  // epilogue: y = alpha yp + beta y in the caller's numbering
+  // epilogue: y = alpha yp + beta y in the caller's numbering; yp and t (tx) are zeroed for
+  // the next launch (every entry by the thread that read it; t is no longer read after the
+  // last barrier)
   {
-    const D* yp = (const D*)a.yp;
+    D* yp = (D*)a.yp;
     D* y = (D*)f.y;
     const D al = mk_d<D>(f.alpha[0], f.alpha[1]), be = mk_d<D>(f.beta[0], f.beta[1]);
     for (long long k = ct; k < f.n_out; k += cs) {
@@ -814,6 +843,15 @@ __global__ void __launch_bounds__(MV_THREADS, 1) mv_fused_kernel(MVFusedArgs f) 
       D v = al * yp[k];
       if (f.use_beta) v += be * (*dst);
       *dst = v;
+      yp[k] = D{};
+    }
+    if (!t32) {
+      D* t = (D*)a.t;
+      for (long long k = ct; k < f.t_len; k += cs) t[k] = D{};
+    }
+    if (FP32S) {
+      X* tx = (X*)a.tx;
+      for (long long k = ct; k < f.t_len; k += cs) tx[k] = X{};
     }
   }
 }
@@ -1062,11 +1100,16 @@ static cudaError_t fused_t(const MVFusedArgs& f, cudaStream_t s) {
     if (e != cudaSuccess) return e;
     attr = true;
   }
-  int dev = 0, nsm = 0, nb = 0;
+  // SM count and residency, queried once per device (host time on every matvec otherwise)
+  static int cached_dev = -1, nsm = 0, nb = 0;
+  int dev = 0;
   cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-  cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, mv_fused_kernel<VS, COMP>, MV_THREADS, smem);
-  if (e != cudaSuccess) return e;
+  if (dev != cached_dev) {
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, mv_fused_kernel<VS, COMP>, MV_THREADS, smem);
+    if (e != cudaSuccess) return e;
+    cached_dev = dev;
+  }
   if (nb < 1) return cudaErrorCooperativeLaunchTooLarge;
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(nsm);  // one CTA per SM, all resident: the grid barriers rely on it

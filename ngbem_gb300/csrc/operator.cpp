@@ -938,6 +938,10 @@ void HOperator::mult(int trans, const double* alpha, const void* x, const double
     d_t.alloc((size_t)std::max(t_len, 1) * nrhs * dsz + 32);
     d_tx.alloc((size_t)std::max(t_len, 1) * nrhs * xsz + 32);
     ws_nrhs = nrhs;
+    // the accumulators are zero between matvecs (see the single-launch kernel)
+    BEM_CUDA(cudaMemsetAsync(d_yp.p, 0, d_yp.bytes, s));
+    BEM_CUDA(cudaMemsetAsync(d_t.p, 0, d_t.bytes, s));
+    BEM_CUDA(cudaMemsetAsync(d_tx.p, 0, d_tx.bytes, s));
   }
   const int* pin = trans ? (ttest == ttrial ? d_perm_trial.as<int>() : d_perm_test.as<int>()) : d_perm_trial.as<int>();
   const int* pout = trans ? d_perm_trial.as<int>() : (ttest == ttrial ? d_perm_trial.as<int>() : d_perm_test.as<int>());
@@ -961,6 +965,8 @@ void HOperator::mult(int trans, const double* alpha, const void* x, const double
     f.a.compensated = mv_compensated;
     f.a.in_esz = cplx ? 16 : 8;
     f.a.err = d_err.as<int>();
+    // plain FP32 arithmetic: t accumulates in FP32 in the high parts of its input form
+    f.a.t_f32 = (prec == 1 && !mv_compensated) ? 1 : 0;
     const int p0 = trans ? 6 : 4;
     for (int ph = 0; ph < 2; ++ph) {
       f.items[ph] = d_items[p0 + ph].as<MVTItem>();
@@ -1057,6 +1063,12 @@ void HOperator::mult(int trans, const double* alpha, const void* x, const double
   }
   if (profiling) BEM_CUDA(cudaEventRecord(ev[3], s));
   launch_permute_out(cplx, pout, out_n, nrhs, out_n, alpha, beta, d_yp.p, y, s);
+  // leave the accumulators zero for the single-launch kernel
+  BEM_CUDA(cudaMemsetAsync(d_yp.p, 0, (size_t)out_n * nrhs * dsz, s));
+  if (t_len > 0) {
+    BEM_CUDA(cudaMemsetAsync(d_t.p, 0, (size_t)t_len * nrhs * dsz, s));
+    if (prec == 1) BEM_CUDA(cudaMemsetAsync(d_tx.p, 0, (size_t)t_len * nrhs * xsz, s));
+  }
   if (profiling) {
     BEM_CUDA(cudaEventRecord(ev[4], s));
     pending.push_back(ev);
