@@ -131,7 +131,10 @@ int bem_operator_blocks(bem_operator_t op, int* rowcl, int* colcl, int* near, in
 /* y = alpha * op(A) x + beta * y on the device (reference HMatrix::Mult / MultAdd /
  * MultTrans / MultTransAdd, src/hmat.cpp:632-666).  trans=1 is the plain transpose (no
  * conjugation).  alpha/beta point to (re, im) pairs.  nrhs column-major right-hand sides
- * (leading dimension = vector length).  Stream-ordered, asynchronous. */
+ * (leading dimension = vector length).  Stream-ordered, asynchronous.  Assembly builds the
+ * work lists of the single right-hand-side product; the first call of another form (the
+ * transpose, several right-hand sides) builds its lists then, so make it outside a stream
+ * capture (BEM_ERR_STATE inside one). */
 int bem_operator_mult(bem_operator_t op, int trans, const double* alpha, const void* x,
                       const double* beta, void* y, int nrhs, void* stream);
 
@@ -146,9 +149,10 @@ int bem_operator_mult(bem_operator_t op, int trans, const double* alpha, const v
  * additions).  H-matrix operators only (BEM_ERR_STATE for a mass operator).  A call whose
  * scratch would exceed the area -- about 2 * (height + width + sum of block ranks) * nrhs
  * values -- returns BEM_ERR_ARG before launching anything.  The first call on a device looks
- * the array up (and may load device code): make it before any stream capture.  The area is
- * shared by every call on a device, so overlapping calls (several streams or host threads)
- * race: serialise them. */
+ * the array up (and may load device code), and the first call of an operator in a direction
+ * (trans = 0 or 1) builds that direction's work lists, which the operator keeps: make those
+ * calls before any stream capture.  The area is shared by every call on a device, so
+ * overlapping calls (several streams or host threads) race: serialise them. */
 int bem_operator_mult_noalloc(bem_operator_t op, int trans, const double* alpha, const void* x,
                               const double* beta, void* y, int nrhs, void* stream);
 

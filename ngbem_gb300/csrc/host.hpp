@@ -218,7 +218,13 @@ struct HOperator : OperatorBase {
   ~HOperator() override;
 
   void assemble();
-  void build_mv_items();
+  // Matvec work lists.  Bit p of `mask` builds pass list p (see d_items); `multi` the lists of
+  // several right-hand sides.  keep = false drops every other list (piece size changed).  The
+  // lists a matvec needs are built on its first call (ensure_mv) outside a stream capture.
+  void build_mv_items(unsigned mask, bool multi, bool keep);
+  void ensure_mv(unsigned mask, bool multi, cudaStream_t s);
+  unsigned mv_built = 0;
+  bool mv_multi_built = false;
   int device_status();   // matvec pipeline error flags (0 = ok)
   void mult(int trans, const double* alpha, const void* x, const double* beta, void* y, int nrhs,
             cudaStream_t s) override;

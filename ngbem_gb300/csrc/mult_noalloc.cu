@@ -58,6 +58,7 @@ size_t round256(size_t b) { return (b + 255) & ~(size_t)255; }
 void mult_noalloc(HOperator& op, int trans, const double* alpha, const void* x, const double* beta, void* y,
                   int nrhs, cudaStream_t s) {
   if (nrhs < 1) throw Error(BEM_ERR_ARG, "nrhs must be >= 1");
+  op.ensure_mv(trans ? 0x0Cu : 0x03u, false, s);  // the four-pass lists (built on first use)
   const int in_n = trans ? op.height : op.width;
   const int out_n = trans ? op.width : op.height;
   const size_t dsz = op.cplx ? 16 : 8;                          // FP64 accumulators

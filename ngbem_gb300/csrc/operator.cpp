@@ -492,7 +492,8 @@ void HOperator::assemble() {
   }
   const auto t_items = clk::now();
   mv_fused = mv_fused_supported();
-  build_mv_items();
+  // the lists of the single right-hand-side matvec; the others on first use
+  build_mv_items(mv_fused ? 0x30u : 0x03u, false, false);
   info.ms_mvitems = ms_since(t_items);
   BEM_CUDA(cudaDeviceSynchronize());
   keep.clear();
@@ -534,7 +535,25 @@ bool pairs_overflow(size_t ntiles) { return ntiles > (size_t)INT_MAX; }
 // ---------------------------------------------------------------------------------------------
 // Groups the payload (dense blocks, U2 chunks, V2 chunks) into work items of at most one
 // matvec stage: consecutive segments whose bytes are contiguous share one bulk copy.
-void HOperator::build_mv_items() {
+void HOperator::ensure_mv(unsigned mask, bool multi, cudaStream_t s) {
+  const unsigned miss = mask & ~mv_built;
+  const bool mmiss = multi && !mv_multi_built;
+  if (!miss && !mmiss) return;
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  BEM_CUDA(cudaStreamIsCapturing(s, &cs));
+  if (cs != cudaStreamCaptureStatusNone)
+    throw Error(BEM_ERR_STATE, "this matvec form has not run before: apply it once outside the stream capture");
+  build_mv_items(miss, mmiss, true);
+}
+
+void HOperator::build_mv_items(unsigned mask, bool multi, bool keep) {
+  if (!keep) {
+    mv_built = 0;
+    mv_multi_built = false;
+    for (int p = 0; p < MV_NPASS; ++p) n_items[p] = 0;
+    n_mr_items[0] = n_mr_items[1] = 0;
+    n_ro_leaves = 0;
+  }
   const size_t stage = (size_t)mv_stage_bytes();
   const int piece = mv_piece > 0 ? mv_piece : mv_piece_elems();  // target elements per piece (one warp's task)
   // A span is one contiguous payload range (a block, or a chunk of one) with its generic
@@ -686,6 +705,7 @@ void HOperator::build_mv_items() {
   std::vector<Task> tasks;
   for (int pass = 0; pass < MV_NPASS; ++pass)
     for (const LS& ls : lists[pass]) {
+      if (!(mask & (1u << pass))) continue;
       const size_t n = ls.L->size(), chunk = std::max<size_t>(128, (n + 7) / 8);
       for (size_t i0 = 0; i0 < n; i0 += chunk) tasks.push_back(Task{pass, &ls, i0, std::min(n, i0 + chunk), {}, {}, {}});
     }
@@ -836,22 +856,25 @@ void HOperator::build_mv_items() {
     }
   }
   for (int pass = 0; pass < MV_NPASS; ++pass) {
+    if (!(mask & (1u << pass))) continue;
     d_items[pass].upload(pass_items[pass]);
     d_pieces[pass].upload(pass_pcs[pass]);
     d_ranges[pass].upload(pass_rngs[pass]);
     n_items[pass] = (int)pass_items[pass].size();
-    if (pass < 4) {
-      info.mv_ranges[pass] = (int)pass_rngs[pass].size();
-      info.mv_items[pass] = n_items[pass];
-      npieces += (long long)pass_pcs[pass].size();
-    }
+    const int ip = pass < 4 ? pass : (pass == 4 ? 0 : (pass == 5 ? 1 : (pass == 6 ? 2 : 3)));
+    info.mv_ranges[ip] = (int)pass_rngs[pass].size();
+    info.mv_items[ip] = n_items[pass];
+    npieces += (long long)pass_pcs[pass].size();
   }
-  info.mv_segments = (int)npieces;
+  if (npieces > 0 && (mask & 0x30u)) info.mv_segments = (int)npieces;
+  else if (npieces > 0 && !keep) info.mv_segments = (int)npieces;
+  mv_built |= mask;
   // lists for several right-hand sides (the pass kernel reads the blocks in place there): one
   // piece per span (a dense column chunk, a V2 column chunk, a U2 row chunk, each at most one
   // stage of bytes), so a piece reduces over the whole chunk and each output row receives one
   // atomic per chunk instead of one per column slice; chunks keep the items balanced
-  {
+  if (multi) {
+    mv_multi_built = true;
     std::vector<MVTItem> mi[2];
     std::vector<MVPiece> mp[2];
     auto add = [&](int ph, unsigned long long src, MVPiece pc) {
@@ -910,6 +933,7 @@ void HOperator::build_mv_items() {
       n_mr_items[ph] = (int)mi[ph].size();
     }
   }
+  if (d_err.p) return;  // the shared device tables exist already
   d_mvdense.upload(mvdense);
   d_mvlr.upload(mvlr);
   d_err.alloc(sizeof(int));
@@ -954,6 +978,9 @@ void HOperator::mult(int trans, const double* alpha, const void* x, const double
     mult_tc(alpha, x, beta, y, nrhs, s);
     return;
   }
+  if (mv_fused && nrhs == 1) ensure_mv(trans ? 0xC0u : 0x30u, false, s);
+  else if (nrhs > 1 && !trans) ensure_mv(prec == 0 ? 0u : 0u, true, s);
+  else ensure_mv(trans ? 0x0Cu : 0x03u, false, s);
   if (mv_fused && nrhs == 1) {
     // one cooperative launch: permute, phase A, t -> input form, phase B, un-permute
     MVFusedArgs f{};
@@ -1702,7 +1729,7 @@ double HOperator::autotune(int reps, int* best_piece, int* best_fused) {
   int bp = mv_piece > 0 ? mv_piece : mv_piece_elems(), bf = mv_fused ? 1 : 0;
   for (int pc : cand) {
     mv_piece = pc;
-    build_mv_items();
+    build_mv_items(fused_ok ? 0x33u : 0x03u, false, false);
     for (int f = fused_ok ? 1 : 0; f >= 0; --f) {
       mv_fused = f != 0;
       for (int w = 0; w < 2; ++w) mult(0, one, x.p, zero, y.p, 1, s);
@@ -1722,7 +1749,7 @@ double HOperator::autotune(int reps, int* best_piece, int* best_fused) {
   }
   mv_piece = bp;
   mv_fused = bf != 0;
-  build_mv_items();
+  build_mv_items(mv_fused ? 0x30u : 0x03u, false, false);
   BEM_CUDA(cudaStreamSynchronize(s));
   profiling = was_profiling;
   if (best_piece) *best_piece = bp;
