@@ -156,7 +156,9 @@ int bem_operator_mult(bem_operator_t op, int trans, const double* alpha, const v
 int bem_operator_mult_noalloc(bem_operator_t op, int trans, const double* alpha, const void* x,
                               const double* beta, void* y, int nrhs, void* stream);
 
-/* Same with HOST buffers: copies x up, applies, copies y back (synchronous). */
+/* Same with HOST buffers (synchronous).  Page-locked buffers (cudaHostAlloc, torch
+ * pin_memory) are read and written by the kernels in place through their device mapping;
+ * other host memory is copied up, applied and copied back. */
 int bem_operator_mult_host(bem_operator_t op, int trans, const double* alpha, const void* x,
                            const double* beta, void* y, int nrhs);
 

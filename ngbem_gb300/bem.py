@@ -322,7 +322,8 @@ class _NativeMatrix(BaseMatrix):
             y.copy_(yt.t())
 
     def mult_host(self, x: np.ndarray, trans=False, alpha=1.0, beta=0.0, y: np.ndarray | None = None):
-        """Apply with host buffers through bem_operator_mult_host (copies inside the call)."""
+        """Apply with host buffers through bem_operator_mult_host: page-locked buffers are read and
+        written by the kernels in place, others are staged through device copies."""
         dt = np.complex128 if self.is_complex else np.float64
         x = np.ascontiguousarray(x, dtype=dt)
         nrhs = 1 if x.ndim == 1 else x.shape[1]

@@ -244,6 +244,24 @@ int bem_operator_mult_host(bem_operator_t op, int trans, const double* alpha, co
     const size_t esz = o->cplx ? 16 : 8;
     const size_t nin = (size_t)(trans ? o->height : o->width) * nrhs;
     const size_t nout = (size_t)(trans ? o->width : o->height) * nrhs;
+    // Page-locked host buffers are mapped into the device's address space: the kernels read x
+    // and write y across the host link themselves, with no staging copies (each step still
+    // moves x to the device and y back).  Other host memory goes through device staging.
+    auto mapped = [](const void* p) -> void* {
+      cudaPointerAttributes at{};
+      if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+      }
+      return at.type == cudaMemoryTypeHost ? at.devicePointer : nullptr;
+    };
+    void* xm = mapped(x);
+    void* ym = xm ? mapped(y) : nullptr;
+    if (xm && ym) {
+      o->mult(trans, alpha, xm, beta, ym, nrhs, 0);
+      BEM_CUDA(cudaStreamSynchronize(0));
+      return;
+    }
     if (o->stage_x.bytes < nin * esz) o->stage_x.alloc(nin * esz);
     if (o->stage_y.bytes < nout * esz) o->stage_y.alloc(nout * esz);
     BEM_CUDA(cudaMemcpyAsync(o->stage_x.p, x, nin * esz, cudaMemcpyHostToDevice, 0));

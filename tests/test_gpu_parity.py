@@ -178,3 +178,22 @@ def test_testhmatrix_diagnostic(capsys):
     rate, err = V.testhmatrix_result
     assert 0 < rate < 1.5 and err < 1e-6
     assert "compression rate" in capsys.readouterr().out
+
+
+def test_host_buffers_pinned_and_pageable():
+    """bem_operator_mult_host with page-locked buffers (read and written by the kernels in place)
+    and with pageable ones (staged), y = s A x + y, against the device entry point."""
+    m = icosphere(3)
+    op, trs, tes = _op(CASES[0], m, precision="mixed")
+    x = _vec(trs.ndof, False, 21)
+    y0 = _vec(tes.ndof, False, 22)
+    ref = y0 + 0.75 * (op.mat * torch.from_numpy(x).cuda()).cpu().numpy()
+    for pinned in (True, False):
+        if pinned:
+            xt = torch.from_numpy(x.copy()).pin_memory()
+            yt = torch.from_numpy(y0.copy()).pin_memory()
+            xh, yh = xt.numpy(), yt.numpy()
+        else:
+            xh, yh = x.copy(), y0.copy()
+        op.mat.mult_host(xh, alpha=0.75, beta=1.0, y=yh)
+        assert rel(yh, ref) < 1e-12
