@@ -58,9 +58,10 @@ typedef struct {
   double eps;             /* ACA tolerance (default 1e-6) */
   int method;             /* BEM_METHOD_ACA or BEM_METHOD_DENSE */
   int precision;          /* BEM_FP64 or BEM_MIXED */
-  int max_rank;           /* ACA rank cap per block; a block reaching it is assembled densely (0: 128) */
+  int max_rank;           /* ACA rank cap per block; a block reaching it is assembled densely (0: 128).
+                             ACA runs first with a cap of 48; blocks reaching that run again with this cap */
   double aca_eps_floor;   /* mixed precision: ACA tolerance floor (0: 2e-7) */
-  long long scratch_bytes;/* ACA scratch budget in bytes (0: 4 GiB) */
+  long long scratch_bytes;/* ACA scratch budget in bytes (0: an eighth of the device memory, at most 16 GiB) */
 } bem_params_t;
 
 /* Assembly and storage summary (reference HMatrix::NZE, src/hmat.cpp:623-630). */

@@ -83,7 +83,14 @@ void HOperator::assemble() {
   kcap = std::min(kcap, 256);
   double eps = prm.eps;
   if (prec == 1) eps = std::max(eps, prm.aca_eps_floor > 0 ? prm.aca_eps_floor : 2e-7);
-  const long long budget = prm.scratch_bytes > 0 ? prm.scratch_bytes : (4LL << 30);
+  // ACA scratch budget: the parameter, else an eighth of the device memory up to 16 GiB
+  long long budget = prm.scratch_bytes;
+  if (budget <= 0) {
+    size_t freeb = 0, totalb = 0;
+    BEM_CUDA(cudaMemGetInfo(&freeb, &totalb));
+    budget = std::min<long long>(16LL << 30, (long long)(totalb / 8));
+    budget = std::max<long long>(budget, 1LL << 30);
+  }
   MeshH& mesh = *trial->mesh;
   height = test->ndof;
   width = trial->ndof;
@@ -284,19 +291,27 @@ void HOperator::assemble() {
     if (maxc < 4) return full;  // too wide for a stage: one chunk, read in place
     return std::min(full, maxc);
   };
-  // plan the batches first so that the scratch is allocated once: cudaFree would
+  // ACA in rounds: every block first with a provisional rank cap; blocks that reach it while
+  // the operator's cap is larger run again from the start with that cap.  ACA is deterministic,
+  // so a block gets the factors it would get with the full cap in one round, while the scratch
+  // (cap x points per block) of the first round is a fraction of the full-cap one and fits in
+  // few batches (each batch waits for the host between its ACA and its projection).
+  std::vector<std::unique_ptr<DevBuf>> keep;
+  auto newbuf = [&]() { keep.push_back(std::make_unique<DevBuf>()); return keep.back().get(); };
+  auto aca_round = [&](const std::vector<int>& ids, int cap, std::vector<int>* retry) {
+  // plan the batches first so that the scratch is allocated once per round: cudaFree would
   // synchronise the device and serialise the near-field stream with the ACA stream
   std::vector<std::vector<FarDesc>> batches;
   std::vector<size_t> batch_first;
   long long max_su = 0, max_sv = 0;
   {
     size_t f0 = 0;
-    while (f0 < far_ids.size()) {
+    while (f0 < ids.size()) {
     std::vector<FarDesc> fd;
     long long su = 0, sv = 0;
     size_t f1 = f0;
-    while (f1 < far_ids.size()) {
-      const BlockH& B = blocks[far_ids[f1]];
+    while (f1 < ids.size()) {
+      const BlockH& B = blocks[ids[f1]];
       FarDesc d;
       const ClusterH& ci = ttest->cl[B.rowcl];
       const ClusterH& cj = ttrial->cl[B.colcl];
@@ -306,7 +321,7 @@ void HOperator::assemble() {
       d.pj0 = ttrial->patch_ptr[B.colcl];
       d.nj = ttrial->patch_ptr[B.colcl + 1] - d.pj0;
       const long long M = (long long)d.ni * nq, N = (long long)d.nj * nq;
-      d.kcap = (int)std::min<long long>(kcap, std::min(M, N));
+      d.kcap = (int)std::min<long long>(cap, std::min(M, N));
       d.pad = 0;
       const long long need = (long long)NC * d.kcap * (M + N) * (long long)psz;
       if (f1 > f0 && (su + sv) * (long long)psz + need > budget) break;
@@ -324,13 +339,12 @@ void HOperator::assemble() {
     f0 = f1;
     }
   }
-  DevBuf d_U, d_V;
+  DevBuf& d_U = *newbuf();
+  DevBuf& d_V = *newbuf();
   if (!batches.empty()) {
     d_U.alloc((size_t)max_su * psz);
     d_V.alloc((size_t)max_sv * psz);
   }
-  std::vector<std::unique_ptr<DevBuf>> keep;
-  auto newbuf = [&]() { keep.push_back(std::make_unique<DevBuf>()); return keep.back().get(); };
   for (size_t bi = 0; bi < batches.size(); ++bi) {
     const std::vector<FarDesc>& fd = batches[bi];
     const size_t f0 = batch_first[bi];
@@ -371,11 +385,15 @@ void HOperator::assemble() {
     std::vector<int> pranks((size_t)nf * NC, 0);
     long long usz = 0, vsz = 0;
     for (int f = 0; f < nf; ++f) {
-      const int b = far_ids[f0 + f];
+      const int b = ids[f0 + f];
       LRDesc& L = lr[f];
       L.r0 = fd[f].r0; L.m = fd[f].m; L.c0 = fd[f].c0; L.n = fd[f].n;
       L.R = 0; L.toff = 0; L.u = 0; L.v = 0; L.cu = 4; L.cv = 4;
-      if (status[f]) { overflow_ids.push_back(b); block_fallback[b] = 2; continue; }
+      if (status[f]) {
+        if (retry && fd[f].kcap < kcap) retry->push_back(b);  // the full cap may still converge
+        else { overflow_ids.push_back(b); block_fallback[b] = 2; }
+        continue;
+      }
       int R = 0;
       const int nt = (kid == K_LAPLACE_HS) ? 3 : ((kid == K_HELMHOLTZ_HS || kid == K_MAXWELL_SL) ? 4 : 1);
       for (int tt = 0; tt < nt; ++tt) {
@@ -430,13 +448,20 @@ void HOperator::assemble() {
     ms_proj += t;
     for (int f = 0; f < nf; ++f) {
       if (status[f]) continue;
-      const int b = far_ids[f0 + f];
+      const int b = ids[f0 + f];
       block_rank[b] = lr[f].R;
       lr_all.push_back(lr[f]);
       lr_block.push_back(b);
     }
     pools.push_back(std::move(upool));
     pools.push_back(std::move(vpool));
+  }
+  };
+  {
+    const int cap1 = std::min(kcap, 48);
+    std::vector<int> retry;
+    aca_round(far_ids, cap1, cap1 < kcap ? &retry : nullptr);
+    if (!retry.empty()) aca_round(retry, kcap, nullptr);
   }
 
   // ---- near-field pass 1 done; pass 2 for ACA rank-cap blocks ------------------------------
@@ -497,8 +522,6 @@ void HOperator::assemble() {
   info.ms_mvitems = ms_since(t_items);
   BEM_CUDA(cudaDeviceSynchronize());
   keep.clear();
-  d_U.release();
-  d_V.release();
 
   // ---- info -----------------------------------------------------------------------------------
   info.is_complex = cplx ? 1 : 0;
