@@ -1,6 +1,8 @@
 // Far-field compression (reference CalcFarFieldBlock, src/ngbem.cpp:743-1163).
 //
-// aca_kernel: one CTA per admissible block, many uneven blocks per launch.  Partially
+// aca_warp_kernel / aca_kernel: one warp per small admissible block (at most ACA_WARP_PTS row
+//   plus column points; 8 blocks per CTA), one CTA per larger block; both launched over the
+//   whole batch, each skipping the other's blocks, on two streams.  Partially
 //   pivoted ACA on the point kernel matrix (rows = test quadrature points, cols = trial
 //   quadrature points), one pass per kernel component, restating src/ngbem.cpp:902-1049:
 //   start row 0, column pivot = argmax |v_j| over j != previous column pivot, symmetric
@@ -19,6 +21,9 @@ namespace bem {
 #define ACA_T 256
 #define ACA_NW (ACA_T / 32)
 #define KCAP_MAX 256
+// blocks with at most this many row + column points are compressed by one warp each
+// (aca_warp_kernel, 8 blocks per CTA); larger ones by a whole CTA (aca_kernel)
+#define ACA_WARP_PTS 1536
 
 template <class V, int N>
 __device__ __forceinline__ void block_sum_arr(V (&v)[N], V* sbuf) {
@@ -94,6 +99,7 @@ __global__ void __launch_bounds__(ACA_T, sizeof(P) == 4 ? 4 : 2) aca_kernel(AcaA
   const FarDesc d = a.far[blockIdx.x];
   const int nq = a.nq;
   const int M = d.ni * nq, N = d.nj * nq;
+  if (M + N <= ACA_WARP_PTS) return;  // a warp of aca_warp_kernel takes it
   const int p = min(M, N);
   const int kcap = min(d.kcap, KCAP_MAX);
   const APt<P>* PT = (const APt<P>*)a.apts;
@@ -201,6 +207,132 @@ __global__ void __launch_bounds__(ACA_T, sizeof(P) == 4 ? 4 : 2) aca_kernel(AcaA
   if (threadIdx.x == 0) a.status[blockIdx.x] = status;
 }
 
+// The same partially pivoted ACA as aca_kernel (identical steps, pivot and stopping rules),
+// one warp per block: the reductions are warp shuffles and no CTA barrier is needed, so the
+// many small admissible blocks (a few hundred points a side) run 64 to an SM instead of 4.
+template <int KID, class P>
+__global__ void __launch_bounds__(256, 4) aca_warp_kernel(AcaArgs a) {
+  using G = Green<KID>;
+  using V = VT<G::CPLX, P>;
+  constexpr int NC = G::NC;
+  __shared__ V s_lw[8][KCAP_MAX];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int b = blockIdx.x * 8 + wid;
+  if (b >= a.nfar) return;
+  const FarDesc d = a.far[b];
+  const int nq = a.nq;
+  const int M = d.ni * nq, N = d.nj * nq;
+  if (M + N > ACA_WARP_PTS) return;  // aca_kernel takes it
+  V* s_l = s_lw[wid];
+  const int p = min(M, N);
+  const int kcap = min(d.kcap, KCAP_MAX);
+  const APt<P>* PT = (const APt<P>*)a.apts;
+  const ElemRecP<P>* E = (const ElemRecP<P>*)a.erecP;
+  const P kappa = (P)a.kappa;
+  const double eps = a.eps;
+  int status = 0;
+
+  for (int comp = 0; comp < NC; ++comp) {
+    V* U = (V*)a.U + d.su + (size_t)comp * d.kcap * M;
+    V* Vm = (V*)a.V + d.sv + (size_t)comp * d.kcap * N;
+    int ik = 0, ikm1 = 0, jkm1 = N + 1;
+    double norm2 = 0.0;
+    int rank = p;
+    bool stopped = false;
+    const int kmax = min(p, kcap);
+    for (int k = 0; k < kmax; ++k) {
+      // ---- row ik: v_j = K(x_ik, y_j) - sum_l U(ik,l) V(l,j)
+      for (int l = lane; l < k; l += 32) s_l[l] = U[(size_t)l * M + ik];
+      __syncwarp();
+      const PtData<P> x = load_pt<P, G::NEEDS_NX>(PT, E, a.patch_test, d.pi0, ik, nq);
+      P best = P(0);
+      int bi = -1;
+      V* Vk = Vm + (size_t)k * N;
+      for (int j = lane; j < N; j += 32) {
+        const PtData<P> y = load_pt<P, G::NEEDS_NY>(PT, E, a.patch_trial, d.pj0, j, nq);
+        V v = kern_entry<G, P, V>(x, y, kappa, comp);
+        for (int l = 0; l < k; ++l) v -= s_l[l] * Vm[(size_t)l * N + j];
+        Vk[j] = v;
+        const P av = absv(v);
+        if (j != jkm1 && av > best) { best = av; bi = j; }
+      }
+      warp_argmax(best, bi);
+      if (bi < 0) { rank = k; stopped = true; break; }
+      const int jk = bi;
+      const P vkj = best;
+      __syncwarp();
+      const V piv = Vk[jk];
+      const V sc = invv(piv) * sqrt_(vkj);
+      P nv = P(0);
+      for (int j = lane; j < N; j += 32) {
+        V v = Vk[j] * sc;
+        Vk[j] = v;
+        nv += norm2v(v);
+      }
+      // ---- column jk: u_i = (K(x_i, y_jk) - sum_l U(i,l) V(l,jk)) / sqrt(vkj)
+      __syncwarp();
+      for (int l = lane; l < k; l += 32) s_l[l] = Vm[(size_t)l * N + jk];
+      __syncwarp();
+      const PtData<P> y = load_pt<P, G::NEEDS_NY>(PT, E, a.patch_trial, d.pj0, jk, nq);
+      const P isq = P(1) / sqrt_(vkj);
+      P nu = P(0), bu = P(0);
+      int biu = -1;
+      V* Uk = U + (size_t)k * M;
+      for (int i = lane; i < M; i += 32) {
+        const PtData<P> xi = load_pt<P, G::NEEDS_NX>(PT, E, a.patch_test, d.pi0, i, nq);
+        V u = kern_entry<G, P, V>(xi, y, kappa, comp);
+        for (int l = 0; l < k; ++l) u -= U[(size_t)l * M + i] * s_l[l];
+        u *= isq;
+        Uk[i] = u;
+        nu += norm2v(u);
+        const P au = absv(u);
+        if (i != ikm1 && au > bu) { bu = au; biu = i; }
+      }
+      warp_argmax(bu, biu);
+      nv = warp_sum(nv);
+      nu = warp_sum(nu);
+      const int iknew = biu >= 0 ? biu : ik;
+      const double norm_k = sqrt((double)nv) * sqrt((double)nu);
+      norm2 += norm_k * norm_k;
+      __syncwarp();
+      // ---- cross terms 2 Re(conj(<V_k, V_l>) <U_k, U_l>) for l < k, 8 at a time
+      for (int l0 = 0; l0 < k; l0 += 8) {
+        V dd[16];
+#pragma unroll
+        for (int c = 0; c < 16; ++c) dd[c] = vzero<V>();
+        const int nl = min(8, k - l0);
+        for (int j = lane; j < N; j += 32) {
+          const V vk = Vk[j];
+#pragma unroll
+          for (int c = 0; c < 8; ++c)
+            if (c < nl) dd[c] += vk * conjv(Vm[(size_t)(l0 + c) * N + j]);
+        }
+        for (int i = lane; i < M; i += 32) {
+          const V uk = Uk[i];
+#pragma unroll
+          for (int c = 0; c < 8; ++c)
+            if (c < nl) dd[8 + c] += uk * conjv(U[(size_t)(l0 + c) * M + i]);
+        }
+#pragma unroll
+        for (int c = 0; c < 16; ++c) dd[c] = warp_sum(dd[c]);
+        for (int c = 0; c < nl; ++c) norm2 += 2.0 * (double)realv(conjv(dd[c]) * dd[8 + c]);
+      }
+      ikm1 = iknew;
+      jkm1 = jk;
+      ik = iknew;
+      const double noise = sizeof(P) == 4 ? 4.0 * 5.9604644775390625e-8 * sqrt((double)(k + 1)) : 0.0;
+      if (norm_k < fmax(eps, noise) * sqrt(norm2)) { rank = k + 1; stopped = true; break; }
+    }
+    if (!stopped) {
+      if (kmax < p) { status = 1; rank = kmax; }
+      else rank = p;
+    }
+    if (lane == 0) a.ranks[b * NC + comp] = rank;
+    __syncwarp();
+  }
+  if (lane == 0) a.status[b] = status;
+}
+
 __device__ __forceinline__ int i4c_(const int4& v, int a) { return a == 0 ? v.x : (a == 1 ? v.y : v.z); }
 template <class P> struct P2_ { P x, y; };
 
@@ -295,15 +427,41 @@ __global__ void __launch_bounds__(256) aca_project_kernel(ProjArgs a) {
 
 void launch_aca(int kid, int prec, const AcaArgs& a, cudaStream_t s) {
   if (a.nfar <= 0) return;
+  // small blocks (a warp each) on the caller's stream, large blocks (a CTA each) beside them
+  // on a second stream, joined before returning
+  cudaStream_t s2 = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  if (cudaStreamCreateWithFlags(&s2, cudaStreamNonBlocking) != cudaSuccess) s2 = s;
+  if (s2 != s) {
+    cudaEventCreateWithFlags(&e0, cudaEventDisableTiming);
+    cudaEventCreateWithFlags(&e1, cudaEventDisableTiming);
+    cudaEventRecord(e0, s);
+    cudaStreamWaitEvent(s2, e0, 0);
+  }
+  auto join = [&]() {
+    if (s2 == s) return;
+    cudaEventRecord(e1, s2);
+    cudaStreamWaitEvent(s, e1, 0);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaStreamDestroy(s2);
+  };
 #define X(K)                                                                   \
   if (kid == K) {                                                              \
-    if (prec == 0) aca_kernel<K, double><<<a.nfar, ACA_T, 0, s>>>(a);          \
-    else aca_kernel<K, float><<<a.nfar, ACA_T, 0, s>>>(a);                     \
+    if (prec == 0) {                                                           \
+      aca_kernel<K, double><<<a.nfar, ACA_T, 0, s2>>>(a);                      \
+      aca_warp_kernel<K, double><<<(a.nfar + 7) / 8, 256, 0, s>>>(a);          \
+    } else {                                                                   \
+      aca_kernel<K, float><<<a.nfar, ACA_T, 0, s2>>>(a);                       \
+      aca_warp_kernel<K, float><<<(a.nfar + 7) / 8, 256, 0, s>>>(a);           \
+    }                                                                          \
+    join();                                                                    \
     return;                                                                    \
   }
   X(K_LAPLACE_SL) X(K_LAPLACE_DL) X(K_LAPLACE_HS) X(K_HELMHOLTZ_SL) X(K_HELMHOLTZ_DL)
   X(K_HELMHOLTZ_HS) X(K_HELMHOLTZ_CF) X(K_MAXWELL_SL) X(K_HELMHOLTZ_SL_DKAPPA)
 #undef X
+  join();
 }
 
 #define BEM_PJ_COMBOS(X)                                                              \
