@@ -225,6 +225,19 @@ int bem_operator_set_tensor_cores(bem_operator_t op, int enable);
 int bem_operator_tensor_cores(bem_operator_t op, int* state, long long* bytes, int* items0, int* items1,
                               double* ms_build);
 
+/* Potential of a density (reference GenericIntegralOperator::GetPotential / PotentialCF,
+ * src/ngbem.cpp:1166-1301): out[p * dim + c] = sum over the trial elements, the points y of
+ * the regular rule (the operator's intorder) and the kernel terms of
+ * w_y K(x_p, y, n_p, n_y) (trial evaluator applied to the density)_c, in FP64; as in the
+ * reference, term factors are not applied.  density: trial dofs (double, or complex128 for
+ * complex kernels); points, normals: 3 doubles per point (normals may be NULL unless the
+ * kernel uses n_x: the Helmholtz hypersingular); out: dim values per point.  All device
+ * pointers; synchronous on `stream`.  dim is the trial evaluator's dimension (1 for P0/P1
+ * identity traces), 0 when the operator has no potential. */
+int bem_operator_potential_dim(bem_operator_t op, int* dim);
+int bem_operator_potential(bem_operator_t op, const void* density, int npts, const double* points,
+                           const double* normals, void* out, void* stream);
+
 /* Known-answer check of the tensor-core encodings on the current device (one 128 x 32 x 16
  * split-TF32 product of exactly representable values).  passed = 1 when every entry is exact. */
 int bem_tc_selftest(int* passed);

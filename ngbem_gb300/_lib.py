@@ -75,6 +75,8 @@ SIGNATURES = {
     "bem_operator_set_tensor_cores": ([_vp, C.c_int], C.c_int),
     "bem_operator_tensor_cores": ([_vp, _ip, C.POINTER(C.c_longlong), _ip, _ip, _dp], C.c_int),
     "bem_tc_selftest": ([_ip], C.c_int),
+    "bem_operator_potential_dim": ([_vp, _ip], C.c_int),
+    "bem_operator_potential": ([_vp, _vp, C.c_int, _vp, _vp, _vp, _vp], C.c_int),
     "bem_operator_kernel_times": ([_vp, _dp, C.POINTER(C.c_longlong)], C.c_int),
     "bem_sl_batch_create": ([C.c_int, _ip, _ip, _ip, C.c_int, C.c_int, C.c_int, C.c_int, C.POINTER(_vp)], C.c_int),
     "bem_sl_batch_eval": ([_vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp], C.c_int),

@@ -133,6 +133,43 @@ def cluster_tree(space: TraceSpace, leafsize: int = 40):
     return perm, ci[: 7 * n].reshape(n, 7), cd[: 23 * n].reshape(n, 23)
 
 
+class Potential:
+    """Field of a density at arbitrary points (the role of the reference's PotentialCF): FP64,
+    all trial elements and the regular rule's points, the operator's kernel terms."""
+
+    def __init__(self, op: "IntegralOperator", gf):
+        torch = _torch()
+        self.op = op
+        h = op.mat.h
+        d = C.c_int()
+        check(lib.bem_operator_potential_dim(h, C.byref(d)))
+        if d.value == 0:
+            raise ValueError("this operator has no potential")
+        self.dim = d.value
+        dt = torch.complex128 if op.mat.is_complex else torch.float64
+        if not isinstance(gf, torch.Tensor):
+            gf = torch.as_tensor(np.asarray(gf)).cuda()
+        self.density = _as_device(gf, dt).contiguous()
+        if self.density.shape[0] != op.mat.width:
+            raise ValueError("density length does not match the trial space")
+
+    def __call__(self, points, normals=None):
+        torch = _torch()
+
+        def dev(a):
+            return _as_device(a if isinstance(a, torch.Tensor) else torch.as_tensor(np.asarray(a)).cuda(),
+                              torch.float64).reshape(-1, 3).contiguous()
+        P = dev(points)
+        Nn = None if normals is None else dev(normals)
+        out = torch.empty((P.shape[0], self.dim), dtype=self.density.dtype, device=P.device)
+        stream = torch.cuda.current_stream().cuda_stream
+        check(lib.bem_operator_potential(self.op.mat.h, C.c_void_p(self.density.data_ptr()), P.shape[0],
+                                         C.c_void_p(P.data_ptr()),
+                                         C.c_void_p(Nn.data_ptr()) if Nn is not None else None,
+                                         C.c_void_p(out.data_ptr()), C.c_void_p(stream)))
+        return out[:, 0] if self.dim == 1 else out
+
+
 def tc_selftest() -> bool:
     """Known-answer check of the tensor-core encodings on the current GPU (True: exact)."""
     ok = C.c_int()
@@ -439,7 +476,10 @@ class IntegralOperator:
         return self.mat.info
 
     def GetPotential(self, gf):
-        raise NotImplementedError("potential evaluation (PotentialCF) is not part of this build")
+        """Potential of the trial-space density gf (reference GetPotential, src/ngbem.cpp:1166-1172):
+        a callable ``pot(points, normals=None)`` giving the field at points (n, 3) on the GPU, shape
+        (n,) for scalar trial traces, else (n, dim)."""
+        return Potential(self, gf)
 
     def _test_hmatrix(self):
         """Reference testhmatrix diagnostic (src/ngbem.cpp:332-369): dense assembly plus 30

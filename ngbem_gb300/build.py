@@ -23,7 +23,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 HOST_SOURCES = ["quadrature.cpp", "geometry.cpp", "operator.cpp", "energy_host.cpp", "tc_host.cpp", "capi.cpp"]
 CUDA_SOURCES = ["nearfield.cu", "aca.cu", "matvec.cu", "mult_noalloc.cu", "energy.cu", "gmres_batch.cu",
-                "tc_matvec.cu"]
+                "tc_matvec.cu", "potential.cu"]
 HEADERS = ["bem_shared.h", "bem_device.cuh", "kernels.h", "host.hpp"]
 
 

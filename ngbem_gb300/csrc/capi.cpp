@@ -291,6 +291,25 @@ int bem_operator_set_accuracy(bem_operator_t op, int compensated) {
   });
 }
 
+int bem_operator_potential_dim(bem_operator_t op, int* dim) {
+  return guarded([&] {
+    REQUIRE(op && dim, "null argument");
+    auto* h = dynamic_cast<HOperator*>(op->op.get());
+    if (!h) throw Error(BEM_ERR_STATE, "not an H-matrix operator");
+    *dim = potential_dim(h->kid, h->trt);
+  });
+}
+
+int bem_operator_potential(bem_operator_t op, const void* density, int npts, const double* points,
+                           const double* normals, void* out, void* stream) {
+  return guarded([&] {
+    REQUIRE(op && density && (npts == 0 || (points && out)), "null argument");
+    auto* h = dynamic_cast<HOperator*>(op->op.get());
+    if (!h) throw Error(BEM_ERR_STATE, "not an H-matrix operator");
+    h->potential(density, npts, points, normals, out, (cudaStream_t)stream);
+  });
+}
+
 int bem_operator_set_tensor_cores(bem_operator_t op, int enable) {
   return guarded([&] {
     REQUIRE(op, "null argument");

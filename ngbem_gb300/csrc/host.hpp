@@ -229,6 +229,9 @@ struct HOperator : OperatorBase {
   void mult(int trans, const double* alpha, const void* x, const double* beta, void* y, int nrhs,
             cudaStream_t s) override;
   void to_dense(void* out);
+  // potential of a trial-space density at points (device buffers; synchronous)
+  void potential(const void* density, int npts, const double* pts, const double* normals, void* out,
+                 cudaStream_t s);
 };
 
 struct MassOperator : OperatorBase {

@@ -229,6 +229,26 @@ void launch_bnrm2(bool cplx, int n, int nrhs, const void* w, double* out, cudaSt
 void launch_bscale(bool cplx, int n, int nrhs, const void* w, const double* inv, void* q, cudaStream_t s);
 void launch_residual(bool cplx, int n, const void* b, void* r, cudaStream_t s);
 
+// ---- potential evaluation (potential.cu) ----------------------------------------------------
+struct PotArgs {
+  const void* erec;       // ElemRecP<double>[nt]
+  const void* qoff;       // QPt<double>[nt * nq]: rule points relative to the centroid, w * |J|
+  const double* rq;       // reference points (xi, eta) of the rule
+  int nt, nq;
+  SpaceDev trial;
+  const void* density;    // trial dofs (double or complex128)
+  double* src_pos;        // 6 per rule point: y, n_y
+  void* src_val;          // trial dimension per rule point: weighted evaluator values
+  int npts;
+  const double* pts;      // 3 per evaluation point
+  const double* normals;  // 3 per evaluation point, or null
+  double kappa;
+  void* out;              // trial dimension per evaluation point
+};
+// components of the potential for (kernel, trial trace), 0 if there is none
+int potential_dim(int kid, int trt);
+int launch_potential(int kid, int trt, const PotArgs& a, cudaStream_t s);
+
 // ---- tensor-core products for several right-hand sides (tc_matvec.cu) ---------------------
 // Operand panels are in the canonical K-major, no-swizzle layout of tcgen05 (core matrices of
 // 8 rows x 16 bytes), K counted in "cores" of 4 FP32 values:

@@ -1127,6 +1127,41 @@ void HOperator::mult(int trans, const double* alpha, const void* x, const double
   BEM_CUDA(cudaGetLastError());
 }
 
+void HOperator::potential(const void* density, int npts, const double* pts, const double* normals, void* out,
+                          cudaStream_t s) {
+  const int dim = potential_dim(kid, trt);
+  if (dim == 0) throw Error(BEM_ERR_ARG, "no potential for this kernel and trial space");
+  if (npts < 0) throw Error(BEM_ERR_ARG, "npts must be >= 0");
+  if (kid == K_HELMHOLTZ_HS && !normals) throw Error(BEM_ERR_ARG, "this kernel needs the normals at the points");
+  MeshH& mesh = *trial->mesh;
+  mesh.ensure_device();
+  trial->ensure_device();
+  const int order_r = prm.intorder_regular > 0 ? prm.intorder_regular : prm.intorder;
+  MeshH::RuleTables& rt = mesh.rule_tables(order_r);
+  const size_t nsrc = (size_t)mesh.nt * rt.nq;
+  DevBuf src_pos, src_val;
+  src_pos.alloc(nsrc * 6 * sizeof(double));
+  src_val.alloc(nsrc * dim * (cplx ? 16 : 8));
+  PotArgs a{};
+  a.erec = rt.rec[0].p;
+  a.qoff = rt.qoff[0].p;
+  a.rq = rt.rq[0].as<double>();
+  a.nt = mesh.nt;
+  a.nq = rt.nq;
+  a.trial = space_dev(*trial, trt, d_pinv_trial);
+  a.density = density;
+  a.src_pos = src_pos.as<double>();
+  a.src_val = src_val.p;
+  a.npts = npts;
+  a.pts = pts;
+  a.normals = normals;
+  a.kappa = kappa;
+  a.out = out;
+  if (!launch_potential(kid, trt, a, s)) throw Error(BEM_ERR_ARG, "no potential for this kernel and trial space");
+  BEM_CUDA(cudaGetLastError());
+  BEM_CUDA(cudaStreamSynchronize(s));
+}
+
 int HOperator::device_status() {
   int e = 0;
   BEM_CUDA(cudaMemcpy(&e, d_err.p, sizeof(int), cudaMemcpyDeviceToHost));

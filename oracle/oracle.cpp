@@ -1249,6 +1249,55 @@ void orc_operator_destroy(void* h_) {
   delete h;
 }
 
+extern "C++" {
+// PotentialCF::T_Evaluate (src/ngbem.cpp:1187-1238): for each point, every element of the trial
+// space, the evaluator applied to the element vector at the regular rule's points, and the
+// kernel terms (term factors are not applied there, as in the reference)
+template <class T>
+static void potential_t(int kernel, double kappa, const Mesh& m, const Space& sp, int ev, int intorder,
+                        const T* density, int npts, const double* pts, const double* normals, T* out) {
+  Kernel K(kernel, kappa);
+  TrigRule r = trig_rule(intorder);
+  const int dim = trace_dim(sp.kind, ev);
+  std::fill(out, out + (size_t)npts * dim, T(0));
+  const double nz[3] = {0.0, 0.0, 0.0};
+  for (int p = 0; p < npts; ++p) {
+    const double* x = pts + 3 * (size_t)p;
+    const double* nx = normals ? normals + 3 * (size_t)p : nz;
+    for (int e = 0; e < m.nt; ++e) {
+      for (size_t q = 0; q < r.w.size(); ++q) {
+        double S[3][4] = {{0}};
+        eval_trace(m, sp, ev, e, r.xi[q], r.eta[q], S);
+        T vals[4] = {T(0), T(0), T(0), T(0)};
+        for (int a = 0; a < sp.nd; ++a)
+          for (int c = 0; c < dim; ++c) vals[c] += density[sp.el_dofs(e)[a]] * S[a][c];
+        double y[3];
+        m.map(e, r.xi[q], r.eta[q], y);
+        const double w = r.w[q] * m.geo[e].detJ;
+        T kv[2];
+        K.eval<T>(x, y, nx, m.geo[e].n, kv);
+        for (const Term& t : K.terms) out[(size_t)p * dim + t.tec] += w * kv[t.kc] * vals[t.trc];
+      }
+    }
+  }
+}
+}
+
+int orc_potential(int kernel, double kappa, int nv, const double* xyz, int nt, const int* tri, int trial_kind,
+                  int trial_eval, int trial_dual, int intorder, const double* density, int npts, const double* pts,
+                  const double* normals, double* out) {
+  Mesh m;
+  m.build(nv, xyz, nt, tri);
+  Space sp;
+  sp.build(m, trial_kind, trial_dual != 0);
+  if (kernel >= ORC_HELMHOLTZ_SL)
+    potential_t<cplx>(kernel, kappa, m, sp, trial_eval, intorder, (const cplx*)density, npts, pts, normals,
+                      (cplx*)out);
+  else
+    potential_t<double>(kernel, kappa, m, sp, trial_eval, intorder, density, npts, pts, normals, out);
+  return 0;
+}
+
 int orc_mass_matrix(int nv, const double* xyz, int nt, const int* tri, int trial_kind, int test_kind,
                     int order, double* out) {
   Mesh m; m.build(nv, xyz, nt, tri);

@@ -91,6 +91,13 @@ void orc_operator_destroy(void* op);
 // Galerkin mass matrix <u, v> for scalar/vector identity traces (dense, row = test)
 int orc_mass_matrix(int nv, const double* xyz, int nt, const int* tri,
                     int trial_kind, int test_kind, int order, double* out);
+// Potential of a density at points (reference PotentialCF::T_Evaluate, src/ngbem.cpp:1187-1238):
+// out[p * dim + tec] = sum over elements, regular points y and kernel terms of
+// w_y K_kc(x_p, y, n_p, n_y) (trial evaluator applied to the density)_trc, dim = trial
+// evaluator dimension; normals (3 per point) may be NULL for kernels without n_x.
+int orc_potential(int kernel, double kappa, int nv, const double* xyz, int nt, const int* tri,
+                  int trial_kind, int trial_eval, int trial_dual, int intorder, const double* density,
+                  int npts, const double* pts, const double* normals, double* out);
 
 #ifdef __cplusplus
 }

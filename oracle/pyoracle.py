@@ -58,6 +58,8 @@ def lib():
                                        C.POINTER(Params), dp]
         L.orc_operator_destroy.argtypes = [C.c_void_p]
         L.orc_mass_matrix.argtypes = [C.c_int, dp, C.c_int, ip, C.c_int, C.c_int, C.c_int, dp]
+        L.orc_potential.argtypes = [C.c_int, C.c_double, C.c_int, dp, C.c_int, ip, C.c_int, C.c_int, C.c_int,
+                                    C.c_int, dp, C.c_int, dp, dp, dp]
         _LIB = L
     return _LIB
 
@@ -190,6 +192,23 @@ def dense_matrix(kernel, mesh, trial="P0", test=None, kappa=0.0, trial_eval="id"
     lib().orc_dense_matrix(KERNELS[kernel], float(kappa), mesh.nv, _dp(X), mesh.nt, _ip(T),
                            KINDS[trial], EVALS[trial_eval], int(trial_dual), KINDS[test],
                            EVALS[test_eval], int(test_dual), C.byref(p), _dp(out.view(np.float64)))
+    return out
+
+
+def potential(kernel, mesh, trial, density, points, normals=None, kappa=0.0, trial_eval="id", intorder=3,
+              trial_dual=False):
+    """Potential of `density` (trial dofs) at `points` (reference PotentialCF): (npts, dim)."""
+    X = np.ascontiguousarray(mesh.vertices, dtype=np.float64)
+    T = np.ascontiguousarray(mesh.triangles, dtype=np.int32)
+    cplx = KERNELS[kernel] >= 3
+    dens = np.ascontiguousarray(density, dtype=np.complex128 if cplx else np.float64)
+    P = np.ascontiguousarray(points, dtype=np.float64).reshape(-1, 3)
+    Nn = None if normals is None else np.ascontiguousarray(normals, dtype=np.float64).reshape(-1, 3)
+    dim = 3 if (trial == "RT0" and trial_eval == "id") else (1 if trial_eval == "id" else (3 if trial_eval == "rot" else 4))
+    out = np.zeros((P.shape[0], dim), dtype=dens.dtype)
+    lib().orc_potential(KERNELS[kernel], float(kappa), mesh.nv, _dp(X), mesh.nt, _ip(T), KINDS[trial],
+                        EVALS[trial_eval], int(trial_dual), int(intorder), _dp(dens.view(np.float64)), P.shape[0],
+                        _dp(P), None if Nn is None else _dp(Nn), _dp(out.view(np.float64)))
     return out
 
 

@@ -131,3 +131,18 @@ def test_dkappa_kernel_is_the_kappa_derivative(oracle, kind):
     assert np.linalg.norm(D - fd) / np.linalg.norm(fd) < 1e-7
     # symmetric up to the quadrature (the Sauter-Schwab rules are not symmetric in the pair)
     assert np.linalg.norm(D - D.T) / np.linalg.norm(D) < 1e-4
+
+
+def test_potential_known_answers(oracle):
+    """Single-layer potential of the constant density 1 on the unit sphere: 1/|x| outside and 1
+    inside (the surface is a polyhedron, so the answers hold to the discretisation error); the
+    double-layer potential of 1: 0 outside, -1 inside (jump relation, outward normals)."""
+    m = icosphere(4)
+    P0 = np.ones(m.nt)
+    pts = np.array([[0.0, 0.0, 2.0], [1.5, 1.0, 0.5], [0.1, -0.2, 0.3], [0.0, 0.0, 0.0]])
+    r = np.linalg.norm(pts, axis=1)
+    sl = oracle.potential("laplace_sl", m, "P0", P0, pts, intorder=4)[:, 0]
+    assert np.allclose(sl[:2], 1.0 / r[:2], rtol=5e-3)
+    assert np.allclose(sl[2:], 1.0, rtol=5e-3)
+    dl = oracle.potential("laplace_dl", m, "P0", P0, pts, intorder=4)[:, 0]
+    assert np.allclose(dl, [0.0, 0.0, -1.0, -1.0], atol=5e-3)
