@@ -225,6 +225,13 @@ int bem_operator_set_tensor_cores(bem_operator_t op, int enable);
 int bem_operator_tensor_cores(bem_operator_t op, int* state, long long* bytes, int* items0, int* items1,
                               double* ms_build);
 
+/* An assembled H-matrix to a file and back (no counterpart in the reference, which reassembles
+ * each session).  The file holds the partition, ranks, dense blocks and factors; loading needs
+ * the same trial and test spaces (checked through their cluster trees) and applies exactly
+ * like the saved operator.  test may be NULL (= trial). */
+int bem_operator_save(bem_operator_t op, const char* path);
+int bem_operator_load(const char* path, bem_space_t trial, bem_space_t test, bem_operator_t* out);
+
 /* Potential of a density (reference GenericIntegralOperator::GetPotential / PotentialCF,
  * src/ngbem.cpp:1166-1301): out[p * dim + c] = sum over the trial elements, the points y of
  * the regular rule (the operator's intorder) and the kernel terms of

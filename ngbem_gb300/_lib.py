@@ -76,6 +76,8 @@ SIGNATURES = {
     "bem_operator_tensor_cores": ([_vp, _ip, C.POINTER(C.c_longlong), _ip, _ip, _dp], C.c_int),
     "bem_tc_selftest": ([_ip], C.c_int),
     "bem_operator_potential_dim": ([_vp, _ip], C.c_int),
+    "bem_operator_save": ([_vp, C.c_char_p], C.c_int),
+    "bem_operator_load": ([C.c_char_p, _vp, _vp, C.POINTER(_vp)], C.c_int),
     "bem_operator_potential": ([_vp, _vp, C.c_int, _vp, _vp, _vp, _vp], C.c_int),
     "bem_operator_kernel_times": ([_vp, _dp, C.POINTER(C.c_longlong)], C.c_int),
     "bem_sl_batch_create": ([C.c_int, _ip, _ip, _ip, C.c_int, C.c_int, C.c_int, C.c_int, C.POINTER(_vp)], C.c_int),

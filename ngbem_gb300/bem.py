@@ -398,6 +398,18 @@ class HMatrix(_NativeMatrix):
         self.tuned = {"piece": piece.value, "fused": bool(fused.value), "ms": ms.value}
         return self.tuned
 
+    def save(self, path: str):
+        """Write the assembled H-matrix (partition, ranks, dense blocks, factors) to a file."""
+        check(lib.bem_operator_save(self.h, str(path).encode()))
+
+    @classmethod
+    def load(cls, path: str, trial_space: "TraceSpace", test_space: "TraceSpace | None" = None) -> "HMatrix":
+        """An H-matrix saved by save(), on the same trial and test spaces, without assembly."""
+        h = C.c_void_p()
+        check(lib.bem_operator_load(str(path).encode(), trial_space.h,
+                                    (test_space or trial_space).h, C.byref(h)))
+        return cls(h)
+
     def set_tensor_cores(self, enable: bool = True):
         """Tensor-core products for 2..32 right-hand sides at plain accuracy (complex FP32 storage):
         True builds the packed panels now when the operator qualifies, False turns them off."""

@@ -291,6 +291,27 @@ int bem_operator_set_accuracy(bem_operator_t op, int compensated) {
   });
 }
 
+int bem_operator_save(bem_operator_t op, const char* path) {
+  return guarded([&] {
+    REQUIRE(op && path, "null argument");
+    auto* h = dynamic_cast<HOperator*>(op->op.get());
+    if (!h) throw Error(BEM_ERR_STATE, "not an H-matrix operator");
+    save_operator(*h, path);
+  });
+}
+
+int bem_operator_load(const char* path, bem_space_t trial, bem_space_t test, bem_operator_t* out) {
+  return guarded([&] {
+    REQUIRE(path && trial && out, "null argument");
+    if (!test) test = trial;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) throw Error(BEM_ERR_CUDA, "no CUDA device");
+    auto h = std::make_unique<bem_operator_s>();
+    h->op = load_operator(path, &trial->s, &test->s);
+    *out = h.release();
+  });
+}
+
 int bem_operator_potential_dim(bem_operator_t op, int* dim) {
   return guarded([&] {
     REQUIRE(op && dim, "null argument");

@@ -267,6 +267,10 @@ struct SLBatch {
 // 1 when the tensor-core encodings passed their known-answer product on this device (run once)
 int tc_selftest();
 
+// an assembled H-matrix to / from a file (serialize.cpp)
+void save_operator(const HOperator& op, const char* path);
+std::unique_ptr<HOperator> load_operator(const char* path, SpaceH* trial, SpaceH* test);
+
 void mult_noalloc(HOperator& op, int trans, const double* alpha, const void* x, const double* beta, void* y,
                   int nrhs, cudaStream_t s);
 
