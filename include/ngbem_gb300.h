@@ -26,17 +26,26 @@ extern "C" {
 /* kernel ids: reference src/ngbem.hpp:226-434 (LaplaceSL/DL/HS, HelmholtzSL/DL/HS,
  * CombinedField, MaxwellSL).  BEM_HELMHOLTZ_SL_DKAPPA (no counterpart in the reference) is the
  * derivative of the Helmholtz single layer with respect to kappa, kernel i e^{i kappa r}/(4 pi):
- * its operator is the kappa-derivative of the single-layer bilinear form. */
+ * its operator is the kappa-derivative of the single-layer bilinear form.  BEM_MAXWELL_DL is
+ * MaxwellDLKernel<3> (src/ngbem.hpp:475-510): three components e^{i kappa r}(i kappa r - 1)
+ * (x - y)/(4 pi r^3) and six cross-product terms. */
 enum {
   BEM_LAPLACE_SL = 0, BEM_LAPLACE_DL = 1, BEM_LAPLACE_HS = 2,
   BEM_HELMHOLTZ_SL = 3, BEM_HELMHOLTZ_DL = 4, BEM_HELMHOLTZ_HS = 5,
-  BEM_HELMHOLTZ_CF = 6, BEM_MAXWELL_SL = 7, BEM_HELMHOLTZ_SL_DKAPPA = 8
+  BEM_HELMHOLTZ_CF = 6, BEM_MAXWELL_SL = 7, BEM_HELMHOLTZ_SL_DKAPPA = 8, BEM_MAXWELL_DL = 9
 };
-/* trace spaces: SurfaceL2 order 0 (P0), H1 order 1 trace (P1), HDivSurface order 0 (RT0) */
-enum { BEM_P0 = 0, BEM_P1 = 1, BEM_RT0 = 2 };
+/* trace spaces: SurfaceL2 order 0 (P0), H1 order 1 trace (P1), HDivSurface order 0 (RT0),
+ * and the surface trace of HCurl order 0 (HCURL: lowest-order Nedelec on the surface
+ * triangles, one dof per edge like RT0; on each triangle its shape functions are n x the RT0
+ * shape functions of the same edges and signs) */
+enum { BEM_P0 = 0, BEM_P1 = 1, BEM_RT0 = 2, BEM_HCURL = 3 };
 /* trace evaluators: GetEvaluator(BND) (ID), DiffOpBoundaryRot (ROT), DiffOpHelmholtz (HELM),
- * DiffOpMaxwellNew (MAXWELL); reference src/diffops.hpp:12-338 */
-enum { BEM_EV_ID = 0, BEM_EV_ROT = 1, BEM_EV_HELM = 2, BEM_EV_MAXWELL = 3 };
+ * DiffOpMaxwellNew (MAXWELL); reference src/diffops.hpp:12-338.  On BEM_HCURL: ID is the
+ * tangential trace (GetEvaluator(BND) of an HCurl space), ROTATED_TRACE is
+ * DiffOpRotatedTrace (src/diffops.hpp:62-104: n x the shape function) and MAXWELL_CURL is
+ * DiffOpMaxwell (src/diffops.hpp:172-255: [n x shape; surface curl]). */
+enum { BEM_EV_ID = 0, BEM_EV_ROT = 1, BEM_EV_HELM = 2, BEM_EV_MAXWELL = 3,
+       BEM_EV_ROTATED_TRACE = 4, BEM_EV_MAXWELL_CURL = 5 };
 /* precision modes: plain FP64 on the GPU, or mixed (FP64 singular pairs, FP32 regular
  * near field, ACA and factors) */
 enum { BEM_FP64 = 0, BEM_MIXED = 1 };

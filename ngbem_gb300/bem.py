@@ -25,7 +25,7 @@ from . import _lib
 from ._lib import KERNELS, KINDS, EVALS, check, cplx2, lib
 from .meshes import Mesh
 
-__all__ = ["SurfaceL2", "H1", "HDivSurface", "TraceSpace", "BaseMatrix", "HMatrix", "MassMatrix",
+__all__ = ["SurfaceL2", "H1", "HDivSurface", "HCurl", "TraceSpace", "BaseMatrix", "HMatrix", "MassMatrix",
            "IntegralOperator", "IntegralOperatorC",
            "SingleLayerPotentialOperator", "DoubleLayerPotentialOperator", "HypersingularOperator",
            "HelmholtzSingleLayerPotentialOperator", "HelmholtzDoubleLayerPotentialOperator",
@@ -74,7 +74,8 @@ class _MeshHandle:
 
 
 class TraceSpace:
-    """Surface trace space: kind "P0" (SurfaceL2 order 0), "P1" (H1 order 1), "RT0" (HDivSurface order 0)."""
+    """Surface trace space: kind "P0" (SurfaceL2 order 0), "P1" (H1 order 1), "RT0" (HDivSurface order 0),
+    "HCURL" (surface trace of HCurl order 0)."""
 
     def __init__(self, mesh: Mesh, kind: str, dual_mapping: bool = False, complex: bool = False):
         if kind not in KINDS:
@@ -118,6 +119,14 @@ def HDivSurface(mesh: Mesh, order: int = 0, complex: bool = False) -> TraceSpace
     if order != 0:
         raise NotImplementedError("HDivSurface: only order 0 (RT0) is supported")
     return TraceSpace(mesh, "RT0", False, complex)
+
+
+def HCurl(mesh: Mesh, order: int = 0, complex: bool = False) -> TraceSpace:
+    """Surface trace of the lowest-order Nedelec space (NGSolve HCurl order 0 restricted to the
+    boundary): one dof per edge, on each triangle n x the RT0 shape function of that edge."""
+    if order != 0:
+        raise NotImplementedError("HCurl: only order 0 is supported")
+    return TraceSpace(mesh, "HCURL", False, complex)
 
 
 def cluster_tree(space: TraceSpace, leafsize: int = 40):
@@ -612,12 +621,33 @@ def MaxwellSingleLayerPotentialOperator(space, kappa, definedon=None, intorder=3
                             eta, eps, "aca", testhmatrix, **gb)
 
 
-def MaxwellSingleLayerPotentialOperatorCurl(space, kappa, definedon=None, **kw):
-    raise NotImplementedError("MaxwellSingleLayerPotentialOperatorCurl (HCurl traces) is not part of this build")
+def _need_hcurl(space, what):
+    if space.kind != "HCURL":
+        raise TypeError(f"{what} needs an HCurl space, got {space.kind}")
 
 
-def MaxwellDoubleLayerPotentialOperator(trial_space, test_space, kappa, **kw):
-    raise NotImplementedError("MaxwellDoubleLayerPotentialOperator (HCurl rotated traces) is not part of this build")
+def MaxwellSingleLayerPotentialOperatorCurl(space, kappa, definedon=None, intorder=3, leafsize=40, eta=2.,
+                                            eps=1e-6, method="aca", testhmatrix=False, **gb):
+    """Maxwell single layer on HCurl with DiffOpMaxwell traces [n x u; curl u] (reference
+    python_bem.cpp:137-150): kappa <n x u, n x v> - 1/kappa <curl u, curl v> weighted by G."""
+    _no_regions(definedon)
+    _need_hcurl(space, "MaxwellSingleLayerPotentialOperatorCurl")
+    return IntegralOperator("maxwell_sl", _kappa(kappa), space, space, "maxwellcurl", "maxwellcurl", intorder,
+                            leafsize, eta, eps, "aca", testhmatrix, **gb)
+
+
+def MaxwellDoubleLayerPotentialOperator(trial_space, test_space, kappa, trial_definedon=None, test_definedon=None,
+                                        intorder=3, leafsize=40, eta=2., eps=1e-6, method="aca", testhmatrix=False,
+                                        **gb):
+    """Maxwell double layer (reference python_bem.cpp:154-171): MaxwellDLKernel on the rotated
+    trace n x u of the HCurl trial space and the identity trace of the test space (HDivSurface,
+    as in the reference's Maxwell tests, or HCurl).  method "dense" gives one root block."""
+    _no_regions(trial_definedon, test_definedon)
+    _need_hcurl(trial_space, "MaxwellDoubleLayerPotentialOperator (trial space)")
+    if test_space.kind not in ("RT0", "HCURL"):
+        raise TypeError("MaxwellDoubleLayerPotentialOperator: the test space must be HDivSurface or HCurl")
+    return IntegralOperator("maxwell_dl", _kappa(kappa), trial_space, test_space, "rotatedtrace", "id", intorder,
+                            leafsize, eta, eps, method, testhmatrix, **gb)
 
 
 # ----------------------------------------------------------------------------------------

@@ -370,8 +370,9 @@ __global__ void __launch_bounds__(256) aca_project_kernel(ProjArgs a) {
       P rot[3][3], o[3][3];
       for (int x = 0; x < 3; ++x)
         for (int y = 0; y < 3; ++y) { rot[x][y] = Ee.rot[x][y]; o[x][y] = Ee.o[x][y]; }
+      const P nrm[3] = {Ee.n[0], Ee.n[1], Ee.n[2]};
       int sg[3] = {1, 1, 1};
-      if (TET == TR_MAX || TET == TR_RT0ID) { int4 s = a.test.sign[e]; sg[0] = s.x; sg[1] = s.y; sg[2] = s.z; }
+      if (edge_trace(TET)) { int4 s = a.test.sign[e]; sg[0] = s.x; sg[1] = s.y; sg[2] = s.z; }
       V acc[NDI];
 #pragma unroll
       for (int x = 0; x < NDI; ++x) acc[x] = vzero<V>();
@@ -383,7 +384,7 @@ __global__ void __launch_bounds__(256) aca_project_kernel(ProjArgs a) {
         const V u = Us[(size_t)kk * M + ie * nq + q] * qo.w;
 #pragma unroll
         for (int x = 0; x < NDI; ++x)
-          acc[x] += u * trace_val<TET, P>(x, G::tec(t), rp.x, rp.y, xp, Ee.invdetJ, rot, sg[x], a.test.dual != 0);
+          acc[x] += u * trace_val<TET, P>(x, G::tec(t), rp.x, rp.y, xp, Ee.invdetJ, rot, sg[x], a.test.dual != 0, nrm);
       }
       const int4 dn = a.test.dofs[e];
 #pragma unroll
@@ -399,8 +400,9 @@ __global__ void __launch_bounds__(256) aca_project_kernel(ProjArgs a) {
       P rot[3][3], o[3][3];
       for (int x = 0; x < 3; ++x)
         for (int y = 0; y < 3; ++y) { rot[x][y] = Ee.rot[x][y]; o[x][y] = Ee.o[x][y]; }
+      const P nrm[3] = {Ee.n[0], Ee.n[1], Ee.n[2]};
       int sg[3] = {1, 1, 1};
-      if (TRT == TR_MAX || TRT == TR_RT0ID) { int4 s = a.trial.sign[e]; sg[0] = s.x; sg[1] = s.y; sg[2] = s.z; }
+      if (edge_trace(TRT)) { int4 s = a.trial.sign[e]; sg[0] = s.x; sg[1] = s.y; sg[2] = s.z; }
       V acc[NDJ];
 #pragma unroll
       for (int x = 0; x < NDJ; ++x) acc[x] = vzero<V>();
@@ -412,7 +414,7 @@ __global__ void __launch_bounds__(256) aca_project_kernel(ProjArgs a) {
         const V v = Vs[(size_t)kk * N + je * nq + q] * qo.w;
 #pragma unroll
         for (int x = 0; x < NDJ; ++x)
-          acc[x] += v * trace_val<TRT, P>(x, G::trc(t), rp.x, rp.y, xp, Ee.invdetJ, rot, sg[x], a.trial.dual != 0);
+          acc[x] += v * trace_val<TRT, P>(x, G::trc(t), rp.x, rp.y, xp, Ee.invdetJ, rot, sg[x], a.trial.dual != 0, nrm);
       }
       const int4 dn = a.trial.dofs[e];
 #pragma unroll
@@ -460,6 +462,7 @@ void launch_aca(int kid, int prec, const AcaArgs& a, cudaStream_t s) {
   }
   X(K_LAPLACE_SL) X(K_LAPLACE_DL) X(K_LAPLACE_HS) X(K_HELMHOLTZ_SL) X(K_HELMHOLTZ_DL)
   X(K_HELMHOLTZ_HS) X(K_HELMHOLTZ_CF) X(K_MAXWELL_SL) X(K_HELMHOLTZ_SL_DKAPPA)
+  X(K_MAXWELL_DL)
 #undef X
   join();
 }
@@ -479,7 +482,8 @@ void launch_aca(int kid, int prec, const AcaArgs& a, cudaStream_t s) {
   X(K_HELMHOLTZ_CF, TR_P0, TR_P0) X(K_HELMHOLTZ_CF, TR_P1, TR_P1)                     \
   X(K_HELMHOLTZ_CF, TR_P1, TR_P0) X(K_HELMHOLTZ_CF, TR_P0, TR_P1)                     \
   X(K_HELMHOLTZ_HS, TR_HELM, TR_HELM)                                                 \
-  X(K_MAXWELL_SL, TR_MAX, TR_MAX)
+  X(K_MAXWELL_SL, TR_MAX, TR_MAX) X(K_MAXWELL_SL, TR_NEDMAX, TR_NEDMAX)                \
+  X(K_MAXWELL_DL, TR_NEDROT, TR_NED) X(K_MAXWELL_DL, TR_NEDROT, TR_RT0ID)
 
 void launch_projection(int kid, int prec, int trt, int tet, const ProjArgs& a, cudaStream_t s) {
   if (a.nfar <= 0) return;

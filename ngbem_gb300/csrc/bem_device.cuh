@@ -248,10 +248,35 @@ template <> struct Green<K_HELMHOLTZ_HS> {
   }
 };
 
+// Maxwell double layer (reference MaxwellDLKernel<3>, src/ngbem.hpp:475-510): the gradient
+// e^{ikr}/(4 pi r^3) (i k r - 1)(x - y) in three components, applied as the cross product
+// test . (grad x trial) through six terms of factor +-1
+template <> struct Green<K_MAXWELL_DL> {
+  static constexpr bool CPLX = true; static constexpr int NC = 3; static constexpr int NT = 6;
+  static constexpr bool NEEDS_NX = false, NEEDS_NY = false;
+  __host__ __device__ static constexpr int kc(int t) { return t >> 1; }
+  __host__ __device__ static constexpr int trc(int t) { return t == 0 ? 1 : (t == 1 ? 2 : (t == 2 ? 2 : (t == 3 ? 0 : (t == 4 ? 0 : 1)))); }
+  __host__ __device__ static constexpr int tec(int t) { return t == 0 ? 2 : (t == 1 ? 1 : (t == 2 ? 0 : (t == 3 ? 2 : (t == 4 ? 1 : 0)))); }
+  __host__ __device__ static constexpr int fk(int t) { return (t & 1) ? 3 : 0; }
+  template <class R>
+  __device__ static __forceinline__ void eval(R dx, R dy, R dz, const R*, const R*, R kappa, cpx<R>* out) {
+    R r2 = dx * dx + dy * dy + dz * dz;
+    R ir = rsqrt_(r2);
+    R r = r2 * ir;
+    R s, c;
+    sincos_(kappa * r, &s, &c);
+    R f = (ir * ir * ir) * R(BEM_INV4PI);
+    const cpx<R> g = mkc(c * f, s * f) * mkc(R(-1), kappa * r);
+    out[0] = g * dx;
+    out[1] = g * dy;
+    out[2] = g * dz;
+  }
+};
+
 template <class G, class R>
 __device__ __forceinline__ R term_fac(int t, R kappa) {
   int k = G::fk(t);
-  return k == 0 ? R(1) : (k == 1 ? kappa : R(-1) / kappa);
+  return k == 0 ? R(1) : (k == 1 ? kappa : (k == 3 ? R(-1) : R(-1) / kappa));
 }
 
 // ----------------------------------------------------------------------------------------
@@ -272,11 +297,14 @@ template <> struct TraceInfo<TR_ROT> { static constexpr int ND = 3, DIM = 3; };
 template <> struct TraceInfo<TR_HELM> { static constexpr int ND = 3, DIM = 4; };
 template <> struct TraceInfo<TR_MAX> { static constexpr int ND = 3, DIM = 4; };
 template <> struct TraceInfo<TR_RT0ID> { static constexpr int ND = 3, DIM = 3; };
+template <> struct TraceInfo<TR_NED> { static constexpr int ND = 3, DIM = 3; };
+template <> struct TraceInfo<TR_NEDROT> { static constexpr int ND = 3, DIM = 3; };
+template <> struct TraceInfo<TR_NEDMAX> { static constexpr int ND = 3, DIM = 4; };
 
-// value of trace component c of local dof a
+// value of trace component c of local dof a (nrm: the element's unit normal, read by TR_NED)
 template <int TR, class R>
 __device__ __forceinline__ R trace_val(int a, int c, R xi, R eta, const R (*xp)[3], R invdetJ,
-                                       const R (*rot)[3], int sgn, bool dual) {
+                                       const R (*rot)[3], int sgn, bool dual, const R* nrm) {
   if (TR == TR_P0) return dual ? invdetJ : R(1);
   if (TR == TR_P1) return a == 0 ? xi : (a == 1 ? eta : R(1) - xi - eta);
   if (TR == TR_ROT) return rot[a][c];
@@ -284,12 +312,17 @@ __device__ __forceinline__ R trace_val(int a, int c, R xi, R eta, const R (*xp)[
     if (c < 3) return rot[a][c];
     return a == 0 ? xi : (a == 1 ? eta : R(1) - xi - eta);
   }
-  // MAX and RT0ID
-  if (c < 3) {
-    int o = (a + 2) % 3;
-    return R(sgn) * xp[o][c] * invdetJ;
+  // edge dofs: the RT0 shape sgn (x - p_o) / |J| (o the vertex opposite the edge)
+  const int o = (a + 2) % 3;
+  if (TR == TR_NED) {  // n x RT0 shape
+    const int c1 = (c + 1) % 3, c2 = (c + 2) % 3;
+    return R(sgn) * (nrm[c1] * xp[o][c2] - nrm[c2] * xp[o][c1]) * invdetJ;
   }
-  return R(2 * sgn) * invdetJ;
+  if (c < 3) {
+    const R v = R(sgn) * xp[o][c] * invdetJ;
+    return (TR == TR_NEDROT || TR == TR_NEDMAX) ? -v : v;
+  }
+  return R(2 * sgn) * invdetJ;  // surface divergence (RT0) = surface curl (Nedelec)
 }
 
 // ----------------------------------------------------------------------------------------

@@ -8,11 +8,21 @@ enum KernelId {
   K_LAPLACE_SL = 0, K_LAPLACE_DL = 1, K_LAPLACE_HS = 2, K_HELMHOLTZ_SL = 3,
   K_HELMHOLTZ_DL = 4, K_HELMHOLTZ_HS = 5, K_HELMHOLTZ_CF = 6, K_MAXWELL_SL = 7,
   K_HELMHOLTZ_SL_DKAPPA = 8,  // d/dkappa of the Helmholtz single layer (no counterpart in the reference)
-  K_NUM = 9
+  K_MAXWELL_DL = 9,
+  K_NUM = 10
 };
 
 // trace kinds = (space kind, evaluator) combinations the operators use
-enum TraceKind { TR_P0 = 0, TR_P1 = 1, TR_ROT = 2, TR_HELM = 3, TR_MAX = 4, TR_RT0ID = 5 };
+// TR_NED, TR_NEDROT, TR_NEDMAX: the HCurl (lowest-order Nedelec) traces of the edge dofs:
+// the tangential shape n x phi_RT0, the rotated trace n x (n x phi_RT0) = -phi_RT0, and the
+// Maxwell trace [-phi_RT0; surface curl] (reference DiffOpRotatedTrace, DiffOpMaxwell,
+// src/diffops.hpp:62-255, for the Whitney edge shapes, which are n x the RT0 shapes)
+enum TraceKind { TR_P0 = 0, TR_P1 = 1, TR_ROT = 2, TR_HELM = 3, TR_MAX = 4, TR_RT0ID = 5,
+                 TR_NED = 6, TR_NEDROT = 7, TR_NEDMAX = 8 };
+// traces whose local dofs carry an edge orientation sign
+__host__ __device__ constexpr bool edge_trace(int tr) {
+  return tr == TR_MAX || tr == TR_RT0ID || tr == TR_NED || tr == TR_NEDROT || tr == TR_NEDMAX;
+}
 
 // Per-element record (FP64): vertices, unit normal, |J|, rotated surface gradients of the
 // P1 hat functions (n x grad lambda_a), vertex ids.  128 bytes + 64 bytes, read by the

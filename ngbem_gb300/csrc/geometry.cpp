@@ -206,7 +206,7 @@ void SpaceH::build(MeshH* m, int kind_, int dual_) {
     nd = 3;
     ndof = m->nv;
     dofs = m->T;
-  } else if (kind == BEM_RT0) {
+  } else if (kind == BEM_RT0 || kind == BEM_HCURL) {
     nd = 3;
     ndof = m->ne;
     dofs = m->TE;
@@ -251,6 +251,12 @@ int trace_kind(int space_kind, int ev) {
   if (space_kind == BEM_RT0) {
     if (ev == BEM_EV_MAXWELL) return TR_MAX;
     if (ev == BEM_EV_ID) return TR_RT0ID;
+    return -1;
+  }
+  if (space_kind == BEM_HCURL) {
+    if (ev == BEM_EV_ID) return TR_NED;
+    if (ev == BEM_EV_ROTATED_TRACE) return TR_NEDROT;
+    if (ev == BEM_EV_MAXWELL_CURL) return TR_NEDMAX;
     return -1;
   }
   return -1;

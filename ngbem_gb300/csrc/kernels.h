@@ -88,6 +88,8 @@ void launch_nf_singular(int kid, int prec, int trt, int tet, const NFArgs& a, cu
 void launch_aca(int kid, int prec, const AcaArgs& a, cudaStream_t s);
 void launch_projection(int kid, int prec, int trt, int tet, const ProjArgs& a, cudaStream_t s);
 int kernel_ncomp(int kid);
+int kernel_nterms(int kid);          // kernel terms (factor, component, trial, test)
+int kernel_term_comp(int kid, int t);  // the kernel component term t reads
 bool kernel_complex(int kid);
 
 // ---- matvec -----------------------------------------------------------------------------

@@ -70,21 +70,21 @@ __global__ void __launch_bounds__(128) nf_regular_kernel(NFArgs a) {
 #pragma unroll
       for (int c = 0; c < 3; ++c) rotj[r][c] = Ej.rot[r][c];
   }
-  if (TET == TR_MAX || TET == TR_RT0ID) {
+  if (edge_trace(TET)) {
 #pragma unroll
     for (int r = 0; r < 3; ++r)
 #pragma unroll
       for (int c = 0; c < 3; ++c) oi[r][c] = Ei.o[r][c];
   }
-  if (TRT == TR_MAX || TRT == TR_RT0ID) {
+  if (edge_trace(TRT)) {
 #pragma unroll
     for (int r = 0; r < 3; ++r)
 #pragma unroll
       for (int c = 0; c < 3; ++c) oj[r][c] = Ej.o[r][c];
   }
   int sgi[3] = {1, 1, 1}, sgj[3] = {1, 1, 1};
-  if (TET == TR_MAX || TET == TR_RT0ID) { int4 s = a.test.sign[ei]; sgi[0] = s.x; sgi[1] = s.y; sgi[2] = s.z; }
-  if (TRT == TR_MAX || TRT == TR_RT0ID) { int4 s = a.trial.sign[ej]; sgj[0] = s.x; sgj[1] = s.y; sgj[2] = s.z; }
+  if (edge_trace(TET)) { int4 s = a.test.sign[ei]; sgi[0] = s.x; sgi[1] = s.y; sgi[2] = s.z; }
+  if (edge_trace(TRT)) { int4 s = a.trial.sign[ej]; sgj[0] = s.x; sgj[1] = s.y; sgj[2] = s.z; }
   const bool duali = a.test.dual != 0, dualj = a.trial.dual != 0;
   const P kappa = (P)a.kappa;
 
@@ -101,7 +101,7 @@ __global__ void __launch_bounds__(128) nf_regular_kernel(NFArgs a) {
     const QPt<P> qi = Qi[p];
     const P2<P> rp = RQ[p];
     P xpi[3][3];
-    if (TET == TR_MAX || TET == TR_RT0ID) {
+    if (edge_trace(TET)) {
 #pragma unroll
       for (int r = 0; r < 3; ++r) { xpi[r][0] = qi.x - oi[r][0]; xpi[r][1] = qi.y - oi[r][1]; xpi[r][2] = qi.z - oi[r][2]; }
     }
@@ -118,7 +118,7 @@ __global__ void __launch_bounds__(128) nf_regular_kernel(NFArgs a) {
       const P w = qi.w * qj.w;
       P xpj[3][3];
       const P2<P> rqq = RQ[q];
-      if (TRT == TR_MAX || TRT == TR_RT0ID) {
+      if (edge_trace(TRT)) {
 #pragma unroll
         for (int r = 0; r < 3; ++r) { xpj[r][0] = qj.x - oj[r][0]; xpj[r][1] = qj.y - oj[r][1]; xpj[r][2] = qj.z - oj[r][2]; }
       }
@@ -127,7 +127,7 @@ __global__ void __launch_bounds__(128) nf_regular_kernel(NFArgs a) {
         const V kw = kv[G::kc(t)] * w;
 #pragma unroll
         for (int b = 0; b < NDJ; ++b) {
-          P s = trace_val<TRT, P>(b, G::trc(t), rqq.x, rqq.y, xpj, invj, rotj, sgj[b], dualj);
+          P s = trace_val<TRT, P>(b, G::trc(t), rqq.x, rqq.y, xpj, invj, rotj, sgj[b], dualj, ny);
           ks[t][b] += kw * s;
         }
       }
@@ -137,7 +137,7 @@ __global__ void __launch_bounds__(128) nf_regular_kernel(NFArgs a) {
       const P fac = term_fac<G, P>(t, kappa);
 #pragma unroll
       for (int r = 0; r < NDI; ++r) {
-        P s = fac * trace_val<TET, P>(r, G::tec(t), rp.x, rp.y, xpi, invi, roti, sgi[r], duali);
+        P s = fac * trace_val<TET, P>(r, G::tec(t), rp.x, rp.y, xpi, invi, roti, sgi[r], duali, nx);
 #pragma unroll
         for (int b = 0; b < NDJ; ++b) elmat[r][b] += ks[t][b] * s;
       }
@@ -242,8 +242,8 @@ __global__ void __launch_bounds__(256) nf_singular_kernel(NFArgs a) {
     const double detJ2 = Ei.detJ * Ej.detJ;
     const double invi = Ei.invdetJ, invj = Ej.invdetJ;
     int sgi[3] = {1, 1, 1}, sgj[3] = {1, 1, 1};
-    if (TET == TR_MAX || TET == TR_RT0ID) { int4 g = a.test.sign[s.ei]; sgi[0] = g.x; sgi[1] = g.y; sgi[2] = g.z; }
-    if (TRT == TR_MAX || TRT == TR_RT0ID) { int4 g = a.trial.sign[s.ej]; sgj[0] = g.x; sgj[1] = g.y; sgj[2] = g.z; }
+    if (edge_trace(TET)) { int4 g = a.test.sign[s.ei]; sgi[0] = g.x; sgi[1] = g.y; sgi[2] = g.z; }
+    if (edge_trace(TRT)) { int4 g = a.trial.sign[s.ej]; sgj[0] = g.x; sgj[1] = g.y; sgj[2] = g.z; }
 
     V acc[NDI][NDJ];
 #pragma unroll
@@ -278,13 +278,13 @@ __global__ void __launch_bounds__(256) nf_singular_kernel(NFArgs a) {
       G::eval(x[0] - y[0], x[1] - y[1], x[2] - y[2], nx, ny, kappa, kv);
       const double fac = detJ2 * w;
       double xpi[3][3], xpj[3][3];
-      if (TET == TR_MAX || TET == TR_RT0ID) {
+      if (edge_trace(TET)) {
 #pragma unroll
         for (int r = 0; r < 3; ++r)
 #pragma unroll
           for (int c = 0; c < 3; ++c) xpi[r][c] = x[c] - pi[r][c];
       }
-      if (TRT == TR_MAX || TRT == TR_RT0ID) {
+      if (edge_trace(TRT)) {
 #pragma unroll
         for (int r = 0; r < 3; ++r)
 #pragma unroll
@@ -295,10 +295,10 @@ __global__ void __launch_bounds__(256) nf_singular_kernel(NFArgs a) {
         const V kf = kv[G::kc(t)] * (fac * term_fac<G, double>(t, kappa));
 #pragma unroll
         for (int r = 0; r < NDI; ++r) {
-          const V ka = kf * trace_val<TET, double>(r, G::tec(t), xi, xe, xpi, invi, roti, sgi[r], duali);
+          const V ka = kf * trace_val<TET, double>(r, G::tec(t), xi, xe, xpi, invi, roti, sgi[r], duali, nx);
 #pragma unroll
           for (int c = 0; c < NDJ; ++c)
-            acc[r][c] += ka * trace_val<TRT, double>(c, G::trc(t), yi, ye, xpj, invj, rotj, sgj[c], dualj);
+            acc[r][c] += ka * trace_val<TRT, double>(c, G::trc(t), yi, ye, xpj, invj, rotj, sgj[c], dualj, ny);
         }
       }
     }
@@ -346,7 +346,8 @@ __global__ void __launch_bounds__(256) nf_singular_kernel(NFArgs a) {
   X(K_HELMHOLTZ_CF, TR_P0, TR_P0) X(K_HELMHOLTZ_CF, TR_P1, TR_P1)                     \
   X(K_HELMHOLTZ_CF, TR_P1, TR_P0) X(K_HELMHOLTZ_CF, TR_P0, TR_P1)                     \
   X(K_HELMHOLTZ_HS, TR_HELM, TR_HELM)                                                 \
-  X(K_MAXWELL_SL, TR_MAX, TR_MAX)
+  X(K_MAXWELL_SL, TR_MAX, TR_MAX) X(K_MAXWELL_SL, TR_NEDMAX, TR_NEDMAX)                \
+  X(K_MAXWELL_DL, TR_NEDROT, TR_NED) X(K_MAXWELL_DL, TR_NEDROT, TR_RT0ID)
 
 bool nf_combo_supported(int kid, int trt, int tet) {
 #define X(K, A, B) if (kid == K && trt == A && tet == B) return true;
@@ -386,7 +387,28 @@ void launch_nf_singular(int kid, int prec, int trt, int tet, const NFArgs& a, cu
 #undef X
 }
 
-int kernel_ncomp(int kid) { return kid == K_HELMHOLTZ_HS ? 2 : 1; }
+#define BEM_ALL_KERNELS(X)                                                                     \
+  X(K_LAPLACE_SL) X(K_LAPLACE_DL) X(K_LAPLACE_HS) X(K_HELMHOLTZ_SL) X(K_HELMHOLTZ_DL)          \
+  X(K_HELMHOLTZ_HS) X(K_HELMHOLTZ_CF) X(K_MAXWELL_SL) X(K_HELMHOLTZ_SL_DKAPPA) X(K_MAXWELL_DL)
+
+int kernel_ncomp(int kid) {
+#define X(K) if (kid == K) return Green<K>::NC;
+  BEM_ALL_KERNELS(X)
+#undef X
+  return 1;
+}
+int kernel_nterms(int kid) {
+#define X(K) if (kid == K) return Green<K>::NT;
+  BEM_ALL_KERNELS(X)
+#undef X
+  return 1;
+}
+int kernel_term_comp(int kid, int t) {
+#define X(K) if (kid == K) return Green<K>::kc(t);
+  BEM_ALL_KERNELS(X)
+#undef X
+  return 0;
+}
 bool kernel_complex(int kid) { return kid >= K_HELMHOLTZ_SL; }
 
 }  // namespace bem

@@ -395,11 +395,7 @@ void HOperator::assemble() {
         continue;
       }
       int R = 0;
-      const int nt = (kid == K_LAPLACE_HS) ? 3 : ((kid == K_HELMHOLTZ_HS || kid == K_MAXWELL_SL) ? 4 : 1);
-      for (int tt = 0; tt < nt; ++tt) {
-        const int kc = (kid == K_HELMHOLTZ_HS && tt == 3) ? 1 : 0;
-        R += ranks[(size_t)f * NC + kc];
-      }
+      for (int tt = 0; tt < kernel_nterms(kid); ++tt) R += ranks[(size_t)f * NC + kernel_term_comp(kid, tt)];
       for (int c = 0; c < NC; ++c) pranks[(size_t)f * NC + c] = ranks[(size_t)f * NC + c];
       L.R = R;
       L.cu = chunk_len(L.m, R);
@@ -1235,7 +1231,11 @@ void MassOperator::build(SpaceH* trial, SpaceH* test, bool complex_vectors) {
     m.map(e, xi, eta, x);
     for (int a = 0; a < 3; ++a) {
       const int o = (a + 2) % 3;
-      for (int c = 0; c < 3; ++c) S[a][c] = sp.sign[3 * e + a] * (x[c] - g.p[o][c]) * g.invdetJ;
+      double v[3];
+      for (int c = 0; c < 3; ++c) v[c] = sp.sign[3 * e + a] * (x[c] - g.p[o][c]) * g.invdetJ;
+      // HCurl trace: n x the RT0 shape of the same edge
+      for (int c = 0; c < 3; ++c)
+        S[a][c] = sp.kind == BEM_HCURL ? g.n[(c + 1) % 3] * v[(c + 2) % 3] - g.n[(c + 2) % 3] * v[(c + 1) % 3] : v[c];
     }
     dim = 3;
   };

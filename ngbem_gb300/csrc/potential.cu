@@ -39,8 +39,9 @@ __global__ void pot_sources_kernel(PotArgs a) {
         rot[x][y] = Ee.rot[x][y];
         xp[x][y] = (y == 0 ? qo.x : (y == 1 ? qo.y : qo.z)) - Ee.o[x][y];
       }
+    const double nrm[3] = {Ee.n[0], Ee.n[1], Ee.n[2]};
     int sg[3] = {1, 1, 1};
-    if (TRT == TR_MAX || TRT == TR_RT0ID) {
+    if (edge_trace(TRT)) {
       const int4 s = a.trial.sign[e];
       sg[0] = s.x;
       sg[1] = s.y;
@@ -57,7 +58,7 @@ __global__ void pot_sources_kernel(PotArgs a) {
 #pragma unroll
       for (int c = 0; c < DIM; ++c)
         val[c] += dv * trace_val<TRT, double>(x, c, RQ[2 * q], RQ[2 * q + 1], xp, Ee.invdetJ, rot, sg[x],
-                                               a.trial.dual != 0);
+                                               a.trial.dual != 0, nrm);
     }
     double* py = a.src_pos + 6 * t;
     py[0] = Ee.chi[0] + Ee.clo[0] + qo.x;

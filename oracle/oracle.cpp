@@ -256,9 +256,9 @@ struct Space {
 };
 
 static int trace_dim(int kind, int ev) {
-  if (ev == ORC_EV_ID) return kind == ORC_RT0 ? 3 : 1;
-  if (ev == ORC_EV_ROT) return 3;
-  return 4;  // HELM, MAXWELL
+  if (ev == ORC_EV_ID) return (kind == ORC_RT0 || kind == ORC_HCURL) ? 3 : 1;
+  if (ev == ORC_EV_ROT || ev == ORC_EV_ROTATED_TRACE) return 3;
+  return 4;  // HELM, MAXWELL, MAXWELL_CURL
 }
 
 static void cross3(const double* a, const double* b, double* c) {
@@ -272,6 +272,9 @@ static void cross3(const double* a, const double* b, double* c) {
 // (reference DiffOpBoundaryRot, src/diffops.hpp:12-57); HELM: [n x grad; value]
 // (DiffOpHelmholtz :110-165); MAXWELL: [Piola shape; surface div] (DiffOpMaxwellNew
 // :263-338) with RT0 shapes sigma*(xhat - vhat_opposite) on the reference triangle.
+// HCURL: shape phi = n x psi (psi the RT0 shape of the same edge and sign); ID is phi,
+// ROTATED_TRACE n x phi (DiffOpRotatedTrace :62-104), MAXWELL_CURL [n x phi; curl phi]
+// (DiffOpMaxwell :172-255) with the surface curl of phi = div psi = 2 sigma / |J|.
 static void eval_trace(const Mesh& m, const Space& sp, int ev, int e, double xi, double eta,
                        double S[3][4]) {
   const Geo& g = m.geo[e];
@@ -308,7 +311,19 @@ static void eval_trace(const Mesh& m, const Space& sp, int ev, int e, double xi,
     double sg = sp.sign[3 * e + k];
     double ph0 = sg * (xi - vh[o][0]), ph1 = sg * (eta - vh[o][1]);
     for (int c = 0; c < 3; ++c) S[k][c] = (g.J0[c] * ph0 + g.J1[c] * ph1) / g.detJ;
-    if (ev == ORC_EV_MAXWELL) S[k][3] = 2.0 * sg / g.detJ;
+    if (sp.kind == ORC_RT0) {
+      if (ev == ORC_EV_MAXWELL) S[k][3] = 2.0 * sg / g.detJ;
+      continue;
+    }
+    double phi[3], rot[3];
+    cross3(g.n, S[k], phi);
+    if (ev == ORC_EV_ID) {
+      for (int c = 0; c < 3; ++c) S[k][c] = phi[c];
+    } else {
+      cross3(g.n, phi, rot);
+      for (int c = 0; c < 3; ++c) S[k][c] = rot[c];
+      if (ev == ORC_EV_MAXWELL_CURL) S[k][3] = 2.0 * sg / g.detJ;
+    }
   }
 }
 
@@ -321,7 +336,7 @@ struct Kernel {
   std::vector<Term> terms;
   Kernel(int id_, double kappa_) : id(id_), kappa(kappa_) {
     complex_valued = id >= ORC_HELMHOLTZ_SL;
-    ncomp = (id == ORC_HELMHOLTZ_HS) ? 2 : 1;
+    ncomp = (id == ORC_HELMHOLTZ_HS) ? 2 : (id == ORC_MAXWELL_DL ? 3 : 1);
     switch (id) {
       case ORC_LAPLACE_HS:
         terms = {{1.0, 0, 0, 0}, {1.0, 0, 1, 1}, {1.0, 0, 2, 2}};
@@ -332,6 +347,9 @@ struct Kernel {
       case ORC_MAXWELL_SL:
         for (int i = 0; i < 3; ++i) terms.push_back({kappa, 0, i, i});
         terms.push_back({-1.0 / kappa, 0, 3, 3});
+        break;
+      case ORC_MAXWELL_DL:  // {factor, component, trial, test}: the cross product of curl
+        terms = {{1.0, 0, 1, 2}, {-1.0, 0, 2, 1}, {1.0, 1, 2, 0}, {-1.0, 1, 0, 2}, {1.0, 2, 0, 1}, {-1.0, 2, 1, 0}};
         break;
       default:
         terms = {{1.0, 0, 0, 0}};
@@ -383,6 +401,11 @@ void Kernel::eval<cplx>(const double* x, const double* y, const double* nx, cons
     case ORC_HELMHOLTZ_SL_DKAPPA:
       out[0] = cplx(0.0, 1.0) * ex / (4 * PI);
       break;
+    case ORC_MAXWELL_DL: {
+      const cplx g = ex / (4 * PI * norm * norm * norm) * (cplx(0.0, kappa) * norm - 1.0);
+      for (int c = 0; c < 3; ++c) out[c] = g * d[c];
+      break;
+    }
     default:  // HELMHOLTZ_SL, MAXWELL_SL
       out[0] = ex / (4 * PI * norm);
   }
@@ -661,7 +684,7 @@ struct Operator {
       double x[3], y[3];
       mesh.map(ei, xi, xe, x);
       mesh.map(ej, yi, ye, y);
-      T kv[2];
+      T kv[3];
       kernel.eval<T>(x, y, gi.n, gj.n, kv);
       double fac = gi.detJ * gj.detJ * r.w[k];
       for (int c = 0; c < kernel.ncomp; ++c) kv[c] = fac * kv[c];
@@ -764,7 +787,7 @@ struct Operator {
               for (int iy = 0; iy < nq; ++iy) {
                 const double* X = &pxi[(i * nq + ix) * 4];
                 const double* Y = &pyj[(j * nq + iy) * 4];
-                T kv[2];
+                T kv[3];
                 kernel.eval<T>(X, Y, nx, ny, kv);
                 double fac = X[3] * Y[3];
                 kern[ix * nq + iy] = t.fac * fac * kv[t.kc];
@@ -833,11 +856,11 @@ struct Operator {
       }
     const size_t p = std::min(M, N);
     auto getrow = [&](size_t i, T* row, int comp) {
-      T kv[2];
+      T kv[3];
       for (size_t j = 0; j < N; ++j) { kernel.eval<T>(&xi[3 * i], &yj[3 * j], &nxi[3 * i], &nyj[3 * j], kv); row[j] = kv[comp]; }
     };
     auto getcol = [&](size_t j, T* col, int comp) {
-      T kv[2];
+      T kv[3];
       for (size_t i = 0; i < M; ++i) { kernel.eval<T>(&xi[3 * i], &yj[3 * j], &nxi[3 * i], &nyj[3 * j], kv); col[i] = kv[comp]; }
     };
     int ncomp = 0;
@@ -1274,7 +1297,7 @@ static void potential_t(int kernel, double kappa, const Mesh& m, const Space& sp
         double y[3];
         m.map(e, r.xi[q], r.eta[q], y);
         const double w = r.w[q] * m.geo[e].detJ;
-        T kv[2];
+        T kv[3];
         K.eval<T>(x, y, nx, m.geo[e].n, kv);
         for (const Term& t : K.terms) out[(size_t)p * dim + t.tec] += w * kv[t.kc] * vals[t.trc];
       }

@@ -34,12 +34,17 @@ enum {
   ORC_HELMHOLTZ_CF = 6, ORC_MAXWELL_SL = 7,
   // d/dkappa of the Helmholtz single layer, i e^{i kappa r}/(4 pi): no counterpart in the
   // reference (which has no derivatives); pinned by central differences of ORC_HELMHOLTZ_SL
-  ORC_HELMHOLTZ_SL_DKAPPA = 8
+  ORC_HELMHOLTZ_SL_DKAPPA = 8,
+  // MaxwellDLKernel<3>, src/ngbem.hpp:475-510
+  ORC_MAXWELL_DL = 9
 };
 // space kinds
-enum { ORC_P0 = 0, ORC_P1 = 1, ORC_RT0 = 2 };
-// trace evaluators
-enum { ORC_EV_ID = 0, ORC_EV_ROT = 1, ORC_EV_HELM = 2, ORC_EV_MAXWELL = 3 };
+// (ORC_HCURL: surface Nedelec order 0, shape n x the RT0 shape of the same edge and sign)
+enum { ORC_P0 = 0, ORC_P1 = 1, ORC_RT0 = 2, ORC_HCURL = 3 };
+// trace evaluators; on ORC_HCURL: ID the tangential trace, ROTATED_TRACE DiffOpRotatedTrace,
+// MAXWELL_CURL DiffOpMaxwell
+enum { ORC_EV_ID = 0, ORC_EV_ROT = 1, ORC_EV_HELM = 2, ORC_EV_MAXWELL = 3,
+       ORC_EV_ROTATED_TRACE = 4, ORC_EV_MAXWELL_CURL = 5 };
 
 typedef struct {
   int intorder_singular;   // Sauter-Schwab rules (reference: param.intorder)

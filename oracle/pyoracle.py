@@ -16,9 +16,9 @@ _LIB = None
 
 KERNELS = {"laplace_sl": 0, "laplace_dl": 1, "laplace_hs": 2, "helmholtz_sl": 3,
            "helmholtz_dl": 4, "helmholtz_hs": 5, "helmholtz_cf": 6, "maxwell_sl": 7,
-           "helmholtz_sl_dkappa": 8}
-KINDS = {"P0": 0, "P1": 1, "RT0": 2}
-EVALS = {"id": 0, "rot": 1, "helm": 2, "maxwell": 3}
+           "helmholtz_sl_dkappa": 8, "maxwell_dl": 9}
+KINDS = {"P0": 0, "P1": 1, "RT0": 2, "HCURL": 3}
+EVALS = {"id": 0, "rot": 1, "helm": 2, "maxwell": 3, "rotatedtrace": 4, "maxwellcurl": 5}
 
 
 class Params(C.Structure):
@@ -204,7 +204,10 @@ def potential(kernel, mesh, trial, density, points, normals=None, kappa=0.0, tri
     dens = np.ascontiguousarray(density, dtype=np.complex128 if cplx else np.float64)
     P = np.ascontiguousarray(points, dtype=np.float64).reshape(-1, 3)
     Nn = None if normals is None else np.ascontiguousarray(normals, dtype=np.float64).reshape(-1, 3)
-    dim = 3 if (trial == "RT0" and trial_eval == "id") else (1 if trial_eval == "id" else (3 if trial_eval == "rot" else 4))
+    if trial_eval == "id":
+        dim = 3 if trial in ("RT0", "HCURL") else 1
+    else:
+        dim = 3 if trial_eval in ("rot", "rotatedtrace") else 4
     out = np.zeros((P.shape[0], dim), dtype=dens.dtype)
     lib().orc_potential(KERNELS[kernel], float(kappa), mesh.nv, _dp(X), mesh.nt, _ip(T), KINDS[trial],
                         EVALS[trial_eval], int(trial_dual), int(intorder), _dp(dens.view(np.float64)), P.shape[0],

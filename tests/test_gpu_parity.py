@@ -27,6 +27,9 @@ CASES = [
     ("helmholtz_hs", "P1", "P1", "helm", "helm", 3.0),
     ("maxwell_sl", "RT0", "RT0", "maxwell", "maxwell", 2.0),
     ("helmholtz_sl_dkappa", "P1", "P0", "id", "id", 3.0),
+    ("maxwell_dl", "HCURL", "RT0", "rotatedtrace", "id", 2.0),
+    ("maxwell_dl", "HCURL", "HCURL", "rotatedtrace", "id", 2.0),
+    ("maxwell_sl", "HCURL", "HCURL", "maxwellcurl", "maxwellcurl", 2.0),
 ]
 
 
