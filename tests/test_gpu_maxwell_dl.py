@@ -30,7 +30,7 @@ def test_calderon_identity_hmatrix(oracle, precision):
     kw = dict(intorder=3, leafsize=20, eps=1e-6, precision=precision)
     V = nb.MaxwellSingleLayerPotentialOperator(RT, kappa, **kw)
     K = nb.MaxwellDoubleLayerPotentialOperator(HC, RT, kappa, **kw)
-    assert K.mat.height == RT.ndof and K.mat.width == HC.ndof and K.mat.info["n_lowrank"] > 0
+    assert K.mat.height == RT.ndof and K.mat.width == HC.ndof and K.mat.info["nfar"] > 0 and K.mat.info["sum_rank"] > 0
     mh, jh, M = traces(oracle, m, kappa)
     Mg = nb.MassOperator(HC, RT, complex=True)
     Mm = (Mg * torch.from_numpy(mh).cuda()).cpu().numpy()
