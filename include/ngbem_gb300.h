@@ -105,6 +105,16 @@ int bem_mesh_destroy(bem_mesh_t mesh);
  * reference src/python_bem.cpp:27-173).  RT0 dofs are edges numbered by first
  * appearance (element order, local edges (0,1),(1,2),(2,0)). */
 int bem_space_create(bem_mesh_t mesh, int kind, int dual_mapping, bem_space_t* out);
+/* Trace space on a region of the mesh: element_mask holds nt flags (nonzero: the space lives
+ * on that element); null means every element.  Replaces a `definedon` FESpace (NGSolve's
+ * SurfaceL2(..., definedon=...)): the reference's operators read only the dofs of the
+ * boundary elements the space has (src/ngbem.cpp:43-66, src/hmat.cpp:19-41).  The dofs are
+ * numbered as on the mesh made of the region's elements (elements in order, vertices in
+ * ascending order, edges by first appearance); bem_space_global_dofs maps them back. */
+int bem_space_create_on(bem_mesh_t mesh, int kind, int dual_mapping, const unsigned char* element_mask,
+                        bem_space_t* out);
+/* dof -> element (P0), vertex (P1) or mesh edge (RT0, HCURL); out holds ndof entries */
+int bem_space_global_dofs(bem_space_t space, int* out);
 int bem_space_ndof(bem_space_t space, int* ndof);
 int bem_space_destroy(bem_space_t space);
 
@@ -251,6 +261,12 @@ int bem_operator_load(const char* path, bem_space_t trial, bem_space_t test, bem
  * pointers; synchronous on `stream`.  dim is the trial evaluator's dimension (1 for P0/P1
  * identity traces), 0 when the operator has no potential. */
 int bem_operator_potential_dim(bem_operator_t op, int* dim);
+
+/* The operator's trial / test `definedon` regions (reference IntegralOperator ctor,
+ * src/ngbem.cpp:17-113): nt element flags each, null for none.  As in the reference, the
+ * assembled matrix does not depend on them (its dofs are the spaces' dofs); the trial region
+ * restricts the elements bem_operator_potential sums over (PotentialCF, src/ngbem.cpp:1205). */
+int bem_operator_set_definedon(bem_operator_t op, const unsigned char* trial_mask, const unsigned char* test_mask);
 int bem_operator_potential(bem_operator_t op, const void* density, int npts, const double* points,
                            const double* normals, void* out, void* stream);
 

@@ -4,8 +4,8 @@ Drop-in for ngbem's operator path: the factory functions below keep the referenc
 and keywords (reference src/python_bem.cpp).  Assembly and application run as hand-written
 CUDA kernels for sm_103a behind the C-ABI of include/ngbem_gb300.h.
 """
-from .meshes import Mesh, icosphere, ellipsoid, perturbed_icosphere
+from .meshes import Mesh, Region, icosphere, ellipsoid, perturbed_icosphere
 from .bem import *  # noqa: F401,F403
 from .bem import __all__ as _bem_all
 
-__all__ = ["Mesh", "icosphere", "ellipsoid", "perturbed_icosphere"] + list(_bem_all)
+__all__ = ["Mesh", "Region", "icosphere", "ellipsoid", "perturbed_icosphere"] + list(_bem_all)

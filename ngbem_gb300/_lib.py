@@ -56,6 +56,8 @@ SIGNATURES = {
     "bem_mesh_num_edges": ([_vp, _ip], C.c_int),
     "bem_mesh_destroy": ([_vp], C.c_int),
     "bem_space_create": ([_vp, C.c_int, C.c_int, C.POINTER(_vp)], C.c_int),
+    "bem_space_create_on": ([_vp, C.c_int, C.c_int, _vp, C.POINTER(_vp)], C.c_int),
+    "bem_space_global_dofs": ([_vp, _ip], C.c_int),
     "bem_space_ndof": ([_vp, _ip], C.c_int),
     "bem_space_destroy": ([_vp], C.c_int),
     "bem_cluster_tree": ([_vp, C.c_int, _ip, C.c_int, _ip, _lp, _dp], C.c_int),
@@ -77,6 +79,7 @@ SIGNATURES = {
     "bem_operator_tensor_cores": ([_vp, _ip, C.POINTER(C.c_longlong), _ip, _ip, _dp], C.c_int),
     "bem_tc_selftest": ([_ip], C.c_int),
     "bem_operator_potential_dim": ([_vp, _ip], C.c_int),
+    "bem_operator_set_definedon": ([_vp, _vp, _vp], C.c_int),
     "bem_operator_save": ([_vp, C.c_char_p], C.c_int),
     "bem_operator_load": ([C.c_char_p, _vp, _vp, C.POINTER(_vp)], C.c_int),
     "bem_operator_potential": ([_vp, _vp, C.c_int, _vp, _vp, _vp, _vp], C.c_int),

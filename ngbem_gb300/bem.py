@@ -23,7 +23,7 @@ import numpy as np
 
 from . import _lib
 from ._lib import KERNELS, KINDS, EVALS, check, cplx2, lib
-from .meshes import Mesh
+from .meshes import Mesh, Region
 
 __all__ = ["SurfaceL2", "H1", "HDivSurface", "HCurl", "TraceSpace", "BaseMatrix", "HMatrix", "MassMatrix",
            "IntegralOperator", "IntegralOperatorC",
@@ -77,19 +77,33 @@ class TraceSpace:
     """Surface trace space: kind "P0" (SurfaceL2 order 0), "P1" (H1 order 1), "RT0" (HDivSurface order 0),
     "HCURL" (surface trace of HCurl order 0)."""
 
-    def __init__(self, mesh: Mesh, kind: str, dual_mapping: bool = False, complex: bool = False):
+    def __init__(self, mesh: Mesh, kind: str, dual_mapping: bool = False, complex: bool = False, definedon=None):
         if kind not in KINDS:
             raise ValueError(f"unknown space kind {kind!r}")
         self.mesh = mesh
         self.kind = kind
         self.dual_mapping = bool(dual_mapping)
         self.is_complex = bool(complex)
+        self.definedon = definedon
         self._mh = _MeshHandle.of(mesh)
         self.h = C.c_void_p()
-        check(lib.bem_space_create(self._mh.h, KINDS[kind], int(self.dual_mapping), C.byref(self.h)))
+        if definedon is None:
+            check(lib.bem_space_create(self._mh.h, KINDS[kind], int(self.dual_mapping), C.byref(self.h)))
+        else:
+            mask = _region_mask(definedon, mesh)
+            check(lib.bem_space_create_on(self._mh.h, KINDS[kind], int(self.dual_mapping),
+                                          C.c_void_p(mask.ctypes.data), C.byref(self.h)))
         n = C.c_int()
         check(lib.bem_space_ndof(self.h, C.byref(n)))
         self.ndof = n.value
+
+    @property
+    def global_dofs(self) -> np.ndarray:
+        """dof -> element (P0), vertex (P1) or edge (RT0, HCURL) of the whole mesh.  A space on a
+        region numbers its dofs like the mesh made of the region's elements (Mesh.submesh)."""
+        out = np.zeros(self.ndof, dtype=np.int32)
+        check(lib.bem_space_global_dofs(self.h, out.ctypes.data_as(_lib._ip)))
+        return out
 
     def __repr__(self):
         return f"TraceSpace({self.kind}, ndof={self.ndof})"
@@ -100,33 +114,43 @@ class TraceSpace:
             self.h = C.c_void_p()
 
 
-def SurfaceL2(mesh: Mesh, order: int = 0, dual_mapping: bool = False, complex: bool = False) -> TraceSpace:
-    """Piecewise constants on the surface (the reference uses NGSolve SurfaceL2; order 0 here)."""
+def _region_mask(region, mesh: Mesh) -> np.ndarray:
+    if not isinstance(region, Region):
+        raise TypeError("definedon must be a Region (mesh.Boundaries(...))")
+    if region.mesh is not mesh:
+        raise ValueError("the region belongs to another mesh")
+    return np.ascontiguousarray(region.mask, dtype=np.uint8)
+
+
+def SurfaceL2(mesh: Mesh, order: int = 0, dual_mapping: bool = False, complex: bool = False,
+              definedon=None) -> TraceSpace:
+    """Piecewise constants on the surface (the reference uses NGSolve SurfaceL2; order 0 here).
+    definedon: a Region; the space then lives on those triangles only."""
     if order != 0:
         raise NotImplementedError("SurfaceL2: only order 0 (piecewise constants) is supported")
-    return TraceSpace(mesh, "P0", dual_mapping, complex)
+    return TraceSpace(mesh, "P0", dual_mapping, complex, definedon)
 
 
-def H1(mesh: Mesh, order: int = 1, complex: bool = False) -> TraceSpace:
+def H1(mesh: Mesh, order: int = 1, complex: bool = False, definedon=None) -> TraceSpace:
     """Continuous piecewise linears on the surface (trace of NGSolve H1, order 1)."""
     if order != 1:
         raise NotImplementedError("H1: only order 1 is supported")
-    return TraceSpace(mesh, "P1", False, complex)
+    return TraceSpace(mesh, "P1", False, complex, definedon)
 
 
-def HDivSurface(mesh: Mesh, order: int = 0, complex: bool = False) -> TraceSpace:
+def HDivSurface(mesh: Mesh, order: int = 0, complex: bool = False, definedon=None) -> TraceSpace:
     """Lowest-order Raviart-Thomas on the surface (NGSolve HDivSurface order 0)."""
     if order != 0:
         raise NotImplementedError("HDivSurface: only order 0 (RT0) is supported")
-    return TraceSpace(mesh, "RT0", False, complex)
+    return TraceSpace(mesh, "RT0", False, complex, definedon)
 
 
-def HCurl(mesh: Mesh, order: int = 0, complex: bool = False) -> TraceSpace:
+def HCurl(mesh: Mesh, order: int = 0, complex: bool = False, definedon=None) -> TraceSpace:
     """Surface trace of the lowest-order Nedelec space (NGSolve HCurl order 0 restricted to the
     boundary): one dof per edge, on each triangle n x the RT0 shape function of that edge."""
     if order != 0:
         raise NotImplementedError("HCurl: only order 0 is supported")
-    return TraceSpace(mesh, "HCURL", False, complex)
+    return TraceSpace(mesh, "HCURL", False, complex, definedon)
 
 
 def cluster_tree(space: TraceSpace, leafsize: int = 40):
@@ -467,7 +491,7 @@ class IntegralOperator:
 
     def __init__(self, kernel, kappa, trial, test, trial_eval, test_eval, intorder, leafsize, eta, eps, method,
                  testhmatrix, precision="fp64", intorder_singular=None, intorder_regular=None, max_rank=None,
-                 aca_eps_floor=None):
+                 aca_eps_floor=None, trial_definedon=None, test_definedon=None):
         test = trial if test is None else test
         p = _lib.Params()
         check(lib.bem_params_default(C.byref(p)))
@@ -489,6 +513,14 @@ class IntegralOperator:
         check(lib.bem_operator_create(KERNELS[kernel], float(kappa), trial.h, test.h, EVALS[trial_eval],
                                       EVALS[test_eval], C.byref(p), C.byref(h)))
         self.mat = HMatrix(h)
+        # definedon regions (reference IntegralOperator ctor, src/ngbem.cpp:17-113): as there,
+        # the assembled matrix does not read them; GetPotential sums over the trial region only
+        self.trial_definedon, self.test_definedon = trial_definedon, test_definedon
+        if trial_definedon is not None or test_definedon is not None:
+            masks = [None if r is None else _region_mask(r, sp.mesh)
+                     for r, sp in ((trial_definedon, trial), (test_definedon, test))]
+            check(lib.bem_operator_set_definedon(h, *[None if m is None else C.c_void_p(m.ctypes.data)
+                                                      for m in masks]))
         if testhmatrix:
             self._test_hmatrix()
 
@@ -538,9 +570,6 @@ def _dense_args(method, leafsize, eta):
     return method, leafsize, eta
 
 
-def _no_regions(*regions):
-    if any(r is not None for r in regions):
-        raise NotImplementedError("definedon region masks are not supported")
 
 
 def SingleLayerPotentialOperator(space, intorder=3, leafsize=40, eta=2., eps=1e-6, method="aca",
@@ -553,18 +582,17 @@ def SingleLayerPotentialOperator(space, intorder=3, leafsize=40, eta=2., eps=1e-
 def DoubleLayerPotentialOperator(trial_space, test_space, trial_definedon=None, test_definedon=None, intorder=3,
                                  leafsize=40, eta=2., eps=1e-6, method="aca", testhmatrix=False, **gb):
     """Laplace double layer K (reference python_bem.cpp:41-60)."""
-    _no_regions(trial_definedon, test_definedon)
     return IntegralOperator("laplace_dl", 0.0, trial_space, test_space, "id", "id", intorder, leafsize, eta, eps,
-                            method, testhmatrix, **gb)
+                            method, testhmatrix, trial_definedon=trial_definedon, test_definedon=test_definedon,
+                            **gb)
 
 
 def HypersingularOperator(space, definedon=None, intorder=3, leafsize=40, eta=2., eps=1e-6, method="aca",
                           testhmatrix=False, **gb):
     """Laplace hypersingular W with surface-curl traces (reference python_bem.cpp:63-75).
     As in the reference, method is not consulted (always an ACA H-matrix)."""
-    _no_regions(definedon)
     return IntegralOperator("laplace_hs", 0.0, space, space, "rot", "rot", intorder, leafsize, eta, eps, "aca",
-                            testhmatrix, **gb)
+                            testhmatrix, trial_definedon=definedon, test_definedon=definedon, **gb)
 
 
 def _kappa(kappa):
@@ -616,9 +644,8 @@ def MaxwellSingleLayerPotentialOperator(space, kappa, definedon=None, intorder=3
                                         method="aca", testhmatrix=False, **gb):
     """Maxwell single layer on HDivSurface with [Piola u; div u] traces (reference
     python_bem.cpp:122-134): kappa <u,v> - 1/kappa <div u, div v> weighted by G."""
-    _no_regions(definedon)
     return IntegralOperator("maxwell_sl", _kappa(kappa), space, space, "maxwell", "maxwell", intorder, leafsize,
-                            eta, eps, "aca", testhmatrix, **gb)
+                            eta, eps, "aca", testhmatrix, trial_definedon=definedon, test_definedon=definedon, **gb)
 
 
 def _need_hcurl(space, what):
@@ -630,10 +657,10 @@ def MaxwellSingleLayerPotentialOperatorCurl(space, kappa, definedon=None, intord
                                             eps=1e-6, method="aca", testhmatrix=False, **gb):
     """Maxwell single layer on HCurl with DiffOpMaxwell traces [n x u; curl u] (reference
     python_bem.cpp:137-150): kappa <n x u, n x v> - 1/kappa <curl u, curl v> weighted by G."""
-    _no_regions(definedon)
     _need_hcurl(space, "MaxwellSingleLayerPotentialOperatorCurl")
     return IntegralOperator("maxwell_sl", _kappa(kappa), space, space, "maxwellcurl", "maxwellcurl", intorder,
-                            leafsize, eta, eps, "aca", testhmatrix, **gb)
+                            leafsize, eta, eps, "aca", testhmatrix, trial_definedon=definedon,
+                            test_definedon=definedon, **gb)
 
 
 def MaxwellDoubleLayerPotentialOperator(trial_space, test_space, kappa, trial_definedon=None, test_definedon=None,
@@ -642,12 +669,12 @@ def MaxwellDoubleLayerPotentialOperator(trial_space, test_space, kappa, trial_de
     """Maxwell double layer (reference python_bem.cpp:154-171): MaxwellDLKernel on the rotated
     trace n x u of the HCurl trial space and the identity trace of the test space (HDivSurface,
     as in the reference's Maxwell tests, or HCurl).  method "dense" gives one root block."""
-    _no_regions(trial_definedon, test_definedon)
     _need_hcurl(trial_space, "MaxwellDoubleLayerPotentialOperator (trial space)")
     if test_space.kind not in ("RT0", "HCURL"):
         raise TypeError("MaxwellDoubleLayerPotentialOperator: the test space must be HDivSurface or HCurl")
     return IntegralOperator("maxwell_dl", _kappa(kappa), trial_space, test_space, "rotatedtrace", "id", intorder,
-                            leafsize, eta, eps, method, testhmatrix, **gb)
+                            leafsize, eta, eps, method, testhmatrix, trial_definedon=trial_definedon,
+                            test_definedon=test_definedon, **gb)
 
 
 # ----------------------------------------------------------------------------------------

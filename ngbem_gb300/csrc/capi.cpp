@@ -80,6 +80,25 @@ int bem_space_create(bem_mesh_t mesh, int kind, int dual_mapping, bem_space_t* o
   });
 }
 
+int bem_space_create_on(bem_mesh_t mesh, int kind, int dual_mapping, const unsigned char* element_mask,
+                        bem_space_t* out) {
+  return guarded([&] {
+    REQUIRE(mesh && out, "null argument");
+    REQUIRE(kind == BEM_P0 || kind == BEM_P1 || kind == BEM_RT0 || kind == BEM_HCURL, "unknown space kind");
+    REQUIRE(!dual_mapping || kind == BEM_P0, "dual mapping is defined for P0 only");
+    auto s = std::make_unique<bem_space_s>();
+    s->s.build(&mesh->m, kind, dual_mapping, element_mask);
+    *out = s.release();
+  });
+}
+
+int bem_space_global_dofs(bem_space_t space, int* out) {
+  return guarded([&] {
+    REQUIRE(space && out, "null argument");
+    std::copy(space->s.global_dof.begin(), space->s.global_dof.end(), out);
+  });
+}
+
 int bem_space_ndof(bem_space_t space, int* ndof) {
   return guarded([&] {
     REQUIRE(space && ndof, "null argument");
@@ -309,6 +328,19 @@ int bem_operator_load(const char* path, bem_space_t trial, bem_space_t test, bem
     auto h = std::make_unique<bem_operator_s>();
     h->op = load_operator(path, &trial->s, &test->s);
     *out = h.release();
+  });
+}
+
+int bem_operator_set_definedon(bem_operator_t op, const unsigned char* trial_mask, const unsigned char* test_mask) {
+  return guarded([&] {
+    REQUIRE(op, "null argument");
+    auto* h = dynamic_cast<HOperator*>(op->op.get());
+    REQUIRE(h, "not an integral operator");
+    const int nt = h->trial->mesh->nt;
+    h->def_trial.clear();
+    h->def_test.clear();
+    if (trial_mask) h->def_trial.assign(trial_mask, trial_mask + nt);
+    if (test_mask) h->def_test.assign(test_mask, test_mask + nt);
   });
 }
 

@@ -192,37 +192,63 @@ MeshH::RuleTables& MeshH::rule_tables(int order) {
 // ------------------------------------------------------------------------------------------
 // trace spaces
 // ------------------------------------------------------------------------------------------
-void SpaceH::build(MeshH* m, int kind_, int dual_) {
+void SpaceH::build(MeshH* m, int kind_, int dual_, const unsigned char* mask) {
   mesh = m;
   kind = kind_;
   dual = dual_ ? 1 : 0;
-  dofs.assign(3 * (size_t)m->nt, 0);
+  elems.clear();
+  for (int e = 0; e < m->nt; ++e)
+    if (!mask || mask[e]) elems.push_back(e);
+  if (elems.empty()) throw Error(BEM_ERR_ARG, "the space's region has no elements");
+  dofs.assign(3 * (size_t)m->nt, -1);
   sign.assign(3 * (size_t)m->nt, 1);
+  global_dof.clear();
+  // On a region the dofs are numbered like those of the mesh made of the region's elements
+  // (in element order, vertices renumbered in ascending order): P0 the elements in order, P1
+  // the vertices in ascending order, RT0 / HCURL the edges by first appearance.
   if (kind == BEM_P0) {
     nd = 1;
-    ndof = m->nt;
-    for (int e = 0; e < m->nt; ++e) dofs[3 * e] = dofs[3 * e + 1] = dofs[3 * e + 2] = e;
+    for (int e : elems) {
+      dofs[3 * e] = dofs[3 * e + 1] = dofs[3 * e + 2] = (int)global_dof.size();
+      global_dof.push_back(e);
+    }
   } else if (kind == BEM_P1) {
     nd = 3;
-    ndof = m->nv;
-    dofs = m->T;
+    std::vector<int> map(m->nv, -1);
+    for (int e : elems)
+      for (int k = 0; k < 3; ++k) map[m->T[3 * e + k]] = 0;
+    for (int v = 0; v < m->nv; ++v)
+      if (map[v] == 0) {
+        map[v] = (int)global_dof.size();
+        global_dof.push_back(v);
+      }
+    for (int e : elems)
+      for (int k = 0; k < 3; ++k) dofs[3 * e + k] = map[m->T[3 * e + k]];
   } else if (kind == BEM_RT0 || kind == BEM_HCURL) {
     nd = 3;
-    ndof = m->ne;
-    dofs = m->TE;
-    for (int e = 0; e < m->nt; ++e)
-      for (int k = 0; k < 3; ++k) sign[3 * e + k] = m->T[3 * e + k] < m->T[3 * e + (k + 1) % 3] ? 1 : -1;
+    std::vector<int> map(m->ne, -1);
+    for (int e : elems)
+      for (int k = 0; k < 3; ++k) {
+        const int g = m->TE[3 * e + k];
+        if (map[g] < 0) {
+          map[g] = (int)global_dof.size();
+          global_dof.push_back(g);
+        }
+        dofs[3 * e + k] = map[g];
+        sign[3 * e + k] = m->T[3 * e + k] < m->T[3 * e + (k + 1) % 3] ? 1 : -1;
+      }
   } else {
     throw Error(BEM_ERR_ARG, "unknown space kind");
   }
+  ndof = (int)global_dof.size();
   // dof -> elements (CSR, ascending element ids)
   e4d_ptr.assign(ndof + 1, 0);
-  for (int e = 0; e < m->nt; ++e)
+  for (int e : elems)
     for (int a = 0; a < nd; ++a) e4d_ptr[dofs[3 * e + a] + 1]++;
   for (int d = 0; d < ndof; ++d) e4d_ptr[d + 1] += e4d_ptr[d];
   e4d.assign(e4d_ptr[ndof], 0);
   std::vector<int> fill(e4d_ptr.begin(), e4d_ptr.end() - 1);
-  for (int e = 0; e < m->nt; ++e)
+  for (int e : elems)
     for (int a = 0; a < nd; ++a) e4d[fill[dofs[3 * e + a]]++] = e;
   for (int d = 0; d < ndof; ++d)
     if (e4d_ptr[d + 1] == e4d_ptr[d]) throw Error(BEM_ERR_ARG, "space has a dof without elements");
@@ -273,14 +299,14 @@ static void cluster_data(const SpaceH& sp, std::vector<double>& G, std::vector<s
   G.assign(ndof, 0.0);
   X.assign(ndof, {0.0, 0.0, 0.0});
   std::vector<int> cnt(ndof, 0);
-  for (int e = 0; e < m.nt; ++e)
+  for (int e : sp.elems)
     for (int a = 0; a < sp.nd; ++a) {
       const int d = sp.el_dofs(e)[a];
       G[d] += m.area(e);
       cnt[d] += 1;
     }
   static const double xhat[7][2] = {{1, 0}, {0, 1}, {0, 0}, {0.5, 0.5}, {0, 0.5}, {0.5, 0}, {1. / 3, 1. / 3}};
-  for (int e = 0; e < m.nt; ++e) {
+  for (int e : sp.elems) {
     double pt[7][3];
     for (int j = 0; j < 7; ++j) m.map(e, xhat[j][0], xhat[j][1], pt[j]);
     const int* dn = sp.el_dofs(e);
@@ -291,7 +317,9 @@ static void cluster_data(const SpaceH& sp, std::vector<double>& G, std::vector<s
       if (c == 2) ++nedge;
       if (c == 1) X[dn[a]] = {pt[6][0], pt[6][1], pt[6][2]};
     }
-    const int per_edge = nedge / 3;
+    // fewer than three two-element dofs (an element at the border of an open surface or of a
+    // region): each is its own edge (the reference's loop would not advance with 0 per edge)
+    const int per_edge = std::max(1, nedge / 3);
     int ie = 0;
     for (int a = 0; a < sp.nd; ++a) {
       if (cnt[dn[a]] != 2) continue;
@@ -463,8 +491,9 @@ void ClusterTreeH::build_patches(const SpaceH& sp) {
   for (int c = nc - 1; c >= 0; --c) {
     const ClusterH& C = cl[c];
     std::vector<int>& out = pl[c];
-    if (sp.kind == BEM_P0) {
-      out.assign(perm.begin() + C.PermuPos, perm.begin() + C.PermuPos + C.Number);
+    if (sp.kind == BEM_P0) {  // one element per dof, in cluster order
+      out.resize(C.Number);
+      for (long k = 0; k < C.Number; ++k) out[k] = sp.global_dof[perm[C.PermuPos + k]];
       continue;
     }
     if (C.Child1 >= 0) {

@@ -105,11 +105,15 @@ struct ClusterTreeH;
 struct SpaceH {
   MeshH* mesh = nullptr;
   int kind = BEM_P0, nd = 1, ndof = 0, dual = 0;
-  std::vector<int> dofs;      // 3*nt (unused entries = dof 0 for P0)
+  std::vector<int> dofs;      // 3*nt (P0: the element's dof three times; -1 off the region)
   std::vector<int> sign;      // 3*nt
   std::vector<int> e4d_ptr, e4d;  // dof -> elements (CSR, element order)
+  std::vector<int> global_dof;    // dof -> element (P0), vertex (P1) or mesh edge (RT0, HCURL)
+  std::vector<int> elems;         // the elements the space lives on, ascending
   DevBuf d_dofs, d_sign;
-  void build(MeshH* m, int kind_, int dual_);
+  // mask: nt flags of the elements the space lives on (null: all of them)
+  void build(MeshH* m, int kind_, int dual_, const unsigned char* mask = nullptr);
+  bool on(int e) const { return dofs[3 * e] >= 0; }
   const int* el_dofs(int e) const { return &dofs[3 * e]; }
   void ensure_device();
   // cluster tree with element patches for a leaf size, built on first use and shared by the
@@ -232,6 +236,9 @@ struct HOperator : OperatorBase {
   // potential of a trial-space density at points (device buffers; synchronous)
   void potential(const void* density, int npts, const double* pts, const double* normals, void* out,
                  cudaStream_t s);
+  // trial / test definedon regions (nt element flags; empty: none).  As in the reference they
+  // do not change the assembled matrix; the trial region restricts the potential's elements.
+  std::vector<unsigned char> def_trial, def_test;
 };
 
 struct MassOperator : OperatorBase {

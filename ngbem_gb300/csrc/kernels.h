@@ -236,6 +236,7 @@ struct PotArgs {
   const void* erec;       // ElemRecP<double>[nt]
   const void* qoff;       // QPt<double>[nt * nq]: rule points relative to the centroid, w * |J|
   const double* rq;       // reference points (xi, eta) of the rule
+  const int* elems;       // the nt source elements (null: elements 0 .. nt-1)
   int nt, nq;
   SpaceDev trial;
   const void* density;    // trial dofs (double or complex128)

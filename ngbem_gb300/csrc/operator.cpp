@@ -1134,7 +1134,15 @@ void HOperator::potential(const void* density, int npts, const double* pts, cons
   trial->ensure_device();
   const int order_r = prm.intorder_regular > 0 ? prm.intorder_regular : prm.intorder;
   MeshH::RuleTables& rt = mesh.rule_tables(order_r);
-  const size_t nsrc = (size_t)mesh.nt * rt.nq;
+  // source elements: the trial space's, within the trial definedon region when there is one
+  // (PotentialCF skips the elements outside it, src/ngbem.cpp:1205)
+  std::vector<int> el;
+  for (int e : trial->elems)
+    if (def_trial.empty() || def_trial[e]) el.push_back(e);
+  const bool all = (int)el.size() == mesh.nt;
+  DevBuf d_el;
+  if (!all && !el.empty()) d_el.upload(el, s);
+  const size_t nsrc = std::max<size_t>(1, el.size() * (size_t)rt.nq);
   DevBuf src_pos, src_val;
   src_pos.alloc(nsrc * 6 * sizeof(double));
   src_val.alloc(nsrc * dim * (cplx ? 16 : 8));
@@ -1142,7 +1150,8 @@ void HOperator::potential(const void* density, int npts, const double* pts, cons
   a.erec = rt.rec[0].p;
   a.qoff = rt.qoff[0].p;
   a.rq = rt.rq[0].as<double>();
-  a.nt = mesh.nt;
+  a.elems = all ? nullptr : d_el.as<int>();
+  a.nt = (int)el.size();
   a.nq = rt.nq;
   a.trial = space_dev(*trial, trt, d_pinv_trial);
   a.density = density;
@@ -1240,7 +1249,7 @@ void MassOperator::build(SpaceH* trial, SpaceH* test, bool complex_vectors) {
     dim = 3;
   };
   for (int e = 0; e < m.nt; ++e)
-    for (int q = 0; q < nq; ++q) {
+    for (int q = 0; q < nq && trial->on(e) && test->on(e); ++q) {
       double Si[3][3], Sj[3][3];
       int di, dj;
       shape(*test, e, r.xi[q], r.eta[q], Si, di);

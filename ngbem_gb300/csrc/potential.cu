@@ -30,9 +30,10 @@ __global__ void pot_sources_kernel(PotArgs a) {
   const long long total = (long long)a.nt * a.nq;
   for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total;
        t += (long long)gridDim.x * blockDim.x) {
-    const int e = (int)(t / a.nq), q = (int)(t - (long long)e * a.nq);
+    const int k = (int)(t / a.nq), q = (int)(t - (long long)k * a.nq);
+    const int e = a.elems ? a.elems[k] : k;
     const ElemRecP<double>& Ee = E[e];
-    const QPt<double> qo = Q[t];
+    const QPt<double> qo = Q[(size_t)e * a.nq + q];
     double rot[3][3], xp[3][3];
     for (int x = 0; x < 3; ++x)
       for (int y = 0; y < 3; ++y) {

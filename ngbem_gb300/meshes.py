@@ -18,13 +18,39 @@ from __future__ import annotations
 
 import numpy as np
 
-__all__ = ["Mesh", "icosphere", "ellipsoid", "perturbed_icosphere"]
+__all__ = ["Mesh", "Region", "icosphere", "ellipsoid", "perturbed_icosphere"]
+
+
+class Region:
+    """A set of boundary elements of a mesh (the role of NGSolve's Region, e.g.
+    ``mesh.Boundaries("outer")``): ``mask`` holds one flag per triangle."""
+
+    def __init__(self, mesh: "Mesh", mask):
+        self.mesh = mesh
+        self.mask = np.ascontiguousarray(mask, dtype=bool)
+        if self.mask.shape != (mesh.nt,):
+            raise ValueError("a region mask has one flag per triangle")
+
+    def Mask(self) -> np.ndarray:
+        return self.mask
+
+    def __or__(self, other: "Region") -> "Region":
+        if other.mesh is not self.mesh:
+            raise ValueError("regions of different meshes")
+        return Region(self.mesh, self.mask | other.mask)
+
+    __add__ = __or__
+
+    def __repr__(self):
+        return f"Region({int(self.mask.sum())} of {self.mesh.nt} triangles)"
 
 
 class Mesh:
-    """A triangle surface mesh: ``vertices`` (nv x 3 float64), ``triangles`` (nt x 3 int32)."""
+    """A triangle surface mesh: ``vertices`` (nv x 3 float64), ``triangles`` (nt x 3 int32), and
+    optionally a boundary-region index per triangle (``regions``, default 0) with the regions'
+    names (``region_names``, default ``["default"]``)."""
 
-    def __init__(self, vertices, triangles):
+    def __init__(self, vertices, triangles, regions=None, region_names=None):
         self.vertices = np.ascontiguousarray(vertices, dtype=np.float64)
         self.triangles = np.ascontiguousarray(triangles, dtype=np.int32)
         if self.vertices.ndim != 2 or self.vertices.shape[1] != 3:
@@ -33,6 +59,33 @@ class Mesh:
             raise ValueError("triangles must be (nt, 3)")
         if self.triangles.size and (self.triangles.min() < 0 or self.triangles.max() >= len(self.vertices)):
             raise ValueError("triangle vertex index out of range")
+        nt = self.triangles.shape[0]
+        self.regions = np.zeros(nt, dtype=np.int32) if regions is None else \
+            np.ascontiguousarray(regions, dtype=np.int32)
+        if self.regions.shape != (nt,):
+            raise ValueError("regions must hold one index per triangle")
+        nreg = int(self.regions.max()) + 1 if nt else 1
+        self.region_names = list(region_names) if region_names is not None else \
+            (["default"] if nreg == 1 else [f"region{i}" for i in range(nreg)])
+        if nt and (self.regions.min() < 0 or nreg > len(self.region_names)):
+            raise ValueError("region index without a name")
+
+    def Boundaries(self, pattern: str) -> Region:
+        """The triangles whose region name matches the regular expression ``pattern`` (as
+        NGSolve's ``mesh.Boundaries("outer|inner")``)."""
+        import re
+        rx = re.compile(pattern)
+        hit = np.array([rx.fullmatch(n) is not None for n in self.region_names], dtype=bool)
+        return Region(self, hit[self.regions])
+
+    def submesh(self, region: Region):
+        """The mesh made of the region's triangles (in order), its vertices renumbered in
+        ascending order: (mesh, vertex ids, triangle ids) in this mesh's numbering."""
+        tids = np.flatnonzero(region.mask).astype(np.int32)
+        vids = np.unique(self.triangles[tids])
+        remap = np.full(self.nv, -1, dtype=np.int32)
+        remap[vids] = np.arange(len(vids), dtype=np.int32)
+        return Mesh(self.vertices[vids], remap[self.triangles[tids]]), vids.astype(np.int32), tids
 
     @property
     def nv(self) -> int:

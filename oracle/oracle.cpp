@@ -452,7 +452,10 @@ static void compute_cluster_data(const Mesh& m, const Space& sp, std::vector<dou
       if (clc == 2) edgecounter++;
       if (clc == 1) X[dn[ii]] = {mip[6][0], mip[6][1], mip[6][2]};
     }
-    int edgeoffset = edgecounter / 3;
+    // An element with one or two two-element dofs (at the border of an open surface or of a
+    // region) takes each as its own edge: with edgeoffset 0 the reference's loop below would
+    // not advance (src/hmat.cpp:122-138).  Closed surfaces never get there.
+    int edgeoffset = std::max(1, edgecounter / 3);
     edgecounter = 0;
     for (int ii = 0; ii < sp.nd; ++ii) {
       int clc = cnt[dn[ii]];

@@ -100,3 +100,61 @@ def test_edge_numbering_matches_oracle(oracle):
     sp = nb.HDivSurface(m)
     edges, te = oracle.mesh_edges(m)
     assert sp.ndof == len(edges) == 3 * m.nt // 2
+
+
+def _capped_sphere(level=3, z0=0.3):
+    from ngbem_gb300.meshes import Mesh
+    m0 = icosphere(level)
+    cap = (m0.centroids()[:, 2] > z0).astype(np.int32)
+    return Mesh(m0.vertices, m0.triangles, regions=cap, region_names=["rest", "cap"])
+
+
+@pytest.mark.parametrize("kind", ["P0", "P1", "RT0", "HCURL"])
+def test_region_space_is_the_submesh_space(oracle, kind):
+    """A space on a region (definedon) numbers its dofs like the space on the mesh made of the
+    region's triangles, and has the same cluster tree and block partition, bit for bit."""
+    m = _capped_sphere()
+    R = m.Boundaries("cap")
+    sub, vids, tids = m.submesh(R)
+    sr, ss = nb.TraceSpace(m, kind, definedon=R), nb.TraceSpace(sub, kind)
+    assert sr.ndof == ss.ndof
+    g = sr.global_dofs
+    if kind == "P0":
+        assert np.array_equal(g, tids)
+    elif kind == "P1":
+        assert np.array_equal(g, vids)
+    else:
+        E, _ = oracle.mesh_edges(m)
+        Es, _ = oracle.mesh_edges(sub)
+        assert np.array_equal(np.sort(E[g], axis=1), np.sort(vids[Es], axis=1))
+    for leaf in (10, 40):
+        p1, ci1, cd1 = nb.cluster_tree(sr, leaf)
+        p2, ci2, cd2 = nb.cluster_tree(ss, leaf)
+        assert np.array_equal(p1, p2) and np.array_equal(ci1, ci2)
+        assert np.array_equal(cd1.view(np.int64), cd2.view(np.int64))
+        b1, b2 = nb.partition(sr, leafsize=leaf), nb.partition(ss, leafsize=leaf)
+        for k in b1:
+            assert np.array_equal(b1[k], b2[k])
+
+
+def test_regions_and_masks():
+    from ngbem_gb300.meshes import Mesh
+    m = _capped_sphere(2)
+    cap, rest, both = m.Boundaries("cap"), m.Boundaries("rest"), m.Boundaries("cap|rest")
+    assert not (cap.Mask() & rest.Mask()).any() and (cap | rest).Mask().all() and both.Mask().all()
+    assert m.Boundaries(".*").Mask().all() and not m.Boundaries("outer").Mask().any()
+    with pytest.raises(ValueError):
+        Mesh(m.vertices, m.triangles, regions=np.zeros(3, dtype=np.int32))
+    with pytest.raises(ValueError):
+        Mesh(m.vertices, m.triangles, regions=np.full(m.nt, 2), region_names=["a", "b"])
+    other = icosphere(2)
+    with pytest.raises(ValueError):
+        nb.SurfaceL2(other, definedon=cap)
+    with pytest.raises(TypeError):
+        nb.SurfaceL2(m, definedon=cap.Mask())
+    # a region without triangles is refused by the library
+    with pytest.raises(Exception):
+        nb.H1(m, definedon=m.Boundaries("outer"))
+    # the whole mesh as a region gives the plain space
+    a, b = nb.HDivSurface(m, definedon=m.Boundaries(".*")), nb.HDivSurface(m)
+    assert a.ndof == b.ndof and np.array_equal(a.global_dofs, np.arange(b.ndof))
