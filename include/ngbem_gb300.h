@@ -132,7 +132,9 @@ int bem_partition(bem_space_t trial, bem_space_t test, int leafsize, double eta,
 
 /* Operator construction = assembly on the GPU (reference GenericIntegralOperator ctor,
  * src/ngbem.cpp:314-330, and CalcHMatrix :118-157; factories src/python_bem.cpp:27-173).
- * test may equal trial.  Synchronous: returns when the H-matrix is resident in HBM. */
+ * test may equal trial.  The spaces may live on two meshes (the reference's trial and test
+ * MeshAccess, src/ngbem.cpp:33-34): elements of different meshes share no vertex, so every
+ * pair between them is regular.  Synchronous: returns when the H-matrix is resident in HBM. */
 int bem_operator_create(int kernel, double kappa, bem_space_t trial, bem_space_t test,
                         int trial_eval, int test_eval, const bem_params_t* params,
                         bem_operator_t* out);
@@ -263,7 +265,8 @@ int bem_operator_load(const char* path, bem_space_t trial, bem_space_t test, bem
 int bem_operator_potential_dim(bem_operator_t op, int* dim);
 
 /* The operator's trial / test `definedon` regions (reference IntegralOperator ctor,
- * src/ngbem.cpp:17-113): nt element flags each, null for none.  As in the reference, the
+ * src/ngbem.cpp:17-113): one flag per element of the trial space's mesh and of the test
+ * space's mesh, null for none.  As in the reference, the
  * assembled matrix does not depend on them (its dofs are the spaces' dofs); the trial region
  * restricts the elements bem_operator_potential sums over (PotentialCF, src/ngbem.cpp:1205). */
 int bem_operator_set_definedon(bem_operator_t op, const unsigned char* trial_mask, const unsigned char* test_mask);

@@ -336,11 +336,18 @@ int bem_operator_set_definedon(bem_operator_t op, const unsigned char* trial_mas
     REQUIRE(op, "null argument");
     auto* h = dynamic_cast<HOperator*>(op->op.get());
     REQUIRE(h, "not an integral operator");
+    // masks over the caller's meshes, stored over the operator's (merged) mesh
     const int nt = h->trial->mesh->nt;
     h->def_trial.clear();
     h->def_test.clear();
-    if (trial_mask) h->def_trial.assign(trial_mask, trial_mask + nt);
-    if (test_mask) h->def_test.assign(test_mask, test_mask + nt);
+    if (trial_mask) {
+      h->def_trial.assign(nt, 0);
+      std::copy(trial_mask, trial_mask + h->trial_nt0, h->def_trial.begin() + h->trial_e0);
+    }
+    if (test_mask) {
+      h->def_test.assign(nt, 0);
+      std::copy(test_mask, test_mask + h->test_nt0, h->def_test.begin());
+    }
   });
 }
 

@@ -162,6 +162,14 @@ struct HOperator : OperatorBase {
   double kappa = 0.0;
   SpaceH* trial = nullptr;
   SpaceH* test = nullptr;
+  // Spaces on two meshes: merge_meshes() builds one mesh of both (the test mesh's vertices and
+  // elements first, then the trial mesh's) and rebuilds each space on its part as a region
+  // space, which has the same dofs in the same order; trial / test then point at those.
+  std::unique_ptr<MeshH> own_mesh;
+  std::unique_ptr<SpaceH> own_trial_space, own_test_space;
+  int trial_e0 = 0;       // first element of the trial space's mesh in trial->mesh
+  int trial_nt0 = 0, test_nt0 = 0;  // elements of the meshes the caller's spaces live on
+  void merge_meshes();
   int trial_ev = 0, test_ev = 0, trt = 0, tet = 0;
   bem_params_t prm{};
   int prec = 0;           // 0 fp64, 1 mixed

@@ -60,13 +60,39 @@ struct NearPass {
   int sing_cap = 0;
 };
 
+void HOperator::merge_meshes() {
+  trial_nt0 = trial->mesh->nt;
+  test_nt0 = test->mesh->nt;
+  if (trial->mesh == test->mesh) return;
+  const MeshH& a = *test->mesh;
+  const MeshH& b = *trial->mesh;
+  std::vector<double> X(a.X);
+  X.insert(X.end(), b.X.begin(), b.X.end());
+  std::vector<int> T(a.T);
+  for (int v : b.T) T.push_back(v + a.nv);
+  own_mesh = std::make_unique<MeshH>();
+  own_mesh->build(a.nv + b.nv, X.data(), a.nt + b.nt, T.data());
+  std::vector<unsigned char> on_test(own_mesh->nt, 0), on_trial(own_mesh->nt, 0);
+  for (int e = 0; e < a.nt; ++e) on_test[e] = test->on(e);
+  for (int e = 0; e < b.nt; ++e) on_trial[a.nt + e] = trial->on(e);
+  own_test_space = std::make_unique<SpaceH>();
+  own_test_space->build(own_mesh.get(), test->kind, test->dual, on_test.data());
+  own_trial_space = std::make_unique<SpaceH>();
+  own_trial_space->build(own_mesh.get(), trial->kind, trial->dual, on_trial.data());
+  if (own_test_space->ndof != test->ndof || own_trial_space->ndof != trial->ndof)
+    throw Error(BEM_ERR_INTERNAL, "merged-mesh spaces differ from the caller's spaces");
+  test = own_test_space.get();
+  trial = own_trial_space.get();
+  trial_e0 = a.nt;
+}
+
 void HOperator::assemble() {
   const auto t_start = clk::now();
+  merge_meshes();
   trt = trace_kind(trial->kind, trial_ev);
   tet = trace_kind(test->kind, test_ev);
   if (trt < 0 || tet < 0) throw Error(BEM_ERR_ARG, "evaluator not available for this space");
   if (!nf_combo_supported(kid, trt, tet)) throw Error(BEM_ERR_ARG, "kernel / trace combination not supported");
-  if (trial->mesh != test->mesh) throw Error(BEM_ERR_ARG, "trial and test spaces must live on one mesh");
   cplx = kernel_complex(kid);
   const int NC = kernel_ncomp(kid);
   prec = prm.precision == BEM_MIXED ? 1 : 0;

@@ -132,10 +132,15 @@ std::unique_ptr<HOperator> load_operator(const char* path, SpaceH* trial, SpaceH
   get(f, ts, sizeof(ts));
   const int nv = get_v<int>(f), nt = get_v<int>(f);
   if (ts[0] != trial->kind || ts[1] != trial->ndof || ts[2] != trial->dual || ts[3] != test->kind ||
-      ts[4] != test->ndof || ts[5] != test->dual || nv != trial->mesh->nv || nt != trial->mesh->nt)
+      ts[4] != test->ndof || ts[5] != test->dual)
     throw Error(BEM_ERR_ARG, "the spaces do not match the saved operator");
   op->trial = trial;
   op->test = test;
+  op->merge_meshes();  // spaces on two meshes: the same merged mesh as at assembly
+  trial = op->trial;
+  test = op->test;
+  if (nv != trial->mesh->nv || nt != trial->mesh->nt)
+    throw Error(BEM_ERR_ARG, "the spaces do not match the saved operator");
   op->trt = trace_kind(trial->kind, op->trial_ev);
   op->tet = trace_kind(test->kind, op->test_ev);
   op->cplx = kernel_complex(op->kid);
