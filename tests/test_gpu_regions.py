@@ -110,37 +110,42 @@ TWO_MESH_CASES = [("laplace_sl", "P0", "P1", "id", "id", 0.0), ("helmholtz_dl", 
                   ("maxwell_sl", "RT0", "RT0", "maxwell", "maxwell", 2.0)]
 
 
+def _union(a, b):
+    return Mesh(np.vstack([a.vertices, b.vertices]), np.vstack([a.triangles, b.triangles + a.nv]))
+
+
 @pytest.mark.parametrize("case", TWO_MESH_CASES, ids=[c[0] for c in TWO_MESH_CASES])
 def test_trial_and_test_on_two_meshes(oracle, case):
     """Trial space on one mesh, test space on another (the reference's trial and test
     MeshAccess): the operator equals the block of the oracle's operator on the union of both
-    meshes (test rows of the first, trial columns of the second), dense 1e-10 and H-matrix
-    within the ACA tolerance; the potential sums over the trial mesh."""
+    meshes (test rows of the first, trial columns of the second).  Dense 1e-10 with a small
+    sphere 0.24 from the unit sphere (close regular pairs); H-matrix within the ACA tolerance
+    with it 1.6 away (the root block is admissible, low rank); the potential sums over the
+    trial mesh."""
     k, tr, te, e1, e2, kap = case
     a = icosphere(3)
     b0 = icosphere(2)
-    b = Mesh(0.4 * b0.vertices + np.array([1.6, 0.3, -0.2]), b0.triangles)
-    trs, tes = nb.TraceSpace(b, tr), nb.TraceSpace(a, te)
-    dense = nb.bem.IntegralOperator(k, kap, trs, tes, e1, e2, 3, 20, 2.0, 1e-8, "dense", False)
-    hmat = nb.bem.IntegralOperator(k, kap, trs, tes, e1, e2, 3, 10, 2.0, 1e-8, "aca", False)
-    both = Mesh(np.vstack([a.vertices, b.vertices]), np.vstack([a.triangles, b.triangles + a.nv]))
-    Do = oracle.dense_matrix(k, both, tr, te, kappa=kap, trial_eval=e1, test_eval=e2, intorder=3)
-    rows = np.arange(tes.ndof)
-    cols = oracle.ndof(a, tr) + np.arange(trs.ndof)
-    Db = Do[np.ix_(rows, cols)]
-    D = dense.mat.to_dense()
-    assert D.shape == Db.shape and rel(D, Db) < 1e-10
-    assert hmat.mat.info["nfar"] > 0
-    cplx = hmat.mat.is_complex
     r = np.random.default_rng(6)
-    x = r.standard_normal(trs.ndof) + (1j * r.standard_normal(trs.ndof) if cplx else 0)
-    y = (hmat.mat * torch.from_numpy(x).cuda()).cpu().numpy()
-    assert rel(y, Db @ x) < 1e-6
-    z = r.standard_normal(tes.ndof) + (1j * r.standard_normal(tes.ndof) if cplx else 0)
-    yt = (hmat.mat.T * torch.from_numpy(z).cuda()).cpu().numpy()
-    assert rel(yt, Db.T @ z) < 1e-6
-    if k == "laplace_sl":
-        pts = np.array([[0.0, 0.0, 0.0], [3.0, 0.0, 0.0]])
-        p = hmat.GetPotential(torch.from_numpy(x).cuda())(torch.from_numpy(pts).cuda()).cpu().numpy()
-        po = oracle.potential(k, b, tr, x, pts, intorder=3)[:, 0]
-        assert rel(p, po) < 1e-11
+    for centre, method in (((1.6, 0.3, -0.2), "dense"), ((3.0, 0.3, -0.2), "aca")):
+        b = Mesh(0.4 * b0.vertices + np.array(centre), b0.triangles)
+        trs, tes = nb.TraceSpace(b, tr), nb.TraceSpace(a, te)
+        op = nb.bem.IntegralOperator(k, kap, trs, tes, e1, e2, 3, 10, 2.0, 1e-8, method, False)
+        Do = oracle.dense_matrix(k, _union(a, b), tr, te, kappa=kap, trial_eval=e1, test_eval=e2, intorder=3)
+        Db = Do[np.ix_(np.arange(tes.ndof), oracle.ndof(a, tr) + np.arange(trs.ndof))]
+        if method == "dense":
+            D = op.mat.to_dense()
+            assert D.shape == Db.shape and rel(D, Db) < 1e-10
+            continue
+        assert op.mat.info["nfar"] > 0
+        cplx = op.mat.is_complex
+        x = r.standard_normal(trs.ndof) + (1j * r.standard_normal(trs.ndof) if cplx else 0)
+        y = (op.mat * torch.from_numpy(x).cuda()).cpu().numpy()
+        assert rel(y, Db @ x) < 1e-6
+        z = r.standard_normal(tes.ndof) + (1j * r.standard_normal(tes.ndof) if cplx else 0)
+        yt = (op.mat.T * torch.from_numpy(z).cuda()).cpu().numpy()
+        assert rel(yt, Db.T @ z) < 1e-6
+        if k == "laplace_sl":
+            pts = np.array([[0.0, 0.0, 0.0], [4.0, 0.0, 0.0]])
+            p = op.GetPotential(torch.from_numpy(x).cuda())(torch.from_numpy(pts).cuda()).cpu().numpy()
+            po = oracle.potential(k, b, tr, x, pts, intorder=3)[:, 0]
+            assert rel(p, po) < 1e-11
