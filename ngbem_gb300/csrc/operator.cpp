@@ -61,6 +61,7 @@ struct NearPass {
 };
 
 void HOperator::merge_meshes() {
+  if (own_mesh) return;  // already merged: trial / test are the merged-mesh spaces
   trial_nt0 = trial->mesh->nt;
   test_nt0 = test->mesh->nt;
   if (trial->mesh == test->mesh) return;
