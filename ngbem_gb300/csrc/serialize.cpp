@@ -5,8 +5,9 @@
 // flags, every dense block (column-major) and every low-rank block's U2 and V2 factors in
 // their chunked device layouts, the operator description and its assembly summary.  Loading
 // rebuilds the cluster trees from the spaces (deterministic), checks them against the saved
-// permutations, uploads the blocks into fresh device pools and builds the work lists, so the
-// loaded operator applies exactly like the saved one.  Little-endian binary, version 1.
+// permutations and the dofs' elements / vertices / edges, uploads the blocks into fresh device
+// pools and builds the work lists, so the loaded operator applies exactly like the saved one.
+// Little-endian binary, version 1.
 #include <climits>
 #include <cstdio>
 #include <cstring>
@@ -93,6 +94,8 @@ void save_operator(const HOperator& op, const char* path) {
   put_v<int>(f, op.trial->mesh->nt);
   put_vec(f, op.ttrial->perm);
   put_vec(f, op.ttest->perm);
+  put_vec(f, op.trial->global_dof);  // which elements / vertices / edges the dofs are
+  put_vec(f, op.test->global_dof);
   put_vec(f, op.blocks);
   put_vec(f, op.block_rank);
   put_vec(f, op.block_fallback);
@@ -149,6 +152,9 @@ std::unique_ptr<HOperator> load_operator(const char* path, SpaceH* trial, SpaceH
   op->width = trial->ndof;
   const long long lim = 1LL << 34;
   const std::vector<int> perm_trial = get_vec<int>(f, lim), perm_test = get_vec<int>(f, lim);
+  const std::vector<int> gd_trial = get_vec<int>(f, lim), gd_test = get_vec<int>(f, lim);
+  if (gd_trial != trial->global_dof || gd_test != test->global_dof)
+    throw Error(BEM_ERR_ARG, "the spaces' dofs differ from the saved operator's (another region?)");
   // the trees are rebuilt from the spaces (the same deterministic construction as assembly)
   const bool dense_method = op->prm.method == BEM_METHOD_DENSE;
   const int leaf = dense_method ? INT_MAX : op->prm.leafsize;
