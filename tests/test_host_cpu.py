@@ -80,6 +80,33 @@ def test_argument_errors_are_status_codes():
     sp = nb.SurfaceL2(m)
     with pytest.raises(_lib.BemError):
         nb.cluster_tree(sp, 0)
+    # region spaces and operator regions
+    out = C.c_void_p()
+    assert _lib.lib.bem_space_create_on(None, 0, 0, None, C.byref(out)) == _lib.BEM_ERR_ARG
+    assert _lib.lib.bem_space_create_on(sp._mh.h, 9, 0, None, C.byref(out)) == _lib.BEM_ERR_ARG
+    none = np.zeros(m.nt, dtype=np.uint8)
+    assert _lib.lib.bem_space_create_on(sp._mh.h, 0, 0, C.c_void_p(none.ctypes.data), C.byref(out)) == \
+        _lib.BEM_ERR_ARG and b"no elements" in _lib.lib.bem_last_error()
+    assert _lib.lib.bem_space_global_dofs(None, None) == _lib.BEM_ERR_ARG
+    assert _lib.lib.bem_operator_set_definedon(None, None, None) == _lib.BEM_ERR_ARG
+
+
+def test_maxwell_factory_argument_checks():
+    """The HCurl space and the Maxwell double-layer / curl factories check their spaces before
+    any assembly (no GPU needed)."""
+    m = icosphere(1)
+    HC, RT, P0 = nb.HCurl(m), nb.HDivSurface(m), nb.SurfaceL2(m)
+    assert HC.ndof == RT.ndof and HC.kind == "HCURL"
+    with pytest.raises(TypeError):
+        nb.MaxwellDoubleLayerPotentialOperator(RT, RT, 1.0)
+    with pytest.raises(TypeError):
+        nb.MaxwellDoubleLayerPotentialOperator(HC, P0, 1.0)
+    with pytest.raises(TypeError):
+        nb.MaxwellSingleLayerPotentialOperatorCurl(RT, 1.0)
+    with pytest.raises(TypeError):
+        nb.MaxwellSingleLayerPotentialOperator(RT, None)
+    with pytest.raises(NotImplementedError):
+        nb.HCurl(m, order=1)
 
 
 def test_mesh_generators():
