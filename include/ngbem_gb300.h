@@ -115,6 +115,11 @@ int bem_space_create_on(bem_mesh_t mesh, int kind, int dual_mapping, const unsig
                         bem_space_t* out);
 /* dof -> element (P0), vertex (P1) or mesh edge (RT0, HCURL); out holds ndof entries */
 int bem_space_global_dofs(bem_space_t space, int* out);
+/* The dofs of every element (FESpace::GetDofNrs, as the reference reads them throughout
+ * src/ngbem.cpp): dofs holds 3 ints per element (P0: the element's dof in the first; -1 on
+ * elements outside the space's region); signs (may be null) the RT0 / HCURL orientation
+ * +1/-1 of the local edges (0,1), (1,2), (2,0). */
+int bem_space_element_dofs(bem_space_t space, int* dofs, int* signs);
 int bem_space_ndof(bem_space_t space, int* ndof);
 int bem_space_destroy(bem_space_t space);
 

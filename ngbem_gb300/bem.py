@@ -97,6 +97,15 @@ class TraceSpace:
         check(lib.bem_space_ndof(self.h, C.byref(n)))
         self.ndof = n.value
 
+    def element_dofs(self):
+        """(dofs, signs), each (nt, 3): the dofs of every triangle (FESpace::GetDofNrs; P0 uses
+        column 0; -1 off the space's region) and the RT0 / HCURL edge orientations."""
+        nt = self.mesh.nt
+        d = np.zeros((nt, 3), dtype=np.int32)
+        s = np.zeros((nt, 3), dtype=np.int32)
+        check(lib.bem_space_element_dofs(self.h, d.ctypes.data_as(_lib._ip), s.ctypes.data_as(_lib._ip)))
+        return d, s
+
     @property
     def global_dofs(self) -> np.ndarray:
         """dof -> element (P0), vertex (P1) or edge (RT0, HCURL) of the whole mesh.  A space on a

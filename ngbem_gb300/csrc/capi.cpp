@@ -99,6 +99,19 @@ int bem_space_global_dofs(bem_space_t space, int* out) {
   });
 }
 
+int bem_space_element_dofs(bem_space_t space, int* dofs, int* signs) {
+  return guarded([&] {
+    REQUIRE(space && dofs, "null argument");
+    const SpaceH& s = space->s;
+    const int nt = s.mesh->nt;
+    for (int e = 0; e < nt; ++e)
+      for (int k = 0; k < 3; ++k) {
+        dofs[3 * e + k] = (s.nd == 1 && k > 0) ? -1 : s.dofs[3 * e + k];
+        if (signs) signs[3 * e + k] = s.sign[3 * e + k];
+      }
+  });
+}
+
 int bem_space_ndof(bem_space_t space, int* ndof) {
   return guarded([&] {
     REQUIRE(space && ndof, "null argument");

@@ -11,7 +11,8 @@ import numpy as np
 
 from .meshes import Mesh
 
-__all__ = ["triangle_rule", "p1_load_vector", "p0_load_vector", "plane_wave_bm_source", "random_directions"]
+__all__ = ["triangle_rule", "load_vector", "p1_load_vector", "p0_load_vector", "plane_wave_bm_source",
+           "random_directions"]
 
 
 def triangle_rule(order: int):
@@ -62,6 +63,40 @@ def p0_load_vector(mesh: Mesh, f, order: int = 6) -> np.ndarray:
     if fv.ndim == 3:
         return np.einsum("q,tqm->tm", w, fv) * detj[:, None]
     return (fv @ w) * detj
+
+
+def load_vector(space, f, order: int = 6) -> np.ndarray:
+    """b_i = int f v_i over the space's triangles for the basis v_i of any trace space (the
+    role of LinearForm(f * v.Trace() * ds).Assemble() on that space; a space on a region
+    integrates over the region only).  P0 / P1: f(x, n) returns (nt, nq) or (nt, nq, m)
+    values.  RT0 / HCURL (the RT0 shape sigma (x - p_opp) / |J|, or n x it): f returns
+    (nt, nq, 3) vectors or (nt, nq, 3, m); b_i = int f . v_i.  P0 with the dual mapping uses
+    v = 1 / |J|."""
+    mesh = space.mesh
+    dofs, signs = space.element_dofs()
+    on = dofs[:, 0] >= 0
+    x, n, detj, lam, w = _geometry(mesh, order)
+    fv = np.asarray(f(x, n))
+    vector = space.kind in ("RT0", "HCURL")
+    multi = fv.ndim == (4 if vector else 3)
+    if not multi:
+        fv = fv[..., None]
+    out = np.zeros((space.ndof, fv.shape[-1]), dtype=np.result_type(fv.dtype, np.float64))
+    if space.kind == "P0":
+        scale = np.ones_like(detj) if space.dual_mapping else detj
+        np.add.at(out, dofs[on, 0], np.einsum("q,tqm->tm", w, fv)[on] * scale[on, None])
+    elif space.kind == "P1":
+        for a in range(3):
+            np.add.at(out, dofs[on, a], (np.einsum("q,tqm->tm", w * lam[:, a], fv) * detj[:, None])[on])
+    else:
+        P = mesh.vertices[mesh.triangles]
+        for k in range(3):
+            psi = signs[:, k, None, None] * (x - P[:, (k + 2) % 3][:, None, :]) / detj[:, None, None]
+            if space.kind == "HCURL":
+                psi = np.cross(n[:, None, :], psi)
+            contrib = np.einsum("q,tqcm,tqc->tm", w, fv, psi) * detj[:, None]
+            np.add.at(out, dofs[on, k], contrib[on])
+    return out if multi else out[:, 0]
 
 
 def plane_wave_bm_source(kappa: float, directions: np.ndarray):
