@@ -145,6 +145,24 @@ def dist_setup(args):
     return world, rank, local
 
 
+def max_over_ranks(values, device="cpu"):
+    """Element-wise maximum of a list of timings over all ranks of the process group (the
+    values themselves when there is no group): the whole job takes as long as its slowest
+    replica."""
+    import torch
+    if not (torch.distributed.is_available() and torch.distributed.is_initialized()):
+        return [float(v) for v in values]
+    t = torch.tensor([float(v) for v in values], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return [float(v) for v in t]
+
+
+def whole_job_rate(world, units_per_rank, seconds):
+    """Units processed by all ranks per second of the slowest rank (replicas: every rank does
+    the same work)."""
+    return world * units_per_rank / seconds
+
+
 # ---------------------------------------------------------------------------------------------
 def cpu_reference(level, nthreads=0, steps=20, warmup=2):
     """Oracle (FP64 C++ restatement of the reference, all host threads): assembly of V and
@@ -356,14 +374,9 @@ def run_ours(args):
     clocks = sampler.stop()
     e2e_check = float(np.linalg.norm(yh_np - y.cpu().numpy()) / np.linalg.norm(y.cpu().numpy()))
 
-    if world > 1:
-        tt = torch.tensor([dev_ms, sum(e2e_t)], dtype=torch.float64, device=dev)
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        dev_ms, e2e_sum = float(tt[0]), float(tt[1])
-    else:
-        e2e_sum = sum(e2e_t)
-    value = world * args.steps / (dev_ms / 1e3)
-    e2e_value = world * args.steps / e2e_sum
+    dev_ms, e2e_sum = max_over_ranks([dev_ms, sum(e2e_t)], dev)
+    value = whole_job_rate(world, args.steps, dev_ms / 1e3)
+    e2e_value = whole_job_rate(world, args.steps, e2e_sum)
 
     # ---- roofline of the dominant kernel (apply: dense near field + U2 t)
     import json as _j
@@ -485,13 +498,11 @@ def run_shape(args):
         a1.record()
         torch.cuda.synchronize()
         fw.append(a0.elapsed_time(a1))
-    if world > 1:
-        tt = torch.tensor([ms], dtype=torch.float64, device=dev)
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        ms = float(tt[0])
+    ms, = max_over_ranks([ms], dev)
     nq = 4
     pairs = info["regular_pairs"] + info["singular_pairs"]
-    line = {"metric": "batched SL energy + shape gradient (64 meshes) per second", "value": world * args.steps / (ms / 1e3),
+    line = {"metric": "batched SL energy + shape gradient (64 meshes) per second",
+            "value": whole_job_rate(world, args.steps, ms / 1e3),
             "unit": "batch/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32 (regular pairs) / f64 (singular pairs)", "data": "synthetic",
