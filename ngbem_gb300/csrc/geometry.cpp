@@ -8,6 +8,8 @@
 #include <thread>
 #include <atomic>
 #include <cmath>
+#include <condition_variable>
+#include <functional>
 #include <numeric>
 #include <unordered_map>
 
@@ -331,29 +333,82 @@ static void cluster_data(const SpaceH& sp, std::vector<double>& G, std::vector<s
   for (int i = 0; i < ndof; ++i) G[i] /= (double)cnt[i];
 }
 
-// Runs f(i) for i in [0, n) on up to 16 host threads (or inline when n is small).
-template <class F>
-static void parallel_for(int n, int min_per_thread, F&& f) {
-  const int nth = (int)std::min<unsigned>(16u, std::max(1u, std::thread::hardware_concurrency()));
-  const int use = std::min(nth, std::max(1, n / std::max(1, min_per_thread)));
-  if (use <= 1) {
-    for (int i = 0; i < n; ++i) f(i);
-    return;
+// cluster trees of at least this many dofs are built on a team of host threads
+static const int kTreeTeamMinDofs = 4096;
+
+// Host threads kept for the levels of one tree build (starting threads per level cost more
+// than a level's work at 20k dofs).  run(n, f) calls f(i) for i in [0, n) on the team and
+// the calling thread and returns when every call has returned.
+class LevelTeam {
+ public:
+  explicit LevelTeam(int workers) {
+    for (int t = 0; t < workers; ++t) th_.emplace_back([this] { loop(); });
   }
-  std::atomic<int> next{0};
-  std::vector<std::thread> th;
-  for (int t = 0; t < use; ++t)
-    th.emplace_back([&] {
-      for (int i = next++; i < n; i = next++) f(i);
-    });
-  for (auto& t : th) t.join();
+  ~LevelTeam() {
+    {
+      std::lock_guard<std::mutex> lk(mu_);
+      stop_ = true;
+      ++gen_;
+    }
+    cv_.notify_all();
+    for (auto& t : th_) t.join();
+  }
+  void run(int n, const std::function<void(int)>& f) {
+    {
+      std::lock_guard<std::mutex> lk(mu_);
+      job_ = &f;
+      n_ = n;
+      next_.store(0);
+      busy_ = (int)th_.size();
+      ++gen_;
+    }
+    cv_.notify_all();
+    work();
+    std::unique_lock<std::mutex> lk(mu_);
+    done_.wait(lk, [this] { return busy_ == 0; });
+    job_ = nullptr;
+  }
+
+ private:
+  void work() {
+    for (int i = next_++; i < n_; i = next_++) (*job_)(i);
+  }
+  void loop() {
+    long long seen = 0;
+    for (;;) {
+      {
+        std::unique_lock<std::mutex> lk(mu_);
+        cv_.wait(lk, [&] { return gen_ != seen; });
+        seen = gen_;
+        if (stop_) return;
+      }
+      work();
+      std::lock_guard<std::mutex> lk(mu_);
+      if (--busy_ == 0) done_.notify_one();
+    }
+  }
+  std::vector<std::thread> th_;
+  std::mutex mu_;
+  std::condition_variable cv_, done_;
+  const std::function<void(int)>* job_ = nullptr;
+  int n_ = 0, busy_ = 0;
+  long long gen_ = 0;
+  bool stop_ = false;
+  std::atomic<int> next_{0};
+};
+
+// a team for a tree of n dofs (null below kTreeTeamMinDofs or on one core)
+static std::unique_ptr<LevelTeam> make_tree_team(int n) {
+  const int hw = (int)std::min<unsigned>(16u, std::max(1u, std::thread::hardware_concurrency()));
+  if (n < kTreeTeamMinDofs || hw < 2) return nullptr;
+  return std::make_unique<LevelTeam>(hw - 1);
 }
 
 // PCA bisection tree (reference Rja_ClusterTree, src/hmat.cpp:155-407), breadth first.  The
 // clusters of one level own disjoint ranges of the permutation, so a level is split on parallel
 // threads; the children are then appended in cluster order, which gives the numbering of the
 // one-cluster-at-a-time traversal.  Each cluster's arithmetic is the serial one (bit-identical).
-void ClusterTreeH::build(const SpaceH& sp, int leafsize) {
+void ClusterTreeH::build(const SpaceH& sp, int leafsize, LevelTeam* team) {
   std::vector<double> G;
   std::vector<std::array<double, 3>> X;
   cluster_data(sp, G, X);
@@ -384,7 +439,7 @@ void ClusterTreeH::build(const SpaceH& sp, int leafsize) {
       mom[9] += G[j] * X[j][2] * X[j][2];
     }
     const double ctr[3] = {mom[1] / mom[0], mom[2] / mom[0], mom[3] / mom[0]};
-    std::vector<double> cov(9);
+    double cov[9];
     cov[0] = mom[4] - ctr[0] * mom[1];
     cov[1] = mom[5] - ctr[0] * mom[2];
     cov[2] = mom[6] - ctr[0] * mom[3];
@@ -394,12 +449,12 @@ void ClusterTreeH::build(const SpaceH& sp, int leafsize) {
     cov[6] = cov[2];
     cov[7] = cov[5];
     cov[8] = mom[9] - ctr[2] * mom[3];
-    std::vector<double> W, A;
-    sym_eigen(3, cov, W, A);
+    double W[3], A[9];
+    sym_eigen3(cov, W, A);
 
     int jmin = 0;
     double xmin[3] = {0, 0, 0}, xmax[3] = {0, 0, 0};
-    double radius = 0.0, dmin = 0.0;
+    double r2max = 0.0, dmin = 0.0;
     for (int i = b; i <= e; ++i) {
       const int j = perm[i];
       const double df[3] = {X[j][0] - ctr[0], X[j][1] - ctr[1], X[j][2] - ctr[2]};
@@ -407,7 +462,9 @@ void ClusterTreeH::build(const SpaceH& sp, int leafsize) {
       if (i == b || dist < dmin) { jmin = j; dmin = dist; }
       double xt[3];
       for (int r = 0; r < 3; ++r) xt[r] = A[3 * r] * df[0] + A[3 * r + 1] * df[1] + A[3 * r + 2] * df[2];
-      radius = std::fmax(radius, std::sqrt(xt[0] * xt[0] + xt[1] * xt[1] + xt[2] * xt[2]));
+      // max of the squares, one square root at the end: sqrt is monotone and correctly rounded,
+      // so this is the maximum of the square roots bit for bit
+      r2max = std::fmax(r2max, xt[0] * xt[0] + xt[1] * xt[1] + xt[2] * xt[2]);
       if (i == b) {
         for (int r = 0; r < 3; ++r) xmin[r] = xmax[r] = xt[r];
       } else {
@@ -417,6 +474,7 @@ void ClusterTreeH::build(const SpaceH& sp, int leafsize) {
         }
       }
     }
+    const double radius = std::sqrt(r2max);
     const double dg[3] = {xmax[0] - xmin[0], xmax[1] - xmin[1], xmax[2] - xmin[2]};
     {
       ClusterH& C = cl[ic];
@@ -453,15 +511,18 @@ void ClusterTreeH::build(const SpaceH& sp, int leafsize) {
     out.split = n1 > 0 && n2 > 0;
   };
   std::vector<Split> res;
+  // a team of threads for trees large enough to pay for starting it; a level runs on it when
+  // it has several clusters (the top levels have one, two, ... and stay on this thread)
+  std::unique_ptr<LevelTeam> own;
+  if (!team) {
+    own = make_tree_team(n);
+    team = own.get();
+  }
   for (size_t lo = 0; lo < cl.size();) {
     const size_t hi = cl.size();
     res.assign(hi - lo, Split{});
-    // threads only for levels with enough work to pay for starting them (measured: at 20k
-    // dofs a threaded build was slower on the 16-core host than the serial one)
-    long long lw = 0;
-    for (size_t ic = lo; ic < hi; ++ic) lw += cl[ic].Number;
-    if (hi - lo >= 32 && lw >= 65536)
-      parallel_for((int)(hi - lo), 2, [&](int k) { process(lo + k, res[k]); });
+    if (team && hi - lo >= 4)
+      team->run((int)(hi - lo), [&](int k) { process(lo + k, res[k]); });
     else
       for (size_t k = 0; k < hi - lo; ++k) process(lo + k, res[k]);
     for (size_t ic = lo; ic < hi; ++ic) {
@@ -485,16 +546,25 @@ void ClusterTreeH::build(const SpaceH& sp, int leafsize) {
   for (int k = 0; k < n; ++k) pinv[perm[k]] = k;
 }
 
-void ClusterTreeH::build_patches(const SpaceH& sp) {
+void ClusterTreeH::build_patches(const SpaceH& sp, LevelTeam* team) {
   const int nc = (int)cl.size();
+  std::unique_ptr<LevelTeam> own;
+  if (!team) {
+    own = make_tree_team(sp.ndof);
+    team = own.get();
+  }
+  auto run = [&](int n, const std::function<void(int)>& f) {
+    if (team && n >= 4) team->run(n, f);
+    else for (int i = 0; i < n; ++i) f(i);
+  };
   std::vector<std::vector<int>> pl(nc);
-  for (int c = nc - 1; c >= 0; --c) {
+  auto make = [&](int c) {
     const ClusterH& C = cl[c];
     std::vector<int>& out = pl[c];
     if (sp.kind == BEM_P0) {  // one element per dof, in cluster order
       out.resize(C.Number);
       for (long k = 0; k < C.Number; ++k) out[k] = sp.global_dof[perm[C.PermuPos + k]];
-      continue;
+      return;
     }
     if (C.Child1 >= 0) {
       const auto& a = pl[C.Child1];
@@ -509,13 +579,23 @@ void ClusterTreeH::build_patches(const SpaceH& sp) {
       std::sort(out.begin(), out.end());
       out.erase(std::unique(out.begin(), out.end()), out.end());
     }
+  };
+  // levels from the deepest up (children before their parents); clusters are numbered level
+  // by level, so a level is a contiguous range
+  std::vector<int> lstart;
+  for (int c = 0; c < nc; ++c)
+    if (c == 0 || cl[c].Level != cl[c - 1].Level) lstart.push_back(c);
+  lstart.push_back(nc);
+  for (int l = (int)lstart.size() - 2; l >= 0; --l) {
+    const int c0 = lstart[l];
+    run(lstart[l + 1] - c0, [&](int k) { make(c0 + k); });
   }
   patch_ptr.assign(nc + 1, 0);
   for (int c = 0; c < nc; ++c) patch_ptr[c + 1] = patch_ptr[c] + (int)pl[c].size();
   patch.resize(patch_ptr[nc]);
   patch_rad.assign(nc, 0.0);
   const MeshH& m = *sp.mesh;
-  for (int c = 0; c < nc; ++c) {
+  run(nc, [&](int c) {
     std::copy(pl[c].begin(), pl[c].end(), patch.begin() + patch_ptr[c]);
     double r2 = 0.0;
     for (int e : pl[c])
@@ -525,7 +605,7 @@ void ClusterTreeH::build_patches(const SpaceH& sp) {
         r2 = std::max(r2, dx * dx + dy * dy + dz * dz);
       }
     patch_rad[c] = std::sqrt(r2);
-  }
+  });
 }
 
 // ------------------------------------------------------------------------------------------
@@ -566,8 +646,9 @@ std::shared_ptr<ClusterTreeH> SpaceH::tree(int leafsize) {
   auto it = trees.find(leafsize);
   if (it != trees.end()) return it->second;
   auto t = std::make_shared<ClusterTreeH>();
-  t->build(*this, leafsize);
-  t->build_patches(*this);
+  std::unique_ptr<LevelTeam> team = make_tree_team(ndof);  // one team for both steps
+  t->build(*this, leafsize, team.get());
+  t->build_patches(*this, team.get());
   trees[leafsize] = t;
   return t;
 }

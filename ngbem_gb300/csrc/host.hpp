@@ -65,6 +65,7 @@ struct DevBuf {
 
 // ---- quadrature (quadrature.cpp) -------------------------------------------------------
 void sym_eigen(int n, std::vector<double> A, std::vector<double>& evals, std::vector<double>& evecs);
+void sym_eigen3(const double* A, double* evals, double* evecs);  // n = 3, same bits
 struct TrigRule { std::vector<double> xi, eta, w; };
 TrigRule make_trig_rule(int order);
 // Sauter-Schwab rule of a singularity class (0 identical, 1 common edge, 2 common vertex).
@@ -101,6 +102,7 @@ struct MeshH {
 };
 
 struct ClusterTreeH;
+class LevelTeam;  // host threads kept for the levels of a cluster-tree build (geometry.cpp)
 
 struct SpaceH {
   MeshH* mesh = nullptr;
@@ -137,8 +139,9 @@ struct ClusterTreeH {
   // element patches per cluster (elements touching a dof of the cluster)
   std::vector<int> patch_ptr, patch;
   std::vector<double> patch_rad;  // radius of the patch vertices around Centre
-  void build(const SpaceH& sp, int leafsize);
-  void build_patches(const SpaceH& sp);
+  // team: threads to split the work of a level on (null: a team of its own for large trees)
+  void build(const SpaceH& sp, int leafsize, LevelTeam* team = nullptr);
+  void build_patches(const SpaceH& sp, LevelTeam* team = nullptr);
 };
 
 struct BlockH {

@@ -74,6 +74,59 @@ void sym_eigen(int n, std::vector<double> A, std::vector<double>& evals, std::ve
   }
 }
 
+// The same cyclic Jacobi iteration for n = 3 on stack arrays (the cluster tree calls it once
+// per cluster): identical operations in the identical order, so identical bits, without the
+// heap traffic of the general version.
+void sym_eigen3(const double* A0, double* evals, double* evecs) {
+  double A[9], Vm[9] = {1, 0, 0, 0, 1, 0, 0, 0, 1};
+  for (int k = 0; k < 9; ++k) A[k] = A0[k];
+  for (int sweep = 0; sweep < 64; ++sweep) {
+    const double off = A[1] * A[1] + A[2] * A[2] + A[5] * A[5];
+    if (off == 0.0) break;
+    for (int p = 0; p < 2; ++p) {
+      for (int q = p + 1; q < 3; ++q) {
+        const double apq = A[p * 3 + q];
+        if (apq == 0.0) continue;
+        const double tau = (A[q * 3 + q] - A[p * 3 + p]) / (2.0 * apq);
+        const double t = (tau >= 0.0 ? 1.0 : -1.0) / (std::fabs(tau) + std::sqrt(1.0 + tau * tau));
+        const double c = 1.0 / std::sqrt(1.0 + t * t);
+        const double s = t * c;
+        const int r = 3 - p - q;  // the one row that is neither p nor q
+        const double arp = A[r * 3 + p], arq = A[r * 3 + q];
+        const double nrp = c * arp - s * arq;
+        const double nrq = s * arp + c * arq;
+        A[r * 3 + p] = nrp;
+        A[p * 3 + r] = nrp;
+        A[r * 3 + q] = nrq;
+        A[q * 3 + r] = nrq;
+        A[p * 3 + p] = A[p * 3 + p] - t * apq;
+        A[q * 3 + q] = A[q * 3 + q] + t * apq;
+        A[p * 3 + q] = 0.0;
+        A[q * 3 + p] = 0.0;
+        for (int k = 0; k < 3; ++k) {
+          const double vrp = Vm[k * 3 + p], vrq = Vm[k * 3 + q];
+          Vm[k * 3 + p] = c * vrp - s * vrq;
+          Vm[k * 3 + q] = s * vrp + c * vrq;
+        }
+      }
+    }
+  }
+  // stable ascending order of the diagonal (insertion sort moves only on a strict <)
+  int order[3] = {0, 1, 2};
+  for (int i = 1; i < 3; ++i)
+    for (int j = i; j > 0 && A[order[j] * 3 + order[j]] < A[order[j - 1] * 3 + order[j - 1]]; --j)
+      std::swap(order[j], order[j - 1]);
+  for (int k = 0; k < 3; ++k) {
+    const int col = order[k];
+    evals[k] = A[col * 3 + col];
+    int big = 0;
+    for (int r = 1; r < 3; ++r)
+      if (std::fabs(Vm[r * 3 + col]) > std::fabs(Vm[big * 3 + col])) big = r;
+    const double sg = Vm[big * 3 + col] < 0.0 ? -1.0 : 1.0;
+    for (int r = 0; r < 3; ++r) evecs[k * 3 + r] = sg * Vm[r * 3 + col];
+  }
+}
+
 // Gauss-Jacobi nodes and weights on [0,1] for the weight (1-u)^alpha u^beta.
 static void gauss_jacobi_unit(int n, double alpha, double beta, std::vector<double>& x, std::vector<double>& w) {
   std::vector<double> J(n * n, 0.0);
