@@ -21,8 +21,8 @@ CUDA_HOME = os.environ.get("CUDA_HOME", "/usr/local/cuda")
 NVCC = os.path.join(CUDA_HOME, "bin", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
-HOST_SOURCES = ["quadrature.cpp", "geometry.cpp", "operator.cpp", "energy_host.cpp", "tc_host.cpp", "serialize.cpp",
-                "capi.cpp"]
+HOST_SOURCES = ["quadrature.cpp", "geometry.cpp", "operator.cpp", "apply.cpp", "gmres.cpp", "energy_host.cpp",
+                "tc_host.cpp", "serialize.cpp", "capi.cpp"]
 CUDA_SOURCES = ["nearfield.cu", "aca.cu", "matvec.cu", "mult_noalloc.cu", "energy.cu", "gmres_batch.cu",
                 "tc_matvec.cu", "potential.cu"]
 HEADERS = ["bem_shared.h", "bem_device.cuh", "kernels.h", "host.hpp"]

@@ -125,6 +125,9 @@ struct SpaceH {
   std::map<int, std::shared_ptr<ClusterTreeH>> trees;
 };
 
+// device view of a space's dofs, signs and cluster positions (operator.cpp)
+SpaceDev space_dev(const SpaceH& s, int tr, const DevBuf& pinv);
+
 // ---- cluster tree and partition (geometry.cpp) -----------------------------------------
 struct ClusterH {
   long Level = 0, Parent = -1, Child1 = -1, Child2 = -1, Number = 0, PermuPos = 0, BasisElement = 0;
@@ -150,7 +153,7 @@ struct BlockH {
 };
 void partition_blocks(const ClusterTreeH& row, const ClusterTreeH& col, double eta, std::vector<BlockH>& out);
 
-// ---- operators (operator.cpp) ------------------------------------------------------------
+// ---- operators (assembly operator.cpp, products apply.cpp, solvers gmres.cpp) ---------------
 struct OperatorBase {
   virtual ~OperatorBase() = default;
   bool cplx = false;

@@ -1,5 +1,6 @@
-// Assembly and application of the H-matrix on the GPU (reference GenericIntegralOperator
-// ctor src/ngbem.cpp:314-330, CalcHMatrix :118-157, HMatrix src/hmat.cpp:614-681).
+// Assembly of the H-matrix on the GPU and its matvec work lists (reference
+// GenericIntegralOperator ctor src/ngbem.cpp:314-330, CalcHMatrix :118-157, HMatrix
+// src/hmat.cpp:614-621).  The products are in apply.cpp, the solvers in gmres.cpp.
 //
 // Assembly pipeline (one operator, two CUDA streams):
 //   host : cluster trees, element patches per cluster, partition, far blocks whose patches
@@ -39,7 +40,7 @@ struct StreamPair {
   }
 };
 
-static SpaceDev space_dev(const SpaceH& s, int tr, const DevBuf& pinv) {
+SpaceDev space_dev(const SpaceH& s, int tr, const DevBuf& pinv) {
   SpaceDev d;
   d.tr = tr;
   d.nd = s.nd;
@@ -993,862 +994,4 @@ void HOperator::build_mv_items(unsigned mask, bool multi, bool keep) {
   BEM_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
   mv_grid = nsm;
 }
-
-void HOperator::mult(int trans, const double* alpha, const void* x, const double* beta, void* y, int nrhs,
-                     cudaStream_t s) {
-  if (nrhs < 1) throw Error(BEM_ERR_ARG, "nrhs must be >= 1");
-  const int in_n = trans ? height : width;
-  const int out_n = trans ? width : height;
-  const int nmax = std::max(height, width);
-  const size_t dsz = cplx ? 16 : 8;                 // FP64 accumulators
-  const size_t xsz = (size_t)mv_x_bytes(prec, cplx);  // permuted input values
-  if (ws_nrhs < nrhs) {
-    d_xp.alloc((size_t)nmax * nrhs * xsz + 32);
-    d_yp.alloc((size_t)nmax * nrhs * dsz + 32);
-    d_t.alloc((size_t)std::max(t_len, 1) * nrhs * dsz + 32);
-    d_tx.alloc((size_t)std::max(t_len, 1) * nrhs * xsz + 32);
-    ws_nrhs = nrhs;
-    // the accumulators are zero between matvecs (see the single-launch kernel)
-    BEM_CUDA(cudaMemsetAsync(d_yp.p, 0, d_yp.bytes, s));
-    BEM_CUDA(cudaMemsetAsync(d_t.p, 0, d_t.bytes, s));
-    BEM_CUDA(cudaMemsetAsync(d_tx.p, 0, d_tx.bytes, s));
-  }
-  const int* pin = trans ? (ttest == ttrial ? d_perm_trial.as<int>() : d_perm_test.as<int>()) : d_perm_trial.as<int>();
-  const int* pout = trans ? d_perm_trial.as<int>() : (ttest == ttrial ? d_perm_trial.as<int>() : d_perm_test.as<int>());
-  std::array<cudaEvent_t, 5> ev{};
-  if (profiling) {
-    for (auto& e : ev) BEM_CUDA(cudaEventCreate(&e));
-    BEM_CUDA(cudaEventRecord(ev[0], s));
-  }
-  if (tc_eligible(trans, nrhs, s)) {
-    mult_tc(alpha, x, beta, y, nrhs, s);
-    return;
-  }
-  if (mv_fused && nrhs == 1) ensure_mv(trans ? 0xC0u : 0x30u, false, s);
-  else if (nrhs > 1 && !trans) ensure_mv(prec == 0 ? 0u : 0u, true, s);
-  else ensure_mv(trans ? 0x0Cu : 0x03u, false, s);
-  if (mv_fused && nrhs == 1) {
-    // one cooperative launch: permute, phase A, t -> input form, phase B, un-permute
-    MVFusedArgs f{};
-    f.a.xp = d_xp.p;
-    f.a.t = d_t.p;
-    f.a.tx = prec == 0 ? d_t.p : d_tx.p;
-    f.a.yp = d_yp.p;
-    f.a.nrhs = 1;
-    f.a.compensated = mv_compensated;
-    f.a.in_esz = cplx ? 16 : 8;
-    f.a.err = d_err.as<int>();
-    // plain FP32 arithmetic: t accumulates in FP32 in the high parts of its input form
-    f.a.t_f32 = (prec == 1 && !mv_compensated) ? 1 : 0;
-    const int p0 = trans ? 6 : 4;
-    for (int ph = 0; ph < 2; ++ph) {
-      f.items[ph] = d_items[p0 + ph].as<MVTItem>();
-      f.pieces[ph] = d_pieces[p0 + ph].as<MVPiece>();
-      f.ranges[ph] = d_ranges[p0 + ph].as<MVRange>();
-      f.nitems[ph] = n_items[p0 + ph];
-      f.ctr[ph] = d_sched.as<int>() + 2 + ph;
-    }
-    f.bar = (unsigned long long*)(d_sched.as<int>() + 4);
-    f.perm_in = pin;
-    f.n_in = in_n;
-    f.x = x;
-    f.perm_out = pout;
-    f.n_out = out_n;
-    f.y = y;
-    f.alpha[0] = alpha[0];
-    f.alpha[1] = alpha[1];
-    f.beta[0] = beta[0];
-    f.beta[1] = beta[1];
-    f.use_beta = (beta[0] != 0.0 || beta[1] != 0.0) ? 1 : 0;
-    f.t_len = t_len;
-    if (profiling) {
-      BEM_CUDA(cudaEventRecord(ev[1], s));
-      BEM_CUDA(cudaEventRecord(ev[2], s));
-    }
-    BEM_CUDA(launch_mv_fused(prec, cplx, f, s));
-    if (profiling) {
-      BEM_CUDA(cudaEventRecord(ev[3], s));
-      BEM_CUDA(cudaEventRecord(ev[4], s));
-      pending.push_back(ev);
-      pending_fused.push_back(true);
-    }
-    return;
-  }
-  launch_permute_in(prec, cplx, pin, in_n, nrhs, in_n, x, d_xp.p, s);
-  BEM_CUDA(cudaMemsetAsync(d_yp.p, 0, (size_t)out_n * nrhs * dsz, s));
-  if (profiling) BEM_CUDA(cudaEventRecord(ev[1], s));
-  MVArgs2 a{};
-  a.xp = d_xp.p;
-  a.t = d_t.p;
-  a.tx = prec == 0 ? d_t.p : d_tx.p;
-  a.yp = d_yp.p;
-  a.nrhs = nrhs;
-  a.compensated = mv_compensated;
-  a.in_esz = cplx ? 16 : 8;
-  a.err = d_err.as<int>();
-  a.sched = d_sched.as<int>();
-  if (t_len > 0) {
-    BEM_CUDA(cudaMemsetAsync(d_t.p, 0, (size_t)t_len * nrhs * dsz, s));
-    a.pass = trans ? 2 : 0;
-    a.items = d_items[a.pass].as<MVTItem>();
-    a.pieces = d_pieces[a.pass].as<MVPiece>();
-    a.ranges = d_ranges[a.pass].as<MVRange>();
-    a.nitems = n_items[a.pass];
-    if (nrhs > 1 && !trans) {
-      a.items = d_mr_items[0].as<MVTItem>();
-      a.pieces = d_mr_pieces[0].as<MVPiece>();
-      a.nitems = n_mr_items[0];
-      a.chunked = 1;
-    }
-    launch_mv_pass(prec, cplx, a, mv_grid, s);
-    launch_t_to_x(prec, cplx, d_t.p, d_tx.p, (long long)t_len * nrhs, s);
-  }
-  if (profiling) BEM_CUDA(cudaEventRecord(ev[2], s));
-  a.pass = trans ? 3 : 1;
-  a.items = d_items[a.pass].as<MVTItem>();
-  a.pieces = d_pieces[a.pass].as<MVPiece>();
-  a.ranges = d_ranges[a.pass].as<MVRange>();
-  a.nitems = n_items[a.pass];
-  a.chunked = 0;
-  if (nrhs > 1 && !trans && prec == 0) {
-    a.items = d_mr_items[1].as<MVTItem>();
-    a.pieces = d_mr_pieces[1].as<MVPiece>();
-    a.nitems = n_mr_items[1];
-    a.chunked = 1;
-    launch_mv_pass(prec, cplx, a, mv_grid, s);
-  } else if (nrhs > 1 && !trans) {
-    // FP32 storage, owner computes: each leaf row cluster sums its dense and U2 contributions
-    // and stores y (FP64 storage keeps the chunk pass: its wider accumulators favour it)
-    MVRowArgs ra{};
-    ra.leaves = d_ro_leaves.as<int4>();
-    ra.nleaves = n_ro_leaves;
-    ra.ents = d_ro_ents.as<int4>();
-    ra.dense = d_mvdense.as<MVDense>();
-    ra.lr = d_mvlr.as<LRDesc>();
-    ra.xp = d_xp.p;
-    ra.tx = prec == 0 ? d_t.p : d_tx.p;
-    ra.yp = d_yp.p;
-    ra.nrhs = nrhs;
-    ra.compensated = mv_compensated;
-    launch_mv_rowowner(prec, cplx, ra, s);
-  } else {
-    launch_mv_pass(prec, cplx, a, mv_grid, s);
-  }
-  if (profiling) BEM_CUDA(cudaEventRecord(ev[3], s));
-  launch_permute_out(cplx, pout, out_n, nrhs, out_n, alpha, beta, d_yp.p, y, s);
-  // leave the accumulators zero for the single-launch kernel
-  BEM_CUDA(cudaMemsetAsync(d_yp.p, 0, (size_t)out_n * nrhs * dsz, s));
-  if (t_len > 0) {
-    BEM_CUDA(cudaMemsetAsync(d_t.p, 0, (size_t)t_len * nrhs * dsz, s));
-    if (prec == 1) BEM_CUDA(cudaMemsetAsync(d_tx.p, 0, (size_t)t_len * nrhs * xsz, s));
-  }
-  if (profiling) {
-    BEM_CUDA(cudaEventRecord(ev[4], s));
-    pending.push_back(ev);
-    pending_fused.push_back(false);
-  }
-  BEM_CUDA(cudaGetLastError());
-}
-
-void HOperator::potential(const void* density, int npts, const double* pts, const double* normals, void* out,
-                          cudaStream_t s) {
-  const int dim = potential_dim(kid, trt);
-  if (dim == 0) throw Error(BEM_ERR_ARG, "no potential for this kernel and trial space");
-  if (npts < 0) throw Error(BEM_ERR_ARG, "npts must be >= 0");
-  if (kid == K_HELMHOLTZ_HS && !normals) throw Error(BEM_ERR_ARG, "this kernel needs the normals at the points");
-  MeshH& mesh = *trial->mesh;
-  mesh.ensure_device();
-  trial->ensure_device();
-  const int order_r = prm.intorder_regular > 0 ? prm.intorder_regular : prm.intorder;
-  MeshH::RuleTables& rt = mesh.rule_tables(order_r);
-  // source elements: the trial space's, within the trial definedon region when there is one
-  // (PotentialCF skips the elements outside it, src/ngbem.cpp:1205)
-  std::vector<int> el;
-  for (int e : trial->elems)
-    if (def_trial.empty() || def_trial[e]) el.push_back(e);
-  const bool all = (int)el.size() == mesh.nt;
-  DevBuf d_el;
-  if (!all && !el.empty()) d_el.upload(el, s);
-  const size_t nsrc = std::max<size_t>(1, el.size() * (size_t)rt.nq);
-  DevBuf src_pos, src_val;
-  src_pos.alloc(nsrc * 6 * sizeof(double));
-  src_val.alloc(nsrc * dim * (cplx ? 16 : 8));
-  PotArgs a{};
-  a.erec = rt.rec[0].p;
-  a.qoff = rt.qoff[0].p;
-  a.rq = rt.rq[0].as<double>();
-  a.elems = all ? nullptr : d_el.as<int>();
-  a.nt = (int)el.size();
-  a.nq = rt.nq;
-  a.trial = space_dev(*trial, trt, d_pinv_trial);
-  a.density = density;
-  a.src_pos = src_pos.as<double>();
-  a.src_val = src_val.p;
-  a.npts = npts;
-  a.pts = pts;
-  a.normals = normals;
-  a.kappa = kappa;
-  a.out = out;
-  if (!launch_potential(kid, trt, a, s)) throw Error(BEM_ERR_ARG, "no potential for this kernel and trial space");
-  BEM_CUDA(cudaGetLastError());
-  BEM_CUDA(cudaStreamSynchronize(s));
-}
-
-int HOperator::device_status() {
-  int e = 0;
-  BEM_CUDA(cudaMemcpy(&e, d_err.p, sizeof(int), cudaMemcpyDeviceToHost));
-  return e;
-}
-
-void HOperator::collect_profile() {
-  for (size_t i = 0; i < pending.size(); ++i) {
-    auto& ev = pending[i];
-    BEM_CUDA(cudaEventSynchronize(ev[4]));
-    for (int k = 0; k < 4; ++k) {
-      if (pending_fused[i] && k != 2) continue;  // one launch: its time is the apply slot
-      float t = 0.f;
-      BEM_CUDA(cudaEventElapsedTime(&t, ev[k], ev[k + 1]));
-      kms[k] += t;
-      kcount[k] += 1;
-    }
-    for (auto& e : ev) cudaEventDestroy(e);
-  }
-  pending.clear();
-  pending_fused.clear();
-}
-
-HOperator::~HOperator() {
-  for (auto& ev : pending)
-    for (auto& e : ev) cudaEventDestroy(e);
-}
-
-void HOperator::to_dense(void* out) {
-  const size_t esz = cplx ? 16 : 8;
-  const int chunk = std::min(width, 32);
-  DevBuf X, Y;
-  X.alloc((size_t)width * chunk * esz);
-  Y.alloc((size_t)height * chunk * esz);
-  std::vector<char> hx((size_t)width * chunk * esz), hy((size_t)height * chunk * esz);
-  const double one[2] = {1.0, 0.0}, zero[2] = {0.0, 0.0};
-  for (int c0 = 0; c0 < width; c0 += chunk) {
-    const int nc = std::min(chunk, width - c0);
-    std::fill(hx.begin(), hx.end(), 0);
-    for (int c = 0; c < nc; ++c) {
-      double* col = (double*)(hx.data() + (size_t)c * width * esz);
-      col[(size_t)(c0 + c) * (cplx ? 2 : 1)] = 1.0;
-    }
-    BEM_CUDA(cudaMemcpy(X.p, hx.data(), (size_t)width * nc * esz, cudaMemcpyHostToDevice));
-    mult(0, one, X.p, zero, Y.p, nc, 0);
-    BEM_CUDA(cudaMemcpy(hy.data(), Y.p, (size_t)height * nc * esz, cudaMemcpyDeviceToHost));
-    for (int c = 0; c < nc; ++c)
-      for (int r = 0; r < height; ++r)
-        std::memcpy((char*)out + ((size_t)r * width + c0 + c) * esz, hy.data() + ((size_t)c * height + r) * esz, esz);
-  }
-}
-
-// ---------------------------------------------------------------------------------------------
-// mass matrix <u, v> of identity traces, CSR in fp64 (rows = test dofs)
-void MassOperator::build(SpaceH* trial, SpaceH* test, bool complex_vectors) {
-  if (trial->mesh != test->mesh) throw Error(BEM_ERR_ARG, "mass matrix needs one mesh");
-  MeshH& m = *trial->mesh;
-  cplx = complex_vectors;
-  nrows = test->ndof;
-  ncols = trial->ndof;
-  height = nrows;
-  width = ncols;
-  TrigRule r = make_trig_rule(4);
-  const int nq = (int)r.w.size();
-  std::vector<std::vector<std::pair<int, double>>> rows(nrows);
-  auto shape = [&](const SpaceH& sp, int e, double xi, double eta, double S[3][3], int& dim) {
-    const ElemRec64& g = m.rec[e];
-    if (sp.kind == BEM_P0) { S[0][0] = sp.dual ? g.invdetJ : 1.0; dim = 1; return; }
-    if (sp.kind == BEM_P1) { S[0][0] = xi; S[1][0] = eta; S[2][0] = 1.0 - xi - eta; dim = 1; return; }
-    double x[3];
-    m.map(e, xi, eta, x);
-    for (int a = 0; a < 3; ++a) {
-      const int o = (a + 2) % 3;
-      double v[3];
-      for (int c = 0; c < 3; ++c) v[c] = sp.sign[3 * e + a] * (x[c] - g.p[o][c]) * g.invdetJ;
-      // HCurl trace: n x the RT0 shape of the same edge
-      for (int c = 0; c < 3; ++c)
-        S[a][c] = sp.kind == BEM_HCURL ? g.n[(c + 1) % 3] * v[(c + 2) % 3] - g.n[(c + 2) % 3] * v[(c + 1) % 3] : v[c];
-    }
-    dim = 3;
-  };
-  for (int e = 0; e < m.nt; ++e)
-    for (int q = 0; q < nq && trial->on(e) && test->on(e); ++q) {
-      double Si[3][3], Sj[3][3];
-      int di, dj;
-      shape(*test, e, r.xi[q], r.eta[q], Si, di);
-      shape(*trial, e, r.xi[q], r.eta[q], Sj, dj);
-      if (di != dj) throw Error(BEM_ERR_ARG, "mass matrix of scalar and vector spaces");
-      const double w = r.w[q] * m.rec[e].detJ;
-      for (int a = 0; a < test->nd; ++a)
-        for (int b = 0; b < trial->nd; ++b) {
-          double s = 0.0;
-          for (int c = 0; c < di; ++c) s += Si[a][c] * Sj[b][c];
-          rows[test->el_dofs(e)[a]].push_back({trial->el_dofs(e)[b], w * s});
-        }
-    }
-  h_rowptr.assign(nrows + 1, 0);
-  h_col.clear();
-  h_val.clear();
-  for (int i = 0; i < nrows; ++i) {
-    auto& rw = rows[i];
-    std::sort(rw.begin(), rw.end(), [](auto& a, auto& b) { return a.first < b.first; });
-    for (size_t k = 0; k < rw.size();) {
-      size_t l = k;
-      double s = 0.0;
-      while (l < rw.size() && rw[l].first == rw[k].first) s += rw[l++].second;
-      h_col.push_back(rw[k].first);
-      h_val.push_back(s);
-      k = l;
-    }
-    h_rowptr[i + 1] = (int)h_col.size();
-  }
-  rowptr.upload(h_rowptr);
-  col.upload(h_col);
-  val.upload(h_val);
-  BEM_CUDA(cudaDeviceSynchronize());
-}
-
-void MassOperator::mult(int trans, const double* alpha, const void* x, const double* beta, void* y, int nrhs,
-                        cudaStream_t s) {
-  launch_spmv(cplx, trans != 0, nrows, ncols, rowptr.as<int>(), col.as<int>(), val.as<double>(), alpha, beta,
-              x, y, nrhs, s);
-  BEM_CUDA(cudaGetLastError());
-}
-
-// ---------------------------------------------------------------------------------------------
-// GMRES(restart) with CGS2 Arnoldi in fp64; the operator application is a CUDA graph.
-static int gmres_impl(int nterms, OperatorBase* const* ops, const double* coef, const void* b, void* x, int maxiter,
-                      int restart, double tol, int* iters, double* resid, cudaStream_t s);
-
-// GMRES runs on a private stream (the legacy default stream cannot be captured into a graph),
-// ordered after the caller's stream on entry and before it on exit.
-int gmres_solve(int nterms, OperatorBase* const* ops, const double* coef, const void* b, void* x, int maxiter,
-                int restart, double tol, int* iters, double* resid, cudaStream_t caller) {
-  cudaStream_t s = nullptr;
-  cudaEvent_t e0 = nullptr, e1 = nullptr;
-  BEM_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
-  struct Guard {
-    cudaStream_t& s; cudaEvent_t& a; cudaEvent_t& b;
-    ~Guard() { if (a) cudaEventDestroy(a); if (b) cudaEventDestroy(b); if (s) cudaStreamDestroy(s); }
-  } guard{s, e0, e1};
-  BEM_CUDA(cudaEventCreateWithFlags(&e0, cudaEventDisableTiming));
-  BEM_CUDA(cudaEventCreateWithFlags(&e1, cudaEventDisableTiming));
-  BEM_CUDA(cudaEventRecord(e0, caller));
-  BEM_CUDA(cudaStreamWaitEvent(s, e0, 0));
-  int rc = gmres_impl(nterms, ops, coef, b, x, maxiter, restart, tol, iters, resid, s);
-  BEM_CUDA(cudaEventRecord(e1, s));
-  BEM_CUDA(cudaStreamWaitEvent(caller, e1, 0));
-  BEM_CUDA(cudaStreamSynchronize(s));
-  return rc;
-}
-
-// One restarted GMRES(restart) run on the operator replayed by `exec` (input gin, output
-// gout): x is the initial guess and the result; stops at ||b - A x|| <= tol * scale.
-struct GmresWS {
-  bool cplx = false;
-  int n = 0, restart = 0;
-  size_t esz = 8;
-  DevBuf Q, gin, gout, hdev, nrm, one;
-  cudaStream_t s = nullptr;
-  double dnorm(const void* v) {
-    launch_nrm2(cplx, n, v, nrm.as<double>(), s);
-    double h;
-    BEM_CUDA(cudaMemcpyAsync(&h, nrm.p, sizeof(double), cudaMemcpyDeviceToHost, s));
-    BEM_CUDA(cudaStreamSynchronize(s));
-    return h;
-  }
-  // r = b - A x into gout; returns ||r||
-  double residual(cudaGraphExec_t exec, const void* b, const void* x) {
-    BEM_CUDA(cudaMemcpyAsync(gin.p, x, (size_t)n * esz, cudaMemcpyDeviceToDevice, s));
-    BEM_CUDA(cudaGraphLaunch(exec, s));
-    launch_residual(cplx, n, b, gout.p, s);
-    return dnorm(gout.p);
-  }
-};
-
-static void gmres_run(GmresWS& w, cudaGraphExec_t exec, const void* b, void* x, int maxiter, double tol, double scale,
-                      int& it, double& rel) {
-  using C = std::complex<double>;
-  const int n = w.n, restart = w.restart;
-  const size_t esz = w.esz;
-  const bool cplx = w.cplx;
-  cudaStream_t s = w.s;
-  char* Qp = (char*)w.Q.p;
-  it = 0;
-  rel = 0.0;
-  for (;;) {
-    const double beta = w.residual(exec, b, x);
-    rel = beta / scale;
-    if (rel <= tol || it >= maxiter || beta == 0.0) break;
-    launch_scale_copy(cplx, n, w.gout.p, 1.0 / beta, Qp, s);
-    std::vector<C> H((size_t)(restart + 1) * restart, C(0)), cs(restart), sn(restart), g(restart + 1, C(0));
-    g[0] = beta;
-    int j = 0;
-    for (; j < restart && it < maxiter; ++j, ++it) {
-      BEM_CUDA(cudaMemcpyAsync(w.gin.p, Qp + (size_t)j * n * esz, (size_t)n * esz, cudaMemcpyDeviceToDevice, s));
-      BEM_CUDA(cudaGraphLaunch(exec, s));
-      std::vector<C> h(j + 1, C(0));
-      for (int pass = 0; pass < 2; ++pass) {
-        launch_gemv_ct(cplx, n, j + 1, w.Q.p, w.gout.p, w.hdev.p, s);
-        launch_gemv_sub(cplx, n, j + 1, w.Q.p, w.hdev.p, w.gout.p, s);
-        std::vector<double> hh((size_t)(j + 1) * (cplx ? 2 : 1));
-        BEM_CUDA(cudaMemcpyAsync(hh.data(), w.hdev.p, hh.size() * 8, cudaMemcpyDeviceToHost, s));
-        BEM_CUDA(cudaStreamSynchronize(s));
-        for (int i = 0; i <= j; ++i) h[i] += cplx ? C(hh[2 * i], hh[2 * i + 1]) : C(hh[i], 0.0);
-      }
-      const double hn = w.dnorm(w.gout.p);
-      if (hn > 0.0) launch_scale_copy(cplx, n, w.gout.p, 1.0 / hn, Qp + (size_t)(j + 1) * n * esz, s);
-      for (int i = 0; i <= j; ++i) H[(size_t)i * restart + j] = h[i];
-      H[(size_t)(j + 1) * restart + j] = hn;
-      for (int i = 0; i < j; ++i) {
-        C a = H[(size_t)i * restart + j], c2 = H[(size_t)(i + 1) * restart + j];
-        H[(size_t)i * restart + j] = std::conj(cs[i]) * a + std::conj(sn[i]) * c2;
-        H[(size_t)(i + 1) * restart + j] = -sn[i] * a + cs[i] * c2;
-      }
-      C a = H[(size_t)j * restart + j], c2 = H[(size_t)(j + 1) * restart + j];
-      const double den = std::sqrt(std::norm(a) + std::norm(c2));
-      if (den == 0.0) { cs[j] = 1.0; sn[j] = 0.0; }
-      else { cs[j] = a / den; sn[j] = c2 / den; }
-      H[(size_t)j * restart + j] = std::conj(cs[j]) * a + std::conj(sn[j]) * c2;
-      H[(size_t)(j + 1) * restart + j] = 0.0;
-      g[j + 1] = -sn[j] * g[j];
-      g[j] = std::conj(cs[j]) * g[j];
-      rel = std::abs(g[j + 1]) / scale;
-      if (rel <= tol || hn == 0.0) { ++j; ++it; break; }
-    }
-    const int k = j;
-    std::vector<C> yv(k, C(0));
-    for (int i = k - 1; i >= 0; --i) {
-      C sacc = g[i];
-      for (int l = i + 1; l < k; ++l) sacc -= H[(size_t)i * restart + l] * yv[l];
-      yv[i] = sacc / H[(size_t)i * restart + i];
-    }
-    std::vector<double> yh((size_t)k * (cplx ? 2 : 1));
-    for (int i = 0; i < k; ++i) {
-      if (cplx) { yh[2 * i] = yv[i].real(); yh[2 * i + 1] = yv[i].imag(); }
-      else yh[i] = yv[i].real();
-    }
-    BEM_CUDA(cudaMemcpyAsync(w.hdev.p, yh.data(), yh.size() * 8, cudaMemcpyHostToDevice, s));
-    launch_axpy_basis(cplx, n, k, w.Q.p, w.hdev.p, x, s);
-    BEM_CUDA(cudaStreamSynchronize(s));
-    if (rel <= tol || it >= maxiter) {
-      rel = w.residual(exec, b, x) / scale;
-      break;
-    }
-  }
-}
-
-// GMRES for sum_k coef[k] ops[k].  When an operator stores its blocks in FP32, the solve is a
-// GMRES-based iterative refinement: the Krylov iterations apply the plain FP32 matvec, each
-// outer step recomputes the residual with the error-free (compensated) matvec and corrects x,
-// so the final residual reaches the tolerance for the stored operator.
-static int gmres_impl(int nterms, OperatorBase* const* ops, const double* coef, const void* b, void* x, int maxiter,
-                      int restart, double tol, int* iters, double* resid, cudaStream_t s) {
-  if (nterms < 1) throw Error(BEM_ERR_ARG, "gmres needs at least one operator");
-  const int n = ops[0]->height;
-  bool cplx = false, mixed = false;
-  std::vector<HOperator*> hops;
-  for (int k = 0; k < nterms; ++k) {
-    if (ops[k]->height != n || ops[k]->width != n) throw Error(BEM_ERR_ARG, "gmres operators must be square and equal-sized");
-    cplx = cplx || ops[k]->cplx || coef[2 * k + 1] != 0.0;
-    if (auto* h = dynamic_cast<HOperator*>(ops[k])) {
-      hops.push_back(h);
-      mixed = mixed || h->prec == 1;
-    }
-  }
-  for (int k = 0; k < nterms; ++k)
-    if (ops[k]->cplx != cplx)
-      throw Error(BEM_ERR_ARG, "gmres operators must all act on real or all on complex vectors");
-  restart = std::max(1, std::min(restart, maxiter > 0 ? maxiter : restart));
-  GmresWS w;
-  w.cplx = cplx;
-  w.n = n;
-  w.restart = restart;
-  w.esz = cplx ? 16 : 8;
-  w.s = s;
-  w.Q.alloc((size_t)n * (restart + 1) * w.esz);
-  w.gin.alloc((size_t)n * w.esz);
-  w.gout.alloc((size_t)n * w.esz);
-  w.hdev.alloc((size_t)(restart + 2) * w.esz);
-  w.nrm.alloc(sizeof(double));
-  const double onev[2] = {1.0, 0.0};
-  w.one.alloc(16);
-  BEM_CUDA(cudaMemcpy(w.one.p, onev, 16, cudaMemcpyHostToDevice));
-  const double zero[2] = {0.0, 0.0}, one[2] = {1.0, 0.0};
-  std::vector<int> saved;
-  for (auto* h : hops) saved.push_back(h->mv_compensated);
-  struct Restore {
-    std::vector<HOperator*>& h;
-    std::vector<int>& v;
-    ~Restore() { for (size_t i = 0; i < h.size(); ++i) h[i]->mv_compensated = v[i]; }
-  } restore{hops, saved};
-  auto capture = [&](int compensated, cudaGraph_t& g, cudaGraphExec_t& e) {
-    for (auto* h : hops) h->mv_compensated = compensated;
-    auto apply = [&]() {
-      for (int k = 0; k < nterms; ++k) ops[k]->mult(0, coef + 2 * k, w.gin.p, k == 0 ? zero : one, w.gout.p, 1, s);
-    };
-    apply();  // allocates the operators' workspaces outside the capture
-    BEM_CUDA(cudaStreamSynchronize(s));
-    BEM_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-    apply();
-    BEM_CUDA(cudaStreamEndCapture(s, &g));
-    BEM_CUDA(cudaGraphInstantiate(&e, g, 0));
-  };
-  struct GraphGuard {
-    cudaGraph_t g = nullptr;
-    cudaGraphExec_t e = nullptr;
-    ~GraphGuard() { if (e) cudaGraphExecDestroy(e); if (g) cudaGraphDestroy(g); }
-  } acc, fast;
-  capture(1, acc.g, acc.e);
-  const double bnorm = w.dnorm(b);
-  const double scale = bnorm > 0.0 ? bnorm : 1.0;
-  int it = 0;
-  double rel = 0.0;
-  if (!mixed) {
-    gmres_run(w, acc.e, b, x, maxiter, tol, scale, it, rel);
-  } else {
-    capture(0, fast.g, fast.e);
-    DevBuf r, e;
-    r.alloc((size_t)n * w.esz);
-    e.alloc((size_t)n * w.esz);
-    for (int outer = 0; outer < 50; ++outer) {
-      rel = w.residual(acc.e, b, x) / scale;
-      if (rel <= tol || it >= maxiter) break;
-      BEM_CUDA(cudaMemcpyAsync(r.p, w.gout.p, (size_t)n * w.esz, cudaMemcpyDeviceToDevice, s));
-      BEM_CUDA(cudaMemsetAsync(e.p, 0, (size_t)n * w.esz, s));
-      // the inner solve reduces the residual to what the outer step still needs, but not
-      // below the rounding level of the FP32 matvec
-      const double inner_tol = std::max(0.5 * tol / rel, 1e-6);
-      int iit = 0;
-      double irel = 0.0;
-      gmres_run(w, fast.e, r.p, e.p, maxiter - it, inner_tol, rel * scale, iit, irel);
-      it += std::max(iit, 1);
-      launch_axpy_basis(cplx, n, 1, e.p, w.one.p, x, s);  // x += e
-    }
-  }
-  BEM_CUDA(cudaStreamSynchronize(s));
-  if (iters) *iters = it;
-  if (resid) *resid = rel;
-  return BEM_OK;
-}
-
-}  // namespace bem
-
-namespace bem {
-
-// ---------------------------------------------------------------------------------------------
-// Batched GMRES: nrhs independent systems sum_k coef[k] ops[k] x_r = b_r advanced in lockstep,
-// so that each Arnoldi step applies the operators once to all right-hand sides (the H-matrix is
-// streamed once per step for all of them).  FP64 CGS2 Arnoldi per column, Givens rotations and
-// least squares per column on the host; a column stops extending its Krylov space once it has
-// converged.  With FP32-stored operators: iterative refinement as in gmres_impl.
-struct BGmresWS {
-  bool cplx = false;
-  int n = 0, nrhs = 0, restart = 0;
-  size_t esz = 8;
-  DevBuf Q, gin, gout, hdev, nrm, inv;
-  cudaStream_t s = nullptr;
-  size_t block() const { return (size_t)n * nrhs * esz; }
-  std::vector<double> norms(const void* v) {
-    launch_bnrm2(cplx, n, nrhs, v, nrm.as<double>(), s);
-    std::vector<double> h(nrhs);
-    BEM_CUDA(cudaMemcpyAsync(h.data(), nrm.p, nrhs * sizeof(double), cudaMemcpyDeviceToHost, s));
-    BEM_CUDA(cudaStreamSynchronize(s));
-    return h;
-  }
-  std::vector<double> residual(cudaGraphExec_t exec, const void* b, const void* x) {
-    BEM_CUDA(cudaMemcpyAsync(gin.p, x, block(), cudaMemcpyDeviceToDevice, s));
-    BEM_CUDA(cudaGraphLaunch(exec, s));
-    launch_residual(cplx, n * nrhs, b, gout.p, s);
-    return norms(gout.p);
-  }
-  void scale_into(const void* w, const std::vector<double>& f, void* q) {
-    BEM_CUDA(cudaMemcpyAsync(inv.p, f.data(), nrhs * sizeof(double), cudaMemcpyHostToDevice, s));
-    launch_bscale(cplx, n, nrhs, w, inv.as<double>(), q, s);
-  }
-};
-
-static void bgmres_run(BGmresWS& w, cudaGraphExec_t exec, const void* b, void* x, int maxiter, double tol,
-                       const std::vector<double>& scale, int& it, std::vector<double>& rel) {
-  using C = std::complex<double>;
-  const int n = w.n, R = w.nrhs, restart = w.restart;
-  const bool cplx = w.cplx;
-  cudaStream_t s = w.s;
-  char* Qp = (char*)w.Q.p;
-  it = 0;
-  rel.assign(R, 0.0);
-  for (;;) {
-    std::vector<double> beta = w.residual(exec, b, x);
-    bool done = true;
-    for (int r = 0; r < R; ++r) {
-      rel[r] = beta[r] / scale[r];
-      if (rel[r] > tol && beta[r] > 0.0) done = false;
-    }
-    if (done || it >= maxiter) break;
-    std::vector<double> f(R);
-    for (int r = 0; r < R; ++r) f[r] = beta[r] > 0.0 ? 1.0 / beta[r] : 0.0;
-    w.scale_into(w.gout.p, f, Qp);
-    std::vector<C> H((size_t)R * (restart + 1) * restart, C(0)), cs((size_t)R * restart), sn((size_t)R * restart),
-        g((size_t)R * (restart + 1), C(0));
-    std::vector<int> kr(R, 0);
-    std::vector<char> active(R, 0);
-    for (int r = 0; r < R; ++r) {
-      g[(size_t)r * (restart + 1)] = beta[r];
-      active[r] = rel[r] > tol && beta[r] > 0.0;
-    }
-    auto Hs = [&](int r, int i, int j) -> C& { return H[((size_t)r * (restart + 1) + i) * restart + j]; };
-    int j = 0;
-    for (; j < restart && it < maxiter; ++j, ++it) {
-      BEM_CUDA(cudaMemcpyAsync(w.gin.p, Qp + (size_t)j * w.block(), w.block(), cudaMemcpyDeviceToDevice, s));
-      BEM_CUDA(cudaGraphLaunch(exec, s));
-      std::vector<C> h((size_t)(j + 1) * R, C(0));
-      for (int pass = 0; pass < 2; ++pass) {
-        launch_bgemv_ct(cplx, n, j + 1, R, w.Q.p, w.gout.p, w.hdev.p, s);
-        launch_bgemv_sub(cplx, n, j + 1, R, w.Q.p, w.hdev.p, w.gout.p, s);
-        std::vector<double> hh((size_t)(j + 1) * R * (cplx ? 2 : 1));
-        BEM_CUDA(cudaMemcpyAsync(hh.data(), w.hdev.p, hh.size() * 8, cudaMemcpyDeviceToHost, s));
-        BEM_CUDA(cudaStreamSynchronize(s));
-        for (size_t q = 0; q < h.size(); ++q) h[q] += cplx ? C(hh[2 * q], hh[2 * q + 1]) : C(hh[q], 0.0);
-      }
-      const std::vector<double> hn = w.norms(w.gout.p);
-      std::vector<double> fi(R);
-      for (int r = 0; r < R; ++r) fi[r] = hn[r] > 0.0 ? 1.0 / hn[r] : 0.0;
-      w.scale_into(w.gout.p, fi, Qp + (size_t)(j + 1) * w.block());
-      bool any = false;
-      for (int r = 0; r < R; ++r) {
-        if (!active[r]) continue;
-        for (int i = 0; i <= j; ++i) Hs(r, i, j) = h[(size_t)i * R + r];
-        Hs(r, j + 1, j) = hn[r];
-        C* csr = &cs[(size_t)r * restart];
-        C* snr = &sn[(size_t)r * restart];
-        C* gr = &g[(size_t)r * (restart + 1)];
-        for (int i = 0; i < j; ++i) {
-          const C a = Hs(r, i, j), c2 = Hs(r, i + 1, j);
-          Hs(r, i, j) = std::conj(csr[i]) * a + std::conj(snr[i]) * c2;
-          Hs(r, i + 1, j) = -snr[i] * a + csr[i] * c2;
-        }
-        const C a = Hs(r, j, j), c2 = Hs(r, j + 1, j);
-        const double den = std::sqrt(std::norm(a) + std::norm(c2));
-        if (den == 0.0) { csr[j] = 1.0; snr[j] = 0.0; }
-        else { csr[j] = a / den; snr[j] = c2 / den; }
-        Hs(r, j, j) = std::conj(csr[j]) * a + std::conj(snr[j]) * c2;
-        Hs(r, j + 1, j) = 0.0;
-        gr[j + 1] = -snr[j] * gr[j];
-        gr[j] = std::conj(csr[j]) * gr[j];
-        kr[r] = j + 1;
-        rel[r] = std::abs(gr[j + 1]) / scale[r];
-        if (rel[r] <= tol || hn[r] == 0.0) active[r] = 0;
-        any = any || active[r];
-      }
-      if (!any) { ++j; ++it; break; }
-    }
-    // per-column least squares over its own Krylov dimension
-    const int kmax = *std::max_element(kr.begin(), kr.end());
-    std::vector<double> yh((size_t)kmax * R * (cplx ? 2 : 1), 0.0);
-    for (int r = 0; r < R; ++r) {
-      const int k = kr[r];
-      std::vector<C> yv(k, C(0));
-      for (int i = k - 1; i >= 0; --i) {
-        C sacc = g[(size_t)r * (restart + 1) + i];
-        for (int l = i + 1; l < k; ++l) sacc -= Hs(r, i, l) * yv[l];
-        yv[i] = sacc / Hs(r, i, i);
-      }
-      for (int i = 0; i < k; ++i) {
-        const size_t q = (size_t)i * R + r;
-        if (cplx) { yh[2 * q] = yv[i].real(); yh[2 * q + 1] = yv[i].imag(); }
-        else yh[q] = yv[i].real();
-      }
-    }
-    if (kmax > 0) {
-      BEM_CUDA(cudaMemcpyAsync(w.hdev.p, yh.data(), yh.size() * 8, cudaMemcpyHostToDevice, s));
-      launch_baxpy_basis(cplx, n, kmax, R, w.Q.p, w.hdev.p, x, s);
-    }
-    BEM_CUDA(cudaStreamSynchronize(s));
-    bool conv = true;
-    for (int r = 0; r < R; ++r) conv = conv && rel[r] <= tol;
-    if (conv || it >= maxiter) {
-      const std::vector<double> fin = w.residual(exec, b, x);
-      for (int r = 0; r < R; ++r) rel[r] = fin[r] / scale[r];
-      break;
-    }
-  }
-}
-
-int gmres_batched_solve(int nterms, OperatorBase* const* ops, const double* coef, int nrhs, const void* b, void* x,
-                        int maxiter, int restart, double tol, int* iters, double* resid, cudaStream_t caller) {
-  if (nterms < 1) throw Error(BEM_ERR_ARG, "gmres needs at least one operator");
-  if (nrhs < 1) throw Error(BEM_ERR_ARG, "nrhs must be >= 1");
-  const int n = ops[0]->height;
-  bool cplx = false, mixed = false;
-  std::vector<HOperator*> hops;
-  for (int k = 0; k < nterms; ++k) {
-    if (ops[k]->height != n || ops[k]->width != n) throw Error(BEM_ERR_ARG, "gmres operators must be square and equal-sized");
-    cplx = cplx || ops[k]->cplx || coef[2 * k + 1] != 0.0;
-    if (auto* h = dynamic_cast<HOperator*>(ops[k])) {
-      hops.push_back(h);
-      mixed = mixed || h->prec == 1;
-    }
-  }
-  for (int k = 0; k < nterms; ++k)
-    if (ops[k]->cplx != cplx) throw Error(BEM_ERR_ARG, "gmres operators must all act on real or all on complex vectors");
-  restart = std::max(1, std::min(restart, maxiter > 0 ? maxiter : restart));
-  cudaStream_t s = nullptr;
-  cudaEvent_t e0 = nullptr, e1 = nullptr;
-  BEM_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
-  struct Guard {
-    cudaStream_t& s; cudaEvent_t& a; cudaEvent_t& b;
-    ~Guard() { if (a) cudaEventDestroy(a); if (b) cudaEventDestroy(b); if (s) cudaStreamDestroy(s); }
-  } guard{s, e0, e1};
-  BEM_CUDA(cudaEventCreateWithFlags(&e0, cudaEventDisableTiming));
-  BEM_CUDA(cudaEventCreateWithFlags(&e1, cudaEventDisableTiming));
-  BEM_CUDA(cudaEventRecord(e0, caller));
-  BEM_CUDA(cudaStreamWaitEvent(s, e0, 0));
-  BGmresWS w;
-  w.cplx = cplx;
-  w.n = n;
-  w.nrhs = nrhs;
-  w.restart = restart;
-  w.esz = cplx ? 16 : 8;
-  w.s = s;
-  w.Q.alloc(w.block() * (restart + 1));
-  w.gin.alloc(w.block());
-  w.gout.alloc(w.block());
-  w.hdev.alloc((size_t)(restart + 2) * nrhs * w.esz);
-  w.nrm.alloc(nrhs * sizeof(double));
-  w.inv.alloc(nrhs * sizeof(double));
-  const double zero[2] = {0.0, 0.0}, one[2] = {1.0, 0.0};
-  std::vector<int> saved;
-  for (auto* h : hops) saved.push_back(h->mv_compensated);
-  struct Restore {
-    std::vector<HOperator*>& h;
-    std::vector<int>& v;
-    ~Restore() { for (size_t i = 0; i < h.size(); ++i) h[i]->mv_compensated = v[i]; }
-  } restore{hops, saved};
-  struct GraphGuard {
-    cudaGraph_t g = nullptr;
-    cudaGraphExec_t e = nullptr;
-    ~GraphGuard() { if (e) cudaGraphExecDestroy(e); if (g) cudaGraphDestroy(g); }
-  } acc, fast;
-  auto capture = [&](int compensated, GraphGuard& gg) {
-    for (auto* h : hops) h->mv_compensated = compensated;
-    auto apply = [&]() {
-      for (int k = 0; k < nterms; ++k)
-        ops[k]->mult(0, coef + 2 * k, w.gin.p, k == 0 ? zero : one, w.gout.p, nrhs, s);
-    };
-    apply();  // allocates the operators' workspaces outside the capture
-    BEM_CUDA(cudaStreamSynchronize(s));
-    BEM_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-    apply();
-    BEM_CUDA(cudaStreamEndCapture(s, &gg.g));
-    BEM_CUDA(cudaGraphInstantiate(&gg.e, gg.g, 0));
-  };
-  capture(1, acc);
-  std::vector<double> scale = w.norms(b);
-  for (double& v : scale) v = v > 0.0 ? v : 1.0;
-  int it = 0;
-  std::vector<double> rel(nrhs, 0.0);
-  if (!mixed) {
-    bgmres_run(w, acc.e, b, x, maxiter, tol, scale, it, rel);
-  } else {
-    capture(0, fast);
-    DevBuf r, e, onev;
-    r.alloc(w.block());
-    e.alloc(w.block());
-    std::vector<double> ones((size_t)nrhs * (cplx ? 2 : 1), 0.0);
-    for (int q = 0; q < nrhs; ++q) ones[(size_t)q * (cplx ? 2 : 1)] = 1.0;
-    onev.upload(ones, s);
-    for (int outer = 0; outer < 50; ++outer) {
-      const std::vector<double> res = w.residual(acc.e, b, x);
-      double worst = 0.0;
-      std::vector<double> inner_scale(nrhs);
-      for (int q = 0; q < nrhs; ++q) {
-        rel[q] = res[q] / scale[q];
-        worst = std::max(worst, rel[q]);
-        inner_scale[q] = res[q] > 0.0 ? res[q] : 1.0;
-      }
-      if (worst <= tol || it >= maxiter) break;
-      BEM_CUDA(cudaMemcpyAsync(r.p, w.gout.p, w.block(), cudaMemcpyDeviceToDevice, s));
-      BEM_CUDA(cudaMemsetAsync(e.p, 0, w.block(), s));
-      const double inner_tol = std::max(0.5 * tol / worst, 1e-6);
-      int iit = 0;
-      std::vector<double> irel;
-      bgmres_run(w, fast.e, r.p, e.p, maxiter - it, inner_tol, inner_scale, iit, irel);
-      it += std::max(iit, 1);
-      launch_baxpy_basis(cplx, n, 1, nrhs, e.p, onev.p, x, s);  // x += e (column-wise weight 1)
-    }
-  }
-  BEM_CUDA(cudaStreamSynchronize(s));
-  BEM_CUDA(cudaEventRecord(e1, s));
-  BEM_CUDA(cudaStreamWaitEvent(caller, e1, 0));
-  if (iters) *iters = it;
-  if (resid)
-    for (int q = 0; q < nrhs; ++q) resid[q] = rel[q];
-  return BEM_OK;
-}
-
-}  // namespace bem
-
-namespace bem {
-
-// Picks the matvec work decomposition for this operator by timing it: the piece size (stored
-// elements per consumer-warp task, which also shapes the work items) and the schedule (one
-// cooperative launch, or the four-pass pipeline).  Each candidate is timed over `reps`
-// matvecs with CUDA events after a warm-up; the fastest is kept.
-double HOperator::autotune(int reps, int* best_piece, int* best_fused) {
-  if (reps < 1) reps = 1;
-  const int cand[] = {256, 384, 512, 768, 1024, 1536, 2048};
-  const size_t esz = cplx ? 16 : 8;
-  DevBuf x, y;
-  x.alloc((size_t)width * esz);
-  y.alloc((size_t)height * esz);
-  BEM_CUDA(cudaMemset(x.p, 0, (size_t)width * esz));
-  cudaStream_t s = nullptr;
-  cudaEvent_t e0 = nullptr, e1 = nullptr;
-  BEM_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
-  struct Guard {
-    cudaStream_t& s; cudaEvent_t& a; cudaEvent_t& b;
-    ~Guard() { if (a) cudaEventDestroy(a); if (b) cudaEventDestroy(b); if (s) cudaStreamDestroy(s); }
-  } guard{s, e0, e1};
-  BEM_CUDA(cudaEventCreate(&e0));
-  BEM_CUDA(cudaEventCreate(&e1));
-  const double one[2] = {1.0, 0.0}, zero[2] = {0.0, 0.0};
-  const bool fused_ok = mv_fused_supported();
-  const bool was_profiling = profiling;
-  profiling = false;
-  double best = 1e300;
-  int bp = mv_piece > 0 ? mv_piece : mv_piece_elems(), bf = mv_fused ? 1 : 0;
-  for (int pc : cand) {
-    mv_piece = pc;
-    build_mv_items(fused_ok ? 0x33u : 0x03u, false, false);
-    for (int f = fused_ok ? 1 : 0; f >= 0; --f) {
-      mv_fused = f != 0;
-      for (int w = 0; w < 2; ++w) mult(0, one, x.p, zero, y.p, 1, s);
-      BEM_CUDA(cudaEventRecord(e0, s));
-      for (int r = 0; r < reps; ++r) mult(0, one, x.p, zero, y.p, 1, s);
-      BEM_CUDA(cudaEventRecord(e1, s));
-      BEM_CUDA(cudaEventSynchronize(e1));
-      float ms = 0.f;
-      BEM_CUDA(cudaEventElapsedTime(&ms, e0, e1));
-      const double per = ms / reps;
-      if (per < best) {
-        best = per;
-        bp = pc;
-        bf = f;
-      }
-    }
-  }
-  mv_piece = bp;
-  mv_fused = bf != 0;
-  build_mv_items(mv_fused ? 0x30u : 0x03u, false, false);
-  BEM_CUDA(cudaStreamSynchronize(s));
-  profiling = was_profiling;
-  if (best_piece) *best_piece = bp;
-  if (best_fused) *best_fused = bf;
-  return best;
-}
-
 }  // namespace bem
