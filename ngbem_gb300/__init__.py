@@ -7,5 +7,7 @@ CUDA kernels for sm_103a behind the C-ABI of include/ngbem_gb300.h.
 from .meshes import Mesh, Region, icosphere, ellipsoid, perturbed_icosphere
 from .bem import *  # noqa: F401,F403
 from .bem import __all__ as _bem_all
+from .krylov import BlockMatrix, BlockVector
 
-__all__ = ["Mesh", "Region", "icosphere", "ellipsoid", "perturbed_icosphere"] + list(_bem_all)
+__all__ = ["Mesh", "Region", "icosphere", "ellipsoid", "perturbed_icosphere", "BlockMatrix",
+           "BlockVector"] + list(_bem_all)

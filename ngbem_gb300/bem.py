@@ -484,6 +484,43 @@ class HMatrix(_NativeMatrix):
 class MassMatrix(_NativeMatrix):
     """Sparse Galerkin mass matrix <u, v> of identity traces (rows = test dofs)."""
 
+    def Inverse(self, freedofs=None, tol=1e-14, maxiter=2000):
+        """The inverse (the role of ``BilinearForm(...).Assemble().mat.Inverse(freedofs=...)`` as
+        the reference's tests use it for GMRes preconditioners): conjugate gradients on the
+        GPU with this matrix's products, to tol relative; dofs outside freedofs map to 0."""
+        if self.height != self.width:
+            raise ValueError("only square mass matrices have an inverse")
+        return _MassInverse(self, freedofs, tol, maxiter)
+
+
+class _MassInverse(BaseMatrix):
+    """M^-1 of a symmetric positive definite mass matrix by conjugate gradients (real M; it
+    applies to real and complex vectors alike)."""
+    any_field = True
+
+    def __init__(self, M, freedofs, tol, maxiter):
+        self.M, self.tol, self.maxiter = M, float(tol), int(maxiter)
+        self.height = self.width = M.height
+        self.is_complex = M.is_complex
+        self.freedofs = None if freedofs is None else np.asarray(freedofs, dtype=bool)
+        self.last = None
+
+    def _apply(self, trans, alpha, x, beta, y):
+        from . import krylov
+        torch = _torch()
+        mask = None if self.freedofs is None else torch.as_tensor(self.freedofs).to(x.device)
+        Mop = krylov.as_operator(self.M)
+
+        def proj(v):
+            return v if mask is None else torch.where(mask, v, torch.zeros((), dtype=v.dtype, device=v.device))
+        z, it, rel = krylov.cg(lambda v: proj(Mop(proj(v))), proj(x), self.tol, self.maxiter)
+        self.last = dict(iterations=it, residual=rel)
+        z = z.to(y.dtype) if torch.is_complex(y) else z.real
+        if beta == 0.0:
+            y.copy_(alpha * z)
+        else:
+            y.mul_(beta).add_(alpha * z)
+
 
 def MassOperator(trial_space: TraceSpace, test_space: TraceSpace | None = None, complex: bool = False) -> MassMatrix:
     test_space = trial_space if test_space is None else test_space
@@ -695,8 +732,28 @@ def GMRes(A, b, pre=None, freedofs=None, x=None, maxsteps=100, tol=1e-7, innerpr
     ngsolve.krylovspace.GMRes in the reference tests).  Returns the solution vector; the
     iteration count and final relative residual are in GMRes.last."""
     torch = _torch()
-    if pre is not None or freedofs is not None or innerproduct is not None:
-        raise NotImplementedError("GMRes: preconditioners, freedofs and inner products are not supported")
+    from . import krylov
+    if innerproduct is not None:
+        raise NotImplementedError("GMRes: inner products other than the Euclidean one are not supported")
+    if pre is not None or freedofs is not None or isinstance(A, krylov.BlockMatrix) or \
+            isinstance(b, krylov.BlockVector):
+        # preconditioned or block systems: the Krylov iteration in torch on the GPU, every
+        # operator and preconditioner application the library's own
+        bd = krylov._data(b)
+        if not isinstance(bd, torch.Tensor):
+            bd = torch.as_tensor(np.asarray(bd)).cuda()
+        cplx = bd.is_complex() or A.is_complex
+        dt = torch.complex128 if cplx else torch.float64
+        bd = bd.to(dt)
+        x0 = None if x is None else krylov._data(x).to(dt)
+        sol, it, res = krylov.gmres(krylov.as_operator(A), bd, pre=krylov.as_operator(pre), x0=x0,
+                                    maxsteps=int(maxsteps), tol=float(reltol if reltol is not None else tol),
+                                    restart=restart, freedofs=freedofs, callback=callback, printrates=printrates)
+        GMRes.last = dict(iterations=it, residual=res)
+        if x is not None:
+            krylov._data(x).copy_(sol)
+            return x
+        return krylov.BlockVector.wrap(sol, b.sizes) if isinstance(b, krylov.BlockVector) else sol
     terms = A._terms() if isinstance(A, BaseMatrix) else [(1.0, A)]
     for _, M in terms:
         if not isinstance(M, _NativeMatrix):
