@@ -521,6 +521,15 @@ class _MassInverse(BaseMatrix):
         else:
             y.mul_(beta).add_(alpha * z)
 
+    def __mul__(self, x):
+        # the result lives in the vector's field (a real inverse applies to complex vectors)
+        torch = _torch()
+        if isinstance(x, np.ndarray):
+            return (self * torch.from_numpy(np.ascontiguousarray(x)).cuda()).cpu().numpy()
+        y = torch.zeros(self.height, dtype=x.dtype if x.is_complex() else torch.float64, device=x.device)
+        self._apply(False, 1.0, x, 0.0, y)
+        return y
+
 
 def MassOperator(trial_space: TraceSpace, test_space: TraceSpace | None = None, complex: bool = False) -> MassMatrix:
     test_space = trial_space if test_space is None else test_space

@@ -111,6 +111,10 @@ def test_mass_inverse_and_block_preconditioned_gmres():
     y = torch.zeros(30, dtype=torch.complex128)
     inv1._apply(False, 1.0, (M1.A.to(x.dtype) @ x), 0.0, y)
     assert torch.allclose(y, x, atol=1e-11)
+    # products keep the vector's field: a real inverse on a complex vector
+    assert torch.allclose(inv1 * (M1.A.to(x.dtype) @ x), x, atol=1e-11)
+    xr = x.real.contiguous()
+    assert torch.allclose(inv1 * (M1.A @ xr), xr, atol=1e-11) and not (inv1 * (M1.A @ xr)).is_complex()
     V, K, W = _rand(30, seed=16) + 40 * np.eye(30), 0.3 * _rand(30, 20, seed=17), _rand(20, seed=18) + 30 * np.eye(20)
     lhs = nb.BlockMatrix([[Dense(V), Dense(-K)], [Dense(K.T), Dense(W)]])
     pre = nb.BlockMatrix([[inv1, None], [None, inv2]])
