@@ -57,7 +57,8 @@ def gmres(apply, b, pre=None, x0=None, maxsteps=100, tol=1e-7, restart=None, fre
     """Restarted GMRES, left preconditioned: minimises |pre (b - A x)| over the Krylov space of
     pre A (classical Gram-Schmidt applied twice, Givens rotations).  Stops when that residual
     is below tol times its initial value.  freedofs (boolean mask) restricts the unknowns:
-    entries outside it stay zero.  Returns (x, iterations, relative preconditioned residual)."""
+    entries outside it keep their initial values (x0, else zero), as with a Dirichlet lift.
+    Returns (x, iterations, relative preconditioned residual)."""
     torch = _torch()
     dev, dt = b.device, b.dtype
     cplx = torch.is_complex(b)
@@ -74,7 +75,7 @@ def gmres(apply, b, pre=None, x0=None, maxsteps=100, tol=1e-7, restart=None, fre
     def scal(z):  # a host scalar in the vectors' field
         return complex(z) if cplx else float(complex(z).real)
 
-    x = torch.zeros_like(b) if x0 is None else proj(x0.clone().to(dt))
+    x = torch.zeros_like(b) if x0 is None else x0.clone().to(dt)
     m = int(restart or min(maxsteps, 200))
     r = P(b - apply(x))
     beta0 = float(torch.linalg.vector_norm(r))

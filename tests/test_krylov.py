@@ -76,6 +76,13 @@ def test_gmres_freedofs():
     assert (x[~f] == 0).all()
     xr = torch.linalg.solve(A[f][:, f], b[f])
     assert torch.allclose(x[f], xr, rtol=0, atol=1e-10)
+    # a start vector carries fixed values on the other dofs (a Dirichlet lift)
+    x0 = torch.zeros(n, dtype=torch.float64)
+    x0[~f] = 2.0
+    x2, _, _ = krylov.gmres(lambda v: A @ v, b, x0=x0, freedofs=free, maxsteps=200, tol=1e-13)
+    assert (x2[~f] == 2.0).all()
+    xr2 = torch.linalg.solve(A[f][:, f], b[f] - A[f][:, ~f] @ x0[~f])
+    assert torch.allclose(x2[f], xr2, rtol=0, atol=1e-10)
 
 
 def test_block_matrix_and_vector():
