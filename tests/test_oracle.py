@@ -178,3 +178,18 @@ def test_hcurl_traces(oracle):
     Vc = oracle.dense_matrix("maxwell_sl", m, "HCURL", kappa=2.0, trial_eval="maxwellcurl", intorder=4)
     Vd = oracle.dense_matrix("maxwell_sl", m, "RT0", kappa=2.0, trial_eval="maxwell", intorder=4)
     assert np.linalg.norm(Vc - Vd) / np.linalg.norm(Vd) < 1e-13
+
+
+def test_aca_against_dense_maxwell_double_layer(oracle):
+    """The three-component kernel with six cross-product terms through the oracle's ACA: each
+    component compressed on its own, the terms projected with their traces (HCurl rotated trace
+    against RT0), matvec within the tolerance of the dense operator."""
+    m = ellipsoid(2)
+    eps = 1e-6
+    args = dict(kappa=2.0, trial_eval="rotatedtrace", test_eval="id")
+    H = oracle.OracleOperator("maxwell_dl", m, "HCURL", "RT0", intorder=3, leafsize=20, eta=2.0, eps=eps, **args)
+    D = oracle.dense_matrix("maxwell_dl", m, "HCURL", "RT0", intorder=3, **args)
+    assert H.nfar > 0
+    r = np.random.default_rng(5)
+    x = r.standard_normal(H.width) + 1j * r.standard_normal(H.width)
+    assert np.linalg.norm(D @ x - H.mult(x)) / np.linalg.norm(D @ x) < 10 * eps
