@@ -9,6 +9,7 @@
 #include <atomic>
 #include <cmath>
 #include <condition_variable>
+#include <exception>
 #include <functional>
 #include <numeric>
 #include <unordered_map>
@@ -338,7 +339,8 @@ static const int kTreeTeamMinDofs = 4096;
 
 // Host threads kept for the levels of one tree build (starting threads per level cost more
 // than a level's work at 20k dofs).  run(n, f) calls f(i) for i in [0, n) on the team and
-// the calling thread and returns when every call has returned.
+// the calling thread and returns when every call has returned; an exception from f is
+// rethrown there after the team has stopped touching f.
 class LevelTeam {
  public:
   explicit LevelTeam(int workers) {
@@ -367,11 +369,22 @@ class LevelTeam {
     std::unique_lock<std::mutex> lk(mu_);
     done_.wait(lk, [this] { return busy_ == 0; });
     job_ = nullptr;
+    if (failure_) {
+      std::exception_ptr e = failure_;
+      failure_ = nullptr;
+      std::rethrow_exception(e);
+    }
   }
 
  private:
   void work() {
-    for (int i = next_++; i < n_; i = next_++) (*job_)(i);
+    try {
+      for (int i = next_++; i < n_; i = next_++) (*job_)(i);
+    } catch (...) {
+      next_.store(n_);  // the others stop taking items
+      std::lock_guard<std::mutex> lk(mu_);
+      if (!failure_) failure_ = std::current_exception();
+    }
   }
   void loop() {
     long long seen = 0;
@@ -395,6 +408,7 @@ class LevelTeam {
   long long gen_ = 0;
   bool stop_ = false;
   std::atomic<int> next_{0};
+  std::exception_ptr failure_;
 };
 
 // a team for a tree of n dofs (null below kTreeTeamMinDofs or on one core)
