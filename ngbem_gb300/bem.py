@@ -33,7 +33,7 @@ __all__ = ["SurfaceL2", "H1", "HDivSurface", "HCurl", "TraceSpace", "BaseMatrix"
            "HelmholtzSingleLayerPotentialOperatorDKappa",
            "MaxwellSingleLayerPotentialOperator", "MaxwellSingleLayerPotentialOperatorCurl",
            "MaxwellDoubleLayerPotentialOperator", "MassOperator", "GMRes", "cluster_tree", "partition",
-           "tc_selftest"]
+           "tc_selftest", "TestCompression"]
 
 
 def _torch():
@@ -808,3 +808,111 @@ def GMRes(A, b, pre=None, freedofs=None, x=None, maxsteps=100, tol=1e-7, innerpr
 
 
 GMRes.last = {}
+
+
+# ----------------------------------------------------------------------------------------
+# compression diagnostic
+# ----------------------------------------------------------------------------------------
+def TestCompression(nx=100, ny=100, eta=2.0, eps=1e-10, method="svd", seed=None, device=None):
+    """The reference's compression diagnostic (python_bem.cpp:177-193, test_compression.cpp):
+    the block 1/|x - y| between nx and ny random points of two unit cubes, the second shifted
+    by 1 + sqrt(3)/eta along x (admissible for eta), compressed by a full SVD ("svd"), a
+    randomized SVD of growing rank ("tsvd") or ACA with the eps scaling 2/3 eps / sqrt(nx ny)
+    ("aca").  Returns (rank, Frobenius error, seconds), or (0, 0) for another method.  The
+    reference draws the points with an unseeded rand(); here seed picks them (None: fresh).
+    Runs in torch on device (default: the GPU when there is one)."""
+    import time
+    torch = _torch()
+    if method not in ("svd", "tsvd", "aca"):
+        return (0, 0)
+    dev = torch.device(device) if device is not None else torch.device("cuda" if torch.cuda.is_available() else "cpu")
+    rng = np.random.default_rng(seed)
+    ax = rng.random((nx, 3))
+    ay = rng.random((ny, 3))
+    ay[:, 0] += 1.0 + np.sqrt(3.0) / eta
+    A = torch.as_tensor(1.0 / np.linalg.norm(ax[:, None, :] - ay[None, :, :], axis=2), device=dev)
+
+    def sync():
+        if dev.type == "cuda":
+            torch.cuda.synchronize(dev)
+
+    sync()
+    t0 = time.perf_counter()
+    if method == "svd":
+        U, S, Vh = torch.linalg.svd(A, full_matrices=False)
+        num = int((S.abs() > eps).sum())
+        Uk, Vk = U[:, :num] * S[:num].sqrt(), S[:num].sqrt()[:, None] * Vh[:num]
+    elif method == "tsvd":
+        Uk, Vk, num = _tsvd(A, eps, rng)
+    else:
+        Uk, Vk, num = _aca_dense(A, eps)
+    sync()
+    t = time.perf_counter() - t0
+    err = float(torch.linalg.norm(A - Uk[:, :num] @ Vk[:num]))
+    return (num, err, t)
+
+
+def _tsvd(A, eps, rng):
+    """Randomized SVD of growing rank (test_compression.cpp:80-122): ranks 5, 7, 10, ... until
+    the last singular value drops below eps; rank = the index before the first one below eps."""
+    torch = _torch()
+    p = min(A.shape)
+    rank = 5
+
+    def cut(S):
+        for j in range(1, len(S)):
+            if S[j] < eps:
+                return j - 1
+        return None
+
+    while rank < p:
+        V = torch.as_tensor(rng.random((rank, A.shape[1])), device=A.device)
+        U, S, _ = torch.linalg.svd(A @ V.T, full_matrices=False)
+        U2, S, Vh = torch.linalg.svd(U.T @ A, full_matrices=False)
+        U = U @ U2
+        if float(S[rank - 1]) < eps:
+            num = cut(S)
+            if num is not None:
+                return U * S.sqrt(), S.sqrt()[:, None] * Vh, num
+        rank = int(rank * 1.5)
+    U, S, Vh = torch.linalg.svd(A, full_matrices=False)
+    num = cut(S)
+    num = p if num is None else num
+    return U * S.sqrt(), S.sqrt()[:, None] * Vh, num
+
+
+def _aca_dense(A, eps):
+    """ACA with partial pivoting on a dense matrix (test_compression.cpp:155-207): row pivot,
+    column pivot excluding the previous ones, stop when |u_k||v_k| < eps' |A_k|_F with
+    eps' = 2/3 eps / sqrt(m n)."""
+    torch = _torch()
+    m, n = A.shape
+    U = torch.zeros((m, m), dtype=A.dtype, device=A.device)
+    V = torch.zeros((n, n), dtype=A.dtype, device=A.device)
+    epsk = 2.0 / 3.0 * eps / np.sqrt(m * n)
+    ik, jk, ikm1, jkm1 = 0, 0, -1, -1
+    norm2 = 0.0
+    kmax = min(m, n)
+    for k in range(kmax):
+        v = A[ik] - V[:k].T @ U[ik, :k]
+        av = v.abs()
+        if jkm1 >= 0:
+            av[jkm1] = -1.0
+        jk = int(torch.argmax(av))
+        v = v / v[jk]
+        V[k] = v
+        u = A[:, jk] - U[:, :k] @ V[:k, jk]
+        U[:, k] = u
+        au = u.abs()
+        if ikm1 >= 0:
+            au[ikm1] = -1.0
+        ik = int(torch.argmax(au))
+        nk = float(torch.linalg.vector_norm(v) * torch.linalg.vector_norm(u))
+        norm2 += nk * nk
+        if k:
+            norm2 += 2.0 * float(((V[:k] @ v) * (U[:, :k].T @ u)).sum())
+        ikm1, jkm1 = ik, jk
+        if nk < epsk * np.sqrt(norm2):
+            return U, V, k + 1
+    return U, V, kmax
+

@@ -1,7 +1,8 @@
 """Preconditioned GMRES, conjugate gradients, block systems and the mass-matrix inverse of
 ngbem_gb300.krylov / bem.GMRes on the CPU, with dense stand-ins for the library's matrices (the
 library's own products are tested on the GPU).  The reference's tests solve with
-ngsolve.krylovspace.GMRes(A, b, pre=mass inverse or a BlockMatrix of them)."""
+ngsolve.krylovspace.GMRes(A, b, pre=mass inverse or a BlockMatrix of them).  Also the
+TestCompression diagnostic (torch on the CPU here)."""
 import numpy as np
 import pytest
 import torch
@@ -141,3 +142,19 @@ def test_mass_inverse_and_block_preconditioned_gmres():
     invf._apply(False, 1.0, r, 0.0, z)
     Mf = M1.A[free][:, free]
     assert (z[:4] == 0).all() and torch.allclose(z[4:], torch.linalg.solve(Mf, r[4:]), atol=1e-11)
+
+
+def test_compression_diagnostic():
+    """TestCompression (the reference's python_bem.cpp:177-193): the truncated SVD leaves an
+    error below eps sqrt(rank deficit); the randomized SVD and ACA reach the same order of
+    accuracy with ranks near the SVD's; other methods give (0, 0)."""
+    eps = 1e-10
+    r_svd, e_svd, t = nb.TestCompression(100, 120, 2.0, eps, "svd", seed=3, device="cpu")
+    assert 0 < r_svd < 100 and e_svd <= eps * np.sqrt(100) and t >= 0
+    r_t, e_t, _ = nb.TestCompression(100, 120, 2.0, eps, "tsvd", seed=3, device="cpu")
+    assert abs(r_t - r_svd) <= 3 and e_t < 10 * eps * np.sqrt(100)
+    r_a, e_a, _ = nb.TestCompression(100, 120, 2.0, eps, "aca", seed=3, device="cpu")
+    assert r_svd <= r_a <= r_svd + 20 and e_a < 1e-8
+    # better separated clusters compress further
+    assert nb.TestCompression(100, 120, 0.5, eps, "svd", seed=3, device="cpu")[0] < r_svd
+    assert nb.TestCompression(method="other", device="cpu") == (0, 0)
