@@ -28,7 +28,9 @@ def test_library_exports_header_symbols():
     (lambda: icosphere(2), "P0", 20), (lambda: icosphere(3), "P0", 20), (lambda: icosphere(3), "P1", 20),
     (lambda: icosphere(3), "RT0", 40), (lambda: ellipsoid(3), "P0", 40), (lambda: ellipsoid(3), "P1", 10),
     (lambda: perturbed_icosphere(3, 0.05, 7), "P0", 20), (lambda: icosphere(4), "P0", 40),
-    (lambda: icosphere(2), "P0", 2 ** 31 - 1)])
+    (lambda: icosphere(2), "P0", 2 ** 31 - 1),
+    # 4096 dofs and more: levels split over the host thread team
+    (lambda: icosphere(5), "P1", 20), (lambda: icosphere(4), "RT0", 20), (lambda: ellipsoid(5), "P0", 20)])
 def test_cluster_tree_bit_exact(oracle, mesh_fn, kind, leaf):
     m = mesh_fn()
     sp = nb.TraceSpace(m, kind)
