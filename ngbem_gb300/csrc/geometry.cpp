@@ -344,7 +344,13 @@ static const int kTreeTeamMinDofs = 4096;
 class LevelTeam {
  public:
   explicit LevelTeam(int workers) {
-    for (int t = 0; t < workers; ++t) th_.emplace_back([this] { loop(); });
+    for (int t = 0; t < workers; ++t) {
+      try {
+        th_.emplace_back([this] { loop(); });
+      } catch (...) {
+        break;  // no more threads to be had: the team works with those it has (or none)
+      }
+    }
   }
   ~LevelTeam() {
     {
