@@ -116,7 +116,9 @@ __global__ void __launch_bounds__(POT_THREADS) pot_eval_kernel(PotArgs a) {
 }
 
 // (kernel, trial trace) pairs of the operators: the scalar kernels with P0 / P1 identity
-// traces, the hypersingular kernels with their curl traces, Maxwell with RT0
+// traces, the hypersingular kernels with their curl traces, the Maxwell single layer with RT0
+// and in its curl form with HCurl (the double layer has none: the reference's PotentialCF
+// sums its cross-product terms without their signs)
 #define BEM_POT_COMBOS(X)                                                                        \
   X(K_LAPLACE_SL, TR_P0, double) X(K_LAPLACE_SL, TR_P1, double) X(K_LAPLACE_DL, TR_P0, double)  \
   X(K_LAPLACE_DL, TR_P1, double) X(K_LAPLACE_HS, TR_ROT, double)                                 \
@@ -124,6 +126,7 @@ __global__ void __launch_bounds__(POT_THREADS) pot_eval_kernel(PotArgs a) {
   X(K_HELMHOLTZ_DL, TR_P0, cpx<double>) X(K_HELMHOLTZ_DL, TR_P1, cpx<double>)                   \
   X(K_HELMHOLTZ_CF, TR_P0, cpx<double>) X(K_HELMHOLTZ_CF, TR_P1, cpx<double>)                   \
   X(K_HELMHOLTZ_HS, TR_HELM, cpx<double>) X(K_MAXWELL_SL, TR_MAX, cpx<double>)                  \
+  X(K_MAXWELL_SL, TR_NEDMAX, cpx<double>)                                                        \
   X(K_HELMHOLTZ_SL_DKAPPA, TR_P0, cpx<double>) X(K_HELMHOLTZ_SL_DKAPPA, TR_P1, cpx<double>)
 
 int potential_dim(int kid, int trt) {

@@ -193,3 +193,15 @@ def test_aca_against_dense_maxwell_double_layer(oracle):
     r = np.random.default_rng(5)
     x = r.standard_normal(H.width) + 1j * r.standard_normal(H.width)
     assert np.linalg.norm(D @ x - H.mult(x)) / np.linalg.norm(D @ x) < 10 * eps
+
+
+def test_potential_of_the_curl_single_layer(oracle):
+    """GetPotential of the curl form of the Maxwell single layer (HCurl, DiffOpMaxwell trial
+    trace [n x phi; curl phi] = [-psi; div psi]): the RT0 potential with its vector part negated."""
+    m = icosphere(2)
+    d = np.random.default_rng(9).standard_normal(oracle.ndof(m, "RT0")) + 0j
+    pts = np.array([[0.0, 0.0, 2.0], [0.3, -0.2, 0.1]])
+    pc = oracle.potential("maxwell_sl", m, "HCURL", d, pts, kappa=2.0, trial_eval="maxwellcurl", intorder=3)
+    pr = oracle.potential("maxwell_sl", m, "RT0", d, pts, kappa=2.0, trial_eval="maxwell", intorder=3)
+    assert pc.shape == (2, 4)
+    assert np.allclose(pc[:, :3], -pr[:, :3], rtol=1e-12, atol=1e-14) and np.allclose(pc[:, 3], pr[:, 3], rtol=1e-12)
