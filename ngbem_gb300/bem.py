@@ -177,7 +177,8 @@ def cluster_tree(space: TraceSpace, leafsize: int = 40):
 
 class Potential:
     """Field of a density at arbitrary points (the role of the reference's PotentialCF): FP64,
-    all trial elements and the regular rule's points, the operator's kernel terms."""
+    the trial space's elements (within the operator's trial definedon region, if any) and the
+    regular rule's points, the operator's kernel terms without their factors (as there)."""
 
     def __init__(self, op: "IntegralOperator", gf):
         torch = _torch()
