@@ -1,22 +1,35 @@
 #!/usr/bin/env python
-"""Benchmark of the operator path on the Laplace Dirichlet-to-Neumann workload.
+"""Benchmark of the operator path (assembly + H-matrix application) on one GB300.
 
-Workload (the reference's headline config for this metric): unit icosphere at subdivision
-level 5 (20480 triangles), Laplace single layer V on P0 (20480 dofs) and double layer K from
-P1 (10242 dofs) to P0, H-matrices with leaf size 20, eta = 2, ACA eps = 1e-8, intorder 3,
-mixed precision (FP64 Sauter-Schwab pairs, FP32 regular near field, ACA and factors),
-Dirichlet data x^2 - y^2, GMRES to 1e-8 with the matvec replayed from a CUDA graph.
-Synthetic data: the mesh is generated, the density of the timed steps is N(0,1) (seeded).
+Default workload: Helmholtz Burton-Miller at kappa = 8 on the ellipsoid with semi-axes
+(1, 0.7, 0.5) at icosphere level 6 (81920 triangles), P1 trace space (40962 complex dofs),
+H-matrix leaf 20, eta = 2, ACA eps = 1e-8, intorder 3, 32 incident plane waves (directions
+uniform on the sphere, seeded).  Synthetic data: mesh and right-hand sides are generated.
 
-A step is one H-matrix application y = V x (the per-iteration cost of the DtN solve) with
-x resident in HBM; L2 is flushed before every step (a 512 MiB write, then by default a 512 MiB
-read of a second buffer, so that the write-back of the flush's dirty lines does not land inside
-the step) and each step is timed with CUDA events on the launch stream.  value = H-matvec/s over all ranks.  The assembly
-time (metric's first half) is reported as assembly_s.  e2e = the same step through the
-host-buffer C-ABI entry point (H2D of x, D2H of y inside the timed region).
+A step is one application Y = C X of the combined-field H-matrix to the 32 right-hand sides
+(the product every batched-GMRES iteration makes) in mixed precision: complex64 factors,
+split-TF32 tcgen05 products with FP32 accumulation.  X and the operator are resident in HBM;
+L2 is flushed before every step (a 512 MiB write, then a 512 MiB read of a second buffer, so
+that the write-back of the flush's dirty lines does not land inside the step); each step is
+timed with CUDA events on the launch stream.  value = single-right-hand-side H-matvecs per
+second (32 per step) over all ranks.  e2e = the same step through the host-buffer C-ABI entry
+point (page-locked X read and Y written by the kernels across the host link).
 
---impl reference times the reference algorithm's CPU implementation (the FP64 C++ oracle,
-all host threads) on the same workload and prints the same JSON line with impl=reference.
+The same line carries the metric's other half and its comparators: assembly seconds of the
+mixed and the plain FP64 GPU path, the batched 32-right-hand-side solve of both paths, the
+FP64 path's application rate, the solution error of the mixed path against the FP64 path,
+the products' errors against the FP64 path and the FP64 oracle, the roofline of the
+tensor-core GEMM kernels and the FP64 oracle on the host cores (cpu_baseline).
+
+--impl reference times the reference algorithm's CPU implementation (the FP64 C++ oracle, all
+host threads: the combined-field H-matrix assembled on the host cores, then per step its
+product with a bounded sample of the 32 right-hand sides, one vector at a time as the
+reference's HMatrix::Mult does) and prints the same JSON line with impl=reference.  That arm
+loads only the oracle's library: the mesh and right-hand-side generators are loaded from their
+source files without the package (whose import loads the CUDA library).
+
+--workload dtn (Laplace Dirichlet-to-Neumann, icosphere level 5, single-vector V matvec),
+shape (batched energy + shape gradient) and maxwell (EFIE on RT0) print secondary lines.
 """
 from __future__ import annotations
 
@@ -42,14 +55,17 @@ def parse():
     ap.add_argument("--steps", type=int, default=50)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--level", type=int, default=None, help="mesh level (dtn: 5, bm: 6)")
+    ap.add_argument("--level", type=int, default=None, help="mesh level (bm: 6, dtn: 5, maxwell: 5)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 plain-path comparison")
     ap.add_argument("--no-gmres", action="store_true", help="skip the DtN GMRES solve (profiling runs)")
-    ap.add_argument("--workload", default="dtn", choices=["dtn", "shape", "bm", "maxwell"],
-                    help="dtn: the headline H-matvec workload (default); shape: batched single-layer "
-                         "energy + adjoint shape gradient over 64 perturbed icospheres (L2..L5); bm: "
-                         "Helmholtz Burton-Miller kappa 8 on the L6 ellipsoid, 32 plane waves (batched GMRES)")
+    ap.add_argument("--workload", default="bm", choices=["bm", "dtn", "shape", "maxwell"],
+                    help="bm: Helmholtz Burton-Miller kappa 8 on the L6 ellipsoid, 32 plane waves (default, "
+                         "the headline); dtn: Laplace DtN on the L5 icosphere, single-vector V matvec; shape: "
+                         "batched single-layer energy + adjoint shape gradient over 64 perturbed icospheres "
+                         "(L2..L5); maxwell: EFIE on RT0 of the L5 icosphere")
+    ap.add_argument("--ref-sample", type=int, default=4,
+                    help="bm reference arm: right-hand sides per step (the oracle applies one vector at a time)")
     ap.add_argument("--l2-flush", default="write+read", choices=["write+read", "write"],
                     help="before every step: write a 512 MiB buffer, then (default) read another 512 MiB "
                          "buffer so that the write-back of the dirty lines is not charged to the step")
@@ -69,13 +85,40 @@ def workload(level, l2="write+read"):
             "gmres": "V u = (M/2 + K) g, g = x^2 - y^2, tol 1e-8, CUDA graph"}
 
 
-def traffic_from_profile(kernel):
-    """DRAM bytes per launch of `kernel` from the committed ncu summary (profiles/), or None.
+BM_KAPPA, BM_NRHS, BM_AXES = 8.0, 32, (1.0, 0.7, 0.5)
+BM_OPTS = dict(intorder=3, leafsize=20, eta=2.0, eps=1e-8)
+BM_SEED = SEED + 3
+
+
+def bm_workload(level, l2="write+read"):
+    nt = 20 * 4 ** level
+    return {"workload": f"helmholtz_bm_ellipsoid_L{level}_kappa8_32rhs",
+            "mesh": f"ellipsoid, semi-axes (1, 0.7, 0.5), icosphere level {level}", "triangles": nt,
+            "dofs": nt // 2 + 2, "space": "P1 (H1 order 1), complex",
+            "operator": "Helmholtz combined field C = K - i kappa V; system (M/2 + C) u = f",
+            "kappa": BM_KAPPA, "nrhs": BM_NRHS,
+            "rhs": "32 incident plane waves exp(i kappa d.x), d uniform on the sphere (seeded)",
+            "leafsize": 20, "eta": 2.0, "eps": 1e-8, "intorder": 3,
+            "precision": "mixed: FP64 Sauter-Schwab pairs; complex64 regular near field, ACA and factors; "
+                         "split-TF32 tensor-core products, FP32 accumulation",
+            "step": "one application Y = C X to the 32 right-hand sides (the batched-GMRES product)",
+            "l2": L2_NOTE[l2], "gmres": "batched, 32 right-hand sides in lockstep, tol 1e-8, restart 100"}
+
+
+def bm_rhs(meshes, forms, level):
+    """The ellipsoid and its 32 Burton-Miller plane-wave load vectors (n x 32, complex128)."""
+    mesh = meshes.ellipsoid(level, BM_AXES)
+    d = forms.random_directions(BM_NRHS, BM_SEED)
+    return mesh, forms.p1_load_vector(mesh, forms.plane_wave_bm_source(BM_KAPPA, d), order=6)
+
+
+def traffic_from_profile(kernel, summary="mv_fused_kernel_laplace_dtn_L5.md"):
+    """DRAM bytes per launch of `kernel` from a committed ncu summary (profiles/), or None.
 
     The summary holds a line 'traffic_bytes_per_launch <kernel-name> <bytes>' taken from
     dram__bytes_read.sum + dram__bytes_write.sum of one capture of the same workload."""
     name = kernel.split()[0]
-    path = os.path.join(ROOT, "profiles", "mv_fused_kernel_laplace_dtn_L5.md")
+    path = os.path.join(ROOT, "profiles", summary)
     if not os.path.exists(path):
         return None
     for line in open(path):
@@ -83,6 +126,29 @@ def traffic_from_profile(kernel):
         if len(f) == 3 and f[0] == "traffic_bytes_per_launch" and f[1] == name:
             return float(f[2])
     return None
+
+
+def _pure_modules():
+    """ngbem_gb300/meshes.py and forms.py loaded from their source files, without the package's
+    __init__ (which loads the CUDA library): the reference arm maps no library of this repo
+    except the oracle's."""
+    import importlib.util
+    import types
+    pkg_name = "_ngbem_sources"
+    if pkg_name not in sys.modules:
+        pkg = types.ModuleType(pkg_name)
+        pkg.__path__ = [os.path.join(ROOT, "ngbem_gb300")]
+        sys.modules[pkg_name] = pkg
+    out = []
+    for m in ("meshes", "forms"):
+        full = f"{pkg_name}.{m}"
+        if full not in sys.modules:
+            spec = importlib.util.spec_from_file_location(full, os.path.join(ROOT, "ngbem_gb300", m + ".py"))
+            mod = importlib.util.module_from_spec(spec)
+            sys.modules[full] = mod
+            spec.loader.exec_module(mod)
+        out.append(sys.modules[full])
+    return tuple(out)
 
 
 class ClockSampler:
@@ -166,12 +232,12 @@ def whole_job_rate(world, units_per_rank, seconds):
 # ---------------------------------------------------------------------------------------------
 def cpu_reference(level, nthreads=0, steps=20, warmup=2):
     """Oracle (FP64 C++ restatement of the reference, all host threads): assembly of V and
-    matvec throughput on the same workload."""
+    matvec throughput on the Laplace DtN workload."""
     import numpy as np
-    from ngbem_gb300.meshes import icosphere
     from oracle import pyoracle as O
+    meshes, _ = _pure_modules()
     O.build()
-    m = icosphere(level)
+    m = meshes.icosphere(level)
     t0 = time.perf_counter()
     V = O.OracleOperator("laplace_sl", m, "P0", intorder=3, leafsize=20, eta=2.0, eps=1e-8, nthreads=nthreads)
     t_asm = time.perf_counter() - t0
@@ -188,20 +254,61 @@ def cpu_reference(level, nthreads=0, steps=20, warmup=2):
             "ms_per_step": 1e3 * sum(times) / steps, "oracle": V, "x": x}
 
 
+def cpu_reference_bm(level, sample, steps, warmup, nthreads=0):
+    """Oracle on the Burton-Miller workload: the combined-field H-matrix assembled on all host
+    threads (CalcHMatrix restated), then per step its product with `sample` of the 32
+    right-hand sides, one vector at a time (HMatrix::Mult restated), cycling through them."""
+    from oracle import pyoracle as O
+    meshes, forms = _pure_modules()
+    O.build()
+    mesh, X = bm_rhs(meshes, forms, level)
+    t0 = time.perf_counter()
+    Cop = O.OracleOperator("helmholtz_cf", mesh, "P1", kappa=BM_KAPPA, nthreads=nthreads, **BM_OPTS)
+    t_asm = time.perf_counter() - t0
+    ys = {}
+
+    def step(k):
+        for c in range(sample):
+            col = (k * sample + c) % X.shape[1]
+            ys[col] = Cop.mult(X[:, col])
+
+    for k in range(warmup):
+        step(k)
+    times = []
+    for k in range(steps):
+        t = time.perf_counter()
+        step(warmup + k)
+        times.append(time.perf_counter() - t)
+    cores = nthreads or os.cpu_count()
+    return {"matvec_per_s": steps * sample / sum(times), "assembly_s": t_asm, "cores": cores, "nze": Cop.nze,
+            "max_rank": Cop.max_rank, "nfallback": Cop.nfallback, "ms_per_step": 1e3 * sum(times) / steps,
+            "products": ys, "X": X}
+
+
 def run_reference(args):
     world, rank, _ = dist_setup(args)
     if rank != 0:
         return
-    r = cpu_reference(args.level or 5, 0, steps=args.steps, warmup=args.warmup)
+    if args.workload == "bm":
+        L = args.level or 6
+        r = cpu_reference_bm(L, args.ref_sample, args.steps, args.warmup)
+        cfg = bm_workload(L, args.l2_flush)
+        sample = (f"oracle FP64 assembly of C on {r['cores']} threads ({r['assembly_s']:.1f} s, untimed), then per "
+                  f"step C applied to {args.ref_sample} of the 32 right-hand sides, one vector at a time")
+        extra = {"assembly_s": r["assembly_s"], "nze": r["nze"], "max_rank": r["max_rank"],
+                 "nfallback": r["nfallback"]}
+    else:
+        L = args.level or 5
+        r = cpu_reference(L, 0, steps=args.steps, warmup=args.warmup)
+        cfg = workload(L, args.l2_flush)
+        sample = f"full workload: oracle assembly of V ({r['assembly_s']:.2f} s) then {args.steps} timed matvecs"
+        extra = {"assembly_s": r["assembly_s"], "nze": r["nze"]}
     v = r["matvec_per_s"]
     line = {"metric": METRIC, "impl": "reference", "value": v, "unit": "matvec/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": r["ms_per_step"],
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic", "config": workload(args.level or 5),
-            "assembly_s": r["assembly_s"], "nze": r["nze"],
-            "cpu_baseline": {"value": v, "unit": "matvec/s", "cores": r["cores"], "kind": "port",
-                             "sample": f"full workload: oracle assembly of V ({r['assembly_s']:.2f} s) then "
-                                       f"{args.steps} timed matvecs"},
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c128" if args.workload == "bm"
+            else "f64", "data": "synthetic", "config": cfg, **extra,
+            "cpu_baseline": {"value": v, "unit": "matvec/s", "cores": r["cores"], "kind": "port", "sample": sample},
             "e2e": {"value": v, "unit": "matvec/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -236,7 +343,7 @@ def dtn_solve(nb, mesh, P0, P1, V, K, V64, K64, dev, acc):
 
 
 # ---------------------------------------------------------------------------------------------
-def run_ours(args):
+def run_dtn(args):
     import numpy as np
     import torch
 
@@ -329,7 +436,6 @@ def run_ours(args):
     sampler = ClockSampler(local)
     sampler.start()
     time.sleep(0.3)
-    V.mat.set_profiling(True)
     evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
     t_wall0 = time.perf_counter()
     for k in range(args.steps):
@@ -339,10 +445,17 @@ def run_ours(args):
         evs[k][1].record(stream)
     torch.cuda.synchronize()
     t_wall = time.perf_counter() - t_wall0
-    kms, kcount = V.mat.kernel_times()
-    V.mat.set_profiling(False)
     step_ms = [a.elapsed_time(b) for a, b in evs]
     dev_ms = sum(step_ms)
+    # kernel times from a separate, untimed pass with the operator's event profiling on
+    V.mat.set_profiling(True)
+    for _ in range(min(args.steps, 20)):
+        flush_l2()
+        V.mat.Mult(x, y)
+    torch.cuda.synchronize()
+    kms, kcount = V.mat.kernel_times()
+    V.mat.set_profiling(False)
+    per_step_launches = sum(kcount) / max(1, min(args.steps, 20))
     # the same steps with the compensated (error-free) arithmetic used for GMRES residuals
     V.mat.set_accuracy(True)
     for _ in range(2):
@@ -407,7 +520,7 @@ def run_ours(args):
                 "frac": achieved / peak, "peak_source": peak_src, "traffic": traffic_from_profile(kernel),
                 "algorithmic_bytes": alg_bytes, "avg_launch_ms": launch_ms,
                 "matvec_GBps": matvec_bytes / (dev_ms / args.steps * 1e-3) / 1e9, **extra}
-    launches = int(sum(kcount))
+    launches = int(round(per_step_launches * args.steps))
 
     line = {"metric": METRIC, "value": value, "unit": "matvec/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": dev_ms / args.steps, "higher_is_better": True,
@@ -519,113 +632,239 @@ def run_shape(args):
 
 
 def run_bm(args):
-    """Burton-Miller (1/2 M + C) u = f, kappa = 8, ellipsoid (1, 0.7, 0.5) at level args.level
-    (default workload: 6, 81920 triangles), P1 (40962 complex dofs), 32 incident plane waves
-    (directions uniform on the sphere, seeded), H-matrix leaf 20, eta 2, ACA eps 1e-8, intorder 3.
-    Both paths assemble C and solve all 32 right-hand sides with the batched GMRES to 1e-8:
-    mixed precision (complex64 far field and factors, FP64 singular pairs and Arnoldi) and the
-    plain FP64 GPU path.  Reported: wall time of each path (assembly + solve), the ratio, the
-    solution error of the mixed path against FP64, iterations, and the 32-RHS matvec time."""
+    """Burton-Miller (M/2 + C) u = f at kappa 8 on the ellipsoid (1, 0.7, 0.5), icosphere level
+    args.level (default 6: 81920 triangles, 40962 complex P1 dofs), 32 plane waves.  Both the
+    mixed path and the plain FP64 GPU path assemble C (timed, fresh space so that the cluster tree
+    is built inside the timed region) and solve the 32 right-hand sides with the batched GMRES to
+    1e-8.  The timed steps apply the mixed C to the 32 right-hand sides (tensor cores)."""
+    import ctypes as C
+
     import numpy as np
     import torch
 
     import ngbem_gb300 as nb
+    from ngbem_gb300 import _lib
     from ngbem_gb300.forms import p1_load_vector, plane_wave_bm_source, random_directions
 
     world, rank, local = dist_setup(args)
     torch.cuda.set_device(local)
     if world > 1:
         torch.distributed.init_process_group("nccl")
+    dev = torch.device("cuda", local)
     L = args.level or 6
-    kappa, nrhs = 8.0, 32
+    nrhs = BM_NRHS
 
-    # untimed warm-up of both paths on a small ellipsoid (module loading, workspaces, graphs)
-    wm = nb.ellipsoid(2, (1.0, 0.7, 0.5))
+    # untimed warm-up of both paths on a small ellipsoid (module loading, workspaces, graphs,
+    # the tensor-core self-test)
+    wm = nb.ellipsoid(2, BM_AXES)
     wP = nb.H1(wm, complex=True)
-    wF = torch.from_numpy(p1_load_vector(wm, plane_wave_bm_source(kappa, random_directions(nrhs, 1)))).cuda()
+    wF = torch.from_numpy(p1_load_vector(wm, plane_wave_bm_source(BM_KAPPA, random_directions(nrhs, 1)))).to(dev)
     for prec in ("mixed", "fp64"):
-        wC = nb.HelmholtzCombinedFieldOperator(wP, wP, kappa=kappa, intorder=3, leafsize=20, eta=2.0, eps=1e-8,
-                                               precision=prec)
+        wC = nb.HelmholtzCombinedFieldOperator(wP, wP, kappa=BM_KAPPA, precision=prec, **BM_OPTS)
         nb.GMRes(0.5 * nb.MassOperator(wP, wP, complex=True) + wC.mat, wF, maxsteps=50, tol=1e-8, restart=100)
         wC.mat.Mult(wF, torch.empty_like(wF))
         del wC
     torch.cuda.synchronize()
-    mesh = nb.ellipsoid(L, (1.0, 0.7, 0.5))
-    P1 = nb.H1(mesh, complex=True)
-    d = random_directions(nrhs, SEED + 3)
-    F = torch.from_numpy(p1_load_vector(mesh, plane_wave_bm_source(kappa, d), order=6)).cuda()
-    M = nb.MassOperator(P1, P1, complex=True)
-    out = {}
-    sols = {}
+
+    mesh = nb.ellipsoid(L, BM_AXES)
+    Fh = p1_load_vector(mesh, plane_wave_bm_source(BM_KAPPA, random_directions(nrhs, BM_SEED)), order=6)
+    F = torch.from_numpy(Fh).to(dev)
+    Xc = F.t().contiguous()  # column-major n x 32: one contiguous column per right-hand side
+    M = nb.MassOperator(nb.H1(mesh, complex=True), None, complex=True)
+    stream = torch.cuda.current_stream()
+    one, zero = _lib.cplx2(1.0), _lib.cplx2(0.0)
+
+    def apply(op, X, Y):
+        _lib.check(_lib.lib.bem_operator_mult(op.h, 0, one, C.c_void_p(X.data_ptr()), zero,
+                                              C.c_void_p(Y.data_ptr()), nrhs, C.c_void_p(stream.cuda_stream)))
+
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+    def timed_apply(op, X, Y, reps):
+        apply(op, X, Y)
+        e0.record(stream)
+        for _ in range(reps):
+            apply(op, X, Y)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    info_keys = ("ms_setup", "ms_aca", "ms_nearfield", "ms_projection", "ms_mvitems", "ms_total")
+    paths, ops, sols = {}, {}, {}
     for prec in ("mixed", "fp64"):
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        Cop = nb.HelmholtzCombinedFieldOperator(P1, P1, kappa=kappa, intorder=3, leafsize=20, eta=2.0, eps=1e-8,
-                                                precision=prec)
+        P1 = nb.H1(mesh, complex=True)
+        Cop = nb.HelmholtzCombinedFieldOperator(P1, P1, kappa=BM_KAPPA, precision=prec, **BM_OPTS)
         torch.cuda.synchronize()
         t1 = time.perf_counter()
         U = nb.GMRes(0.5 * M + Cop.mat, F, maxsteps=1000, tol=1e-8, restart=100)
         torch.cuda.synchronize()
         t2 = time.perf_counter()
         last = dict(nb.GMRes.last)
-        # one application of C to the 32 right-hand sides, CUDA events
-        Y = torch.empty_like(F)
-        for _ in range(2):
-            Cop.mat.Mult(F, Y)
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record()
-        for _ in range(5):
-            Cop.mat.Mult(F, Y)
-        e1.record()
-        torch.cuda.synchronize()
-        mv_comp = e0.elapsed_time(e1) / 5
-        mv_fast = mv_comp
-        extra = {}
-        if prec == "mixed":
-            # plain accuracy (the GMRES inner iterations): tensor-core low-rank products, then
-            # the CUDA-core products of the same operator for comparison
-            def timed_mult(reps=5):
-                Cop.mat.Mult(F, Y)
-                e0.record()
-                for _ in range(reps):
-                    Cop.mat.Mult(F, Y)
-                e1.record()
-                torch.cuda.synchronize()
-                return e0.elapsed_time(e1) / reps
-            Ycomp = Y.cpu().numpy()
-            Cop.mat.set_accuracy(False)
-            tc = Cop.mat.tensor_cores()
-            mv_fast = timed_mult()
-            Yt = Y.cpu().numpy()
-            Cop.mat.set_tensor_cores(False)
-            mv_cc = timed_mult()
-            Ycc = Y.cpu().numpy()
-            Cop.mat.set_tensor_cores(True)
-            Cop.mat.set_accuracy(True)
-            extra = {"tensor_cores": tc, "matvec32_cuda_core_fast_ms": mv_cc,
-                     "matvec32_fast_rel_err_vs_compensated": float(np.linalg.norm(Yt - Ycomp) / np.linalg.norm(Ycomp)),
-                     "matvec32_cuda_core_fast_rel_err": float(np.linalg.norm(Ycc - Ycomp) / np.linalg.norm(Ycomp))}
         info = Cop.mat.info
-        out[prec] = {"assembly_s": t1 - t0, "solve_s": t2 - t1, "total_s": t2 - t0,
-                     "iterations": last["iterations"], "max_residual": last["residual"],
-                     "matvec32_ms": mv_comp, "matvec32_fast_ms": mv_fast, "nze": info["nze"],
-                     "max_rank": info["max_rank"],
-                     "bytes": info["bytes_dense"] + info["bytes_lowrank"], "nfallback": info["nfallback"], **extra}
-        sols[prec] = U.cpu().numpy()
-        del Cop, U, Y
-        torch.cuda.empty_cache()
-    um, u64 = sols["mixed"], sols["fp64"]
-    errs = [float(np.linalg.norm(um[:, r] - u64[:, r]) / np.linalg.norm(u64[:, r])) for r in range(nrhs)]
-    speed = out["fp64"]["total_s"] / out["mixed"]["total_s"]
-    line = {"metric": "Burton-Miller assembly + 32-RHS solve, mixed vs plain FP64 GPU path", "value": speed,
-            "unit": "x (fp64 time / mixed time)", "n_gpus": world, "steps": 1, "warmup": 0,
-            "ms_per_step": out["mixed"]["total_s"] * 1e3, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "c64 far field / f64 singular pairs and Arnoldi", "data": "synthetic",
-            "config": {"workload": f"helmholtz_bm_ellipsoid_L{L}_kappa8_32rhs", "triangles": mesh.nt, "dofs": P1.ndof,
-                       "space": "P1 (H1 order 1, complex)", "kappa": kappa, "nrhs": nrhs, "leafsize": 20, "eta": 2.0,
-                       "eps": 1e-8, "intorder": 3, "gmres_tol": 1e-8},
-            "mixed": out["mixed"], "fp64": out["fp64"], "solution_rel_err_max": max(errs),
-            "solution_rel_err_median": float(np.median(errs))}
+        paths[prec] = {"assembly_s": t1 - t0, "solve_s": t2 - t1, "total_s": t2 - t0,
+                       "iterations": last["iterations"], "max_residual": last["residual"], "nze": info["nze"],
+                       "max_rank": info["max_rank"], "nfallback": info["nfallback"],
+                       "bytes_stored": info["bytes_dense"] + info["bytes_lowrank"],
+                       "assembly_breakdown_ms": {k: info[k] for k in info_keys}}
+        ops[prec], sols[prec] = Cop, U
+    Cm, C64 = ops["mixed"].mat, ops["fp64"].mat
+    Y = torch.empty_like(Xc)
+    # the FP64 GPU path's application to the same 32 right-hand sides
+    t64 = timed_apply(C64, Xc, Y, 3)
+    Y64 = Y.clone()
+    # mixed, error-free FP32 products on the CUDA cores (the GMRES residuals)
+    Cm.set_accuracy(True)
+    t_comp = timed_apply(Cm, Xc, Y, 3)
+    Ycomp = Y.clone()
+    # mixed, plain accuracy: the tensor-core products of the GMRES iterations (the timed step)
+    Cm.set_accuracy(False)
+    tc = Cm.tensor_cores()
+
+    flush = torch.empty(512 * 2 ** 20 // 4, dtype=torch.float32, device=dev)
+    sweep = torch.zeros(512 * 2 ** 20 // 4, dtype=torch.float32, device=dev) if args.l2_flush == "write+read" else None
+    sweep_out = torch.zeros((), dtype=torch.float32, device=dev)
+
+    def flush_l2():
+        flush.fill_(1.0)
+        if sweep is not None:
+            torch.amax(sweep, dim=0, out=sweep_out)
+
+    for _ in range(args.warmup):
+        flush_l2()
+        apply(Cm, Xc, Y)
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    sampler = ClockSampler(local)
+    sampler.start()
+    time.sleep(0.3)
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    t_wall0 = time.perf_counter()
+    for k in range(args.steps):
+        flush_l2()
+        evs[k][0].record(stream)
+        apply(Cm, Xc, Y)
+        evs[k][1].record(stream)
+    torch.cuda.synchronize()
+    t_wall = time.perf_counter() - t_wall0
+    dev_ms = sum(a.elapsed_time(b) for a, b in evs)
+    Ytc = Y.clone()
+
+    # e2e: page-locked host buffers through bem_operator_mult_host (the kernels read X and
+    # write Y across the host link inside every step)
+    xh = Xc.cpu().pin_memory()
+    yh = torch.zeros_like(xh).pin_memory()
+
+    def apply_host():
+        _lib.check(_lib.lib.bem_operator_mult_host(Cm.h, 0, one, C.c_void_p(xh.data_ptr()), zero,
+                                                   C.c_void_p(yh.data_ptr()), nrhs))
+
+    for _ in range(args.warmup):
+        apply_host()
+    e2e_t = []
+    for _ in range(args.steps):
+        flush_l2()
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        apply_host()
+        e2e_t.append(time.perf_counter() - t)
+    clocks = sampler.stop()
+    e2e_check = float(torch.linalg.vector_norm(yh - Ytc.cpu()) / torch.linalg.vector_norm(Ytc.cpu()))
+
+    # kernel times from a separate, untimed pass with the operator's event profiling on:
+    # [X panels, GEMM pass 0, GEMM pass 1, partial-row sum + output]
+    nprof = 10
+    Cm.set_profiling(True)
+    for _ in range(nprof):
+        flush_l2()
+        apply(Cm, Xc, Y)
+    torch.cuda.synchronize()
+    kms, kcount = Cm.kernel_times()
+    Cm.set_profiling(False)
+    per_app = [kms[i] / max(1, kcount[i]) for i in range(4)]
+    launches_per_step = sum(kcount) / nprof
+
+    dev_ms, e2e_sum = max_over_ranks([dev_ms, sum(e2e_t)], dev)
+    value = whole_job_rate(world, args.steps * nrhs, dev_ms / 1e3)
+    e2e_value = whole_job_rate(world, args.steps * nrhs, e2e_sum)
+
+    # ---- accuracy against the FP64 GPU path (per right-hand side, max over the 32)
+    def colmax(a, b):
+        d = torch.linalg.vector_norm(a - b, dim=1) / torch.linalg.vector_norm(b, dim=1)
+        return float(d.max())
+
+    um, u64 = sols["mixed"].t(), sols["fp64"].t()
+    acc = {"solution_rel_err_vs_fp64": colmax(um, u64),
+           "solution_rel_err_vs_fp64_median": float((torch.linalg.vector_norm(um - u64, dim=1) /
+                                                     torch.linalg.vector_norm(u64, dim=1)).median()),
+           "C_matvec_tensor_core_rel_err_vs_fp64": colmax(Ytc, Y64),
+           "C_matvec_compensated_rel_err_vs_fp64": colmax(Ycomp, Y64),
+           "C_matvec_tensor_core_rel_err_vs_compensated": colmax(Ytc, Ycomp)}
+
+    # ---- roofline of the tensor-core GEMM passes (tc_gemm_kernel<0> + <1>)
+    peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    peak, peak_src = 6800.0, "fallback"
+    if os.path.exists(peaks_path):
+        peak, peak_src = float(json.load(open(peaks_path))["hbm_gbs"]), "measured"
+    im = Cm.info
+    n = Cm.width
+    # algorithmic bytes: the stored operator once (complex64 dense blocks and factors) plus the
+    # 32 right-hand sides read and the 32 results written once (complex64)
+    alg_bytes = im["bytes_dense"] + im["bytes_lowrank"] + 2 * n * nrhs * 8
+    gemm_ms = per_app[1] + per_app[2]
+    achieved = alg_bytes / (gemm_ms * 1e-3) / 1e9
+    t0p = traffic_from_profile("tc_gemm_kernel<0>", f"tc_gemm_kernel_bm_ellipsoid_L{L}.md")
+    t1p = traffic_from_profile("tc_gemm_kernel<1>", f"tc_gemm_kernel_bm_ellipsoid_L{L}.md")
+    roofline = {"bound": "hbm", "kernel": "tc_gemm_kernel<0> + tc_gemm_kernel<1>", "achieved": achieved,
+                "peak": peak, "unit": "GB/s", "frac": achieved / peak, "peak_source": peak_src,
+                "traffic": (t0p + t1p) if (t0p is not None and t1p is not None) else None,
+                "algorithmic_bytes": alg_bytes, "avg_launch_ms": gemm_ms,
+                "kernel_ms": {"tc_xprep": per_app[0], "tc_gemm_pass0": per_app[1], "tc_gemm_pass1": per_app[2],
+                              "tc_ysum_out": per_app[3]},
+                "application_GBps": alg_bytes / (dev_ms / args.steps * 1e-3) / 1e9,
+                "tensor_flops_per_step": 8 * im["nze"] * nrhs,
+                "tensor_TFLOPs": 8 * im["nze"] * nrhs / (gemm_ms * 1e-3) / 1e12}
+
+    mixed, fp64 = paths["mixed"], paths["fp64"]
+    mixed.update({"matvec32_ms": dev_ms / args.steps, "matvec32_compensated_ms": t_comp, "tensor_cores": tc})
+    fp64.update({"matvec32_ms": t64, "matvec_per_s": nrhs / (t64 * 1e-3)})
+    vs_fp64 = {"assembly": fp64["assembly_s"] / mixed["assembly_s"], "solve": fp64["solve_s"] / mixed["solve_s"],
+               "assembly_plus_solve": fp64["total_s"] / mixed["total_s"],
+               "matvec": t64 / (dev_ms / args.steps),
+               "target": ">= 5x for assembly + solve at solution error <= 1e-6"}
+    line = {"metric": METRIC, "value": value, "unit": "matvec/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": dev_ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None,
+            "dtype": "c64 (split-TF32 tensor-core products, FP32 accumulation)", "data": "synthetic",
+            "config": bm_workload(L, args.l2_flush), "assembly_s": mixed["assembly_s"],
+            "assembly_s_fp64": fp64["assembly_s"], "solve_s": mixed["solve_s"], "vs_fp64": vs_fp64,
+            "mixed": mixed, "fp64": fp64, "accuracy": acc, "roofline": roofline,
+            "gpu_launches": int(round(launches_per_step * args.steps)), "wall_s_timed_region": t_wall,
+            "clocks": clocks,
+            "e2e": {"value": e2e_value, "unit": "matvec/s", "h2d_bytes_per_step": n * nrhs * 16,
+                    "d2h_bytes_per_step": n * nrhs * 16, "check_rel_err": e2e_check,
+                    "note": "page-locked buffers read and written by the kernels across the host link"}}
+
+    if rank == 0 and not args.no_cpu_baseline:
+        r = cpu_reference_bm(L, 2, 2, 0)
+        # the oracle's products against the GPU paths' products of the same columns
+        errs = {"fp64": [], "tensor_core": [], "compensated": []}
+        for col, yo in r["products"].items():
+            yo_t = torch.from_numpy(yo)
+            for k, Yk in (("fp64", Y64), ("tensor_core", Ytc), ("compensated", Ycomp)):
+                yg = Yk[col].cpu()
+                errs[k].append(float(torch.linalg.vector_norm(yg - yo_t) / torch.linalg.vector_norm(yo_t)))
+        for k, v in errs.items():
+            line["accuracy"][f"C_matvec_{k}_rel_err_vs_oracle"] = max(v)
+        line["accuracy"]["oracle_columns"] = sorted(r["products"])
+        line["cpu_baseline"] = {"value": r["matvec_per_s"], "unit": "matvec/s", "cores": r["cores"], "kind": "port",
+                                "assembly_s": r["assembly_s"], "nze": r["nze"],
+                                "sample": f"oracle FP64 assembly of C on {r['cores']} threads "
+                                          f"({r['assembly_s']:.1f} s), then 4 of the 32 right-hand sides "
+                                          f"applied one vector at a time (2 timed steps of 2)"}
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:
@@ -710,10 +949,9 @@ def main():
         return
     if args.workload == "bm":
         if args.impl == "reference":
-            print(json.dumps({"impl": "reference", "unavailable": "the oracle's dense complex solve at 40962 dofs "
-                              "does not fit a bounded CPU sample; the dtn workload carries the CPU baseline"}))
-            return
-        run_bm(args)
+            run_reference(args)
+        else:
+            run_bm(args)
         return
     if args.workload == "shape":
         if args.impl == "reference":
@@ -725,7 +963,7 @@ def main():
     if args.impl == "reference":
         run_reference(args)
     else:
-        run_ours(args)
+        run_dtn(args)
 
 
 if __name__ == "__main__":

@@ -31,14 +31,14 @@ void HOperator::mult(int trans, const double* alpha, const void* x, const double
   }
   const int* pin = trans ? (ttest == ttrial ? d_perm_trial.as<int>() : d_perm_test.as<int>()) : d_perm_trial.as<int>();
   const int* pout = trans ? d_perm_trial.as<int>() : (ttest == ttrial ? d_perm_trial.as<int>() : d_perm_test.as<int>());
+  if (tc_eligible(trans, nrhs, s)) {
+    mult_tc(alpha, x, beta, y, nrhs, s);  // records its own profiling events
+    return;
+  }
   std::array<cudaEvent_t, 5> ev{};
   if (profiling) {
     for (auto& e : ev) BEM_CUDA(cudaEventCreate(&e));
     BEM_CUDA(cudaEventRecord(ev[0], s));
-  }
-  if (tc_eligible(trans, nrhs, s)) {
-    mult_tc(alpha, x, beta, y, nrhs, s);
-    return;
   }
   if (mv_fused && nrhs == 1) ensure_mv(trans ? 0xC0u : 0x30u, false, s);
   else if (nrhs > 1 && !trans) ensure_mv(prec == 0 ? 0u : 0u, true, s);

@@ -73,6 +73,64 @@ void get_dev(FILE* f, void* dptr, size_t bytes, std::vector<unsigned char>& buf)
 size_t u_elems(const LRDesc& L) { return (size_t)((L.m + L.cu - 1) / L.cu) * L.cu * L.R; }
 size_t v_elems(const LRDesc& L) { return (size_t)((L.n + L.cv - 1) / L.cv) * L.cv * L.R; }
 
+// Every value read from a file that the kernels or the host index with is checked before
+// anything is uploaded: a truncated or corrupt file is refused with BEM_ERR_ARG instead of
+// giving blocks that read or write outside the vectors on the device.
+void validate_loaded(const HOperator& op) {
+  auto bad = [](const char* what) { throw Error(BEM_ERR_ARG, std::string("corrupt operator file: ") + what); };
+  if (op.prec != 0 && op.prec != 1) bad("precision");
+  if (op.trt < 0 || op.tet < 0) bad("trace evaluators");
+  const bem_params_t& p = op.prm;
+  if (p.method != BEM_METHOD_ACA && p.method != BEM_METHOD_DENSE) bad("method");
+  if (p.method == BEM_METHOD_ACA && p.leafsize < 1) bad("leaf size");
+  if (p.intorder < 0 || p.intorder > 40 || p.intorder_singular < 0 || p.intorder_singular > 40 ||
+      p.intorder_regular < 0 || p.intorder_regular > 40)
+    bad("quadrature orders");
+  const size_t nb = op.blocks.size();
+  if (op.block_rank.size() != nb || op.block_fallback.size() != nb) bad("block list sizes");
+  const long long ncr = (long long)op.ttest->cl.size(), ncc = (long long)op.ttrial->cl.size();
+  size_t nlow = 0;
+  for (size_t b = 0; b < nb; ++b) {
+    const BlockH& B = op.blocks[b];
+    if (B.rowcl < 0 || B.rowcl >= ncr || B.colcl < 0 || B.colcl >= ncc) bad("block clusters");
+    if (op.block_rank[b] < -1) bad("block rank");
+    if (op.block_fallback[b] < 0 || op.block_fallback[b] > 2) bad("fallback flag");
+    if (op.block_rank[b] >= 0) ++nlow;
+  }
+  if (op.mvlr.size() != nlow || op.mvdense.size() != nb - nlow) bad("descriptor counts");
+  auto in_range = [](long long o, long long n, long long lim) { return o >= 0 && n >= 0 && o + n <= lim; };
+  for (const MVDense& d : op.mvdense)
+    if (!in_range(d.r0, d.m, op.height) || !in_range(d.c0, d.n, op.width)) bad("dense block extent");
+  // A block's rank is the sum of its kernel terms' ranks (up to six terms), so it may exceed
+  // min(m, n); it is bounded here only against overflow, and the payload against the file.
+  for (const LRDesc& L : op.mvlr) {
+    if (!in_range(L.r0, L.m, op.height) || !in_range(L.c0, L.n, op.width)) bad("low-rank block extent");
+    if (L.R < 0 || L.R > (1 << 20)) bad("low-rank block rank");
+    if (L.cu < 1 || L.cv < 1 || L.cu > (std::max(L.m, 1) + 3) / 4 * 4 || L.cv > (std::max(L.n, 1) + 3) / 4 * 4)
+      bad("factor chunk sizes");
+  }
+}
+
+// The payload the descriptors announce must be in the file: no allocation is sized by a
+// corrupt count.
+void check_payload(FILE* f, const HOperator& op) {
+  const long pos = ftell(f);
+  if (pos < 0 || fseek(f, 0, SEEK_END) != 0) throw Error(BEM_ERR_ARG, "operator file is not seekable");
+  const long end = ftell(f);
+  if (end < 0 || fseek(f, pos, SEEK_SET) != 0) throw Error(BEM_ERR_ARG, "operator file is not seekable");
+  const unsigned long long left = (unsigned long long)(end - pos);
+  unsigned long long need = 0;
+  auto add = [&](unsigned long long elems) {
+    need += elems * (unsigned long long)op.vsize;  // elems < 2^52 and vsize <= 16: no overflow
+    if (need > left) throw Error(BEM_ERR_ARG, "corrupt operator file: payload larger than the file");
+  };
+  for (const MVDense& d : op.mvdense) add((unsigned long long)d.m * (unsigned long long)d.n);
+  for (const LRDesc& L : op.mvlr) {
+    add(u_elems(L));
+    add(v_elems(L));
+  }
+}
+
 }  // namespace
 
 void save_operator(const HOperator& op, const char* path) {
@@ -174,6 +232,8 @@ std::unique_ptr<HOperator> load_operator(const char* path, SpaceH* trial, SpaceH
   op->info = get_v<bem_operator_info_t>(f);
   op->mvdense = get_vec<MVDense>(f, lim);
   op->mvlr = get_vec<LRDesc>(f, lim);
+  validate_loaded(*op);
+  check_payload(f, *op);
   // device pools: every dense block at a 16-byte aligned offset, then the U2 and V2 factors
   const size_t al = 16;
   auto up = [&](size_t b) { return (b + al - 1) / al * al; };
