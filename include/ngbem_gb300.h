@@ -172,14 +172,17 @@ int bem_operator_mult(bem_operator_t op, int trans, const double* alpha, const v
  * (no counterpart in the reference).  bem_operator_mult grows operator-owned scratch on first
  * use and when nrhs grows (cudaFree + cudaMalloc; cudaFree waits for the whole device).  This
  * entry point allocates nothing: its scratch is a fixed file-scope device array of
- * BEM_NOALLOC_SCRATCH_BYTES.  Same arguments, same result (up to the order of FP64 atomic
- * additions).  H-matrix operators only (BEM_ERR_STATE for a mass operator).  A call whose
- * scratch would exceed the area -- about 2 * (height + width + sum of block ranks) * nrhs
- * values -- returns BEM_ERR_ARG before launching anything.  The first call on a device looks
- * the array up (and may load device code), and the first call of an operator in a direction
- * (trans = 0 or 1) builds that direction's work lists, which the operator keeps: make those
- * calls before any stream capture.  The area is shared by every call on a device, so
- * overlapping calls (several streams or host threads) race: serialise them. */
+ * BEM_NOALLOC_SCRATCH_BYTES, and it never builds work lists (which would allocate).  Same
+ * arguments, same result (up to the order of FP64 atomic additions).  H-matrix operators only
+ * (BEM_ERR_STATE for a mass operator).  A call whose scratch would exceed the area -- about
+ * 2 * (height + width + sum of block ranks) * nrhs values -- returns BEM_ERR_ARG before
+ * launching anything.  The work lists of the non-transposed single-vector product exist from
+ * assembly (or loading); those of another form (trans = 1, or nrhs > 1) are built by one
+ * bem_operator_mult call of that form, and until then this call returns BEM_ERR_STATE.  The
+ * first call on a device looks the array up (and may load device code): make it before any
+ * stream capture.  The area is shared by every call on a device, so overlapping calls
+ * (several streams or host threads) race: serialise them.  Bounded device waits that run out
+ * are reported by bem_operator_status. */
 int bem_operator_mult_noalloc(bem_operator_t op, int trans, const double* alpha, const void* x,
                               const double* beta, void* y, int nrhs, void* stream);
 
@@ -188,6 +191,26 @@ int bem_operator_mult_noalloc(bem_operator_t op, int trans, const double* alpha,
  * other host memory is copied up, applied and copied back. */
 int bem_operator_mult_host(bem_operator_t op, int trans, const double* alpha, const void* x,
                            const double* beta, void* y, int nrhs);
+
+/* Error flags of the operator's products on the device (no counterpart in the reference,
+ * whose products run on host threads and raise C++ exceptions).  Every wait of the product
+ * kernels is bounded; a wait that runs out sets a flag (2: a pipeline wait of the CUDA-core
+ * product kernels; 4: a grid barrier of the single-launch product; 0x100: a pipeline wait of
+ * the tensor-core products) and the kernel finishes without
+ * hanging, leaving y invalid.  bem_operator_mult and bem_operator_mult_noalloc are
+ * stream-ordered and do not read the flags; this call synchronizes the device and returns
+ * them in *flags (0 = every product since the last reset was complete).  reset != 0 clears
+ * the flags and the operator's scheduling counters and accumulators, which a product whose
+ * waits ran out leaves in an unknown state.  bem_operator_mult_host checks the flags itself
+ * and returns BEM_ERR_INTERNAL (after the reset) when one is set. */
+int bem_operator_status(bem_operator_t op, int* flags, int reset);
+
+/* Test hook of the bounded waits (no counterpart in the reference): the grid-barrier waits of
+ * the single-launch product poll at most `limit` times (0: the default, about a second) and,
+ * with extra_arrivals = 1, wait for one arrival more than the grid can make, so that every
+ * such wait runs out.  Lets a test check that a wait that runs out is reported, without a
+ * fault or a hang.  (0, 0) restores normal operation. */
+int bem_operator_test_waits(bem_operator_t op, long long limit, int extra_arrivals);
 
 /* Dense height x width matrix of the operator (row-major, host), for small cases. */
 int bem_operator_to_dense(bem_operator_t op, void* out);

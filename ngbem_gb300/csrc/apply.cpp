@@ -77,6 +77,8 @@ void HOperator::mult(int trans, const double* alpha, const void* x, const double
     f.beta[1] = beta[1];
     f.use_beta = (beta[0] != 0.0 || beta[1] != 0.0) ? 1 : 0;
     f.t_len = t_len;
+    f.wait_limit = wait_limit;
+    f.bar_extra = bar_extra;
     if (profiling) {
       BEM_CUDA(cudaEventRecord(ev[1], s));
       BEM_CUDA(cudaEventRecord(ev[2], s));
@@ -212,8 +214,19 @@ void HOperator::potential(const void* density, int npts, const double* pts, cons
 
 int HOperator::device_status() {
   int e = 0;
+  if (!d_err.p) return 0;
+  BEM_CUDA(cudaDeviceSynchronize());
   BEM_CUDA(cudaMemcpy(&e, d_err.p, sizeof(int), cudaMemcpyDeviceToHost));
   return e;
+}
+
+void HOperator::reset_device_state() {
+  BEM_CUDA(cudaDeviceSynchronize());
+  if (d_err.p) BEM_CUDA(cudaMemset(d_err.p, 0, d_err.bytes));
+  if (d_sched.p) BEM_CUDA(cudaMemset(d_sched.p, 0, d_sched.bytes));
+  for (DevBuf* b : {&d_yp, &d_t, &d_tx})
+    if (b->p) BEM_CUDA(cudaMemset(b->p, 0, b->bytes));
+  BEM_CUDA(cudaDeviceSynchronize());
 }
 
 void HOperator::collect_profile() {

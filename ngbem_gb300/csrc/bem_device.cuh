@@ -4,9 +4,27 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <atomic>
+
 #include "bem_shared.h"
 
 namespace bem {
+
+// cudaFuncSetAttribute(MaxDynamicSharedMemorySize) once per kernel and device.  The opt-in is
+// a per-device property of the function, so a process that launches FN on several devices
+// sets it on each (devices 0..63 are remembered; others set it on every call).
+template <auto FN>
+cudaError_t smem_optin(int smem) {
+  static std::atomic<unsigned long long> done{0};
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  const bool track = dev >= 0 && dev < 64;
+  if (track && ((done.load(std::memory_order_acquire) >> dev) & 1ull)) return cudaSuccess;
+  e = cudaFuncSetAttribute(FN, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  if (e == cudaSuccess && track) done.fetch_or(1ull << dev, std::memory_order_acq_rel);
+  return e;
+}
 
 // ----------------------------------------------------------------------------------------
 // complex numbers

@@ -289,9 +289,22 @@ int bem_operator_mult_host(bem_operator_t op, int trans, const double* alpha, co
     };
     void* xm = mapped(x);
     void* ym = xm ? mapped(y) : nullptr;
+    // a synchronous call reports a product whose bounded device waits ran out (and clears the
+    // operator's device state so that the next product starts clean)
+    auto check_status = [&]() {
+      auto* h = dynamic_cast<HOperator*>(o);
+      if (!h) return;
+      const int st = h->device_status();
+      if (st != 0) {
+        h->reset_device_state();
+        throw Error(BEM_ERR_INTERNAL, "a bounded device wait of the product ran out (flags " + std::to_string(st) +
+                                          "): the result is not valid");
+      }
+    };
     if (xm && ym) {
       o->mult(trans, alpha, xm, beta, ym, nrhs, 0);
       BEM_CUDA(cudaStreamSynchronize(0));
+      check_status();
       return;
     }
     if (o->stage_x.bytes < nin * esz) o->stage_x.alloc(nin * esz);
@@ -302,6 +315,31 @@ int bem_operator_mult_host(bem_operator_t op, int trans, const double* alpha, co
     o->mult(trans, alpha, o->stage_x.p, beta, o->stage_y.p, nrhs, 0);
     BEM_CUDA(cudaMemcpyAsync(y, o->stage_y.p, nout * esz, cudaMemcpyDeviceToHost, 0));
     BEM_CUDA(cudaStreamSynchronize(0));
+    check_status();
+  });
+}
+
+int bem_operator_status(bem_operator_t op, int* flags, int reset) {
+  return guarded([&] {
+    REQUIRE(op && flags, "null argument");
+    auto* h = dynamic_cast<HOperator*>(op->op.get());
+    if (!h) {
+      *flags = 0;  // a mass operator has no bounded waits
+      return;
+    }
+    *flags = h->device_status();
+    if (reset) h->reset_device_state();
+  });
+}
+
+int bem_operator_test_waits(bem_operator_t op, long long limit, int extra_arrivals) {
+  return guarded([&] {
+    REQUIRE(op, "null argument");
+    REQUIRE(limit >= 0 && extra_arrivals >= 0 && extra_arrivals <= 1, "limit >= 0, extra_arrivals 0 or 1");
+    auto* h = dynamic_cast<HOperator*>(op->op.get());
+    if (!h) throw Error(BEM_ERR_STATE, "not an H-matrix operator");
+    h->wait_limit = limit;
+    h->bar_extra = (unsigned long long)extra_arrivals;
   });
 }
 

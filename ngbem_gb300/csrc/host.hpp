@@ -244,6 +244,12 @@ struct HOperator : OperatorBase {
   unsigned mv_built = 0;
   bool mv_multi_built = false;
   int device_status();   // matvec pipeline error flags (0 = ok)
+  // Clears the error flags, the claim counters and the accumulators of the products (after a
+  // product whose bounded waits ran out: its schedule state is not the one a product leaves).
+  void reset_device_state();
+  // test hook of the single-launch product's grid-barrier waits (MVFusedArgs)
+  long long wait_limit = 0;
+  unsigned long long bar_extra = 0;
   void mult(int trans, const double* alpha, const void* x, const double* beta, void* y, int nrhs,
             cudaStream_t s) override;
   void to_dense(void* out);

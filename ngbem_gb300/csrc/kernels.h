@@ -139,7 +139,14 @@ struct MVFusedArgs {
   double alpha[2], beta[2];
   int use_beta;
   long long t_len;
+  // bounded waits of the grid barriers: polls before a wait gives up (sets error bit 4 and
+  // goes on), and arrivals added to every target (0 normally; 1 makes every barrier wait run
+  // out, which a test uses to check that the error is reported without a hang or a fault)
+  long long wait_limit;
+  unsigned long long bar_extra;
 };
+// default poll limit of the grid-barrier waits (about a second on a GB300)
+#define MV_WAIT_LIMIT (1LL << 24)
 // false if the device cannot run it (no cooperative launch or the pipeline does not fit an SM)
 bool mv_fused_supported();
 cudaError_t launch_mv_fused(int prec, bool cplx, const MVFusedArgs& f, cudaStream_t s);

@@ -720,6 +720,8 @@ struct MVGridBar {
   unsigned long long* ctr;
   unsigned long long base;
   int n;  // barriers passed in this launch
+  long long limit;            // polls before the wait gives up
+  unsigned long long extra;   // added to every target (a test makes the waits run out with 1)
 };
 __device__ __forceinline__ unsigned long long ld_acquire_u64(const unsigned long long* p) {
   unsigned long long v;
@@ -733,10 +735,10 @@ __device__ bool mv_grid_sync_cons(MVGridBar& g, int* err, int* flag) {
     __threadfence();
     asm volatile("red.release.gpu.global.add.u64 [%0], 1;" ::"l"(g.ctr) : "memory");
     g.n += 1;
-    const unsigned long long target = g.base + (unsigned long long)g.n * gridDim.x;
-    int i = 0;
+    const unsigned long long target = g.base + (unsigned long long)g.n * gridDim.x + g.extra;
+    long long i = 0;
     while (ld_acquire_u64(g.ctr) < target) {
-      if (++i > (1 << 24)) {
+      if (++i > g.limit) {
         ok = 0;
         atomicOr(err, 4);
         break;
@@ -783,7 +785,7 @@ __global__ void __launch_bounds__(MV_THREADS, 1) mv_fused_kernel(MVFusedArgs f) 
   }
   const long long ct = (long long)blockIdx.x * (MV_THREADS - 32) + (tid - 32);
   const long long cs = (long long)gridDim.x * (MV_THREADS - 32);
-  MVGridBar gb{f.bar, 0ull, 0};
+  MVGridBar gb{f.bar, 0ull, 0, f.wait_limit > 0 ? f.wait_limit : MV_WAIT_LIMIT, f.bar_extra};
   if (tid == 32) {
     // no CTA of this launch can have passed its first barrier yet: round down to the launch's base
     const unsigned long long c0 = ld_acquire_u64(f.bar);
@@ -1064,11 +1066,7 @@ static void pass_t(const MVArgs2& a, int grid, cudaStream_t s) {
   if (a.nitems <= 0) return;
   if (a.nrhs == 1) {
     const int smem = mv_smem_bytes();
-    static bool attr = false;
-    if (!attr) {
-      cudaFuncSetAttribute(mv_tma_kernel<VS, COMP>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-      attr = true;
-    }
+    if (smem_optin<mv_tma_kernel<VS, COMP>>(smem) != cudaSuccess) return;  // left for cudaGetLastError
     mv_tma_kernel<VS, COMP><<<std::min(grid, a.nitems), MV_THREADS, smem, s>>>(a);
   } else if (a.chunked) {
     mv_multi_chunk_kernel<VS, COMP><<<a.nitems, 256, 0, s>>>(a);
@@ -1096,21 +1094,24 @@ int mv_piece_elems() { return MV_PIECE; }
 template <class VS, bool COMP>
 static cudaError_t fused_t(const MVFusedArgs& f, cudaStream_t s) {
   const int smem = mv_smem_bytes();
-  static bool attr = false;
-  if (!attr) {
-    cudaError_t e = cudaFuncSetAttribute(mv_fused_kernel<VS, COMP>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-    if (e != cudaSuccess) return e;
-    attr = true;
-  }
+  cudaError_t e = smem_optin<mv_fused_kernel<VS, COMP>>(smem);
+  if (e != cudaSuccess) return e;
   // SM count and residency, queried once per device (host time on every matvec otherwise)
-  static int cached_dev = -1, nsm = 0, nb = 0;
+  static std::atomic<int> cache_nsm[64], cache_nb[64];
   int dev = 0;
-  cudaGetDevice(&dev);
-  if (dev != cached_dev) {
-    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, mv_fused_kernel<VS, COMP>, MV_THREADS, smem);
+  e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  int nsm = dev >= 0 && dev < 64 ? cache_nsm[dev].load() : 0;
+  int nb = dev >= 0 && dev < 64 ? cache_nb[dev].load() : 0;
+  if (nsm <= 0 || nb <= 0) {
+    e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
     if (e != cudaSuccess) return e;
-    cached_dev = dev;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, mv_fused_kernel<VS, COMP>, MV_THREADS, smem);
+    if (e != cudaSuccess) return e;
+    if (dev >= 0 && dev < 64) {
+      cache_nsm[dev].store(nsm);
+      cache_nb[dev].store(nb);
+    }
   }
   if (nb < 1) return cudaErrorCooperativeLaunchTooLarge;
   cudaLaunchConfig_t cfg = {};

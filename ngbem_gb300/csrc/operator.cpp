@@ -11,6 +11,7 @@
 //          persistent FP64 Sauter-Schwab kernel over the binned singular pairs
 //   host : blocks whose ACA hit the rank cap are assembled densely in a second near pass
 #include <algorithm>
+#include <cstdlib>
 #include <atomic>
 #include <chrono>
 #include <exception>
@@ -107,6 +108,10 @@ void HOperator::assemble() {
   const int leaf = dense_method ? INT_MAX : prm.leafsize;
   const double eta = dense_method ? 0.0 : prm.eta;
   if (leaf < 1) throw Error(BEM_ERR_ARG, "leafsize must be positive");
+  // NGBEM_GB300_ACA_FAIL=k (k > 0): the ACA of every far block whose number in the block list
+  // is a multiple of k fails on the host (fault injection; such blocks are assembled densely)
+  int aca_fail_every = 0;
+  if (const char* ev = std::getenv("NGBEM_GB300_ACA_FAIL")) aca_fail_every = std::max(0, std::atoi(ev));
   int kcap = prm.max_rank > 0 ? prm.max_rank : 128;
   kcap = std::min(kcap, 256);
   double eps = prm.eps;
@@ -405,6 +410,11 @@ void HOperator::assemble() {
     BEM_CUDA(cudaMemcpyAsync(ranks.data(), d_ranks.p, ranks.size() * sizeof(int), cudaMemcpyDeviceToHost, sp.a));
     BEM_CUDA(cudaMemcpyAsync(status.data(), d_status.p, status.size() * sizeof(int), cudaMemcpyDeviceToHost, sp.a));
     BEM_CUDA(cudaStreamSynchronize(sp.a));
+    // host-side fault injection for the tests of the dense fallback: the ACA of the chosen
+    // far blocks counts as failed (as if it had reached the rank cap), in every round
+    if (aca_fail_every > 0)
+      for (int f = 0; f < nf; ++f)
+        if (ids[f0 + f] % aca_fail_every == 0) status[f] = 1;
     float t;
     BEM_CUDA(cudaEventElapsedTime(&t, evA0, evA1));
     ms_aca += t;

@@ -425,13 +425,8 @@ int tc_supported() {
 
 template <int PASS>
 static cudaError_t tc_gemm_t(const TCGemmArgs& g, int grid, cudaStream_t s) {
-  static bool attr = false;
-  if (!attr) {
-    cudaError_t e = cudaFuncSetAttribute(tc_gemm_kernel<PASS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         tc_smem_bytes());
-    if (e != cudaSuccess) return e;
-    attr = true;
-  }
+  cudaError_t e = smem_optin<tc_gemm_kernel<PASS>>(tc_smem_bytes());
+  if (e != cudaSuccess) return e;
   tc_gemm_kernel<PASS><<<grid, TC_THREADS, tc_smem_bytes(), s>>>(g);
   return cudaGetLastError();
 }

@@ -93,6 +93,15 @@ def test_argument_errors_are_status_codes():
     assert _lib.lib.bem_operator_set_definedon(None, None, None) == _lib.BEM_ERR_ARG
 
 
+def test_status_plumbing_without_a_device():
+    """The device-status query and the wait test hook check their arguments on the host."""
+    flags = C.c_int(-1)
+    assert _lib.lib.bem_operator_status(None, C.byref(flags), 0) == _lib.BEM_ERR_ARG
+    assert b"null" in _lib.lib.bem_last_error()
+    assert _lib.lib.bem_operator_test_waits(None, 0, 0) == _lib.BEM_ERR_ARG
+    assert _lib.lib.bem_operator_mult_noalloc(None, 0, None, None, None, None, 1, None) == _lib.BEM_ERR_ARG
+
+
 def test_maxwell_factory_argument_checks():
     """The HCurl space and the Maxwell double-layer / curl factories check their spaces before
     any assembly (no GPU needed)."""

@@ -4,7 +4,8 @@ Both entry points run the same kernels on the same operator data, so they agree 
 order of the FP64 atomic additions: 1e-12 relative is the tolerance.  Each case calls the
 no-allocation entry point twice in a row with different inputs (and then the first input
 again), which checks that every call starts from cleared accumulators even though the
-scratch area keeps the previous call's contents.  Kept last in collection order so that it
+scratch area keeps the previous call's contents.  The reference products come first: they
+build the work lists of each form, which the no-allocation entry point uses but never builds.  Kept last in collection order so that it
 runs both after the other GPU tests and, alone, in a fresh process.
 """
 import ctypes as C
@@ -79,15 +80,37 @@ def test_noalloc_matches_mult(case):
 
 
 def test_noalloc_leaves_device_memory_alone():
+    # the first call on the device looks the array up (and may load the device code holding it)
+    warm = _operator("laplace_sl", "P0", "P0", 0.0, "mixed", level=2)
+    xw, yw = _vectors(warm, 0, 1, 3)
+    _call(_lib.lib.bem_operator_mult_noalloc, warm, 0, 1.0, xw, 0.0, yw, 1)
+    # a fresh operator: already its first no-allocation product allocates nothing
     mat = _operator("laplace_sl", "P0", "P0", 0.0, "mixed")
     x, y = _vectors(mat, 0, 1, 3)
-    _call(_lib.lib.bem_operator_mult_noalloc, mat, 0, 1.0, x, 0.0, y, 1)  # first call: set-up
+    ref = y.clone()
+    _call(_lib.lib.bem_operator_mult, mat, 0, 1.0, x, 0.0, ref, 1)
     torch.cuda.synchronize()
     free0 = torch.cuda.mem_get_info()[0]
     for _ in range(3):
         _call(_lib.lib.bem_operator_mult_noalloc, mat, 0, 1.0, x, 0.0, y, 1)
     torch.cuda.synchronize()
     assert torch.cuda.mem_get_info()[0] >= free0
+    assert _rel(y, ref) < TOL
+
+
+def test_noalloc_never_builds_work_lists():
+    """A form whose work lists the operator does not have yet is refused (BEM_ERR_STATE)
+    instead of building them; one bem_operator_mult of that form builds them."""
+    mat = _operator("laplace_dl", "P1", "P0", 0.0, "mixed")
+    x, y = _vectors(mat, 1, 1, 5)
+    with pytest.raises(_lib.BemError) as e:
+        _call(_lib.lib.bem_operator_mult_noalloc, mat, 1, 1.0, x, 0.0, y, 1)
+    assert e.value.code == _lib.BEM_ERR_STATE and "bem_operator_mult" in str(e.value)
+    ref = y.clone()
+    _call(_lib.lib.bem_operator_mult, mat, 1, 1.0, x, 0.0, ref, 1)
+    _call(_lib.lib.bem_operator_mult_noalloc, mat, 1, 1.0, x, 0.0, y, 1)
+    torch.cuda.synchronize()
+    assert _rel(y, ref) < TOL
 
 
 def test_noalloc_rejects_oversized_scratch():
