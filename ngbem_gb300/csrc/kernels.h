@@ -272,11 +272,19 @@ struct TCSeg {
   int pad[3];
 };
 struct TCItem {
-  int seg0, nseg;  // segments accumulated into one TMEM accumulator
+  int seg0, nseg;  // segments summed into the item's result
   int N;           // MMA N: multiple of 16, 16..256
   int out0, nout;  // pass 0: outputs [out0, out0+nout); pass 1: partial row offset, rows
-  int pad[3];
+  int nk2;         // MMA K steps (K = 8) of all its segments
+  int pad[2];
 };
+// The accumulation inside tcgen05.mma rounds toward zero, so its error grows linearly with the
+// number of MMAs into one accumulator (about 2.5e-8 relative per MMA, measured on GB300).  An
+// item's K steps therefore go round-robin to the A = 256 / round_up(N, 32) accumulators of a
+// 256-column tensor-memory buffer, each taking at most TC_CHAIN of them (2 TC_CHAIN MMAs: high
+// and low B parts) before the buffer is handed to the epilogue, which adds the accumulators
+// into FP32 sums that round to nearest; the other buffer takes the next K steps meanwhile.
+#define TC_CHAIN 4
 struct TCOut {            // pass 0: one low-rank block of a column tile
   unsigned long long ta;  // its A panel for pass 1 (128 x 2 rpad)
   int col, rpad;          // first accumulator column; rank padded to a multiple of 4

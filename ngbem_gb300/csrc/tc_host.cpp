@@ -224,6 +224,7 @@ void HOperator::build_tc() {
       I.seg0 = (int)sg0.size();
       I.nseg = 1;
       I.N = N;
+      I.nk2 = nkc / 2;
       I.out0 = (int)outs.size();
       I.nout = (int)tile.size();
       for (const OutRef& o : tile) {
@@ -278,6 +279,7 @@ void HOperator::build_tc() {
       I.N = N;
       I.out0 = (int)(yrows + i0);
       I.nout = nr;
+      I.nk2 = 0;
       double c = 256.0 * N;
       for (int f : kv.second) {
         TCUJob J{};
@@ -294,6 +296,7 @@ void HOperator::build_tc() {
         sg1.push_back(S);
         sg1_kind.push_back(0);
         ujobs.push_back(J);
+        I.nk2 += S.nkc / 2;
         c += (double)J.nkc * (2048.0 + 32.0 * N);
         up_bytes += (long long)J.nkc * 32 * N;
       }
@@ -314,6 +317,7 @@ void HOperator::build_tc() {
         sg1.push_back(S);
         sg1_kind.push_back(1);
         djobs.push_back(J);
+        I.nk2 += S.nkc / 2;
         c += (double)J.nkc * (2048.0 + 32.0 * N);
         dp_bytes += (long long)J.nkc * 32 * N;
       }

@@ -18,13 +18,18 @@
 // into one accumulator.  Summing the two h rows gives (a_hi + a_lo)(b_hi + b_lo): a split-TF32
 // product about 2^-21 from the exact one, accumulated in FP32 (TMEM).
 //
-// Kernel roles (192 threads, one CTA per SM, persistent over a host-balanced item list):
+// Kernel roles (320 threads, one CTA per SM, persistent over a host-balanced item list):
 //   warp 0      bulk copies (cp.async.bulk + mbarrier complete_tx) of A and B K-ranges into a
 //               4-stage ring;
-//   warp 1      owns the tensor memory (512 columns: two 256-column accumulators) and one
-//               thread issues tcgen05.mma, releasing stages and accumulators by tcgen05.commit;
-//   warps 2-5   epilogue: tcgen05.ld of their TMEM lane quarter, combination of the real and
-//               imaginary and high and low rows with warp shuffles, global stores.
+//   warp 1      owns the tensor memory (512 columns: two 256-column buffers) and one thread
+//               issues tcgen05.mma, releasing stages and buffers by tcgen05.commit;
+//   warps 2-9   epilogue: tcgen05.ld of their TMEM lane quarter (two warps per quarter, one
+//               per half of the item's columns), FP32 sums of the accumulators, combination of
+//               the real and imaginary and high and low rows with warp shuffles, global stores.
+// Accuracy: tcgen05.mma accumulates with rounding toward zero, so the error of one accumulator
+// grows linearly with the MMAs it takes.  A buffer holds A = 256 / round_up(N, 32) accumulators
+// of the item; its K steps go to them round-robin, at most TC_CHAIN each, and the buffer then
+// goes to the epilogue, whose sums round to nearest (kernels.h).
 // Every wait is bounded: a wait that runs out sets an error bit, the CTA drains what it
 // issued and frees its tensor memory.
 #include <algorithm>
@@ -36,7 +41,7 @@
 namespace bem {
 
 #define TC_NST 4
-#define TC_THREADS 192
+#define TC_THREADS 320  // warp 0 copies, warp 1 MMAs, warps 2-9 epilogue
 #define TC_ACC_COLS 256
 #define TC_HDR 4096  // barriers, then the range descriptors of each stage (TC_MAXCH x 32 bytes)
 #define TC_DESC 1024
@@ -133,9 +138,9 @@ __device__ __forceinline__ void tmem_ld8(uint32_t taddr, float (&v)[8]) {
 #pragma unroll
   for (int k = 0; k < 8; ++k) v[k] = __uint_as_float(r[k]);
 }
-// 8 columns into v[8 J .. 8 J + 7] of a 32-value batch (tmem_wait32 completes the batch)
+// 8 columns into v[8 J .. 8 J + 7] of a 16-value batch (tmem_wait16 completes the batch)
 template <int J>
-__device__ __forceinline__ void tmem_ld8_at(uint32_t taddr, float (&v)[32]) {
+__device__ __forceinline__ void tmem_ld8_at(uint32_t taddr, float (&v)[16]) {
   uint32_t r[8];
   asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0, %1, %2, %3, %4, %5, %6, %7}, [%8];"
                : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7])
@@ -144,13 +149,11 @@ __device__ __forceinline__ void tmem_ld8_at(uint32_t taddr, float (&v)[32]) {
 #pragma unroll
   for (int k = 0; k < 8; ++k) v[8 * J + k] = __uint_as_float(r[k]);
 }
-__device__ __forceinline__ void tmem_wait32(float (&v)[32]) {
+__device__ __forceinline__ void tmem_wait16(float (&v)[16]) {
   asm volatile("tcgen05.wait::ld.sync.aligned;"
                : "+f"(v[0]), "+f"(v[1]), "+f"(v[2]), "+f"(v[3]), "+f"(v[4]), "+f"(v[5]), "+f"(v[6]), "+f"(v[7]),
                  "+f"(v[8]), "+f"(v[9]), "+f"(v[10]), "+f"(v[11]), "+f"(v[12]), "+f"(v[13]), "+f"(v[14]),
-                 "+f"(v[15]), "+f"(v[16]), "+f"(v[17]), "+f"(v[18]), "+f"(v[19]), "+f"(v[20]), "+f"(v[21]),
-                 "+f"(v[22]), "+f"(v[23]), "+f"(v[24]), "+f"(v[25]), "+f"(v[26]), "+f"(v[27]), "+f"(v[28]),
-                 "+f"(v[29]), "+f"(v[30]), "+f"(v[31])
+                 "+f"(v[15])
                :
                : "memory");
 }
@@ -196,7 +199,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) tc_gemm_kernel(TCGemmArgs g) {
     }
     for (int a = 0; a < 2; ++a) {
       bar_init(&S.accf[a], 1);
-      bar_init(&S.acce[a], 4);
+      bar_init(&S.acce[a], TC_THREADS / 32 - 2);  // one arrival per epilogue warp
     }
     bar_init(&S.fin, 1);
     S.abort_flag = 0;
@@ -258,9 +261,17 @@ __global__ void __launch_bounds__(TC_THREADS, 1) tc_gemm_kernel(TCGemmArgs g) {
         bar_wait(&S.empty[j % TC_NST], (j / TC_NST) & 1, abort_flag, g.err);
   } else if (warp == 1) {
     if (lane == 0) {
-      int acc_it = 0, acc = 0;
-      uint32_t d = 0, idesc = 0, accumulate = 0;
-      bool ok = true, issued = false;
+      int acc_it = 0, buf = 0, A = 1, stride = TC_ACC_COLS, rlen = TC_CHAIN, r = 0, ai = 0;
+      uint32_t base = 0, idesc = 0;
+      bool ok = true, issued = false, fresh = true;
+      // the next buffer, once the epilogue has released it
+      auto take_buffer = [&]() -> bool {
+        buf = acc_it & 1;
+        if (!bar_wait(&S.acce[buf], ((acc_it >> 1) & 1) ^ 1, abort_flag, g.err)) return false;
+        tc_fence_after();
+        base = tmem + (uint32_t)(buf * TC_ACC_COLS);
+        return true;
+      };
       for (int it = 0; ok && it < my.w; ++it) {
         const int slot = it % TC_NST;
         if (!bar_wait(&S.full[slot], (it / TC_NST) & 1, abort_flag, g.err)) break;
@@ -270,31 +281,47 @@ __global__ void __launch_bounds__(TC_THREADS, 1) tc_gemm_kernel(TCGemmArgs g) {
         for (int c = 0; c < TC_MAXCH; ++c) {
           const TCChunk cd = cds[c];
           if (cd.flags & 1) {
-            // first range of an item: take the accumulator the epilogue released
-            acc = acc_it & 1;
-            if (!bar_wait(&S.acce[acc], ((acc_it >> 1) & 1) ^ 1, abort_flag, g.err)) {
+            // first range of an item: its accumulators, round-robin over a fresh buffer
+            stride = ((int)cd.N + 31) & ~31;
+            A = TC_ACC_COLS / stride;
+            rlen = A * TC_CHAIN;
+            r = 0;
+            ai = 0;
+            fresh = true;
+            idesc = idesc_tf32(128, cd.N);
+            if (!take_buffer()) {
               ok = false;
               break;
             }
-            tc_fence_after();
-            d = tmem + (uint32_t)(acc * TC_ACC_COLS);
-            idesc = idesc_tf32(128, cd.N);
-            accumulate = 0;
           }
           const uint32_t N = cd.N, bstride = 32u * N, kcs = cd.abytes / 2048u;
           const uint32_t sa = sp + cd.off, sb = sa + cd.abytes;
           for (uint32_t k2 = 0; k2 < kcs; k2 += 2) {
+            if (r == 0 && !fresh) {
+              // every accumulator of the buffer took TC_CHAIN K steps: the epilogue adds them
+              // into its sums while the other buffer takes the next ones
+              mma_commit(&S.accf[buf]);
+              ++acc_it;
+              if (!take_buffer()) {
+                ok = false;
+                break;
+              }
+            }
+            fresh = false;
+            const uint32_t d = base + (uint32_t)(ai * stride);
             const uint64_t ad = sdesc(sa + k2 * 2048u, 2048u, 128u);
             const uint64_t bh = sdesc(sb + k2 * bstride, bstride, 128u);
             const uint64_t bl = sdesc(sb + k2 * bstride + 16u * N, bstride, 128u);
-            mma_tf32(d, ad, bh, idesc, accumulate);
+            mma_tf32(d, ad, bh, idesc, r >= A ? 1u : 0u);  // the first K step of an accumulator overwrites it
             mma_tf32(d, ad, bl, idesc, 1u);
-            accumulate = 1;
+            if (++ai == A) ai = 0;
+            if (++r == rlen) r = 0;
           }
+          if (!ok) break;
           issued = true;
           if (cd.flags & 2) {
-            // last range of the item: hand the accumulator to the epilogue
-            mma_commit(&S.accf[acc]);
+            // last range of the item: hand its last buffer to the epilogue
+            mma_commit(&S.accf[buf]);
             ++acc_it;
           }
           if (cd.flags & 4) break;
@@ -308,102 +335,139 @@ __global__ void __launch_bounds__(TC_THREADS, 1) tc_gemm_kernel(TCGemmArgs g) {
       }
     }
   } else {
-    // epilogue: warp w reads TMEM lanes [32 (w % 4), +32): accumulator row 32 (w % 4) + lane
-    const int q4 = warp & 3;
+    // epilogue: warps 2..9.  Warp w reads TMEM lanes [32 (w % 4), +32) (accumulator row
+    // 32 (w % 4) + lane) and half of the item's columns (hc = (w - 2) / 4 picks the half).
+    // Every buffer of an item is added into the warp's FP32 sums (round to nearest); after the
+    // last one the sums are combined and stored.
+    const int q4 = warp & 3, hc = (warp - 2) >> 2;
     const int row = 32 * q4 + lane;
     const int rhs = row >> 2, a = (row >> 1) & 1, h = row & 1;
     const unsigned FULL = 0xffffffffu;
     int acc_it = 0;
     TCItem In{};
     if (my.y > 0) In = g.items[my.x];
-    for (int ii = my.x; ii < iend; ++ii) {
+    bool ok = true;
+    for (int ii = my.x; ok && ii < iend; ++ii) {
       const TCItem I = In;
       if (ii + 1 < iend) In = g.items[ii + 1];  // next item's descriptor, loaded early
       // pass 0: lane o holds the output descriptor of block o of the tile (at most 32 blocks:
       // N <= 256 and a block takes at least 8 columns), loaded before the accumulator wait
       TCOut oc{};
       if (PASS == 0 && lane < I.nout) oc = g.outs[I.out0 + lane];
-      const int acc = acc_it & 1;
-      int ok = 1;
-      if (lane == 0) ok = bar_wait(&S.accf[acc], (acc_it >> 1) & 1, abort_flag, g.err) ? 1 : 0;
-      ok = __shfl_sync(FULL, ok, 0);
+      // the two warps of a lane quarter split the item's columns (N is a multiple of 16)
+      const int half = I.N >> 1;
+      const int c0 = hc * half;   // first column of this warp
+      const int ng8 = half >> 3;  // its 8-column groups (<= 16)
+      const int stride = (I.N + 31) & ~31, A = TC_ACC_COLS / stride, rlen = A * TC_CHAIN;
+      const int nround = (I.nk2 + rlen - 1) / rlen;
+      float sum[4][32];
+#pragma unroll
+      for (int b = 0; b < 4; ++b)
+#pragma unroll
+        for (int k = 0; k < 32; ++k) sum[b][k] = 0.f;
+      for (int rd = 0; rd < nround; ++rd) {
+        const int used = min(A, I.nk2 - rd * rlen);  // accumulators written in this round
+        const int buf = acc_it & 1;
+        int w = 1;
+        if (lane == 0) w = bar_wait(&S.accf[buf], (acc_it >> 1) & 1, abort_flag, g.err) ? 1 : 0;
+        if (!__shfl_sync(FULL, w, 0)) {
+          ok = false;
+          break;
+        }
+        tc_fence_after();
+        for (int ac = 0; ac < used; ++ac) {
+          const uint32_t tb = tmem + ((uint32_t)(32 * q4) << 16) + (uint32_t)(buf * TC_ACC_COLS + ac * stride + c0);
+#pragma unroll
+          for (int b = 0; b < 4; ++b) {
+#pragma unroll
+            for (int hf = 0; hf < 2; ++hf) {
+              // 16 columns at a time (register pressure: the sums hold 128)
+              const int g0 = 4 * b + 2 * hf;
+              if (g0 < ng8) {
+                float v[16];
+                const uint32_t t0 = tb + (uint32_t)(8 * g0);
+                tmem_ld8_at<0>(t0, v);
+                if (g0 + 1 < ng8) tmem_ld8_at<1>(t0 + 8, v);
+                tmem_wait16(v);
+#pragma unroll
+                for (int J = 0; J < 2; ++J)
+                  if (g0 + J < ng8)  // only the groups that were loaded
+#pragma unroll
+                    for (int k = 0; k < 8; ++k) sum[b][16 * hf + 8 * J + k] += v[8 * J + k];
+              }
+            }
+          }
+        }
+        tc_fence_before();
+        __syncwarp();
+        if (lane == 0) bar_arrive(&S.acce[buf]);
+        ++acc_it;
+      }
       if (!ok) break;
-      tc_fence_after();
-      const uint32_t tb = tmem + ((uint32_t)(32 * q4) << 16) + (uint32_t)(acc * TC_ACC_COLS);
+      const int nb = (ng8 + 3) >> 2;
       if (PASS == 0) {
         // columns (rank k, real/imaginary c) of each block: T = V2 x combined from the four
         // real products, written as the block's pass-1 A panel: row (r, a', h') holds, for
         // K = (k, c), the h' part of  a' = 0: (Re T_k, -Im T_k);  a' = 1: (Im T_k, Re T_k)
-        for (int o = 0; o < I.nout; ++o) {
-          float4* ta = (float4*)__shfl_sync(FULL, oc.ta, o);
-          const int col = __shfl_sync(FULL, oc.col, o), nc = 2 * __shfl_sync(FULL, oc.rpad, o);
-          for (int c = 0; c < nc; c += 32) {
-            const int ng = min(4, (nc - c) >> 3);  // 8-column groups in this batch (warp-uniform)
-            float v[32];
-            const uint32_t t0 = tb + (uint32_t)(col + c);
-            tmem_ld8_at<0>(t0, v);
-            if (ng > 1) tmem_ld8_at<1>(t0 + 8, v);
-            if (ng > 2) tmem_ld8_at<2>(t0 + 16, v);
-            if (ng > 3) tmem_ld8_at<3>(t0 + 24, v);
-            tmem_wait32(v);
 #pragma unroll
-            for (int j = 0; j < 4; ++j) {
-              if (j >= ng) break;
-              float sm[8], pm[8], out[8];
+        for (int b = 0; b < 4; ++b) {
+          if (b >= nb) break;
 #pragma unroll
-              for (int k = 0; k < 8; ++k) sm[k] = v[8 * j + k] + __shfl_xor_sync(FULL, v[8 * j + k], 1);  // hi + lo
+          for (int j = 0; j < 4; ++j) {
+            if (4 * b + j >= ng8) break;           // past this warp's columns
+            const int gcol = c0 + 32 * b + 8 * j;  // warp-uniform
+            const unsigned m = __ballot_sync(FULL, lane < I.nout && oc.col <= gcol);
+            const int o = __popc(m) - 1;
+            float4* ta = (float4*)__shfl_sync(FULL, oc.ta, o < 0 ? 0 : o);
+            const int col = __shfl_sync(FULL, oc.col, o < 0 ? 0 : o);
+            const int nc = 2 * __shfl_sync(FULL, oc.rpad, o < 0 ? 0 : o);
+            if (o < 0 || gcol >= col + nc) continue;  // padding columns after the last block
+            float sm[8], pm[8], out[8];
 #pragma unroll
-              for (int k = 0; k < 8; ++k) pm[k] = __shfl_xor_sync(FULL, sm[k], 2);  // the other part a
+            for (int k = 0; k < 8; ++k) sm[k] = sum[b][8 * j + k] + __shfl_xor_sync(FULL, sum[b][8 * j + k], 1);
 #pragma unroll
-              for (int k = 0; k < 4; ++k) {
-                const float rr = a ? pm[2 * k] : sm[2 * k];          // sum_j Re x Re V
-                const float ri = a ? pm[2 * k + 1] : sm[2 * k + 1];  // sum_j Re x Im V
-                const float ir = a ? sm[2 * k] : pm[2 * k];          // sum_j Im x Re V
-                const float ii2 = a ? sm[2 * k + 1] : pm[2 * k + 1]; // sum_j Im x Im V
-                const float tr = rr - ii2, ti = ri + ir;
-                out[2 * k] = tf32_part(a ? ti : tr, h);
-                out[2 * k + 1] = tf32_part(a ? tr : -ti, h);
-              }
-              const int kc = (c + 8 * j) >> 2;
-              ta[(size_t)kc * 128 + row] = make_float4(out[0], out[1], out[2], out[3]);
-              ta[(size_t)(kc + 1) * 128 + row] = make_float4(out[4], out[5], out[6], out[7]);
+            for (int k = 0; k < 8; ++k) pm[k] = __shfl_xor_sync(FULL, sm[k], 2);  // the other part a
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+              const float rr = a ? pm[2 * k] : sm[2 * k];          // sum_j Re x Re V
+              const float ri = a ? pm[2 * k + 1] : sm[2 * k + 1];  // sum_j Re x Im V
+              const float ir = a ? sm[2 * k] : pm[2 * k];          // sum_j Im x Re V
+              const float ii2 = a ? sm[2 * k + 1] : pm[2 * k + 1]; // sum_j Im x Im V
+              const float tr = rr - ii2, ti = ri + ir;
+              out[2 * k] = tf32_part(a ? ti : tr, h);
+              out[2 * k + 1] = tf32_part(a ? tr : -ti, h);
             }
+            const int kc = (gcol - col) >> 2;
+            ta[(size_t)kc * 128 + row] = make_float4(out[0], out[1], out[2], out[3]);
+            ta[(size_t)(kc + 1) * 128 + row] = make_float4(out[4], out[5], out[6], out[7]);
           }
         }
       } else {
         // columns = rows i of the row tile; row (r, a, h) holds the h part of Re/Im (U2 T)_i
         float2* yp = (float2*)g.ypart;
         const int u = lane & 3;
-        for (int c = 0; c < I.nout; c += 32) {
-          const int ng = min(4, (I.nout - c + 7) >> 3);
-          float v[32];
-          const uint32_t t0 = tb + (uint32_t)c;
-          tmem_ld8_at<0>(t0, v);
-          if (ng > 1) tmem_ld8_at<1>(t0 + 8, v);
-          if (ng > 2) tmem_ld8_at<2>(t0 + 16, v);
-          if (ng > 3) tmem_ld8_at<3>(t0 + 24, v);
-          tmem_wait32(v);
+#pragma unroll
+        for (int b = 0; b < 4; ++b) {
+          if (b >= nb) break;
 #pragma unroll
           for (int j = 0; j < 4; ++j) {
-            if (j >= ng) break;
+            if (4 * b + j >= ng8) break;  // past this warp's columns
+            const int i0 = c0 + 32 * b + 8 * j;
+            if (i0 >= I.nout) break;
             float sm[8], pm[8];
 #pragma unroll
-            for (int k = 0; k < 8; ++k) sm[k] = v[8 * j + k] + __shfl_xor_sync(FULL, v[8 * j + k], 1);
+            for (int k = 0; k < 8; ++k) sm[k] = sum[b][8 * j + k] + __shfl_xor_sync(FULL, sum[b][8 * j + k], 1);
 #pragma unroll
             for (int k = 0; k < 8; ++k) pm[k] = __shfl_xor_sync(FULL, sm[k], 2);
 #pragma unroll
             for (int k = 0; k < 8; ++k) {
-              const int i = c + 8 * j + k;
+              const int i = i0 + k;
               if ((k >> 1) == u && i < I.nout)
                 yp[(size_t)(I.out0 + i) * 32 + rhs] = make_float2(a ? pm[k] : sm[k], a ? sm[k] : pm[k]);
             }
           }
         }
       }
-      tc_fence_before();
-      __syncwarp();
-      if (lane == 0) bar_arrive(&S.acce[acc]);
-      ++acc_it;
     }
   }
   tc_fence_before();

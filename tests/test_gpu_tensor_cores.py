@@ -66,10 +66,12 @@ def test_tensor_core_products(bm, nrhs):
     assert info["state"] == 1 and info["bytes"] > 0 and min(info["items"]) > 0
     y_tc = _apply(A32, x)
     y64 = _apply(A64, x)
-    assert rel(y_tc, y_comp) < 1e-5
-    assert rel(y_tc, y64) < 2e-5
+    # split-TF32 products, accumulators of at most 2 TC_CHAIN MMAs summed with round-to-nearest:
+    # the product meets the 1e-6 bar against the FP64 path
+    assert rel(y_tc, y_comp) < 1e-6
+    assert rel(y_tc, y64) < 1.5e-6
     for r in range(nrhs):
-        assert rel(y_tc[:, r], y_comp[:, r]) < 2e-5
+        assert rel(y_tc[:, r], y_comp[:, r]) < 2e-6
     # off: the CUDA-core plain products
     A32.set_tensor_cores(False)
     assert A32.tensor_cores()["state"] == 0
