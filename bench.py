@@ -64,6 +64,9 @@ def parse():
                          "the headline); dtn: Laplace DtN on the L5 icosphere, single-vector V matvec; shape: "
                          "batched single-layer energy + adjoint shape gradient over 64 perturbed icospheres "
                          "(L2..L5); maxwell: EFIE on RT0 of the L5 icosphere")
+    ap.add_argument("--apply-only", action="store_true",
+                    help="bm: assemble the mixed operator, then only the warm-up and timed applications "
+                         "(profiling runs: no FP64 path, no solves, no host-buffer steps)")
     ap.add_argument("--ref-sample", type=int, default=4,
                     help="bm reference arm: right-hand sides per step (the oracle applies one vector at a time)")
     ap.add_argument("--l2-flush", default="write+read", choices=["write+read", "write"],
@@ -654,6 +657,9 @@ def run_bm(args):
     L = args.level or 6
     nrhs = BM_NRHS
 
+    if args.apply_only:
+        run_bm_apply(args, nb, _lib, dev, L)
+        return
     # untimed warm-up of both paths on a small ellipsoid (module loading, workspaces, graphs,
     # the tensor-core self-test)
     wm = nb.ellipsoid(2, BM_AXES)
@@ -869,6 +875,49 @@ def run_bm(args):
         print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
+
+
+def run_bm_apply(args, nb, _lib, dev, L):
+    """Profiling form of the Burton-Miller line: the mixed operator is assembled, then W warm-up
+    and K timed applications to the 32 right-hand sides run back to back (kernel launches in
+    order: per application tc_xprep, tc_gemm pass 0, tc_gemm pass 1, tc_ysum_out)."""
+    import ctypes as C
+
+    import torch
+
+    from ngbem_gb300.forms import p1_load_vector, plane_wave_bm_source, random_directions
+    nrhs = BM_NRHS
+    mesh = nb.ellipsoid(L, BM_AXES)
+    Fh = p1_load_vector(mesh, plane_wave_bm_source(BM_KAPPA, random_directions(nrhs, BM_SEED)), order=6)
+    Xc = torch.from_numpy(Fh).to(dev).t().contiguous()
+    P1 = nb.H1(mesh, complex=True)
+    Cop = nb.HelmholtzCombinedFieldOperator(P1, P1, kappa=BM_KAPPA, precision="mixed", **BM_OPTS)
+    Cm = Cop.mat
+    Cm.set_accuracy(False)
+    Cm.set_tensor_cores(True)
+    Y = torch.empty_like(Xc)
+    stream = torch.cuda.current_stream()
+    one, zero = _lib.cplx2(1.0), _lib.cplx2(0.0)
+
+    def apply():
+        _lib.check(_lib.lib.bem_operator_mult(Cm.h, 0, one, C.c_void_p(Xc.data_ptr()), zero,
+                                              C.c_void_p(Y.data_ptr()), nrhs, C.c_void_p(stream.cuda_stream)))
+
+    for _ in range(args.warmup):
+        apply()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        apply()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / max(1, args.steps)
+    info = Cm.info
+    print(json.dumps({"metric": "tensor-core application to 32 right-hand sides (profiling form)",
+                      "value": nrhs * 1e3 / ms, "unit": "matvec/s", "ms_per_step": ms, "steps": args.steps,
+                      "warmup": args.warmup, "config": dict(bm_workload(L), l2="not flushed (back to back)"),
+                      "bytes_stored": info["bytes_dense"] + info["bytes_lowrank"], "nze": info["nze"],
+                      "tensor_cores": Cm.tensor_cores()}), flush=True)
 
 
 def run_maxwell(args):

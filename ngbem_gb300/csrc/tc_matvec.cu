@@ -57,25 +57,24 @@ __device__ __forceinline__ void bar_init(uint64_t* b, int count) {
 __device__ __forceinline__ void bar_arrive(uint64_t* b) {
   asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(su32(b)) : "memory");
 }
+// One potentially blocking test of the phase of `parity`: the warp is suspended in hardware
+// until the phase completes or about a microsecond has passed (no issue slots spent polling).
 __device__ __forceinline__ bool bar_try(uint64_t* b, uint32_t parity) {
   uint32_t ok;
   asm volatile(
-      "{\n .reg .pred p;\n mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n selp.u32 %0, 1, 0, p;\n}\n"
       : "=r"(ok)
-      : "r"(su32(b)), "r"(parity)
+      : "r"(su32(b)), "r"(parity), "r"(1000u)
       : "memory");
   return ok != 0;
 }
-// Bounded wait for the phase of `parity` to complete (non-blocking polls, a short sleep every
-// 256 of them: the limit is well under a second).  Returns false when the CTA is aborting or
-// when the limit ran out (then the error bit is set and the CTA aborts).
+// Bounded wait for the phase of `parity` to complete (at most 2^21 suspended tests: about two
+// seconds at most).  Returns false when the CTA is aborting or when the limit ran out (then the
+// error bit is set and the CTA aborts).
 __device__ bool bar_wait(uint64_t* b, uint32_t parity, volatile int* abort_flag, int* err) {
-  for (int i = 0; i < (1 << 22); ++i) {
+  for (int i = 0; i < (1 << 21); ++i) {
     if (bar_try(b, parity)) return true;
-    if ((i & 255) == 255) {
-      if (*abort_flag) return false;
-      __nanosleep(128);
-    }
+    if ((i & 255) == 255 && *abort_flag) return false;
   }
   atomicOr(err, TC_ERR_WAIT);
   *abort_flag = 1;
