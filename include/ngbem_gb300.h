@@ -186,6 +186,21 @@ int bem_operator_mult(bem_operator_t op, int trans, const double* alpha, const v
 int bem_operator_mult_noalloc(bem_operator_t op, int trans, const double* alpha, const void* x,
                               const double* beta, void* y, int nrhs, void* stream);
 
+/* Global dof numbering of the vectors the products act on (reference: the HMatrix of an
+ * IntegralOperator is width_vol_dof x height_vol_dof, src/hmat.hpp:178-179, and its blocks
+ * gather x and scatter y through the FE space's global dof numbers, src/hmat.cpp:473-515, from
+ * the boundary maps of src/ngbem.cpp:43-65).  trial_map[d] (test_map[d]) is the global number
+ * of dof d of the trial (test) space in a vector of trial_nglobal (test_nglobal) entries: e.g.
+ * the volume dof of a boundary dof of a definedon space.  Maps are injective; entries that hold
+ * no dof of the output space are set to beta * y (0 for a plain product), as the reference's
+ * Mult zeroes y and MultAdd leaves them.  After this call bem_operator_mult,
+ * bem_operator_mult_noalloc and bem_operator_mult_host take x and y in the global numbering
+ * (leading dimension trial_nglobal / test_nglobal for several right-hand sides); a NULL map
+ * restores the compact numbering of that space.  bem_gmres and bem_operator_to_dense keep the
+ * compact numbering.  H-matrix operators only. */
+int bem_operator_set_global_dofs(bem_operator_t op, int trial_nglobal, const int* trial_map, int test_nglobal,
+                                 const int* test_map);
+
 /* Same with HOST buffers (synchronous).  Page-locked buffers (cudaHostAlloc, torch
  * pin_memory) are read and written by the kernels in place through their device mapping;
  * other host memory is copied up, applied and copied back. */

@@ -73,6 +73,7 @@ SIGNATURES = {
     "bem_operator_mult_host": ([_vp, C.c_int, _dp, _vp, _dp, _vp, C.c_int], C.c_int),
     "bem_operator_to_dense": ([_vp, _vp], C.c_int),
     "bem_operator_status": ([_vp, _ip, C.c_int], C.c_int),
+    "bem_operator_set_global_dofs": ([_vp, C.c_int, _ip, C.c_int, _ip], C.c_int),
     "bem_operator_test_waits": ([_vp, C.c_longlong, C.c_int], C.c_int),
     "bem_operator_destroy": ([_vp], C.c_int),
     "bem_operator_set_profiling": ([_vp, C.c_int], C.c_int),

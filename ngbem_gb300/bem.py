@@ -453,6 +453,25 @@ class HMatrix(_NativeMatrix):
                                     (test_space or trial_space).h, C.byref(h)))
         return cls(h)
 
+    def set_global_dofs(self, trial_map, trial_nglobal: int, test_map=None, test_nglobal: int | None = None):
+        """Apply the matrix to vectors in a global dof numbering (the reference's HMatrix acts on
+        the FE space's full vectors, width_vol_dof x height_vol_dof, src/hmat.hpp:178-179):
+        dof d of the trial space is entry trial_map[d] of a vector of trial_nglobal entries
+        (test likewise; test_map None: the compact test numbering).  Entries that hold no dof of
+        the output are
+        set to beta * y (Mult: 0).  trial_map None restores the compact numbering.  Solves with
+        GMRes keep the compact numbering and refuse a matrix with global numbering."""
+        def arr(m):
+            return None if m is None else np.ascontiguousarray(m, dtype=np.int32)
+        tm, em = arr(trial_map), arr(test_map)
+        check(lib.bem_operator_set_global_dofs(self.h, int(trial_nglobal or 0),
+                                               None if tm is None else tm.ctypes.data_as(_lib._ip),
+                                               int(test_nglobal or 0),
+                                               None if em is None else em.ctypes.data_as(_lib._ip)))
+        self.width = int(trial_nglobal) if tm is not None else self.info["width"]
+        self.height = int(test_nglobal) if em is not None else self.info["height"]
+        self.global_numbering = tm is not None or em is not None
+
     def set_tensor_cores(self, enable: bool = True):
         """Tensor-core products for 2..32 right-hand sides at plain accuracy (complex FP32 storage):
         True builds the packed panels now when the operator qualifies, False turns them off."""
@@ -768,6 +787,9 @@ def GMRes(A, b, pre=None, freedofs=None, x=None, maxsteps=100, tol=1e-7, innerpr
     for _, M in terms:
         if not isinstance(M, _NativeMatrix):
             raise TypeError("GMRes needs sums of H-matrices and mass matrices")
+        if getattr(M, "global_numbering", False):
+            raise ValueError("GMRes works in the compact dof numbering: reset the matrix's global numbering "
+                             "(set_global_dofs(None, 0))")
     cplx = any(M.is_complex or isinstance(c, complex) for c, M in terms)
     dt = torch.complex128 if cplx else torch.float64
     bd = _as_device(b, dt)

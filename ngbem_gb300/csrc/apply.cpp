@@ -10,6 +10,65 @@
 
 namespace bem {
 
+HOperator::VecMap HOperator::vec_map(int trans) const {
+  const bool shared = ttest == ttrial;
+  const int* p_trial = d_perm_trial.as<int>();
+  const int* p_test = shared ? d_perm_trial.as<int>() : d_perm_test.as<int>();
+  VecMap m{};
+  const bool gt = apply_gmap && gn_trial > 0, ge = apply_gmap && gn_test > 0;
+  const int* g_trial = gt ? d_gperm_trial.as<int>() : p_trial;
+  const int* g_test = ge ? d_gperm_test.as<int>() : p_test;
+  const int l_trial = gt ? gn_trial : width, l_test = ge ? gn_test : height;
+  if (!trans) {
+    m.pin = g_trial;
+    m.pout = g_test;
+    m.ld_in = l_trial;
+    m.ld_out = l_test;
+    m.free_out = ge ? d_gfree_test.as<int>() : nullptr;
+    m.n_free_out = ge ? n_gfree_test : 0;
+  } else {
+    m.pin = g_test;
+    m.pout = g_trial;
+    m.ld_in = l_test;
+    m.ld_out = l_trial;
+    m.free_out = gt ? d_gfree_trial.as<int>() : nullptr;
+    m.n_free_out = gt ? n_gfree_trial : 0;
+  }
+  return m;
+}
+
+void HOperator::set_global_dofs(int trial_n, const int* trial_map, int test_n, const int* test_map) {
+  auto build = [&](const SpaceH* sp, const ClusterTreeH* t, int n, const int* map, int& gn, int& nfree, DevBuf& gperm,
+                   DevBuf& gfree) {
+    if (!map) {
+      gn = 0;
+      nfree = 0;
+      gperm.release();
+      gfree.release();
+      return;
+    }
+    if (n < sp->ndof) throw Error(BEM_ERR_ARG, "a global numbering has fewer entries than the space has dofs");
+    std::vector<char> hit((size_t)n, 0);
+    for (int d = 0; d < sp->ndof; ++d) {
+      if (map[d] < 0 || map[d] >= n) throw Error(BEM_ERR_ARG, "global dof out of range");
+      if (hit[(size_t)map[d]]) throw Error(BEM_ERR_ARG, "two dofs map to the same global dof");
+      hit[(size_t)map[d]] = 1;
+    }
+    std::vector<int> gp(t->perm.size()), fr;
+    for (size_t k = 0; k < t->perm.size(); ++k) gp[k] = map[t->perm[k]];
+    for (int i = 0; i < n; ++i)
+      if (!hit[(size_t)i]) fr.push_back(i);
+    gperm.upload(gp);
+    if (fr.empty()) gfree.release();
+    else gfree.upload(fr);
+    gn = n;
+    nfree = (int)fr.size();
+  };
+  build(trial, ttrial, trial_n, trial_map, gn_trial, n_gfree_trial, d_gperm_trial, d_gfree_trial);
+  build(test, ttest, test_n, test_map, gn_test, n_gfree_test, d_gperm_test, d_gfree_test);
+  BEM_CUDA(cudaDeviceSynchronize());
+}
+
 void HOperator::mult(int trans, const double* alpha, const void* x, const double* beta, void* y, int nrhs,
                      cudaStream_t s) {
   if (nrhs < 1) throw Error(BEM_ERR_ARG, "nrhs must be >= 1");
@@ -29,8 +88,13 @@ void HOperator::mult(int trans, const double* alpha, const void* x, const double
     BEM_CUDA(cudaMemsetAsync(d_t.p, 0, d_t.bytes, s));
     BEM_CUDA(cudaMemsetAsync(d_tx.p, 0, d_tx.bytes, s));
   }
-  const int* pin = trans ? (ttest == ttrial ? d_perm_trial.as<int>() : d_perm_test.as<int>()) : d_perm_trial.as<int>();
-  const int* pout = trans ? d_perm_trial.as<int>() : (ttest == ttrial ? d_perm_trial.as<int>() : d_perm_test.as<int>());
+  const VecMap vm = vec_map(trans);
+  const int* pin = vm.pin;
+  const int* pout = vm.pout;
+  if (vm.n_free_out > 0) {
+    // entries of a globally numbered output that hold no dof: y = beta y there (Mult: 0)
+    launch_scale_rows(cplx, vm.free_out, vm.n_free_out, nrhs, vm.ld_out, beta, y, s);
+  }
   if (tc_eligible(trans, nrhs, s)) {
     mult_tc(alpha, x, beta, y, nrhs, s);  // records its own profiling events
     return;
@@ -92,7 +156,7 @@ void HOperator::mult(int trans, const double* alpha, const void* x, const double
     }
     return;
   }
-  launch_permute_in(prec, cplx, pin, in_n, nrhs, in_n, x, d_xp.p, s);
+  launch_permute_in(prec, cplx, pin, in_n, nrhs, vm.ld_in, x, d_xp.p, s);
   BEM_CUDA(cudaMemsetAsync(d_yp.p, 0, (size_t)out_n * nrhs * dsz, s));
   if (profiling) BEM_CUDA(cudaEventRecord(ev[1], s));
   MVArgs2 a{};
@@ -153,7 +217,7 @@ void HOperator::mult(int trans, const double* alpha, const void* x, const double
     launch_mv_pass(prec, cplx, a, mv_grid, s);
   }
   if (profiling) BEM_CUDA(cudaEventRecord(ev[3], s));
-  launch_permute_out(cplx, pout, out_n, nrhs, out_n, alpha, beta, d_yp.p, y, s);
+  launch_permute_out(cplx, pout, out_n, nrhs, vm.ld_out, alpha, beta, d_yp.p, y, s);
   // leave the accumulators zero for the single-launch kernel
   BEM_CUDA(cudaMemsetAsync(d_yp.p, 0, (size_t)out_n * nrhs * dsz, s));
   if (t_len > 0) {

@@ -53,7 +53,7 @@ int bem_mesh_create(int nv, const double* xyz, int nt, const int* tri, bem_mesh_
   return guarded([&] {
     REQUIRE(out && xyz && tri, "null argument");
     auto m = std::make_unique<bem_mesh_s>();
-    m->m.build(nv, xyz, nt, tri);
+    m->m->build(nv, xyz, nt, tri);
     *out = m.release();
   });
 }
@@ -61,7 +61,7 @@ int bem_mesh_create(int nv, const double* xyz, int nt, const int* tri, bem_mesh_
 int bem_mesh_num_edges(bem_mesh_t mesh, int* ne) {
   return guarded([&] {
     REQUIRE(mesh && ne, "null argument");
-    *ne = mesh->m.ne;
+    *ne = mesh->m->ne;
   });
 }
 
@@ -75,7 +75,8 @@ int bem_space_create(bem_mesh_t mesh, int kind, int dual_mapping, bem_space_t* o
     REQUIRE(kind == BEM_P0 || kind == BEM_P1 || kind == BEM_RT0 || kind == BEM_HCURL, "unknown space kind");
     REQUIRE(!dual_mapping || kind == BEM_P0, "dual mapping is defined for P0 only");
     auto s = std::make_unique<bem_space_s>();
-    s->s.build(&mesh->m, kind, dual_mapping);
+    s->mesh = mesh->m;
+    s->s->build(mesh->m.get(), kind, dual_mapping);
     *out = s.release();
   });
 }
@@ -87,7 +88,8 @@ int bem_space_create_on(bem_mesh_t mesh, int kind, int dual_mapping, const unsig
     REQUIRE(kind == BEM_P0 || kind == BEM_P1 || kind == BEM_RT0 || kind == BEM_HCURL, "unknown space kind");
     REQUIRE(!dual_mapping || kind == BEM_P0, "dual mapping is defined for P0 only");
     auto s = std::make_unique<bem_space_s>();
-    s->s.build(&mesh->m, kind, dual_mapping, element_mask);
+    s->mesh = mesh->m;
+    s->s->build(mesh->m.get(), kind, dual_mapping, element_mask);
     *out = s.release();
   });
 }
@@ -95,14 +97,14 @@ int bem_space_create_on(bem_mesh_t mesh, int kind, int dual_mapping, const unsig
 int bem_space_global_dofs(bem_space_t space, int* out) {
   return guarded([&] {
     REQUIRE(space && out, "null argument");
-    std::copy(space->s.global_dof.begin(), space->s.global_dof.end(), out);
+    std::copy(space->s->global_dof.begin(), space->s->global_dof.end(), out);
   });
 }
 
 int bem_space_element_dofs(bem_space_t space, int* dofs, int* signs) {
   return guarded([&] {
     REQUIRE(space && dofs, "null argument");
-    const SpaceH& s = space->s;
+    const SpaceH& s = *space->s;
     const int nt = s.mesh->nt;
     for (int e = 0; e < nt; ++e)
       for (int k = 0; k < 3; ++k) {
@@ -115,7 +117,7 @@ int bem_space_element_dofs(bem_space_t space, int* dofs, int* signs) {
 int bem_space_ndof(bem_space_t space, int* ndof) {
   return guarded([&] {
     REQUIRE(space && ndof, "null argument");
-    *ndof = space->s.ndof;
+    *ndof = space->s->ndof;
   });
 }
 
@@ -129,7 +131,7 @@ int bem_cluster_tree(bem_space_t space, int leafsize, int* perm, int max_cluster
     REQUIRE(space && perm && nclusters, "null argument");
     REQUIRE(leafsize >= 1, "leafsize must be positive");
     ClusterTreeH t;
-    t.build(space->s, leafsize);
+    t.build(*space->s, leafsize);
     const int nc = (int)t.cl.size();
     *nclusters = nc;
     std::memcpy(perm, t.perm.data(), t.perm.size() * sizeof(int));
@@ -162,10 +164,10 @@ int bem_partition(bem_space_t trial, bem_space_t test, int leafsize, double eta,
   return guarded([&] {
     REQUIRE(trial && test && nblocks, "null argument");
     ClusterTreeH tt, ts;
-    tt.build(trial->s, leafsize);
+    tt.build(*trial->s, leafsize);
     const ClusterTreeH* row = &tt;
     if (test != trial) {
-      ts.build(test->s, leafsize);
+      ts.build(*test->s, leafsize);
       row = &ts;
     }
     std::vector<BlockH> bl;
@@ -192,13 +194,14 @@ int bem_operator_create(int kernel, double kappa, bem_space_t trial, bem_space_t
     auto op = std::make_unique<HOperator>();
     op->kid = kernel;
     op->kappa = kappa;
-    op->trial = &trial->s;
-    op->test = &test->s;
+    op->trial = trial->s.get();
+    op->test = test->s.get();
     op->trial_ev = trial_eval;
     op->test_ev = test_eval;
     op->prm = *params;
     op->assemble();
     auto h = std::make_unique<bem_operator_s>();
+    h->keep(trial, test);
     h->op = std::move(op);
     *out = h.release();
   });
@@ -210,8 +213,9 @@ int bem_mass_create(bem_space_t trial, bem_space_t test, int complex_vectors, be
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) throw Error(BEM_ERR_CUDA, "no CUDA device");
     auto op = std::make_unique<MassOperator>();
-    op->build(&trial->s, &test->s, complex_vectors != 0);
+    op->build(trial->s.get(), test->s.get(), complex_vectors != 0);
     auto h = std::make_unique<bem_operator_s>();
+    h->keep(trial, test);
     h->op = std::move(op);
     *out = h.release();
   });
@@ -249,12 +253,38 @@ int bem_operator_blocks(bem_operator_t op, int* rowcl, int* colcl, int* near, in
   });
 }
 
+namespace {
+// The C-ABI products act on vectors in the operator's global numbering when one is set
+// (bem_operator_set_global_dofs); the library's own callers (GMRES, the dense copy, the
+// autotuner) use the compact numbering.
+struct GlobalNumbering {
+  HOperator* h;
+  explicit GlobalNumbering(OperatorBase* o) : h(dynamic_cast<HOperator*>(o)) {
+    if (h) h->apply_gmap = true;
+  }
+  ~GlobalNumbering() {
+    if (h) h->apply_gmap = false;
+  }
+};
+}  // namespace
+
 int bem_operator_mult(bem_operator_t op, int trans, const double* alpha, const void* x, const double* beta, void* y,
                       int nrhs, void* stream) {
   return guarded([&] {
     REQUIRE(op && alpha && beta && x && y, "null argument");
     REQUIRE(nrhs >= 1, "nrhs must be >= 1");
+    GlobalNumbering g(op->op.get());
     op->op->mult(trans, alpha, x, beta, y, nrhs, (cudaStream_t)stream);
+  });
+}
+
+int bem_operator_set_global_dofs(bem_operator_t op, int trial_nglobal, const int* trial_map, int test_nglobal,
+                                 const int* test_map) {
+  return guarded([&] {
+    REQUIRE(op, "null argument");
+    auto* h = dynamic_cast<HOperator*>(op->op.get());
+    if (!h) throw Error(BEM_ERR_STATE, "not an H-matrix operator");
+    h->set_global_dofs(trial_nglobal, trial_map, test_nglobal, test_map);
   });
 }
 
@@ -264,6 +294,7 @@ int bem_operator_mult_noalloc(bem_operator_t op, int trans, const double* alpha,
     REQUIRE(op && alpha && beta && x && y, "null argument");
     auto* h = dynamic_cast<HOperator*>(op->op.get());
     if (!h) throw Error(BEM_ERR_STATE, "not an H-matrix operator");
+    GlobalNumbering g(h);
     mult_noalloc(*h, trans, alpha, x, beta, y, nrhs, (cudaStream_t)stream);
   });
 }
@@ -273,9 +304,15 @@ int bem_operator_mult_host(bem_operator_t op, int trans, const double* alpha, co
   return guarded([&] {
     REQUIRE(op && alpha && beta && x && y, "null argument");
     OperatorBase* o = op->op.get();
+    GlobalNumbering g(o);
     const size_t esz = o->cplx ? 16 : 8;
-    const size_t nin = (size_t)(trans ? o->height : o->width) * nrhs;
-    const size_t nout = (size_t)(trans ? o->width : o->height) * nrhs;
+    size_t nin = (size_t)(trans ? o->height : o->width) * nrhs;
+    size_t nout = (size_t)(trans ? o->width : o->height) * nrhs;
+    if (g.h) {
+      const HOperator::VecMap vm = g.h->vec_map(trans);
+      nin = (size_t)vm.ld_in * nrhs;
+      nout = (size_t)vm.ld_out * nrhs;
+    }
     // Page-locked host buffers are mapped into the device's address space: the kernels read x
     // and write y across the host link themselves, with no staging copies (each step still
     // moves x to the device and y back).  Other host memory goes through device staging.
@@ -377,7 +414,8 @@ int bem_operator_load(const char* path, bem_space_t trial, bem_space_t test, bem
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) throw Error(BEM_ERR_CUDA, "no CUDA device");
     auto h = std::make_unique<bem_operator_s>();
-    h->op = load_operator(path, &trial->s, &test->s);
+    h->keep(trial, test);
+    h->op = load_operator(path, trial->s.get(), test->s.get());
     *out = h.release();
   });
 }

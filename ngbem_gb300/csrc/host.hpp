@@ -188,6 +188,25 @@ struct HOperator : OperatorBase {
 
   // device data
   DevBuf d_perm_trial, d_perm_test, d_pinv_trial, d_pinv_test;
+  // Optional global numbering of the vectors the C-ABI products act on (the FE space's full dof
+  // numbering, of which the operator's spaces hold the boundary dofs): dof d of the trial
+  // (test) space is entry map[d] of a vector of gn_trial (gn_test) entries; 0 = the compact
+  // numbering.  d_gperm_* are the cluster permutations composed with the maps, d_gfree_* the
+  // global entries that hold no dof (an output's such entries are scaled by beta).
+  int gn_trial = 0, gn_test = 0, n_gfree_trial = 0, n_gfree_test = 0;
+  DevBuf d_gperm_trial, d_gperm_test, d_gfree_trial, d_gfree_test;
+  bool apply_gmap = false;  // set by the C-ABI product entry points for the call
+  void set_global_dofs(int trial_n, const int* trial_map, int test_n, const int* test_map);
+  // what a product in direction `trans` reads and writes: permutations into x and y, leading
+  // dimensions of x and y, and the output entries outside the output space
+  struct VecMap {
+    const int* pin;
+    const int* pout;
+    int ld_in, ld_out;
+    const int* free_out;
+    int n_free_out;
+  };
+  VecMap vec_map(int trans) const;
   std::vector<std::unique_ptr<DevBuf>> pools;  // dense and factor pools
   DevBuf d_mvdense, d_mvlr, d_err, d_sched;
   // per pass: 0 t=V2 x, 1 y+=Dx+U2 t, 2 t=U2^T x, 3 y+=D^T x+V2^T t; 4-7 the two phases of the
@@ -310,14 +329,25 @@ int gmres_batched_solve(int nterms, OperatorBase* const* ops, const double* coef
 
 }  // namespace bem
 
+// Handles share what they point into: a space keeps its mesh alive and an operator its spaces,
+// so the caller may destroy the handles in any order.
 struct bem_mesh_s {
-  bem::MeshH m;
+  std::shared_ptr<bem::MeshH> m = std::make_shared<bem::MeshH>();
 };
 struct bem_space_s {
-  bem::SpaceH s;
+  std::shared_ptr<bem::MeshH> mesh;
+  std::shared_ptr<bem::SpaceH> s = std::make_shared<bem::SpaceH>();
 };
 struct bem_operator_s {
+  std::shared_ptr<bem::MeshH> keep_mesh_trial, keep_mesh_test;  // declared before op: destroyed after it
+  std::shared_ptr<bem::SpaceH> keep_trial, keep_test;
   std::unique_ptr<bem::OperatorBase> op;
+  void keep(bem_space_s* trial, bem_space_s* test) {
+    keep_trial = trial->s;
+    keep_mesh_trial = trial->mesh;
+    keep_test = test->s;
+    keep_mesh_test = test->mesh;
+  }
 };
 struct bem_slbatch_s {
   bem::SLBatch b;

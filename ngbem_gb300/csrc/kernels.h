@@ -215,6 +215,10 @@ inline int mv_x_bytes(int prec, bool cplx) { return (prec == 0 ? 8 : 8) * (cplx 
 void launch_permute_in(int prec, bool cplx, const int* perm, int n, int nrhs, int ld,
                        const void* x, void* xp, cudaStream_t s);
 // y[r*ld + perm[k]] = alpha * yp[k*nrhs + r] + beta * y[...]   (fp64 / complex128)
+// y[r * ld + rows[i]] = beta y[...] (0 when beta = 0) for i < nrows: the entries of a vector
+// in a global numbering that hold no dof of the operator's output space
+void launch_scale_rows(bool cplx, const int* rows, int nrows, int nrhs, int ld, const double* beta, void* y,
+                       cudaStream_t s);
 void launch_permute_out(bool cplx, const int* perm, int n, int nrhs, int ld, const double* alpha,
                         const double* beta, const void* yp, void* y, cudaStream_t s);
 // CSR SpMV in fp64: y = alpha*A x + beta*y (A real; vectors real or complex; nrhs columns)

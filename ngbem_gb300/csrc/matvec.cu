@@ -1196,6 +1196,28 @@ void launch_permute_out(bool cplx, const int* perm, int n, int nrhs, int ld, con
                                                  (double*)y);
 }
 
+template <class D>
+__global__ void scale_rows_kernel(const int* rows, int nrows, int nrhs, int ld, D beta, int zero, D* y) {
+  const long long total = (long long)nrows * nrhs;
+  for (long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x; t < total; t += (long long)gridDim.x * blockDim.x) {
+    const int i = (int)(t % nrows), r = (int)(t / nrows);
+    D* dst = y + (size_t)r * ld + rows[i];
+    *dst = zero ? vzero<D>() : beta * (*dst);
+  }
+}
+
+void launch_scale_rows(bool cplx, const int* rows, int nrows, int nrhs, int ld, const double* beta, void* y,
+                       cudaStream_t s) {
+  if (nrows <= 0) return;
+  const int g = grid_for((long long)nrows * nrhs);
+  const int zero = (beta[0] == 0.0 && beta[1] == 0.0) ? 1 : 0;
+  if (cplx)
+    scale_rows_kernel<cpx<double>><<<g, 256, 0, s>>>(rows, nrows, nrhs, ld, mkc(beta[0], beta[1]), zero,
+                                                     (cpx<double>*)y);
+  else
+    scale_rows_kernel<double><<<g, 256, 0, s>>>(rows, nrows, nrhs, ld, beta[0], zero, (double*)y);
+}
+
 // ---------------------------------------------------------------------------------------
 // CSR SpMV (mass matrices).  trans: y = alpha A^T x + beta y via atomics into y after scaling.
 template <class VD>

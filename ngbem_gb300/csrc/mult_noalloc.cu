@@ -93,10 +93,10 @@ void mult_noalloc(HOperator& op, int trans, const double* alpha, const void* x, 
                                    "call of the same form builds them (with the tensor cores off for several "
                                    "complex right-hand sides: bem_operator_set_tensor_cores(op, 0))");
   unsigned char* base = (unsigned char*)scratch_on_current_device();
-  const int* pin = trans ? (op.ttest == op.ttrial ? op.d_perm_trial.as<int>() : op.d_perm_test.as<int>())
-                         : op.d_perm_trial.as<int>();
-  const int* pout = trans ? op.d_perm_trial.as<int>()
-                          : (op.ttest == op.ttrial ? op.d_perm_trial.as<int>() : op.d_perm_test.as<int>());
+  const HOperator::VecMap vm = op.vec_map(trans);
+  const int* pin = vm.pin;
+  const int* pout = vm.pout;
+  if (vm.n_free_out > 0) launch_scale_rows(op.cplx, vm.free_out, vm.n_free_out, nrhs, vm.ld_out, beta, y, s);
   BEM_CUDA(cudaMemsetAsync(base, 0, off_xp, s));
   void* tx = op.prec == 0 ? (void*)(base + off_t) : (void*)(base + off_tx);
   if (use_fused) {
@@ -138,7 +138,7 @@ void mult_noalloc(HOperator& op, int trans, const double* alpha, const void* x, 
     BEM_CUDA(launch_mv_fused(op.prec, op.cplx, f, s));
     return;
   }
-  launch_permute_in(op.prec, op.cplx, pin, in_n, nrhs, in_n, x, base + off_xp, s);
+  launch_permute_in(op.prec, op.cplx, pin, in_n, nrhs, vm.ld_in, x, base + off_xp, s);
   MVArgs2 a{};
   a.xp = base + off_xp;
   a.t = base + off_t;
@@ -192,7 +192,7 @@ void mult_noalloc(HOperator& op, int trans, const double* alpha, const void* x, 
   } else {
     launch_mv_pass(op.prec, op.cplx, a, op.mv_grid, s);
   }
-  launch_permute_out(op.cplx, pout, out_n, nrhs, out_n, alpha, beta, base + off_yp, y, s);
+  launch_permute_out(op.cplx, pout, out_n, nrhs, vm.ld_out, alpha, beta, base + off_yp, y, s);
   BEM_CUDA(cudaGetLastError());
 }
 

@@ -433,14 +433,15 @@ void HOperator::release_tc() {
 }
 
 void HOperator::mult_tc(const double* alpha, const void* x, const double* beta, void* y, int nrhs, cudaStream_t s) {
-  const int* perm = d_perm_trial.as<int>();
-  const int* pout = ttest == ttrial ? d_perm_trial.as<int>() : d_perm_test.as<int>();
+  const VecMap vm = vec_map(0);
+  const int* perm = vm.pin;
+  const int* pout = vm.pout;
   std::array<cudaEvent_t, 5> ev{};
   if (profiling) {
     for (auto& e : ev) BEM_CUDA(cudaEventCreate(&e));
     BEM_CUDA(cudaEventRecord(ev[0], s));
   }
-  launch_tc_xprep(perm, width, nrhs, width, x, d_tc_xa.p, tc_nkc_x, d_tc_xa2.p, tc_nkc_x2, s);
+  launch_tc_xprep(perm, width, nrhs, vm.ld_in, x, d_tc_xa.p, tc_nkc_x, d_tc_xa2.p, tc_nkc_x2, s);
   if (profiling) BEM_CUDA(cudaEventRecord(ev[1], s));
   for (int pass = 0; pass < 2; ++pass) {
     TCGemmArgs g{};
@@ -455,7 +456,7 @@ void HOperator::mult_tc(const double* alpha, const void* x, const double* beta, 
     if (profiling && pass == 0) BEM_CUDA(cudaEventRecord(ev[2], s));
   }
   if (profiling) BEM_CUDA(cudaEventRecord(ev[3], s));
-  launch_tc_ysum_out(d_tc_leaves.as<int4>(), n_tc_leaves, d_tc_deltas.as<int>(), d_tc_y.p, pout, nrhs, height, alpha,
+  launch_tc_ysum_out(d_tc_leaves.as<int4>(), n_tc_leaves, d_tc_deltas.as<int>(), d_tc_y.p, pout, nrhs, vm.ld_out, alpha,
                      beta, y, s);
   if (profiling) {
     BEM_CUDA(cudaEventRecord(ev[4], s));

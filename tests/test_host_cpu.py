@@ -196,3 +196,32 @@ def test_regions_and_masks():
     # the whole mesh as a region gives the plain space
     a, b = nb.HDivSurface(m, definedon=m.Boundaries(".*")), nb.HDivSurface(m)
     assert a.ndof == b.ndof and np.array_equal(a.global_dofs, np.arange(b.ndof))
+
+
+def test_handles_keep_what_they_point_into():
+    """A space keeps its mesh alive (and an operator its spaces): destroying the handles in any
+    order leaves the others usable.  The space's cluster tree needs the mesh coordinates."""
+    m = icosphere(3)
+    X = np.ascontiguousarray(m.vertices)
+    T = np.ascontiguousarray(m.triangles, dtype=np.int32)
+    mh, sh = C.c_void_p(), C.c_void_p()
+    _lib.check(_lib.lib.bem_mesh_create(m.nv, X.ctypes.data_as(_lib._dp), m.nt, T.ctypes.data_as(_lib._ip),
+                                        C.byref(mh)))
+    _lib.check(_lib.lib.bem_space_create(mh, _lib.KINDS["P1"], 0, C.byref(sh)))
+
+    def tree():
+        perm = np.zeros(m.nv, dtype=np.int32)
+        nc = C.c_int()
+        maxc = 4 * m.nv
+        ci = np.zeros(7 * maxc, dtype=np.int64)
+        cd = np.zeros(23 * maxc, dtype=np.float64)
+        _lib.check(_lib.lib.bem_cluster_tree(sh, 20, perm.ctypes.data_as(_lib._ip), maxc, C.byref(nc),
+                                             ci.ctypes.data_as(_lib._lp), cd.ctypes.data_as(_lib._dp)))
+        return perm, cd[: 23 * nc.value].copy()
+
+    p0, c0 = tree()
+    _lib.check(_lib.lib.bem_mesh_destroy(mh))
+    X[:] = 0.0  # the caller's arrays are not what the space reads either
+    p1, c1 = tree()
+    assert np.array_equal(p0, p1) and np.array_equal(c0.view(np.int64), c1.view(np.int64))
+    _lib.check(_lib.lib.bem_space_destroy(sh))
