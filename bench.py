@@ -108,6 +108,21 @@ def bm_workload(level, l2="write+read"):
             "l2": L2_NOTE[l2], "gmres": "batched, 32 right-hand sides in lockstep, tol 1e-8, restart 100"}
 
 
+def assembly_rates(info):
+    """Kernel evaluations per second of the two assembly phases that dominate (from the
+    operator's counters and its CUDA-event phase times).  ACA counts, per far block and kernel
+    component, (steps + 1) x (row + column points) evaluations; the near field counts its
+    regular pairs x nq^2 (its time also holds the Sauter-Schwab pairs, which run concurrently
+    in the same phase)."""
+    r = {"aca_evals": info["aca_evals"], "nf_regular_evals": info["nf_regular_evals"],
+         "n_singular_pairs": info["n_singular_pairs"]}
+    if info["ms_aca"] > 0:
+        r["aca_evals_per_s"] = info["aca_evals"] / (info["ms_aca"] * 1e-3)
+    if info["ms_nearfield"] > 0:
+        r["nf_regular_evals_per_s"] = info["nf_regular_evals"] / (info["ms_nearfield"] * 1e-3)
+    return r
+
+
 def bm_rhs(meshes, forms, level):
     """The ellipsoid and its 32 Burton-Miller plane-wave load vectors (n x 32, complex128)."""
     mesh = meshes.ellipsoid(level, BM_AXES)
@@ -713,7 +728,8 @@ def run_bm(args):
                        "iterations": last["iterations"], "max_residual": last["residual"], "nze": info["nze"],
                        "max_rank": info["max_rank"], "nfallback": info["nfallback"],
                        "bytes_stored": info["bytes_dense"] + info["bytes_lowrank"],
-                       "assembly_breakdown_ms": {k: info[k] for k in info_keys}}
+                       "assembly_breakdown_ms": {k: info[k] for k in info_keys},
+                       "assembly_rates": assembly_rates(info)}
         ops[prec], sols[prec] = Cop, U
     Cm, C64 = ops["mixed"].mat, ops["fp64"].mat
     Y = torch.empty_like(Xc)

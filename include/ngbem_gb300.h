@@ -90,6 +90,9 @@ typedef struct {
   int mv_segments;             /* matvec segments (block pieces) */
   int mv_ranges[4];            /* staged input ranges per pass */
   double ms_mvitems;           /* host time grouping the blocks into matvec work items */
+  long long nf_regular_evals;  /* kernel evaluations of the regular near-field pairs (pairs x nq^2) */
+  long long aca_evals;         /* kernel evaluations of ACA: per block and kernel component,
+                                  (steps + 1) x (row points + column points), every round */
 } bem_operator_info_t;
 
 /* Fill *p with the reference defaults (intorder 3, leafsize 40, eta 2, eps 1e-6, aca). */

@@ -44,7 +44,7 @@ class OperatorInfo(C.Structure):
                 ("n_regular_pairs", C.c_longlong), ("ms_setup", C.c_double), ("ms_aca", C.c_double),
                 ("ms_nearfield", C.c_double), ("ms_projection", C.c_double), ("ms_total", C.c_double),
                 ("mv_items", C.c_int * 4), ("mv_segments", C.c_int), ("mv_ranges", C.c_int * 4),
-                ("ms_mvitems", C.c_double)]
+                ("ms_mvitems", C.c_double), ("nf_regular_evals", C.c_longlong), ("aca_evals", C.c_longlong)]
 
 
 _vp, _dp, _ip, _lp = C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_int), C.POINTER(C.c_long)

@@ -110,6 +110,7 @@ void HOperator::assemble() {
   if (leaf < 1) throw Error(BEM_ERR_ARG, "leafsize must be positive");
   // NGBEM_GB300_ACA_FAIL=k (k > 0): the ACA of every far block whose number in the block list
   // is a multiple of k fails on the host (fault injection; such blocks are assembled densely)
+  long long aca_evals = 0;
   int aca_fail_every = 0;
   if (const char* ev = std::getenv("NGBEM_GB300_ACA_FAIL")) aca_fail_every = std::max(0, std::atoi(ev));
   int kcap = prm.max_rank > 0 ? prm.max_rank : 128;
@@ -410,6 +411,11 @@ void HOperator::assemble() {
     BEM_CUDA(cudaMemcpyAsync(ranks.data(), d_ranks.p, ranks.size() * sizeof(int), cudaMemcpyDeviceToHost, sp.a));
     BEM_CUDA(cudaMemcpyAsync(status.data(), d_status.p, status.size() * sizeof(int), cudaMemcpyDeviceToHost, sp.a));
     BEM_CUDA(cudaStreamSynchronize(sp.a));
+    for (int f = 0; f < nf; ++f) {
+      const long long pts = (long long)(fd[f].ni + fd[f].nj) * nq;
+      for (int c = 0; c < NC; ++c)
+        aca_evals += (long long)(status[f] ? fd[f].kcap : ranks[(size_t)f * NC + c] + 1) * pts;
+    }
     // host-side fault injection for the tests of the dense fallback: the ACA of the chosen
     // far blocks counts as failed (as if it had reached the rank cap), in every round
     if (aca_fail_every > 0)
@@ -510,6 +516,7 @@ void HOperator::assemble() {
     if (err || cnt > np.sing_cap) throw Error(BEM_ERR_INTERNAL, "singular pair list overflow");
     info.n_singular_pairs += cnt;
     info.n_regular_pairs += np.npairs - cnt;
+    info.nf_regular_evals += (np.npairs - cnt) * (long long)nq * nq;
   };
   check_pass(np1);
   NearPass np2;
@@ -562,6 +569,7 @@ void HOperator::assemble() {
   info.height = height;
   info.width = width;
   info.nblocks = nb;
+  info.aca_evals = aca_evals;
   info.nnear = 0;
   info.nfar = (int)mvlr.size();
   info.nfallback = 0;
