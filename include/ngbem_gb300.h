@@ -38,7 +38,10 @@ enum {
  * and the surface trace of HCurl order 0 (HCURL: lowest-order Nedelec on the surface
  * triangles, one dof per edge like RT0; on each triangle its shape functions are n x the RT0
  * shape functions of the same edges and signs) */
-enum { BEM_P0 = 0, BEM_P1 = 1, BEM_RT0 = 2, BEM_HCURL = 3 };
+/* BEM_L2P1..3: SurfaceL2 of order 1..3 (NGSolve SurfaceL2(mesh, order=p)): (p+1)(p+2)/2
+ * consecutive dofs per element, the Dubiner basis on the element's vertices taken in the order
+ * of their global numbers; identity trace only. */
+enum { BEM_P0 = 0, BEM_P1 = 1, BEM_RT0 = 2, BEM_HCURL = 3, BEM_L2P1 = 4, BEM_L2P2 = 5, BEM_L2P3 = 6 };
 /* trace evaluators: GetEvaluator(BND) (ID), DiffOpBoundaryRot (ROT), DiffOpHelmholtz (HELM),
  * DiffOpMaxwellNew (MAXWELL); reference src/diffops.hpp:12-338.  On BEM_HCURL: ID is the
  * tangential trace (GetEvaluator(BND) of an HCurl space), ROTATED_TRACE is
@@ -121,7 +124,9 @@ int bem_space_global_dofs(bem_space_t space, int* out);
 /* The dofs of every element (FESpace::GetDofNrs, as the reference reads them throughout
  * src/ngbem.cpp): dofs holds 3 ints per element (P0: the element's dof in the first; -1 on
  * elements outside the space's region); signs (may be null) the RT0 / HCURL orientation
- * +1/-1 of the local edges (0,1), (1,2), (2,0). */
+ * +1/-1 of the local edges (0,1), (1,2), (2,0).  BEM_L2P1..3: the first holds the element's
+ * first dof (its (p+1)(p+2)/2 dofs are consecutive), the others -1, and signs the element's
+ * local vertices in the order of their global numbers. */
 int bem_space_element_dofs(bem_space_t space, int* dofs, int* signs);
 int bem_space_ndof(bem_space_t space, int* ndof);
 int bem_space_destroy(bem_space_t space);

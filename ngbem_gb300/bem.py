@@ -133,11 +133,16 @@ def _region_mask(region, mesh: Mesh) -> np.ndarray:
 
 def SurfaceL2(mesh: Mesh, order: int = 0, dual_mapping: bool = False, complex: bool = False,
               definedon=None) -> TraceSpace:
-    """Piecewise constants on the surface (the reference uses NGSolve SurfaceL2; order 0 here).
-    definedon: a Region; the space then lives on those triangles only."""
-    if order != 0:
-        raise NotImplementedError("SurfaceL2: only order 0 (piecewise constants) is supported")
-    return TraceSpace(mesh, "P0", dual_mapping, complex, definedon)
+    """Discontinuous polynomials of degree `order` on the surface triangles (NGSolve SurfaceL2):
+    order 0 the piecewise constants, orders 1..3 the Dubiner basis ((p+1)(p+2)/2 dofs per
+    triangle, numbered consecutively per triangle, built on the triangle's vertices in the order
+    of their global numbers).  dual_mapping (order 0 only): the basis 1/|J|.  definedon: a
+    Region; the space then lives on those triangles only."""
+    if order not in (0, 1, 2, 3):
+        raise NotImplementedError("SurfaceL2: orders 0 to 3 are supported")
+    if order > 0 and dual_mapping:
+        raise NotImplementedError("SurfaceL2: dual_mapping is defined for order 0")
+    return TraceSpace(mesh, "P0" if order == 0 else f"L2P{order}", dual_mapping, complex, definedon)
 
 
 def H1(mesh: Mesh, order: int = 1, complex: bool = False, definedon=None) -> TraceSpace:

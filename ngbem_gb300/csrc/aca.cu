@@ -371,8 +371,8 @@ __global__ void __launch_bounds__(256) aca_project_kernel(ProjArgs a) {
       for (int x = 0; x < 3; ++x)
         for (int y = 0; y < 3; ++y) { rot[x][y] = Ee.rot[x][y]; o[x][y] = Ee.o[x][y]; }
       const P nrm[3] = {Ee.n[0], Ee.n[1], Ee.n[2]};
-      int sg[3] = {1, 1, 1};
-      if (edge_trace(TET)) { int4 s = a.test.sign[e]; sg[0] = s.x; sg[1] = s.y; sg[2] = s.z; }
+      int sg[SignSlots<TET>::N];
+      elem_signs<TET>(a.test.sign, e, sg);
       V acc[NDI];
 #pragma unroll
       for (int x = 0; x < NDI; ++x) acc[x] = vzero<V>();
@@ -389,7 +389,7 @@ __global__ void __launch_bounds__(256) aca_project_kernel(ProjArgs a) {
       const int4 dn = a.test.dofs[e];
 #pragma unroll
       for (int x = 0; x < NDI; ++x) {
-        const int li = a.test.pinv[i4c_(dn, x)] - L.r0;
+        const int li = a.test.pinv[elem_dof<TET>(dn, x)] - L.r0;
         if (li >= 0 && li < L.m) atomic_add(&U2[lr_u_index(L, li, off + kk)], acc[x] * fac);
       }
     }
@@ -401,8 +401,8 @@ __global__ void __launch_bounds__(256) aca_project_kernel(ProjArgs a) {
       for (int x = 0; x < 3; ++x)
         for (int y = 0; y < 3; ++y) { rot[x][y] = Ee.rot[x][y]; o[x][y] = Ee.o[x][y]; }
       const P nrm[3] = {Ee.n[0], Ee.n[1], Ee.n[2]};
-      int sg[3] = {1, 1, 1};
-      if (edge_trace(TRT)) { int4 s = a.trial.sign[e]; sg[0] = s.x; sg[1] = s.y; sg[2] = s.z; }
+      int sg[SignSlots<TRT>::N];
+      elem_signs<TRT>(a.trial.sign, e, sg);
       V acc[NDJ];
 #pragma unroll
       for (int x = 0; x < NDJ; ++x) acc[x] = vzero<V>();
@@ -419,7 +419,7 @@ __global__ void __launch_bounds__(256) aca_project_kernel(ProjArgs a) {
       const int4 dn = a.trial.dofs[e];
 #pragma unroll
       for (int x = 0; x < NDJ; ++x) {
-        const int lj = a.trial.pinv[i4c_(dn, x)] - L.c0;
+        const int lj = a.trial.pinv[elem_dof<TRT>(dn, x)] - L.c0;
         if (lj >= 0 && lj < L.n) atomic_add(&V2[lr_v_index(L, off + kk, lj)], acc[x]);
       }
     }
@@ -467,6 +467,15 @@ void launch_aca(int kid, int prec, const AcaArgs& a, cudaStream_t s) {
   join();
 }
 
+// SurfaceL2 of order 1..3 on both sides, for the kernels with identity traces
+#define BEM_L2P_COMBOS(X)                                                                      \
+  X(K_LAPLACE_SL, TR_L2P1, TR_L2P1) X(K_LAPLACE_SL, TR_L2P2, TR_L2P2) X(K_LAPLACE_SL, TR_L2P3, TR_L2P3) \
+  X(K_LAPLACE_DL, TR_L2P1, TR_L2P1) X(K_LAPLACE_DL, TR_L2P2, TR_L2P2) X(K_LAPLACE_DL, TR_L2P3, TR_L2P3) \
+  X(K_HELMHOLTZ_SL, TR_L2P1, TR_L2P1) X(K_HELMHOLTZ_SL, TR_L2P2, TR_L2P2)                        \
+  X(K_HELMHOLTZ_SL, TR_L2P3, TR_L2P3) X(K_HELMHOLTZ_DL, TR_L2P1, TR_L2P1)                        \
+  X(K_HELMHOLTZ_DL, TR_L2P2, TR_L2P2) X(K_HELMHOLTZ_DL, TR_L2P3, TR_L2P3)                        \
+  X(K_HELMHOLTZ_CF, TR_L2P1, TR_L2P1) X(K_HELMHOLTZ_CF, TR_L2P2, TR_L2P2)                        \
+  X(K_HELMHOLTZ_CF, TR_L2P3, TR_L2P3)
 #define BEM_PJ_COMBOS(X)                                                              \
   X(K_LAPLACE_SL, TR_P0, TR_P0) X(K_LAPLACE_SL, TR_P1, TR_P1)                         \
   X(K_LAPLACE_SL, TR_P1, TR_P0) X(K_LAPLACE_SL, TR_P0, TR_P1)                         \
@@ -483,7 +492,8 @@ void launch_aca(int kid, int prec, const AcaArgs& a, cudaStream_t s) {
   X(K_HELMHOLTZ_CF, TR_P1, TR_P0) X(K_HELMHOLTZ_CF, TR_P0, TR_P1)                     \
   X(K_HELMHOLTZ_HS, TR_HELM, TR_HELM)                                                 \
   X(K_MAXWELL_SL, TR_MAX, TR_MAX) X(K_MAXWELL_SL, TR_NEDMAX, TR_NEDMAX)                \
-  X(K_MAXWELL_DL, TR_NEDROT, TR_NED) X(K_MAXWELL_DL, TR_NEDROT, TR_RT0ID)
+  X(K_MAXWELL_DL, TR_NEDROT, TR_NED) X(K_MAXWELL_DL, TR_NEDROT, TR_RT0ID)  \
+  BEM_L2P_COMBOS(X)
 
 void launch_projection(int kid, int prec, int trt, int tet, const ProjArgs& a, cudaStream_t s) {
   if (a.nfar <= 0) return;

@@ -352,9 +352,15 @@ void MassOperator::build(SpaceH* trial, SpaceH* test, bool complex_vectors) {
   TrigRule r = make_trig_rule(4);
   const int nq = (int)r.w.size();
   std::vector<std::vector<std::pair<int, double>>> rows(nrows);
-  auto shape = [&](const SpaceH& sp, int e, double xi, double eta, double S[3][3], int& dim) {
+  auto shape = [&](const SpaceH& sp, int e, double xi, double eta, double S[10][3], int& dim) {
     const ElemRec64& g = m.rec[e];
     if (sp.kind == BEM_P0) { S[0][0] = sp.dual ? g.invdetJ : 1.0; dim = 1; return; }
+    if (sp.kind >= BEM_L2P1) {
+      const int code = sp.sign[3 * e] + 3 * sp.sign[3 * e + 1];
+      for (int a = 0; a < sp.nd; ++a) S[a][0] = dubiner<double>(sp.kind - BEM_L2P1 + 1, a, xi, eta, code);
+      dim = 1;
+      return;
+    }
     if (sp.kind == BEM_P1) { S[0][0] = xi; S[1][0] = eta; S[2][0] = 1.0 - xi - eta; dim = 1; return; }
     double x[3];
     m.map(e, xi, eta, x);
@@ -370,7 +376,7 @@ void MassOperator::build(SpaceH* trial, SpaceH* test, bool complex_vectors) {
   };
   for (int e = 0; e < m.nt; ++e)
     for (int q = 0; q < nq && trial->on(e) && test->on(e); ++q) {
-      double Si[3][3], Sj[3][3];
+      double Si[10][3], Sj[10][3];
       int di, dj;
       shape(*test, e, r.xi[q], r.eta[q], Si, di);
       shape(*trial, e, r.xi[q], r.eta[q], Sj, dj);
@@ -380,7 +386,7 @@ void MassOperator::build(SpaceH* trial, SpaceH* test, bool complex_vectors) {
         for (int b = 0; b < trial->nd; ++b) {
           double s = 0.0;
           for (int c = 0; c < di; ++c) s += Si[a][c] * Sj[b][c];
-          rows[test->el_dofs(e)[a]].push_back({trial->el_dofs(e)[b], w * s});
+          rows[test->dof(e, a)].push_back({trial->dof(e, b), w * s});
         }
     }
   h_rowptr.assign(nrows + 1, 0);

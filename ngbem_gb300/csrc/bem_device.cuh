@@ -318,6 +318,37 @@ template <> struct TraceInfo<TR_RT0ID> { static constexpr int ND = 3, DIM = 3; }
 template <> struct TraceInfo<TR_NED> { static constexpr int ND = 3, DIM = 3; };
 template <> struct TraceInfo<TR_NEDROT> { static constexpr int ND = 3, DIM = 3; };
 template <> struct TraceInfo<TR_NEDMAX> { static constexpr int ND = 3, DIM = 4; };
+template <> struct TraceInfo<TR_L2P1> { static constexpr int ND = 3, DIM = 1; };
+template <> struct TraceInfo<TR_L2P2> { static constexpr int ND = 6, DIM = 1; };
+template <> struct TraceInfo<TR_L2P3> { static constexpr int ND = 10, DIM = 1; };
+// sign slots a kernel keeps per element (at least the three edge signs)
+template <int TR> struct SignSlots { static constexpr int N = TraceInfo<TR>::ND > 3 ? TraceInfo<TR>::ND : 3; };
+
+// global dof of local dof a of an element (dn: the element's dof record)
+template <int TR>
+__device__ __forceinline__ int elem_dof(const int4& dn, int a) {
+  if (l2p_trace(TR)) return dn.x + a;
+  return a == 0 ? dn.x : (a == 1 ? dn.y : dn.z);
+}
+// per-local-dof sign argument of trace_val: edge orientations, or the vertex order code of an
+// L2 element of order >= 1 (the same for all its dofs), else 1
+template <int TR, int N>
+__device__ __forceinline__ void elem_signs(const int4* sign, int e, int (&sg)[N]) {
+#pragma unroll
+  for (int k = 0; k < N; ++k) sg[k] = 1;
+  if (edge_trace(TR)) {
+    const int4 g = sign[e];
+    sg[0] = g.x;
+    sg[1] = g.y;
+    sg[2] = g.z;
+  }
+  if (l2p_trace(TR)) {
+    const int4 g = sign[e];
+    const int code = g.x + 3 * g.y;
+#pragma unroll
+    for (int k = 0; k < N; ++k) sg[k] = code;
+  }
+}
 
 // value of trace component c of local dof a (nrm: the element's unit normal, read by TR_NED)
 template <int TR, class R>
@@ -325,6 +356,7 @@ __device__ __forceinline__ R trace_val(int a, int c, R xi, R eta, const R (*xp)[
                                        const R (*rot)[3], int sgn, bool dual, const R* nrm) {
   if (TR == TR_P0) return dual ? invdetJ : R(1);
   if (TR == TR_P1) return a == 0 ? xi : (a == 1 ? eta : R(1) - xi - eta);
+  if (l2p_trace(TR)) return dubiner<R>(l2p_order(TR), a, xi, eta, sgn);
   if (TR == TR_ROT) return rot[a][c];
   if (TR == TR_HELM) {
     if (c < 3) return rot[a][c];

@@ -17,8 +17,60 @@ enum KernelId {
 // the tangential shape n x phi_RT0, the rotated trace n x (n x phi_RT0) = -phi_RT0, and the
 // Maxwell trace [-phi_RT0; surface curl] (reference DiffOpRotatedTrace, DiffOpMaxwell,
 // src/diffops.hpp:62-255, for the Whitney edge shapes, which are n x the RT0 shapes)
+// TR_L2P1..3: SurfaceL2 of order 1..3 (the identity trace of the Dubiner basis)
 enum TraceKind { TR_P0 = 0, TR_P1 = 1, TR_ROT = 2, TR_HELM = 3, TR_MAX = 4, TR_RT0ID = 5,
-                 TR_NED = 6, TR_NEDROT = 7, TR_NEDMAX = 8 };
+                 TR_NED = 6, TR_NEDROT = 7, TR_NEDMAX = 8, TR_L2P1 = 9, TR_L2P2 = 10, TR_L2P3 = 11 };
+// traces of a discontinuous space of order >= 1: the element's dofs are consecutive
+// (first dof + local index) and its "signs" hold the order of its vertices by global number
+__host__ __device__ constexpr bool l2p_trace(int tr) { return tr >= TR_L2P1 && tr <= TR_L2P3; }
+__host__ __device__ constexpr int l2p_order(int tr) { return tr - TR_L2P1 + 1; }
+
+// Dubiner basis function a of order P on a triangle (Dubiner 1991; Karniadakis and Sherwin,
+// Spectral/hp Element Methods, ch. 3), in the form NGSolve's L2 triangle element uses it:
+// with x = lambda_f0, y = lambda_f1 (f0, f1 the element's vertices of the lowest and the next
+// global number), s = 2x + y - 1, t = 1 - y, z = 2y - 1,
+//   phi_ij = t^i P_i(s / t) * P_j^(2i+1, 0)(z),   i = 0..P, j = 0..P-i,
+// numbered with i outer and j inner.  P_i: Legendre (scaled by t^i through its recurrence),
+// P_j^(alpha, 0): Jacobi.  code = f0 + 3 f1.
+template <class R>
+__host__ __device__ inline R dubiner(int P, int a, R xi, R eta, int code) {
+  const int f0 = code % 3, f1 = code / 3;
+  const R l2 = R(1) - xi - eta;
+  const R x = f0 == 0 ? xi : (f0 == 1 ? eta : l2);
+  const R y = f1 == 0 ? xi : (f1 == 1 ? eta : l2);
+  int i = 0, first = 0;
+  while (a >= first + (P - i + 1)) {
+    first += P - i + 1;
+    ++i;
+  }
+  const int j = a - first;
+  const R s = R(2) * x + y - R(1), t = R(1) - y, z = R(2) * y - R(1);
+  // scaled Legendre: L_0 = 1, L_1 = s, (n+1) L_{n+1} = (2n+1) s L_n - n t^2 L_{n-1}
+  R l0 = R(1), l1 = s;
+  R L = i == 0 ? l0 : l1;
+  for (int n = 1; n < i; ++n) {
+    const R ln = (R(2 * n + 1) * s * l1 - R(n) * t * t * l0) / R(n + 1);
+    l0 = l1;
+    l1 = ln;
+    L = ln;
+  }
+  // Jacobi P^(al, 0): P_0 = 1, P_1 = ((al + 2) z + al) / 2,
+  // 2n(n+al)(2n+al-2) P_n = (2n+al-1)((2n+al)(2n+al-2) z + al^2) P_{n-1} - 2(n+al-1)(n-1)(2n+al) P_{n-2}
+  const int al = 2 * i + 1;
+  R j0 = R(1), j1 = (R(al + 2) * z + R(al)) * R(0.5);
+  R J = j == 0 ? j0 : j1;
+  for (int n = 2; n <= j; ++n) {
+    const R c1 = R((2 * n + al - 1) * (2 * n + al) * (2 * n + al - 2));
+    const R c0 = R((2 * n + al - 1) * al * al);
+    const R cm = R(2 * (n + al - 1) * (n - 1) * (2 * n + al));
+    const R jn = ((c1 * z + c0) * j1 - cm * j0) / R(2 * n * (n + al) * (2 * n + al - 2));
+    j0 = j1;
+    j1 = jn;
+    J = jn;
+  }
+  return L * J;
+}
+
 // traces whose local dofs carry an edge orientation sign
 __host__ __device__ constexpr bool edge_trace(int tr) {
   return tr == TR_MAX || tr == TR_RT0ID || tr == TR_NED || tr == TR_NEDROT || tr == TR_NEDMAX;

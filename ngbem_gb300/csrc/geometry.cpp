@@ -240,6 +240,19 @@ void SpaceH::build(MeshH* m, int kind_, int dual_, const unsigned char* mask) {
         dofs[3 * e + k] = map[g];
         sign[3 * e + k] = m->T[3 * e + k] < m->T[3 * e + (k + 1) % 3] ? 1 : -1;
       }
+  } else if (kind >= BEM_L2P1 && kind <= BEM_L2P3) {
+    // SurfaceL2 of order p: (p+1)(p+2)/2 consecutive dofs per element; the signs hold the
+    // element's local vertices in the order of their global numbers (the Dubiner basis is
+    // built on that order, as NGSolve's L2 triangle element builds it)
+    const int p = kind - BEM_L2P1 + 1;
+    nd = (p + 1) * (p + 2) / 2;
+    for (int e : elems) {
+      dofs[3 * e] = dofs[3 * e + 1] = dofs[3 * e + 2] = (int)global_dof.size();
+      for (int a = 0; a < nd; ++a) global_dof.push_back(e);
+      int f[3] = {0, 1, 2};
+      std::sort(f, f + 3, [&](int x, int y) { return m->T[3 * e + x] < m->T[3 * e + y]; });
+      for (int k = 0; k < 3; ++k) sign[3 * e + k] = f[k];
+    }
   } else {
     throw Error(BEM_ERR_ARG, "unknown space kind");
   }
@@ -247,12 +260,12 @@ void SpaceH::build(MeshH* m, int kind_, int dual_, const unsigned char* mask) {
   // dof -> elements (CSR, ascending element ids)
   e4d_ptr.assign(ndof + 1, 0);
   for (int e : elems)
-    for (int a = 0; a < nd; ++a) e4d_ptr[dofs[3 * e + a] + 1]++;
+    for (int a = 0; a < nd; ++a) e4d_ptr[dof(e, a) + 1]++;
   for (int d = 0; d < ndof; ++d) e4d_ptr[d + 1] += e4d_ptr[d];
   e4d.assign(e4d_ptr[ndof], 0);
   std::vector<int> fill(e4d_ptr.begin(), e4d_ptr.end() - 1);
   for (int e : elems)
-    for (int a = 0; a < nd; ++a) e4d[fill[dofs[3 * e + a]]++] = e;
+    for (int a = 0; a < nd; ++a) e4d[fill[dof(e, a)]++] = e;
   for (int d = 0; d < ndof; ++d)
     if (e4d_ptr[d + 1] == e4d_ptr[d]) throw Error(BEM_ERR_ARG, "space has a dof without elements");
 }
@@ -271,6 +284,7 @@ void SpaceH::ensure_device() {
 
 int trace_kind(int space_kind, int ev) {
   if (space_kind == BEM_P0) return ev == BEM_EV_ID ? TR_P0 : -1;
+  if (space_kind >= BEM_L2P1 && space_kind <= BEM_L2P3) return ev == BEM_EV_ID ? TR_L2P1 + space_kind - BEM_L2P1 : -1;
   if (space_kind == BEM_P1) {
     if (ev == BEM_EV_ID) return TR_P1;
     if (ev == BEM_EV_ROT) return TR_ROT;
@@ -304,7 +318,7 @@ static void cluster_data(const SpaceH& sp, std::vector<double>& G, std::vector<s
   std::vector<int> cnt(ndof, 0);
   for (int e : sp.elems)
     for (int a = 0; a < sp.nd; ++a) {
-      const int d = sp.el_dofs(e)[a];
+      const int d = sp.dof(e, a);
       G[d] += m.area(e);
       cnt[d] += 1;
     }
@@ -312,21 +326,21 @@ static void cluster_data(const SpaceH& sp, std::vector<double>& G, std::vector<s
   for (int e : sp.elems) {
     double pt[7][3];
     for (int j = 0; j < 7; ++j) m.map(e, xhat[j][0], xhat[j][1], pt[j]);
-    const int* dn = sp.el_dofs(e);
+    auto dn = [&](int a) { return sp.dof(e, a); };
     int nvert = 0, nedge = 0;
     for (int a = 0; a < sp.nd; ++a) {
-      const int c = cnt[dn[a]];
-      if (c > 2) { X[dn[a]] = {pt[nvert][0], pt[nvert][1], pt[nvert][2]}; ++nvert; }
+      const int c = cnt[dn(a)];
+      if (c > 2) { X[dn(a)] = {pt[nvert][0], pt[nvert][1], pt[nvert][2]}; ++nvert; }
       if (c == 2) ++nedge;
-      if (c == 1) X[dn[a]] = {pt[6][0], pt[6][1], pt[6][2]};
+      if (c == 1) X[dn(a)] = {pt[6][0], pt[6][1], pt[6][2]};
     }
     // fewer than three two-element dofs (an element at the border of an open surface or of a
     // region): each is its own edge (the reference's loop would not advance with 0 per edge)
     const int per_edge = std::max(1, nedge / 3);
     int ie = 0;
     for (int a = 0; a < sp.nd; ++a) {
-      if (cnt[dn[a]] != 2) continue;
-      for (int o = 0; o < per_edge; ++o) X[dn[a + o]] = {pt[3 + ie][0], pt[3 + ie][1], pt[3 + ie][2]};
+      if (cnt[dn(a)] != 2) continue;
+      for (int o = 0; o < per_edge; ++o) X[dn(a + o)] = {pt[3 + ie][0], pt[3 + ie][1], pt[3 + ie][2]};
       ++ie;
       a += per_edge - 1;
     }

@@ -116,7 +116,9 @@ struct SpaceH {
   // mask: nt flags of the elements the space lives on (null: all of them)
   void build(MeshH* m, int kind_, int dual_, const unsigned char* mask = nullptr);
   bool on(int e) const { return dofs[3 * e] >= 0; }
-  const int* el_dofs(int e) const { return &dofs[3 * e]; }
+  const int* el_dofs(int e) const { return &dofs[3 * e]; }  // kinds with at most 3 dofs per element
+  // dof of local dof a of element e (SurfaceL2 of order >= 1: consecutive from dofs[3 e])
+  int dof(int e, int a) const { return kind >= BEM_L2P1 ? dofs[3 * e] + a : dofs[3 * e + a]; }
   void ensure_device();
   // cluster tree with element patches for a leaf size, built on first use and shared by the
   // operators on this space (a tree depends only on the space and the leaf size)

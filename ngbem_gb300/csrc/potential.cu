@@ -41,21 +41,15 @@ __global__ void pot_sources_kernel(PotArgs a) {
         xp[x][y] = (y == 0 ? qo.x : (y == 1 ? qo.y : qo.z)) - Ee.o[x][y];
       }
     const double nrm[3] = {Ee.n[0], Ee.n[1], Ee.n[2]};
-    int sg[3] = {1, 1, 1};
-    if (edge_trace(TRT)) {
-      const int4 s = a.trial.sign[e];
-      sg[0] = s.x;
-      sg[1] = s.y;
-      sg[2] = s.z;
-    }
+    int sg[SignSlots<TRT>::N];
+    elem_signs<TRT>(a.trial.sign, e, sg);
     const int4 dn = a.trial.dofs[e];
-    const int dof[3] = {dn.x, dn.y, dn.z};
     V val[DIM];
 #pragma unroll
     for (int c = 0; c < DIM; ++c) val[c] = vzero<V>();
 #pragma unroll
     for (int x = 0; x < ND; ++x) {
-      const V dv = dens[dof[x]];
+      const V dv = dens[elem_dof<TRT>(dn, x)];
 #pragma unroll
       for (int c = 0; c < DIM; ++c)
         val[c] += dv * trace_val<TRT, double>(x, c, RQ[2 * q], RQ[2 * q + 1], xp, Ee.invdetJ, rot, sg[x],
@@ -115,8 +109,8 @@ __global__ void __launch_bounds__(POT_THREADS) pot_eval_kernel(PotArgs a) {
   }
 }
 
-// (kernel, trial trace) pairs of the operators: the scalar kernels with P0 / P1 identity
-// traces, the hypersingular kernels with their curl traces, the Maxwell single layer with RT0
+// (kernel, trial trace) pairs of the operators: the scalar kernels with P0 / P1 (and
+// SurfaceL2 of order 1..3) identity traces, the hypersingular kernels with their curl traces, the Maxwell single layer with RT0
 // and in its curl form with HCurl (the double layer has none: the reference's PotentialCF
 // sums its cross-product terms without their signs)
 #define BEM_POT_COMBOS(X)                                                                        \
@@ -127,7 +121,11 @@ __global__ void __launch_bounds__(POT_THREADS) pot_eval_kernel(PotArgs a) {
   X(K_HELMHOLTZ_CF, TR_P0, cpx<double>) X(K_HELMHOLTZ_CF, TR_P1, cpx<double>)                   \
   X(K_HELMHOLTZ_HS, TR_HELM, cpx<double>) X(K_MAXWELL_SL, TR_MAX, cpx<double>)                  \
   X(K_MAXWELL_SL, TR_NEDMAX, cpx<double>)                                                        \
-  X(K_HELMHOLTZ_SL_DKAPPA, TR_P0, cpx<double>) X(K_HELMHOLTZ_SL_DKAPPA, TR_P1, cpx<double>)
+  X(K_HELMHOLTZ_SL_DKAPPA, TR_P0, cpx<double>) X(K_HELMHOLTZ_SL_DKAPPA, TR_P1, cpx<double>)      \
+  X(K_LAPLACE_SL, TR_L2P1, double) X(K_LAPLACE_SL, TR_L2P2, double) X(K_LAPLACE_SL, TR_L2P3, double) \
+  X(K_LAPLACE_DL, TR_L2P1, double) X(K_LAPLACE_DL, TR_L2P2, double) X(K_LAPLACE_DL, TR_L2P3, double) \
+  X(K_HELMHOLTZ_SL, TR_L2P1, cpx<double>) X(K_HELMHOLTZ_SL, TR_L2P2, cpx<double>)               \
+  X(K_HELMHOLTZ_SL, TR_L2P3, cpx<double>)
 
 int potential_dim(int kid, int trt) {
 #define X(K, T, V) \

@@ -12,7 +12,7 @@ import numpy as np
 from .meshes import Mesh
 
 __all__ = ["triangle_rule", "load_vector", "p1_load_vector", "p0_load_vector", "plane_wave_bm_source",
-           "random_directions"]
+           "random_directions", "dubiner"]
 
 
 def triangle_rule(order: int):
@@ -65,6 +65,29 @@ def p0_load_vector(mesh: Mesh, f, order: int = 6) -> np.ndarray:
     return (fv @ w) * detj
 
 
+def dubiner(p: int, lam: np.ndarray, f0: np.ndarray, f1: np.ndarray) -> np.ndarray:
+    """The SurfaceL2 basis of order p at barycentric points lam (nq, 3) of every triangle, whose
+    vertices in the order of their global numbers start with local vertices f0, f1 (nt,):
+    (nt, nq, (p+1)(p+2)/2) values of t^i P_i(s/t) P_j^(2i+1,0)(z), x = lam_f0, y = lam_f1,
+    s = 2x + y - 1, t = 1 - y, z = 2y - 1, i outer, j inner (the library's basis)."""
+    x = lam[:, f0].T  # (nt, nq)
+    y = lam[:, f1].T
+    s, t, z = 2 * x + y - 1, 1 - y, 2 * y - 1
+    leg = [np.ones_like(s), s]
+    for n in range(1, p):
+        leg.append(((2 * n + 1) * s * leg[n] - n * t * t * leg[n - 1]) / (n + 1))
+    out = []
+    for i in range(p + 1):
+        al = 2 * i + 1
+        jac = [np.ones_like(z), ((al + 2) * z + al) / 2]
+        for n in range(2, p - i + 1):
+            jac.append(((2 * n + al - 1) * ((2 * n + al) * (2 * n + al - 2) * z + al * al) * jac[n - 1]
+                        - 2 * (n + al - 1) * (n - 1) * (2 * n + al) * jac[n - 2]) / (2 * n * (n + al) * (2 * n + al - 2)))
+        for j in range(p - i + 1):
+            out.append(leg[i] * jac[j])
+    return np.stack(out, axis=-1)
+
+
 def load_vector(space, f, order: int = 6) -> np.ndarray:
     """b_i = int f v_i over the space's triangles for the basis v_i of any trace space (the
     role of LinearForm(f * v.Trace() * ds).Assemble() on that space; a space on a region
@@ -88,6 +111,13 @@ def load_vector(space, f, order: int = 6) -> np.ndarray:
     elif space.kind == "P1":
         for a in range(3):
             np.add.at(out, dofs[on, a], (np.einsum("q,tqm->tm", w * lam[:, a], fv) * detj[:, None])[on])
+    elif space.kind.startswith("L2P"):
+        p = int(space.kind[3:])
+        phi = dubiner(p, lam, signs[:, 0], signs[:, 1])  # (nt, nq, nd)
+        contrib = np.einsum("q,tqa,tqm->tam", w, phi, fv) * detj[:, None, None]
+        nd = phi.shape[-1]
+        idx = dofs[on, 0][:, None] + np.arange(nd)[None, :]
+        np.add.at(out, idx.ravel(), contrib[on].reshape(-1, contrib.shape[-1]))
     else:
         P = mesh.vertices[mesh.triangles]
         for k in range(3):

@@ -231,6 +231,39 @@ struct Mesh {
   double area(int e) const { return 0.5 * geo[e].detJ; }
 };
 
+// SurfaceL2 of order p >= 1 has (p+1)(p+2)/2 dofs per element (at most 10 for p = 3)
+constexpr int ORC_MAXND = 10;
+
+// Dubiner basis function a of order P on a triangle (Dubiner 1991; Karniadakis and Sherwin,
+// Spectral/hp Element Methods, ch. 3), as NGSolve's L2 triangle element uses it (third-party
+// code the reference calls through SurfaceL2; restated): x = lambda_f0, y = lambda_f1 with f0,
+// f1 the element's vertices of the lowest and the next global number; s = 2x + y - 1,
+// t = 1 - y, z = 2y - 1;  phi_ij = t^i P_i(s / t) P_j^(2i+1, 0)(z), i = 0..P, j = 0..P-i,
+// numbered with i outer.  Legendre by its three-term recurrence (scaled by t^i), Jacobi by
+// the recurrence of P_n^(alpha, 0).
+static double dubiner(int P, int a, double xi, double eta, int f0, int f1) {
+  const double lam[3] = {xi, eta, 1.0 - xi - eta};
+  const double x = lam[f0], y = lam[f1];
+  int i = 0, first = 0;
+  while (a >= first + (P - i + 1)) { first += P - i + 1; ++i; }
+  const int j = a - first;
+  const double s = 2.0 * x + y - 1.0, t = 1.0 - y, z = 2.0 * y - 1.0;
+  double l0 = 1.0, l1 = s, L = i == 0 ? 1.0 : s;
+  for (int n = 1; n < i; ++n) {
+    const double ln = ((2 * n + 1) * s * l1 - n * t * t * l0) / (n + 1);
+    l0 = l1; l1 = ln; L = ln;
+  }
+  const int al = 2 * i + 1;
+  double j0 = 1.0, j1 = 0.5 * ((al + 2) * z + al), J = j == 0 ? 1.0 : j1;
+  for (int n = 2; n <= j; ++n) {
+    const double jn = ((2.0 * n + al - 1) * ((2.0 * n + al) * (2.0 * n + al - 2) * z + (double)al * al) * j1 -
+                       2.0 * (n + al - 1) * (n - 1) * (2.0 * n + al) * j0) /
+                      (2.0 * n * (n + al) * (2.0 * n + al - 2));
+    j0 = j1; j1 = jn; J = jn;
+  }
+  return L * J;
+}
+
 struct Space {
   int kind = ORC_P0, ndof = 0, nd = 1;
   bool dual = false;
@@ -243,6 +276,17 @@ struct Space {
       for (int e = 0; e < m.nt; ++e) dofs[e] = e;
     } else if (kind == ORC_P1) {
       nd = 3; ndof = m.nv; dofs = m.T;
+    } else if (kind >= ORC_L2P1 && kind <= ORC_L2P3) {
+      // SurfaceL2 of order p: consecutive dofs per element; sign holds the element's local
+      // vertices in the order of their global numbers (the Dubiner basis is built on it)
+      const int pp = kind - ORC_L2P1 + 1;
+      nd = (pp + 1) * (pp + 2) / 2; ndof = m.nt * nd; dofs.resize((size_t)m.nt * nd); sign.resize(3 * m.nt);
+      for (int e = 0; e < m.nt; ++e) {
+        for (int a = 0; a < nd; ++a) dofs[(size_t)e * nd + a] = e * nd + a;
+        int f[3] = {0, 1, 2};
+        std::sort(f, f + 3, [&](int x, int y) { return m.T[3 * e + x] < m.T[3 * e + y]; });
+        for (int k = 0; k < 3; ++k) sign[3 * e + k] = f[k];
+      }
     } else {
       nd = 3; ndof = m.ne; dofs = m.TE; sign.resize(3 * m.nt);
       for (int e = 0; e < m.nt; ++e)
@@ -276,10 +320,15 @@ static void cross3(const double* a, const double* b, double* c) {
 // ROTATED_TRACE n x phi (DiffOpRotatedTrace :62-104), MAXWELL_CURL [n x phi; curl phi]
 // (DiffOpMaxwell :172-255) with the surface curl of phi = div psi = 2 sigma / |J|.
 static void eval_trace(const Mesh& m, const Space& sp, int ev, int e, double xi, double eta,
-                       double S[3][4]) {
+                       double S[ORC_MAXND][4]) {
   const Geo& g = m.geo[e];
   if (sp.kind == ORC_P0) {
     S[0][0] = sp.dual ? 1.0 / g.detJ : 1.0;
+    return;
+  }
+  if (sp.kind >= ORC_L2P1 && sp.kind <= ORC_L2P3) {
+    for (int a = 0; a < sp.nd; ++a)
+      S[a][0] = dubiner(sp.kind - ORC_L2P1 + 1, a, xi, eta, sp.sign[3 * e], sp.sign[3 * e + 1]);
     return;
   }
   if (sp.kind == ORC_P1) {
@@ -691,7 +740,7 @@ struct Operator {
       kernel.eval<T>(x, y, gi.n, gj.n, kv);
       double fac = gi.detJ * gj.detJ * r.w[k];
       for (int c = 0; c < kernel.ncomp; ++c) kv[c] = fac * kv[c];
-      double Si[3][4], Sj[3][4];
+      double Si[ORC_MAXND][4], Sj[ORC_MAXND][4];
       eval_trace(mesh, test, test_ev, ei, xi, xe, Si);
       eval_trace(mesh, trial, trial_ev, ej, yi, ye, Sj);
       for (const Term& t : kernel.terms) {
@@ -718,15 +767,15 @@ struct Operator {
     const int ndi = test.nd, ndj = trial.nd;
     const int nq = (int)irtrig.w.size();
     // shapes of the regular rule per patch element
-    std::vector<double> shi((size_t)patchi.size() * nq * 12), shj((size_t)patchj.size() * nq * 12);
+    std::vector<double> shi((size_t)patchi.size() * nq * 4 * ORC_MAXND), shj((size_t)patchj.size() * nq * 4 * ORC_MAXND);
     for (size_t i = 0; i < patchi.size(); ++i)
       for (int q = 0; q < nq; ++q)
         eval_trace(mesh, test, test_ev, patchi[i], irtrig.xi[q], irtrig.eta[q],
-                   reinterpret_cast<double(*)[4]>(&shi[(i * nq + q) * 12]));
+                   reinterpret_cast<double(*)[4]>(&shi[(i * nq + q) * 4 * ORC_MAXND]));
     for (size_t j = 0; j < patchj.size(); ++j)
       for (int q = 0; q < nq; ++q)
         eval_trace(mesh, trial, trial_ev, patchj[j], irtrig.xi[q], irtrig.eta[q],
-                   reinterpret_cast<double(*)[4]>(&shj[(j * nq + q) * 12]));
+                   reinterpret_cast<double(*)[4]>(&shj[(j * nq + q) * 4 * ORC_MAXND]));
     std::vector<double> pxi((size_t)patchi.size() * nq * 4), pyj((size_t)patchj.size() * nq * 4);
     for (size_t i = 0; i < patchi.size(); ++i)
       for (int q = 0; q < nq; ++q) {
@@ -741,13 +790,13 @@ struct Operator {
         P[3] = irtrig.w[q] * mesh.geo[patchj[j]].detJ;
       }
     std::vector<T> kern((size_t)nq * nq), ks((size_t)nq * ndj);
-    T elmat[9];
+    T elmat[ORC_MAXND * ORC_MAXND];
     for (size_t i = 0; i < patchi.size(); ++i)
       for (size_t j = 0; j < patchj.size(); ++j) {
         int ei = patchi[i], ej = patchj[j];
         const int* vi = &mesh.T[3 * ei];
         const int* vj = &mesh.T[3 * ej];
-        for (int k = 0; k < 9; ++k) elmat[k] = T(0.0);
+        for (int k = 0; k < ndi * ndj; ++k) elmat[k] = T(0.0);
         int ncommon = 0;
         for (int a = 0; a < 3; ++a)
           for (int b = 0; b < 3; ++b)
@@ -799,13 +848,13 @@ struct Operator {
             for (int ix = 0; ix < nq; ++ix)
               for (int b = 0; b < ndj; ++b) {
                 T s = T(0.0);
-                for (int iy = 0; iy < nq; ++iy) s += kern[ix * nq + iy] * shj[(j * nq + iy) * 12 + b * 4 + t.trc];
+                for (int iy = 0; iy < nq; ++iy) s += kern[ix * nq + iy] * shj[(j * nq + iy) * 4 * ORC_MAXND + b * 4 + t.trc];
                 ks[ix * ndj + b] = s;
               }
             for (int a = 0; a < ndi; ++a)
               for (int b = 0; b < ndj; ++b) {
                 T s = T(0.0);
-                for (int ix = 0; ix < nq; ++ix) s += shi[(i * nq + ix) * 12 + a * 4 + t.tec] * ks[ix * ndj + b];
+                for (int ix = 0; ix < nq; ++ix) s += shi[(i * nq + ix) * 4 * ORC_MAXND + a * 4 + t.tec] * ks[ix * ndj + b];
                 elmat[a * ndj + b] += s;
               }
           }
@@ -941,7 +990,7 @@ struct Operator {
       int e = patchi[ie];
       const int* dn = test.el_dofs(e);
       for (int q = 0; q < nq; ++q) {
-        double S[3][4];
+        double S[ORC_MAXND][4];
         eval_trace(mesh, test, test_ev, e, irtrig.xi[q], irtrig.eta[q], S);
         size_t row = ie * nq + q;
         for (size_t t = 0; t < kernel.terms.size(); ++t) {
@@ -960,7 +1009,7 @@ struct Operator {
       int e = patchj[je];
       const int* dn = trial.el_dofs(e);
       for (int q = 0; q < nq; ++q) {
-        double S[3][4];
+        double S[ORC_MAXND][4];
         eval_trace(mesh, trial, trial_ev, e, irtrig.xi[q], irtrig.eta[q], S);
         size_t col = je * nq + q;
         for (size_t t = 0; t < kernel.terms.size(); ++t) {
@@ -1292,7 +1341,7 @@ static void potential_t(int kernel, double kappa, const Mesh& m, const Space& sp
     const double* nx = normals ? normals + 3 * (size_t)p : nz;
     for (int e = 0; e < m.nt; ++e) {
       for (size_t q = 0; q < r.w.size(); ++q) {
-        double S[3][4] = {{0}};
+        double S[ORC_MAXND][4] = {{0}};
         eval_trace(m, sp, ev, e, r.xi[q], r.eta[q], S);
         T vals[4] = {T(0), T(0), T(0), T(0)};
         for (int a = 0; a < sp.nd; ++a)
@@ -1334,7 +1383,7 @@ int orc_mass_matrix(int nv, const double* xyz, int nt, const int* tri, int trial
   int dim = trace_dim(tr.kind, evtr);
   for (int e = 0; e < m.nt; ++e)
     for (size_t q = 0; q < r.w.size(); ++q) {
-      double Si[3][4], Sj[3][4];
+      double Si[ORC_MAXND][4], Sj[ORC_MAXND][4];
       eval_trace(m, te, evte, e, r.xi[q], r.eta[q], Si);
       eval_trace(m, tr, evtr, e, r.xi[q], r.eta[q], Sj);
       double w = r.w[q] * m.geo[e].detJ;

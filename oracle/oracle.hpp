@@ -40,7 +40,8 @@ enum {
 };
 // space kinds
 // (ORC_HCURL: surface Nedelec order 0, shape n x the RT0 shape of the same edge and sign)
-enum { ORC_P0 = 0, ORC_P1 = 1, ORC_RT0 = 2, ORC_HCURL = 3 };
+// ORC_L2P1..3: SurfaceL2 of order 1..3 (Dubiner basis on the vertices sorted by global number)
+enum { ORC_P0 = 0, ORC_P1 = 1, ORC_RT0 = 2, ORC_HCURL = 3, ORC_L2P1 = 4, ORC_L2P2 = 5, ORC_L2P3 = 6 };
 // trace evaluators; on ORC_HCURL: ID the tangential trace, ROTATED_TRACE DiffOpRotatedTrace,
 // MAXWELL_CURL DiffOpMaxwell
 enum { ORC_EV_ID = 0, ORC_EV_ROT = 1, ORC_EV_HELM = 2, ORC_EV_MAXWELL = 3,

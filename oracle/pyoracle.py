@@ -17,7 +17,7 @@ _LIB = None
 KERNELS = {"laplace_sl": 0, "laplace_dl": 1, "laplace_hs": 2, "helmholtz_sl": 3,
            "helmholtz_dl": 4, "helmholtz_hs": 5, "helmholtz_cf": 6, "maxwell_sl": 7,
            "helmholtz_sl_dkappa": 8, "maxwell_dl": 9}
-KINDS = {"P0": 0, "P1": 1, "RT0": 2, "HCURL": 3}
+KINDS = {"P0": 0, "P1": 1, "RT0": 2, "HCURL": 3, "L2P1": 4, "L2P2": 5, "L2P3": 6}
 EVALS = {"id": 0, "rot": 1, "helm": 2, "maxwell": 3, "rotatedtrace": 4, "maxwellcurl": 5}
 
 
@@ -102,6 +102,9 @@ def ss_rule(cls, order):
 def ndof(mesh, kind):
     if kind == "P0":
         return mesh.nt
+    if kind.startswith("L2P"):
+        p = int(kind[3:])
+        return mesh.nt * (p + 1) * (p + 2) // 2
     if kind == "P1":
         return mesh.nv
     return len(mesh_edges(mesh)[0])

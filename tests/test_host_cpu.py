@@ -78,7 +78,7 @@ def test_argument_errors_are_status_codes():
     with pytest.raises(ValueError):
         nb.TraceSpace(m, "P2")
     with pytest.raises(NotImplementedError):
-        nb.SurfaceL2(m, order=2)
+        nb.SurfaceL2(m, order=4)
     sp = nb.SurfaceL2(m)
     with pytest.raises(_lib.BemError):
         nb.cluster_tree(sp, 0)
