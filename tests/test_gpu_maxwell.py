@@ -46,3 +46,27 @@ def test_maxwell_mixed_against_fp64():
     y64 = (ops["fp64"].mat * x).cpu().numpy()
     y32 = (ops["mixed"].mat * x).cpu().numpy()
     assert rel(y32, y64) < 1e-5
+
+
+def test_maxwell_config_size_against_oracle_hmatrix(oracle):
+    """The Maxwell workload's own size: RT0 on the L5 icosphere (30 720 edge dofs), kappa 2,
+    leaf 20, eta 2, ACA eps 1e-6.  Both GPU paths against the oracle's H-matrix of the same
+    partition (its assembly takes about ten seconds on the host cores), product and transposed
+    product, within the ACA tolerance; the block lists are equal block for block."""
+    m = icosphere(5)
+    RT = nb.HDivSurface(m, complex=True)
+    H = oracle.OracleOperator("maxwell_sl", m, "RT0", kappa=2.0, trial_eval="maxwell", intorder=3, leafsize=20,
+                              eta=2.0, eps=1e-6)
+    x = _x(RT.ndof, 5)
+    yo, yto = H.mult(x), H.mult(x, trans=True)
+    ob = H.blocks()
+    for precision in ("fp64", "mixed"):
+        op = nb.MaxwellSingleLayerPotentialOperator(RT, kappa=2.0, intorder=3, leafsize=20, eta=2.0, eps=1e-6,
+                                                    precision=precision)
+        b = op.mat.blocks()
+        for k in ("rowcl", "colcl", "near"):
+            assert np.array_equal(b[k], ob[k])
+        xd = torch.from_numpy(x).cuda()
+        assert rel((op.mat * xd).cpu().numpy(), yo) < 1e-5
+        assert rel((op.mat.T * xd).cpu().numpy(), yto) < 1e-5
+        del op
