@@ -8,6 +8,11 @@ application captured in a CUDA graph).  With one, the iteration below runs in to
 vectors' device while every operator and preconditioner application is the library's own
 (H-matrix products, sparse mass matrices and their inverses).  The functions here take
 callables on vectors and are device-agnostic.
+
+This module is a convenience for the solver pattern of the reference's tests, outside the
+accelerated path: its loops are torch operations on a handful of vectors, launched one by one.
+The accelerated solves are the library's native GMRES (CUDA-graph matvec) and its batched GMRES
+for many right-hand sides.
 """
 from __future__ import annotations
 
