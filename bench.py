@@ -13,7 +13,7 @@ L2 is flushed before every step (a 512 MiB write, then a 512 MiB read of a secon
 that the write-back of the flush's dirty lines does not land inside the step); each step is
 timed with CUDA events on the launch stream.  value = single-right-hand-side H-matvecs per
 second (32 per step) over all ranks.  e2e = the same step through the host-buffer C-ABI entry
-point (page-locked X read and Y written by the kernels across the host link).
+point (page-locked X and Y, staged by one bulk copy each way).
 
 The same line carries the metric's other half and its comparators: assembly seconds of the
 mixed and the plain FP64 GPU path, the batched 32-right-hand-side solve of both paths, the
@@ -868,7 +868,7 @@ def run_bm(args):
             "clocks": clocks,
             "e2e": {"value": e2e_value, "unit": "matvec/s", "h2d_bytes_per_step": n * nrhs * 16,
                     "d2h_bytes_per_step": n * nrhs * 16, "check_rel_err": e2e_check,
-                    "note": "page-locked buffers read and written by the kernels across the host link"}}
+                    "note": "page-locked host buffers, staged by one bulk copy each way (products above 1 MiB)"}}
 
     if rank == 0 and not args.no_cpu_baseline:
         r = cpu_reference_bm(L, 2, 2, 0)

@@ -209,9 +209,11 @@ int bem_operator_mult_noalloc(bem_operator_t op, int trans, const double* alpha,
 int bem_operator_set_global_dofs(bem_operator_t op, int trial_nglobal, const int* trial_map, int test_nglobal,
                                  const int* test_map);
 
-/* Same with HOST buffers (synchronous).  Page-locked buffers (cudaHostAlloc, torch
- * pin_memory) are read and written by the kernels in place through their device mapping;
- * other host memory is copied up, applied and copied back. */
+/* Same with HOST buffers (synchronous).  When x and y together hold at most
+ * BEM_HOST_MAPPED_MAX_BYTES and both are page-locked (cudaHostAlloc, torch pin_memory), the
+ * kernels read and write them in place through their device mapping; larger products and
+ * other host memory are copied up, applied and copied back. */
+#define BEM_HOST_MAPPED_MAX_BYTES (1u << 20)
 int bem_operator_mult_host(bem_operator_t op, int trans, const double* alpha, const void* x,
                            const double* beta, void* y, int nrhs);
 

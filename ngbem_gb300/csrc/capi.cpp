@@ -313,9 +313,12 @@ int bem_operator_mult_host(bem_operator_t op, int trans, const double* alpha, co
       nin = (size_t)vm.ld_in * nrhs;
       nout = (size_t)vm.ld_out * nrhs;
     }
-    // Page-locked host buffers are mapped into the device's address space: the kernels read x
-    // and write y across the host link themselves, with no staging copies (each step still
-    // moves x to the device and y back).  Other host memory goes through device staging.
+    // Page-locked host buffers are mapped into the device's address space.  For small products
+    // the kernels read x and write y across the host link themselves (no copy launches); their
+    // accesses go through the cluster permutations, so each is a scattered access across the
+    // link, which for large products costs more than one bulk copy each way.  Larger products,
+    // and other host memory, go through device staging.
+    const bool small = (nin + nout) * esz <= BEM_HOST_MAPPED_MAX_BYTES;
     auto mapped = [](const void* p) -> void* {
       cudaPointerAttributes at{};
       if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
@@ -324,7 +327,7 @@ int bem_operator_mult_host(bem_operator_t op, int trans, const double* alpha, co
       }
       return at.type == cudaMemoryTypeHost ? at.devicePointer : nullptr;
     };
-    void* xm = mapped(x);
+    void* xm = small ? mapped(x) : nullptr;
     void* ym = xm ? mapped(y) : nullptr;
     // a synchronous call reports a product whose bounded device waits ran out (and clears the
     // operator's device state so that the next product starts clean)
