@@ -163,13 +163,14 @@ __device__ __forceinline__ void tmem_wait(float (&v)[8]) {
                : "memory");
 }
 
-// round to TF32 (10 stored mantissa bits, nearest, ties away), low 13 bits cleared
+// round to TF32 (10 stored mantissa bits, nearest, ties away from zero), low 13 bits cleared:
+// adding half a TF32 unit (bit 12) to the bit pattern rounds the magnitude, a carry moving into
+// the exponent as it should (finite values far below FLT_MAX).  Two integer operations on the
+// full-rate pipes instead of a conversion: the epilogue rounds every T entry twice.
 __device__ __forceinline__ float tf32_rn(float x) {
-  uint32_t r;
-  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
-  return __uint_as_float(r & 0xFFFFE000u);
+  return __uint_as_float((__float_as_uint(x) + 0x1000u) & 0xFFFFE000u);
 }
-// high (h = 0) or low (h = 1) TF32 part of v
+// high (h = 0) or low (h = 1) TF32 part of v; v - hi is exact in FP32
 __device__ __forceinline__ float tf32_part(float v, int h) {
   const float hi = tf32_rn(v);
   return h ? tf32_rn(v - hi) : hi;
@@ -408,6 +409,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1) tc_gemm_kernel(TCGemmArgs g) {
         // columns (rank k, real/imaginary c) of each block: T = V2 x combined from the four
         // real products, written as the block's pass-1 A panel: row (r, a', h') holds, for
         // K = (k, c), the h' part of  a' = 0: (Re T_k, -Im T_k);  a' = 1: (Im T_k, Re T_k)
+        // the block holding the current column group: its T panel and columns [col, cend);
+        // blocks are stacked in column order, so it is looked up again only past cend
+        float4* ta = nullptr;
+        int col = 0, cend = -1;
 #pragma unroll
         for (int b = 0; b < 4; ++b) {
           if (b >= nb) break;
@@ -415,12 +420,14 @@ __global__ void __launch_bounds__(TC_THREADS, 1) tc_gemm_kernel(TCGemmArgs g) {
           for (int j = 0; j < 4; ++j) {
             if (4 * b + j >= ng8) break;           // past this warp's columns
             const int gcol = c0 + 32 * b + 8 * j;  // warp-uniform
-            const unsigned m = __ballot_sync(FULL, lane < I.nout && oc.col <= gcol);
-            const int o = __popc(m) - 1;
-            float4* ta = (float4*)__shfl_sync(FULL, oc.ta, o < 0 ? 0 : o);
-            const int col = __shfl_sync(FULL, oc.col, o < 0 ? 0 : o);
-            const int nc = 2 * __shfl_sync(FULL, oc.rpad, o < 0 ? 0 : o);
-            if (o < 0 || gcol >= col + nc) continue;  // padding columns after the last block
+            if (gcol >= cend) {
+              const unsigned m = __ballot_sync(FULL, lane < I.nout && oc.col <= gcol);
+              const int o = __popc(m) - 1;
+              ta = (float4*)__shfl_sync(FULL, oc.ta, o < 0 ? 0 : o);
+              col = __shfl_sync(FULL, oc.col, o < 0 ? 0 : o);
+              cend = o < 0 ? -1 : col + 2 * __shfl_sync(FULL, oc.rpad, o < 0 ? 0 : o);
+              if (gcol >= cend) continue;  // padding columns after the last block
+            }
             float sm[8], pm[8], out[8];
 #pragma unroll
             for (int k = 0; k < 8; ++k) sm[k] = sum[b][8 * j + k] + __shfl_xor_sync(FULL, sum[b][8 * j + k], 1);
