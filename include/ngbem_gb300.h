@@ -40,8 +40,14 @@ enum {
  * shape functions of the same edges and signs) */
 /* BEM_L2P1..3: SurfaceL2 of order 1..3 (NGSolve SurfaceL2(mesh, order=p)): (p+1)(p+2)/2
  * consecutive dofs per element, the Dubiner basis on the element's vertices taken in the order
- * of their global numbers; identity trace only. */
-enum { BEM_P0 = 0, BEM_P1 = 1, BEM_RT0 = 2, BEM_HCURL = 3, BEM_L2P1 = 4, BEM_L2P2 = 5, BEM_L2P3 = 6 };
+ * of their global numbers; identity trace only.
+ * BEM_H1P2, BEM_H1P3: H1 of order 2, 3 (NGSolve H1(mesh, order=p) on a surface mesh): the
+ * vertex dofs (ascending vertex numbers), then p - 1 dofs per edge (edges by first
+ * appearance), then (p - 1)(p - 2) / 2 per element; a hierarchical basis (vertex hats, edge
+ * bubbles l_i l_j (l_j - l_i)^m oriented from the lower to the higher vertex number, the face
+ * bubble l_0 l_1 l_2).  Traces ID and ROT. */
+enum { BEM_P0 = 0, BEM_P1 = 1, BEM_RT0 = 2, BEM_HCURL = 3, BEM_L2P1 = 4, BEM_L2P2 = 5, BEM_L2P3 = 6,
+       BEM_H1P2 = 7, BEM_H1P3 = 8 };
 /* trace evaluators: GetEvaluator(BND) (ID), DiffOpBoundaryRot (ROT), DiffOpHelmholtz (HELM),
  * DiffOpMaxwellNew (MAXWELL); reference src/diffops.hpp:12-338.  On BEM_HCURL: ID is the
  * tangential trace (GetEvaluator(BND) of an HCurl space), ROTATED_TRACE is
@@ -119,7 +125,10 @@ int bem_space_create(bem_mesh_t mesh, int kind, int dual_mapping, bem_space_t* o
  * ascending order, edges by first appearance); bem_space_global_dofs maps them back. */
 int bem_space_create_on(bem_mesh_t mesh, int kind, int dual_mapping, const unsigned char* element_mask,
                         bem_space_t* out);
-/* dof -> element (P0), vertex (P1) or mesh edge (RT0, HCURL); out holds ndof entries */
+/* dof -> element (P0), vertex (P1) or mesh edge (RT0, HCURL); out holds ndof entries.
+ * BEM_H1P2/3: the dof of the same basis function in the space on the whole mesh (vertex v:
+ * v; dof j of mesh edge g: nv + g (p - 1) + j; face dof j of element e: nv + ne (p - 1) +
+ * e (p - 1)(p - 2) / 2 + j). */
 int bem_space_global_dofs(bem_space_t space, int* out);
 /* The dofs of every element (FESpace::GetDofNrs, as the reference reads them throughout
  * src/ngbem.cpp): dofs holds 3 ints per element (P0: the element's dof in the first; -1 on
@@ -128,6 +137,12 @@ int bem_space_global_dofs(bem_space_t space, int* out);
  * first dof (its (p+1)(p+2)/2 dofs are consecutive), the others -1, and signs the element's
  * local vertices in the order of their global numbers. */
 int bem_space_element_dofs(bem_space_t space, int* dofs, int* signs);
+/* Every local dof of every element (FESpace::GetDofNrs for any space kind): *nd = the dofs per
+ * element; dofs (may be null to query nd) holds nd ints per element in the local order of the
+ * basis (-1 on elements outside the space's region).  BEM_H1P2/3: vertices 0..2, the p - 1
+ * dofs of the local edges (0,1), (1,2), (2,0), then the face dofs; bem_space_element_dofs
+ * gives their vertex dofs and, in signs, the edges' orientations. */
+int bem_space_dof_table(bem_space_t space, int* nd, int* dofs);
 int bem_space_ndof(bem_space_t space, int* ndof);
 int bem_space_destroy(bem_space_t space);
 

@@ -75,7 +75,8 @@ class _MeshHandle:
 
 class TraceSpace:
     """Surface trace space: kind "P0" (SurfaceL2 order 0), "P1" (H1 order 1), "RT0" (HDivSurface order 0),
-    "HCURL" (surface trace of HCurl order 0)."""
+    "HCURL" (surface trace of HCurl order 0), "L2P1".."L2P3" (SurfaceL2 orders 1-3), "H1P2",
+    "H1P3" (H1 orders 2, 3)."""
 
     def __init__(self, mesh: Mesh, kind: str, dual_mapping: bool = False, complex: bool = False, definedon=None):
         if kind not in KINDS:
@@ -105,6 +106,15 @@ class TraceSpace:
         s = np.zeros((nt, 3), dtype=np.int32)
         check(lib.bem_space_element_dofs(self.h, d.ctypes.data_as(_lib._ip), s.ctypes.data_as(_lib._ip)))
         return d, s
+
+    def dof_table(self):
+        """(nt, nd) array of every local dof of every triangle in the basis's local order
+        (FESpace::GetDofNrs for any kind; -1 off the space's region)."""
+        nd = C.c_int()
+        check(lib.bem_space_dof_table(self.h, C.byref(nd), None))
+        t = np.zeros((self.mesh.nt, nd.value), dtype=np.int32)
+        check(lib.bem_space_dof_table(self.h, C.byref(nd), t.ctypes.data_as(_lib._ip)))
+        return t
 
     @property
     def global_dofs(self) -> np.ndarray:
@@ -146,10 +156,15 @@ def SurfaceL2(mesh: Mesh, order: int = 0, dual_mapping: bool = False, complex: b
 
 
 def H1(mesh: Mesh, order: int = 1, complex: bool = False, definedon=None) -> TraceSpace:
-    """Continuous piecewise linears on the surface (trace of NGSolve H1, order 1)."""
-    if order != 1:
-        raise NotImplementedError("H1: only order 1 is supported")
-    return TraceSpace(mesh, "P1", False, complex, definedon)
+    """Continuous piecewise polynomials of degree `order` on the surface (NGSolve H1 on a
+    surface mesh).  Order 1: the hat functions (one dof per vertex).  Orders 2, 3: a
+    hierarchical basis: the vertex hats, then p - 1 edge bubbles l_i l_j (l_j - l_i)^m per edge
+    (oriented from the lower to the higher vertex number), then the face bubble l_0 l_1 l_2
+    (order 3); dofs numbered vertices, edges (by first appearance), faces.  The traces are the
+    identity and the surface curl (hypersingular operator)."""
+    if order not in (1, 2, 3):
+        raise NotImplementedError("H1: orders 1 to 3 are supported")
+    return TraceSpace(mesh, "P1" if order == 1 else f"H1P{order}", False, complex, definedon)
 
 
 def HDivSurface(mesh: Mesh, order: int = 0, complex: bool = False, definedon=None) -> TraceSpace:

@@ -386,10 +386,10 @@ __global__ void __launch_bounds__(256) aca_project_kernel(ProjArgs a) {
         for (int x = 0; x < NDI; ++x)
           acc[x] += u * trace_val<TET, P>(x, G::tec(t), rp.x, rp.y, xp, Ee.invdetJ, rot, sg[x], a.test.dual != 0, nrm);
       }
-      const int4 dn = a.test.dofs[e];
+      const int4 dn = a.test.dofs[e], dx = dof_aux<TET>(a.test.sign, e);
 #pragma unroll
       for (int x = 0; x < NDI; ++x) {
-        const int li = a.test.pinv[elem_dof<TET>(dn, x)] - L.r0;
+        const int li = a.test.pinv[elem_dof<TET>(dn, dx, x)] - L.r0;
         if (li >= 0 && li < L.m) atomic_add(&U2[lr_u_index(L, li, off + kk)], acc[x] * fac);
       }
     }
@@ -416,10 +416,10 @@ __global__ void __launch_bounds__(256) aca_project_kernel(ProjArgs a) {
         for (int x = 0; x < NDJ; ++x)
           acc[x] += v * trace_val<TRT, P>(x, G::trc(t), rp.x, rp.y, xp, Ee.invdetJ, rot, sg[x], a.trial.dual != 0, nrm);
       }
-      const int4 dn = a.trial.dofs[e];
+      const int4 dn = a.trial.dofs[e], dx = dof_aux<TRT>(a.trial.sign, e);
 #pragma unroll
       for (int x = 0; x < NDJ; ++x) {
-        const int lj = a.trial.pinv[elem_dof<TRT>(dn, x)] - L.c0;
+        const int lj = a.trial.pinv[elem_dof<TRT>(dn, dx, x)] - L.c0;
         if (lj >= 0 && lj < L.n) atomic_add(&V2[lr_v_index(L, off + kk, lj)], acc[x]);
       }
     }
@@ -493,7 +493,7 @@ void launch_aca(int kid, int prec, const AcaArgs& a, cudaStream_t s) {
   X(K_HELMHOLTZ_HS, TR_HELM, TR_HELM)                                                 \
   X(K_MAXWELL_SL, TR_MAX, TR_MAX) X(K_MAXWELL_SL, TR_NEDMAX, TR_NEDMAX)                \
   X(K_MAXWELL_DL, TR_NEDROT, TR_NED) X(K_MAXWELL_DL, TR_NEDROT, TR_RT0ID)  \
-  BEM_L2P_COMBOS(X)
+  BEM_L2P_COMBOS(X) BEM_H1P_COMBOS(X)
 
 void launch_projection(int kid, int prec, int trt, int tet, const ProjArgs& a, cudaStream_t s) {
   if (a.nfar <= 0) return;

@@ -349,12 +349,33 @@ void MassOperator::build(SpaceH* trial, SpaceH* test, bool complex_vectors) {
   ncols = trial->ndof;
   height = nrows;
   width = ncols;
-  TrigRule r = make_trig_rule(4);
+  // a rule exact for the product of the two spaces' polynomials (at least order 4)
+  auto degree = [](const SpaceH& sp) {
+    if (sp.kind == BEM_P0) return 0;
+    if (sp.kind >= BEM_L2P1 && sp.kind <= BEM_L2P3) return sp.kind - BEM_L2P1 + 1;
+    if (sp.kind == BEM_H1P2) return 2;
+    if (sp.kind == BEM_H1P3) return 3;
+    return 1;
+  };
+  TrigRule r = make_trig_rule(std::max(4, degree(*trial) + degree(*test)));
   const int nq = (int)r.w.size();
   std::vector<std::vector<std::pair<int, double>>> rows(nrows);
   auto shape = [&](const SpaceH& sp, int e, double xi, double eta, double S[10][3], int& dim) {
     const ElemRec64& g = m.rec[e];
     if (sp.kind == BEM_P0) { S[0][0] = sp.dual ? g.invdetJ : 1.0; dim = 1; return; }
+    if (sp.kind == BEM_H1P2 || sp.kind == BEM_H1P3) {
+      // vertex hats, edge bubbles (orientation sign to the power m), face bubble
+      const int P = sp.kind == BEM_H1P2 ? 2 : 3;
+      const double l[3] = {xi, eta, 1.0 - xi - eta};
+      for (int a = 0; a < sp.nd; ++a) {
+        double d[3];
+        double v = h1p_shape<double>(P, a, l, d);
+        if (a >= 3 && a < 3 + 3 * (P - 1) && (a - 3) % (P - 1) == 1) v *= sp.sign[3 * e + (a - 3) / (P - 1)];
+        S[a][0] = v;
+      }
+      dim = 1;
+      return;
+    }
     if (sp.kind >= BEM_L2P1) {
       const int code = sp.sign[3 * e] + 3 * sp.sign[3 * e + 1];
       for (int a = 0; a < sp.nd; ++a) S[a][0] = dubiner<double>(sp.kind - BEM_L2P1 + 1, a, xi, eta, code);

@@ -321,13 +321,36 @@ template <> struct TraceInfo<TR_NEDMAX> { static constexpr int ND = 3, DIM = 4; 
 template <> struct TraceInfo<TR_L2P1> { static constexpr int ND = 3, DIM = 1; };
 template <> struct TraceInfo<TR_L2P2> { static constexpr int ND = 6, DIM = 1; };
 template <> struct TraceInfo<TR_L2P3> { static constexpr int ND = 10, DIM = 1; };
+template <> struct TraceInfo<TR_H1P2> { static constexpr int ND = 6, DIM = 1; };
+template <> struct TraceInfo<TR_H1P3> { static constexpr int ND = 10, DIM = 1; };
+template <> struct TraceInfo<TR_H1P2ROT> { static constexpr int ND = 6, DIM = 3; };
+template <> struct TraceInfo<TR_H1P3ROT> { static constexpr int ND = 10, DIM = 3; };
+// traces that read the element's n x grad(lambda_a) table
+__host__ __device__ constexpr bool needs_rot(int tr) { return tr == TR_ROT || tr == TR_HELM || h1p_rot(tr); }
 // sign slots a kernel keeps per element (at least the three edge signs)
 template <int TR> struct SignSlots { static constexpr int N = TraceInfo<TR>::ND > 3 ? TraceInfo<TR>::ND : 3; };
 
-// global dof of local dof a of an element (dn: the element's dof record)
+// the element's second dof record, read only by traces that need it (H1 of order >= 2)
 template <int TR>
-__device__ __forceinline__ int elem_dof(const int4& dn, int a) {
+__device__ __forceinline__ int4 dof_aux(const int4* sign, int e) {
+  if constexpr (h1p_trace(TR)) return sign[e];
+  else return make_int4(0, 0, 0, 0);
+}
+// global dof of local dof a of an element (dn: the element's dof record; aux: dof_aux).  H1 of
+// order p >= 2: dn = (the three vertex dofs, first face dof), aux = per local edge its
+// orientation sign times (first edge dof + 1)
+template <int TR>
+__device__ __forceinline__ int elem_dof(const int4& dn, const int4& aux, int a) {
   if (l2p_trace(TR)) return dn.x + a;
+  if constexpr (h1p_trace(TR)) {
+    constexpr int P = h1p_order(TR);
+    if (a >= 3 && a < 3 + 3 * (P - 1)) {
+      const int k = (a - 3) / (P - 1), m = (a - 3) % (P - 1);
+      const int g = k == 0 ? aux.x : (k == 1 ? aux.y : aux.z);
+      return (g < 0 ? -g : g) - 1 + m;
+    }
+    if (a >= 3) return dn.w + (a - 3 - 3 * (P - 1));
+  }
   return a == 0 ? dn.x : (a == 1 ? dn.y : dn.z);
 }
 // per-local-dof sign argument of trace_val: edge orientations, or the vertex order code of an
@@ -348,6 +371,17 @@ __device__ __forceinline__ void elem_signs(const int4* sign, int e, int (&sg)[N]
 #pragma unroll
     for (int k = 0; k < N; ++k) sg[k] = code;
   }
+  if constexpr (h1p_trace(TR)) {
+    // edge dof of degree m + 2: the edge's orientation sign to the power m
+    constexpr int P = h1p_order(TR);
+    const int4 g = sign[e];
+#pragma unroll
+    for (int a = 3; a < 3 + 3 * (P - 1) && a < N; ++a) {
+      const int k = (a - 3) / (P - 1), m = (a - 3) % (P - 1);
+      const int o = (k == 0 ? g.x : (k == 1 ? g.y : g.z)) < 0 ? -1 : 1;
+      sg[a] = (m & 1) ? o : 1;
+    }
+  }
 }
 
 // value of trace component c of local dof a (nrm: the element's unit normal, read by TR_NED)
@@ -357,6 +391,13 @@ __device__ __forceinline__ R trace_val(int a, int c, R xi, R eta, const R (*xp)[
   if (TR == TR_P0) return dual ? invdetJ : R(1);
   if (TR == TR_P1) return a == 0 ? xi : (a == 1 ? eta : R(1) - xi - eta);
   if (l2p_trace(TR)) return dubiner<R>(l2p_order(TR), a, xi, eta, sgn);
+  if constexpr (h1p_trace(TR)) {
+    const R l[3] = {xi, eta, R(1) - xi - eta};
+    R d[3];
+    const R v = h1p_shape<R>(h1p_order(TR), a, l, d);
+    if (!h1p_rot(TR)) return R(sgn) * v;
+    return R(sgn) * (d[0] * rot[0][c] + d[1] * rot[1][c] + d[2] * rot[2][c]);
+  }
   if (TR == TR_ROT) return rot[a][c];
   if (TR == TR_HELM) {
     if (c < 3) return rot[a][c];

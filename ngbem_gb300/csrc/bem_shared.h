@@ -18,12 +18,60 @@ enum KernelId {
 // Maxwell trace [-phi_RT0; surface curl] (reference DiffOpRotatedTrace, DiffOpMaxwell,
 // src/diffops.hpp:62-255, for the Whitney edge shapes, which are n x the RT0 shapes)
 // TR_L2P1..3: SurfaceL2 of order 1..3 (the identity trace of the Dubiner basis)
+// TR_H1P2, TR_H1P3: H1 of order 2, 3 (identity trace); TR_H1P2ROT, TR_H1P3ROT: their surface
+// curl n x grad_Gamma phi (DiffOpBoundaryRot, src/diffops.hpp:12-60, for the hierarchical basis
+// h1p_shape below)
 enum TraceKind { TR_P0 = 0, TR_P1 = 1, TR_ROT = 2, TR_HELM = 3, TR_MAX = 4, TR_RT0ID = 5,
-                 TR_NED = 6, TR_NEDROT = 7, TR_NEDMAX = 8, TR_L2P1 = 9, TR_L2P2 = 10, TR_L2P3 = 11 };
+                 TR_NED = 6, TR_NEDROT = 7, TR_NEDMAX = 8, TR_L2P1 = 9, TR_L2P2 = 10, TR_L2P3 = 11,
+                 TR_H1P2 = 12, TR_H1P3 = 13, TR_H1P2ROT = 14, TR_H1P3ROT = 15 };
 // traces of a discontinuous space of order >= 1: the element's dofs are consecutive
 // (first dof + local index) and its "signs" hold the order of its vertices by global number
 __host__ __device__ constexpr bool l2p_trace(int tr) { return tr >= TR_L2P1 && tr <= TR_L2P3; }
 __host__ __device__ constexpr int l2p_order(int tr) { return tr - TR_L2P1 + 1; }
+// traces of H1 of order 2, 3: vertex dofs, then the p - 1 dofs of each local edge (0,1),
+// (1,2), (2,0), then the (p - 1)(p - 2) / 2 face dofs
+__host__ __device__ constexpr bool h1p_trace(int tr) { return tr >= TR_H1P2 && tr <= TR_H1P3ROT; }
+__host__ __device__ constexpr int h1p_order(int tr) { return tr == TR_H1P2 || tr == TR_H1P2ROT ? 2 : 3; }
+__host__ __device__ constexpr bool h1p_rot(int tr) { return tr == TR_H1P2ROT || tr == TR_H1P3ROT; }
+
+// Hierarchical H1 basis of order P <= 3 on a triangle in barycentric coordinates l[3] (our own
+// choice of basis; the reference takes NGSolve's H1 element, whose shapes differ but span
+// the same space): local dof a
+//   a < 3               vertex:  l_a
+//   3 <= a < 3 + 3(P-1) edge k = (a - 3) / (P - 1) between local vertices i = k, j = k + 1
+//                       (mod 3), degree m + 2 with m = (a - 3) % (P - 1):
+//                       l_i l_j (l_j - l_i)^m, in the element's local orientation; the
+//                       global one (i the vertex of the lower global number) multiplies it
+//                       by the edge's orientation sign to the power m (passed by the caller)
+//   a = 9 (P = 3)       face:    l_0 l_1 l_2
+// Returns the value and, in d[3], its partial derivatives in l_0, l_1, l_2 (as if the three
+// were independent: the surface gradient is sum_i d_i grad l_i, and sum_i grad l_i = 0).
+template <class R>
+__host__ __device__ inline R h1p_shape(int P, int a, const R* l, R* d) {
+  d[0] = d[1] = d[2] = R(0);
+  if (a < 3) {
+    d[a] = R(1);
+    return l[a];
+  }
+  const int ne = 3 * (P - 1);
+  if (a < 3 + ne) {
+    const int k = (a - 3) / (P - 1), m = (a - 3) % (P - 1);
+    const int i = k, j = (k + 1) % 3;
+    if (m == 0) {
+      d[i] = l[j];
+      d[j] = l[i];
+      return l[i] * l[j];
+    }
+    const R s = l[j] - l[i];  // m == 1
+    d[i] = l[j] * s - l[i] * l[j];
+    d[j] = l[i] * s + l[i] * l[j];
+    return l[i] * l[j] * s;
+  }
+  d[0] = l[1] * l[2];
+  d[1] = l[0] * l[2];
+  d[2] = l[0] * l[1];
+  return l[0] * l[1] * l[2];
+}
 
 // Dubiner basis function a of order P on a triangle (Dubiner 1991; Karniadakis and Sherwin,
 // Spectral/hp Element Methods, ch. 3), in the form NGSolve's L2 triangle element uses it:

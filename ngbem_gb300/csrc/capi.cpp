@@ -72,7 +72,7 @@ int bem_mesh_destroy(bem_mesh_t mesh) {
 int bem_space_create(bem_mesh_t mesh, int kind, int dual_mapping, bem_space_t* out) {
   return guarded([&] {
     REQUIRE(mesh && out, "null argument");
-    REQUIRE(kind >= BEM_P0 && kind <= BEM_L2P3, "unknown space kind");
+    REQUIRE(kind >= BEM_P0 && kind <= BEM_H1P3, "unknown space kind");
     REQUIRE(!dual_mapping || kind == BEM_P0, "dual mapping is defined for P0 only");
     auto s = std::make_unique<bem_space_s>();
     s->mesh = mesh->m;
@@ -85,7 +85,7 @@ int bem_space_create_on(bem_mesh_t mesh, int kind, int dual_mapping, const unsig
                         bem_space_t* out) {
   return guarded([&] {
     REQUIRE(mesh && out, "null argument");
-    REQUIRE(kind >= BEM_P0 && kind <= BEM_L2P3, "unknown space kind");
+    REQUIRE(kind >= BEM_P0 && kind <= BEM_H1P3, "unknown space kind");
     REQUIRE(!dual_mapping || kind == BEM_P0, "dual mapping is defined for P0 only");
     auto s = std::make_unique<bem_space_s>();
     s->mesh = mesh->m;
@@ -108,9 +108,22 @@ int bem_space_element_dofs(bem_space_t space, int* dofs, int* signs) {
     const int nt = s.mesh->nt;
     for (int e = 0; e < nt; ++e)
       for (int k = 0; k < 3; ++k) {
-        dofs[3 * e + k] = ((s.nd == 1 || s.kind >= BEM_L2P1) && k > 0) ? -1 : s.dofs[3 * e + k];
+        const bool l2p = s.kind >= BEM_L2P1 && s.kind <= BEM_L2P3;
+        dofs[3 * e + k] = ((s.nd == 1 || l2p) && k > 0) ? -1 : s.dofs[3 * e + k];
         if (signs) signs[3 * e + k] = s.sign[3 * e + k];
       }
+  });
+}
+
+int bem_space_dof_table(bem_space_t space, int* nd, int* dofs) {
+  return guarded([&] {
+    REQUIRE(space && nd, "null argument");
+    const SpaceH& s = *space->s;
+    *nd = s.nd;
+    if (!dofs) return;
+    const int nt = s.mesh->nt;
+    for (int e = 0; e < nt; ++e)
+      for (int a = 0; a < s.nd; ++a) dofs[(size_t)s.nd * e + a] = s.on(e) ? s.dof(e, a) : -1;
   });
 }
 

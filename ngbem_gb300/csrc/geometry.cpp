@@ -253,6 +253,42 @@ void SpaceH::build(MeshH* m, int kind_, int dual_, const unsigned char* mask) {
       std::sort(f, f + 3, [&](int x, int y) { return m->T[3 * e + x] < m->T[3 * e + y]; });
       for (int k = 0; k < 3; ++k) sign[3 * e + k] = f[k];
     }
+  } else if (kind == BEM_H1P2 || kind == BEM_H1P3) {
+    // H1 of order p: vertex dofs (vertices ascending), p - 1 per edge (edges by first
+    // appearance on the region), (p - 1)(p - 2) / 2 per element; sign: the orientation of
+    // local edge k (+1 when its first vertex has the lower global number).  global_dof: the
+    // dof of the same function in the space on the whole mesh (edges in mesh order).
+    const int p = kind == BEM_H1P2 ? 2 : 3, pe = p - 1, pf = (p - 1) * (p - 2) / 2;
+    nd = (p + 1) * (p + 2) / 2;
+    xdof.assign((size_t)nd * m->nt, -1);
+    std::vector<int> vmap(m->nv, -1), emap(m->ne, -1);
+    for (int e : elems)
+      for (int k = 0; k < 3; ++k) vmap[m->T[3 * e + k]] = 0;
+    for (int v = 0; v < m->nv; ++v)
+      if (vmap[v] == 0) {
+        vmap[v] = (int)global_dof.size();
+        global_dof.push_back(v);
+      }
+    for (int e : elems)
+      for (int k = 0; k < 3; ++k) {
+        const int g = m->TE[3 * e + k];
+        if (emap[g] < 0) {
+          emap[g] = (int)global_dof.size();
+          for (int j = 0; j < pe; ++j) global_dof.push_back(m->nv + g * pe + j);
+        }
+      }
+    for (int e : elems) {
+      const int f0 = (int)global_dof.size();
+      for (int j = 0; j < pf; ++j) global_dof.push_back(m->nv + m->ne * pe + e * pf + j);
+      int* xd = &xdof[(size_t)nd * e];
+      for (int k = 0; k < 3; ++k) {
+        dofs[3 * e + k] = vmap[m->T[3 * e + k]];
+        sign[3 * e + k] = m->T[3 * e + k] < m->T[3 * e + (k + 1) % 3] ? 1 : -1;
+        xd[k] = dofs[3 * e + k];
+        for (int j = 0; j < pe; ++j) xd[3 + k * pe + j] = emap[m->TE[3 * e + k]] + j;
+      }
+      for (int j = 0; j < pf; ++j) xd[3 + 3 * pe + j] = f0 + j;
+    }
   } else {
     throw Error(BEM_ERR_ARG, "unknown space kind");
   }
@@ -276,6 +312,14 @@ void SpaceH::ensure_device() {
   for (int e = 0; e < mesh->nt; ++e) {
     d4[e] = make_int4(dofs[3 * e], dofs[3 * e + 1], dofs[3 * e + 2], 0);
     s4[e] = make_int4(sign[3 * e], sign[3 * e + 1], sign[3 * e + 2], 0);
+    if ((kind == BEM_H1P2 || kind == BEM_H1P3) && on(e)) {
+      // H1 of order p: w = the first face dof; the signs carry (first edge dof + 1)
+      const int pe = nd == 6 ? 1 : 2;
+      const int* xd = &xdof[(size_t)nd * e];
+      d4[e].w = nd > 3 + 3 * pe ? xd[3 + 3 * pe] : 0;
+      s4[e] = make_int4(sign[3 * e] * (xd[3] + 1), sign[3 * e + 1] * (xd[3 + pe] + 1),
+                        sign[3 * e + 2] * (xd[3 + 2 * pe] + 1), 0);
+    }
   }
   d_dofs.upload(d4);
   d_sign.upload(s4);
@@ -285,6 +329,12 @@ void SpaceH::ensure_device() {
 int trace_kind(int space_kind, int ev) {
   if (space_kind == BEM_P0) return ev == BEM_EV_ID ? TR_P0 : -1;
   if (space_kind >= BEM_L2P1 && space_kind <= BEM_L2P3) return ev == BEM_EV_ID ? TR_L2P1 + space_kind - BEM_L2P1 : -1;
+  if (space_kind == BEM_H1P2 || space_kind == BEM_H1P3) {
+    const int q = space_kind - BEM_H1P2;
+    if (ev == BEM_EV_ID) return TR_H1P2 + q;
+    if (ev == BEM_EV_ROT) return TR_H1P2ROT + q;
+    return -1;
+  }
   if (space_kind == BEM_P1) {
     if (ev == BEM_EV_ID) return TR_P1;
     if (ev == BEM_EV_ROT) return TR_ROT;

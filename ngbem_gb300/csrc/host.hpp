@@ -110,15 +110,21 @@ struct SpaceH {
   std::vector<int> dofs;      // 3*nt (P0: the element's dof three times; -1 off the region)
   std::vector<int> sign;      // 3*nt
   std::vector<int> e4d_ptr, e4d;  // dof -> elements (CSR, element order)
-  std::vector<int> global_dof;    // dof -> element (P0), vertex (P1) or mesh edge (RT0, HCURL)
+  std::vector<int> global_dof;    // dof -> element (P0), vertex (P1) or mesh edge (RT0, HCURL);
+                                  // H1 of order p: the dof of the space on the whole mesh
+  std::vector<int> xdof;          // H1 of order p >= 2: nd dofs per element (local order)
   std::vector<int> elems;         // the elements the space lives on, ascending
   DevBuf d_dofs, d_sign;
   // mask: nt flags of the elements the space lives on (null: all of them)
   void build(MeshH* m, int kind_, int dual_, const unsigned char* mask = nullptr);
   bool on(int e) const { return dofs[3 * e] >= 0; }
   const int* el_dofs(int e) const { return &dofs[3 * e]; }  // kinds with at most 3 dofs per element
-  // dof of local dof a of element e (SurfaceL2 of order >= 1: consecutive from dofs[3 e])
-  int dof(int e, int a) const { return kind >= BEM_L2P1 ? dofs[3 * e] + a : dofs[3 * e + a]; }
+  // dof of local dof a of element e (SurfaceL2 of order >= 1: consecutive from dofs[3 e]; H1
+  // of order >= 2: the element's row of xdof)
+  int dof(int e, int a) const {
+    if (kind >= BEM_H1P2) return xdof[(size_t)nd * e + a];
+    return kind >= BEM_L2P1 ? dofs[3 * e] + a : dofs[3 * e + a];
+  }
   void ensure_device();
   // cluster tree with element patches for a leaf size, built on first use and shared by the
   // operators on this space (a tree depends only on the space and the leaf size)

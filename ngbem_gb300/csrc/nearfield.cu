@@ -28,6 +28,7 @@ bool nf_combo_supported(int kid, int trt, int tet) {
 #define X(K, A, B) if (kid == K && trt == A && tet == B) return true;
   BEM_NF_COMBOS(X)
   BEM_L2P_COMBOS(X)
+  BEM_H1P_COMBOS(X)
 #undef X
   return false;
 }
@@ -39,6 +40,11 @@ void launch_nf_regular(int kid, int prec, int trt, int tet, const NFArgs& a, cud
     if (trt == TR_L2P1) launch_nf_regular_l2p1(kid, prec, a, s);
     if (trt == TR_L2P2) launch_nf_regular_l2p2(kid, prec, a, s);
     if (trt == TR_L2P3) launch_nf_regular_l2p3(kid, prec, a, s);
+    return;
+  }
+  if (h1p_trace(trt)) {
+    if (h1p_order(trt) == 2) launch_nf_regular_h1p2(kid, prec, trt, tet, a, s);
+    else launch_nf_regular_h1p3(kid, prec, trt, tet, a, s);
     return;
   }
 #define X(K, A, B)                                                                    \
@@ -57,6 +63,11 @@ void launch_nf_singular(int kid, int prec, int trt, int tet, const NFArgs& a, cu
     if (trt == TR_L2P1) launch_nf_singular_l2p1(kid, prec, a, s);
     if (trt == TR_L2P2) launch_nf_singular_l2p2(kid, prec, a, s);
     if (trt == TR_L2P3) launch_nf_singular_l2p3(kid, prec, a, s);
+    return;
+  }
+  if (h1p_trace(trt)) {
+    if (h1p_order(trt) == 2) launch_nf_singular_h1p2(kid, prec, trt, tet, a, s);
+    else launch_nf_singular_h1p3(kid, prec, trt, tet, a, s);
     return;
   }
 #define X(K, A, B)                                                          \

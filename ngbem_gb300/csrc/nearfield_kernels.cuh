@@ -61,13 +61,13 @@ __global__ void __launch_bounds__(128) nf_regular_kernel(NFArgs a) {
   for (int c = 0; c < 3; ++c) { nx[c] = Ei.n[c]; ny[c] = Ej.n[c]; }
   P roti[3][3], rotj[3][3], oi[3][3], oj[3][3];
   const P invi = Ei.invdetJ, invj = Ej.invdetJ;
-  if (TET == TR_ROT || TET == TR_HELM) {
+  if (needs_rot(TET)) {
 #pragma unroll
     for (int r = 0; r < 3; ++r)
 #pragma unroll
       for (int c = 0; c < 3; ++c) roti[r][c] = Ei.rot[r][c];
   }
-  if (TRT == TR_ROT || TRT == TR_HELM) {
+  if (needs_rot(TRT)) {
 #pragma unroll
     for (int r = 0; r < 3; ++r)
 #pragma unroll
@@ -148,15 +148,16 @@ __global__ void __launch_bounds__(128) nf_regular_kernel(NFArgs a) {
   }
   // scatter into the dense block (src/ngbem.cpp:733-736)
   const int4 dni = a.test.dofs[ei], dnj = a.trial.dofs[ej];
+  const int4 xi_ = dof_aux<TET>(a.test.sign, ei), xj_ = dof_aux<TRT>(a.trial.sign, ej);
   int rows[NDI], cols[NDJ];
 #pragma unroll
   for (int r = 0; r < NDI; ++r) {
-    int pos = a.test.pinv[elem_dof<TET>(dni, r)] - d.r0;
+    int pos = a.test.pinv[elem_dof<TET>(dni, xi_, r)] - d.r0;
     rows[r] = (pos >= 0 && pos < d.m) ? pos : -1;
   }
 #pragma unroll
   for (int c = 0; c < NDJ; ++c) {
-    int pos = a.trial.pinv[elem_dof<TRT>(dnj, c)] - d.c0;
+    int pos = a.trial.pinv[elem_dof<TRT>(dnj, xj_, c)] - d.c0;
     cols[c] = (pos >= 0 && pos < d.n) ? pos : -1;
   }
   V* pool = (V*)a.pool + d.off;
@@ -326,14 +327,15 @@ __global__ void __launch_bounds__(256) nf_singular_kernel(NFArgs a) {
       for (int c = 0; c < NDJ; ++c) acc[r][c] = warp_sum(acc[r][c]);
     if (lane == 0) {
       const int4 dni = a.test.dofs[s.ei], dnj = a.trial.dofs[s.ej];
+      const int4 xi_ = dof_aux<TET>(a.test.sign, s.ei), xj_ = dof_aux<TRT>(a.trial.sign, s.ej);
       VS* pool = (VS*)a.pool + d.off;
 #pragma unroll
       for (int r = 0; r < NDI; ++r) {
-        int row = a.test.pinv[elem_dof<TET>(dni, r)] - d.r0;
+        int row = a.test.pinv[elem_dof<TET>(dni, xi_, r)] - d.r0;
         if (row < 0 || row >= d.m) continue;
 #pragma unroll
         for (int c = 0; c < NDJ; ++c) {
-          int col = a.trial.pinv[elem_dof<TRT>(dnj, c)] - d.c0;
+          int col = a.trial.pinv[elem_dof<TRT>(dnj, xj_, c)] - d.c0;
           if (col < 0 || col >= d.n) continue;
           VS v;
           cvt(v, acc[r][c]);
@@ -352,6 +354,25 @@ __global__ void __launch_bounds__(256) nf_singular_kernel(NFArgs a) {
 #define BEM_L2P_KERNELS(X, T) \
   X(K_LAPLACE_SL, T, T) X(K_LAPLACE_DL, T, T) X(K_HELMHOLTZ_SL, T, T) X(K_HELMHOLTZ_DL, T, T) X(K_HELMHOLTZ_CF, T, T)
 #define BEM_L2P_COMBOS(X) BEM_L2P_KERNELS(X, TR_L2P1) BEM_L2P_KERNELS(X, TR_L2P2) BEM_L2P_KERNELS(X, TR_L2P3)
+// H1 of order 2, 3 (BEM_H1P_COMBOS, kernels.h): each order in translation units of its own,
+// nearfield_h1p*.cu
+void launch_nf_regular_h1p2(int kid, int prec, int trt, int tet, const NFArgs& a, cudaStream_t s);
+void launch_nf_singular_h1p2(int kid, int prec, int trt, int tet, const NFArgs& a, cudaStream_t s);
+void launch_nf_regular_h1p3(int kid, int prec, int trt, int tet, const NFArgs& a, cudaStream_t s);
+void launch_nf_singular_h1p3(int kid, int prec, int trt, int tet, const NFArgs& a, cudaStream_t s);
+// bodies of those launchers: one (kernel, trial trace, test trace) combination
+#define BEM_NF_REGULAR_X3(K, A, B)                                                     \
+  if (kid == K && trt == A && tet == B) {                                              \
+    if (prec == 0) nf_regular_kernel<K, double, A, B><<<a.ntiles, 128, 0, s>>>(a);    \
+    else nf_regular_kernel<K, float, A, B><<<a.ntiles, 128, 0, s>>>(a);               \
+    return;                                                                            \
+  }
+#define BEM_NF_SINGULAR_X3(K, A, B)                                                    \
+  if (kid == K && trt == A && tet == B) {                                              \
+    if (prec == 0) run_singular<K, double, A, B>(a, s);                                \
+    else run_singular<K, float, A, B>(a, s);                                           \
+    return;                                                                            \
+  }
 void launch_nf_regular_l2p1(int kid, int prec, const NFArgs& a, cudaStream_t s);
 void launch_nf_singular_l2p1(int kid, int prec, const NFArgs& a, cudaStream_t s);
 void launch_nf_regular_l2p2(int kid, int prec, const NFArgs& a, cudaStream_t s);

@@ -43,13 +43,13 @@ __global__ void pot_sources_kernel(PotArgs a) {
     const double nrm[3] = {Ee.n[0], Ee.n[1], Ee.n[2]};
     int sg[SignSlots<TRT>::N];
     elem_signs<TRT>(a.trial.sign, e, sg);
-    const int4 dn = a.trial.dofs[e];
+    const int4 dn = a.trial.dofs[e], dx = dof_aux<TRT>(a.trial.sign, e);
     V val[DIM];
 #pragma unroll
     for (int c = 0; c < DIM; ++c) val[c] = vzero<V>();
 #pragma unroll
     for (int x = 0; x < ND; ++x) {
-      const V dv = dens[elem_dof<TRT>(dn, x)];
+      const V dv = dens[elem_dof<TRT>(dn, dx, x)];
 #pragma unroll
       for (int c = 0; c < DIM; ++c)
         val[c] += dv * trace_val<TRT, double>(x, c, RQ[2 * q], RQ[2 * q + 1], xp, Ee.invdetJ, rot, sg[x],
@@ -125,7 +125,10 @@ __global__ void __launch_bounds__(POT_THREADS) pot_eval_kernel(PotArgs a) {
   X(K_LAPLACE_SL, TR_L2P1, double) X(K_LAPLACE_SL, TR_L2P2, double) X(K_LAPLACE_SL, TR_L2P3, double) \
   X(K_LAPLACE_DL, TR_L2P1, double) X(K_LAPLACE_DL, TR_L2P2, double) X(K_LAPLACE_DL, TR_L2P3, double) \
   X(K_HELMHOLTZ_SL, TR_L2P1, cpx<double>) X(K_HELMHOLTZ_SL, TR_L2P2, cpx<double>)               \
-  X(K_HELMHOLTZ_SL, TR_L2P3, cpx<double>)
+  X(K_HELMHOLTZ_SL, TR_L2P3, cpx<double>)                                                       \
+  X(K_LAPLACE_SL, TR_H1P2, double) X(K_LAPLACE_SL, TR_H1P3, double) X(K_LAPLACE_DL, TR_H1P2, double) \
+  X(K_LAPLACE_DL, TR_H1P3, double) X(K_HELMHOLTZ_SL, TR_H1P2, cpx<double>)                          \
+  X(K_HELMHOLTZ_SL, TR_H1P3, cpx<double>)
 
 int potential_dim(int kid, int trt) {
 #define X(K, T, V) \

@@ -12,7 +12,7 @@ import numpy as np
 from .meshes import Mesh
 
 __all__ = ["triangle_rule", "load_vector", "p1_load_vector", "p0_load_vector", "plane_wave_bm_source",
-           "random_directions", "dubiner"]
+           "random_directions", "dubiner", "h1p_shapes"]
 
 
 def triangle_rule(order: int):
@@ -88,6 +88,24 @@ def dubiner(p: int, lam: np.ndarray, f0: np.ndarray, f1: np.ndarray) -> np.ndarr
     return np.stack(out, axis=-1)
 
 
+def h1p_shapes(p: int, lam: np.ndarray, signs: np.ndarray) -> np.ndarray:
+    """The H1 basis of order p (2 or 3) at barycentric points lam (nq, 3) of every triangle
+    whose local edges (0,1), (1,2), (2,0) have the orientations signs (nt, 3) (+1: the edge's
+    first vertex has the lower global number): (nt, nq, (p+1)(p+2)/2) values of the vertex hats
+    l_a, the edge bubbles l_i l_j (l_j - l_i)^m times the orientation to the power m, and the
+    face bubble l_0 l_1 l_2 (the library's basis and local order)."""
+    nt = signs.shape[0]
+    out = [np.broadcast_to(lam[:, a], (nt, lam.shape[0])) for a in range(3)]
+    for k in range(3):
+        i, j = k, (k + 1) % 3
+        q = lam[:, i] * lam[:, j]
+        for m in range(p - 1):
+            out.append(signs[:, k, None] ** m * (q * (lam[:, j] - lam[:, i]) ** m)[None, :])
+    if p == 3:
+        out.append(np.broadcast_to(lam[:, 0] * lam[:, 1] * lam[:, 2], (nt, lam.shape[0])))
+    return np.stack(out, axis=-1)
+
+
 def load_vector(space, f, order: int = 6) -> np.ndarray:
     """b_i = int f v_i over the space's triangles for the basis v_i of any trace space (the
     role of LinearForm(f * v.Trace() * ds).Assemble() on that space; a space on a region
@@ -111,6 +129,12 @@ def load_vector(space, f, order: int = 6) -> np.ndarray:
     elif space.kind == "P1":
         for a in range(3):
             np.add.at(out, dofs[on, a], (np.einsum("q,tqm->tm", w * lam[:, a], fv) * detj[:, None])[on])
+    elif space.kind.startswith("H1P"):
+        p = int(space.kind[3:])
+        phi = h1p_shapes(p, lam, signs)  # (nt, nq, nd)
+        contrib = np.einsum("q,tqa,tqm->tam", w, phi, fv) * detj[:, None, None]
+        table = space.dof_table()
+        np.add.at(out, table[on].ravel(), contrib[on].reshape(-1, contrib.shape[-1]))
     elif space.kind.startswith("L2P"):
         p = int(space.kind[3:])
         phi = dubiner(p, lam, signs[:, 0], signs[:, 1])  # (nt, nq, nd)

@@ -287,6 +287,20 @@ struct Space {
         std::sort(f, f + 3, [&](int x, int y) { return m.T[3 * e + x] < m.T[3 * e + y]; });
         for (int k = 0; k < 3; ++k) sign[3 * e + k] = f[k];
       }
+    } else if (kind == ORC_H1P2 || kind == ORC_H1P3) {
+      // H1 of order p: vertex dofs = vertex ids, then p - 1 dofs per edge, then the face dofs
+      const int pp = kind == ORC_H1P2 ? 2 : 3, pe = pp - 1, pf = (pp - 1) * (pp - 2) / 2;
+      nd = (pp + 1) * (pp + 2) / 2;
+      ndof = m.nv + m.ne * pe + m.nt * pf;
+      dofs.resize((size_t)m.nt * nd);
+      for (int e = 0; e < m.nt; ++e) {
+        int* d = &dofs[(size_t)e * nd];
+        for (int k = 0; k < 3; ++k) {
+          d[k] = m.T[3 * e + k];
+          for (int j = 0; j < pe; ++j) d[3 + k * pe + j] = m.nv + m.TE[3 * e + k] * pe + j;
+        }
+        for (int j = 0; j < pf; ++j) d[3 + 3 * pe + j] = m.nv + m.ne * pe + e * pf + j;
+      }
     } else {
       nd = 3; ndof = m.ne; dofs = m.TE; sign.resize(3 * m.nt);
       for (int e = 0; e < m.nt; ++e)
@@ -329,6 +343,55 @@ static void eval_trace(const Mesh& m, const Space& sp, int ev, int e, double xi,
   if (sp.kind >= ORC_L2P1 && sp.kind <= ORC_L2P3) {
     for (int a = 0; a < sp.nd; ++a)
       S[a][0] = dubiner(sp.kind - ORC_L2P1 + 1, a, xi, eta, sp.sign[3 * e], sp.sign[3 * e + 1]);
+    return;
+  }
+  if (sp.kind == ORC_H1P2 || sp.kind == ORC_H1P3) {
+    // values, and surface curls n x sum_i (dphi / dl_i) grad_Gamma l_i (the surface gradients
+    // of the barycentrics through the metric of the element map)
+    const int pp = sp.kind == ORC_H1P2 ? 2 : 3, pe = pp - 1;
+    const double lam[3] = {xi, eta, 1.0 - xi - eta};
+    double gl[3][3];
+    {
+      double g00 = g.J0[0] * g.J0[0] + g.J0[1] * g.J0[1] + g.J0[2] * g.J0[2];
+      double g01 = g.J0[0] * g.J1[0] + g.J0[1] * g.J1[1] + g.J0[2] * g.J1[2];
+      double g11 = g.J1[0] * g.J1[0] + g.J1[1] * g.J1[1] + g.J1[2] * g.J1[2];
+      double det = g00 * g11 - g01 * g01;
+      const double gh[3][2] = {{1.0, 0.0}, {0.0, 1.0}, {-1.0, -1.0}};
+      for (int a = 0; a < 3; ++a) {
+        double c0 = (g11 * gh[a][0] - g01 * gh[a][1]) / det;
+        double c1 = (-g01 * gh[a][0] + g00 * gh[a][1]) / det;
+        for (int c = 0; c < 3; ++c) gl[a][c] = g.J0[c] * c0 + g.J1[c] * c1;
+      }
+    }
+    for (int a = 0; a < sp.nd; ++a) {
+      double phi = 0.0, dl[3] = {0.0, 0.0, 0.0};
+      if (a < 3) {
+        phi = lam[a];
+        dl[a] = 1.0;
+      } else if (a < 3 + 3 * pe) {
+        const int k = (a - 3) / pe, mm = (a - 3) % pe;
+        int lo = k, hi = (k + 1) % 3;  // the edge's local vertices by global number
+        if (m.T[3 * e + lo] > m.T[3 * e + hi]) std::swap(lo, hi);
+        const double s = lam[hi] - lam[lo], q = lam[lo] * lam[hi];
+        const double sm = mm == 0 ? 1.0 : s;
+        phi = q * sm;
+        dl[lo] = lam[hi] * sm - (mm == 0 ? 0.0 : q);
+        dl[hi] = lam[lo] * sm + (mm == 0 ? 0.0 : q);
+      } else {
+        phi = lam[0] * lam[1] * lam[2];
+        dl[0] = lam[1] * lam[2];
+        dl[1] = lam[0] * lam[2];
+        dl[2] = lam[0] * lam[1];
+      }
+      if (ev == ORC_EV_ID) {
+        S[a][0] = phi;
+        continue;
+      }
+      double grad[3], rot[3];
+      for (int c = 0; c < 3; ++c) grad[c] = dl[0] * gl[0][c] + dl[1] * gl[1][c] + dl[2] * gl[2][c];
+      cross3(g.n, grad, rot);
+      for (int c = 0; c < 3; ++c) S[a][c] = rot[c];
+    }
     return;
   }
   if (sp.kind == ORC_P1) {
@@ -1371,6 +1434,18 @@ int orc_potential(int kernel, double kappa, int nv, const double* xyz, int nt, c
   else
     potential_t<double>(kernel, kappa, m, sp, trial_eval, intorder, density, npts, pts, normals, out);
   return 0;
+}
+
+int orc_eval_trace(int nv, const double* xyz, int nt, const int* tri, int kind, int ev, int e, double xi,
+                   double eta, double* out, int* dofs) {
+  Mesh m; m.build(nv, xyz, nt, tri);
+  Space sp; sp.build(m, kind, false);
+  double S[ORC_MAXND][4] = {{0.0}};
+  eval_trace(m, sp, ev, e, xi, eta, S);
+  for (int a = 0; a < ORC_MAXND; ++a)
+    for (int c = 0; c < 4; ++c) out[4 * a + c] = a < sp.nd ? S[a][c] : 0.0;
+  for (int a = 0; a < sp.nd; ++a) dofs[a] = sp.el_dofs(e)[a];
+  return sp.nd;
 }
 
 int orc_mass_matrix(int nv, const double* xyz, int nt, const int* tri, int trial_kind, int test_kind,

@@ -17,7 +17,7 @@ _LIB = None
 KERNELS = {"laplace_sl": 0, "laplace_dl": 1, "laplace_hs": 2, "helmholtz_sl": 3,
            "helmholtz_dl": 4, "helmholtz_hs": 5, "helmholtz_cf": 6, "maxwell_sl": 7,
            "helmholtz_sl_dkappa": 8, "maxwell_dl": 9}
-KINDS = {"P0": 0, "P1": 1, "RT0": 2, "HCURL": 3, "L2P1": 4, "L2P2": 5, "L2P3": 6}
+KINDS = {"P0": 0, "P1": 1, "RT0": 2, "HCURL": 3, "L2P1": 4, "L2P2": 5, "L2P3": 6, "H1P2": 7, "H1P3": 8}
 EVALS = {"id": 0, "rot": 1, "helm": 2, "maxwell": 3, "rotatedtrace": 4, "maxwellcurl": 5}
 
 
@@ -42,6 +42,8 @@ def lib():
         dp, ip, lp = C.POINTER(C.c_double), C.POINTER(C.c_int), C.POINTER(C.c_long)
         L.orc_mesh_edges.argtypes = [C.c_int, C.c_int, ip, ip, ip]
         L.orc_trig_rule.argtypes = [C.c_int, dp, dp, dp]
+        L.orc_eval_trace.argtypes = [C.c_int, dp, C.c_int, ip, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double,
+                                     dp, ip]
         L.orc_ss_rule.argtypes = [C.c_int, C.c_int, dp, dp, dp, dp, dp]
         L.orc_cluster_tree.argtypes = [C.c_int, dp, C.c_int, ip, C.c_int, C.c_int, ip, C.c_int, lp, dp]
         L.orc_operator_create.restype = C.c_void_p
@@ -99,6 +101,17 @@ def ss_rule(cls, order):
     return [x[:k] for x in a]
 
 
+def eval_trace(mesh, kind, ev, e, xi, eta):
+    """(values (nd, 4), dofs (nd,)): the trace values of element e's local dofs at (xi, eta)."""
+    X = np.ascontiguousarray(mesh.vertices, dtype=np.float64)
+    T = np.ascontiguousarray(mesh.triangles, dtype=np.int32)
+    out = np.zeros(40)
+    dofs = np.zeros(10, dtype=np.int32)
+    nd = lib().orc_eval_trace(mesh.nv, _dp(X), mesh.nt, _ip(T), KINDS[kind], EVALS[ev], int(e), float(xi),
+                              float(eta), _dp(out), _ip(dofs))
+    return out.reshape(10, 4)[:nd], dofs[:nd]
+
+
 def ndof(mesh, kind):
     if kind == "P0":
         return mesh.nt
@@ -107,7 +120,11 @@ def ndof(mesh, kind):
         return mesh.nt * (p + 1) * (p + 2) // 2
     if kind == "P1":
         return mesh.nv
-    return len(mesh_edges(mesh)[0])
+    ne = len(mesh_edges(mesh)[0])
+    if kind.startswith("H1P"):
+        p = int(kind[3:])
+        return mesh.nv + ne * (p - 1) + mesh.nt * (p - 1) * (p - 2) // 2
+    return ne
 
 
 def cluster_tree(mesh, kind, leafsize):
