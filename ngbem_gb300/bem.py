@@ -626,7 +626,9 @@ class IntegralOperator:
     def GetPotential(self, gf):
         """Potential of the trial-space density gf (reference GetPotential, src/ngbem.cpp:1166-1172):
         a callable ``pot(points, normals=None)`` giving the field at points (n, 3) on the GPU, shape
-        (n,) for scalar trial traces, else (n, dim)."""
+        (n,) for scalar trial traces, else (n, dim).  As the reference's PotentialCF, the sum leaves
+        out the kernel terms' factors; for the Maxwell double layer (six cross-product terms with
+        factors +-1) it is therefore the reference's field, not the signed double-layer field."""
         return Potential(self, gf)
 
     def _test_hmatrix(self):

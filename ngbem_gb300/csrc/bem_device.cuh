@@ -325,8 +325,10 @@ template <> struct TraceInfo<TR_H1P2> { static constexpr int ND = 6, DIM = 1; };
 template <> struct TraceInfo<TR_H1P3> { static constexpr int ND = 10, DIM = 1; };
 template <> struct TraceInfo<TR_H1P2ROT> { static constexpr int ND = 6, DIM = 3; };
 template <> struct TraceInfo<TR_H1P3ROT> { static constexpr int ND = 10, DIM = 3; };
+template <> struct TraceInfo<TR_H1P2HELM> { static constexpr int ND = 6, DIM = 4; };
+template <> struct TraceInfo<TR_H1P3HELM> { static constexpr int ND = 10, DIM = 4; };
 // traces that read the element's n x grad(lambda_a) table
-__host__ __device__ constexpr bool needs_rot(int tr) { return tr == TR_ROT || tr == TR_HELM || h1p_rot(tr); }
+__host__ __device__ constexpr bool needs_rot(int tr) { return tr == TR_ROT || tr == TR_HELM || h1p_rot(tr); }  // incl. HELM
 // sign slots a kernel keeps per element (at least the three edge signs)
 template <int TR> struct SignSlots { static constexpr int N = TraceInfo<TR>::ND > 3 ? TraceInfo<TR>::ND : 3; };
 
@@ -395,7 +397,7 @@ __device__ __forceinline__ R trace_val(int a, int c, R xi, R eta, const R (*xp)[
     const R l[3] = {xi, eta, R(1) - xi - eta};
     R d[3];
     const R v = h1p_shape<R>(h1p_order(TR), a, l, d);
-    if (!h1p_rot(TR)) return R(sgn) * v;
+    if (!h1p_rot(TR) || c == 3) return R(sgn) * v;
     return R(sgn) * (d[0] * rot[0][c] + d[1] * rot[1][c] + d[2] * rot[2][c]);
   }
   if (TR == TR_ROT) return rot[a][c];

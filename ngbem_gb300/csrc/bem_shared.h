@@ -20,19 +20,24 @@ enum KernelId {
 // TR_L2P1..3: SurfaceL2 of order 1..3 (the identity trace of the Dubiner basis)
 // TR_H1P2, TR_H1P3: H1 of order 2, 3 (identity trace); TR_H1P2ROT, TR_H1P3ROT: their surface
 // curl n x grad_Gamma phi (DiffOpBoundaryRot, src/diffops.hpp:12-60, for the hierarchical basis
-// h1p_shape below)
+// h1p_shape below); TR_H1P2HELM, TR_H1P3HELM: [n x grad_Gamma phi; phi] (DiffOpHelmholtz)
 enum TraceKind { TR_P0 = 0, TR_P1 = 1, TR_ROT = 2, TR_HELM = 3, TR_MAX = 4, TR_RT0ID = 5,
                  TR_NED = 6, TR_NEDROT = 7, TR_NEDMAX = 8, TR_L2P1 = 9, TR_L2P2 = 10, TR_L2P3 = 11,
-                 TR_H1P2 = 12, TR_H1P3 = 13, TR_H1P2ROT = 14, TR_H1P3ROT = 15 };
+                 TR_H1P2 = 12, TR_H1P3 = 13, TR_H1P2ROT = 14, TR_H1P3ROT = 15, TR_H1P2HELM = 16,
+                 TR_H1P3HELM = 17 };
 // traces of a discontinuous space of order >= 1: the element's dofs are consecutive
 // (first dof + local index) and its "signs" hold the order of its vertices by global number
 __host__ __device__ constexpr bool l2p_trace(int tr) { return tr >= TR_L2P1 && tr <= TR_L2P3; }
 __host__ __device__ constexpr int l2p_order(int tr) { return tr - TR_L2P1 + 1; }
 // traces of H1 of order 2, 3: vertex dofs, then the p - 1 dofs of each local edge (0,1),
 // (1,2), (2,0), then the (p - 1)(p - 2) / 2 face dofs
-__host__ __device__ constexpr bool h1p_trace(int tr) { return tr >= TR_H1P2 && tr <= TR_H1P3ROT; }
-__host__ __device__ constexpr int h1p_order(int tr) { return tr == TR_H1P2 || tr == TR_H1P2ROT ? 2 : 3; }
-__host__ __device__ constexpr bool h1p_rot(int tr) { return tr == TR_H1P2ROT || tr == TR_H1P3ROT; }
+__host__ __device__ constexpr bool h1p_trace(int tr) { return tr >= TR_H1P2 && tr <= TR_H1P3HELM; }
+__host__ __device__ constexpr int h1p_order(int tr) {
+  return tr == TR_H1P2 || tr == TR_H1P2ROT || tr == TR_H1P2HELM ? 2 : 3;
+}
+// the traces with the surface curl in components 0..2 (and, HELM, the value in 3)
+__host__ __device__ constexpr bool h1p_rot(int tr) { return tr >= TR_H1P2ROT && tr <= TR_H1P3HELM; }
+__host__ __device__ constexpr bool h1p_helm(int tr) { return tr == TR_H1P2HELM || tr == TR_H1P3HELM; }
 
 // Hierarchical H1 basis of order P <= 3 on a triangle in barycentric coordinates l[3] (our own
 // choice of basis; the reference takes NGSolve's H1 element, whose shapes differ but span

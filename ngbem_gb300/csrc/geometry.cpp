@@ -333,6 +333,7 @@ int trace_kind(int space_kind, int ev) {
     const int q = space_kind - BEM_H1P2;
     if (ev == BEM_EV_ID) return TR_H1P2 + q;
     if (ev == BEM_EV_ROT) return TR_H1P2ROT + q;
+    if (ev == BEM_EV_HELM) return TR_H1P2HELM + q;
     return -1;
   }
   if (space_kind == BEM_P1) {

@@ -265,14 +265,16 @@ int launch_potential(int kid, int trt, const PotArgs& a, cudaStream_t s);
 
 // (kernel, trial trace, test trace) combinations of H1 of order 2, 3 (near field, projection):
 // the Laplace single and double layer and the Helmholtz identity-trace operators on H1 x H1,
-// the Laplace double layer from H1 of order p to SurfaceL2 of order p - 1 and the Laplace
-// hypersingular operator on H1 (the pairings of the reference's Laplace test,
-// tests/test_Laplace.py:23-45)
-#define BEM_H1P_KERNELS(X, T, TROT, TL2)                                                     \
+// the Laplace double layer from H1 of order p to SurfaceL2 of order p - 1 (the pairings of the
+// reference's Laplace test, tests/test_Laplace.py:23-45) and the Laplace and Helmholtz
+// hypersingular operators on H1
+#define BEM_H1P_KERNELS(X, T, TROT, THELM, TL2)                                              \
   X(K_LAPLACE_SL, T, T) X(K_LAPLACE_DL, T, T) X(K_LAPLACE_DL, T, TL2) X(K_LAPLACE_HS, TROT, TROT) \
-  X(K_HELMHOLTZ_SL, T, T) X(K_HELMHOLTZ_DL, T, T) X(K_HELMHOLTZ_CF, T, T)
-#define BEM_H1P_COMBOS(X) \
-  BEM_H1P_KERNELS(X, TR_H1P2, TR_H1P2ROT, TR_L2P1) BEM_H1P_KERNELS(X, TR_H1P3, TR_H1P3ROT, TR_L2P2)
+  X(K_HELMHOLTZ_SL, T, T) X(K_HELMHOLTZ_DL, T, T) X(K_HELMHOLTZ_CF, T, T)                       \
+  X(K_HELMHOLTZ_HS, THELM, THELM)
+#define BEM_H1P_COMBOS(X)                                              \
+  BEM_H1P_KERNELS(X, TR_H1P2, TR_H1P2ROT, TR_H1P2HELM, TR_L2P1)         \
+  BEM_H1P_KERNELS(X, TR_H1P3, TR_H1P3ROT, TR_H1P3HELM, TR_L2P2)
 
 // ---- tensor-core products for several right-hand sides (tc_matvec.cu) ---------------------
 // Operand panels are in the canonical K-major, no-swizzle layout of tcgen05 (core matrices of

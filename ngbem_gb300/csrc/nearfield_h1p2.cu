@@ -6,11 +6,11 @@
 namespace bem {
 
 void launch_nf_regular_h1p2(int kid, int prec, int trt, int tet, const NFArgs& a, cudaStream_t s) {
-  BEM_H1P_KERNELS(BEM_NF_REGULAR_X3, TR_H1P2, TR_H1P2ROT, TR_L2P1)
+  BEM_H1P_KERNELS(BEM_NF_REGULAR_X3, TR_H1P2, TR_H1P2ROT, TR_H1P2HELM, TR_L2P1)
 }
 
 void launch_nf_singular_h1p2(int kid, int prec, int trt, int tet, const NFArgs& a, cudaStream_t s) {
-  BEM_H1P_KERNELS(BEM_NF_SINGULAR_X3, TR_H1P2, TR_H1P2ROT, TR_L2P1)
+  BEM_H1P_KERNELS(BEM_NF_SINGULAR_X3, TR_H1P2, TR_H1P2ROT, TR_H1P2HELM, TR_L2P1)
 }
 
 }  // namespace bem

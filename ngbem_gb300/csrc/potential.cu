@@ -109,10 +109,12 @@ __global__ void __launch_bounds__(POT_THREADS) pot_eval_kernel(PotArgs a) {
   }
 }
 
-// (kernel, trial trace) pairs of the operators: the scalar kernels with P0 / P1 (and
-// SurfaceL2 of order 1..3) identity traces, the hypersingular kernels with their curl traces, the Maxwell single layer with RT0
-// and in its curl form with HCurl (the double layer has none: the reference's PotentialCF
-// sums its cross-product terms without their signs)
+// (kernel, trial trace) pairs of the operators: the scalar kernels with P0 / P1 (SurfaceL2 of
+// order 1..3, H1 of order 2, 3) identity traces, the hypersingular kernels with their curl
+// traces, the Maxwell single layer with RT0 and in its curl form with HCurl, and the Maxwell
+// double layer with the rotated trace of HCurl.  The sum leaves out the kernel terms' factors,
+// as the reference's PotentialCF does (src/ngbem.cpp:1228-1232); for the double layer's six
+// cross-product terms (factors +-1) that is the reference's field, not the signed one.
 #define BEM_POT_COMBOS(X)                                                                        \
   X(K_LAPLACE_SL, TR_P0, double) X(K_LAPLACE_SL, TR_P1, double) X(K_LAPLACE_DL, TR_P0, double)  \
   X(K_LAPLACE_DL, TR_P1, double) X(K_LAPLACE_HS, TR_ROT, double)                                 \
@@ -128,7 +130,7 @@ __global__ void __launch_bounds__(POT_THREADS) pot_eval_kernel(PotArgs a) {
   X(K_HELMHOLTZ_SL, TR_L2P3, cpx<double>)                                                       \
   X(K_LAPLACE_SL, TR_H1P2, double) X(K_LAPLACE_SL, TR_H1P3, double) X(K_LAPLACE_DL, TR_H1P2, double) \
   X(K_LAPLACE_DL, TR_H1P3, double) X(K_HELMHOLTZ_SL, TR_H1P2, cpx<double>)                          \
-  X(K_HELMHOLTZ_SL, TR_H1P3, cpx<double>)
+  X(K_HELMHOLTZ_SL, TR_H1P3, cpx<double>) X(K_MAXWELL_DL, TR_NEDROT, cpx<double>)
 
 int potential_dim(int kid, int trt) {
 #define X(K, T, V) \

@@ -391,6 +391,7 @@ static void eval_trace(const Mesh& m, const Space& sp, int ev, int e, double xi,
       for (int c = 0; c < 3; ++c) grad[c] = dl[0] * gl[0][c] + dl[1] * gl[1][c] + dl[2] * gl[2][c];
       cross3(g.n, grad, rot);
       for (int c = 0; c < 3; ++c) S[a][c] = rot[c];
+      if (ev == ORC_EV_HELM) S[a][3] = phi;  // DiffOpHelmholtz: [n x grad phi; phi]
     }
     return;
   }

@@ -22,7 +22,7 @@ pytestmark = pytest.mark.gpu
 COMBOS = [("laplace_sl", 0.0, "H1", "H1", "id"), ("laplace_dl", 0.0, "H1", "H1", "id"),
           ("laplace_dl", 0.0, "H1", "L2", "id"), ("laplace_hs", 0.0, "H1", "H1", "rot"),
           ("helmholtz_sl", 3.0, "H1", "H1", "id"), ("helmholtz_dl", 3.0, "H1", "H1", "id"),
-          ("helmholtz_cf", 4.0, "H1", "H1", "id")]
+          ("helmholtz_cf", 4.0, "H1", "H1", "id"), ("helmholtz_hs", 3.0, "H1", "H1", "helm")]
 IDS = [f"{k}-{a}-{b}" for k, _, a, b, _ in COMBOS]
 
 

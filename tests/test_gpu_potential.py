@@ -24,6 +24,11 @@ CASES = [
     ("helmholtz_hs", "P1", "helm", 3.0),
     ("maxwell_sl", "RT0", "maxwell", 2.0),
     ("helmholtz_sl_dkappa", "P1", "id", 3.0),
+    # the curl single layer on HCurl, and the double layer (HCurl rotated trace; tested with the
+    # HCurl identity trace, as MaxwellDoubleLayerPotentialOperator pairs them), whose potential
+    # is the reference's sum of its six cross-product terms without their signs
+    ("maxwell_sl", "HCURL", "maxwellcurl", 2.0),
+    ("maxwell_dl", "HCURL", "rotatedtrace", 2.0, "id"),
 ]
 
 
@@ -39,10 +44,11 @@ def _points(seed):
 
 @pytest.mark.parametrize("case", CASES, ids=[c[0] + "-" + c[1] for c in CASES])
 def test_potential_against_oracle(oracle, case):
-    kernel, kind, ev, kappa = case
+    kernel, kind, ev, kappa = case[:4]
+    tev = case[4] if len(case) > 4 else ev
     m = icosphere(2)
     sp = nb.TraceSpace(m, kind, complex=kernel not in ("laplace_sl", "laplace_dl", "laplace_hs"))
-    op = bem.IntegralOperator(kernel, kappa, sp, sp, ev, ev, 3, 20, 2.0, 1e-8, "aca", False)
+    op = bem.IntegralOperator(kernel, kappa, sp, sp, ev, tev, 3, 20, 2.0, 1e-8, "aca", False)
     r = np.random.default_rng(7)
     dens = r.standard_normal(sp.ndof)
     if op.mat.is_complex:

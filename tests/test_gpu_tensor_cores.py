@@ -4,10 +4,10 @@
   known-answer product (exact small-integer GEMM).
 * The Helmholtz combined-field operator (kappa 8, FP32 storage, plain accuracy) applied to 32
   and to 5 right-hand sides through the tensor cores agrees with the compensated CUDA-core
-  products of the same operator to 1e-5, and with the FP64-stored operator to 2e-5.  The
-  operands are split-TF32 (about 2^-21 per product); the bound is set by the FP32 accumulation
-  in tensor memory over a whole block row (hundreds of accumulator updates, an error growing
-  like 2^-24 times their square root; 3.4e-6 measured on the ellipsoid at level 4).
+  products of the same operator to 1e-6, and with the FP64-stored operator to 1.5e-6.  The
+  operands are split-TF32 (about 2^-21 per product); tensor memory accumulates with rounding
+  toward zero, so no accumulator takes more than 2 TC_CHAIN MMAs before the epilogue adds it
+  into sums that round to nearest.
 * Switching the path off gives the CUDA-core products again; one right-hand side never takes it.
 """
 import numpy as np
