@@ -740,9 +740,11 @@ def run_bm(args):
     Cm.set_accuracy(True)
     t_comp = timed_apply(Cm, Xc, Y, 3)
     Ycomp = Y.clone()
-    # mixed, plain accuracy: the tensor-core products of the GMRES iterations (the timed step)
+    # mixed, plain accuracy: the tensor-core products of the GMRES iterations (the timed step),
+    # with the stage plan picked by the autotuner on this operator
     Cm.set_accuracy(False)
-    tc = Cm.tensor_cores()
+    tc_tune = Cm.autotune_tensor_cores(reps=5)
+    tc = dict(Cm.tensor_cores(), autotune=tc_tune)
 
     flush = torch.empty(512 * 2 ** 20 // 4, dtype=torch.float32, device=dev)
     sweep = torch.zeros(512 * 2 ** 20 // 4, dtype=torch.float32, device=dev) if args.l2_flush == "write+read" else None

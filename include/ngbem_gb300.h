@@ -302,8 +302,9 @@ int bem_operator_autotune(bem_operator_t op, int reps, int* piece, int* fused, d
  * applies HMatrix::MultAdd, src/hmat.cpp:647-655, one vector at a time).  For complex
  * operators with FP32 storage, plain accuracy (bem_operator_set_accuracy(op, 0)) and 2..32
  * right-hand sides, bem_operator_mult runs the low-rank products T = V2 X and Y += U2 T on the
- * tcgen05 tensor cores with split-TF32 operands (high + low parts, FP32 accumulation over a
- * block row; about 5e-6 relative), the dense blocks included.  The packed operand panels
+ * tcgen05 tensor cores with split-TF32 operands (high + low parts; FP32 accumulation in tensor
+ * memory over at most 8 MMAs per accumulator, summed with rounding to nearest; about 5e-7
+ * relative), the dense blocks included.  The packed operand panels
  * (about 3x the low-rank storage) are built on the first such call outside a stream capture,
  * or here.
  * enable = 1 (default) builds them now when the operator qualifies; 0 turns the path off and
@@ -313,6 +314,12 @@ int bem_operator_autotune(bem_operator_t op, int reps, int* piece, int* fused, d
 int bem_operator_set_tensor_cores(bem_operator_t op, int enable);
 int bem_operator_tensor_cores(bem_operator_t op, int* state, long long* bytes, int* items0, int* items1,
                               double* ms_build);
+/* Autotuner of the tensor-core stage plan (no counterpart in the reference): builds the panels
+ * if needed, times `reps` applications to 32 right-hand sides (zero vectors: the kernels do the
+ * same work for any values) with the pipeline ring cut into 2, 3 and 4 stages, and keeps the
+ * fastest.  nstages: the stages kept; ms: the time per application of 2, 3, 4 stages (3
+ * doubles; either may be NULL).  BEM_ERR_STATE if the operator has no tensor-core path. */
+int bem_operator_autotune_tc(bem_operator_t op, int reps, int* nstages, double* ms);
 
 /* An assembled H-matrix to a file and back (no counterpart in the reference, which reassembles
  * each session).  The file holds the partition, ranks, dense blocks and factors; loading needs

@@ -60,6 +60,7 @@ SIGNATURES = {
     "bem_space_global_dofs": ([_vp, _ip], C.c_int),
     "bem_space_element_dofs": ([_vp, _ip, _ip], C.c_int),
     "bem_space_dof_table": ([_vp, _ip, _ip], C.c_int),
+    "bem_operator_autotune_tc": ([_vp, C.c_int, _ip, _dp], C.c_int),
     "bem_space_ndof": ([_vp, _ip], C.c_int),
     "bem_space_destroy": ([_vp], C.c_int),
     "bem_cluster_tree": ([_vp, C.c_int, _ip, C.c_int, _ip, _lp, _dp], C.c_int),

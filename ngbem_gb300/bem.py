@@ -504,6 +504,14 @@ class HMatrix(_NativeMatrix):
                                             C.byref(ms)))
         return {"state": st.value, "bytes": nb_.value, "items": (i0.value, i1.value), "ms_build": ms.value}
 
+    def autotune_tensor_cores(self, reps: int = 5) -> dict:
+        """Tune the tensor-core stage plan (2, 3 or 4 pipeline stages) on this operator: the kept
+        stage count and the time per 32-right-hand-side application of each."""
+        n = C.c_int()
+        ms = (C.c_double * 3)()
+        check(lib.bem_operator_autotune_tc(self.h, int(reps), C.byref(n), ms))
+        return {"stages": n.value, "ms": {2: ms[0], 3: ms[1], 4: ms[2]}}
+
     def set_profiling(self, enable: bool = True):
         check(lib.bem_operator_set_profiling(self.h, int(bool(enable))))
 

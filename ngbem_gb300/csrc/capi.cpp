@@ -504,6 +504,18 @@ int bem_operator_tensor_cores(bem_operator_t op, int* state, long long* bytes, i
   });
 }
 
+int bem_operator_autotune_tc(bem_operator_t op, int reps, int* nstages, double* ms) {
+  return guarded([&] {
+    REQUIRE(op && reps > 0, "null operator or reps < 1");
+    auto* h = dynamic_cast<HOperator*>(op->op.get());
+    if (!h) throw Error(BEM_ERR_STATE, "not an H-matrix operator");
+    h->autotune_tc(reps);
+    if (nstages) *nstages = h->tc_nst;
+    if (ms)
+      for (int k = 0; k < 3; ++k) ms[k] = h->tc_tune_ms[k];
+  });
+}
+
 int bem_tc_selftest(int* passed) {
   return guarded([&] {
     REQUIRE(passed, "null argument");

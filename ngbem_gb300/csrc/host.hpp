@@ -247,8 +247,19 @@ struct HOperator : OperatorBase {
   int tc_grid[2] = {0, 0}, tc_items[2] = {0, 0}, tc_nkc_x = 0, tc_nkc_x2 = 0, n_tc_leaves = 0;
   long long tc_bytes = 0;
   double tc_ms_build = 0.0;
+  // the stage plan: ring stages (2..4, TC_NST_DEFAULT until autotune_tc), the balanced items,
+  // segments and CTA schedules it is planned from, and the tuner's timings of 2, 3, 4 stages
+  int tc_nst = TC_NST_DEFAULT;
+  std::vector<TCItem> tc_it[2];
+  std::vector<TCSeg> tc_sg[2];
+  std::vector<int2> tc_sch[2];
+  double tc_tune_ms[3] = {0.0, 0.0, 0.0};
   bool tc_eligible(int trans, int nrhs, cudaStream_t s);
   void build_tc();
+  void plan_tc(int nst);  // stage plans of both passes for nst stages, uploaded
+  // times `reps` 32-right-hand-side applications with each stage count and keeps the fastest;
+  // returns its time per application (ms)
+  double autotune_tc(int reps);
   void release_tc();
   void mult_tc(const double* alpha, const void* x, const double* beta, void* y, int nrhs, cudaStream_t s);
   bem_operator_info_t info{};

@@ -337,7 +337,13 @@ struct TCDJob {  // pack the panel of (row tile, dense block): K = (column, real
   unsigned long long dst;
   int blk, i0, rows, N, kc0, nkc;
 };
-#define TC_CAP (48 * 1024)  // bytes of one pipeline stage (one MMA step of N = 256 takes 20 KB)
+// The pipeline ring holds TC_STAGE_BYTES, cut into 2, 3 or 4 stages (the operator's stage plan,
+// picked by bem_operator_autotune_tc; 2 by default: fewer, larger stages measured fastest).
+// One MMA step of N = 256 takes 20 KB.
+#define TC_STAGE_BYTES (192 * 1024)
+#define TC_NST_MAX 4
+#define TC_NST_DEFAULT 2
+__host__ __device__ constexpr int tc_cap(int nst) { return TC_STAGE_BYTES / nst; }
 int tc_smem_bytes();
 // 1 when the running device executes the tcgen05 kernels (compute capability 10.x)
 int tc_supported();
@@ -356,7 +362,7 @@ void launch_tc_pack_d(const TCDJob* jobs, int njobs, const MVDense* dense, cudaS
 void launch_tc_ysum_out(const int4* leaves, int nleaves, const int* deltas, const void* ypart, const int* perm,
                         int nrhs, int ld, const double* alpha, const double* beta, void* y, cudaStream_t s);
 // pass 0 (pass = 0): T panels of every low-rank block; pass 1: partial rows of U2 T
-cudaError_t launch_tc_gemm(int pass, const TCGemmArgs& g, int grid, cudaStream_t s);
+cudaError_t launch_tc_gemm(int pass, int nst, const TCGemmArgs& g, int grid, cudaStream_t s);
 // one 128 x N x (4 nkc) product D = A B^T on the tensor cores from ready panels (self-test):
 // d[row * N + n] (FP32); the B panel holds high and low parts, both are issued
 cudaError_t launch_tc_selftest(const void* a, const void* b, int N, int nkc, float* d, int* err, cudaStream_t s);

@@ -94,10 +94,10 @@ void balance(std::vector<TCItem>& items, const std::vector<double>& cost, int ns
 }
 
 // Stage plans of every CTA: the K ranges of its items' segments in order, packed into
-// pipeline stages of TC_CAP bytes (at most TC_MAXCH ranges, each at least one MMA step of
+// pipeline stages of `cap` bytes (at most TC_MAXCH ranges, each at least one MMA step of
 // K = 8), so that the kernel reads one contiguous run of descriptors per stage.
 void plan_stages(const std::vector<TCItem>& items, const std::vector<TCSeg>& segs, const std::vector<int2>& sched,
-                 std::vector<int4>& sched4, std::vector<int2>& stages, std::vector<TCChunk>& chunks) {
+                 int cap, std::vector<int4>& sched4, std::vector<int2>& stages, std::vector<TCChunk>& chunks) {
   sched4.assign(sched.size(), make_int4(0, 0, 0, 0));
   for (size_t c = 0; c < sched.size(); ++c) {
     const int s0 = (int)stages.size();
@@ -117,7 +117,7 @@ void plan_stages(const std::vector<TCItem>& items, const std::vector<TCSeg>& seg
       for (int sg = I.seg0; sg < I.seg0 + I.nseg; ++sg) {
         const TCSeg& S = segs[sg];
         for (int kc = 0; kc < S.nkc;) {
-          const int fit = ((TC_CAP - used) / per) & ~1;
+          const int fit = ((cap - used) / per) & ~1;
           if (fit < 2 || (int)chunks.size() - first >= TC_MAXCH) {
             close();
             continue;
@@ -358,24 +358,15 @@ void HOperator::build_tc() {
   balance(it1, cost1, nsm, sch1);
   tc_grid[0] = it0.empty() ? 0 : (int)sch0.size();
   tc_grid[1] = it1.empty() ? 0 : (int)sch1.size();
-  {
-    std::vector<int4> s4;
-    std::vector<int2> stg;
-    std::vector<TCChunk> chk;
-    plan_stages(it0, sg0, sch0, s4, stg, chk);
-    d_tc_sched[0].upload(s4);
-    d_tc_stages[0].upload(stg);
-    d_tc_chunks[0].upload(chk);
-    s4.clear();
-    stg.clear();
-    chk.clear();
-    plan_stages(it1, sg1, sch1, s4, stg, chk);
-    d_tc_sched[1].upload(s4);
-    d_tc_stages[1].upload(stg);
-    d_tc_chunks[1].upload(chk);
-  }
   d_tc_items[0].upload(it0);
   d_tc_items[1].upload(it1);
+  tc_it[0].swap(it0);
+  tc_it[1].swap(it1);
+  tc_sg[0].swap(sg0);
+  tc_sg[1].swap(sg1);
+  tc_sch[0].swap(sch0);
+  tc_sch[1].swap(sch1);
+  plan_tc(tc_nst);
   d_tc_outs.upload(outs);
   // pack the factors (once)
   {
@@ -417,13 +408,73 @@ void HOperator::build_tc() {
   BEM_CUDA(cudaDeviceSynchronize());
   tc_bytes = (long long)(d_tc_xa.bytes + d_tc_xa2.bytes + d_tc_ta.bytes + d_tc_vp.bytes + d_tc_up.bytes +
                          d_tc_dp.bytes + d_tc_y.bytes);
-  tc_items[0] = (int)it0.size();
-  tc_items[1] = (int)it1.size();
+  tc_items[0] = (int)tc_it[0].size();
+  tc_items[1] = (int)tc_it[1].size();
   tc_ms_build = std::chrono::duration<double, std::milli>(clk::now() - t0).count();
   tc_state = 1;
 }
 
+void HOperator::plan_tc(int nst) {
+  if (nst < 2 || nst > TC_NST_MAX) throw Error(BEM_ERR_ARG, "stage count out of range");
+  for (int pass = 0; pass < 2; ++pass) {
+    std::vector<int4> s4;
+    std::vector<int2> stg;
+    std::vector<TCChunk> chk;
+    plan_stages(tc_it[pass], tc_sg[pass], tc_sch[pass], tc_cap(nst), s4, stg, chk);
+    d_tc_sched[pass].upload(s4);
+    d_tc_stages[pass].upload(stg);
+    d_tc_chunks[pass].upload(chk);
+  }
+  BEM_CUDA(cudaDeviceSynchronize());
+  tc_nst = nst;
+}
+
+double HOperator::autotune_tc(int reps) {
+  if (tc_state == 0 && tc_mode) build_tc();
+  if (tc_state != 1) throw Error(BEM_ERR_STATE, "the operator has no tensor-core path");
+  reps = std::max(1, reps);
+  // zero right-hand sides in both numberings' extents: the kernels do the same work for any values
+  const VecMap vm = vec_map(0);
+  const int nrhs = 32;
+  DevBuf x, y;
+  x.alloc((size_t)std::max(vm.ld_in, 1) * nrhs * 16);
+  y.alloc((size_t)std::max(vm.ld_out, 1) * nrhs * 16);
+  BEM_CUDA(cudaMemset(x.p, 0, x.bytes));
+  const double one[2] = {1.0, 0.0}, zero[2] = {0.0, 0.0};
+  cudaEvent_t e0, e1;
+  BEM_CUDA(cudaEventCreate(&e0));
+  BEM_CUDA(cudaEventCreate(&e1));
+  double best = 1e300;
+  int best_nst = tc_nst;
+  for (int nst = 2; nst <= TC_NST_MAX; ++nst) {
+    plan_tc(nst);
+    mult_tc(one, x.p, zero, y.p, nrhs, 0);  // warm-up (shared-memory opt-in of the instance)
+    BEM_CUDA(cudaEventRecord(e0, 0));
+    for (int r = 0; r < reps; ++r) mult_tc(one, x.p, zero, y.p, nrhs, 0);
+    BEM_CUDA(cudaEventRecord(e1, 0));
+    BEM_CUDA(cudaEventSynchronize(e1));
+    float ms = 0.f;
+    BEM_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+    tc_tune_ms[nst - 2] = ms / reps;
+    if (ms / reps < best) {
+      best = ms / reps;
+      best_nst = nst;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  plan_tc(best_nst);
+  BEM_CUDA(cudaGetLastError());
+  if (device_status() != 0) throw Error(BEM_ERR_INTERNAL, "a bounded device wait ran out while tuning");
+  return best;
+}
+
 void HOperator::release_tc() {
+  for (int pass = 0; pass < 2; ++pass) {
+    tc_it[pass].clear();
+    tc_sg[pass].clear();
+    tc_sch[pass].clear();
+  }
   for (DevBuf* b : {&d_tc_xa, &d_tc_xa2, &d_tc_ta, &d_tc_vp, &d_tc_up, &d_tc_dp, &d_tc_y, &d_tc_items[0],
                     &d_tc_items[1], &d_tc_stages[0], &d_tc_stages[1], &d_tc_chunks[0], &d_tc_chunks[1],
                     &d_tc_sched[0], &d_tc_sched[1], &d_tc_outs, &d_tc_leaves, &d_tc_deltas})
@@ -452,7 +503,7 @@ void HOperator::mult_tc(const double* alpha, const void* x, const double* beta, 
     g.chunks = d_tc_chunks[pass].as<TCChunk>();
     g.ypart = d_tc_y.p;
     g.err = d_err.as<int>();
-    BEM_CUDA(launch_tc_gemm(pass, g, tc_grid[pass], s));
+    BEM_CUDA(launch_tc_gemm(pass, tc_nst, g, tc_grid[pass], s));
     if (profiling && pass == 0) BEM_CUDA(cudaEventRecord(ev[2], s));
   }
   if (profiling) BEM_CUDA(cudaEventRecord(ev[3], s));

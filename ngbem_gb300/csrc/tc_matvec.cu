@@ -20,7 +20,7 @@
 //
 // Kernel roles (320 threads, one CTA per SM, persistent over a host-balanced item list):
 //   warp 0      bulk copies (cp.async.bulk + mbarrier complete_tx) of A and B K-ranges into a
-//               4-stage ring;
+//               ring of 2 to 4 stages (NST, the operator's stage plan);
 //   warp 1      owns the tensor memory (512 columns: two 256-column buffers) and one thread
 //               issues tcgen05.mma, releasing stages and buffers by tcgen05.commit;
 //   warps 2-9   epilogue: tcgen05.ld of their TMEM lane quarter (two warps per quarter, one
@@ -40,10 +40,10 @@
 
 namespace bem {
 
-#define TC_NST 4
 #define TC_THREADS 320  // warp 0 copies, warp 1 MMAs, warps 2-9 epilogue
 #define TC_ACC_COLS 256
 #define TC_HDR 4096  // barriers, then the range descriptors of each stage (TC_MAXCH x 32 bytes)
+static_assert(1024 + TC_NST_MAX * TC_MAXCH * 32 <= TC_HDR, "range descriptors fit the header");
 #define TC_DESC 1024
 #define TC_ERR_WAIT 0x100
 
@@ -177,7 +177,7 @@ __device__ __forceinline__ float tf32_part(float v, int h) {
 }
 
 struct TCSmem {
-  uint64_t full[TC_NST], empty[TC_NST], accf[2], acce[2], fin;
+  uint64_t full[TC_NST_MAX], empty[TC_NST_MAX], accf[2], acce[2], fin;
   uint32_t tmem;
   int abort_flag;
 };
@@ -185,8 +185,10 @@ struct TCSmem {
 }  // namespace
 
 // ---- the grouped GEMM -----------------------------------------------------------------------
-template <int PASS>
+template <int PASS, int NST>
 __global__ void __launch_bounds__(TC_THREADS, 1) tc_gemm_kernel(TCGemmArgs g) {
+  constexpr int TC_NST = NST;
+  constexpr int TC_CAP = tc_cap(NST);
   extern __shared__ unsigned char tc_smem_raw[];
   unsigned char* base = (unsigned char*)(((uintptr_t)tc_smem_raw + 1023) & ~(uintptr_t)1023);
   TCSmem& S = *(TCSmem*)base;
@@ -484,7 +486,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) tc_gemm_kernel(TCGemmArgs g) {
   }
 }
 
-int tc_smem_bytes() { return TC_HDR + TC_NST * TC_CAP + 1024; }
+int tc_smem_bytes() { return TC_HDR + TC_STAGE_BYTES + 1024; }
 
 int tc_supported() {
   int dev = 0, major = 0;
@@ -493,17 +495,19 @@ int tc_supported() {
   return major == 10 ? 1 : 0;
 }
 
-template <int PASS>
+template <int PASS, int NST>
 static cudaError_t tc_gemm_t(const TCGemmArgs& g, int grid, cudaStream_t s) {
-  cudaError_t e = smem_optin<tc_gemm_kernel<PASS>>(tc_smem_bytes());
+  cudaError_t e = smem_optin<tc_gemm_kernel<PASS, NST>>(tc_smem_bytes());
   if (e != cudaSuccess) return e;
-  tc_gemm_kernel<PASS><<<grid, TC_THREADS, tc_smem_bytes(), s>>>(g);
+  tc_gemm_kernel<PASS, NST><<<grid, TC_THREADS, tc_smem_bytes(), s>>>(g);
   return cudaGetLastError();
 }
 
-cudaError_t launch_tc_gemm(int pass, const TCGemmArgs& g, int grid, cudaStream_t s) {
+cudaError_t launch_tc_gemm(int pass, int nst, const TCGemmArgs& g, int grid, cudaStream_t s) {
   if (grid <= 0) return cudaSuccess;
-  return pass == 0 ? tc_gemm_t<0>(g, grid, s) : tc_gemm_t<1>(g, grid, s);
+  if (nst == 3) return pass == 0 ? tc_gemm_t<0, 3>(g, grid, s) : tc_gemm_t<1, 3>(g, grid, s);
+  if (nst == 4) return pass == 0 ? tc_gemm_t<0, 4>(g, grid, s) : tc_gemm_t<1, 4>(g, grid, s);
+  return pass == 0 ? tc_gemm_t<0, 2>(g, grid, s) : tc_gemm_t<1, 2>(g, grid, s);
 }
 
 // ---- operand preparation ----------------------------------------------------------------------

@@ -60,3 +60,55 @@ def test_load_refuses_other_spaces(tmp_path):
         bem.HMatrix.load(str(path), nb.SurfaceL2(icosphere(2)))
     with pytest.raises(Exception):
         bem.HMatrix.load(str(path), nb.H1(m))
+
+
+def _dense_descriptor_offset(raw, op):
+    """Byte offset of the first dense-block descriptor (MVDense: ptr, r0, m, c0, n) in a saved
+    operator file, found by walking the file's layout (the save order of serialize.cpp)."""
+    import ctypes as C
+
+    from ngbem_gb300 import _lib
+
+    def count(o):
+        return int(np.frombuffer(raw[o:o + 8], dtype=np.int64)[0])
+
+    o = 8 + 4 + 8 + 4 + 4 + 4 + C.sizeof(_lib.Params) + 6 * 4 + 4 + 4
+    for _ in range(4):  # the two permutations and the two dof maps (int32)
+        o += 8 + 4 * count(o)
+    nb_ = count(o)
+    assert nb_ == op.mat.info["nblocks"]
+    o += 8 + 12 * nb_  # blocks: (rowcl, colcl, near) of 12 bytes
+    for _ in range(2):  # ranks and fallback flags
+        assert count(o) == nb_
+        o += 8 + 4 * nb_
+    o += C.sizeof(_lib.OperatorInfo)
+    assert count(o) == op.mat.info["nnear"]
+    return o + 8
+
+
+def test_load_refuses_corrupt_files(tmp_path):
+    """A truncated file, a precision out of range and a dense block reaching past the matrix
+    are refused with BEM_ERR_ARG before anything is uploaded."""
+    from ngbem_gb300._lib import BemError
+    m = icosphere(2)
+    sp = nb.SurfaceL2(m)
+    V = nb.SingleLayerPotentialOperator(sp, leafsize=20, precision="mixed")
+    path = tmp_path / "v.bin"
+    V.mat.save(str(path))
+    raw = bytearray(path.read_bytes())
+    cases = {"truncated": raw[:-100]}
+    bad = bytearray(raw)
+    bad[28:32] = np.int32(7).tobytes()  # the precision field
+    cases["precision"] = bad
+    bad = bytearray(raw)
+    o = _dense_descriptor_offset(raw, V)
+    bad[o + 8:o + 12] = np.int32(sp.ndof).tobytes()  # r0 of the first dense block
+    cases["extent"] = bad
+    for name, data in cases.items():
+        p = tmp_path / f"{name}.bin"
+        p.write_bytes(bytes(data))
+        with pytest.raises(BemError) as e:
+            bem.HMatrix.load(str(p), nb.SurfaceL2(m))
+        assert e.value.code == 1, name  # BEM_ERR_ARG
+    # the intact file still loads
+    assert bem.HMatrix.load(str(path), nb.SurfaceL2(m)).info["nblocks"] == V.mat.info["nblocks"]

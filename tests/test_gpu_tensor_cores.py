@@ -96,3 +96,19 @@ def test_beta_and_single_rhs(bm):
     y1 = _apply(A32, x1)
     assert rel(y1[:, 0], ref[:, 0]) < 1e-5
     A32.set_accuracy(True)
+
+
+def test_stage_plan_autotuner(bm):
+    """The tuner times 2, 3 and 4 pipeline stages on the operator, keeps the fastest, and the
+    products with the kept plan still agree with the compensated ones."""
+    P1, A32, A64 = bm
+    A32.set_accuracy(True)
+    x = _x(P1.ndof, 32, 5)
+    y_comp = _apply(A32, x)
+    A32.set_accuracy(False)
+    A32.set_tensor_cores(True)
+    res = A32.autotune_tensor_cores(reps=2)
+    assert res["stages"] in (2, 3, 4)
+    assert all(v > 0 for v in res["ms"].values())
+    assert res["ms"][res["stages"]] == min(res["ms"].values())
+    assert rel(_apply(A32, x), y_comp) < 1e-6
