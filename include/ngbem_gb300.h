@@ -286,9 +286,10 @@ int bem_sl_batch_destroy(bem_slbatch_t batch);
  * FP64 throughout): compensated = 1 (default) forms every product and sum error-free (x split
  * into FP32 hi+lo, TwoProd/TwoSum), so the only rounding is that of the stored entries;
  * compensated = 0 uses plain FP32 FMAs (about 1e-7 relative rounding, faster); complex
- * operators applied to 2..32 right-hand sides then use the tensor cores (about 5e-6, see
- * bem_operator_set_tensor_cores).  FP64-stored operators ignore it.  bem_gmres uses the plain form inside its Krylov iterations and the
- * compensated form for its residuals (iterative refinement). */
+ * operators applied to 2..32 right-hand sides then use the tensor cores (about 5e-7, see
+ * bem_operator_set_tensor_cores).  FP64-stored operators ignore it.  bem_gmres uses the plain
+ * form inside its Krylov iterations and the compensated form for its residuals (iterative
+ * refinement). */
 int bem_operator_set_accuracy(bem_operator_t op, int compensated);
 
 /* Autotuner of the single right-hand-side matvec (no counterpart in the reference): times

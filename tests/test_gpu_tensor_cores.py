@@ -112,3 +112,23 @@ def test_stage_plan_autotuner(bm):
     assert all(v > 0 for v in res["ms"].values())
     assert res["ms"][res["stages"]] == min(res["ms"].values())
     assert rel(_apply(A32, x), y_comp) < 1e-6
+
+
+def test_products_against_the_oracle_at_level_5(oracle):
+    """The Burton-Miller operator near the benchmark's size (ellipsoid L5, 10 242 P1 dofs, kappa
+    8): the tensor-core product of 32 right-hand sides against the oracle's FP64 H-matrix
+    (CalcHMatrix and HMatrix::Mult restated) on four of its columns, within the 1e-6 bar."""
+    m = ellipsoid(5, (1.0, 0.7, 0.5))
+    P1 = nb.H1(m, complex=True)
+    kw = dict(kappa=KAPPA, intorder=3, leafsize=20, eta=2.0, eps=1e-8)
+    A = nb.HelmholtzCombinedFieldOperator(P1, P1, precision="mixed", **kw).mat
+    A.set_accuracy(False)
+    A.set_tensor_cores(True)
+    x = _x(P1.ndof, 32, 23)
+    y = _apply(A, x)
+    assert A.tensor_cores()["state"] == 1
+    H = oracle.OracleOperator("helmholtz_cf", m, "P1", kappa=KAPPA, intorder=3, leafsize=20, eta=2.0, eps=1e-8)
+    xh = x.cpu().numpy()
+    for r in (0, 9, 20, 31):
+        yo = H.mult(xh[:, r])
+        assert rel(y[:, r], yo) < 1e-6
