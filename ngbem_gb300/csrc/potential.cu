@@ -130,7 +130,12 @@ __global__ void __launch_bounds__(POT_THREADS) pot_eval_kernel(PotArgs a) {
   X(K_HELMHOLTZ_SL, TR_L2P3, cpx<double>)                                                       \
   X(K_LAPLACE_SL, TR_H1P2, double) X(K_LAPLACE_SL, TR_H1P3, double) X(K_LAPLACE_DL, TR_H1P2, double) \
   X(K_LAPLACE_DL, TR_H1P3, double) X(K_HELMHOLTZ_SL, TR_H1P2, cpx<double>)                          \
-  X(K_HELMHOLTZ_SL, TR_H1P3, cpx<double>) X(K_MAXWELL_DL, TR_NEDROT, cpx<double>)
+  X(K_HELMHOLTZ_SL, TR_H1P3, cpx<double>) X(K_MAXWELL_DL, TR_NEDROT, cpx<double>)                \
+  X(K_HELMHOLTZ_DL, TR_L2P1, cpx<double>) X(K_HELMHOLTZ_DL, TR_L2P2, cpx<double>)               \
+  X(K_HELMHOLTZ_DL, TR_L2P3, cpx<double>) X(K_HELMHOLTZ_DL, TR_H1P2, cpx<double>)               \
+  X(K_HELMHOLTZ_DL, TR_H1P3, cpx<double>) X(K_HELMHOLTZ_CF, TR_L2P1, cpx<double>)               \
+  X(K_HELMHOLTZ_CF, TR_L2P2, cpx<double>) X(K_HELMHOLTZ_CF, TR_L2P3, cpx<double>)               \
+  X(K_HELMHOLTZ_CF, TR_H1P2, cpx<double>) X(K_HELMHOLTZ_CF, TR_H1P3, cpx<double>)
 
 int potential_dim(int kid, int trt) {
 #define X(K, T, V) \

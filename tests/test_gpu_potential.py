@@ -29,6 +29,11 @@ CASES = [
     # is the reference's sum of its six cross-product terms without their signs
     ("maxwell_sl", "HCURL", "maxwellcurl", 2.0),
     ("maxwell_dl", "HCURL", "rotatedtrace", 2.0, "id"),
+    # higher-order spaces with the Helmholtz kernels
+    ("helmholtz_dl", "L2P2", "id", 3.0),
+    ("helmholtz_cf", "L2P3", "id", 4.0),
+    ("helmholtz_dl", "H1P3", "id", 3.0),
+    ("helmholtz_cf", "H1P2", "id", 4.0),
 ]
 
 
