@@ -313,6 +313,16 @@ void HOperator::collect_profile() {
 HOperator::~HOperator() {
   for (auto& ev : pending)
     for (auto& e : ev) cudaEventDestroy(e);
+  if (h_status) cudaFreeHost(h_status);
+}
+
+void HOperator::queue_status(cudaStream_t s) {
+  if (!d_err.p) return;
+  if (!h_status) {
+    BEM_CUDA(cudaHostAlloc((void**)&h_status, sizeof(int), cudaHostAllocDefault));
+    *h_status = 0;
+  }
+  BEM_CUDA(cudaMemcpyAsync(h_status, d_err.p, sizeof(int), cudaMemcpyDeviceToHost, s));
 }
 
 void HOperator::to_dense(void* out) {

@@ -343,11 +343,13 @@ int bem_operator_mult_host(bem_operator_t op, int trans, const double* alpha, co
     void* xm = small ? mapped(x) : nullptr;
     void* ym = xm ? mapped(y) : nullptr;
     // a synchronous call reports a product whose bounded device waits ran out (and clears the
-    // operator's device state so that the next product starts clean)
+    // operator's device state so that the next product starts clean); the flags are copied on
+    // the product's stream before the one synchronisation
+    auto* hop = dynamic_cast<HOperator*>(o);
     auto check_status = [&]() {
-      auto* h = dynamic_cast<HOperator*>(o);
+      auto* h = hop;
       if (!h) return;
-      const int st = h->device_status();
+      const int st = h->queued_status();
       if (st != 0) {
         h->reset_device_state();
         throw Error(BEM_ERR_INTERNAL, "a bounded device wait of the product ran out (flags " + std::to_string(st) +
@@ -356,6 +358,7 @@ int bem_operator_mult_host(bem_operator_t op, int trans, const double* alpha, co
     };
     if (xm && ym) {
       o->mult(trans, alpha, xm, beta, ym, nrhs, 0);
+      if (hop) hop->queue_status(0);
       BEM_CUDA(cudaStreamSynchronize(0));
       check_status();
       return;
@@ -367,6 +370,7 @@ int bem_operator_mult_host(bem_operator_t op, int trans, const double* alpha, co
       BEM_CUDA(cudaMemcpyAsync(o->stage_y.p, y, nout * esz, cudaMemcpyHostToDevice, 0));
     o->mult(trans, alpha, o->stage_x.p, beta, o->stage_y.p, nrhs, 0);
     BEM_CUDA(cudaMemcpyAsync(y, o->stage_y.p, nout * esz, cudaMemcpyDeviceToHost, 0));
+    if (hop) hop->queue_status(0);
     BEM_CUDA(cudaStreamSynchronize(0));
     check_status();
   });

@@ -282,6 +282,11 @@ struct HOperator : OperatorBase {
   unsigned mv_built = 0;
   bool mv_multi_built = false;
   int device_status();   // matvec pipeline error flags (0 = ok)
+  // the same flags copied on stream s into a page-locked word (no device-wide synchronisation):
+  // queue_status before the caller synchronises s, queued_status after
+  void queue_status(cudaStream_t s);
+  int queued_status() const { return h_status ? *(volatile int*)h_status : 0; }
+  int* h_status = nullptr;
   // Clears the error flags, the claim counters and the accumulators of the products (after a
   // product whose bounded waits ran out: its schedule state is not the one a product leaves).
   void reset_device_state();
