@@ -107,11 +107,22 @@ typedef struct {
 /* Fill *p with the reference defaults (intorder 3, leafsize 40, eta 2, eps 1e-6, aca). */
 int bem_params_default(bem_params_t* p);
 
-/* Mesh of flat triangles; vertex order per triangle defines the outward normal.
+/* Mesh of triangles (flat until bem_mesh_set_geometry curves them); vertex order per
+ * triangle defines the outward normal.
  * Replaces NGSolve MeshAccess for the surface (reference src/ngbem.cpp:33-34). */
 int bem_mesh_create(int nv, const double* xyz, int nt, const int* tri, bem_mesh_t* out);
 int bem_mesh_num_edges(bem_mesh_t mesh, int* ne);
 int bem_mesh_destroy(bem_mesh_t mesh);
+/* Curved geometry (NGSolve's Mesh.Curve(order), which the reference's tests call before
+ * assembly, e.g. tests/test_aca.py:7; the operators then integrate through the curved element
+ * maps, mesh->GetTrafo in src/ngbem.cpp:501-737).  order 1: flat triangles; order 2, 3:
+ * isoparametric Lagrange triangles with nodes[nt][(order+1)(order+2)/2][3]: node (i, j, k),
+ * i + j + k = order, at barycentric (i, j, k) / order of the triangle's vertices
+ * (v0, v1, v2), listed for i = order..0, j = order-i..0; the corner nodes must equal the
+ * vertices.  The scalar spaces (P0, P1, SurfaceL2 and H1 of higher order) live on curved
+ * meshes; RT0, HCurl and the dual mapping need flat ones (BEM_ERR_ARG at assembly).  Call
+ * before the first operator on the mesh is created (BEM_ERR_STATE after). */
+int bem_mesh_set_geometry(bem_mesh_t mesh, int order, const double* nodes);
 
 /* Trace space on a mesh (replaces the NGSolve FESpace argument of the factories,
  * reference src/python_bem.cpp:27-173).  RT0 dofs are edges numbered by first

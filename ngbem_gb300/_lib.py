@@ -54,6 +54,7 @@ SIGNATURES = {
     "bem_params_default": ([C.POINTER(Params)], C.c_int),
     "bem_mesh_create": ([C.c_int, _dp, C.c_int, _ip, C.POINTER(_vp)], C.c_int),
     "bem_mesh_num_edges": ([_vp, _ip], C.c_int),
+    "bem_mesh_set_geometry": ([_vp, C.c_int, _dp], C.c_int),
     "bem_mesh_destroy": ([_vp], C.c_int),
     "bem_space_create": ([_vp, C.c_int, C.c_int, C.POINTER(_vp)], C.c_int),
     "bem_space_create_on": ([_vp, C.c_int, C.c_int, _vp, C.POINTER(_vp)], C.c_int),

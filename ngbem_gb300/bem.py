@@ -54,6 +54,10 @@ class _MeshHandle:
         T = np.ascontiguousarray(mesh.triangles, dtype=np.int32)
         check(lib.bem_mesh_create(mesh.nv, X.ctypes.data_as(_lib._dp), mesh.nt, T.ctypes.data_as(_lib._ip),
                                   C.byref(self.h)))
+        self.curve = (getattr(mesh, "curve_order", 1), id(getattr(mesh, "curve_nodes", None)))
+        if self.curve[0] > 1:
+            G = np.ascontiguousarray(mesh.curve_nodes, dtype=np.float64)
+            check(lib.bem_mesh_set_geometry(self.h, self.curve[0], G.ctypes.data_as(_lib._dp)))
         ne = C.c_int()
         check(lib.bem_mesh_num_edges(self.h, C.byref(ne)))
         self.ne = ne.value
@@ -62,7 +66,8 @@ class _MeshHandle:
     def of(cls, mesh: Mesh):
         key = id(mesh)
         h = cls._cache.get(key)
-        if h is None or h.mesh is not mesh:
+        curve = (getattr(mesh, "curve_order", 1), id(getattr(mesh, "curve_nodes", None)))
+        if h is None or h.mesh is not mesh or h.curve != curve:
             h = cls(mesh)
             cls._cache[key] = h
         return h

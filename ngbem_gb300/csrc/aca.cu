@@ -61,8 +61,8 @@ struct PtData {
 };
 
 template <class P, bool NEEDN>
-__device__ __forceinline__ PtData<P> load_pt(const APt<P>* PT, const ElemRecP<P>* E, const int* patch,
-                                             int p0, int idx, int nq) {
+__device__ __forceinline__ PtData<P> load_pt(const APt<P>* PT, const ElemRecP<P>* E, const PGeo<P>* PG,
+                                             const int* patch, int p0, int idx, int nq) {
   const int le = idx / nq;
   const int q = idx - le * nq;
   const int e = patch[p0 + le];
@@ -70,7 +70,11 @@ __device__ __forceinline__ PtData<P> load_pt(const APt<P>* PT, const ElemRecP<P>
   PtData<P> r;
   r.h[0] = a.hx; r.h[1] = a.hy; r.h[2] = a.hz;
   r.l[0] = a.lx; r.l[1] = a.ly; r.l[2] = a.lz;
-  if (NEEDN) { r.n[0] = E[e].n[0]; r.n[1] = E[e].n[1]; r.n[2] = E[e].n[2]; }
+  if (NEEDN) {
+    // curved elements: the normal at the point; flat: the element's
+    const P* n = PG ? PG[(size_t)e * nq + q].n : E[e].n;
+    r.n[0] = n[0]; r.n[1] = n[1]; r.n[2] = n[2];
+  }
   else { r.n[0] = r.n[1] = r.n[2] = P(0); }
   return r;
 }
@@ -104,6 +108,7 @@ __global__ void __launch_bounds__(ACA_T, sizeof(P) == 4 ? 4 : 2) aca_kernel(AcaA
   const int kcap = min(d.kcap, KCAP_MAX);
   const APt<P>* PT = (const APt<P>*)a.apts;
   const ElemRecP<P>* E = (const ElemRecP<P>*)a.erecP;
+  const PGeo<P>* PG = (const PGeo<P>*)a.pgeo;
   const P kappa = (P)a.kappa;
   const double eps = a.eps;
   int status = 0;
@@ -120,12 +125,12 @@ __global__ void __launch_bounds__(ACA_T, sizeof(P) == 4 ? 4 : 2) aca_kernel(AcaA
       // ---- row ik: v_j = K(x_ik, y_j) - sum_l U(ik,l) V(l,j)
       for (int l = threadIdx.x; l < k; l += ACA_T) s_l[l] = U[(size_t)l * M + ik];
       __syncthreads();
-      const PtData<P> x = load_pt<P, G::NEEDS_NX>(PT, E, a.patch_test, d.pi0, ik, nq);
+      const PtData<P> x = load_pt<P, G::NEEDS_NX>(PT, E, PG, a.patch_test, d.pi0, ik, nq);
       P best = P(0);
       int bi = -1;
       V* Vk = Vm + (size_t)k * N;
       for (int j = threadIdx.x; j < N; j += ACA_T) {
-        const PtData<P> y = load_pt<P, G::NEEDS_NY>(PT, E, a.patch_trial, d.pj0, j, nq);
+        const PtData<P> y = load_pt<P, G::NEEDS_NY>(PT, E, PG, a.patch_trial, d.pj0, j, nq);
         V v = kern_entry<G, P, V>(x, y, kappa, comp);
         for (int l = 0; l < k; ++l) v -= s_l[l] * Vm[(size_t)l * N + j];
         Vk[j] = v;
@@ -147,13 +152,13 @@ __global__ void __launch_bounds__(ACA_T, sizeof(P) == 4 ? 4 : 2) aca_kernel(AcaA
       // ---- column jk: u_i = (K(x_i, y_jk) - sum_l U(i,l) V(l,jk)) / sqrt(vkj)
       for (int l = threadIdx.x; l < k; l += ACA_T) s_l[l] = Vm[(size_t)l * N + jk];
       __syncthreads();
-      const PtData<P> y = load_pt<P, G::NEEDS_NY>(PT, E, a.patch_trial, d.pj0, jk, nq);
+      const PtData<P> y = load_pt<P, G::NEEDS_NY>(PT, E, PG, a.patch_trial, d.pj0, jk, nq);
       const P isq = P(1) / sqrt_(vkj);
       P nu = P(0), bu = P(0);
       int biu = -1;
       V* Uk = U + (size_t)k * M;
       for (int i = threadIdx.x; i < M; i += ACA_T) {
-        const PtData<P> xi = load_pt<P, G::NEEDS_NX>(PT, E, a.patch_test, d.pi0, i, nq);
+        const PtData<P> xi = load_pt<P, G::NEEDS_NX>(PT, E, PG, a.patch_test, d.pi0, i, nq);
         V u = kern_entry<G, P, V>(xi, y, kappa, comp);
         for (int l = 0; l < k; ++l) u -= U[(size_t)l * M + i] * s_l[l];
         u *= isq;
@@ -228,6 +233,7 @@ __global__ void __launch_bounds__(256, 4) aca_warp_kernel(AcaArgs a) {
   const int kcap = min(d.kcap, KCAP_MAX);
   const APt<P>* PT = (const APt<P>*)a.apts;
   const ElemRecP<P>* E = (const ElemRecP<P>*)a.erecP;
+  const PGeo<P>* PG = (const PGeo<P>*)a.pgeo;
   const P kappa = (P)a.kappa;
   const double eps = a.eps;
   int status = 0;
@@ -244,12 +250,12 @@ __global__ void __launch_bounds__(256, 4) aca_warp_kernel(AcaArgs a) {
       // ---- row ik: v_j = K(x_ik, y_j) - sum_l U(ik,l) V(l,j)
       for (int l = lane; l < k; l += 32) s_l[l] = U[(size_t)l * M + ik];
       __syncwarp();
-      const PtData<P> x = load_pt<P, G::NEEDS_NX>(PT, E, a.patch_test, d.pi0, ik, nq);
+      const PtData<P> x = load_pt<P, G::NEEDS_NX>(PT, E, PG, a.patch_test, d.pi0, ik, nq);
       P best = P(0);
       int bi = -1;
       V* Vk = Vm + (size_t)k * N;
       for (int j = lane; j < N; j += 32) {
-        const PtData<P> y = load_pt<P, G::NEEDS_NY>(PT, E, a.patch_trial, d.pj0, j, nq);
+        const PtData<P> y = load_pt<P, G::NEEDS_NY>(PT, E, PG, a.patch_trial, d.pj0, j, nq);
         V v = kern_entry<G, P, V>(x, y, kappa, comp);
         for (int l = 0; l < k; ++l) v -= s_l[l] * Vm[(size_t)l * N + j];
         Vk[j] = v;
@@ -273,13 +279,13 @@ __global__ void __launch_bounds__(256, 4) aca_warp_kernel(AcaArgs a) {
       __syncwarp();
       for (int l = lane; l < k; l += 32) s_l[l] = Vm[(size_t)l * N + jk];
       __syncwarp();
-      const PtData<P> y = load_pt<P, G::NEEDS_NY>(PT, E, a.patch_trial, d.pj0, jk, nq);
+      const PtData<P> y = load_pt<P, G::NEEDS_NY>(PT, E, PG, a.patch_trial, d.pj0, jk, nq);
       const P isq = P(1) / sqrt_(vkj);
       P nu = P(0), bu = P(0);
       int biu = -1;
       V* Uk = U + (size_t)k * M;
       for (int i = lane; i < M; i += 32) {
-        const PtData<P> xi = load_pt<P, G::NEEDS_NX>(PT, E, a.patch_test, d.pi0, i, nq);
+        const PtData<P> xi = load_pt<P, G::NEEDS_NX>(PT, E, PG, a.patch_test, d.pi0, i, nq);
         V u = kern_entry<G, P, V>(xi, y, kappa, comp);
         for (int l = 0; l < k; ++l) u -= U[(size_t)l * M + i] * s_l[l];
         u *= isq;
@@ -347,6 +353,7 @@ __global__ void __launch_bounds__(256) aca_project_kernel(ProjArgs a) {
   const int nq = a.nq;
   const int M = d.ni * nq, N = d.nj * nq;
   const ElemRecP<P>* E = (const ElemRecP<P>*)a.erecP;
+  const PGeo<P>* PG = (const PGeo<P>*)a.pgeo;
   const QPt<P>* Q = (const QPt<P>*)a.qoff;
   const P2_<P>* RQ = (const P2_<P>*)a.rq;
   const P kappa = (P)a.kappa;
@@ -370,7 +377,7 @@ __global__ void __launch_bounds__(256) aca_project_kernel(ProjArgs a) {
       P rot[3][3], o[3][3];
       for (int x = 0; x < 3; ++x)
         for (int y = 0; y < 3; ++y) { rot[x][y] = Ee.rot[x][y]; o[x][y] = Ee.o[x][y]; }
-      const P nrm[3] = {Ee.n[0], Ee.n[1], Ee.n[2]};
+      P nrm[3] = {Ee.n[0], Ee.n[1], Ee.n[2]};
       int sg[SignSlots<TET>::N];
       elem_signs<TET>(a.test.sign, e, sg);
       V acc[NDI];
@@ -381,6 +388,7 @@ __global__ void __launch_bounds__(256) aca_project_kernel(ProjArgs a) {
         const P2_<P> rp = RQ[q];
         P xp[3][3];
         for (int x = 0; x < 3; ++x) { xp[x][0] = qo.x - o[x][0]; xp[x][1] = qo.y - o[x][1]; xp[x][2] = qo.z - o[x][2]; }
+        if (PG) point_geo<P>(PG[(size_t)e * nq + q], nrm, rot);
         const V u = Us[(size_t)kk * M + ie * nq + q] * qo.w;
 #pragma unroll
         for (int x = 0; x < NDI; ++x)
@@ -400,7 +408,7 @@ __global__ void __launch_bounds__(256) aca_project_kernel(ProjArgs a) {
       P rot[3][3], o[3][3];
       for (int x = 0; x < 3; ++x)
         for (int y = 0; y < 3; ++y) { rot[x][y] = Ee.rot[x][y]; o[x][y] = Ee.o[x][y]; }
-      const P nrm[3] = {Ee.n[0], Ee.n[1], Ee.n[2]};
+      P nrm[3] = {Ee.n[0], Ee.n[1], Ee.n[2]};
       int sg[SignSlots<TRT>::N];
       elem_signs<TRT>(a.trial.sign, e, sg);
       V acc[NDJ];
@@ -411,6 +419,7 @@ __global__ void __launch_bounds__(256) aca_project_kernel(ProjArgs a) {
         const P2_<P> rp = RQ[q];
         P xp[3][3];
         for (int x = 0; x < 3; ++x) { xp[x][0] = qo.x - o[x][0]; xp[x][1] = qo.y - o[x][1]; xp[x][2] = qo.z - o[x][2]; }
+        if (PG) point_geo<P>(PG[(size_t)e * nq + q], nrm, rot);
         const V v = Vs[(size_t)kk * N + je * nq + q] * qo.w;
 #pragma unroll
         for (int x = 0; x < NDJ; ++x)

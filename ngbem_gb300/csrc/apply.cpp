@@ -259,6 +259,7 @@ void HOperator::potential(const void* density, int npts, const double* pts, cons
   a.erec = rt.rec[0].p;
   a.qoff = rt.qoff[0].p;
   a.rq = rt.rq[0].as<double>();
+  a.pgeo = rt.pgeo[0].p;
   a.elems = all ? nullptr : d_el.as<int>();
   a.nt = (int)el.size();
   a.nq = rt.nq;
@@ -354,6 +355,8 @@ void HOperator::to_dense(void* out) {
 void MassOperator::build(SpaceH* trial, SpaceH* test, bool complex_vectors) {
   if (trial->mesh != test->mesh) throw Error(BEM_ERR_ARG, "mass matrix needs one mesh");
   MeshH& m = *trial->mesh;
+  check_curved(m, *trial, TR_P0);
+  check_curved(m, *test, TR_P0);
   cplx = complex_vectors;
   nrows = test->ndof;
   ncols = trial->ndof;
@@ -412,7 +415,8 @@ void MassOperator::build(SpaceH* trial, SpaceH* test, bool complex_vectors) {
       shape(*test, e, r.xi[q], r.eta[q], Si, di);
       shape(*trial, e, r.xi[q], r.eta[q], Sj, dj);
       if (di != dj) throw Error(BEM_ERR_ARG, "mass matrix of scalar and vector spaces");
-      const double w = r.w[q] * m.rec[e].detJ;
+      double x[3], nrm[3], rt[3][3];
+      const double w = r.w[q] * m.frame(e, r.xi[q], r.eta[q], x, nrm, rt);
       for (int a = 0; a < test->nd; ++a)
         for (int b = 0; b < trial->nd; ++b) {
           double s = 0.0;

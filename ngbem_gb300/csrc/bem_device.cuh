@@ -328,6 +328,32 @@ template <> struct TraceInfo<TR_H1P3ROT> { static constexpr int ND = 10, DIM = 3
 template <> struct TraceInfo<TR_H1P2HELM> { static constexpr int ND = 6, DIM = 4; };
 template <> struct TraceInfo<TR_H1P3HELM> { static constexpr int ND = 10, DIM = 4; };
 // traces that read the element's n x grad(lambda_a) table
+// the geometry of a curved element's rule point (PGeo): normal and rotated gradients
+template <class P>
+__device__ __forceinline__ void point_geo(const PGeo<P>& g, P n[3], P rot[3][3]) {
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    n[c] = g.n[c];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) rot[a][c] = g.rot[a][c];
+  }
+}
+
+// the parts of a rule point's geometry that a kernel side reads
+template <class P, bool N, bool ROT>
+__device__ __forceinline__ void pgeo_load(const PGeo<P>& g, P n[3], P rot[3][3]) {
+  if constexpr (N) {
+#pragma unroll
+    for (int c = 0; c < 3; ++c) n[c] = g.n[c];
+  }
+  if constexpr (ROT) {
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+      for (int c = 0; c < 3; ++c) rot[a][c] = g.rot[a][c];
+  }
+}
+
 __host__ __device__ constexpr bool needs_rot(int tr) { return tr == TR_ROT || tr == TR_HELM || h1p_rot(tr); }  // incl. HELM
 // sign slots a kernel keeps per element (at least the three edge signs)
 template <int TR> struct SignSlots { static constexpr int N = TraceInfo<TR>::ND > 3 ? TraceInfo<TR>::ND : 3; };

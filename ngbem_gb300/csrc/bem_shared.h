@@ -1,5 +1,6 @@
 // Plain-old-data descriptors shared by the host orchestration (C++) and the CUDA kernels.
 #pragma once
+#include <math.h>
 #include <stdint.h>
 
 namespace bem {
@@ -152,6 +153,75 @@ struct ElemRecP {
   P rot[3][3];
   P pad[3];
 };
+
+// Geometry of one regular-rule point of a curved element: the unit normal and the rotated
+// surface gradients n x grad_Gamma(lambda_a) of the barycentrics there (flat elements keep
+// them per element, in ElemRecP).
+template <class P>
+struct PGeo {
+  P n[3];
+  P rot[3][3];
+};
+
+// Curved (isoparametric Lagrange) element map of order g at (xi, eta): the point and its
+// derivatives J0 = dx/dxi, J1 = dx/deta from the element's (g+1)(g+2)/2 nodes P (3 doubles
+// each).  Node (i, j, k), i + j + k = g, sits at barycentric (i, j, k) / g of the vertices
+// (v0, v1, v2) and the nodes are listed for i = g..0, j = g-i..0; its shape function is
+// L_i(l0) L_j(l1) L_k(l2) with (l0, l1, l2) = (xi, eta, 1 - xi - eta) and
+// L_i(t) = prod_{m<i} (g t - m) / (m + 1).
+__host__ __device__ inline void curved_map(int g, const double* P, double xi, double eta, double* x, double* J0,
+                                           double* J1) {
+  const double l[3] = {xi, eta, 1.0 - xi - eta};
+  double L[3][4], D[3][4];
+  for (int s = 0; s < 3; ++s)
+    for (int i = 0; i <= g; ++i) {
+      double v = 1.0, d = 0.0;
+      for (int m = 0; m < i; ++m) {
+        const double f = (g * l[s] - m) / (m + 1);
+        d = d * f + v * g / (m + 1);
+        v = v * f;
+      }
+      L[s][i] = v;
+      D[s][i] = d;
+    }
+  for (int c = 0; c < 3; ++c) x[c] = J0[c] = J1[c] = 0.0;
+  int n = 0;
+  for (int i = g; i >= 0; --i)
+    for (int j = g - i; j >= 0; --j, ++n) {
+      const int k = g - i - j;
+      const double N = L[0][i] * L[1][j] * L[2][k];
+      const double dxi = D[0][i] * L[1][j] * L[2][k] - L[0][i] * L[1][j] * D[2][k];
+      const double deta = L[0][i] * D[1][j] * L[2][k] - L[0][i] * L[1][j] * D[2][k];
+      for (int c = 0; c < 3; ++c) {
+        x[c] += N * P[3 * n + c];
+        J0[c] += dxi * P[3 * n + c];
+        J1[c] += deta * P[3 * n + c];
+      }
+    }
+}
+
+// |J0 x J1|, the unit normal and the rotated surface gradients n x grad_Gamma(lambda_a) of the
+// barycentrics (lambda_0 = xi, lambda_1 = eta): grad_Gamma = J (J^T J)^{-1} grad_ref.
+__host__ __device__ inline double surface_frame(const double* J0, const double* J1, double* n, double rot[3][3]) {
+  const double cr[3] = {J0[1] * J1[2] - J0[2] * J1[1], J0[2] * J1[0] - J0[0] * J1[2], J0[0] * J1[1] - J0[1] * J1[0]};
+  const double detJ = sqrt(cr[0] * cr[0] + cr[1] * cr[1] + cr[2] * cr[2]);
+  for (int c = 0; c < 3; ++c) n[c] = cr[c] / detJ;
+  const double g00 = J0[0] * J0[0] + J0[1] * J0[1] + J0[2] * J0[2];
+  const double g01 = J0[0] * J1[0] + J0[1] * J1[1] + J0[2] * J1[2];
+  const double g11 = J1[0] * J1[0] + J1[1] * J1[1] + J1[2] * J1[2];
+  const double det = g00 * g11 - g01 * g01;
+  const double gh[3][2] = {{1.0, 0.0}, {0.0, 1.0}, {-1.0, -1.0}};
+  for (int a = 0; a < 3; ++a) {
+    const double c0 = (g11 * gh[a][0] - g01 * gh[a][1]) / det;
+    const double c1 = (-g01 * gh[a][0] + g00 * gh[a][1]) / det;
+    double gv[3];
+    for (int c = 0; c < 3; ++c) gv[c] = J0[c] * c0 + J1[c] * c1;
+    rot[a][0] = n[1] * gv[2] - n[2] * gv[1];
+    rot[a][1] = n[2] * gv[0] - n[0] * gv[2];
+    rot[a][2] = n[0] * gv[1] - n[1] * gv[0];
+  }
+  return detJ;
+}
 
 // A dense (near-field or fallback) block of the H-matrix.
 struct DenseDesc {

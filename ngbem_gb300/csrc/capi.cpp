@@ -58,6 +58,13 @@ int bem_mesh_create(int nv, const double* xyz, int nt, const int* tri, bem_mesh_
   });
 }
 
+int bem_mesh_set_geometry(bem_mesh_t mesh, int order, const double* nodes) {
+  return guarded([&] {
+    REQUIRE(mesh, "null argument");
+    mesh->m->set_geometry(order, nodes);
+  });
+}
+
 int bem_mesh_num_edges(bem_mesh_t mesh, int* ne) {
   return guarded([&] {
     REQUIRE(mesh && ne, "null argument");

@@ -86,10 +86,72 @@ void MeshH::build(int nv_, const double* xyz, int nt_, const int* tri) {
   }
 }
 
+void MeshH::set_geometry(int order, const double* nodes) {
+  std::lock_guard<std::mutex> lk(mu);
+  if (order < 1 || order > 3) throw Error(BEM_ERR_ARG, "geometry order must be 1, 2 or 3");
+  if (order > 1 && !nodes) throw Error(BEM_ERR_ARG, "curved geometry needs its nodes");
+  if (dev_ready || !tables.empty())
+    throw Error(BEM_ERR_STATE, "the mesh is in use: curve it before creating operators on it");
+  gorder = order;
+  G.clear();
+  if (order == 1) return;
+  const size_t n = (size_t)nt * 3 * gnodes();
+  G.assign(nodes, nodes + n);
+  for (size_t k = 0; k < n; ++k)
+    if (!std::isfinite(G[k])) throw Error(BEM_ERR_ARG, "curved geometry nodes must be finite");
+  // the vertices of each element are its corner nodes
+  const int g = gorder, nn = gnodes();
+  const int corner[3] = {0, nn - (g + 1), nn - 1};  // (g,0,0), (0,g,0), (0,0,g) in node order
+  for (int e = 0; e < nt; ++e)
+    for (int k = 0; k < 3; ++k)
+      for (int c = 0; c < 3; ++c)
+        if (G[((size_t)e * nn + corner[k]) * 3 + c] != X[3 * (size_t)T[3 * e + k] + c]) {
+          gorder = 1;
+          G.clear();
+          throw Error(BEM_ERR_ARG, "curved element " + std::to_string(e) + ": corner node differs from its vertex");
+        }
+  for (int e = 0; e < nt; ++e) {
+    double x[3], n[3], rt[3][3];
+    for (int q = 0; q < 3; ++q) {
+      const double xi = q == 0 ? 1. / 3 : (q == 1 ? 0.1 : 0.8), eta = q == 0 ? 1. / 3 : 0.1;
+      if (!(frame(e, xi, eta, x, n, rt) > 0.0)) {
+        gorder = 1;
+        G.clear();
+        throw Error(BEM_ERR_ARG, "degenerate curved element " + std::to_string(e));
+      }
+    }
+  }
+}
+
 void MeshH::map(int e, double xi, double eta, double* x) const {
+  if (gorder > 1) {
+    double J0[3], J1[3];
+    curved_map(gorder, &G[(size_t)e * gnodes() * 3], xi, eta, x, J0, J1);
+    return;
+  }
   const ElemRec64& r = rec[e];
   const double l2 = 1.0 - xi - eta;
   for (int c = 0; c < 3; ++c) x[c] = xi * r.p[0][c] + eta * r.p[1][c] + l2 * r.p[2][c];
+}
+
+double MeshH::frame(int e, double xi, double eta, double* x, double* n, double rot[3][3]) const {
+  if (gorder > 1) {
+    double J0[3], J1[3];
+    curved_map(gorder, &G[(size_t)e * gnodes() * 3], xi, eta, x, J0, J1);
+    return surface_frame(J0, J1, n, rot);
+  }
+  const ElemRec64& r = rec[e];
+  map(e, xi, eta, x);
+  for (int c = 0; c < 3; ++c) n[c] = r.n[c];
+  for (int a = 0; a < 3; ++a)
+    for (int c = 0; c < 3; ++c) rot[a][c] = r.rot[a][c];
+  return r.detJ;
+}
+
+double MeshH::area(int e) const {
+  if (gorder == 1) return 0.5 * rec[e].detJ;
+  double x[3], n[3], rt[3][3];
+  return 0.5 * frame(e, 1. / 3, 1. / 3, x, n, rt);
 }
 
 void MeshH::ensure_device() {
@@ -99,17 +161,20 @@ void MeshH::ensure_device() {
   for (int e = 0; e < nt; ++e) t4[e] = make_int4(T[3 * e], T[3 * e + 1], T[3 * e + 2], 0);
   d_tri.upload(t4);
   d_rec64.upload(rec);
+  if (gorder > 1) d_gnodes.upload(G);
   BEM_CUDA(cudaDeviceSynchronize());
   dev_ready = true;
 }
 
 template <class P>
 static void build_tables(const MeshH& m, const TrigRule& r, std::vector<ElemRecP<P>>& recs,
-                         std::vector<QPt<P>>& qoff, std::vector<APt<P>>& apts, std::vector<P>& rq) {
+                         std::vector<QPt<P>>& qoff, std::vector<APt<P>>& apts, std::vector<P>& rq,
+                         std::vector<PGeo<P>>& pgeo) {
   const int nq = (int)r.w.size();
   recs.resize(m.nt);
   qoff.resize((size_t)m.nt * nq);
   apts.resize((size_t)m.nt * nq);
+  pgeo.resize(m.curved() ? (size_t)m.nt * nq : 0);
   rq.resize(2 * nq);
   for (int q = 0; q < nq; ++q) {
     rq[2 * q] = (P)r.xi[q];
@@ -134,9 +199,17 @@ static void build_tables(const MeshH& m, const TrigRule& r, std::vector<ElemRecP
       }
     d.pad[0] = d.pad[1] = d.pad[2] = (P)0;
     for (int q = 0; q < nq; ++q) {
-      double x[3];
-      m.map(e, r.xi[q], r.eta[q], x);
-      const double w = r.w[q] * s.detJ;
+      // the point, and w |J| at it (curved elements: their normal and rotated gradients too)
+      double x[3], nq3[3], rt[3][3];
+      const double detJ = m.frame(e, r.xi[q], r.eta[q], x, nq3, rt);
+      const double w = r.w[q] * detJ;
+      if (m.curved()) {
+        PGeo<P>& g = pgeo[(size_t)e * nq + q];
+        for (int c = 0; c < 3; ++c) {
+          g.n[c] = (P)nq3[c];
+          for (int a = 0; a < 3; ++a) g.rot[a][c] = (P)rt[a][c];
+        }
+      }
       QPt<P>& qo = qoff[(size_t)e * nq + q];
       qo.x = (P)(x[0] - c[0]);
       qo.y = (P)(x[1] - c[1]);
@@ -168,7 +241,9 @@ MeshH::RuleTables& MeshH::rule_tables(int order) {
     std::vector<QPt<double>> qo;
     std::vector<APt<double>> ap;
     std::vector<double> rq;
-    build_tables<double>(*this, r, recs, qo, ap, rq);
+    std::vector<PGeo<double>> pg;
+    build_tables<double>(*this, r, recs, qo, ap, rq, pg);
+    if (!pg.empty()) t->pgeo[0].upload(pg);
     t->rec[0].upload(recs);
     t->qoff[0].upload(qo);
     t->apts[0].upload(ap);
@@ -180,7 +255,9 @@ MeshH::RuleTables& MeshH::rule_tables(int order) {
     std::vector<QPt<float>> qo;
     std::vector<APt<float>> ap;
     std::vector<float> rq;
-    build_tables<float>(*this, r, recs, qo, ap, rq);
+    std::vector<PGeo<float>> pg;
+    build_tables<float>(*this, r, recs, qo, ap, rq, pg);
+    if (!pg.empty()) t->pgeo[1].upload(pg);
     t->rec[1].upload(recs);
     t->qoff[1].upload(qo);
     t->apts[1].upload(ap);

@@ -85,18 +85,30 @@ struct MeshH {
   std::vector<int> E;         // 2*ne
   std::vector<int> TE;        // 3*nt
   std::vector<ElemRec64> rec;
+  // curved geometry (gorder 2, 3): (gorder+1)(gorder+2)/2 nodes per element (curved_map)
+  int gorder = 1;
+  std::vector<double> G;
   // device tables, built on first use
   std::mutex mu;
   bool dev_ready = false;
-  DevBuf d_tri, d_rec64;
+  DevBuf d_tri, d_rec64, d_gnodes;
   struct RuleTables {
     int nq = 0;
     DevBuf rec[2], qoff[2], apts[2], rq[2];  // [0] fp64, [1] fp32
+    DevBuf pgeo[2];                          // PGeo per rule point (curved meshes)
   };
   std::map<int, std::unique_ptr<RuleTables>> tables;  // by regular order
   void build(int nv_, const double* xyz, int nt_, const int* tri);
+  // curve the elements (before any device table is built)
+  void set_geometry(int order, const double* nodes);
+  bool curved() const { return gorder > 1; }
+  int gnodes() const { return (gorder + 1) * (gorder + 2) / 2; }
   void map(int e, double xi, double eta, double* x) const;
-  double area(int e) const { return 0.5 * rec[e].detJ; }
+  // the map at (xi, eta): point, |J0 x J1|, normal and n x grad_Gamma(lambda_a)
+  double frame(int e, double xi, double eta, double* x, double* n, double rot[3][3]) const;
+  // the element's weight in the cluster data: the flat area, or |J0 x J1| / 2 at the
+  // centroid of a curved element
+  double area(int e) const;
   void ensure_device();
   RuleTables& rule_tables(int order);
 };
@@ -135,6 +147,8 @@ struct SpaceH {
 
 // device view of a space's dofs, signs and cluster positions (operator.cpp)
 SpaceDev space_dev(const SpaceH& s, int tr, const DevBuf& pinv);
+// a space and trace on a curved mesh: scalar spaces only (BEM_ERR_ARG otherwise)
+void check_curved(const MeshH& m, const SpaceH& sp, int tr);
 
 // ---- cluster tree and partition (geometry.cpp) -----------------------------------------
 struct ClusterH {

@@ -32,6 +32,7 @@ struct NFArgs {
   const void* erecP;      // ElemRecP<P>[nt]
   const void* qoff;       // QPt<P>[nt*nq]
   const void* rq;         // reference points (xi, eta) of the regular rule, P2[nq]
+  const void* pgeo;       // PGeo<P>[nt*nq] of curved meshes, else null
   int nq;
   double kappa;
   void* pool;             // dense pool, value type of the operator in storage precision
@@ -42,6 +43,8 @@ struct NFArgs {
   int* err;
   // singular kernel
   const ElemRec64* erec64;
+  const double* gnodes;   // curved meshes: the element nodes (curved_map), else null
+  int gorder;
   const double* ss[3];    // Sauter-Schwab tables: x0[n], x1[n], y0[n], y1[n], w[n]
   int ss_n[3];
   int ss_smem_bytes;      // > 0: stage all three tables in shared memory
@@ -55,6 +58,7 @@ struct AcaArgs {
   const int* patch_trial;
   const void* apts;       // APt<P>[nt*nq]
   const void* erecP;      // normals
+  const void* pgeo;       // PGeo<P>[nt*nq] of curved meshes (normals per point), else null
   int nq;
   double kappa;
   double eps;
@@ -74,6 +78,7 @@ struct ProjArgs {
   const void* erecP;
   const void* qoff;
   const void* rq;
+  const void* pgeo;       // PGeo<P>[nt*nq] of curved meshes, else null
   int nq;
   double kappa;
   SpaceDev test, trial;
@@ -247,6 +252,7 @@ struct PotArgs {
   const void* erec;       // ElemRecP<double>[nt]
   const void* qoff;       // QPt<double>[nt * nq]: rule points relative to the centroid, w * |J|
   const double* rq;       // reference points (xi, eta) of the rule
+  const void* pgeo;       // PGeo<double>[nt * nq] of curved meshes, else null
   const int* elems;       // the nt source elements (null: elements 0 .. nt-1)
   int nt, nq;
   SpaceDev trial;

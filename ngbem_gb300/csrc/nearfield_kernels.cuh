@@ -25,6 +25,15 @@ __device__ __forceinline__ int i4c(const int4& v, int a) { return a == 0 ? v.x :
 
 template <class P> struct P2 { P x, y; };
 
+// A curved element's map at (xi, eta): the point, the normal and the rotated gradients; returns
+// |J0 x J1|.
+__device__ __forceinline__ double curved_point(int g, const double* nodes, double xi, double eta, double* x,
+                                               double* n, double rot[3][3]) {
+  double J0[3], J1[3];
+  curved_map(g, nodes, xi, eta, x, J0, J1);
+  return surface_frame(J0, J1, n, rot);
+}
+
 template <int KID, class P, int TRT, int TET>
 __global__ void __launch_bounds__(128) nf_regular_kernel(NFArgs a) {
   using G = Green<KID>;
@@ -100,9 +109,13 @@ __global__ void __launch_bounds__(128) nf_regular_kernel(NFArgs a) {
   const int nq = a.nq;
   const QPt<P>* Qi = Q + (size_t)ei * nq;
   const QPt<P>* Qj = Q + (size_t)ej * nq;
+  // curved elements: normals and rotated gradients per rule point (flat: per element, above)
+  const PGeo<P>* PGi = a.pgeo ? (const PGeo<P>*)a.pgeo + (size_t)ei * nq : nullptr;
+  const PGeo<P>* PGj = a.pgeo ? (const PGeo<P>*)a.pgeo + (size_t)ej * nq : nullptr;
   for (int p = 0; p < nq; ++p) {
     const QPt<P> qi = Qi[p];
     const P2<P> rp = RQ[p];
+    if (PGi) pgeo_load<P, G::NEEDS_NX, needs_rot(TET)>(PGi[p], nx, roti);
     P xpi[3][3];
     if (edge_trace(TET)) {
 #pragma unroll
@@ -115,6 +128,7 @@ __global__ void __launch_bounds__(128) nf_regular_kernel(NFArgs a) {
       for (int b = 0; b < NDJ; ++b) ks[t][b] = vzero<V>();
     for (int q = 0; q < nq; ++q) {
       const QPt<P> qj = Qj[q];
+      if (PGj) pgeo_load<P, G::NEEDS_NY, needs_rot(TRT)>(PGj[q], ny, rotj);
       const P dx = Dx + (qi.x - qj.x), dy = Dy + (qi.y - qj.y), dz = Dz + (qi.z - qj.z);
       V kv[NC];
       G::eval(dx, dy, dz, nx, ny, kappa, kv);
@@ -172,7 +186,8 @@ __global__ void __launch_bounds__(128) nf_regular_kernel(NFArgs a) {
       }
 }
 
-template <int KID, class S, int TRT, int TET>
+// CURVED: the elements are curved (a.gnodes): the maps are evaluated per Sauter-Schwab point
+template <int KID, class S, int TRT, int TET, bool CURVED>
 __global__ void __launch_bounds__(256) nf_singular_kernel(NFArgs a) {
   using G = Green<KID>;
   using V = VT<G::CPLX, double>;
@@ -271,16 +286,25 @@ __global__ void __launch_bounds__(256) nf_singular_kernel(NFArgs a) {
         for (int q = 0; q < 3; ++q) { plx[px[q]] = lx[q]; ply[py[q]] = ly[q]; }
         xi = plx[0]; xe = plx[1]; yi = ply[0]; ye = ply[1];
       }
-      const double l2x = 1.0 - xi - xe, l2y = 1.0 - yi - ye;
       double x[3], y[3];
+      double fac;
+      if constexpr (CURVED) {
+        // curved elements: the maps, normals and rotated gradients at the two points
+        const int nn = (a.gorder + 1) * (a.gorder + 2) / 2;
+        const double dxi = curved_point(a.gorder, a.gnodes + (size_t)s.ei * nn * 3, xi, xe, x, nx, roti);
+        const double dyj = curved_point(a.gorder, a.gnodes + (size_t)s.ej * nn * 3, yi, ye, y, ny, rotj);
+        fac = dxi * dyj * w;
+      } else {
+        const double l2x = 1.0 - xi - xe, l2y = 1.0 - yi - ye;
 #pragma unroll
-      for (int c = 0; c < 3; ++c) {
-        x[c] = xi * pi[0][c] + xe * pi[1][c] + l2x * pi[2][c];
-        y[c] = yi * pj[0][c] + ye * pj[1][c] + l2y * pj[2][c];
+        for (int c = 0; c < 3; ++c) {
+          x[c] = xi * pi[0][c] + xe * pi[1][c] + l2x * pi[2][c];
+          y[c] = yi * pj[0][c] + ye * pj[1][c] + l2y * pj[2][c];
+        }
+        fac = detJ2 * w;
       }
       V kv[NC];
       G::eval(x[0] - y[0], x[1] - y[1], x[2] - y[2], nx, ny, kappa, kv);
-      const double fac = detJ2 * w;
       double xpi[3][3], xpj[3][3];
       if (edge_trace(TET)) {
 #pragma unroll
@@ -395,7 +419,10 @@ void launch_nf_singular_l2p3(int kid, int prec, const NFArgs& a, cudaStream_t s)
 
 template <int K, class S, int A, int B>
 static void run_singular(const NFArgs& a, cudaStream_t s) {
-  auto fn = nf_singular_kernel<K, S, A, B>;
+  auto fn = nf_singular_kernel<K, S, A, B, false>;
+  // curved meshes carry the scalar traces only (the operator checks it before assembly)
+  if constexpr (!edge_trace(A) && !edge_trace(B))
+    if (a.gnodes) fn = nf_singular_kernel<K, S, A, B, true>;
   int smem = a.ss_smem_bytes > 0 ? a.ss_smem_bytes : 0;
   if (smem > 48 * 1024) cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   fn<<<a.sing_grid, 256, smem, s>>>(a);

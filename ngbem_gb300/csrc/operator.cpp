@@ -62,6 +62,16 @@ struct NearPass {
   int sing_cap = 0;
 };
 
+// Curved meshes carry the scalar spaces (P0, P1, SurfaceL2 and H1 of higher order) with their
+// identity, rotated-gradient and Helmholtz traces; the Piola-mapped edge spaces (RT0, HCurl)
+// and the dual mapping are defined on flat triangles only.
+void check_curved(const MeshH& m, const SpaceH& sp, int tr) {
+  if (!m.curved()) return;
+  if (edge_trace(tr) || sp.kind == BEM_RT0 || sp.kind == BEM_HCURL)
+    throw Error(BEM_ERR_ARG, "HDivSurface / HCurl spaces need a flat mesh");
+  if (sp.dual) throw Error(BEM_ERR_ARG, "the dual mapping needs a flat mesh");
+}
+
 void HOperator::merge_meshes() {
   if (own_mesh) return;  // already merged: trial / test are the merged-mesh spaces
   trial_nt0 = trial->mesh->nt;
@@ -75,6 +85,32 @@ void HOperator::merge_meshes() {
   for (int v : b.T) T.push_back(v + a.nv);
   own_mesh = std::make_unique<MeshH>();
   own_mesh->build(a.nv + b.nv, X.data(), a.nt + b.nt, T.data());
+  if (a.curved() || b.curved()) {
+    // one geometry order for the union: a flat mesh joined to a curved one takes the curved
+    // order with its nodes on the flat triangles
+    const int g = std::max(a.gorder, b.gorder), nn = (g + 1) * (g + 2) / 2;
+    std::vector<double> G;
+    G.reserve((size_t)(a.nt + b.nt) * nn * 3);
+    for (const MeshH* m : {&a, &b})
+      for (int e = 0; e < m->nt; ++e) {
+        int n = 0;
+        for (int i = g; i >= 0; --i)
+          for (int j = g - i; j >= 0; --j, ++n) {
+            double x[3];
+            if (m->gorder == g) {
+              for (int c = 0; c < 3; ++c) x[c] = m->G[((size_t)e * nn + n) * 3 + c];
+            } else {
+              m->map(e, (double)i / g, (double)j / g, x);
+              // the corner nodes are the vertices themselves
+              const int corner = i == g ? 0 : (j == g ? 1 : (g - i - j == g ? 2 : -1));
+              if (corner >= 0)
+                for (int c = 0; c < 3; ++c) x[c] = m->X[3 * (size_t)m->T[3 * e + corner] + c];
+            }
+            G.insert(G.end(), x, x + 3);
+          }
+      }
+    own_mesh->set_geometry(g, G.data());
+  }
   std::vector<unsigned char> on_test(own_mesh->nt, 0), on_trial(own_mesh->nt, 0);
   for (int e = 0; e < a.nt; ++e) on_test[e] = test->on(e);
   for (int e = 0; e < b.nt; ++e) on_trial[a.nt + e] = trial->on(e);
@@ -96,6 +132,8 @@ void HOperator::assemble() {
   tet = trace_kind(test->kind, test_ev);
   if (trt < 0 || tet < 0) throw Error(BEM_ERR_ARG, "evaluator not available for this space");
   if (!nf_combo_supported(kid, trt, tet)) throw Error(BEM_ERR_ARG, "kernel / trace combination not supported");
+  check_curved(*trial->mesh, *trial, trt);
+  check_curved(*test->mesh, *test, tet);
   cplx = kernel_complex(kid);
   const int NC = kernel_ncomp(kid);
   prec = prm.precision == BEM_MIXED ? 1 : 0;
@@ -287,6 +325,7 @@ void HOperator::assemble() {
     a.erecP = rt.rec[prec].p;
     a.qoff = rt.qoff[prec].p;
     a.rq = rt.rq[prec].p;
+    a.pgeo = rt.pgeo[prec].p;
     a.nq = nq;
     a.kappa = kappa;
     a.pool = pool->p;
@@ -296,6 +335,8 @@ void HOperator::assemble() {
     a.sing_cap = np.sing_cap;
     a.err = np.d_err.as<int>();
     a.erec64 = mesh.d_rec64.as<ElemRec64>();
+    a.gnodes = mesh.curved() ? mesh.d_gnodes.as<double>() : nullptr;
+    a.gorder = mesh.gorder;
     for (int c = 0; c < 3; ++c) { a.ss[c] = d_ss[c].as<double>(); a.ss_n[c] = ss_n[c]; }
     a.ss_smem_bytes = ss_bytes <= 160 * 1024 ? (int)ss_bytes : 0;
     a.sing_grid = 152 * 4;
@@ -396,6 +437,7 @@ void HOperator::assemble() {
     aa.patch_trial = d_patch_trial.as<int>();
     aa.apts = rt.apts[prec].p;
     aa.erecP = rt.rec[prec].p;
+    aa.pgeo = rt.pgeo[prec].p;
     aa.nq = nq;
     aa.kappa = kappa;
     aa.eps = eps;
@@ -473,6 +515,7 @@ void HOperator::assemble() {
     pa.erecP = rt.rec[prec].p;
     pa.qoff = rt.qoff[prec].p;
     pa.rq = rt.rq[prec].p;
+    pa.pgeo = rt.pgeo[prec].p;
     pa.nq = nq;
     pa.kappa = kappa;
     pa.test = sd_test;

@@ -40,7 +40,9 @@ __global__ void pot_sources_kernel(PotArgs a) {
         rot[x][y] = Ee.rot[x][y];
         xp[x][y] = (y == 0 ? qo.x : (y == 1 ? qo.y : qo.z)) - Ee.o[x][y];
       }
-    const double nrm[3] = {Ee.n[0], Ee.n[1], Ee.n[2]};
+    double nrm[3] = {Ee.n[0], Ee.n[1], Ee.n[2]};
+    // curved elements: the normal and rotated gradients at the rule point
+    if (a.pgeo) point_geo<double>(((const PGeo<double>*)a.pgeo)[(size_t)e * a.nq + q], nrm, rot);
     int sg[SignSlots<TRT>::N];
     elem_signs<TRT>(a.trial.sign, e, sg);
     const int4 dn = a.trial.dofs[e], dx = dof_aux<TRT>(a.trial.sign, e);
@@ -59,9 +61,9 @@ __global__ void pot_sources_kernel(PotArgs a) {
     py[0] = Ee.chi[0] + Ee.clo[0] + qo.x;
     py[1] = Ee.chi[1] + Ee.clo[1] + qo.y;
     py[2] = Ee.chi[2] + Ee.clo[2] + qo.z;
-    py[3] = Ee.n[0];
-    py[4] = Ee.n[1];
-    py[5] = Ee.n[2];
+    py[3] = nrm[0];
+    py[4] = nrm[1];
+    py[5] = nrm[2];
     V* sv = (V*)a.src_val + (size_t)DIM * t;
 #pragma unroll
     for (int c = 0; c < DIM; ++c) sv[c] = val[c] * qo.w;

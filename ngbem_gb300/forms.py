@@ -28,17 +28,55 @@ def triangle_rule(order: int):
     return xi, eta, wt
 
 
+def _lagrange(order: int, xi: np.ndarray, eta: np.ndarray):
+    """Shape functions of the curved (Lagrange) element map and their xi / eta derivatives at
+    the points (xi, eta): three (nq, nn) arrays in the node order of Mesh.Curve."""
+    lam = [xi, eta, 1.0 - xi - eta]
+
+    def one(i, t):
+        v, d = np.ones_like(t), np.zeros_like(t)
+        for m in range(i):
+            f = (order * t - m) / (m + 1)
+            d = d * f + v * order / (m + 1)
+            v = v * f
+        return v, d
+    N, Dxi, Deta = [], [], []
+    for i in range(order, -1, -1):
+        for j in range(order - i, -1, -1):
+            k = order - i - j
+            (a, da), (b, db), (c, dc) = one(i, lam[0]), one(j, lam[1]), one(k, lam[2])
+            N.append(a * b * c)
+            Dxi.append(da * b * c - a * b * dc)
+            Deta.append(a * db * c - a * b * dc)
+    return np.stack(N, 1), np.stack(Dxi, 1), np.stack(Deta, 1)
+
+
 def _geometry(mesh: Mesh, order: int):
+    """Rule points x (nt, nq, 3), normals n, |J| detj, barycentrics lam (nq, 3) and weights w of
+    a triangle rule of the given order on every element.  Flat meshes: n (nt, 3) and detj (nt,)
+    per element; curved meshes (Mesh.Curve): n (nt, nq, 3) and detj (nt, nq) per point."""
     X, T = mesh.vertices, mesh.triangles
+    xi, eta, w = triangle_rule(order)
+    lam = np.stack([xi, eta, 1.0 - xi - eta], axis=1)            # (nq, 3) for (p0, p1, p2)
+    if getattr(mesh, "curve_order", 1) > 1:
+        N, Dxi, Deta = _lagrange(mesh.curve_order, xi, eta)
+        G = mesh.curve_nodes                                       # (nt, nn, 3)
+        x = np.einsum("qn,tnc->tqc", N, G)
+        n = np.cross(np.einsum("qn,tnc->tqc", Dxi, G), np.einsum("qn,tnc->tqc", Deta, G))
+        detj = np.linalg.norm(n, axis=2)
+        return x, n / detj[..., None], detj, lam, w
     p0, p1, p2 = X[T[:, 0]], X[T[:, 1]], X[T[:, 2]]
     n = np.cross(p0 - p2, p1 - p2)
     detj = np.linalg.norm(n, axis=1)
     n = n / detj[:, None]
-    xi, eta, w = triangle_rule(order)
-    lam = np.stack([xi, eta, 1.0 - xi - eta], axis=1)            # (nq, 3) for (p0, p1, p2)
     x = (lam[None, :, 0, None] * p0[:, None] + lam[None, :, 1, None] * p1[:, None]
          + lam[None, :, 2, None] * p2[:, None])                    # (nt, nq, 3)
     return x, n, detj, lam, w
+
+
+def _weights(w: np.ndarray, detj: np.ndarray) -> np.ndarray:
+    """w_q |J| per element and rule point (nt, nq)."""
+    return w[None, :] * (detj[:, None] if detj.ndim == 1 else detj)
 
 
 def p1_load_vector(mesh: Mesh, f, order: int = 6) -> np.ndarray:
@@ -50,8 +88,9 @@ def p1_load_vector(mesh: Mesh, f, order: int = 6) -> np.ndarray:
         fv = fv[..., None]
     m = fv.shape[2]
     out = np.zeros((mesh.nv, m), dtype=np.result_type(fv.dtype, np.float64))
+    W = _weights(w, detj)
     for a in range(3):
-        contrib = np.einsum("q,tqm->tm", w * lam[:, a], fv) * detj[:, None]
+        contrib = np.einsum("tq,q,tqm->tm", W, lam[:, a], fv)
         np.add.at(out, mesh.triangles[:, a], contrib)
     return out if multi else out[:, 0]
 
@@ -60,9 +99,10 @@ def p0_load_vector(mesh: Mesh, f, order: int = 6) -> np.ndarray:
     """b_e = int_{T_e} f for the piecewise-constant basis (element dofs)."""
     x, n, detj, lam, w = _geometry(mesh, order)
     fv = np.asarray(f(x, n))
+    W = _weights(w, detj)
     if fv.ndim == 3:
-        return np.einsum("q,tqm->tm", w, fv) * detj[:, None]
-    return (fv @ w) * detj
+        return np.einsum("tq,tqm->tm", W, fv)
+    return np.einsum("tq,tq->t", W, fv)
 
 
 def dubiner(p: int, lam: np.ndarray, f0: np.ndarray, f1: np.ndarray) -> np.ndarray:
@@ -112,7 +152,8 @@ def load_vector(space, f, order: int = 6) -> np.ndarray:
     integrates over the region only).  P0 / P1: f(x, n) returns (nt, nq) or (nt, nq, m)
     values.  RT0 / HCURL (the RT0 shape sigma (x - p_opp) / |J|, or n x it): f returns
     (nt, nq, 3) vectors or (nt, nq, 3, m); b_i = int f . v_i.  P0 with the dual mapping uses
-    v = 1 / |J|."""
+    v = 1 / |J|.  f receives the rule points x (nt, nq, 3) and the normals n: (nt, 3) per
+    element on flat meshes, (nt, nq, 3) per point on curved ones."""
     mesh = space.mesh
     dofs, signs = space.element_dofs()
     on = dofs[:, 0] >= 0
@@ -123,22 +164,28 @@ def load_vector(space, f, order: int = 6) -> np.ndarray:
     if not multi:
         fv = fv[..., None]
     out = np.zeros((space.ndof, fv.shape[-1]), dtype=np.result_type(fv.dtype, np.float64))
+    curved = getattr(mesh, "curve_order", 1) > 1
+    if curved and (vector or space.dual_mapping):
+        raise ValueError("HDivSurface / HCurl spaces and the dual mapping need a flat mesh")
+    W = _weights(w, detj)
     if space.kind == "P0":
-        scale = np.ones_like(detj) if space.dual_mapping else detj
-        np.add.at(out, dofs[on, 0], np.einsum("q,tqm->tm", w, fv)[on] * scale[on, None])
+        if space.dual_mapping:
+            np.add.at(out, dofs[on, 0], np.einsum("q,tqm->tm", w, fv)[on])
+        else:
+            np.add.at(out, dofs[on, 0], np.einsum("tq,tqm->tm", W, fv)[on])
     elif space.kind == "P1":
         for a in range(3):
-            np.add.at(out, dofs[on, a], (np.einsum("q,tqm->tm", w * lam[:, a], fv) * detj[:, None])[on])
+            np.add.at(out, dofs[on, a], np.einsum("tq,q,tqm->tm", W, lam[:, a], fv)[on])
     elif space.kind.startswith("H1P"):
         p = int(space.kind[3:])
         phi = h1p_shapes(p, lam, signs)  # (nt, nq, nd)
-        contrib = np.einsum("q,tqa,tqm->tam", w, phi, fv) * detj[:, None, None]
+        contrib = np.einsum("tq,tqa,tqm->tam", W, phi, fv)
         table = space.dof_table()
         np.add.at(out, table[on].ravel(), contrib[on].reshape(-1, contrib.shape[-1]))
     elif space.kind.startswith("L2P"):
         p = int(space.kind[3:])
         phi = dubiner(p, lam, signs[:, 0], signs[:, 1])  # (nt, nq, nd)
-        contrib = np.einsum("q,tqa,tqm->tam", w, phi, fv) * detj[:, None, None]
+        contrib = np.einsum("tq,tqa,tqm->tam", W, phi, fv)
         nd = phi.shape[-1]
         idx = dofs[on, 0][:, None] + np.arange(nd)[None, :]
         np.add.at(out, idx.ravel(), contrib[on].reshape(-1, contrib.shape[-1]))
@@ -161,7 +208,9 @@ def plane_wave_bm_source(kappa: float, directions: np.ndarray):
 
     def f(x, n):
         ph = np.einsum("tqc,mc->tqm", x, d)
-        dn = np.einsum("tc,mc->tm", n, d)[:, None, :]
+        dn = np.einsum("...c,mc->...m", n, d)
+        if n.ndim == 2:  # per-element normals of a flat mesh
+            dn = dn[:, None, :]
         return 1j * kappa * np.exp(1j * kappa * ph) * (dn - 1.0)
     return f
 

@@ -1,4 +1,4 @@
-"""Flat triangle surface meshes used as operator inputs.
+"""Triangle surface meshes used as operator inputs, flat or curved.
 
 NGSolve/Netgen meshes (OCC spheres, boxes) are not available here, so the operator path
 works on plain triangle meshes given as vertex coordinates and vertex triples.  The
@@ -9,6 +9,10 @@ generators below build deterministic, consistently outward-oriented meshes:
   20*4**level triangles, 10*4**level + 2 vertices.
 * ``ellipsoid(level, axes)``: the icosphere scaled by the semi-axes.
 * ``perturbed_icosphere(level, sigma, seed)``: vertices moved radially by sigma*N(0,1).
+
+``mesh.Curve(order)`` (NGSolve's ``Mesh.Curve``) makes the triangles isoparametric Lagrange
+elements of order 2 or 3 whose nodes lie on the exact surface (the generators above carry
+their surface's projection; other meshes pass ``project``).
 
 Consistent orientation matters: the common-edge Sauter-Schwab permutation assumes that
 two triangles sharing an edge traverse it in opposite directions (reference
@@ -50,7 +54,10 @@ class Mesh:
     optionally a boundary-region index per triangle (``regions``, default 0) with the regions'
     names (``region_names``, default ``["default"]``)."""
 
-    def __init__(self, vertices, triangles, regions=None, region_names=None):
+    def __init__(self, vertices, triangles, regions=None, region_names=None, project=None):
+        self.project = project
+        self.curve_order = 1
+        self.curve_nodes = None
         self.vertices = np.ascontiguousarray(vertices, dtype=np.float64)
         self.triangles = np.ascontiguousarray(triangles, dtype=np.int32)
         if self.vertices.ndim != 2 or self.vertices.shape[1] != 3:
@@ -70,6 +77,36 @@ class Mesh:
         if nt and (self.regions.min() < 0 or nreg > len(self.region_names)):
             raise ValueError("region index without a name")
 
+    def Curve(self, order: int, project=None) -> "Mesh":
+        """Curve the triangles (NGSolve's ``Mesh.Curve(order)``, in place; returns the mesh).
+
+        Order 1 keeps flat triangles.  Order 2 or 3 makes each triangle an isoparametric
+        Lagrange element: node (i, j, k), i + j + k = order, at barycentric (i, j, k) / order
+        of the triangle's vertices (v0, v1, v2), listed for i = order..0, j = order-i..0, is
+        moved to the surface by ``project`` (points (n, 3) -> points on the surface; default:
+        the projection the mesh was made with).  Nodes on a shared edge are computed from the
+        edge's two vertices alone, so neighbouring elements share them bit for bit.  Curve a
+        mesh before creating spaces on it."""
+        order = int(order)
+        if order == 1:
+            self.curve_order, self.curve_nodes = 1, None
+            return self
+        if order not in (2, 3):
+            raise ValueError("curved geometry of order 2 or 3")
+        proj = project if project is not None else self.project
+        if proj is None:
+            raise ValueError("a mesh without a surface projection needs project=")
+        idx = [(i, j, order - i - j) for i in range(order, -1, -1) for j in range(order - i, -1, -1)]
+        p = self.vertices[self.triangles]  # (nt, 3, 3)
+        nodes = np.empty((self.nt, len(idx), 3))
+        for n, (i, j, k) in enumerate(idx):
+            if order in (i, j, k):
+                nodes[:, n] = p[:, 0 if i == order else (1 if j == order else 2)]
+            else:
+                nodes[:, n] = np.asarray(proj((i * p[:, 0] + j * p[:, 1] + k * p[:, 2]) / order), dtype=np.float64)
+        self.curve_order, self.curve_nodes = order, np.ascontiguousarray(nodes)
+        return self
+
     def Boundaries(self, pattern: str) -> Region:
         """The triangles whose region name matches the regular expression ``pattern`` (as
         NGSolve's ``mesh.Boundaries("outer|inner")``)."""
@@ -85,7 +122,10 @@ class Mesh:
         vids = np.unique(self.triangles[tids])
         remap = np.full(self.nv, -1, dtype=np.int32)
         remap[vids] = np.arange(len(vids), dtype=np.int32)
-        return Mesh(self.vertices[vids], remap[self.triangles[tids]]), vids.astype(np.int32), tids
+        sub = Mesh(self.vertices[vids], remap[self.triangles[tids]], project=self.project)
+        if self.curve_order > 1:
+            sub.curve_order, sub.curve_nodes = self.curve_order, np.ascontiguousarray(self.curve_nodes[tids])
+        return sub, vids.astype(np.int32), tids
 
     @property
     def nv(self) -> int:
@@ -97,6 +137,7 @@ class Mesh:
 
     nt = ne
 
+    # areas, normals and centroids of the flat triangles (the vertices' triangles)
     def areas(self) -> np.ndarray:
         p = self.vertices[self.triangles]
         return 0.5 * np.linalg.norm(np.cross(p[:, 0] - p[:, 2], p[:, 1] - p[:, 2]), axis=1)
@@ -158,6 +199,29 @@ def _subdivide(v, f):
     return np.array(verts, dtype=np.float64), out
 
 
+class _SphereProjection:
+    """Radial projection onto the sphere of the given radius about the origin."""
+
+    def __init__(self, radius):
+        self.radius = float(radius)
+
+    def __call__(self, x):
+        x = np.asarray(x, dtype=np.float64)
+        return self.radius * x / np.linalg.norm(x, axis=-1, keepdims=True)
+
+
+class _EllipsoidProjection:
+    """Projection onto the ellipsoid sum (x_i / a_i)^2 = 1 along the rays of the scaled
+    coordinates x_i / a_i (the map of the unit sphere's radial projection)."""
+
+    def __init__(self, axes):
+        self.axes = np.asarray(axes, dtype=np.float64)
+
+    def __call__(self, x):
+        u = np.asarray(x, dtype=np.float64) / self.axes
+        return self.axes * u / np.linalg.norm(u, axis=-1, keepdims=True)
+
+
 def icosphere(level: int, radius: float = 1.0) -> Mesh:
     """Unit icosphere with 20*4**level triangles (outward normals)."""
     if level < 0:
@@ -165,13 +229,14 @@ def icosphere(level: int, radius: float = 1.0) -> Mesh:
     v, f = _icosahedron()
     for _ in range(level):
         v, f = _subdivide(v, f)
-    return Mesh(v * radius, f.astype(np.int32))
+    return Mesh(v * radius, f.astype(np.int32), project=_SphereProjection(radius))
 
 
 def ellipsoid(level: int, axes=(1.0, 0.7, 0.5)) -> Mesh:
     """Icosphere scaled by semi-axes ``axes``."""
     m = icosphere(level)
-    return Mesh(m.vertices * np.asarray(axes, dtype=np.float64)[None, :], m.triangles)
+    a = np.asarray(axes, dtype=np.float64)
+    return Mesh(m.vertices * a[None, :], m.triangles, project=_EllipsoidProjection(a))
 
 
 def perturbed_icosphere(level: int, sigma: float = 0.05, seed: int = 0) -> Mesh:

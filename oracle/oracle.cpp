@@ -194,11 +194,39 @@ struct Geo {
   double n[3];         // unit normal (J0 x J1)/detJ
 };
 
+// The element map at one reference point (the reference's MappedIntegrationPoint, through
+// mesh->GetTrafo): the point, the derivatives J0 = dx/dxi, J1 = dx/deta, |J0 x J1| and the
+// unit normal.
+struct MP {
+  double x[3], J0[3], J1[3], detJ, n[3];
+};
+
+// Curved elements (NGSolve's Mesh.Curve(order), third-party code the reference's tests call;
+// restated as isoparametric Lagrange triangles): element e of order g holds (g+1)(g+2)/2
+// nodes; node (i, j, k), i + j + k = g, sits at barycentric (i, j, k) / g of the element's
+// vertices (v0, v1, v2), and the nodes are listed for i = g..0, j = g-i..0.  The map is
+// x(xi, eta) = sum N_ijk X_ijk with N_ijk = L_i(l0) L_j(l1) L_k(l2), (l0, l1, l2) =
+// (xi, eta, 1 - xi - eta), L_i(t) = prod_{m<i} (g t - m) / (m + 1).
+static int g_geo_order = 1, g_geo_nt = 0;
+static std::vector<double> g_geo_nodes;
+
+static void lagrange_1d(int g, int i, double t, double& v, double& d) {
+  v = 1.0;
+  d = 0.0;
+  for (int m = 0; m < i; ++m) {
+    const double f = (g * t - m) / (m + 1);
+    d = d * f + v * g / (m + 1);
+    v = v * f;
+  }
+}
+
 struct Mesh {
   int nv = 0, nt = 0, ne = 0;
+  int gorder = 1;            // geometry order (1: flat triangles)
   std::vector<double> X;
   std::vector<int> T, E, TE;
   std::vector<Geo> geo;
+  std::vector<double> G;     // gorder > 1: the nodes, 3 (gorder+1)(gorder+2)/2 per element
   void build(int nv_, const double* xyz, int nt_, const int* tri) {
     nv = nv_; nt = nt_;
     X.assign(xyz, xyz + 3 * nv);
@@ -221,14 +249,64 @@ struct Mesh {
       g.detJ = std::sqrt(cr[0] * cr[0] + cr[1] * cr[1] + cr[2] * cr[2]);
       for (int c = 0; c < 3; ++c) g.n[c] = cr[c] / g.detJ;
     }
+    if (g_geo_order > 1 && g_geo_nt == nt) {
+      gorder = g_geo_order;
+      G = g_geo_nodes;
+    }
   }
-  // x = xi*p0 + eta*p1 + (1-xi-eta)*p2 (shape-function form of the affine map)
+  // the curved map and its derivatives (the sums in node order)
+  void curved(int e, double xi, double eta, double* x, double* J0, double* J1) const {
+    const int g = gorder, nn = (g + 1) * (g + 2) / 2;
+    const double l[3] = {xi, eta, 1.0 - xi - eta};
+    double L[3][4], D[3][4];
+    for (int s = 0; s < 3; ++s)
+      for (int i = 0; i <= g; ++i) lagrange_1d(g, i, l[s], L[s][i], D[s][i]);
+    for (int c = 0; c < 3; ++c) x[c] = J0[c] = J1[c] = 0.0;
+    const double* P = &G[(size_t)e * nn * 3];
+    int n = 0;
+    for (int i = g; i >= 0; --i)
+      for (int j = g - i; j >= 0; --j, ++n) {
+        const int k = g - i - j;
+        const double N = L[0][i] * L[1][j] * L[2][k];
+        const double dxi = D[0][i] * L[1][j] * L[2][k] - L[0][i] * L[1][j] * D[2][k];
+        const double deta = L[0][i] * D[1][j] * L[2][k] - L[0][i] * L[1][j] * D[2][k];
+        for (int c = 0; c < 3; ++c) {
+          x[c] += N * P[3 * n + c];
+          J0[c] += dxi * P[3 * n + c];
+          J1[c] += deta * P[3 * n + c];
+        }
+      }
+  }
+  // flat: x = xi*p0 + eta*p1 + (1-xi-eta)*p2 (shape-function form of the affine map)
   void map(int e, double xi, double eta, double* x) const {
+    if (gorder > 1) {
+      double J0[3], J1[3];
+      curved(e, xi, eta, x, J0, J1);
+      return;
+    }
     const Geo& g = geo[e];
     double l2 = 1.0 - xi - eta;
     for (int c = 0; c < 3; ++c) x[c] = xi * g.p[0][c] + eta * g.p[1][c] + l2 * g.p[2][c];
   }
-  double area(int e) const { return 0.5 * geo[e].detJ; }
+  MP mp(int e, double xi, double eta) const {
+    MP r;
+    if (gorder == 1) {
+      const Geo& g = geo[e];
+      map(e, xi, eta, r.x);
+      for (int c = 0; c < 3; ++c) { r.J0[c] = g.J0[c]; r.J1[c] = g.J1[c]; r.n[c] = g.n[c]; }
+      r.detJ = g.detJ;
+      return r;
+    }
+    curved(e, xi, eta, r.x, r.J0, r.J1);
+    const double cr[3] = {r.J0[1] * r.J1[2] - r.J0[2] * r.J1[1], r.J0[2] * r.J1[0] - r.J0[0] * r.J1[2],
+                          r.J0[0] * r.J1[1] - r.J0[1] * r.J1[0]};
+    r.detJ = std::sqrt(cr[0] * cr[0] + cr[1] * cr[1] + cr[2] * cr[2]);
+    for (int c = 0; c < 3; ++c) r.n[c] = cr[c] / r.detJ;
+    return r;
+  }
+  // the element's weight in the cluster data (the reference's SurfaceElementVolume): the
+  // flat area, or for curved elements |J0 x J1| / 2 at the centroid
+  double area(int e) const { return gorder > 1 ? 0.5 * mp(e, 1. / 3, 1. / 3).detJ : 0.5 * geo[e].detJ; }
 };
 
 // SurfaceL2 of order p >= 1 has (p+1)(p+2)/2 dofs per element (at most 10 for p = 3)
@@ -335,7 +413,7 @@ static void cross3(const double* a, const double* b, double* c) {
 // (DiffOpMaxwell :172-255) with the surface curl of phi = div psi = 2 sigma / |J|.
 static void eval_trace(const Mesh& m, const Space& sp, int ev, int e, double xi, double eta,
                        double S[ORC_MAXND][4]) {
-  const Geo& g = m.geo[e];
+  const MP g = m.mp(e, xi, eta);
   if (sp.kind == ORC_P0) {
     S[0][0] = sp.dual ? 1.0 / g.detJ : 1.0;
     return;
@@ -784,8 +862,6 @@ struct Operator {
     int di = trace_dim(test.kind, test_ev), dj = trace_dim(trial.kind, trial_ev);
     int ndi = test.nd, ndj = trial.nd;
     (void)di; (void)dj;
-    const Geo& gi = mesh.geo[ei];
-    const Geo& gj = mesh.geo[ej];
     const size_t npts = r.w.size();
     for (size_t k = 0; k < npts; ++k) {
       double xi, xe, yi, ye;
@@ -797,11 +873,9 @@ struct Operator {
         for (int q = 0; q < 3; ++q) { plamx[vpermx[q]] = lamx[q]; plamy[vpermy[q]] = lamy[q]; }
         xi = plamx[0]; xe = plamx[1]; yi = plamy[0]; ye = plamy[1];
       }
-      double x[3], y[3];
-      mesh.map(ei, xi, xe, x);
-      mesh.map(ej, yi, ye, y);
+      const MP gi = mesh.mp(ei, xi, xe), gj = mesh.mp(ej, yi, ye);
       T kv[3];
-      kernel.eval<T>(x, y, gi.n, gj.n, kv);
+      kernel.eval<T>(gi.x, gj.x, gi.n, gj.n, kv);
       double fac = gi.detJ * gj.detJ * r.w[k];
       for (int c = 0; c < kernel.ncomp; ++c) kv[c] = fac * kv[c];
       double Si[ORC_MAXND][4], Sj[ORC_MAXND][4];
@@ -840,19 +914,17 @@ struct Operator {
       for (int q = 0; q < nq; ++q)
         eval_trace(mesh, trial, trial_ev, patchj[j], irtrig.xi[q], irtrig.eta[q],
                    reinterpret_cast<double(*)[4]>(&shj[(j * nq + q) * 4 * ORC_MAXND]));
-    std::vector<double> pxi((size_t)patchi.size() * nq * 4), pyj((size_t)patchj.size() * nq * 4);
+    // per rule point: x, w |J|, the unit normal
+    std::vector<double> pxi((size_t)patchi.size() * nq * 7), pyj((size_t)patchj.size() * nq * 7);
+    auto point = [&](int e, int q, double* P) {
+      const MP g = mesh.mp(e, irtrig.xi[q], irtrig.eta[q]);
+      for (int c = 0; c < 3; ++c) { P[c] = g.x[c]; P[4 + c] = g.n[c]; }
+      P[3] = irtrig.w[q] * g.detJ;
+    };
     for (size_t i = 0; i < patchi.size(); ++i)
-      for (int q = 0; q < nq; ++q) {
-        double* P = &pxi[(i * nq + q) * 4];
-        mesh.map(patchi[i], irtrig.xi[q], irtrig.eta[q], P);
-        P[3] = irtrig.w[q] * mesh.geo[patchi[i]].detJ;
-      }
+      for (int q = 0; q < nq; ++q) point(patchi[i], q, &pxi[(i * nq + q) * 7]);
     for (size_t j = 0; j < patchj.size(); ++j)
-      for (int q = 0; q < nq; ++q) {
-        double* P = &pyj[(j * nq + q) * 4];
-        mesh.map(patchj[j], irtrig.xi[q], irtrig.eta[q], P);
-        P[3] = irtrig.w[q] * mesh.geo[patchj[j]].detJ;
-      }
+      for (int q = 0; q < nq; ++q) point(patchj[j], q, &pyj[(j * nq + q) * 7]);
     std::vector<T> kern((size_t)nq * nq), ks((size_t)nq * ndj);
     T elmat[ORC_MAXND * ORC_MAXND];
     for (size_t i = 0; i < patchi.size(); ++i)
@@ -896,15 +968,13 @@ struct Operator {
           integrate4d(ei, ej, ss[2], vpermx, vpermy, false, elmat);
         } else {
           // disjoint panels, src/ngbem.cpp:680-727
-          const double* nx = mesh.geo[ei].n;
-          const double* ny = mesh.geo[ej].n;
           for (const Term& t : kernel.terms) {
             for (int ix = 0; ix < nq; ++ix)
               for (int iy = 0; iy < nq; ++iy) {
-                const double* X = &pxi[(i * nq + ix) * 4];
-                const double* Y = &pyj[(j * nq + iy) * 4];
+                const double* X = &pxi[(i * nq + ix) * 7];
+                const double* Y = &pyj[(j * nq + iy) * 7];
                 T kv[3];
-                kernel.eval<T>(X, Y, nx, ny, kv);
+                kernel.eval<T>(X, Y, X + 4, Y + 4, kv);
                 double fac = X[3] * Y[3];
                 kern[ix * nq + iy] = t.fac * fac * kv[t.kc];
               }
@@ -959,16 +1029,16 @@ struct Operator {
     for (size_t i = 0; i < patchi.size(); ++i)
       for (int q = 0; q < nq; ++q) {
         size_t r = i * nq + q;
-        mesh.map(patchi[i], irtrig.xi[q], irtrig.eta[q], &xi[3 * r]);
-        for (int c = 0; c < 3; ++c) nxi[3 * r + c] = mesh.geo[patchi[i]].n[c];
-        wxi[r] = irtrig.w[q] * mesh.geo[patchi[i]].detJ;
+        const MP g = mesh.mp(patchi[i], irtrig.xi[q], irtrig.eta[q]);
+        for (int c = 0; c < 3; ++c) { xi[3 * r + c] = g.x[c]; nxi[3 * r + c] = g.n[c]; }
+        wxi[r] = irtrig.w[q] * g.detJ;
       }
     for (size_t j = 0; j < patchj.size(); ++j)
       for (int q = 0; q < nq; ++q) {
         size_t r = j * nq + q;
-        mesh.map(patchj[j], irtrig.xi[q], irtrig.eta[q], &yj[3 * r]);
-        for (int c = 0; c < 3; ++c) nyj[3 * r + c] = mesh.geo[patchj[j]].n[c];
-        wyj[r] = irtrig.w[q] * mesh.geo[patchj[j]].detJ;
+        const MP g = mesh.mp(patchj[j], irtrig.xi[q], irtrig.eta[q]);
+        for (int c = 0; c < 3; ++c) { yj[3 * r + c] = g.x[c]; nyj[3 * r + c] = g.n[c]; }
+        wyj[r] = irtrig.w[q] * g.detJ;
       }
     const size_t p = std::min(M, N);
     auto getrow = [&](size_t i, T* row, int comp) {
@@ -1410,11 +1480,10 @@ static void potential_t(int kernel, double kappa, const Mesh& m, const Space& sp
         T vals[4] = {T(0), T(0), T(0), T(0)};
         for (int a = 0; a < sp.nd; ++a)
           for (int c = 0; c < dim; ++c) vals[c] += density[sp.el_dofs(e)[a]] * S[a][c];
-        double y[3];
-        m.map(e, r.xi[q], r.eta[q], y);
-        const double w = r.w[q] * m.geo[e].detJ;
+        const MP g = m.mp(e, r.xi[q], r.eta[q]);
+        const double w = r.w[q] * g.detJ;
         T kv[3];
-        K.eval<T>(x, y, nx, m.geo[e].n, kv);
+        K.eval<T>(x, g.x, nx, g.n, kv);
         for (const Term& t : K.terms) out[(size_t)p * dim + t.tec] += w * kv[t.kc] * vals[t.trc];
       }
     }
@@ -1434,6 +1503,15 @@ int orc_potential(int kernel, double kappa, int nv, const double* xyz, int nt, c
                       (cplx*)out);
   else
     potential_t<double>(kernel, kappa, m, sp, trial_eval, intorder, density, npts, pts, normals, out);
+  return 0;
+}
+
+int orc_set_geometry(int order, int nt, const double* nodes) {
+  if (order < 1 || order > 3 || nt < 0 || (order > 1 && !nodes)) return -1;
+  g_geo_order = order;
+  g_geo_nt = nt;
+  if (order == 1) g_geo_nodes.clear();
+  else g_geo_nodes.assign(nodes, nodes + (size_t)nt * 3 * (order + 1) * (order + 2) / 2);
   return 0;
 }
 
@@ -1462,7 +1540,7 @@ int orc_mass_matrix(int nv, const double* xyz, int nt, const int* tri, int trial
       double Si[ORC_MAXND][4], Sj[ORC_MAXND][4];
       eval_trace(m, te, evte, e, r.xi[q], r.eta[q], Si);
       eval_trace(m, tr, evtr, e, r.xi[q], r.eta[q], Sj);
-      double w = r.w[q] * m.geo[e].detJ;
+      double w = r.w[q] * m.mp(e, r.xi[q], r.eta[q]).detJ;
       for (int a = 0; a < te.nd; ++a)
         for (int b = 0; b < tr.nd; ++b) {
           double s = 0;

@@ -64,6 +64,13 @@ typedef struct {
 // in order and local edges (0,1),(1,2),(2,0).  Returns the number of edges.
 int orc_mesh_edges(int nv, int nt, const int* tri, int* edges /*2*3nt*/, int* tri_edges /*3nt*/);
 
+// Geometry of the meshes that the following calls build (a setting of the library, kept until
+// the next call): order 1 flat triangles; order 2, 3 isoparametric Lagrange triangles with
+// nodes[nt][(order+1)(order+2)/2][3], node (i, j, k) (i + j + k = order) at barycentric
+// (i, j, k) / order of the element's vertices, listed for i = order..0, j = order-i..0.  A
+// mesh with another element count is built flat.  Returns 0, or -1 for a bad order.
+int orc_set_geometry(int order, int nt, const double* nodes);
+
 // Trace values of the local dofs of element e at (xi, eta) (for known-answer tests):
 // out[4 a + c] component c of local dof a, dofs[a] its global dof; returns the dofs per element.
 int orc_eval_trace(int nv, const double* xyz, int nt, const int* tri, int kind, int ev, int e, double xi,

@@ -42,6 +42,7 @@ def lib():
         dp, ip, lp = C.POINTER(C.c_double), C.POINTER(C.c_int), C.POINTER(C.c_long)
         L.orc_mesh_edges.argtypes = [C.c_int, C.c_int, ip, ip, ip]
         L.orc_trig_rule.argtypes = [C.c_int, dp, dp, dp]
+        L.orc_set_geometry.argtypes = [C.c_int, C.c_int, dp]
         L.orc_eval_trace.argtypes = [C.c_int, dp, C.c_int, ip, C.c_int, C.c_int, C.c_int, C.c_double, C.c_double,
                                      dp, ip]
         L.orc_ss_rule.argtypes = [C.c_int, C.c_int, dp, dp, dp, dp, dp]
@@ -101,8 +102,21 @@ def ss_rule(cls, order):
     return [x[:k] for x in a]
 
 
+def _geometry(mesh):
+    """Set the oracle's geometry to the mesh's: flat, or its curved nodes (Mesh.Curve)."""
+    order = int(getattr(mesh, "curve_order", 1))
+    if order > 1:
+        nodes = np.ascontiguousarray(mesh.curve_nodes, dtype=np.float64)
+        rc = lib().orc_set_geometry(order, mesh.nt, _dp(nodes))
+    else:
+        rc = lib().orc_set_geometry(1, 0, None)
+    if rc != 0:
+        raise ValueError("bad geometry order")
+
+
 def eval_trace(mesh, kind, ev, e, xi, eta):
     """(values (nd, 4), dofs (nd,)): the trace values of element e's local dofs at (xi, eta)."""
+    _geometry(mesh)
     X = np.ascontiguousarray(mesh.vertices, dtype=np.float64)
     T = np.ascontiguousarray(mesh.triangles, dtype=np.int32)
     out = np.zeros(40)
@@ -135,6 +149,7 @@ def cluster_tree(mesh, kind, leafsize):
     cd = np.zeros(23 * maxc, dtype=np.float64)
     X = np.ascontiguousarray(mesh.vertices, dtype=np.float64)
     T = np.ascontiguousarray(mesh.triangles, dtype=np.int32)
+    _geometry(mesh)
     nc = lib().orc_cluster_tree(mesh.nv, _dp(X), mesh.nt, _ip(T), KINDS[kind], leafsize,
                                 _ip(perm), maxc, _lp(ci), _dp(cd))
     if nc < 0:
@@ -161,6 +176,7 @@ class OracleOperator:
                          leafsize, eta, eps, nthreads)
         self.X = np.ascontiguousarray(mesh.vertices, dtype=np.float64)
         self.T = np.ascontiguousarray(mesh.triangles, dtype=np.int32)
+        _geometry(mesh)
         self.h = lib().orc_operator_create(KERNELS[kernel], float(kappa), mesh.nv, _dp(self.X),
                                            mesh.nt, _ip(self.T), KINDS[trial], EVALS[trial_eval],
                                            int(trial_dual), KINDS[test], EVALS[test_eval],
@@ -209,6 +225,7 @@ def dense_matrix(kernel, mesh, trial="P0", test=None, kappa=0.0, trial_eval="id"
     H, W = ndof(mesh, test), ndof(mesh, trial)
     dt = np.complex128 if KERNELS[kernel] >= 3 else np.float64
     out = np.zeros((H, W), dtype=dt)
+    _geometry(mesh)
     lib().orc_dense_matrix(KERNELS[kernel], float(kappa), mesh.nv, _dp(X), mesh.nt, _ip(T),
                            KINDS[trial], EVALS[trial_eval], int(trial_dual), KINDS[test],
                            EVALS[test_eval], int(test_dual), C.byref(p), _dp(out.view(np.float64)))
@@ -229,6 +246,7 @@ def potential(kernel, mesh, trial, density, points, normals=None, kappa=0.0, tri
     else:
         dim = 3 if trial_eval in ("rot", "rotatedtrace") else 4
     out = np.zeros((P.shape[0], dim), dtype=dens.dtype)
+    _geometry(mesh)
     lib().orc_potential(KERNELS[kernel], float(kappa), mesh.nv, _dp(X), mesh.nt, _ip(T), KINDS[trial],
                         EVALS[trial_eval], int(trial_dual), int(intorder), _dp(dens.view(np.float64)), P.shape[0],
                         _dp(P), None if Nn is None else _dp(Nn), _dp(out.view(np.float64)))
@@ -239,5 +257,6 @@ def mass_matrix(mesh, trial="P1", test="P0", order=4):
     X = np.ascontiguousarray(mesh.vertices, dtype=np.float64)
     T = np.ascontiguousarray(mesh.triangles, dtype=np.int32)
     out = np.zeros((ndof(mesh, test), ndof(mesh, trial)))
+    _geometry(mesh)
     lib().orc_mass_matrix(mesh.nv, _dp(X), mesh.nt, _ip(T), KINDS[trial], KINDS[test], order, _dp(out))
     return out

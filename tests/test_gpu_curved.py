@@ -1,0 +1,178 @@
+"""Curved geometry on the GPU against the FP64 oracle (Mesh.Curve, order 2 and 3; the
+reference's tests curve every mesh: tests/test_aca.py:7, tests/test_SLIntegration.py:28,
+tests/test_Laplace.py:25).
+
+* Dense FP64 operators within 1e-10 of the oracle's dense matrices for the scalar spaces and
+  their traces (identity, rotated gradient, Helmholtz), with the Sauter-Schwab points mapped
+  through the curved elements.
+* FP64 H-matrices within the ACA tolerance of the oracle's H-matrices in both directions, with
+  the same block lists; mixed precision within 1e-6 of FP64.
+* Potentials and mass matrices against the oracle.
+* The reference's ACA test (tests/test_aca.py:21-28) and its single-layer integration test
+  (tests/test_SLIntegration.py:30-40) on curved meshes.
+* The interior Dirichlet-to-Neumann map on the curved sphere: the error of the flat triangles
+  (O(h^2)) is gone.
+* Spaces that need flat triangles are refused at assembly; a mesh in use cannot be curved.
+"""
+import numpy as np
+import pytest
+import torch
+
+import ngbem_gb300 as nb
+from ngbem_gb300 import bem
+from ngbem_gb300._lib import BEM_ERR_ARG, BemError
+from ngbem_gb300.forms import load_vector
+from ngbem_gb300.meshes import ellipsoid, icosphere
+
+pytestmark = pytest.mark.gpu
+
+# (kernel, kappa, trial kind, test kind, trial evaluator, test evaluator)
+COMBOS = [("laplace_sl", 0.0, "P0", "P0", "id", "id"), ("laplace_dl", 0.0, "P1", "P0", "id", "id"),
+          ("laplace_hs", 0.0, "P1", "P1", "rot", "rot"), ("helmholtz_cf", 4.0, "P1", "P1", "id", "id"),
+          ("helmholtz_hs", 3.0, "P1", "P1", "helm", "helm"), ("laplace_sl", 0.0, "L2P2", "L2P2", "id", "id"),
+          ("laplace_dl", 0.0, "H1P3", "L2P2", "id", "id"), ("laplace_hs", 0.0, "H1P3", "H1P3", "rot", "rot"),
+          ("helmholtz_dl", 3.0, "H1P2", "H1P2", "id", "id")]
+IDS = [f"{c[0]}-{c[2]}-{c[3]}" for c in COMBOS]
+
+
+def rel(a, b):
+    return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+
+def _space(mesh, kind):
+    return nb.TraceSpace(mesh, kind)
+
+
+def _op(kernel, kappa, mesh, tr, te, ev_tr, ev_te, method="aca", precision="fp64", **kw):
+    prm = dict(intorder=3, leafsize=40, eta=2.0, eps=1e-8)
+    prm.update(kw)
+    io = prm.pop("intorder")
+    s_tr, s_te = _space(mesh, tr), _space(mesh, te)
+    op = bem.IntegralOperator(kernel, kappa, s_tr, s_te, ev_tr, ev_te, io, prm.pop("leafsize"), prm.pop("eta"),
+                              prm.pop("eps"), method, False, precision=precision, **prm)
+    return op, s_tr, s_te
+
+
+@pytest.mark.parametrize("g", [2, 3])
+@pytest.mark.parametrize("kernel,kappa,tr,te,ev_tr,ev_te", COMBOS, ids=IDS)
+def test_dense_parity(oracle, kernel, kappa, tr, te, ev_tr, ev_te, g):
+    m = icosphere(1).Curve(g)
+    op, s_tr, s_te = _op(kernel, kappa, m, tr, te, ev_tr, ev_te, "dense", intorder_singular=4,
+                         intorder_regular=3)
+    D = op.mat.to_dense()
+    Do = oracle.dense_matrix(kernel, m, tr, te, kappa=kappa, trial_eval=ev_tr, test_eval=ev_te,
+                             intorder_singular=4, intorder_regular=3)
+    assert D.shape == (s_te.ndof, s_tr.ndof)
+    assert rel(D, Do) < 1e-10
+    # the curved operator is not the flat one
+    flat, _, _ = _op(kernel, kappa, icosphere(1), tr, te, ev_tr, ev_te, "dense", intorder_singular=4,
+                     intorder_regular=3)
+    assert rel(flat.mat.to_dense(), Do) > 1e-4
+
+
+@pytest.mark.parametrize("kernel,kappa,tr,te,ev_tr,ev_te", [COMBOS[0], COMBOS[3], COMBOS[7]],
+                         ids=[IDS[0], IDS[3], IDS[7]])
+def test_hmatrix_parity(oracle, kernel, kappa, tr, te, ev_tr, ev_te):
+    m = ellipsoid(3 if tr in ("P0", "P1") else 2, (1.0, 0.8, 0.6)).Curve(3)
+    op, s_tr, s_te = _op(kernel, kappa, m, tr, te, ev_tr, ev_te)
+    H = oracle.OracleOperator(kernel, m, tr, te, kappa=kappa, trial_eval=ev_tr, test_eval=ev_te, intorder=3,
+                              leafsize=40, eta=2.0, eps=1e-8)
+    b, ob = op.mat.blocks(), H.blocks()
+    for k in ("rowcl", "colcl", "near"):
+        assert np.array_equal(b[k], ob[k])
+    cplx = kappa != 0.0
+    rng = np.random.default_rng(23)
+    dt = torch.complex128 if cplx else torch.float64
+    x = rng.standard_normal(s_tr.ndof) + (1j * rng.standard_normal(s_tr.ndof) if cplx else 0.0)
+    y = (op.mat * torch.from_numpy(x).to(dt).cuda()).cpu().numpy()
+    assert rel(y, H.mult(x)) < 1e-7
+    z = rng.standard_normal(s_te.ndof) + (1j * rng.standard_normal(s_te.ndof) if cplx else 0.0)
+    yt = op.mat.CreateRowVector()
+    op.mat.MultTrans(torch.from_numpy(z).to(dt).cuda(), yt)
+    assert rel(yt.cpu().numpy(), H.mult(z, trans=True)) < 1e-7
+    o32, _, _ = _op(kernel, kappa, m, tr, te, ev_tr, ev_te, precision="mixed")
+    xd = torch.from_numpy(x).to(dt).cuda()
+    assert rel((o32.mat * xd).cpu().numpy(), y) < 1e-6
+
+
+@pytest.mark.parametrize("kind", ["P1", "H1P3"])
+def test_potential_and_mass(oracle, kind):
+    m = icosphere(2).Curve(3)
+    sp = _space(m, kind)
+    dens = np.random.default_rng(13).standard_normal(sp.ndof)
+    pts = np.array([[2.0, 0.3, -0.1], [0.1, 0.2, 0.3], [-1.5, 1.0, 0.5]])
+    for kernel in ("laplace_sl", "laplace_dl"):
+        op, _, _ = _op(kernel, 0.0, m, kind, kind, "id", "id")
+        val = op.GetPotential(torch.from_numpy(dens).cuda())(pts).cpu().numpy().reshape(len(pts), -1)
+        ref = oracle.potential(kernel, m, kind, dens, pts, intorder=3).reshape(len(pts), -1)
+        assert rel(val, ref) < 1e-11
+    M = nb.MassOperator(sp, sp)
+    y = (M * torch.from_numpy(dens).cuda()).cpu().numpy()
+    order = 4 if kind == "P1" else 6
+    assert rel(y, oracle.mass_matrix(m, kind, kind, order=order) @ dens) < 1e-12
+
+
+def test_reference_aca_pattern():
+    """tests/test_aca.py on a curved mesh: Curve(3), SurfaceL2 of order 3, the ACA product
+    within eps of the dense one."""
+    m = ellipsoid(2, (1.0, 0.8, 0.6)).Curve(3)
+    eps = 1e-6
+    Vd, sp, _ = _op("laplace_sl", 0.0, m, "L2P3", "L2P3", "id", "id", "dense", intorder=10)
+    Va, _, _ = _op("laplace_sl", 0.0, m, "L2P3", "L2P3", "id", "id", intorder=10, leafsize=40, eta=3.0, eps=eps)
+    x = torch.from_numpy(np.random.default_rng(4711).standard_normal(sp.ndof)).cuda()
+    yd, ya = Vd.mat * x, Va.mat * x
+    assert (torch.linalg.vector_norm(yd - ya) / torch.linalg.vector_norm(yd)).item() < eps
+    assert Va.mat.nze < Vd.mat.nze
+
+
+def test_reference_sl_integration_pattern():
+    """tests/test_SLIntegration.py on a curved mesh (Curve(2), SurfaceL2 of order 3): the dense
+    single layer converges to the high-order one as the integration order grows."""
+    m = icosphere(1).Curve(2)
+    ref, _, _ = _op("laplace_sl", 0.0, m, "L2P3", "L2P3", "id", "id", "dense", intorder=20)
+    R = ref.mat.to_dense()
+    errs = []
+    for io in (4, 6, 8, 10):
+        a, _, _ = _op("laplace_sl", 0.0, m, "L2P3", "L2P3", "id", "id", "dense", intorder=io)
+        errs.append(rel(a.mat.to_dense(), R))
+    assert errs[-1] < 1e-6
+    assert all(e2 < e1 for e1, e2 in zip(errs, errs[1:]))
+
+
+def _dtn_error(mesh, oracle):
+    h1 = nb.H1(mesh, order=3)
+    l2 = nb.SurfaceL2(mesh, order=2)
+    V = nb.SingleLayerPotentialOperator(l2, intorder=7, eps=1e-10)
+    K = nb.DoubleLayerPotentialOperator(h1, l2, intorder=7, eps=1e-10)
+    M = nb.MassOperator(h1, l2)
+
+    def g(x, n):
+        return x[..., 0] ** 2 - x[..., 1] ** 2
+
+    gh = np.linalg.solve(oracle.mass_matrix(mesh, "H1P3", "H1P3", order=8), load_vector(h1, g, order=10))
+    ghd = torch.from_numpy(gh).cuda()
+    rhs = 0.5 * (M * ghd) + K.mat * ghd
+    u = nb.GMRes(A=V.mat, b=rhs, tol=1e-11, maxsteps=400, printrates=False)
+    u = u.cpu().numpy() if isinstance(u, torch.Tensor) else np.asarray(u)
+    Ml2 = oracle.mass_matrix(mesh, "L2P2", "L2P2", order=8)
+    c = np.linalg.solve(Ml2, load_vector(l2, lambda x, n: 2.0 * g(x, n), order=10))
+    e = u - c
+    return float(np.sqrt(e @ Ml2 @ e / (c @ Ml2 @ c)))
+
+
+def test_dirichlet_to_neumann_on_the_curved_sphere(oracle):
+    """g = x^2 - y^2 on the unit sphere has the interior Neumann data 2 g: on flat triangles the
+    error stalls at the geometry's O(h^2); with Curve(3) it is far smaller."""
+    flat = _dtn_error(icosphere(2), oracle)
+    curved = _dtn_error(icosphere(2).Curve(3), oracle)
+    assert curved < 0.1 * flat
+    assert curved < 5e-3
+
+
+def test_flat_only_spaces_and_curving_in_use():
+    m = icosphere(1).Curve(2)
+    with pytest.raises(BemError) as ei:
+        nb.MaxwellSingleLayerPotentialOperator(nb.HDivSurface(m, complex=True), 1.0, intorder=3)
+    assert ei.value.code == BEM_ERR_ARG
+    with pytest.raises(BemError):
+        nb.SingleLayerPotentialOperator(nb.TraceSpace(m, "P0", dual_mapping=True), intorder=3)
