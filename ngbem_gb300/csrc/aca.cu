@@ -388,11 +388,12 @@ __global__ void __launch_bounds__(256) aca_project_kernel(ProjArgs a) {
         const P2_<P> rp = RQ[q];
         P xp[3][3];
         for (int x = 0; x < 3; ++x) { xp[x][0] = qo.x - o[x][0]; xp[x][1] = qo.y - o[x][1]; xp[x][2] = qo.z - o[x][2]; }
-        if (PG) point_geo<P>(PG[(size_t)e * nq + q], nrm, rot);
+        P inv = Ee.invdetJ;
+        if (PG) point_geo<P>(PG[(size_t)e * nq + q], nrm, rot, inv, xp);
         const V u = Us[(size_t)kk * M + ie * nq + q] * qo.w;
 #pragma unroll
         for (int x = 0; x < NDI; ++x)
-          acc[x] += u * trace_val<TET, P>(x, G::tec(t), rp.x, rp.y, xp, Ee.invdetJ, rot, sg[x], a.test.dual != 0, nrm);
+          acc[x] += u * trace_val<TET, P>(x, G::tec(t), rp.x, rp.y, xp, inv, rot, sg[x], a.test.dual != 0, nrm);
       }
       const int4 dn = a.test.dofs[e], dx = dof_aux<TET>(a.test.sign, e);
 #pragma unroll
@@ -419,11 +420,12 @@ __global__ void __launch_bounds__(256) aca_project_kernel(ProjArgs a) {
         const P2_<P> rp = RQ[q];
         P xp[3][3];
         for (int x = 0; x < 3; ++x) { xp[x][0] = qo.x - o[x][0]; xp[x][1] = qo.y - o[x][1]; xp[x][2] = qo.z - o[x][2]; }
-        if (PG) point_geo<P>(PG[(size_t)e * nq + q], nrm, rot);
+        P inv = Ee.invdetJ;
+        if (PG) point_geo<P>(PG[(size_t)e * nq + q], nrm, rot, inv, xp);
         const V v = Vs[(size_t)kk * N + je * nq + q] * qo.w;
 #pragma unroll
         for (int x = 0; x < NDJ; ++x)
-          acc[x] += v * trace_val<TRT, P>(x, G::trc(t), rp.x, rp.y, xp, Ee.invdetJ, rot, sg[x], a.trial.dual != 0, nrm);
+          acc[x] += v * trace_val<TRT, P>(x, G::trc(t), rp.x, rp.y, xp, inv, rot, sg[x], a.trial.dual != 0, nrm);
       }
       const int4 dn = a.trial.dofs[e], dx = dof_aux<TRT>(a.trial.sign, e);
 #pragma unroll

@@ -355,8 +355,6 @@ void HOperator::to_dense(void* out) {
 void MassOperator::build(SpaceH* trial, SpaceH* test, bool complex_vectors) {
   if (trial->mesh != test->mesh) throw Error(BEM_ERR_ARG, "mass matrix needs one mesh");
   MeshH& m = *trial->mesh;
-  check_curved(m, *trial, TR_P0);
-  check_curved(m, *test, TR_P0);
   cplx = complex_vectors;
   nrows = test->ndof;
   ncols = trial->ndof;
@@ -373,9 +371,31 @@ void MassOperator::build(SpaceH* trial, SpaceH* test, bool complex_vectors) {
   TrigRule r = make_trig_rule(std::max(4, degree(*trial) + degree(*test)));
   const int nq = (int)r.w.size();
   std::vector<std::vector<std::pair<int, double>>> rows(nrows);
-  auto shape = [&](const SpaceH& sp, int e, double xi, double eta, double S[10][3], int& dim) {
+  // curved elements: 1 / |J|, the normal and the Piola offsets at the point (flat: per element)
+  auto piola = [&](int e, double xi, double eta, double& inv, double* n, double xp[3][3]) {
     const ElemRec64& g = m.rec[e];
-    if (sp.kind == BEM_P0) { S[0][0] = sp.dual ? g.invdetJ : 1.0; dim = 1; return; }
+    if (!m.curved()) {
+      double x[3];
+      m.map(e, xi, eta, x);
+      inv = g.invdetJ;
+      for (int c = 0; c < 3; ++c) {
+        n[c] = g.n[c];
+        for (int o = 0; o < 3; ++o) xp[o][c] = x[c] - g.p[o][c];
+      }
+      return;
+    }
+    double x[3], rt[3][3], J0[3], J1[3];
+    inv = 1.0 / m.frame(e, xi, eta, x, n, rt, J0, J1);
+    piola_offsets(J0, J1, xi, eta, xp);
+  };
+  auto shape = [&](const SpaceH& sp, int e, double xi, double eta, double S[10][3], int& dim) {
+    double inv, n[3], xp[3][3];
+    if (sp.kind == BEM_P0) {
+      if (sp.dual) piola(e, xi, eta, inv, n, xp);
+      S[0][0] = sp.dual ? inv : 1.0;
+      dim = 1;
+      return;
+    }
     if (sp.kind == BEM_H1P2 || sp.kind == BEM_H1P3) {
       // vertex hats, edge bubbles (orientation sign to the power m), face bubble
       const int P = sp.kind == BEM_H1P2 ? 2 : 3;
@@ -396,15 +416,14 @@ void MassOperator::build(SpaceH* trial, SpaceH* test, bool complex_vectors) {
       return;
     }
     if (sp.kind == BEM_P1) { S[0][0] = xi; S[1][0] = eta; S[2][0] = 1.0 - xi - eta; dim = 1; return; }
-    double x[3];
-    m.map(e, xi, eta, x);
+    piola(e, xi, eta, inv, n, xp);
     for (int a = 0; a < 3; ++a) {
       const int o = (a + 2) % 3;
       double v[3];
-      for (int c = 0; c < 3; ++c) v[c] = sp.sign[3 * e + a] * (x[c] - g.p[o][c]) * g.invdetJ;
+      for (int c = 0; c < 3; ++c) v[c] = sp.sign[3 * e + a] * xp[o][c] * inv;
       // HCurl trace: n x the RT0 shape of the same edge
       for (int c = 0; c < 3; ++c)
-        S[a][c] = sp.kind == BEM_HCURL ? g.n[(c + 1) % 3] * v[(c + 2) % 3] - g.n[(c + 2) % 3] * v[(c + 1) % 3] : v[c];
+        S[a][c] = sp.kind == BEM_HCURL ? n[(c + 1) % 3] * v[(c + 2) % 3] - n[(c + 2) % 3] * v[(c + 1) % 3] : v[c];
     }
     dim = 3;
   };

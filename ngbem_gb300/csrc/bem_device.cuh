@@ -328,20 +328,30 @@ template <> struct TraceInfo<TR_H1P3ROT> { static constexpr int ND = 10, DIM = 3
 template <> struct TraceInfo<TR_H1P2HELM> { static constexpr int ND = 6, DIM = 4; };
 template <> struct TraceInfo<TR_H1P3HELM> { static constexpr int ND = 10, DIM = 4; };
 // traces that read the element's n x grad(lambda_a) table
-// the geometry of a curved element's rule point (PGeo): normal and rotated gradients
+// the geometry of a curved element's rule point (PGeo): normal, rotated gradients, 1 / |J| and
+// the Piola offsets
 template <class P>
-__device__ __forceinline__ void point_geo(const PGeo<P>& g, P n[3], P rot[3][3]) {
+__device__ __forceinline__ void point_geo(const PGeo<P>& g, P n[3], P rot[3][3], P& inv, P xp[3][3]) {
+  inv = g.invdetJ;
 #pragma unroll
   for (int c = 0; c < 3; ++c) {
     n[c] = g.n[c];
 #pragma unroll
-    for (int a = 0; a < 3; ++a) rot[a][c] = g.rot[a][c];
+    for (int a = 0; a < 3; ++a) {
+      rot[a][c] = g.rot[a][c];
+      xp[a][c] = g.xp[a][c];
+    }
   }
 }
 
-// the parts of a rule point's geometry that a kernel side reads
-template <class P, bool N, bool ROT>
-__device__ __forceinline__ void pgeo_load(const PGeo<P>& g, P n[3], P rot[3][3]) {
+// traces that read 1 / |J| (the dual P0 and the Piola-mapped edge shapes) and, for the edge
+// shapes, the offsets x - p_o
+__host__ __device__ constexpr bool piola_trace(int tr) { return tr == TR_P0 || edge_trace(tr); }
+
+// the parts of a rule point's geometry that a kernel side reads: the normal (N), the rotated
+// gradients (ROT), 1 / |J| and the Piola offsets (PIOLA)
+template <class P, bool N, bool ROT, bool PIOLA>
+__device__ __forceinline__ void pgeo_load(const PGeo<P>& g, P n[3], P rot[3][3], P& inv, P xp[3][3]) {
   if constexpr (N) {
 #pragma unroll
     for (int c = 0; c < 3; ++c) n[c] = g.n[c];
@@ -351,6 +361,13 @@ __device__ __forceinline__ void pgeo_load(const PGeo<P>& g, P n[3], P rot[3][3])
     for (int a = 0; a < 3; ++a)
 #pragma unroll
       for (int c = 0; c < 3; ++c) rot[a][c] = g.rot[a][c];
+  }
+  if constexpr (PIOLA) {
+    inv = g.invdetJ;
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+      for (int c = 0; c < 3; ++c) xp[a][c] = g.xp[a][c];
   }
 }
 

@@ -154,14 +154,26 @@ struct ElemRecP {
   P pad[3];
 };
 
-// Geometry of one regular-rule point of a curved element: the unit normal and the rotated
-// surface gradients n x grad_Gamma(lambda_a) of the barycentrics there (flat elements keep
-// them per element, in ElemRecP).
+// Geometry of one regular-rule point of a curved element (flat elements keep it per element,
+// in ElemRecP): the unit normal, the rotated surface gradients n x grad_Gamma(lambda_a) of the
+// barycentrics, 1 / |J|, and per local vertex o the vector J (xhat - vhat_o), which the RT0
+// shape of the edge opposite o scales by its sign / |J| (the Piola map; on a flat element it is
+// x - p_o).
 template <class P>
 struct PGeo {
   P n[3];
   P rot[3][3];
+  P invdetJ;
+  P xp[3][3];
 };
+
+// J (xhat - vhat_o) for the reference vertices vhat = (1,0), (0,1), (0,0)
+__host__ __device__ inline void piola_offsets(const double* J0, const double* J1, double xi, double eta,
+                                              double xp[3][3]) {
+  const double vx[3] = {1.0, 0.0, 0.0}, vy[3] = {0.0, 1.0, 0.0};
+  for (int o = 0; o < 3; ++o)
+    for (int c = 0; c < 3; ++c) xp[o][c] = J0[c] * (xi - vx[o]) + J1[c] * (eta - vy[o]);
+}
 
 // Curved (isoparametric Lagrange) element map of order g at (xi, eta): the point and its
 // derivatives J0 = dx/dxi, J1 = dx/deta from the element's (g+1)(g+2)/2 nodes P (3 doubles

@@ -134,14 +134,19 @@ void MeshH::map(int e, double xi, double eta, double* x) const {
   for (int c = 0; c < 3; ++c) x[c] = xi * r.p[0][c] + eta * r.p[1][c] + l2 * r.p[2][c];
 }
 
-double MeshH::frame(int e, double xi, double eta, double* x, double* n, double rot[3][3]) const {
+double MeshH::frame(int e, double xi, double eta, double* x, double* n, double rot[3][3], double* J0o,
+                    double* J1o) const {
   if (gorder > 1) {
     double J0[3], J1[3];
     curved_map(gorder, &G[(size_t)e * gnodes() * 3], xi, eta, x, J0, J1);
+    if (J0o)
+      for (int c = 0; c < 3; ++c) { J0o[c] = J0[c]; J1o[c] = J1[c]; }
     return surface_frame(J0, J1, n, rot);
   }
   const ElemRec64& r = rec[e];
   map(e, xi, eta, x);
+  if (J0o)
+    for (int c = 0; c < 3; ++c) { J0o[c] = r.p[0][c] - r.p[2][c]; J1o[c] = r.p[1][c] - r.p[2][c]; }
   for (int c = 0; c < 3; ++c) n[c] = r.n[c];
   for (int a = 0; a < 3; ++a)
     for (int c = 0; c < 3; ++c) rot[a][c] = r.rot[a][c];
@@ -200,14 +205,20 @@ static void build_tables(const MeshH& m, const TrigRule& r, std::vector<ElemRecP
     d.pad[0] = d.pad[1] = d.pad[2] = (P)0;
     for (int q = 0; q < nq; ++q) {
       // the point, and w |J| at it (curved elements: their normal and rotated gradients too)
-      double x[3], nq3[3], rt[3][3];
-      const double detJ = m.frame(e, r.xi[q], r.eta[q], x, nq3, rt);
+      double x[3], nq3[3], rt[3][3], J0[3], J1[3];
+      const double detJ = m.frame(e, r.xi[q], r.eta[q], x, nq3, rt, J0, J1);
       const double w = r.w[q] * detJ;
       if (m.curved()) {
         PGeo<P>& g = pgeo[(size_t)e * nq + q];
+        double xp[3][3];
+        piola_offsets(J0, J1, r.xi[q], r.eta[q], xp);
+        g.invdetJ = (P)(1.0 / detJ);
         for (int c = 0; c < 3; ++c) {
           g.n[c] = (P)nq3[c];
-          for (int a = 0; a < 3; ++a) g.rot[a][c] = (P)rt[a][c];
+          for (int a = 0; a < 3; ++a) {
+            g.rot[a][c] = (P)rt[a][c];
+            g.xp[a][c] = (P)xp[a][c];
+          }
         }
       }
       QPt<P>& qo = qoff[(size_t)e * nq + q];

@@ -104,8 +104,10 @@ struct MeshH {
   bool curved() const { return gorder > 1; }
   int gnodes() const { return (gorder + 1) * (gorder + 2) / 2; }
   void map(int e, double xi, double eta, double* x) const;
-  // the map at (xi, eta): point, |J0 x J1|, normal and n x grad_Gamma(lambda_a)
-  double frame(int e, double xi, double eta, double* x, double* n, double rot[3][3]) const;
+  // the map at (xi, eta): point, |J0 x J1|, normal and n x grad_Gamma(lambda_a); J0, J1 the
+  // derivatives when asked for
+  double frame(int e, double xi, double eta, double* x, double* n, double rot[3][3], double* J0 = nullptr,
+               double* J1 = nullptr) const;
   // the element's weight in the cluster data: the flat area, or |J0 x J1| / 2 at the
   // centroid of a curved element
   double area(int e) const;
@@ -147,8 +149,6 @@ struct SpaceH {
 
 // device view of a space's dofs, signs and cluster positions (operator.cpp)
 SpaceDev space_dev(const SpaceH& s, int tr, const DevBuf& pinv);
-// a space and trace on a curved mesh: scalar spaces only (BEM_ERR_ARG otherwise)
-void check_curved(const MeshH& m, const SpaceH& sp, int tr);
 
 // ---- cluster tree and partition (geometry.cpp) -----------------------------------------
 struct ClusterH {

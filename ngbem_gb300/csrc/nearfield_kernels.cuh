@@ -25,13 +25,17 @@ __device__ __forceinline__ int i4c(const int4& v, int a) { return a == 0 ? v.x :
 
 template <class P> struct P2 { P x, y; };
 
-// A curved element's map at (xi, eta): the point, the normal and the rotated gradients; returns
-// |J0 x J1|.
+// A curved element's map at (xi, eta): the point, the normal, the rotated gradients, and for
+// the traces that read them 1 / |J| and the Piola offsets; returns |J0 x J1|.
+template <int TR>
 __device__ __forceinline__ double curved_point(int g, const double* nodes, double xi, double eta, double* x,
-                                               double* n, double rot[3][3]) {
+                                               double* n, double rot[3][3], double& inv, double xp[3][3]) {
   double J0[3], J1[3];
   curved_map(g, nodes, xi, eta, x, J0, J1);
-  return surface_frame(J0, J1, n, rot);
+  const double detJ = surface_frame(J0, J1, n, rot);
+  if constexpr (piola_trace(TR)) inv = 1.0 / detJ;
+  if constexpr (edge_trace(TR)) piola_offsets(J0, J1, xi, eta, xp);
+  return detJ;
 }
 
 template <int KID, class P, int TRT, int TET>
@@ -69,7 +73,7 @@ __global__ void __launch_bounds__(128) nf_regular_kernel(NFArgs a) {
 #pragma unroll
   for (int c = 0; c < 3; ++c) { nx[c] = Ei.n[c]; ny[c] = Ej.n[c]; }
   P roti[3][3], rotj[3][3], oi[3][3], oj[3][3];
-  const P invi = Ei.invdetJ, invj = Ej.invdetJ;
+  P invi = Ei.invdetJ, invj = Ej.invdetJ;
   if (needs_rot(TET)) {
 #pragma unroll
     for (int r = 0; r < 3; ++r)
@@ -115,12 +119,12 @@ __global__ void __launch_bounds__(128) nf_regular_kernel(NFArgs a) {
   for (int p = 0; p < nq; ++p) {
     const QPt<P> qi = Qi[p];
     const P2<P> rp = RQ[p];
-    if (PGi) pgeo_load<P, G::NEEDS_NX, needs_rot(TET)>(PGi[p], nx, roti);
     P xpi[3][3];
     if (edge_trace(TET)) {
 #pragma unroll
       for (int r = 0; r < 3; ++r) { xpi[r][0] = qi.x - oi[r][0]; xpi[r][1] = qi.y - oi[r][1]; xpi[r][2] = qi.z - oi[r][2]; }
     }
+    if (PGi) pgeo_load<P, G::NEEDS_NX || TET == TR_NED, needs_rot(TET), piola_trace(TET)>(PGi[p], nx, roti, invi, xpi);
     V ks[NT][NDJ];
 #pragma unroll
     for (int t = 0; t < NT; ++t)
@@ -128,17 +132,17 @@ __global__ void __launch_bounds__(128) nf_regular_kernel(NFArgs a) {
       for (int b = 0; b < NDJ; ++b) ks[t][b] = vzero<V>();
     for (int q = 0; q < nq; ++q) {
       const QPt<P> qj = Qj[q];
-      if (PGj) pgeo_load<P, G::NEEDS_NY, needs_rot(TRT)>(PGj[q], ny, rotj);
-      const P dx = Dx + (qi.x - qj.x), dy = Dy + (qi.y - qj.y), dz = Dz + (qi.z - qj.z);
-      V kv[NC];
-      G::eval(dx, dy, dz, nx, ny, kappa, kv);
-      const P w = qi.w * qj.w;
       P xpj[3][3];
-      const P2<P> rqq = RQ[q];
       if (edge_trace(TRT)) {
 #pragma unroll
         for (int r = 0; r < 3; ++r) { xpj[r][0] = qj.x - oj[r][0]; xpj[r][1] = qj.y - oj[r][1]; xpj[r][2] = qj.z - oj[r][2]; }
       }
+      if (PGj) pgeo_load<P, G::NEEDS_NY || TRT == TR_NED, needs_rot(TRT), piola_trace(TRT)>(PGj[q], ny, rotj, invj, xpj);
+      const P dx = Dx + (qi.x - qj.x), dy = Dy + (qi.y - qj.y), dz = Dz + (qi.z - qj.z);
+      V kv[NC];
+      G::eval(dx, dy, dz, nx, ny, kappa, kv);
+      const P w = qi.w * qj.w;
+      const P2<P> rqq = RQ[q];
 #pragma unroll
       for (int t = 0; t < NT; ++t) {
         const V kw = kv[G::kc(t)] * w;
@@ -259,7 +263,7 @@ __global__ void __launch_bounds__(256) nf_singular_kernel(NFArgs a) {
 #pragma unroll
     for (int c = 0; c < 3; ++c) { nx[c] = Ei.n[c]; ny[c] = Ej.n[c]; }
     const double detJ2 = Ei.detJ * Ej.detJ;
-    const double invi = Ei.invdetJ, invj = Ej.invdetJ;
+    double invi = Ei.invdetJ, invj = Ej.invdetJ;
     int sgi[SignSlots<TET>::N], sgj[SignSlots<TRT>::N];
     elem_signs<TET>(a.test.sign, s.ei, sgi);
     elem_signs<TRT>(a.trial.sign, s.ej, sgj);
@@ -286,13 +290,13 @@ __global__ void __launch_bounds__(256) nf_singular_kernel(NFArgs a) {
         for (int q = 0; q < 3; ++q) { plx[px[q]] = lx[q]; ply[py[q]] = ly[q]; }
         xi = plx[0]; xe = plx[1]; yi = ply[0]; ye = ply[1];
       }
-      double x[3], y[3];
+      double x[3], y[3], xpi[3][3], xpj[3][3];
       double fac;
       if constexpr (CURVED) {
-        // curved elements: the maps, normals and rotated gradients at the two points
+        // curved elements: the maps, normals, rotated gradients and Piola data at the two points
         const int nn = (a.gorder + 1) * (a.gorder + 2) / 2;
-        const double dxi = curved_point(a.gorder, a.gnodes + (size_t)s.ei * nn * 3, xi, xe, x, nx, roti);
-        const double dyj = curved_point(a.gorder, a.gnodes + (size_t)s.ej * nn * 3, yi, ye, y, ny, rotj);
+        const double dxi = curved_point<TET>(a.gorder, a.gnodes + (size_t)s.ei * nn * 3, xi, xe, x, nx, roti, invi, xpi);
+        const double dyj = curved_point<TRT>(a.gorder, a.gnodes + (size_t)s.ej * nn * 3, yi, ye, y, ny, rotj, invj, xpj);
         fac = dxi * dyj * w;
       } else {
         const double l2x = 1.0 - xi - xe, l2y = 1.0 - yi - ye;
@@ -305,18 +309,19 @@ __global__ void __launch_bounds__(256) nf_singular_kernel(NFArgs a) {
       }
       V kv[NC];
       G::eval(x[0] - y[0], x[1] - y[1], x[2] - y[2], nx, ny, kappa, kv);
-      double xpi[3][3], xpj[3][3];
-      if (edge_trace(TET)) {
+      if constexpr (!CURVED) {
+        if (edge_trace(TET)) {
 #pragma unroll
-        for (int r = 0; r < 3; ++r)
+          for (int r = 0; r < 3; ++r)
 #pragma unroll
-          for (int c = 0; c < 3; ++c) xpi[r][c] = x[c] - pi[r][c];
-      }
-      if (edge_trace(TRT)) {
+            for (int c = 0; c < 3; ++c) xpi[r][c] = x[c] - pi[r][c];
+        }
+        if (edge_trace(TRT)) {
 #pragma unroll
-        for (int r = 0; r < 3; ++r)
+          for (int r = 0; r < 3; ++r)
 #pragma unroll
-          for (int c = 0; c < 3; ++c) xpj[r][c] = y[c] - pj[r][c];
+            for (int c = 0; c < 3; ++c) xpj[r][c] = y[c] - pj[r][c];
+        }
       }
 #pragma unroll
       for (int t = 0; t < NT; ++t) {
@@ -419,10 +424,7 @@ void launch_nf_singular_l2p3(int kid, int prec, const NFArgs& a, cudaStream_t s)
 
 template <int K, class S, int A, int B>
 static void run_singular(const NFArgs& a, cudaStream_t s) {
-  auto fn = nf_singular_kernel<K, S, A, B, false>;
-  // curved meshes carry the scalar traces only (the operator checks it before assembly)
-  if constexpr (!edge_trace(A) && !edge_trace(B))
-    if (a.gnodes) fn = nf_singular_kernel<K, S, A, B, true>;
+  auto fn = a.gnodes ? nf_singular_kernel<K, S, A, B, true> : nf_singular_kernel<K, S, A, B, false>;
   int smem = a.ss_smem_bytes > 0 ? a.ss_smem_bytes : 0;
   if (smem > 48 * 1024) cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
   fn<<<a.sing_grid, 256, smem, s>>>(a);

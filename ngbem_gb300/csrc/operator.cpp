@@ -62,16 +62,6 @@ struct NearPass {
   int sing_cap = 0;
 };
 
-// Curved meshes carry the scalar spaces (P0, P1, SurfaceL2 and H1 of higher order) with their
-// identity, rotated-gradient and Helmholtz traces; the Piola-mapped edge spaces (RT0, HCurl)
-// and the dual mapping are defined on flat triangles only.
-void check_curved(const MeshH& m, const SpaceH& sp, int tr) {
-  if (!m.curved()) return;
-  if (edge_trace(tr) || sp.kind == BEM_RT0 || sp.kind == BEM_HCURL)
-    throw Error(BEM_ERR_ARG, "HDivSurface / HCurl spaces need a flat mesh");
-  if (sp.dual) throw Error(BEM_ERR_ARG, "the dual mapping needs a flat mesh");
-}
-
 void HOperator::merge_meshes() {
   if (own_mesh) return;  // already merged: trial / test are the merged-mesh spaces
   trial_nt0 = trial->mesh->nt;
@@ -132,8 +122,6 @@ void HOperator::assemble() {
   tet = trace_kind(test->kind, test_ev);
   if (trt < 0 || tet < 0) throw Error(BEM_ERR_ARG, "evaluator not available for this space");
   if (!nf_combo_supported(kid, trt, tet)) throw Error(BEM_ERR_ARG, "kernel / trace combination not supported");
-  check_curved(*trial->mesh, *trial, trt);
-  check_curved(*test->mesh, *test, tet);
   cplx = kernel_complex(kid);
   const int NC = kernel_ncomp(kid);
   prec = prm.precision == BEM_MIXED ? 1 : 0;

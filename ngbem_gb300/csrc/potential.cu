@@ -41,8 +41,9 @@ __global__ void pot_sources_kernel(PotArgs a) {
         xp[x][y] = (y == 0 ? qo.x : (y == 1 ? qo.y : qo.z)) - Ee.o[x][y];
       }
     double nrm[3] = {Ee.n[0], Ee.n[1], Ee.n[2]};
-    // curved elements: the normal and rotated gradients at the rule point
-    if (a.pgeo) point_geo<double>(((const PGeo<double>*)a.pgeo)[(size_t)e * a.nq + q], nrm, rot);
+    double inv = Ee.invdetJ;
+    // curved elements: the normal, rotated gradients and Piola data at the rule point
+    if (a.pgeo) point_geo<double>(((const PGeo<double>*)a.pgeo)[(size_t)e * a.nq + q], nrm, rot, inv, xp);
     int sg[SignSlots<TRT>::N];
     elem_signs<TRT>(a.trial.sign, e, sg);
     const int4 dn = a.trial.dofs[e], dx = dof_aux<TRT>(a.trial.sign, e);
@@ -54,7 +55,7 @@ __global__ void pot_sources_kernel(PotArgs a) {
       const V dv = dens[elem_dof<TRT>(dn, dx, x)];
 #pragma unroll
       for (int c = 0; c < DIM; ++c)
-        val[c] += dv * trace_val<TRT, double>(x, c, RQ[2 * q], RQ[2 * q + 1], xp, Ee.invdetJ, rot, sg[x],
+        val[c] += dv * trace_val<TRT, double>(x, c, RQ[2 * q], RQ[2 * q + 1], xp, inv, rot, sg[x],
                                                a.trial.dual != 0, nrm);
     }
     double* py = a.src_pos + 6 * t;

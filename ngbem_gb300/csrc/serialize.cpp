@@ -204,10 +204,6 @@ std::unique_ptr<HOperator> load_operator(const char* path, SpaceH* trial, SpaceH
     throw Error(BEM_ERR_ARG, "the spaces do not match the saved operator");
   op->trt = trace_kind(trial->kind, op->trial_ev);
   op->tet = trace_kind(test->kind, op->test_ev);
-  if (op->trt >= 0 && op->tet >= 0) {
-    check_curved(*trial->mesh, *trial, op->trt);
-    check_curved(*test->mesh, *test, op->tet);
-  }
   op->cplx = kernel_complex(op->kid);
   op->vsize = (op->prec == 0 ? 8 : 4) * (op->cplx ? 2 : 1);
   op->height = test->ndof;

@@ -165,8 +165,6 @@ def load_vector(space, f, order: int = 6) -> np.ndarray:
         fv = fv[..., None]
     out = np.zeros((space.ndof, fv.shape[-1]), dtype=np.result_type(fv.dtype, np.float64))
     curved = getattr(mesh, "curve_order", 1) > 1
-    if curved and (vector or space.dual_mapping):
-        raise ValueError("HDivSurface / HCurl spaces and the dual mapping need a flat mesh")
     W = _weights(w, detj)
     if space.kind == "P0":
         if space.dual_mapping:
@@ -189,6 +187,21 @@ def load_vector(space, f, order: int = 6) -> np.ndarray:
         nd = phi.shape[-1]
         idx = dofs[on, 0][:, None] + np.arange(nd)[None, :]
         np.add.at(out, idx.ravel(), contrib[on].reshape(-1, contrib.shape[-1]))
+    elif curved:
+        # the Piola map per point: sigma J (xhat - vhat_o) / |J|
+        xi, eta, _ = triangle_rule(order)
+        _, Dxi, Deta = _lagrange(mesh.curve_order, xi, eta)
+        J0 = np.einsum("qn,tnc->tqc", Dxi, mesh.curve_nodes)
+        J1 = np.einsum("qn,tnc->tqc", Deta, mesh.curve_nodes)
+        vhat = np.array([[1.0, 0.0], [0.0, 1.0], [0.0, 0.0]])
+        for k in range(3):
+            o = (k + 2) % 3
+            off = J0 * (xi - vhat[o, 0])[None, :, None] + J1 * (eta - vhat[o, 1])[None, :, None]
+            psi = signs[:, k, None, None] * off / detj[:, :, None]
+            if space.kind == "HCURL":
+                psi = np.cross(n, psi)
+            contrib = np.einsum("tq,tqcm,tqc->tm", W, fv, psi)
+            np.add.at(out, dofs[on, k], contrib[on])
     else:
         P = mesh.vertices[mesh.triangles]
         for k in range(3):

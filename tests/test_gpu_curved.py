@@ -12,7 +12,9 @@ tests/test_Laplace.py:25).
   (tests/test_SLIntegration.py:30-40) on curved meshes.
 * The interior Dirichlet-to-Neumann map on the curved sphere: the error of the flat triangles
   (O(h^2)) is gone.
-* Spaces that need flat triangles are refused at assembly; a mesh in use cannot be curved.
+* HDivSurface and HCurl through the Piola map of the curved elements (Maxwell single and double
+  layer, curl single layer), and the dual mapping of P0.
+* A mesh in use cannot be curved.
 """
 import numpy as np
 import pytest
@@ -20,7 +22,6 @@ import torch
 
 import ngbem_gb300 as nb
 from ngbem_gb300 import bem
-from ngbem_gb300._lib import BEM_ERR_ARG, BemError
 from ngbem_gb300.forms import load_vector
 from ngbem_gb300.meshes import ellipsoid, icosphere
 
@@ -31,7 +32,10 @@ COMBOS = [("laplace_sl", 0.0, "P0", "P0", "id", "id"), ("laplace_dl", 0.0, "P1",
           ("laplace_hs", 0.0, "P1", "P1", "rot", "rot"), ("helmholtz_cf", 4.0, "P1", "P1", "id", "id"),
           ("helmholtz_hs", 3.0, "P1", "P1", "helm", "helm"), ("laplace_sl", 0.0, "L2P2", "L2P2", "id", "id"),
           ("laplace_dl", 0.0, "H1P3", "L2P2", "id", "id"), ("laplace_hs", 0.0, "H1P3", "H1P3", "rot", "rot"),
-          ("helmholtz_dl", 3.0, "H1P2", "H1P2", "id", "id")]
+          ("helmholtz_dl", 3.0, "H1P2", "H1P2", "id", "id"), ("maxwell_sl", 2.0, "RT0", "RT0", "maxwell", "maxwell"),
+          ("maxwell_dl", 2.0, "HCURL", "RT0", "rotatedtrace", "id"),
+          ("maxwell_sl", 2.0, "HCURL", "HCURL", "maxwellcurl", "maxwellcurl"),
+          ("laplace_sl", 0.0, "P0D", "P0D", "id", "id")]
 IDS = [f"{c[0]}-{c[2]}-{c[3]}" for c in COMBOS]
 
 
@@ -40,7 +44,14 @@ def rel(a, b):
 
 
 def _space(mesh, kind):
-    return nb.TraceSpace(mesh, kind)
+    # P0D: P0 with the dual mapping (v = 1 / |J|)
+    if kind == "P0D":
+        return nb.TraceSpace(mesh, "P0", dual_mapping=True)
+    return nb.TraceSpace(mesh, kind, complex=kind in ("RT0", "HCURL"))
+
+
+def _okind(kind):
+    return ("P0", True) if kind == "P0D" else (kind, False)
 
 
 def _op(kernel, kappa, mesh, tr, te, ev_tr, ev_te, method="aca", precision="fp64", **kw):
@@ -60,8 +71,9 @@ def test_dense_parity(oracle, kernel, kappa, tr, te, ev_tr, ev_te, g):
     op, s_tr, s_te = _op(kernel, kappa, m, tr, te, ev_tr, ev_te, "dense", intorder_singular=4,
                          intorder_regular=3)
     D = op.mat.to_dense()
-    Do = oracle.dense_matrix(kernel, m, tr, te, kappa=kappa, trial_eval=ev_tr, test_eval=ev_te,
-                             intorder_singular=4, intorder_regular=3)
+    (otr, dtr), (ote, dte) = _okind(tr), _okind(te)
+    Do = oracle.dense_matrix(kernel, m, otr, ote, kappa=kappa, trial_eval=ev_tr, test_eval=ev_te,
+                             intorder_singular=4, intorder_regular=3, trial_dual=dtr, test_dual=dte)
     assert D.shape == (s_te.ndof, s_tr.ndof)
     assert rel(D, Do) < 1e-10
     # the curved operator is not the flat one
@@ -70,10 +82,10 @@ def test_dense_parity(oracle, kernel, kappa, tr, te, ev_tr, ev_te, g):
     assert rel(flat.mat.to_dense(), Do) > 1e-4
 
 
-@pytest.mark.parametrize("kernel,kappa,tr,te,ev_tr,ev_te", [COMBOS[0], COMBOS[3], COMBOS[7]],
-                         ids=[IDS[0], IDS[3], IDS[7]])
+@pytest.mark.parametrize("kernel,kappa,tr,te,ev_tr,ev_te", [COMBOS[0], COMBOS[3], COMBOS[7], COMBOS[9]],
+                         ids=[IDS[0], IDS[3], IDS[7], IDS[9]])
 def test_hmatrix_parity(oracle, kernel, kappa, tr, te, ev_tr, ev_te):
-    m = ellipsoid(3 if tr in ("P0", "P1") else 2, (1.0, 0.8, 0.6)).Curve(3)
+    m = ellipsoid(3 if tr in ("P0", "P1", "RT0") else 2, (1.0, 0.8, 0.6)).Curve(3)
     op, s_tr, s_te = _op(kernel, kappa, m, tr, te, ev_tr, ev_te)
     H = oracle.OracleOperator(kernel, m, tr, te, kappa=kappa, trial_eval=ev_tr, test_eval=ev_te, intorder=3,
                               leafsize=40, eta=2.0, eps=1e-8)
@@ -95,21 +107,29 @@ def test_hmatrix_parity(oracle, kernel, kappa, tr, te, ev_tr, ev_te):
     assert rel((o32.mat * xd).cpu().numpy(), y) < 1e-6
 
 
-@pytest.mark.parametrize("kind", ["P1", "H1P3"])
+@pytest.mark.parametrize("kind", ["P1", "H1P3", "RT0", "HCURL"])
 def test_potential_and_mass(oracle, kind):
     m = icosphere(2).Curve(3)
     sp = _space(m, kind)
-    dens = np.random.default_rng(13).standard_normal(sp.ndof)
+    rng = np.random.default_rng(13)
     pts = np.array([[2.0, 0.3, -0.1], [0.1, 0.2, 0.3], [-1.5, 1.0, 0.5]])
-    for kernel in ("laplace_sl", "laplace_dl"):
-        op, _, _ = _op(kernel, 0.0, m, kind, kind, "id", "id")
+    if kind in ("RT0", "HCURL"):
+        dens = rng.standard_normal(sp.ndof) + 1j * rng.standard_normal(sp.ndof)
+        ev = "maxwell" if kind == "RT0" else "maxwellcurl"
+        op, _, _ = _op("maxwell_sl", 2.0, m, kind, kind, ev, ev)
+        cases = [("maxwell_sl", 2.0, ev, op)]
+    else:
+        dens = rng.standard_normal(sp.ndof)
+        cases = [(k, 0.0, "id", _op(k, 0.0, m, kind, kind, "id", "id")[0]) for k in ("laplace_sl", "laplace_dl")]
+    for kernel, kappa, ev, op in cases:
         val = op.GetPotential(torch.from_numpy(dens).cuda())(pts).cpu().numpy().reshape(len(pts), -1)
-        ref = oracle.potential(kernel, m, kind, dens, pts, intorder=3).reshape(len(pts), -1)
+        ref = oracle.potential(kernel, m, kind, dens, pts, kappa=kappa, trial_eval=ev, intorder=3).reshape(len(pts), -1)
         assert rel(val, ref) < 1e-11
     M = nb.MassOperator(sp, sp)
-    y = (M * torch.from_numpy(dens).cuda()).cpu().numpy()
-    order = 4 if kind == "P1" else 6
-    assert rel(y, oracle.mass_matrix(m, kind, kind, order=order) @ dens) < 1e-12
+    x = rng.standard_normal(sp.ndof)
+    y = (M * torch.from_numpy(x).to(torch.complex128 if sp.is_complex else torch.float64).cuda()).cpu().numpy()
+    order = 6 if kind == "H1P3" else 4
+    assert rel(y, oracle.mass_matrix(m, kind, kind, order=order) @ x) < 1e-12
 
 
 def test_reference_aca_pattern():
@@ -169,10 +189,11 @@ def test_dirichlet_to_neumann_on_the_curved_sphere(oracle):
     assert curved < 5e-3
 
 
-def test_flat_only_spaces_and_curving_in_use():
-    m = icosphere(1).Curve(2)
-    with pytest.raises(BemError) as ei:
-        nb.MaxwellSingleLayerPotentialOperator(nb.HDivSurface(m, complex=True), 1.0, intorder=3)
-    assert ei.value.code == BEM_ERR_ARG
-    with pytest.raises(BemError):
-        nb.SingleLayerPotentialOperator(nb.TraceSpace(m, "P0", dual_mapping=True), intorder=3)
+def test_a_mesh_in_use_cannot_be_curved():
+    from ngbem_gb300 import _lib
+    from ngbem_gb300.bem import _MeshHandle
+    m = icosphere(1)
+    nb.SingleLayerPotentialOperator(nb.SurfaceL2(m), intorder=3)
+    G = np.ascontiguousarray(icosphere(1).Curve(2).curve_nodes)
+    rc = _lib.lib.bem_mesh_set_geometry(_MeshHandle.of(m).h, 2, G.ctypes.data_as(_lib._dp))
+    assert rc == _lib.BEM_ERR_STATE
