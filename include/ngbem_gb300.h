@@ -119,9 +119,9 @@ int bem_mesh_destroy(bem_mesh_t mesh);
  * isoparametric Lagrange triangles with nodes[nt][(order+1)(order+2)/2][3]: node (i, j, k),
  * i + j + k = order, at barycentric (i, j, k) / order of the triangle's vertices
  * (v0, v1, v2), listed for i = order..0, j = order-i..0; the corner nodes must equal the
- * vertices.  The scalar spaces (P0, P1, SurfaceL2 and H1 of higher order) live on curved
- * meshes; RT0, HCurl and the dual mapping need flat ones (BEM_ERR_ARG at assembly).  Call
- * before the first operator on the mesh is created (BEM_ERR_STATE after). */
+ * vertices.  Every space lives on curved meshes (RT0 and HCurl through the Piola map of the
+ * curved element at each point).  Call before the first operator on the mesh is created
+ * (BEM_ERR_STATE after). */
 int bem_mesh_set_geometry(bem_mesh_t mesh, int order, const double* nodes);
 
 /* Trace space on a mesh (replaces the NGSolve FESpace argument of the factories,

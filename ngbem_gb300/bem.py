@@ -3,8 +3,7 @@
 Factories keep the reference names, argument order, keyword names and defaults
 (intorder=3, leafsize=40, eta=2., eps=1e-6, method="aca", testhmatrix=False).  The NGSolve
 FESpace argument becomes a trace space on a triangle mesh (SurfaceL2 order 0 = P0,
-H1 order 1 = P1, HDivSurface order 0 = RT0), flat or curved by ``Mesh.Curve(order)`` (the
-scalar spaces only).  ``.mat`` is an H-matrix resident in GPU
+H1 order 1 = P1, HDivSurface order 0 = RT0), flat or curved by ``Mesh.Curve(order)``.  ``.mat`` is an H-matrix resident in GPU
 memory with the BaseMatrix surface the reference's callers use: Mult, MultAdd, MultTrans,
 MultTransAdd, ``*``, ``.T``, ``nze``, CreateRowVector, CreateColVector, and sums/scalings
 of matrices (``0.5 * M.mat + K.mat``).

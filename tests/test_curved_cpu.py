@@ -8,7 +8,8 @@ tests/test_aca.py:7 Curve(3), tests/test_SLIntegration.py:28 Curve(2)).
   between the two elements, and every node lies on the surface.
 * The library's cluster trees on curved meshes equal the oracle's bit for bit (the cluster data
   read the mapped points and the curved element weights), and differ from the flat mesh's.
-* Load vectors on curved meshes integrate through the map; the C-ABI rejects bad geometry.
+* Load vectors on curved meshes integrate through the map (the Piola-mapped RT0 and HCurl
+  shapes against the oracle's); the C-ABI rejects bad geometry.
 """
 import ctypes as C
 

@@ -127,7 +127,7 @@ def test_potential_and_mass(oracle, kind):
         assert rel(val, ref) < 1e-11
     M = nb.MassOperator(sp, sp)
     x = rng.standard_normal(sp.ndof)
-    y = (M * torch.from_numpy(x).to(torch.complex128 if sp.is_complex else torch.float64).cuda()).cpu().numpy()
+    y = (M * torch.from_numpy(x).to(torch.complex128 if M.is_complex else torch.float64).cuda()).cpu().numpy()
     order = 6 if kind == "H1P3" else 4
     assert rel(y, oracle.mass_matrix(m, kind, kind, order=order) @ x) < 1e-12
 
