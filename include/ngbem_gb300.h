@@ -45,9 +45,15 @@ enum {
  * vertex dofs (ascending vertex numbers), then p - 1 dofs per edge (edges by first
  * appearance), then (p - 1)(p - 2) / 2 per element; a hierarchical basis (vertex hats, edge
  * bubbles l_i l_j (l_j - l_i)^m oriented from the lower to the higher vertex number, the face
- * bubble l_0 l_1 l_2).  Traces ID and ROT. */
+ * bubble l_0 l_1 l_2).  Traces ID and ROT.
+ * BEM_HDIV1, BEM_HDIV2: HDivSurface of order 1, 2 (NGSolve HDivSurface(mesh, order=K): all
+ * tangential vector polynomials of degree K, normal-continuous): per edge K + 1 dofs, per
+ * element (K + 1)(K - 1); numbered: the lowest-order edge dofs (edges by first appearance, as
+ * BEM_RT0), then K per edge, then the interior ones per element.  A hierarchical basis of our
+ * own (the RT0 shape, surface curls of H1 edge bubbles, interior l_j l_k curl l_i), Piola-mapped.
+ * Traces ID and MAXWELL. */
 enum { BEM_P0 = 0, BEM_P1 = 1, BEM_RT0 = 2, BEM_HCURL = 3, BEM_L2P1 = 4, BEM_L2P2 = 5, BEM_L2P3 = 6,
-       BEM_H1P2 = 7, BEM_H1P3 = 8 };
+       BEM_H1P2 = 7, BEM_H1P3 = 8, BEM_HDIV1 = 9, BEM_HDIV2 = 10 };
 /* trace evaluators: GetEvaluator(BND) (ID), DiffOpBoundaryRot (ROT), DiffOpHelmholtz (HELM),
  * DiffOpMaxwellNew (MAXWELL); reference src/diffops.hpp:12-338.  On BEM_HCURL: ID is the
  * tangential trace (GetEvaluator(BND) of an HCurl space), ROTATED_TRACE is

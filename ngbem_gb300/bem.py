@@ -3,8 +3,9 @@
 Factories keep the reference names, argument order, keyword names and defaults
 (intorder=3, leafsize=40, eta=2., eps=1e-6, method="aca", testhmatrix=False).  The NGSolve
 FESpace argument becomes a trace space on a triangle mesh (SurfaceL2 order 0 = P0,
-H1 order 1 = P1, HDivSurface order 0 = RT0), flat or curved by ``Mesh.Curve(order)``.  ``.mat`` is an H-matrix resident in GPU
-memory with the BaseMatrix surface the reference's callers use: Mult, MultAdd, MultTrans,
+H1 order 1 = P1, HDivSurface order 0 = RT0), flat or curved by ``Mesh.Curve(order)``.
+``.mat`` is an H-matrix resident in GPU memory with the BaseMatrix surface the reference's
+callers use: Mult, MultAdd, MultTrans,
 MultTransAdd, ``*``, ``.T``, ``nze``, CreateRowVector, CreateColVector, and sums/scalings
 of matrices (``0.5 * M.mat + K.mat``).
 
@@ -81,7 +82,7 @@ class _MeshHandle:
 class TraceSpace:
     """Surface trace space: kind "P0" (SurfaceL2 order 0), "P1" (H1 order 1), "RT0" (HDivSurface order 0),
     "HCURL" (surface trace of HCurl order 0), "L2P1".."L2P3" (SurfaceL2 orders 1-3), "H1P2",
-    "H1P3" (H1 orders 2, 3)."""
+    "H1P3" (H1 orders 2, 3), "HDIV1", "HDIV2" (HDivSurface orders 1, 2)."""
 
     def __init__(self, mesh: Mesh, kind: str, dual_mapping: bool = False, complex: bool = False, definedon=None):
         if kind not in KINDS:
@@ -173,10 +174,14 @@ def H1(mesh: Mesh, order: int = 1, complex: bool = False, definedon=None) -> Tra
 
 
 def HDivSurface(mesh: Mesh, order: int = 0, complex: bool = False, definedon=None) -> TraceSpace:
-    """Lowest-order Raviart-Thomas on the surface (NGSolve HDivSurface order 0)."""
-    if order != 0:
-        raise NotImplementedError("HDivSurface: only order 0 (RT0) is supported")
-    return TraceSpace(mesh, "RT0", False, complex, definedon)
+    """Normal-continuous tangential fields on the surface (NGSolve HDivSurface): order 0 the
+    lowest-order Raviart-Thomas space (one dof per edge), order 1, 2 all vector polynomials of
+    that degree (K + 1 dofs per edge, (K + 1)(K - 1) per element) in a hierarchical basis of our
+    own: the RT0 shapes, the surface curls of H1 edge bubbles and, for order 2, the interior
+    fields l_j l_k curl(l_i), all Piola-mapped."""
+    if order not in (0, 1, 2):
+        raise NotImplementedError("HDivSurface: orders 0, 1 and 2 are supported")
+    return TraceSpace(mesh, ("RT0", "HDIV1", "HDIV2")[order], False, complex, definedon)
 
 
 def HCurl(mesh: Mesh, order: int = 0, complex: bool = False, definedon=None) -> TraceSpace:

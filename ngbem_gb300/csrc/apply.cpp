@@ -366,6 +366,8 @@ void MassOperator::build(SpaceH* trial, SpaceH* test, bool complex_vectors) {
     if (sp.kind >= BEM_L2P1 && sp.kind <= BEM_L2P3) return sp.kind - BEM_L2P1 + 1;
     if (sp.kind == BEM_H1P2) return 2;
     if (sp.kind == BEM_H1P3) return 3;
+    if (sp.kind == BEM_HDIV1) return 1;
+    if (sp.kind == BEM_HDIV2) return 2;
     return 1;
   };
   TrigRule r = make_trig_rule(std::max(4, degree(*trial) + degree(*test)));
@@ -388,12 +390,25 @@ void MassOperator::build(SpaceH* trial, SpaceH* test, bool complex_vectors) {
     inv = 1.0 / m.frame(e, xi, eta, x, n, rt, J0, J1);
     piola_offsets(J0, J1, xi, eta, xp);
   };
-  auto shape = [&](const SpaceH& sp, int e, double xi, double eta, double S[10][3], int& dim) {
+  auto shape = [&](const SpaceH& sp, int e, double xi, double eta, double S[12][3], int& dim) {
     double inv, n[3], xp[3][3];
     if (sp.kind == BEM_P0) {
       if (sp.dual) piola(e, xi, eta, inv, n, xp);
       S[0][0] = sp.dual ? inv : 1.0;
       dim = 1;
+      return;
+    }
+    if (sp.kind == BEM_HDIV1 || sp.kind == BEM_HDIV2) {
+      // the Piola map of the reference fields (hdiv_shape), J = (xp_2 - xp_0, xp_2 - xp_1)
+      const int K = sp.kind == BEM_HDIV1 ? 1 : 2;
+      piola(e, xi, eta, inv, n, xp);
+      for (int a = 0; a < sp.nd; ++a) {
+        const int sg = a < 3 * (K + 1) ? sp.sign[3 * e + a / (K + 1)] : 1;
+        double vx, vy;
+        hdiv_shape<double>(K, a, xi, eta, sg, vx, vy);
+        for (int c = 0; c < 3; ++c) S[a][c] = ((xp[2][c] - xp[0][c]) * vx + (xp[2][c] - xp[1][c]) * vy) * inv;
+      }
+      dim = 3;
       return;
     }
     if (sp.kind == BEM_H1P2 || sp.kind == BEM_H1P3) {
@@ -429,7 +444,7 @@ void MassOperator::build(SpaceH* trial, SpaceH* test, bool complex_vectors) {
   };
   for (int e = 0; e < m.nt; ++e)
     for (int q = 0; q < nq && trial->on(e) && test->on(e); ++q) {
-      double Si[10][3], Sj[10][3];
+      double Si[12][3], Sj[12][3];
       int di, dj;
       shape(*test, e, r.xi[q], r.eta[q], Si, di);
       shape(*trial, e, r.xi[q], r.eta[q], Sj, dj);

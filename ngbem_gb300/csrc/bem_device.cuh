@@ -327,6 +327,10 @@ template <> struct TraceInfo<TR_H1P2ROT> { static constexpr int ND = 6, DIM = 3;
 template <> struct TraceInfo<TR_H1P3ROT> { static constexpr int ND = 10, DIM = 3; };
 template <> struct TraceInfo<TR_H1P2HELM> { static constexpr int ND = 6, DIM = 4; };
 template <> struct TraceInfo<TR_H1P3HELM> { static constexpr int ND = 10, DIM = 4; };
+template <> struct TraceInfo<TR_HDIV1ID> { static constexpr int ND = 6, DIM = 3; };
+template <> struct TraceInfo<TR_HDIV2ID> { static constexpr int ND = 12, DIM = 3; };
+template <> struct TraceInfo<TR_HDIV1MAX> { static constexpr int ND = 6, DIM = 4; };
+template <> struct TraceInfo<TR_HDIV2MAX> { static constexpr int ND = 12, DIM = 4; };
 // traces that read the element's n x grad(lambda_a) table
 // the geometry of a curved element's rule point (PGeo): normal, rotated gradients, 1 / |J| and
 // the Piola offsets
@@ -378,15 +382,25 @@ template <int TR> struct SignSlots { static constexpr int N = TraceInfo<TR>::ND 
 // the element's second dof record, read only by traces that need it (H1 of order >= 2)
 template <int TR>
 __device__ __forceinline__ int4 dof_aux(const int4* sign, int e) {
-  if constexpr (h1p_trace(TR)) return sign[e];
+  if constexpr (h1p_trace(TR) || hdiv_trace(TR)) return sign[e];
   else return make_int4(0, 0, 0, 0);
 }
 // global dof of local dof a of an element (dn: the element's dof record; aux: dof_aux).  H1 of
 // order p >= 2: dn = (the three vertex dofs, first face dof), aux = per local edge its
 // orientation sign times (first edge dof + 1)
+// HDivSurface of order K: dn = (the three lowest-order edge dofs, first interior dof), aux = per
+// local edge its orientation sign times (first higher-order dof of the edge + 1)
 template <int TR>
 __device__ __forceinline__ int elem_dof(const int4& dn, const int4& aux, int a) {
   if (l2p_trace(TR)) return dn.x + a;
+  if constexpr (hdiv_trace(TR)) {
+    constexpr int K = hdiv_order(TR);
+    if (a >= 3 * (K + 1)) return dn.w + (a - 3 * (K + 1));
+    const int k = a / (K + 1), m = a % (K + 1);
+    if (m == 0) return k == 0 ? dn.x : (k == 1 ? dn.y : dn.z);
+    const int g = k == 0 ? aux.x : (k == 1 ? aux.y : aux.z);
+    return (g < 0 ? -g : g) - 1 + (m - 1);
+  }
   if constexpr (h1p_trace(TR)) {
     constexpr int P = h1p_order(TR);
     if (a >= 3 && a < 3 + 3 * (P - 1)) {
@@ -404,6 +418,17 @@ template <int TR, int N>
 __device__ __forceinline__ void elem_signs(const int4* sign, int e, int (&sg)[N]) {
 #pragma unroll
   for (int k = 0; k < N; ++k) sg[k] = 1;
+  if constexpr (hdiv_trace(TR)) {
+    // every dof of local edge k: the edge's orientation; interior dofs: 1
+    constexpr int K = hdiv_order(TR);
+    const int4 g = sign[e];
+#pragma unroll
+    for (int a = 0; a < 3 * (K + 1) && a < N; ++a) {
+      const int k = a / (K + 1);
+      sg[a] = (k == 0 ? g.x : (k == 1 ? g.y : g.z)) < 0 ? -1 : 1;
+    }
+    return;
+  }
   if (edge_trace(TR)) {
     const int4 g = sign[e];
     sg[0] = g.x;
@@ -447,6 +472,13 @@ __device__ __forceinline__ R trace_val(int a, int c, R xi, R eta, const R (*xp)[
   if (TR == TR_HELM) {
     if (c < 3) return rot[a][c];
     return a == 0 ? xi : (a == 1 ? eta : R(1) - xi - eta);
+  }
+  if constexpr (hdiv_trace(TR)) {
+    // HDivSurface of order K: the Piola map of the reference field, J = (xp_2 - xp_0, xp_2 - xp_1)
+    R vx, vy;
+    const R dv = hdiv_shape<R>(hdiv_order(TR), a, xi, eta, sgn, vx, vy);
+    if (c == 3) return dv * invdetJ;
+    return ((xp[2][c] - xp[0][c]) * vx + (xp[2][c] - xp[1][c]) * vy) * invdetJ;
   }
   // edge dofs: the RT0 shape sgn (x - p_o) / |J| (o the vertex opposite the edge)
   const int o = (a + 2) % 3;

@@ -22,10 +22,12 @@ enum KernelId {
 // TR_H1P2, TR_H1P3: H1 of order 2, 3 (identity trace); TR_H1P2ROT, TR_H1P3ROT: their surface
 // curl n x grad_Gamma phi (DiffOpBoundaryRot, src/diffops.hpp:12-60, for the hierarchical basis
 // h1p_shape below); TR_H1P2HELM, TR_H1P3HELM: [n x grad_Gamma phi; phi] (DiffOpHelmholtz)
+// TR_HDIV1ID, TR_HDIV2ID: HDivSurface of order 1, 2 (identity trace, the Piola-mapped shape);
+// TR_HDIV1MAX, TR_HDIV2MAX: [shape; surface divergence] (DiffOpMaxwellNew) for hdiv_shape below
 enum TraceKind { TR_P0 = 0, TR_P1 = 1, TR_ROT = 2, TR_HELM = 3, TR_MAX = 4, TR_RT0ID = 5,
                  TR_NED = 6, TR_NEDROT = 7, TR_NEDMAX = 8, TR_L2P1 = 9, TR_L2P2 = 10, TR_L2P3 = 11,
                  TR_H1P2 = 12, TR_H1P3 = 13, TR_H1P2ROT = 14, TR_H1P3ROT = 15, TR_H1P2HELM = 16,
-                 TR_H1P3HELM = 17 };
+                 TR_H1P3HELM = 17, TR_HDIV1ID = 18, TR_HDIV2ID = 19, TR_HDIV1MAX = 20, TR_HDIV2MAX = 21 };
 // traces of a discontinuous space of order >= 1: the element's dofs are consecutive
 // (first dof + local index) and its "signs" hold the order of its vertices by global number
 __host__ __device__ constexpr bool l2p_trace(int tr) { return tr >= TR_L2P1 && tr <= TR_L2P3; }
@@ -39,6 +41,62 @@ __host__ __device__ constexpr int h1p_order(int tr) {
 // the traces with the surface curl in components 0..2 (and, HELM, the value in 3)
 __host__ __device__ constexpr bool h1p_rot(int tr) { return tr >= TR_H1P2ROT && tr <= TR_H1P3HELM; }
 __host__ __device__ constexpr bool h1p_helm(int tr) { return tr == TR_H1P2HELM || tr == TR_H1P3HELM; }
+
+// traces of HDivSurface of order K = 1, 2: per local edge k (vertices k, k + 1 mod 3) K + 1
+// dofs, then (K + 1)(K - 1) interior dofs
+__host__ __device__ constexpr bool hdiv_trace(int tr) { return tr >= TR_HDIV1ID && tr <= TR_HDIV2MAX; }
+__host__ __device__ constexpr int hdiv_order(int tr) { return tr == TR_HDIV1ID || tr == TR_HDIV1MAX ? 1 : 2; }
+__host__ __device__ constexpr bool hdiv_max(int tr) { return tr == TR_HDIV1MAX || tr == TR_HDIV2MAX; }
+
+// Hierarchical basis of HDivSurface of order K = 1, 2 (BDM_K: all vector polynomials of degree
+// K; our own choice of basis, spanning the space of NGSolve's HDivSurface(order=K)) as
+// reference fields (vx, vy) on the triangle with vertices (1,0), (0,1), (0,0), in barycentrics
+// l = (xi, eta, 1 - xi - eta); the physical shape is the Piola map J (vx, vy) / |J| and the
+// surface divergence the returned reference divergence / |J|.  rot f = (df/deta, -df/dxi).
+// Local dof a:
+//   a < 3 (K + 1)  edge k = a / (K + 1) between local vertices i = k, j = k + 1 (mod 3),
+//                  m = a % (K + 1):
+//                  m = 0  sg (xhat - vhat_o), o the vertex opposite (the RT0 shape);
+//                  m = 1  rot(l_i l_j);
+//                  m = 2  sg rot(l_i l_j (l_j - l_i))
+//                  with sg the edge's orientation (+1 when its first vertex has the lower global
+//                  number), so that the m = 2 field is the surface curl of the global H1 edge
+//                  bubble; surface curls of continuous functions are normal-continuous
+//   a >= 3 (K + 1) (K = 2) interior i = a - 9: l_j l_k rot(l_i), (j, k) the other two vertices,
+//                  zero normal trace on every edge
+template <class R>
+__host__ __device__ inline R hdiv_shape(int K, int a, R xi, R eta, int sg, R& vx, R& vy) {
+  const R l[3] = {xi, eta, R(1) - xi - eta};
+  const R rx[3] = {R(0), R(1), R(-1)}, ry[3] = {R(-1), R(0), R(1)};   // rot l_i
+  const R gx[3] = {R(1), R(0), R(-1)}, gy[3] = {R(0), R(1), R(-1)};   // grad l_i
+  if (a < 3 * (K + 1)) {
+    const int k = a / (K + 1), m = a % (K + 1);
+    const int i = k, j = (k + 1) % 3, o = (k + 2) % 3;
+    if (m == 0) {
+      const R ox = o == 0 ? R(1) : R(0), oy = o == 1 ? R(1) : R(0);
+      vx = R(sg) * (xi - ox);
+      vy = R(sg) * (eta - oy);
+      return R(2 * sg);
+    }
+    // d phi / d l_i and d phi / d l_j of the edge bubble phi
+    R di, dj;
+    if (m == 1) {
+      di = l[j];
+      dj = l[i];
+    } else {
+      di = R(sg) * (l[j] * l[j] - R(2) * l[i] * l[j]);
+      dj = R(sg) * (R(2) * l[i] * l[j] - l[i] * l[i]);
+    }
+    vx = di * rx[i] + dj * rx[j];
+    vy = di * ry[i] + dj * ry[j];
+    return R(0);
+  }
+  const int i = a - 3 * (K + 1), j = (i + 1) % 3, k = (i + 2) % 3;
+  const R f = l[j] * l[k];
+  vx = f * rx[i];
+  vy = f * ry[i];
+  return (l[k] * gx[j] + l[j] * gx[k]) * rx[i] + (l[k] * gy[j] + l[j] * gy[k]) * ry[i];
+}
 
 // Hierarchical H1 basis of order P <= 3 on a triangle in barycentric coordinates l[3] (our own
 // choice of basis; the reference takes NGSolve's H1 element, whose shapes differ but span
@@ -127,7 +185,7 @@ __host__ __device__ inline R dubiner(int P, int a, R xi, R eta, int code) {
 
 // traces whose local dofs carry an edge orientation sign
 __host__ __device__ constexpr bool edge_trace(int tr) {
-  return tr == TR_MAX || tr == TR_RT0ID || tr == TR_NED || tr == TR_NEDROT || tr == TR_NEDMAX;
+  return tr == TR_MAX || tr == TR_RT0ID || tr == TR_NED || tr == TR_NEDROT || tr == TR_NEDMAX || hdiv_trace(tr);
 }
 
 // Per-element record (FP64): vertices, unit normal, |J|, rotated surface gradients of the

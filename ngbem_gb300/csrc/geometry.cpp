@@ -377,6 +377,42 @@ void SpaceH::build(MeshH* m, int kind_, int dual_, const unsigned char* mask) {
       }
       for (int j = 0; j < pf; ++j) xd[3 + 3 * pe + j] = f0 + j;
     }
+  } else if (kind == BEM_HDIV1 || kind == BEM_HDIV2) {
+    // HDivSurface of order K: the lowest-order dofs of the edges (by first appearance on the
+    // region), then K per edge in the same order, then (K + 1)(K - 1) per element; local dofs
+    // per edge k (K + 1 of them), then the interior ones (hdiv_shape); sign: the orientation of
+    // local edge k.  global_dof: the dof of the same function in the space on the whole mesh.
+    const int K = kind == BEM_HDIV1 ? 1 : 2, nin = (K + 1) * (K - 1);
+    nd = (K + 1) * (K + 2);
+    xdof.assign((size_t)nd * m->nt, -1);
+    std::vector<int> emap(m->ne, -1), eord;
+    for (int e : elems)
+      for (int k = 0; k < 3; ++k) {
+        const int g = m->TE[3 * e + k];
+        if (emap[g] < 0) {
+          emap[g] = (int)eord.size();
+          eord.push_back(g);
+        }
+      }
+    const int nlo = (int)eord.size();
+    for (int g : eord) global_dof.push_back(g);
+    for (int g : eord)
+      for (int j = 0; j < K; ++j) global_dof.push_back(m->ne + g * K + j);
+    for (int e : elems)
+      for (int j = 0; j < nin; ++j) global_dof.push_back(m->ne * (K + 1) + e * nin + j);
+    int ei = 0;
+    for (int e : elems) {
+      int* xd = &xdof[(size_t)nd * e];
+      for (int k = 0; k < 3; ++k) {
+        const int lo = emap[m->TE[3 * e + k]];
+        dofs[3 * e + k] = lo;
+        sign[3 * e + k] = m->T[3 * e + k] < m->T[3 * e + (k + 1) % 3] ? 1 : -1;
+        xd[k * (K + 1)] = lo;
+        for (int j = 0; j < K; ++j) xd[k * (K + 1) + 1 + j] = nlo + lo * K + j;
+      }
+      for (int j = 0; j < nin; ++j) xd[3 * (K + 1) + j] = nlo * (K + 1) + ei * nin + j;
+      ++ei;
+    }
   } else {
     throw Error(BEM_ERR_ARG, "unknown space kind");
   }
@@ -408,6 +444,15 @@ void SpaceH::ensure_device() {
       s4[e] = make_int4(sign[3 * e] * (xd[3] + 1), sign[3 * e + 1] * (xd[3 + pe] + 1),
                         sign[3 * e + 2] * (xd[3 + 2 * pe] + 1), 0);
     }
+    if ((kind == BEM_HDIV1 || kind == BEM_HDIV2) && on(e)) {
+      // HDivSurface of order K: w = the first interior dof; the signs carry (first
+      // higher-order dof of the edge + 1)
+      const int K = kind == BEM_HDIV1 ? 1 : 2;
+      const int* xd = &xdof[(size_t)nd * e];
+      d4[e].w = nd > 3 * (K + 1) ? xd[3 * (K + 1)] : 0;
+      s4[e] = make_int4(sign[3 * e] * (xd[1] + 1), sign[3 * e + 1] * (xd[K + 2] + 1),
+                        sign[3 * e + 2] * (xd[2 * K + 3] + 1), 0);
+    }
   }
   d_dofs.upload(d4);
   d_sign.upload(s4);
@@ -433,6 +478,12 @@ int trace_kind(int space_kind, int ev) {
   if (space_kind == BEM_RT0) {
     if (ev == BEM_EV_MAXWELL) return TR_MAX;
     if (ev == BEM_EV_ID) return TR_RT0ID;
+    return -1;
+  }
+  if (space_kind == BEM_HDIV1 || space_kind == BEM_HDIV2) {
+    const int q = space_kind - BEM_HDIV1;
+    if (ev == BEM_EV_MAXWELL) return TR_HDIV1MAX + q;
+    if (ev == BEM_EV_ID) return TR_HDIV1ID + q;
     return -1;
   }
   if (space_kind == BEM_HCURL) {

@@ -29,6 +29,7 @@ bool nf_combo_supported(int kid, int trt, int tet) {
   BEM_NF_COMBOS(X)
   BEM_L2P_COMBOS(X)
   BEM_H1P_COMBOS(X)
+  BEM_HDIV_COMBOS(X)
 #undef X
   return false;
 }
@@ -45,6 +46,10 @@ void launch_nf_regular(int kid, int prec, int trt, int tet, const NFArgs& a, cud
   if (h1p_trace(trt)) {
     if (h1p_order(trt) == 2) launch_nf_regular_h1p2(kid, prec, trt, tet, a, s);
     else launch_nf_regular_h1p3(kid, prec, trt, tet, a, s);
+    return;
+  }
+  if (hdiv_trace(trt)) {
+    launch_nf_regular_hdiv(kid, prec, trt, tet, a, s);
     return;
   }
 #define X(K, A, B)                                                                    \
@@ -68,6 +73,10 @@ void launch_nf_singular(int kid, int prec, int trt, int tet, const NFArgs& a, cu
   if (h1p_trace(trt)) {
     if (h1p_order(trt) == 2) launch_nf_singular_h1p2(kid, prec, trt, tet, a, s);
     else launch_nf_singular_h1p3(kid, prec, trt, tet, a, s);
+    return;
+  }
+  if (hdiv_trace(trt)) {
+    launch_nf_singular_hdiv(kid, prec, trt, tet, a, s);
     return;
   }
 #define X(K, A, B)                                                          \

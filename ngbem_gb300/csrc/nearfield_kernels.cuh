@@ -389,6 +389,9 @@ void launch_nf_regular_h1p2(int kid, int prec, int trt, int tet, const NFArgs& a
 void launch_nf_singular_h1p2(int kid, int prec, int trt, int tet, const NFArgs& a, cudaStream_t s);
 void launch_nf_regular_h1p3(int kid, int prec, int trt, int tet, const NFArgs& a, cudaStream_t s);
 void launch_nf_singular_h1p3(int kid, int prec, int trt, int tet, const NFArgs& a, cudaStream_t s);
+// HDivSurface of order 1, 2 (BEM_HDIV_COMBOS): nearfield_hdiv.cu
+void launch_nf_regular_hdiv(int kid, int prec, int trt, int tet, const NFArgs& a, cudaStream_t s);
+void launch_nf_singular_hdiv(int kid, int prec, int trt, int tet, const NFArgs& a, cudaStream_t s);
 // bodies of those launchers: one (kernel, trial trace, test trace) combination
 #define BEM_NF_REGULAR_X3(K, A, B)                                                     \
   if (kid == K && trt == A && tet == B) {                                              \

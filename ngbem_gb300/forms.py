@@ -11,7 +11,7 @@ import numpy as np
 
 from .meshes import Mesh
 
-__all__ = ["triangle_rule", "load_vector", "p1_load_vector", "p0_load_vector", "plane_wave_bm_source",
+__all__ = ["triangle_rule", "load_vector", "hdiv_fields", "p1_load_vector", "p0_load_vector", "plane_wave_bm_source",
            "random_directions", "dubiner", "h1p_shapes"]
 
 
@@ -146,6 +146,45 @@ def h1p_shapes(p: int, lam: np.ndarray, signs: np.ndarray) -> np.ndarray:
     return np.stack(out, axis=-1)
 
 
+def hdiv_fields(k: int, lam: np.ndarray, signs: np.ndarray):
+    """The HDivSurface basis of order k (1, 2) as reference fields at barycentric points lam
+    (nq, 3) of every triangle with local edge orientations signs (nt, 3): ((nt, nq, nd, 2) fields,
+    (nt, nq, nd) reference divergences) in the library's local order (per edge k: the RT0 shape,
+    the curl (d/deta, -d/dxi) of l_i l_j, of sg l_i l_j (l_j - l_i); then l_j l_k curl(l_i))."""
+    nt, nq = signs.shape[0], lam.shape[0]
+    dxi, deta = np.array([1.0, 0.0, -1.0]), np.array([0.0, 1.0, -1.0])
+    vhat = np.array([[1.0, 0.0], [0.0, 1.0], [0.0, 0.0]])
+    xy = lam[:, :2]
+    V, D = [], []
+    for e in range(3):
+        i, j, o = e, (e + 1) % 3, (e + 2) % 3
+        sg = signs[:, e, None].astype(np.float64)                          # (nt, 1)
+        V.append(sg[:, :, None] * (xy - vhat[o])[None])                    # RT0
+        D.append(np.broadcast_to(2.0 * sg, (nt, nq)))
+        for m in range(1, k + 1):
+            d = np.zeros((nq, 3))
+            if m == 1:
+                d[:, i], d[:, j] = lam[:, j], lam[:, i]
+                scale = np.ones((nt, 1))
+            else:
+                d[:, i] = lam[:, j] ** 2 - 2 * lam[:, i] * lam[:, j]
+                d[:, j] = 2 * lam[:, i] * lam[:, j] - lam[:, i] ** 2
+                scale = sg
+            v = np.stack([d @ deta, -(d @ dxi)], axis=1)                   # (nq, 2)
+            V.append(scale[:, :, None] * v[None])
+            D.append(np.zeros((nt, nq)))
+    if k == 2:
+        for i in range(3):
+            j, kk = (i + 1) % 3, (i + 2) % 3
+            f = lam[:, j] * lam[:, kk]
+            c = np.array([deta[i], -dxi[i]])
+            V.append(np.broadcast_to((f[:, None] * c[None])[None], (nt, nq, 2)))
+            fx = lam[:, kk] * dxi[j] + lam[:, j] * dxi[kk]
+            fy = lam[:, kk] * deta[j] + lam[:, j] * deta[kk]
+            D.append(np.broadcast_to((fx * c[0] + fy * c[1])[None], (nt, nq)))
+    return np.stack(V, axis=2), np.stack(D, axis=2)
+
+
 def load_vector(space, f, order: int = 6) -> np.ndarray:
     """b_i = int f v_i over the space's triangles for the basis v_i of any trace space (the
     role of LinearForm(f * v.Trace() * ds).Assemble() on that space; a space on a region
@@ -159,7 +198,7 @@ def load_vector(space, f, order: int = 6) -> np.ndarray:
     on = dofs[:, 0] >= 0
     x, n, detj, lam, w = _geometry(mesh, order)
     fv = np.asarray(f(x, n))
-    vector = space.kind in ("RT0", "HCURL")
+    vector = space.kind in ("RT0", "HCURL", "HDIV1", "HDIV2")
     multi = fv.ndim == (4 if vector else 3)
     if not multi:
         fv = fv[..., None]
@@ -187,6 +226,25 @@ def load_vector(space, f, order: int = 6) -> np.ndarray:
         nd = phi.shape[-1]
         idx = dofs[on, 0][:, None] + np.arange(nd)[None, :]
         np.add.at(out, idx.ravel(), contrib[on].reshape(-1, contrib.shape[-1]))
+    elif space.kind.startswith("HDIV"):
+        # the Piola map J v / |J| of the reference fields, J per element (flat) or per point
+        xi, eta, _ = triangle_rule(order)
+        if curved:
+            _, Dxi, Deta = _lagrange(mesh.curve_order, xi, eta)
+            J0 = np.einsum("qn,tnc->tqc", Dxi, mesh.curve_nodes)
+            J1 = np.einsum("qn,tnc->tqc", Deta, mesh.curve_nodes)
+            dj = detj
+        else:
+            P = mesh.vertices[mesh.triangles]
+            J0 = np.broadcast_to((P[:, 0] - P[:, 2])[:, None], x.shape)
+            J1 = np.broadcast_to((P[:, 1] - P[:, 2])[:, None], x.shape)
+            dj = np.broadcast_to(detj[:, None], x.shape[:2])
+        fields, _ = hdiv_fields(int(space.kind[4:]), lam, signs)           # (nt, nq, nd, 2)
+        psi = (J0[:, :, None, :] * fields[..., 0, None] + J1[:, :, None, :] * fields[..., 1, None]) \
+            / dj[:, :, None, None]
+        contrib = np.einsum("tq,tqcm,tqac->tam", W, fv, psi)
+        table = space.dof_table()
+        np.add.at(out, table[on].ravel(), contrib[on].reshape(-1, contrib.shape[-1]))
     elif curved:
         # the Piola map per point: sigma J (xhat - vhat_o) / |J|
         xi, eta, _ = triangle_rule(order)

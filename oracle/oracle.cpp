@@ -309,8 +309,9 @@ struct Mesh {
   double area(int e) const { return gorder > 1 ? 0.5 * mp(e, 1. / 3, 1. / 3).detJ : 0.5 * geo[e].detJ; }
 };
 
-// SurfaceL2 of order p >= 1 has (p+1)(p+2)/2 dofs per element (at most 10 for p = 3)
-constexpr int ORC_MAXND = 10;
+// SurfaceL2 of order p >= 1 has (p+1)(p+2)/2 dofs per element (at most 10 for p = 3),
+// HDivSurface of order K (K+1)(K+2) (12 for K = 2)
+constexpr int ORC_MAXND = 12;
 
 // Dubiner basis function a of order P on a triangle (Dubiner 1991; Karniadakis and Sherwin,
 // Spectral/hp Element Methods, ch. 3), as NGSolve's L2 triangle element uses it (third-party
@@ -379,6 +380,24 @@ struct Space {
         }
         for (int j = 0; j < pf; ++j) d[3 + 3 * pe + j] = m.nv + m.ne * pe + e * pf + j;
       }
+    } else if (kind == ORC_HDIV1 || kind == ORC_HDIV2) {
+      // HDivSurface of order K: per local edge K + 1 dofs (the edge's lowest-order dof = the
+      // edge id, then ne + edge K + m - 1), then (K + 1)(K - 1) interior dofs per element
+      const int K = kind == ORC_HDIV1 ? 1 : 2, nin = (K + 1) * (K - 1);
+      nd = (K + 1) * (K + 2);
+      ndof = m.ne * (K + 1) + m.nt * nin;
+      dofs.resize((size_t)m.nt * nd);
+      sign.resize(3 * m.nt);
+      for (int e = 0; e < m.nt; ++e) {
+        int* d = &dofs[(size_t)e * nd];
+        for (int k = 0; k < 3; ++k) {
+          const int g = m.TE[3 * e + k];
+          d[k * (K + 1)] = g;
+          for (int j = 0; j < K; ++j) d[k * (K + 1) + 1 + j] = m.ne + g * K + j;
+          sign[3 * e + k] = m.T[3 * e + k] < m.T[3 * e + (k + 1) % 3] ? 1 : -1;
+        }
+        for (int j = 0; j < nin; ++j) d[3 * (K + 1) + j] = m.ne * (K + 1) + e * nin + j;
+      }
     } else {
       nd = 3; ndof = m.ne; dofs = m.TE; sign.resize(3 * m.nt);
       for (int e = 0; e < m.nt; ++e)
@@ -392,7 +411,7 @@ struct Space {
 };
 
 static int trace_dim(int kind, int ev) {
-  if (ev == ORC_EV_ID) return (kind == ORC_RT0 || kind == ORC_HCURL) ? 3 : 1;
+  if (ev == ORC_EV_ID) return (kind == ORC_RT0 || kind == ORC_HCURL || kind == ORC_HDIV1 || kind == ORC_HDIV2) ? 3 : 1;
   if (ev == ORC_EV_ROT || ev == ORC_EV_ROTATED_TRACE) return 3;
   return 4;  // HELM, MAXWELL, MAXWELL_CURL
 }
@@ -421,6 +440,55 @@ static void eval_trace(const Mesh& m, const Space& sp, int ev, int e, double xi,
   if (sp.kind >= ORC_L2P1 && sp.kind <= ORC_L2P3) {
     for (int a = 0; a < sp.nd; ++a)
       S[a][0] = dubiner(sp.kind - ORC_L2P1 + 1, a, xi, eta, sp.sign[3 * e], sp.sign[3 * e + 1]);
+    return;
+  }
+  if (sp.kind == ORC_HDIV1 || sp.kind == ORC_HDIV2) {
+    // HDivSurface of order K (DiffOpMaxwellNew on NGSolve's HDivSurface element, restated for
+    // a hierarchical BDM_K basis of our own): reference fields v on the triangle with vertices
+    // (1,0), (0,1), (0,0), Piola-mapped J v / |J|, surface divergence (div v) / |J|.  Per local
+    // edge k (vertices i = k, j = k+1; orientation s): m = 0 the RT0 shape s (xhat - vhat_o);
+    // m = 1 the curl (d/deta, -d/dxi) of l_i l_j; m = 2 that of s l_i l_j (l_j - l_i).
+    // Interior (K = 2): l_j l_k curl(l_i).
+    const int K = sp.kind == ORC_HDIV1 ? 1 : 2;
+    const double lam[3] = {xi, eta, 1.0 - xi - eta};
+    const double dxi[3] = {1.0, 0.0, -1.0}, deta[3] = {0.0, 1.0, -1.0};  // d lambda / d(xi, eta)
+    const double vh[3][2] = {{1.0, 0.0}, {0.0, 1.0}, {0.0, 0.0}};
+    for (int a = 0; a < sp.nd; ++a) {
+      double vx, vy, dv;
+      if (a < 3 * (K + 1)) {
+        const int k = a / (K + 1), mm = a % (K + 1), i = k, j = (k + 1) % 3, o = (k + 2) % 3;
+        const double sg = sp.sign[3 * e + k];
+        if (mm == 0) {
+          vx = sg * (xi - vh[o][0]);
+          vy = sg * (eta - vh[o][1]);
+          dv = 2.0 * sg;
+        } else {
+          double d[3] = {0.0, 0.0, 0.0};  // d phi / d lambda
+          if (mm == 1) {
+            d[i] = lam[j];
+            d[j] = lam[i];
+          } else {
+            d[i] = sg * (lam[j] * lam[j] - 2.0 * lam[i] * lam[j]);
+            d[j] = sg * (2.0 * lam[i] * lam[j] - lam[i] * lam[i]);
+          }
+          double px = 0.0, py = 0.0;  // d phi / d xi, d phi / d eta
+          for (int t = 0; t < 3; ++t) { px += d[t] * dxi[t]; py += d[t] * deta[t]; }
+          vx = py;
+          vy = -px;
+          dv = 0.0;
+        }
+      } else {
+        const int i = a - 3 * (K + 1), j = (i + 1) % 3, k = (i + 2) % 3;
+        const double f = lam[j] * lam[k];
+        const double cx = deta[i], cy = -dxi[i];  // curl lambda_i
+        vx = f * cx;
+        vy = f * cy;
+        const double fx = lam[k] * dxi[j] + lam[j] * dxi[k], fy = lam[k] * deta[j] + lam[j] * deta[k];
+        dv = fx * cx + fy * cy;
+      }
+      for (int c = 0; c < 3; ++c) S[a][c] = (g.J0[c] * vx + g.J1[c] * vy) / g.detJ;
+      if (ev == ORC_EV_MAXWELL) S[a][3] = dv / g.detJ;
+    }
     return;
   }
   if (sp.kind == ORC_H1P2 || sp.kind == ORC_H1P3) {
