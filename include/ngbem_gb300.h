@@ -51,9 +51,12 @@ enum {
  * element (K + 1)(K - 1); numbered: the lowest-order edge dofs (edges by first appearance, as
  * BEM_RT0), then K per edge, then the interior ones per element.  A hierarchical basis of our
  * own (the RT0 shape, surface curls of H1 edge bubbles, interior l_j l_k curl l_i), Piola-mapped.
- * Traces ID and MAXWELL. */
+ * Traces ID and MAXWELL.
+ * BEM_HCURL1, BEM_HCURL2: HCurl of order 1, 2 on the surface (tangential traces of NGSolve
+ * HCurl(mesh, order=K)): n x the BEM_HDIV1 / BEM_HDIV2 shapes with the same dofs; traces ID,
+ * ROTATED_TRACE and MAXWELL_CURL as on BEM_HCURL. */
 enum { BEM_P0 = 0, BEM_P1 = 1, BEM_RT0 = 2, BEM_HCURL = 3, BEM_L2P1 = 4, BEM_L2P2 = 5, BEM_L2P3 = 6,
-       BEM_H1P2 = 7, BEM_H1P3 = 8, BEM_HDIV1 = 9, BEM_HDIV2 = 10 };
+       BEM_H1P2 = 7, BEM_H1P3 = 8, BEM_HDIV1 = 9, BEM_HDIV2 = 10, BEM_HCURL1 = 11, BEM_HCURL2 = 12 };
 /* trace evaluators: GetEvaluator(BND) (ID), DiffOpBoundaryRot (ROT), DiffOpHelmholtz (HELM),
  * DiffOpMaxwellNew (MAXWELL); reference src/diffops.hpp:12-338.  On BEM_HCURL: ID is the
  * tangential trace (GetEvaluator(BND) of an HCurl space), ROTATED_TRACE is

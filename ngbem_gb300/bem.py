@@ -82,7 +82,8 @@ class _MeshHandle:
 class TraceSpace:
     """Surface trace space: kind "P0" (SurfaceL2 order 0), "P1" (H1 order 1), "RT0" (HDivSurface order 0),
     "HCURL" (surface trace of HCurl order 0), "L2P1".."L2P3" (SurfaceL2 orders 1-3), "H1P2",
-    "H1P3" (H1 orders 2, 3), "HDIV1", "HDIV2" (HDivSurface orders 1, 2)."""
+    "H1P3" (H1 orders 2, 3), "HDIV1", "HDIV2" (HDivSurface orders 1, 2), "HCURL1", "HCURL2" (HCurl
+    orders 1, 2)."""
 
     def __init__(self, mesh: Mesh, kind: str, dual_mapping: bool = False, complex: bool = False, definedon=None):
         if kind not in KINDS:
@@ -185,11 +186,12 @@ def HDivSurface(mesh: Mesh, order: int = 0, complex: bool = False, definedon=Non
 
 
 def HCurl(mesh: Mesh, order: int = 0, complex: bool = False, definedon=None) -> TraceSpace:
-    """Surface trace of the lowest-order Nedelec space (NGSolve HCurl order 0 restricted to the
-    boundary): one dof per edge, on each triangle n x the RT0 shape function of that edge."""
-    if order != 0:
-        raise NotImplementedError("HCurl: only order 0 is supported")
-    return TraceSpace(mesh, "HCURL", False, complex, definedon)
+    """Surface trace of the Nedelec space (NGSolve HCurl restricted to the boundary): order 0
+    one dof per edge, on each triangle n x the RT0 shape function of that edge; order 1, 2 n x the
+    HDivSurface shapes of that order, with the same dofs."""
+    if order not in (0, 1, 2):
+        raise NotImplementedError("HCurl: orders 0, 1 and 2 are supported")
+    return TraceSpace(mesh, ("HCURL", "HCURL1", "HCURL2")[order], False, complex, definedon)
 
 
 def cluster_tree(space: TraceSpace, leafsize: int = 40):
@@ -764,7 +766,7 @@ def MaxwellSingleLayerPotentialOperator(space, kappa, definedon=None, intorder=3
 
 
 def _need_hcurl(space, what):
-    if space.kind != "HCURL":
+    if space.kind not in ("HCURL", "HCURL1", "HCURL2"):
         raise TypeError(f"{what} needs an HCurl space, got {space.kind}")
 
 
@@ -785,7 +787,7 @@ def MaxwellDoubleLayerPotentialOperator(trial_space, test_space, kappa, trial_de
     trace n x u of the HCurl trial space and the identity trace of the test space (HDivSurface,
     as in the reference's Maxwell tests, or HCurl).  method "dense" gives one root block."""
     _need_hcurl(trial_space, "MaxwellDoubleLayerPotentialOperator (trial space)")
-    if test_space.kind not in ("RT0", "HCURL"):
+    if test_space.kind not in ("RT0", "HCURL", "HDIV1", "HDIV2", "HCURL1", "HCURL2"):
         raise TypeError("MaxwellDoubleLayerPotentialOperator: the test space must be HDivSurface or HCurl")
     return IntegralOperator("maxwell_dl", _kappa(kappa), trial_space, test_space, "rotatedtrace", "id", intorder,
                             leafsize, eta, eps, method, testhmatrix, trial_definedon=trial_definedon,

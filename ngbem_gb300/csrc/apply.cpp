@@ -366,8 +366,8 @@ void MassOperator::build(SpaceH* trial, SpaceH* test, bool complex_vectors) {
     if (sp.kind >= BEM_L2P1 && sp.kind <= BEM_L2P3) return sp.kind - BEM_L2P1 + 1;
     if (sp.kind == BEM_H1P2) return 2;
     if (sp.kind == BEM_H1P3) return 3;
-    if (sp.kind == BEM_HDIV1) return 1;
-    if (sp.kind == BEM_HDIV2) return 2;
+    if (sp.kind == BEM_HDIV1 || sp.kind == BEM_HCURL1) return 1;
+    if (sp.kind == BEM_HDIV2 || sp.kind == BEM_HCURL2) return 2;
     return 1;
   };
   TrigRule r = make_trig_rule(std::max(4, degree(*trial) + degree(*test)));
@@ -398,15 +398,19 @@ void MassOperator::build(SpaceH* trial, SpaceH* test, bool complex_vectors) {
       dim = 1;
       return;
     }
-    if (sp.kind == BEM_HDIV1 || sp.kind == BEM_HDIV2) {
-      // the Piola map of the reference fields (hdiv_shape), J = (xp_2 - xp_0, xp_2 - xp_1)
-      const int K = sp.kind == BEM_HDIV1 ? 1 : 2;
+    if (sp.kind == BEM_HDIV1 || sp.kind == BEM_HDIV2 || sp.kind == BEM_HCURL1 || sp.kind == BEM_HCURL2) {
+      // the Piola map of the reference fields (hdiv_shape), J = (xp_2 - xp_0, xp_2 - xp_1);
+      // HCurl: n x it
+      const int K = sp.kind == BEM_HDIV1 || sp.kind == BEM_HCURL1 ? 1 : 2;
+      const bool curl = sp.kind == BEM_HCURL1 || sp.kind == BEM_HCURL2;
       piola(e, xi, eta, inv, n, xp);
       for (int a = 0; a < sp.nd; ++a) {
         const int sg = a < 3 * (K + 1) ? sp.sign[3 * e + a / (K + 1)] : 1;
-        double vx, vy;
+        double vx, vy, v[3];
         hdiv_shape<double>(K, a, xi, eta, sg, vx, vy);
-        for (int c = 0; c < 3; ++c) S[a][c] = ((xp[2][c] - xp[0][c]) * vx + (xp[2][c] - xp[1][c]) * vy) * inv;
+        for (int c = 0; c < 3; ++c) v[c] = ((xp[2][c] - xp[0][c]) * vx + (xp[2][c] - xp[1][c]) * vy) * inv;
+        for (int c = 0; c < 3; ++c)
+          S[a][c] = curl ? n[(c + 1) % 3] * v[(c + 2) % 3] - n[(c + 2) % 3] * v[(c + 1) % 3] : v[c];
       }
       dim = 3;
       return;

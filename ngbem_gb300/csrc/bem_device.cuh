@@ -331,6 +331,12 @@ template <> struct TraceInfo<TR_HDIV1ID> { static constexpr int ND = 6, DIM = 3;
 template <> struct TraceInfo<TR_HDIV2ID> { static constexpr int ND = 12, DIM = 3; };
 template <> struct TraceInfo<TR_HDIV1MAX> { static constexpr int ND = 6, DIM = 4; };
 template <> struct TraceInfo<TR_HDIV2MAX> { static constexpr int ND = 12, DIM = 4; };
+template <> struct TraceInfo<TR_HCURL1ID> { static constexpr int ND = 6, DIM = 3; };
+template <> struct TraceInfo<TR_HCURL2ID> { static constexpr int ND = 12, DIM = 3; };
+template <> struct TraceInfo<TR_HCURL1ROT> { static constexpr int ND = 6, DIM = 3; };
+template <> struct TraceInfo<TR_HCURL2ROT> { static constexpr int ND = 12, DIM = 3; };
+template <> struct TraceInfo<TR_HCURL1MAX> { static constexpr int ND = 6, DIM = 4; };
+template <> struct TraceInfo<TR_HCURL2MAX> { static constexpr int ND = 12, DIM = 4; };
 // traces that read the element's n x grad(lambda_a) table
 // the geometry of a curved element's rule point (PGeo): normal, rotated gradients, 1 / |J| and
 // the Piola offsets
@@ -474,11 +480,19 @@ __device__ __forceinline__ R trace_val(int a, int c, R xi, R eta, const R (*xp)[
     return a == 0 ? xi : (a == 1 ? eta : R(1) - xi - eta);
   }
   if constexpr (hdiv_trace(TR)) {
-    // HDivSurface of order K: the Piola map of the reference field, J = (xp_2 - xp_0, xp_2 - xp_1)
+    // HDivSurface of order K: the Piola map of the reference field, J = (xp_2 - xp_0, xp_2 - xp_1);
+    // HCurl of order K: n x it (ID), its negative (ROT, MAX), the divergence as the curl (MAX)
     R vx, vy;
     const R dv = hdiv_shape<R>(hdiv_order(TR), a, xi, eta, sgn, vx, vy);
     if (c == 3) return dv * invdetJ;
-    return ((xp[2][c] - xp[0][c]) * vx + (xp[2][c] - xp[1][c]) * vy) * invdetJ;
+    if constexpr (normal_trace(TR)) {
+      const int c1 = (c + 1) % 3, c2 = (c + 2) % 3;
+      const R p1 = ((xp[2][c2] - xp[0][c2]) * vx + (xp[2][c2] - xp[1][c2]) * vy) * invdetJ;
+      const R p2 = ((xp[2][c1] - xp[0][c1]) * vx + (xp[2][c1] - xp[1][c1]) * vy) * invdetJ;
+      return nrm[c1] * p1 - nrm[c2] * p2;
+    }
+    const R v = ((xp[2][c] - xp[0][c]) * vx + (xp[2][c] - xp[1][c]) * vy) * invdetJ;
+    return hcurl_hi_trace(TR) ? -v : v;
   }
   // edge dofs: the RT0 shape sgn (x - p_o) / |J| (o the vertex opposite the edge)
   const int o = (a + 2) % 3;

@@ -24,10 +24,15 @@ enum KernelId {
 // h1p_shape below); TR_H1P2HELM, TR_H1P3HELM: [n x grad_Gamma phi; phi] (DiffOpHelmholtz)
 // TR_HDIV1ID, TR_HDIV2ID: HDivSurface of order 1, 2 (identity trace, the Piola-mapped shape);
 // TR_HDIV1MAX, TR_HDIV2MAX: [shape; surface divergence] (DiffOpMaxwellNew) for hdiv_shape below
+// TR_HCURL1*, TR_HCURL2*: HCurl of order 1, 2, whose shapes are n x the HDivSurface shapes of the
+// same order and dofs: ID n x psi, ROT (DiffOpRotatedTrace) n x (n x psi) = -psi, MAX
+// (DiffOpMaxwell) [-psi; surface curl = surface divergence of psi]
 enum TraceKind { TR_P0 = 0, TR_P1 = 1, TR_ROT = 2, TR_HELM = 3, TR_MAX = 4, TR_RT0ID = 5,
                  TR_NED = 6, TR_NEDROT = 7, TR_NEDMAX = 8, TR_L2P1 = 9, TR_L2P2 = 10, TR_L2P3 = 11,
                  TR_H1P2 = 12, TR_H1P3 = 13, TR_H1P2ROT = 14, TR_H1P3ROT = 15, TR_H1P2HELM = 16,
-                 TR_H1P3HELM = 17, TR_HDIV1ID = 18, TR_HDIV2ID = 19, TR_HDIV1MAX = 20, TR_HDIV2MAX = 21 };
+                 TR_H1P3HELM = 17, TR_HDIV1ID = 18, TR_HDIV2ID = 19, TR_HDIV1MAX = 20, TR_HDIV2MAX = 21,
+                 TR_HCURL1ID = 22, TR_HCURL2ID = 23, TR_HCURL1ROT = 24, TR_HCURL2ROT = 25, TR_HCURL1MAX = 26,
+                 TR_HCURL2MAX = 27 };
 // traces of a discontinuous space of order >= 1: the element's dofs are consecutive
 // (first dof + local index) and its "signs" hold the order of its vertices by global number
 __host__ __device__ constexpr bool l2p_trace(int tr) { return tr >= TR_L2P1 && tr <= TR_L2P3; }
@@ -44,9 +49,14 @@ __host__ __device__ constexpr bool h1p_helm(int tr) { return tr == TR_H1P2HELM |
 
 // traces of HDivSurface of order K = 1, 2: per local edge k (vertices k, k + 1 mod 3) K + 1
 // dofs, then (K + 1)(K - 1) interior dofs
-__host__ __device__ constexpr bool hdiv_trace(int tr) { return tr >= TR_HDIV1ID && tr <= TR_HDIV2MAX; }
-__host__ __device__ constexpr int hdiv_order(int tr) { return tr == TR_HDIV1ID || tr == TR_HDIV1MAX ? 1 : 2; }
-__host__ __device__ constexpr bool hdiv_max(int tr) { return tr == TR_HDIV1MAX || tr == TR_HDIV2MAX; }
+// (also the HCurl traces of order 1, 2: the same dofs and reference fields)
+__host__ __device__ constexpr bool hdiv_trace(int tr) { return tr >= TR_HDIV1ID && tr <= TR_HCURL2MAX; }
+__host__ __device__ constexpr int hdiv_order(int tr) {
+  return tr == TR_HDIV1ID || tr == TR_HDIV1MAX || tr == TR_HCURL1ID || tr == TR_HCURL1ROT || tr == TR_HCURL1MAX ? 1 : 2;
+}
+__host__ __device__ constexpr bool hcurl_hi_trace(int tr) { return tr >= TR_HCURL1ID && tr <= TR_HCURL2MAX; }
+// traces that read the unit normal of the point (n x the HDiv shape)
+__host__ __device__ constexpr bool normal_trace(int tr) { return tr == TR_NED || tr == TR_HCURL1ID || tr == TR_HCURL2ID; }
 
 // Hierarchical basis of HDivSurface of order K = 1, 2 (BDM_K: all vector polynomials of degree
 // K; our own choice of basis, spanning the space of NGSolve's HDivSurface(order=K)) as

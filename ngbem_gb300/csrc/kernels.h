@@ -281,8 +281,12 @@ int launch_potential(int kid, int trt, const PotArgs& a, cudaStream_t s);
 #define BEM_H1P_COMBOS(X)                                              \
   BEM_H1P_KERNELS(X, TR_H1P2, TR_H1P2ROT, TR_H1P2HELM, TR_L2P1)         \
   BEM_H1P_KERNELS(X, TR_H1P3, TR_H1P3ROT, TR_H1P3HELM, TR_L2P2)
-// HDivSurface of order 1, 2: the Maxwell single layer (near field, projection, potentials)
-#define BEM_HDIV_COMBOS(X) X(K_MAXWELL_SL, TR_HDIV1MAX, TR_HDIV1MAX) X(K_MAXWELL_SL, TR_HDIV2MAX, TR_HDIV2MAX)
+// HDivSurface and HCurl of order 1, 2: the Maxwell single layer on either, the Maxwell double
+// layer from HCurl to HDivSurface or HCurl (near field, projection)
+#define BEM_HDIV_KERNELS(X, D, C)                                                                        \
+  X(K_MAXWELL_SL, D##MAX, D##MAX) X(K_MAXWELL_SL, C##MAX, C##MAX) X(K_MAXWELL_DL, C##ROT, D##ID)        \
+  X(K_MAXWELL_DL, C##ROT, C##ID)
+#define BEM_HDIV_COMBOS(X) BEM_HDIV_KERNELS(X, TR_HDIV1, TR_HCURL1) BEM_HDIV_KERNELS(X, TR_HDIV2, TR_HCURL2)
 
 // ---- tensor-core products for several right-hand sides (tc_matvec.cu) ---------------------
 // Operand panels are in the canonical K-major, no-swizzle layout of tcgen05 (core matrices of

@@ -124,7 +124,7 @@ __global__ void __launch_bounds__(128) nf_regular_kernel(NFArgs a) {
 #pragma unroll
       for (int r = 0; r < 3; ++r) { xpi[r][0] = qi.x - oi[r][0]; xpi[r][1] = qi.y - oi[r][1]; xpi[r][2] = qi.z - oi[r][2]; }
     }
-    if (PGi) pgeo_load<P, G::NEEDS_NX || TET == TR_NED, needs_rot(TET), piola_trace(TET)>(PGi[p], nx, roti, invi, xpi);
+    if (PGi) pgeo_load<P, G::NEEDS_NX || normal_trace(TET), needs_rot(TET), piola_trace(TET)>(PGi[p], nx, roti, invi, xpi);
     V ks[NT][NDJ];
 #pragma unroll
     for (int t = 0; t < NT; ++t)
@@ -137,7 +137,7 @@ __global__ void __launch_bounds__(128) nf_regular_kernel(NFArgs a) {
 #pragma unroll
         for (int r = 0; r < 3; ++r) { xpj[r][0] = qj.x - oj[r][0]; xpj[r][1] = qj.y - oj[r][1]; xpj[r][2] = qj.z - oj[r][2]; }
       }
-      if (PGj) pgeo_load<P, G::NEEDS_NY || TRT == TR_NED, needs_rot(TRT), piola_trace(TRT)>(PGj[q], ny, rotj, invj, xpj);
+      if (PGj) pgeo_load<P, G::NEEDS_NY || normal_trace(TRT), needs_rot(TRT), piola_trace(TRT)>(PGj[q], ny, rotj, invj, xpj);
       const P dx = Dx + (qi.x - qj.x), dy = Dy + (qi.y - qj.y), dz = Dz + (qi.z - qj.z);
       V kv[NC];
       G::eval(dx, dy, dz, nx, ny, kappa, kv);
@@ -389,7 +389,7 @@ void launch_nf_regular_h1p2(int kid, int prec, int trt, int tet, const NFArgs& a
 void launch_nf_singular_h1p2(int kid, int prec, int trt, int tet, const NFArgs& a, cudaStream_t s);
 void launch_nf_regular_h1p3(int kid, int prec, int trt, int tet, const NFArgs& a, cudaStream_t s);
 void launch_nf_singular_h1p3(int kid, int prec, int trt, int tet, const NFArgs& a, cudaStream_t s);
-// HDivSurface of order 1, 2 (BEM_HDIV_COMBOS): nearfield_hdiv.cu
+// HDivSurface and HCurl of order 1, 2 (BEM_HDIV_COMBOS): nearfield_hdiv.cu, nearfield_hdivs.cu
 void launch_nf_regular_hdiv(int kid, int prec, int trt, int tet, const NFArgs& a, cudaStream_t s);
 void launch_nf_singular_hdiv(int kid, int prec, int trt, int tet, const NFArgs& a, cudaStream_t s);
 // bodies of those launchers: one (kernel, trial trace, test trace) combination

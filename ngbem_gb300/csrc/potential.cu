@@ -115,7 +115,7 @@ __global__ void __launch_bounds__(POT_THREADS) pot_eval_kernel(PotArgs a) {
 // (kernel, trial trace) pairs of the operators: the scalar kernels with P0 / P1 (SurfaceL2 of
 // order 1..3, H1 of order 2, 3) identity traces, the hypersingular kernels with their curl
 // traces, the Maxwell single layer with RT0 (and HDivSurface of order 1, 2) and in its curl
-// form with HCurl, and the Maxwell
+// form with HCurl (of order 0-2), and the Maxwell
 // double layer with the rotated trace of HCurl.  The sum leaves out the kernel terms' factors,
 // as the reference's PotentialCF does (src/ngbem.cpp:1228-1232); for the double layer's six
 // cross-product terms (factors +-1) that is the reference's field, not the signed one.
@@ -140,7 +140,9 @@ __global__ void __launch_bounds__(POT_THREADS) pot_eval_kernel(PotArgs a) {
   X(K_HELMHOLTZ_DL, TR_H1P3, cpx<double>) X(K_HELMHOLTZ_CF, TR_L2P1, cpx<double>)               \
   X(K_HELMHOLTZ_CF, TR_L2P2, cpx<double>) X(K_HELMHOLTZ_CF, TR_L2P3, cpx<double>)               \
   X(K_HELMHOLTZ_CF, TR_H1P2, cpx<double>) X(K_HELMHOLTZ_CF, TR_H1P3, cpx<double>)               \
-  X(K_MAXWELL_SL, TR_HDIV1MAX, cpx<double>) X(K_MAXWELL_SL, TR_HDIV2MAX, cpx<double>)
+  X(K_MAXWELL_SL, TR_HDIV1MAX, cpx<double>) X(K_MAXWELL_SL, TR_HDIV2MAX, cpx<double>)               \
+  X(K_MAXWELL_SL, TR_HCURL1MAX, cpx<double>) X(K_MAXWELL_SL, TR_HCURL2MAX, cpx<double>)             \
+  X(K_MAXWELL_DL, TR_HCURL1ROT, cpx<double>) X(K_MAXWELL_DL, TR_HCURL2ROT, cpx<double>)
 
 int potential_dim(int kid, int trt) {
 #define X(K, T, V) \

@@ -198,7 +198,7 @@ def load_vector(space, f, order: int = 6) -> np.ndarray:
     on = dofs[:, 0] >= 0
     x, n, detj, lam, w = _geometry(mesh, order)
     fv = np.asarray(f(x, n))
-    vector = space.kind in ("RT0", "HCURL", "HDIV1", "HDIV2")
+    vector = space.kind in ("RT0", "HCURL", "HDIV1", "HDIV2", "HCURL1", "HCURL2")
     multi = fv.ndim == (4 if vector else 3)
     if not multi:
         fv = fv[..., None]
@@ -226,7 +226,7 @@ def load_vector(space, f, order: int = 6) -> np.ndarray:
         nd = phi.shape[-1]
         idx = dofs[on, 0][:, None] + np.arange(nd)[None, :]
         np.add.at(out, idx.ravel(), contrib[on].reshape(-1, contrib.shape[-1]))
-    elif space.kind.startswith("HDIV"):
+    elif space.kind.startswith("HDIV") or space.kind in ("HCURL1", "HCURL2"):
         # the Piola map J v / |J| of the reference fields, J per element (flat) or per point
         xi, eta, _ = triangle_rule(order)
         if curved:
@@ -239,9 +239,12 @@ def load_vector(space, f, order: int = 6) -> np.ndarray:
             J0 = np.broadcast_to((P[:, 0] - P[:, 2])[:, None], x.shape)
             J1 = np.broadcast_to((P[:, 1] - P[:, 2])[:, None], x.shape)
             dj = np.broadcast_to(detj[:, None], x.shape[:2])
-        fields, _ = hdiv_fields(int(space.kind[4:]), lam, signs)           # (nt, nq, nd, 2)
+        fields, _ = hdiv_fields(int(space.kind[-1]), lam, signs)           # (nt, nq, nd, 2)
         psi = (J0[:, :, None, :] * fields[..., 0, None] + J1[:, :, None, :] * fields[..., 1, None]) \
             / dj[:, :, None, None]
+        if space.kind.startswith("HCURL"):  # n x the HDivSurface shape
+            nn = n if n.ndim == 3 else np.broadcast_to(n[:, None, :], x.shape)
+            psi = np.cross(nn[:, :, None, :], psi)
         contrib = np.einsum("tq,tqcm,tqac->tam", W, fv, psi)
         table = space.dof_table()
         np.add.at(out, table[on].ravel(), contrib[on].reshape(-1, contrib.shape[-1]))

@@ -380,10 +380,10 @@ struct Space {
         }
         for (int j = 0; j < pf; ++j) d[3 + 3 * pe + j] = m.nv + m.ne * pe + e * pf + j;
       }
-    } else if (kind == ORC_HDIV1 || kind == ORC_HDIV2) {
-      // HDivSurface of order K: per local edge K + 1 dofs (the edge's lowest-order dof = the
-      // edge id, then ne + edge K + m - 1), then (K + 1)(K - 1) interior dofs per element
-      const int K = kind == ORC_HDIV1 ? 1 : 2, nin = (K + 1) * (K - 1);
+    } else if (kind == ORC_HDIV1 || kind == ORC_HDIV2 || kind == ORC_HCURL1 || kind == ORC_HCURL2) {
+      // HDivSurface (and HCurl) of order K: per local edge K + 1 dofs (the edge's lowest-order
+      // dof = the edge id, then ne + edge K + m - 1), then (K + 1)(K - 1) interior dofs per element
+      const int K = kind == ORC_HDIV1 || kind == ORC_HCURL1 ? 1 : 2, nin = (K + 1) * (K - 1);
       nd = (K + 1) * (K + 2);
       ndof = m.ne * (K + 1) + m.nt * nin;
       dofs.resize((size_t)m.nt * nd);
@@ -411,7 +411,7 @@ struct Space {
 };
 
 static int trace_dim(int kind, int ev) {
-  if (ev == ORC_EV_ID) return (kind == ORC_RT0 || kind == ORC_HCURL || kind == ORC_HDIV1 || kind == ORC_HDIV2) ? 3 : 1;
+  if (ev == ORC_EV_ID) return (kind == ORC_RT0 || kind == ORC_HCURL || kind >= ORC_HDIV1) ? 3 : 1;
   if (ev == ORC_EV_ROT || ev == ORC_EV_ROTATED_TRACE) return 3;
   return 4;  // HELM, MAXWELL, MAXWELL_CURL
 }
@@ -442,14 +442,17 @@ static void eval_trace(const Mesh& m, const Space& sp, int ev, int e, double xi,
       S[a][0] = dubiner(sp.kind - ORC_L2P1 + 1, a, xi, eta, sp.sign[3 * e], sp.sign[3 * e + 1]);
     return;
   }
-  if (sp.kind == ORC_HDIV1 || sp.kind == ORC_HDIV2) {
+  if (sp.kind == ORC_HDIV1 || sp.kind == ORC_HDIV2 || sp.kind == ORC_HCURL1 || sp.kind == ORC_HCURL2) {
     // HDivSurface of order K (DiffOpMaxwellNew on NGSolve's HDivSurface element, restated for
     // a hierarchical BDM_K basis of our own): reference fields v on the triangle with vertices
     // (1,0), (0,1), (0,0), Piola-mapped J v / |J|, surface divergence (div v) / |J|.  Per local
     // edge k (vertices i = k, j = k+1; orientation s): m = 0 the RT0 shape s (xhat - vhat_o);
     // m = 1 the curl (d/deta, -d/dxi) of l_i l_j; m = 2 that of s l_i l_j (l_j - l_i).
-    // Interior (K = 2): l_j l_k curl(l_i).
-    const int K = sp.kind == ORC_HDIV1 ? 1 : 2;
+    // Interior (K = 2): l_j l_k curl(l_i).  HCurl of order K: phi = n x those shapes, traces as
+    // on the lowest-order HCurl below (ID phi, ROTATED_TRACE n x phi, MAXWELL_CURL
+    // [n x phi; the divergence of the HDiv shape]).
+    const int K = sp.kind == ORC_HDIV1 || sp.kind == ORC_HCURL1 ? 1 : 2;
+    const bool hcurl = sp.kind == ORC_HCURL1 || sp.kind == ORC_HCURL2;
     const double lam[3] = {xi, eta, 1.0 - xi - eta};
     const double dxi[3] = {1.0, 0.0, -1.0}, deta[3] = {0.0, 1.0, -1.0};  // d lambda / d(xi, eta)
     const double vh[3][2] = {{1.0, 0.0}, {0.0, 1.0}, {0.0, 0.0}};
@@ -486,8 +489,22 @@ static void eval_trace(const Mesh& m, const Space& sp, int ev, int e, double xi,
         const double fx = lam[k] * dxi[j] + lam[j] * dxi[k], fy = lam[k] * deta[j] + lam[j] * deta[k];
         dv = fx * cx + fy * cy;
       }
-      for (int c = 0; c < 3; ++c) S[a][c] = (g.J0[c] * vx + g.J1[c] * vy) / g.detJ;
-      if (ev == ORC_EV_MAXWELL) S[a][3] = dv / g.detJ;
+      double psi[3];
+      for (int c = 0; c < 3; ++c) psi[c] = (g.J0[c] * vx + g.J1[c] * vy) / g.detJ;
+      if (!hcurl) {
+        for (int c = 0; c < 3; ++c) S[a][c] = psi[c];
+        if (ev == ORC_EV_MAXWELL) S[a][3] = dv / g.detJ;
+        continue;
+      }
+      double phi[3], rot[3];
+      cross3(g.n, psi, phi);
+      if (ev == ORC_EV_ID) {
+        for (int c = 0; c < 3; ++c) S[a][c] = phi[c];
+        continue;
+      }
+      cross3(g.n, phi, rot);
+      for (int c = 0; c < 3; ++c) S[a][c] = rot[c];
+      if (ev == ORC_EV_MAXWELL_CURL) S[a][3] = dv / g.detJ;
     }
     return;
   }

@@ -46,8 +46,9 @@ enum {
 // then p - 1 per edge (edge order of orc_mesh_edges), then per element
 // ORC_HDIV1, ORC_HDIV2: HDivSurface of order K = 1, 2 (BDM_K): per local edge K + 1 dofs (the
 // edge id, then ne + edge K + m - 1), then (K + 1)(K - 1) per element after all edge dofs
+// ORC_HCURL1, ORC_HCURL2: HCurl of order K = 1, 2: n x the HDIV shapes, the same dofs
 enum { ORC_P0 = 0, ORC_P1 = 1, ORC_RT0 = 2, ORC_HCURL = 3, ORC_L2P1 = 4, ORC_L2P2 = 5, ORC_L2P3 = 6,
-       ORC_H1P2 = 7, ORC_H1P3 = 8, ORC_HDIV1 = 9, ORC_HDIV2 = 10 };
+       ORC_H1P2 = 7, ORC_H1P3 = 8, ORC_HDIV1 = 9, ORC_HDIV2 = 10, ORC_HCURL1 = 11, ORC_HCURL2 = 12 };
 // trace evaluators; on ORC_HCURL: ID the tangential trace, ROTATED_TRACE DiffOpRotatedTrace,
 // MAXWELL_CURL DiffOpMaxwell
 enum { ORC_EV_ID = 0, ORC_EV_ROT = 1, ORC_EV_HELM = 2, ORC_EV_MAXWELL = 3,

@@ -1,5 +1,5 @@
-"""HDivSurface of order 1 and 2 on the GPU against the FP64 oracle (the reference's Maxwell
-tests use higher-order HDivSurface: tests/test_Maxwell_Mie.py:24, with Curve(order)).
+"""HDivSurface and HCurl of order 1 and 2 on the GPU against the FP64 oracle (the reference's
+Maxwell tests use higher orders: tests/test_Maxwell_Mie.py:24, tests/test_Maxwell_Box.py:19-21).
 
 * The Maxwell single layer (DiffOpMaxwellNew traces, src/diffops.hpp:263-338): dense FP64
   within 1e-10 of the oracle on flat and curved meshes; its block on the lowest-order dofs is
@@ -7,6 +7,10 @@ tests use higher-order HDivSurface: tests/test_Maxwell_Mie.py:24, with Curve(ord
 * H-matrices within the ACA tolerance of the oracle's in both directions with the same block
   lists; mixed precision within 1e-6 of FP64.
 * Potentials and mass matrices against the oracle.
+* HCurl of order 1, 2: the curl single layer and the Maxwell double layer (HCurl to HDivSurface
+  or HCurl) against the oracle, with their lowest-order blocks the order-0 operators; and the
+  Calderon identity of the reference's Maxwell test, V j = (-1/2 M + K) m, on the exact traces
+  of a dipole field, whose residual falls with the order.
 """
 import numpy as np
 import pytest
@@ -89,3 +93,85 @@ def test_potential_and_mass(oracle, K):
     x = rng.standard_normal(sp.ndof)
     y = (M * torch.from_numpy(x).to(torch.complex128 if M.is_complex else torch.float64).cuda()).cpu().numpy()
     assert rel(y, oracle.mass_matrix(m, kind, kind, order=4) @ x) < 1e-12
+
+
+HC_COMBOS = [("maxwell_sl", "HCURL", "HCURL", "maxwellcurl", "maxwellcurl"),
+             ("maxwell_dl", "HCURL", "HDIV", "rotatedtrace", "id"),
+             ("maxwell_dl", "HCURL", "HCURL", "rotatedtrace", "id")]
+ORDER0 = {"HCURL": "HCURL", "HDIV": "RT0"}
+
+
+def _space(m, fam, K):
+    kind = (fam + str(K)) if K else ORDER0[fam]
+    return kind, nb.TraceSpace(m, kind, complex=True)
+
+
+@pytest.mark.parametrize("g", [1, 3])
+@pytest.mark.parametrize("K", [1, 2])
+@pytest.mark.parametrize("kernel,ftr,fte,e1,e2", HC_COMBOS, ids=[f"{c[0]}-{c[2]}" for c in HC_COMBOS])
+def test_hcurl_dense_parity(oracle, kernel, ftr, fte, e1, e2, K, g):
+    m = icosphere(1).Curve(g)
+    (ktr, str_), (kte, ste) = _space(m, ftr, K), _space(m, fte, K)
+    kw = dict(intorder_singular=4, intorder_regular=3)
+    D = bem.IntegralOperator(kernel, KAPPA, str_, ste, e1, e2, 3, 40, 2.0, 1e-8, "dense", False, **kw).mat.to_dense()
+    Do = oracle.dense_matrix(kernel, m, ktr, kte, kappa=KAPPA, trial_eval=e1, test_eval=e2, **kw)
+    assert rel(D, Do) < 1e-10
+    (_, s0), (_, t0) = _space(m, ftr, 0), _space(m, fte, 0)
+    R = bem.IntegralOperator(kernel, KAPPA, s0, t0, e1, e2, 3, 40, 2.0, 1e-8, "dense", False, **kw).mat.to_dense()
+    assert rel(D[: t0.ndof, : s0.ndof], R) < 1e-12
+
+
+def test_hcurl_hmatrix_potential_and_mass(oracle):
+    m = ellipsoid(2, (1.0, 0.8, 0.6)).Curve(2)
+    HC, HD = nb.HCurl(m, order=1, complex=True), nb.HDivSurface(m, order=1, complex=True)
+    op = nb.MaxwellDoubleLayerPotentialOperator(HC, HD, KAPPA, intorder=3, leafsize=40, eps=1e-8)
+    H = oracle.OracleOperator("maxwell_dl", m, "HCURL1", "HDIV1", kappa=KAPPA, trial_eval="rotatedtrace",
+                              test_eval="id", intorder=3, leafsize=40, eta=2.0, eps=1e-8)
+    b, ob = op.mat.blocks(), H.blocks()
+    for k in ("rowcl", "colcl", "near"):
+        assert np.array_equal(b[k], ob[k])
+    rng = np.random.default_rng(41)
+    x = rng.standard_normal(HC.ndof) + 1j * rng.standard_normal(HC.ndof)
+    assert rel((op.mat * torch.from_numpy(x).cuda()).cpu().numpy(), H.mult(x)) < 1e-7
+    pts = np.array([[2.0, 0.3, -0.1], [-1.5, 1.0, 0.5]])
+    for kernel, ev, o in (("maxwell_dl", "rotatedtrace", op),
+                          ("maxwell_sl", "maxwellcurl",
+                           nb.MaxwellSingleLayerPotentialOperatorCurl(HC, KAPPA, intorder=3, eps=1e-8))):
+        val = o.GetPotential(torch.from_numpy(x).cuda())(pts).cpu().numpy().reshape(len(pts), -1)
+        ref = oracle.potential(kernel, m, "HCURL1", x, pts, kappa=KAPPA, trial_eval=ev, intorder=3)
+        assert rel(val, ref.reshape(len(pts), -1)) < 1e-11
+    M = nb.MassOperator(HC, HD, complex=True)
+    y = (M * torch.from_numpy(x).cuda()).cpu().numpy()
+    assert rel(y, oracle.mass_matrix(m, "HCURL1", "HDIV1", order=4) @ x) < 1e-12
+
+
+def test_calderon_identity_higher_order(oracle):
+    """The reference's Maxwell test identity V j = (-1/2 M + K) m with the L2 projections of the
+    exact traces of a dipole field, on the curved sphere: the residual falls with the order."""
+    from _maxwell_fields import calderon_residual, curl, field
+    from ngbem_gb300.forms import load_vector
+    m = icosphere(2).Curve(3)
+    kappa = 1.0
+    res = []
+    for K in (0, 1, 2):
+        HC, HD = nb.HCurl(m, order=K, complex=True), nb.HDivSurface(m, order=K, complex=True)
+        kc, kd = HC.kind, HD.kind
+
+        def mex(x, n):
+            return -np.cross(np.cross(n, field(x, kappa)), n)
+
+        def jex(x, n):
+            return np.cross(n, curl(x, kappa) / kappa)
+
+        mh = np.linalg.solve(oracle.mass_matrix(m, kc, kc, order=8), load_vector(HC, mex, order=10))
+        jh = np.linalg.solve(oracle.mass_matrix(m, kd, kd, order=8), load_vector(HD, jex, order=10))
+        kw = dict(intorder=6, leafsize=40, eps=1e-10)
+        V = nb.MaxwellSingleLayerPotentialOperator(HD, kappa, **kw)
+        Kop = nb.MaxwellDoubleLayerPotentialOperator(HC, HD, kappa, **kw)
+        M = nb.MassOperator(HC, HD, complex=True)
+
+        def mv(A, v):
+            return (A * torch.from_numpy(np.ascontiguousarray(v)).cuda()).cpu().numpy()
+
+        res.append(calderon_residual(mv(V.mat, jh), mv(Kop.mat, mh), mv(M, mh)))
+    assert res[1] < 0.5 * res[0] and res[2] < 0.5 * res[1], res

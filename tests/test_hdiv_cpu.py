@@ -1,4 +1,4 @@
-"""HDivSurface of order 1 and 2 on the CPU (the reference's Maxwell tests use higher-order
+"""HDivSurface and HCurl of order 1 and 2 on the CPU (the reference's Maxwell tests use higher-order
 HDivSurface: tests/test_Maxwell_Mie.py:24).  The oracle's basis against the properties that
 define the space, and the library's spaces against the oracle's:
 
@@ -10,7 +10,9 @@ define the space, and the library's spaces against the oracle's:
 * the span: on one flat triangle the (K + 1)(K + 2) functions span all tangential vector
   polynomials of degree K;
 * the lowest-order dofs are the RT0 functions with RT0's numbering;
-* dof tables, cluster trees and partitions of the library equal the oracle's, bit for bit.
+* dof tables, cluster trees and partitions of the library equal the oracle's, bit for bit;
+* HCurl of order 1, 2 (n x those shapes): tangential continuity, the order-0 HCurl functions as
+  its lowest-order part, the library's space and load vectors against the oracle.
 """
 import numpy as np
 import pytest
@@ -145,3 +147,63 @@ def test_library_space_matches_the_oracle(oracle, K):
                                eta=2.0, eps=1e-3).blocks()
     for k in ("rowcl", "colcl", "near"):
         assert np.array_equal(part[k], ob[k])
+
+
+@pytest.mark.parametrize("K", [1, 2])
+def test_hcurl_tangential_continuity_and_lowest_order(oracle, K):
+    """HCurl of order K (n x the HDivSurface shapes): the tangential component along every edge
+    is the same from both sides, and the lowest-order dofs are the order-0 HCurl functions."""
+    m = ellipsoid(1)
+    kind = f"HCURL{K}"
+    X, T = m.vertices, m.triangles
+    seen = {}
+    for e, t in enumerate(T):
+        for k in range(3):
+            key = tuple(sorted((t[k], t[(k + 1) % 3])))
+            if key not in seen:
+                seen[key] = (e, k)
+                continue
+            e1, k1 = seen[key]
+            tau = X[key[1]] - X[key[0]]
+            for s in (0.2, 0.6):
+                x1 = _ref_point(k1, s)
+                x2 = _ref_point(k, s if T[e1][k1] == t[k] else 1 - s)
+                S1, d1 = oracle.eval_trace(m, kind, "id", e1, *x1)
+                S2, d2 = oracle.eval_trace(m, kind, "id", e, *x2)
+                f1 = dict(zip(d1.tolist(), S1[:, :3] @ tau))
+                f2 = dict(zip(d2.tolist(), S2[:, :3] @ tau))
+                for d in set(f1) | set(f2):
+                    assert abs(f1.get(d, 0.0) - f2.get(d, 0.0)) < 1e-13
+    for ev in ("id", "rotatedtrace", "maxwellcurl"):
+        S, d = oracle.eval_trace(m, kind, ev, 3, 0.21, 0.33)
+        R, dr = oracle.eval_trace(m, "HCURL", ev, 3, 0.21, 0.33)
+        for k in range(3):
+            assert d[k * (K + 1)] == dr[k]
+            assert np.abs(S[k * (K + 1)] - R[k]).max() < 1e-15
+
+
+@pytest.mark.parametrize("K", [1, 2])
+def test_hcurl_library_space_and_load_vector(oracle, K):
+    from ngbem_gb300.forms import _geometry, load_vector
+    m = icosphere(2).Curve(3)
+    kind = f"HCURL{K}"
+    sp = nb.HCurl(m, order=K)
+    assert sp.ndof == oracle.ndof(m, kind)
+    assert np.array_equal(sp.dof_table()[7], oracle.eval_trace(m, kind, "id", 7, 0.2, 0.3)[1])
+    p1, ci1, cd1 = nb.cluster_tree(sp, 30)
+    p2, ci2, cd2 = oracle.cluster_tree(m, kind, 30)
+    assert np.array_equal(p1, p2) and np.array_equal(cd1.view(np.int64), cd2.view(np.int64))
+
+    def f(x, n):
+        return np.stack([x[..., 1], x[..., 2] * x[..., 0], np.ones(x.shape[:2])], axis=-1)
+
+    b = load_vector(sp, f, order=4)
+    x, n, detj, lam, w = _geometry(m, 4)
+    xi, eta, _ = triangle_rule(4)
+    fv = f(x, n)
+    ref = np.zeros(sp.ndof)
+    for e in range(m.nt):
+        for q in range(len(w)):
+            S, d = oracle.eval_trace(m, kind, "id", e, xi[q], eta[q])
+            ref[d] += w[q] * detj[e, q] * (S[:, :3] @ fv[e, q])
+    assert np.abs(b - ref).max() < 1e-13 * np.abs(ref).max()

@@ -85,7 +85,7 @@ def test_argument_errors_are_status_codes():
     # region spaces and operator regions
     out = C.c_void_p()
     assert _lib.lib.bem_space_create_on(None, 0, 0, None, C.byref(out)) == _lib.BEM_ERR_ARG
-    assert _lib.lib.bem_space_create_on(sp._mh.h, 11, 0, None, C.byref(out)) == _lib.BEM_ERR_ARG
+    assert _lib.lib.bem_space_create_on(sp._mh.h, 13, 0, None, C.byref(out)) == _lib.BEM_ERR_ARG
     none = np.zeros(m.nt, dtype=np.uint8)
     assert _lib.lib.bem_space_create_on(sp._mh.h, 0, 0, C.c_void_p(none.ctypes.data), C.byref(out)) == \
         _lib.BEM_ERR_ARG and b"no elements" in _lib.lib.bem_last_error()
