@@ -117,7 +117,7 @@ def test_maxwell_factory_argument_checks():
     with pytest.raises(TypeError):
         nb.MaxwellSingleLayerPotentialOperator(RT, None)
     with pytest.raises(NotImplementedError):
-        nb.HCurl(m, order=1)
+        nb.HCurl(m, order=3)
 
 
 def test_mesh_generators():
