@@ -147,7 +147,10 @@ def test_hcurl_hmatrix_potential_and_mass(oracle):
 
 def test_calderon_identity_higher_order(oracle):
     """The reference's Maxwell test identity V j = (-1/2 M + K) m with the L2 projections of the
-    exact traces of a dipole field, on the curved sphere: the residual falls with the order."""
+    exact traces of a dipole field, on the curved sphere: the residual falls with the order.
+    Order 1 keeps the piecewise-constant divergences of order 0 (BDM_1), which bound the
+    single layer's div-div part, so its gain is small; order 2 has linear divergences
+    (measured on a GB300: 6.9e-3, 4.0e-3, 2.6e-4)."""
     from _maxwell_fields import calderon_residual, curl, field
     from ngbem_gb300.forms import load_vector
     m = icosphere(2).Curve(3)
@@ -174,4 +177,4 @@ def test_calderon_identity_higher_order(oracle):
             return (A * torch.from_numpy(np.ascontiguousarray(v)).cuda()).cpu().numpy()
 
         res.append(calderon_residual(mv(V.mat, jh), mv(Kop.mat, mh), mv(M, mh)))
-    assert res[1] < 0.5 * res[0] and res[2] < 0.5 * res[1], res
+    assert res[1] < 0.8 * res[0] and res[2] < 0.1 * res[1], res
