@@ -54,9 +54,13 @@ enum {
  * Traces ID and MAXWELL.
  * BEM_HCURL1, BEM_HCURL2: HCurl of order 1, 2 on the surface (tangential traces of NGSolve
  * HCurl(mesh, order=K)): n x the BEM_HDIV1 / BEM_HDIV2 shapes with the same dofs; traces ID,
- * ROTATED_TRACE and MAXWELL_CURL as on BEM_HCURL. */
+ * ROTATED_TRACE and MAXWELL_CURL as on BEM_HCURL.
+ * BEM_HDIV3, BEM_HDIV4, BEM_HCURL3, BEM_HCURL4: the same of order 3, 4 (20 and 30 dofs per
+ * element), for the operators of the reference's Maxwell tests: the Maxwell single layer on
+ * HDivSurface of order 3, 4 and the double layer from HCurl to HDivSurface of order 3. */
 enum { BEM_P0 = 0, BEM_P1 = 1, BEM_RT0 = 2, BEM_HCURL = 3, BEM_L2P1 = 4, BEM_L2P2 = 5, BEM_L2P3 = 6,
-       BEM_H1P2 = 7, BEM_H1P3 = 8, BEM_HDIV1 = 9, BEM_HDIV2 = 10, BEM_HCURL1 = 11, BEM_HCURL2 = 12 };
+       BEM_H1P2 = 7, BEM_H1P3 = 8, BEM_HDIV1 = 9, BEM_HDIV2 = 10, BEM_HCURL1 = 11, BEM_HCURL2 = 12,
+       BEM_HDIV3 = 13, BEM_HDIV4 = 14, BEM_HCURL3 = 15, BEM_HCURL4 = 16 };
 /* trace evaluators: GetEvaluator(BND) (ID), DiffOpBoundaryRot (ROT), DiffOpHelmholtz (HELM),
  * DiffOpMaxwellNew (MAXWELL); reference src/diffops.hpp:12-338.  On BEM_HCURL: ID is the
  * tangential trace (GetEvaluator(BND) of an HCurl space), ROTATED_TRACE is

@@ -24,7 +24,8 @@ KERNELS = {"laplace_sl": 0, "laplace_dl": 1, "laplace_hs": 2, "helmholtz_sl": 3,
            "helmholtz_hs": 5, "helmholtz_cf": 6, "maxwell_sl": 7, "helmholtz_sl_dkappa": 8,
            "maxwell_dl": 9}
 KINDS = {"P0": 0, "P1": 1, "RT0": 2, "HCURL": 3, "L2P1": 4, "L2P2": 5, "L2P3": 6, "H1P2": 7, "H1P3": 8,
-         "HDIV1": 9, "HDIV2": 10, "HCURL1": 11, "HCURL2": 12}
+         "HDIV1": 9, "HDIV2": 10, "HCURL1": 11, "HCURL2": 12, "HDIV3": 13, "HDIV4": 14, "HCURL3": 15,
+         "HCURL4": 16}
 EVALS = {"id": 0, "rot": 1, "helm": 2, "maxwell": 3, "rotatedtrace": 4, "maxwellcurl": 5}
 PRECISIONS = {"fp64": 0, "mixed": 1}
 METHODS = {"aca": 0, "dense": 1}

@@ -82,8 +82,8 @@ class _MeshHandle:
 class TraceSpace:
     """Surface trace space: kind "P0" (SurfaceL2 order 0), "P1" (H1 order 1), "RT0" (HDivSurface order 0),
     "HCURL" (surface trace of HCurl order 0), "L2P1".."L2P3" (SurfaceL2 orders 1-3), "H1P2",
-    "H1P3" (H1 orders 2, 3), "HDIV1", "HDIV2" (HDivSurface orders 1, 2), "HCURL1", "HCURL2" (HCurl
-    orders 1, 2)."""
+    "H1P3" (H1 orders 2, 3), "HDIV1".."HDIV4" (HDivSurface orders 1-4), "HCURL1".."HCURL4" (HCurl
+    orders 1-4)."""
 
     def __init__(self, mesh: Mesh, kind: str, dual_mapping: bool = False, complex: bool = False, definedon=None):
         if kind not in KINDS:
@@ -176,22 +176,24 @@ def H1(mesh: Mesh, order: int = 1, complex: bool = False, definedon=None) -> Tra
 
 def HDivSurface(mesh: Mesh, order: int = 0, complex: bool = False, definedon=None) -> TraceSpace:
     """Normal-continuous tangential fields on the surface (NGSolve HDivSurface): order 0 the
-    lowest-order Raviart-Thomas space (one dof per edge), order 1, 2 all vector polynomials of
-    that degree (K + 1 dofs per edge, (K + 1)(K - 1) per element) in a hierarchical basis of our
-    own: the RT0 shapes, the surface curls of H1 edge bubbles and, for order 2, the interior
-    fields l_j l_k curl(l_i), all Piola-mapped."""
-    if order not in (0, 1, 2):
-        raise NotImplementedError("HDivSurface: orders 0, 1 and 2 are supported")
-    return TraceSpace(mesh, ("RT0", "HDIV1", "HDIV2")[order], False, complex, definedon)
+    lowest-order Raviart-Thomas space (one dof per edge), order K = 1..4 all vector polynomials of
+    degree K (K + 1 dofs per edge, (K + 1)(K - 1) per element) in a hierarchical basis of our
+    own: the RT0 shapes, the surface curls of H1 edge bubbles and the interior fields
+    l_j l_k xi^p eta^q curl(l_i), all Piola-mapped.  Orders 3, 4 serve the Maxwell single layer
+    (and the double layer from HCurl of order 3)."""
+    if order not in (0, 1, 2, 3, 4):
+        raise NotImplementedError("HDivSurface: orders 0 to 4 are supported")
+    return TraceSpace(mesh, ("RT0", "HDIV1", "HDIV2", "HDIV3", "HDIV4")[order], False, complex, definedon)
 
 
 def HCurl(mesh: Mesh, order: int = 0, complex: bool = False, definedon=None) -> TraceSpace:
     """Surface trace of the Nedelec space (NGSolve HCurl restricted to the boundary): order 0
-    one dof per edge, on each triangle n x the RT0 shape function of that edge; order 1, 2 n x the
-    HDivSurface shapes of that order, with the same dofs."""
-    if order not in (0, 1, 2):
-        raise NotImplementedError("HCurl: orders 0, 1 and 2 are supported")
-    return TraceSpace(mesh, ("HCURL", "HCURL1", "HCURL2")[order], False, complex, definedon)
+    one dof per edge, on each triangle n x the RT0 shape function of that edge; order 1..4 n x the
+    HDivSurface shapes of that order, with the same dofs (order 3 serves the Maxwell double
+    layer, order 4 mass matrices and load vectors)."""
+    if order not in (0, 1, 2, 3, 4):
+        raise NotImplementedError("HCurl: orders 0 to 4 are supported")
+    return TraceSpace(mesh, ("HCURL", "HCURL1", "HCURL2", "HCURL3", "HCURL4")[order], False, complex, definedon)
 
 
 def cluster_tree(space: TraceSpace, leafsize: int = 40):
@@ -766,7 +768,7 @@ def MaxwellSingleLayerPotentialOperator(space, kappa, definedon=None, intorder=3
 
 
 def _need_hcurl(space, what):
-    if space.kind not in ("HCURL", "HCURL1", "HCURL2"):
+    if not space.kind.startswith("HCURL"):
         raise TypeError(f"{what} needs an HCurl space, got {space.kind}")
 
 
@@ -787,7 +789,7 @@ def MaxwellDoubleLayerPotentialOperator(trial_space, test_space, kappa, trial_de
     trace n x u of the HCurl trial space and the identity trace of the test space (HDivSurface,
     as in the reference's Maxwell tests, or HCurl).  method "dense" gives one root block."""
     _need_hcurl(trial_space, "MaxwellDoubleLayerPotentialOperator (trial space)")
-    if test_space.kind not in ("RT0", "HCURL", "HDIV1", "HDIV2", "HCURL1", "HCURL2"):
+    if not (test_space.kind == "RT0" or test_space.kind.startswith(("HDIV", "HCURL"))):
         raise TypeError("MaxwellDoubleLayerPotentialOperator: the test space must be HDivSurface or HCurl")
     return IntegralOperator("maxwell_dl", _kappa(kappa), trial_space, test_space, "rotatedtrace", "id", intorder,
                             leafsize, eta, eps, method, testhmatrix, trial_definedon=trial_definedon,

@@ -23,7 +23,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 HOST_SOURCES = ["quadrature.cpp", "geometry.cpp", "operator.cpp", "apply.cpp", "gmres.cpp", "energy_host.cpp",
                 "tc_host.cpp", "serialize.cpp", "capi.cpp"]
-CUDA_SOURCES = ["nearfield.cu", "nearfield_l2p12.cu", "nearfield_l2p3r.cu", "nearfield_l2p3s.cu", "nearfield_h1p2.cu", "nearfield_h1p3r.cu", "nearfield_h1p3s.cu", "nearfield_hdiv.cu", "nearfield_hdivs.cu", "aca.cu", "matvec.cu", "mult_noalloc.cu", "energy.cu", "gmres_batch.cu",
+CUDA_SOURCES = ["nearfield.cu", "nearfield_l2p12.cu", "nearfield_l2p3r.cu", "nearfield_l2p3s.cu", "nearfield_h1p2.cu", "nearfield_h1p3r.cu", "nearfield_h1p3s.cu", "nearfield_hdiv.cu", "nearfield_hdivs.cu", "nearfield_hdiv34r.cu", "nearfield_hdiv34s.cu", "aca.cu", "matvec.cu", "mult_noalloc.cu", "energy.cu", "gmres_batch.cu",
                 "tc_matvec.cu", "potential.cu"]
 HEADERS = ["bem_shared.h", "bem_device.cuh", "kernels.h", "host.hpp", "nearfield_kernels.cuh"]
 

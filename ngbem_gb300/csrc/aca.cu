@@ -504,7 +504,7 @@ void launch_aca(int kid, int prec, const AcaArgs& a, cudaStream_t s) {
   X(K_HELMHOLTZ_HS, TR_HELM, TR_HELM)                                                 \
   X(K_MAXWELL_SL, TR_MAX, TR_MAX) X(K_MAXWELL_SL, TR_NEDMAX, TR_NEDMAX)                \
   X(K_MAXWELL_DL, TR_NEDROT, TR_NED) X(K_MAXWELL_DL, TR_NEDROT, TR_RT0ID)  \
-  BEM_L2P_COMBOS(X) BEM_H1P_COMBOS(X) BEM_HDIV_COMBOS(X)
+  BEM_L2P_COMBOS(X) BEM_H1P_COMBOS(X) BEM_HDIV_COMBOS(X) BEM_HDIV34_COMBOS(X)
 
 void launch_projection(int kid, int prec, int trt, int tet, const ProjArgs& a, cudaStream_t s) {
   if (a.nfar <= 0) return;

@@ -366,8 +366,7 @@ void MassOperator::build(SpaceH* trial, SpaceH* test, bool complex_vectors) {
     if (sp.kind >= BEM_L2P1 && sp.kind <= BEM_L2P3) return sp.kind - BEM_L2P1 + 1;
     if (sp.kind == BEM_H1P2) return 2;
     if (sp.kind == BEM_H1P3) return 3;
-    if (sp.kind == BEM_HDIV1 || sp.kind == BEM_HCURL1) return 1;
-    if (sp.kind == BEM_HDIV2 || sp.kind == BEM_HCURL2) return 2;
+    if (bdm_kind_order(sp.kind) > 0) return bdm_kind_order(sp.kind);
     return 1;
   };
   TrigRule r = make_trig_rule(std::max(4, degree(*trial) + degree(*test)));
@@ -390,7 +389,7 @@ void MassOperator::build(SpaceH* trial, SpaceH* test, bool complex_vectors) {
     inv = 1.0 / m.frame(e, xi, eta, x, n, rt, J0, J1);
     piola_offsets(J0, J1, xi, eta, xp);
   };
-  auto shape = [&](const SpaceH& sp, int e, double xi, double eta, double S[12][3], int& dim) {
+  auto shape = [&](const SpaceH& sp, int e, double xi, double eta, double S[30][3], int& dim) {
     double inv, n[3], xp[3][3];
     if (sp.kind == BEM_P0) {
       if (sp.dual) piola(e, xi, eta, inv, n, xp);
@@ -398,11 +397,11 @@ void MassOperator::build(SpaceH* trial, SpaceH* test, bool complex_vectors) {
       dim = 1;
       return;
     }
-    if (sp.kind == BEM_HDIV1 || sp.kind == BEM_HDIV2 || sp.kind == BEM_HCURL1 || sp.kind == BEM_HCURL2) {
+    if (bdm_kind_order(sp.kind) > 0) {
       // the Piola map of the reference fields (hdiv_shape), J = (xp_2 - xp_0, xp_2 - xp_1);
       // HCurl: n x it
-      const int K = sp.kind == BEM_HDIV1 || sp.kind == BEM_HCURL1 ? 1 : 2;
-      const bool curl = sp.kind == BEM_HCURL1 || sp.kind == BEM_HCURL2;
+      const int K = bdm_kind_order(sp.kind);
+      const bool curl = bdm_kind_curl(sp.kind);
       piola(e, xi, eta, inv, n, xp);
       for (int a = 0; a < sp.nd; ++a) {
         const int sg = a < 3 * (K + 1) ? sp.sign[3 * e + a / (K + 1)] : 1;
@@ -448,7 +447,7 @@ void MassOperator::build(SpaceH* trial, SpaceH* test, bool complex_vectors) {
   };
   for (int e = 0; e < m.nt; ++e)
     for (int q = 0; q < nq && trial->on(e) && test->on(e); ++q) {
-      double Si[12][3], Sj[12][3];
+      double Si[30][3], Sj[30][3];
       int di, dj;
       shape(*test, e, r.xi[q], r.eta[q], Si, di);
       shape(*trial, e, r.xi[q], r.eta[q], Sj, dj);

@@ -308,7 +308,12 @@ __device__ __forceinline__ R term_fac(int t, R kappa) {
 //   RT0ID: sigma_a (x - p_opp(a)) / |J|           (HDivSurface identity trace)
 // Local RT0 edge a joins vertices (a, a+1 mod 3); its opposite vertex is (a+2) mod 3.
 // ----------------------------------------------------------------------------------------
-template <int TR> struct TraceInfo;
+// the primary template serves HDivSurface / HCurl of order 1..4 (hdiv_trace)
+template <int TR> struct TraceInfo {
+  static_assert(hdiv_trace(TR), "trace kind without a TraceInfo");
+  static constexpr int ND = (hdiv_order(TR) + 1) * (hdiv_order(TR) + 2);
+  static constexpr int DIM = (bdm_variant(TR) == 1 || bdm_variant(TR) == 4) ? 4 : 3;
+};
 template <> struct TraceInfo<TR_P0> { static constexpr int ND = 1, DIM = 1; };
 template <> struct TraceInfo<TR_P1> { static constexpr int ND = 3, DIM = 1; };
 template <> struct TraceInfo<TR_ROT> { static constexpr int ND = 3, DIM = 3; };
@@ -327,16 +332,6 @@ template <> struct TraceInfo<TR_H1P2ROT> { static constexpr int ND = 6, DIM = 3;
 template <> struct TraceInfo<TR_H1P3ROT> { static constexpr int ND = 10, DIM = 3; };
 template <> struct TraceInfo<TR_H1P2HELM> { static constexpr int ND = 6, DIM = 4; };
 template <> struct TraceInfo<TR_H1P3HELM> { static constexpr int ND = 10, DIM = 4; };
-template <> struct TraceInfo<TR_HDIV1ID> { static constexpr int ND = 6, DIM = 3; };
-template <> struct TraceInfo<TR_HDIV2ID> { static constexpr int ND = 12, DIM = 3; };
-template <> struct TraceInfo<TR_HDIV1MAX> { static constexpr int ND = 6, DIM = 4; };
-template <> struct TraceInfo<TR_HDIV2MAX> { static constexpr int ND = 12, DIM = 4; };
-template <> struct TraceInfo<TR_HCURL1ID> { static constexpr int ND = 6, DIM = 3; };
-template <> struct TraceInfo<TR_HCURL2ID> { static constexpr int ND = 12, DIM = 3; };
-template <> struct TraceInfo<TR_HCURL1ROT> { static constexpr int ND = 6, DIM = 3; };
-template <> struct TraceInfo<TR_HCURL2ROT> { static constexpr int ND = 12, DIM = 3; };
-template <> struct TraceInfo<TR_HCURL1MAX> { static constexpr int ND = 6, DIM = 4; };
-template <> struct TraceInfo<TR_HCURL2MAX> { static constexpr int ND = 12, DIM = 4; };
 // traces that read the element's n x grad(lambda_a) table
 // the geometry of a curved element's rule point (PGeo): normal, rotated gradients, 1 / |J| and
 // the Piola offsets

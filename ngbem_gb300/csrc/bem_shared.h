@@ -22,17 +22,21 @@ enum KernelId {
 // TR_H1P2, TR_H1P3: H1 of order 2, 3 (identity trace); TR_H1P2ROT, TR_H1P3ROT: their surface
 // curl n x grad_Gamma phi (DiffOpBoundaryRot, src/diffops.hpp:12-60, for the hierarchical basis
 // h1p_shape below); TR_H1P2HELM, TR_H1P3HELM: [n x grad_Gamma phi; phi] (DiffOpHelmholtz)
-// TR_HDIV1ID, TR_HDIV2ID: HDivSurface of order 1, 2 (identity trace, the Piola-mapped shape);
-// TR_HDIV1MAX, TR_HDIV2MAX: [shape; surface divergence] (DiffOpMaxwellNew) for hdiv_shape below
-// TR_HCURL1*, TR_HCURL2*: HCurl of order 1, 2, whose shapes are n x the HDivSurface shapes of the
-// same order and dofs: ID n x psi, ROT (DiffOpRotatedTrace) n x (n x psi) = -psi, MAX
-// (DiffOpMaxwell) [-psi; surface curl = surface divergence of psi]
+// TR_HDIVkID: HDivSurface of order k = 1..4 (identity trace, the Piola-mapped shape psi);
+// TR_HDIVkMAX: [psi; surface divergence] (DiffOpMaxwellNew) for hdiv_shape below
+// TR_HCURLk*: HCurl of order k, whose shapes are n x the HDivSurface shapes of the same order and
+// dofs: ID n x psi, ROT (DiffOpRotatedTrace) n x (n x psi) = -psi, MAX (DiffOpMaxwell)
+// [-psi; surface curl = surface divergence of psi]
 enum TraceKind { TR_P0 = 0, TR_P1 = 1, TR_ROT = 2, TR_HELM = 3, TR_MAX = 4, TR_RT0ID = 5,
                  TR_NED = 6, TR_NEDROT = 7, TR_NEDMAX = 8, TR_L2P1 = 9, TR_L2P2 = 10, TR_L2P3 = 11,
                  TR_H1P2 = 12, TR_H1P3 = 13, TR_H1P2ROT = 14, TR_H1P3ROT = 15, TR_H1P2HELM = 16,
-                 TR_H1P3HELM = 17, TR_HDIV1ID = 18, TR_HDIV2ID = 19, TR_HDIV1MAX = 20, TR_HDIV2MAX = 21,
-                 TR_HCURL1ID = 22, TR_HCURL2ID = 23, TR_HCURL1ROT = 24, TR_HCURL2ROT = 25, TR_HCURL1MAX = 26,
-                 TR_HCURL2MAX = 27 };
+                 TR_H1P3HELM = 17,
+                 // HDivSurface / HCurl of order K = 1..4: TR_BDM + 5 (K - 1) + variant
+                 TR_BDM = 18,
+                 TR_HDIV1ID = 18, TR_HDIV1MAX = 19, TR_HCURL1ID = 20, TR_HCURL1ROT = 21, TR_HCURL1MAX = 22,
+                 TR_HDIV2ID = 23, TR_HDIV2MAX = 24, TR_HCURL2ID = 25, TR_HCURL2ROT = 26, TR_HCURL2MAX = 27,
+                 TR_HDIV3ID = 28, TR_HDIV3MAX = 29, TR_HCURL3ID = 30, TR_HCURL3ROT = 31, TR_HCURL3MAX = 32,
+                 TR_HDIV4ID = 33, TR_HDIV4MAX = 34, TR_HCURL4ID = 35, TR_HCURL4ROT = 36, TR_HCURL4MAX = 37 };
 // traces of a discontinuous space of order >= 1: the element's dofs are consecutive
 // (first dof + local index) and its "signs" hold the order of its vertices by global number
 __host__ __device__ constexpr bool l2p_trace(int tr) { return tr >= TR_L2P1 && tr <= TR_L2P3; }
@@ -47,33 +51,36 @@ __host__ __device__ constexpr int h1p_order(int tr) {
 __host__ __device__ constexpr bool h1p_rot(int tr) { return tr >= TR_H1P2ROT && tr <= TR_H1P3HELM; }
 __host__ __device__ constexpr bool h1p_helm(int tr) { return tr == TR_H1P2HELM || tr == TR_H1P3HELM; }
 
-// traces of HDivSurface of order K = 1, 2: per local edge k (vertices k, k + 1 mod 3) K + 1
-// dofs, then (K + 1)(K - 1) interior dofs
-// (also the HCurl traces of order 1, 2: the same dofs and reference fields)
-__host__ __device__ constexpr bool hdiv_trace(int tr) { return tr >= TR_HDIV1ID && tr <= TR_HCURL2MAX; }
-__host__ __device__ constexpr int hdiv_order(int tr) {
-  return tr == TR_HDIV1ID || tr == TR_HDIV1MAX || tr == TR_HCURL1ID || tr == TR_HCURL1ROT || tr == TR_HCURL1MAX ? 1 : 2;
-}
-__host__ __device__ constexpr bool hcurl_hi_trace(int tr) { return tr >= TR_HCURL1ID && tr <= TR_HCURL2MAX; }
+// traces of HDivSurface (and HCurl) of order K = 1..4: per local edge k (vertices k, k + 1 mod 3)
+// K + 1 dofs, then (K + 1)(K - 1) interior dofs
+// (also the HCurl traces of order 1..4: the same dofs and reference fields)
+__host__ __device__ constexpr bool hdiv_trace(int tr) { return tr >= TR_BDM && tr <= TR_HCURL4MAX; }
+__host__ __device__ constexpr int hdiv_order(int tr) { return (tr - TR_BDM) / 5 + 1; }
+__host__ __device__ constexpr int bdm_variant(int tr) { return (tr - TR_BDM) % 5; }
+__host__ __device__ constexpr bool hcurl_hi_trace(int tr) { return hdiv_trace(tr) && bdm_variant(tr) >= 2; }
 // traces that read the unit normal of the point (n x the HDiv shape)
-__host__ __device__ constexpr bool normal_trace(int tr) { return tr == TR_NED || tr == TR_HCURL1ID || tr == TR_HCURL2ID; }
+__host__ __device__ constexpr bool normal_trace(int tr) { return tr == TR_NED || (hdiv_trace(tr) && bdm_variant(tr) == 2); }
+// the trace kind of HDivSurface (curl = false) or HCurl of order k with an evaluator variant:
+// HDivSurface 0 ID, 1 MAXWELL; HCurl 0 ID, 1 ROTATED_TRACE, 2 MAXWELL_CURL
+__host__ __device__ constexpr int bdm_trace(int k, bool curl, int v) { return TR_BDM + 5 * (k - 1) + (curl ? 2 : 0) + v; }
 
-// Hierarchical basis of HDivSurface of order K = 1, 2 (BDM_K: all vector polynomials of degree
-// K; our own choice of basis, spanning the space of NGSolve's HDivSurface(order=K)) as
-// reference fields (vx, vy) on the triangle with vertices (1,0), (0,1), (0,0), in barycentrics
+// Hierarchical basis of HDivSurface of order K = 1..4 (BDM_K: all vector polynomials of degree
+// K; our own choice of basis, spanning the space of NGSolve's HDivSurface(order=K)) as reference
+// fields (vx, vy) on the triangle with vertices (1,0), (0,1), (0,0), in barycentrics
 // l = (xi, eta, 1 - xi - eta); the physical shape is the Piola map J (vx, vy) / |J| and the
 // surface divergence the returned reference divergence / |J|.  rot f = (df/deta, -df/dxi).
 // Local dof a:
 //   a < 3 (K + 1)  edge k = a / (K + 1) between local vertices i = k, j = k + 1 (mod 3),
 //                  m = a % (K + 1):
-//                  m = 0  sg (xhat - vhat_o), o the vertex opposite (the RT0 shape);
-//                  m = 1  rot(l_i l_j);
-//                  m = 2  sg rot(l_i l_j (l_j - l_i))
+//                  m = 0   sg (xhat - vhat_o), o the vertex opposite (the RT0 shape);
+//                  m >= 1  sg^(m-1) rot(l_i l_j (l_j - l_i)^(m-1))
 //                  with sg the edge's orientation (+1 when its first vertex has the lower global
-//                  number), so that the m = 2 field is the surface curl of the global H1 edge
-//                  bubble; surface curls of continuous functions are normal-continuous
-//   a >= 3 (K + 1) (K = 2) interior i = a - 9: l_j l_k rot(l_i), (j, k) the other two vertices,
-//                  zero normal trace on every edge
+//                  number): the surface curls of the global H1 edge bubbles (curls of continuous
+//                  functions are normal-continuous)
+//   a >= 3 (K + 1) interior, zero normal trace on every edge: for i = 0, 1, 2 and the monomials
+//                  xi^p eta^q (p + q <= K - 2; p outer, q inner; for i = 2 only p = 0):
+//                  l_j l_k xi^p eta^q rot(l_i), (j, k) the other two vertices;
+//                  (K + 1)(K - 1) of them
 template <class R>
 __host__ __device__ inline R hdiv_shape(int K, int a, R xi, R eta, int sg, R& vx, R& vy) {
   const R l[3] = {xi, eta, R(1) - xi - eta};
@@ -88,24 +95,55 @@ __host__ __device__ inline R hdiv_shape(int K, int a, R xi, R eta, int sg, R& vx
       vy = R(sg) * (eta - oy);
       return R(2 * sg);
     }
-    // d phi / d l_i and d phi / d l_j of the edge bubble phi
-    R di, dj;
-    if (m == 1) {
-      di = l[j];
-      dj = l[i];
-    } else {
-      di = R(sg) * (l[j] * l[j] - R(2) * l[i] * l[j]);
-      dj = R(sg) * (R(2) * l[i] * l[j] - l[i] * l[i]);
+    // d phi / d l_i and d phi / d l_j of the edge bubble phi = l_i l_j s^e, s = l_j - l_i
+    const int e = m - 1;
+    const R sd = l[j] - l[i];
+    R se = R(1), se1 = R(0);  // s^e, e s^(e-1)
+    for (int t = 0; t < e; ++t) {
+      se1 = se1 * sd + se;
+      se = se * sd;
     }
+    const R q = l[i] * l[j], f = (e & 1) ? R(sg) : R(1);
+    const R di = f * (l[j] * se - q * se1), dj = f * (l[i] * se + q * se1);
     vx = di * rx[i] + dj * rx[j];
     vy = di * ry[i] + dj * ry[j];
     return R(0);
   }
-  const int i = a - 3 * (K + 1), j = (i + 1) % 3, k = (i + 2) % 3;
-  const R f = l[j] * l[k];
+  // interior: find (i, p, q) of index t
+  int t = a - 3 * (K + 1), i = 0, p = 0, q = 0;
+  for (i = 0; i < 3; ++i) {
+    const int cnt = i < 2 ? K * (K - 1) / 2 : K - 1;
+    if (t < cnt) break;
+    t -= cnt;
+  }
+  if (i < 2) {
+    while (t >= K - 1 - p) {
+      t -= K - 1 - p;
+      ++p;
+    }
+    q = t;
+  } else {
+    q = t;
+  }
+  const int j = (i + 1) % 3, k = (i + 2) % 3;
+  R h = R(1), hx = R(0), hy = R(0);  // xi^p eta^q and its derivatives
+  for (int u = 0; u < p; ++u) {
+    hx = hx * xi + h;
+    h = h * xi;
+  }
+  R hq = R(1), hqy = R(0);
+  for (int u = 0; u < q; ++u) {
+    hqy = hqy * eta + hq;
+    hq = hq * eta;
+  }
+  hy = h * hqy;
+  hx = hx * hq;
+  h = h * hq;
+  const R g = l[j] * l[k], gxv = l[k] * gx[j] + l[j] * gx[k], gyv = l[k] * gy[j] + l[j] * gy[k];
+  const R f = g * h;
   vx = f * rx[i];
   vy = f * ry[i];
-  return (l[k] * gx[j] + l[j] * gx[k]) * rx[i] + (l[k] * gy[j] + l[j] * gy[k]) * ry[i];
+  return (gxv * h + g * hx) * rx[i] + (gyv * h + g * hy) * ry[i];
 }
 
 // Hierarchical H1 basis of order P <= 3 on a triangle in barycentric coordinates l[3] (our own

@@ -79,7 +79,7 @@ int bem_mesh_destroy(bem_mesh_t mesh) {
 int bem_space_create(bem_mesh_t mesh, int kind, int dual_mapping, bem_space_t* out) {
   return guarded([&] {
     REQUIRE(mesh && out, "null argument");
-    REQUIRE(kind >= BEM_P0 && kind <= BEM_HCURL2, "unknown space kind");
+    REQUIRE(kind >= BEM_P0 && kind <= BEM_HCURL4, "unknown space kind");
     REQUIRE(!dual_mapping || kind == BEM_P0, "dual mapping is defined for P0 only");
     auto s = std::make_unique<bem_space_s>();
     s->mesh = mesh->m;
@@ -92,7 +92,7 @@ int bem_space_create_on(bem_mesh_t mesh, int kind, int dual_mapping, const unsig
                         bem_space_t* out) {
   return guarded([&] {
     REQUIRE(mesh && out, "null argument");
-    REQUIRE(kind >= BEM_P0 && kind <= BEM_HCURL2, "unknown space kind");
+    REQUIRE(kind >= BEM_P0 && kind <= BEM_HCURL4, "unknown space kind");
     REQUIRE(!dual_mapping || kind == BEM_P0, "dual mapping is defined for P0 only");
     auto s = std::make_unique<bem_space_s>();
     s->mesh = mesh->m;

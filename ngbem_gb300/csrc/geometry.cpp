@@ -377,12 +377,12 @@ void SpaceH::build(MeshH* m, int kind_, int dual_, const unsigned char* mask) {
       }
       for (int j = 0; j < pf; ++j) xd[3 + 3 * pe + j] = f0 + j;
     }
-  } else if (kind == BEM_HDIV1 || kind == BEM_HDIV2 || kind == BEM_HCURL1 || kind == BEM_HCURL2) {
+  } else if (bdm_kind_order(kind) > 0) {
     // HDivSurface of order K: the lowest-order dofs of the edges (by first appearance on the
     // region), then K per edge in the same order, then (K + 1)(K - 1) per element; local dofs
     // per edge k (K + 1 of them), then the interior ones (hdiv_shape); sign: the orientation of
     // local edge k.  global_dof: the dof of the same function in the space on the whole mesh.
-    const int K = kind == BEM_HDIV1 || kind == BEM_HCURL1 ? 1 : 2, nin = (K + 1) * (K - 1);
+    const int K = bdm_kind_order(kind), nin = (K + 1) * (K - 1);
     nd = (K + 1) * (K + 2);
     xdof.assign((size_t)nd * m->nt, -1);
     std::vector<int> emap(m->ne, -1), eord;
@@ -444,10 +444,10 @@ void SpaceH::ensure_device() {
       s4[e] = make_int4(sign[3 * e] * (xd[3] + 1), sign[3 * e + 1] * (xd[3 + pe] + 1),
                         sign[3 * e + 2] * (xd[3 + 2 * pe] + 1), 0);
     }
-    if ((kind == BEM_HDIV1 || kind == BEM_HDIV2 || kind == BEM_HCURL1 || kind == BEM_HCURL2) && on(e)) {
+    if (bdm_kind_order(kind) > 0 && on(e)) {
       // HDivSurface and HCurl of order K: w = the first interior dof; the signs carry (first
       // higher-order dof of the edge + 1)
-      const int K = kind == BEM_HDIV1 || kind == BEM_HCURL1 ? 1 : 2;
+      const int K = bdm_kind_order(kind);
       const int* xd = &xdof[(size_t)nd * e];
       d4[e].w = nd > 3 * (K + 1) ? xd[3 * (K + 1)] : 0;
       s4[e] = make_int4(sign[3 * e] * (xd[1] + 1), sign[3 * e + 1] * (xd[K + 2] + 1),
@@ -480,17 +480,15 @@ int trace_kind(int space_kind, int ev) {
     if (ev == BEM_EV_ID) return TR_RT0ID;
     return -1;
   }
-  if (space_kind == BEM_HDIV1 || space_kind == BEM_HDIV2) {
-    const int q = space_kind - BEM_HDIV1;
-    if (ev == BEM_EV_MAXWELL) return TR_HDIV1MAX + q;
-    if (ev == BEM_EV_ID) return TR_HDIV1ID + q;
-    return -1;
-  }
-  if (space_kind == BEM_HCURL1 || space_kind == BEM_HCURL2) {
-    const int q = space_kind - BEM_HCURL1;
-    if (ev == BEM_EV_ID) return TR_HCURL1ID + q;
-    if (ev == BEM_EV_ROTATED_TRACE) return TR_HCURL1ROT + q;
-    if (ev == BEM_EV_MAXWELL_CURL) return TR_HCURL1MAX + q;
+  if (const int K = bdm_kind_order(space_kind)) {
+    if (!bdm_kind_curl(space_kind)) {
+      if (ev == BEM_EV_ID) return bdm_trace(K, false, 0);
+      if (ev == BEM_EV_MAXWELL) return bdm_trace(K, false, 1);
+      return -1;
+    }
+    if (ev == BEM_EV_ID) return bdm_trace(K, true, 0);
+    if (ev == BEM_EV_ROTATED_TRACE) return bdm_trace(K, true, 1);
+    if (ev == BEM_EV_MAXWELL_CURL) return bdm_trace(K, true, 2);
     return -1;
   }
   if (space_kind == BEM_HCURL) {

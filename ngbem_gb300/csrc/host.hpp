@@ -115,6 +115,20 @@ struct MeshH {
   RuleTables& rule_tables(int order);
 };
 
+// HDivSurface / HCurl of order K >= 1: K (0 for other kinds), and whether the kind is HCurl
+inline int bdm_kind_order(int kind) {
+  switch (kind) {
+    case BEM_HDIV1: case BEM_HCURL1: return 1;
+    case BEM_HDIV2: case BEM_HCURL2: return 2;
+    case BEM_HDIV3: case BEM_HCURL3: return 3;
+    case BEM_HDIV4: case BEM_HCURL4: return 4;
+    default: return 0;
+  }
+}
+inline bool bdm_kind_curl(int kind) {
+  return kind == BEM_HCURL1 || kind == BEM_HCURL2 || kind == BEM_HCURL3 || kind == BEM_HCURL4;
+}
+
 struct ClusterTreeH;
 class LevelTeam;  // host threads kept for the levels of a cluster-tree build (geometry.cpp)
 

@@ -287,6 +287,11 @@ int launch_potential(int kid, int trt, const PotArgs& a, cudaStream_t s);
   X(K_MAXWELL_SL, D##MAX, D##MAX) X(K_MAXWELL_SL, C##MAX, C##MAX) X(K_MAXWELL_DL, C##ROT, D##ID)        \
   X(K_MAXWELL_DL, C##ROT, C##ID)
 #define BEM_HDIV_COMBOS(X) BEM_HDIV_KERNELS(X, TR_HDIV1, TR_HCURL1) BEM_HDIV_KERNELS(X, TR_HDIV2, TR_HCURL2)
+// order 3, 4 (20, 30 dofs per element): the pairings of the reference's Maxwell tests, the single
+// layer on HDivSurface of order 3 and 4 and the double layer from HCurl to HDivSurface of order 3
+#define BEM_HDIV34_COMBOS(X)                                                                 \
+  X(K_MAXWELL_SL, TR_HDIV3MAX, TR_HDIV3MAX) X(K_MAXWELL_DL, TR_HCURL3ROT, TR_HDIV3ID)         \
+  X(K_MAXWELL_SL, TR_HDIV4MAX, TR_HDIV4MAX)
 
 // ---- tensor-core products for several right-hand sides (tc_matvec.cu) ---------------------
 // Operand panels are in the canonical K-major, no-swizzle layout of tcgen05 (core matrices of

@@ -30,6 +30,7 @@ bool nf_combo_supported(int kid, int trt, int tet) {
   BEM_L2P_COMBOS(X)
   BEM_H1P_COMBOS(X)
   BEM_HDIV_COMBOS(X)
+  BEM_HDIV34_COMBOS(X)
 #undef X
   return false;
 }
@@ -49,7 +50,8 @@ void launch_nf_regular(int kid, int prec, int trt, int tet, const NFArgs& a, cud
     return;
   }
   if (hdiv_trace(trt)) {
-    launch_nf_regular_hdiv(kid, prec, trt, tet, a, s);
+    if (hdiv_order(trt) <= 2) launch_nf_regular_hdiv(kid, prec, trt, tet, a, s);
+    else launch_nf_regular_hdiv34(kid, prec, trt, tet, a, s);
     return;
   }
 #define X(K, A, B)                                                                    \
@@ -76,7 +78,8 @@ void launch_nf_singular(int kid, int prec, int trt, int tet, const NFArgs& a, cu
     return;
   }
   if (hdiv_trace(trt)) {
-    launch_nf_singular_hdiv(kid, prec, trt, tet, a, s);
+    if (hdiv_order(trt) <= 2) launch_nf_singular_hdiv(kid, prec, trt, tet, a, s);
+    else launch_nf_singular_hdiv34(kid, prec, trt, tet, a, s);
     return;
   }
 #define X(K, A, B)                                                          \

@@ -104,8 +104,11 @@ __global__ void __launch_bounds__(128) nf_regular_kernel(NFArgs a) {
   const bool duali = a.test.dual != 0, dualj = a.trial.dual != 0;
   const P kappa = (P)a.kappa;
 
+  // element matrices above 144 entries (HDivSurface of order 3, 4) keep their rows in rolled
+  // loops: the matrix lives in (cached) local memory instead of unrolled spill code
+  constexpr int RU = NDI * NDJ > 144 ? 1 : NDI;
   V elmat[NDI][NDJ];
-#pragma unroll
+#pragma unroll RU
   for (int r = 0; r < NDI; ++r)
 #pragma unroll
     for (int c = 0; c < NDJ; ++c) elmat[r][c] = vzero<V>();
@@ -156,7 +159,7 @@ __global__ void __launch_bounds__(128) nf_regular_kernel(NFArgs a) {
 #pragma unroll
     for (int t = 0; t < NT; ++t) {
       const P fac = term_fac<G, P>(t, kappa);
-#pragma unroll
+#pragma unroll RU
       for (int r = 0; r < NDI; ++r) {
         P s = fac * trace_val<TET, P>(r, G::tec(t), rp.x, rp.y, xpi, invi, roti, sgi[r], duali, nx);
 #pragma unroll
@@ -179,7 +182,7 @@ __global__ void __launch_bounds__(128) nf_regular_kernel(NFArgs a) {
     cols[c] = (pos >= 0 && pos < d.n) ? pos : -1;
   }
   V* pool = (V*)a.pool + d.off;
-#pragma unroll
+#pragma unroll RU
   for (int r = 0; r < NDI; ++r)
 #pragma unroll
     for (int c = 0; c < NDJ; ++c)
@@ -392,6 +395,9 @@ void launch_nf_singular_h1p3(int kid, int prec, int trt, int tet, const NFArgs& 
 // HDivSurface and HCurl of order 1, 2 (BEM_HDIV_COMBOS): nearfield_hdiv.cu, nearfield_hdivs.cu
 void launch_nf_regular_hdiv(int kid, int prec, int trt, int tet, const NFArgs& a, cudaStream_t s);
 void launch_nf_singular_hdiv(int kid, int prec, int trt, int tet, const NFArgs& a, cudaStream_t s);
+// order 3, 4 (BEM_HDIV34_COMBOS): nearfield_hdiv34r.cu, nearfield_hdiv34s.cu
+void launch_nf_regular_hdiv34(int kid, int prec, int trt, int tet, const NFArgs& a, cudaStream_t s);
+void launch_nf_singular_hdiv34(int kid, int prec, int trt, int tet, const NFArgs& a, cudaStream_t s);
 // bodies of those launchers: one (kernel, trial trace, test trace) combination
 #define BEM_NF_REGULAR_X3(K, A, B)                                                     \
   if (kid == K && trt == A && tet == B) {                                              \

@@ -142,7 +142,9 @@ __global__ void __launch_bounds__(POT_THREADS) pot_eval_kernel(PotArgs a) {
   X(K_HELMHOLTZ_CF, TR_H1P2, cpx<double>) X(K_HELMHOLTZ_CF, TR_H1P3, cpx<double>)               \
   X(K_MAXWELL_SL, TR_HDIV1MAX, cpx<double>) X(K_MAXWELL_SL, TR_HDIV2MAX, cpx<double>)               \
   X(K_MAXWELL_SL, TR_HCURL1MAX, cpx<double>) X(K_MAXWELL_SL, TR_HCURL2MAX, cpx<double>)             \
-  X(K_MAXWELL_DL, TR_HCURL1ROT, cpx<double>) X(K_MAXWELL_DL, TR_HCURL2ROT, cpx<double>)
+  X(K_MAXWELL_DL, TR_HCURL1ROT, cpx<double>) X(K_MAXWELL_DL, TR_HCURL2ROT, cpx<double>)             \
+  X(K_MAXWELL_SL, TR_HDIV3MAX, cpx<double>) X(K_MAXWELL_SL, TR_HDIV4MAX, cpx<double>)               \
+  X(K_MAXWELL_DL, TR_HCURL3ROT, cpx<double>)
 
 int potential_dim(int kid, int trt) {
 #define X(K, T, V) \

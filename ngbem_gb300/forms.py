@@ -147,10 +147,11 @@ def h1p_shapes(p: int, lam: np.ndarray, signs: np.ndarray) -> np.ndarray:
 
 
 def hdiv_fields(k: int, lam: np.ndarray, signs: np.ndarray):
-    """The HDivSurface basis of order k (1, 2) as reference fields at barycentric points lam
+    """The HDivSurface basis of order k (1..4) as reference fields at barycentric points lam
     (nq, 3) of every triangle with local edge orientations signs (nt, 3): ((nt, nq, nd, 2) fields,
-    (nt, nq, nd) reference divergences) in the library's local order (per edge k: the RT0 shape,
-    the curl (d/deta, -d/dxi) of l_i l_j, of sg l_i l_j (l_j - l_i); then l_j l_k curl(l_i))."""
+    (nt, nq, nd) reference divergences) in the library's local order (per edge: the RT0 shape,
+    the curls (d/deta, -d/dxi) of sg^e l_i l_j (l_j - l_i)^e, e = 0..k-1; then the interior
+    l_j l_k xi^p eta^q curl(l_i), i outer, p + q <= k - 2 with p outer, only p = 0 for i = 2)."""
     nt, nq = signs.shape[0], lam.shape[0]
     dxi, deta = np.array([1.0, 0.0, -1.0]), np.array([0.0, 1.0, -1.0])
     vhat = np.array([[1.0, 0.0], [0.0, 1.0], [0.0, 0.0]])
@@ -162,26 +163,33 @@ def hdiv_fields(k: int, lam: np.ndarray, signs: np.ndarray):
         V.append(sg[:, :, None] * (xy - vhat[o])[None])                    # RT0
         D.append(np.broadcast_to(2.0 * sg, (nt, nq)))
         for m in range(1, k + 1):
+            ex = m - 1
+            s_ = lam[:, j] - lam[:, i]
+            pw = s_ ** ex
+            pw1 = ex * s_ ** (ex - 1) if ex > 0 else np.zeros(nq)
             d = np.zeros((nq, 3))
-            if m == 1:
-                d[:, i], d[:, j] = lam[:, j], lam[:, i]
-                scale = np.ones((nt, 1))
-            else:
-                d[:, i] = lam[:, j] ** 2 - 2 * lam[:, i] * lam[:, j]
-                d[:, j] = 2 * lam[:, i] * lam[:, j] - lam[:, i] ** 2
-                scale = sg
+            d[:, i] = lam[:, j] * pw - lam[:, i] * lam[:, j] * pw1
+            d[:, j] = lam[:, i] * pw + lam[:, i] * lam[:, j] * pw1
+            scale = sg if ex % 2 else np.ones((nt, 1))
             v = np.stack([d @ deta, -(d @ dxi)], axis=1)                   # (nq, 2)
             V.append(scale[:, :, None] * v[None])
             D.append(np.zeros((nt, nq)))
-    if k == 2:
-        for i in range(3):
-            j, kk = (i + 1) % 3, (i + 2) % 3
-            f = lam[:, j] * lam[:, kk]
-            c = np.array([deta[i], -dxi[i]])
-            V.append(np.broadcast_to((f[:, None] * c[None])[None], (nt, nq, 2)))
-            fx = lam[:, kk] * dxi[j] + lam[:, j] * dxi[kk]
-            fy = lam[:, kk] * deta[j] + lam[:, j] * deta[kk]
-            D.append(np.broadcast_to((fx * c[0] + fy * c[1])[None], (nt, nq)))
+    xi, eta = lam[:, 0], lam[:, 1]
+    for i in range(3):
+        j, kk = (i + 1) % 3, (i + 2) % 3
+        for p in range(k - 1):
+            for q in range(k - 1 - p):
+                if i == 2 and p > 0:
+                    continue
+                mon = xi ** p * eta ** q
+                mx = p * xi ** (p - 1) * eta ** q if p > 0 else np.zeros(nq)
+                my = q * xi ** p * eta ** (q - 1) if q > 0 else np.zeros(nq)
+                b = lam[:, j] * lam[:, kk]
+                bx = lam[:, kk] * dxi[j] + lam[:, j] * dxi[kk]
+                by = lam[:, kk] * deta[j] + lam[:, j] * deta[kk]
+                c = np.array([deta[i], -dxi[i]])
+                V.append(np.broadcast_to(((b * mon)[:, None] * c[None])[None], (nt, nq, 2)))
+                D.append(np.broadcast_to(((bx * mon + b * mx) * c[0] + (by * mon + b * my) * c[1])[None], (nt, nq)))
     return np.stack(V, axis=2), np.stack(D, axis=2)
 
 
@@ -198,7 +206,7 @@ def load_vector(space, f, order: int = 6) -> np.ndarray:
     on = dofs[:, 0] >= 0
     x, n, detj, lam, w = _geometry(mesh, order)
     fv = np.asarray(f(x, n))
-    vector = space.kind in ("RT0", "HCURL", "HDIV1", "HDIV2", "HCURL1", "HCURL2")
+    vector = space.kind == "RT0" or space.kind.startswith(("HCURL", "HDIV"))
     multi = fv.ndim == (4 if vector else 3)
     if not multi:
         fv = fv[..., None]
@@ -226,7 +234,7 @@ def load_vector(space, f, order: int = 6) -> np.ndarray:
         nd = phi.shape[-1]
         idx = dofs[on, 0][:, None] + np.arange(nd)[None, :]
         np.add.at(out, idx.ravel(), contrib[on].reshape(-1, contrib.shape[-1]))
-    elif space.kind.startswith("HDIV") or space.kind in ("HCURL1", "HCURL2"):
+    elif space.kind.startswith("HDIV") or (space.kind.startswith("HCURL") and space.kind != "HCURL"):
         # the Piola map J v / |J| of the reference fields, J per element (flat) or per point
         xi, eta, _ = triangle_rule(order)
         if curved:

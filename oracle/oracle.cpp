@@ -310,8 +310,8 @@ struct Mesh {
 };
 
 // SurfaceL2 of order p >= 1 has (p+1)(p+2)/2 dofs per element (at most 10 for p = 3),
-// HDivSurface of order K (K+1)(K+2) (12 for K = 2)
-constexpr int ORC_MAXND = 12;
+// HDivSurface of order K (K+1)(K+2) (30 for K = 4)
+constexpr int ORC_MAXND = 30;
 
 // Dubiner basis function a of order P on a triangle (Dubiner 1991; Karniadakis and Sherwin,
 // Spectral/hp Element Methods, ch. 3), as NGSolve's L2 triangle element uses it (third-party
@@ -341,6 +341,18 @@ static double dubiner(int P, int a, double xi, double eta, int f0, int f1) {
     j0 = j1; j1 = jn; J = jn;
   }
   return L * J;
+}
+
+// HDivSurface / HCurl of order K >= 1: K, else 0
+static int bdm_order(int kind) {
+  if (kind == ORC_HDIV1 || kind == ORC_HCURL1) return 1;
+  if (kind == ORC_HDIV2 || kind == ORC_HCURL2) return 2;
+  if (kind == ORC_HDIV3 || kind == ORC_HCURL3) return 3;
+  if (kind == ORC_HDIV4 || kind == ORC_HCURL4) return 4;
+  return 0;
+}
+static bool bdm_curl(int kind) {
+  return kind == ORC_HCURL1 || kind == ORC_HCURL2 || kind == ORC_HCURL3 || kind == ORC_HCURL4;
 }
 
 struct Space {
@@ -380,10 +392,10 @@ struct Space {
         }
         for (int j = 0; j < pf; ++j) d[3 + 3 * pe + j] = m.nv + m.ne * pe + e * pf + j;
       }
-    } else if (kind == ORC_HDIV1 || kind == ORC_HDIV2 || kind == ORC_HCURL1 || kind == ORC_HCURL2) {
+    } else if (kind >= ORC_HDIV1) {
       // HDivSurface (and HCurl) of order K: per local edge K + 1 dofs (the edge's lowest-order
       // dof = the edge id, then ne + edge K + m - 1), then (K + 1)(K - 1) interior dofs per element
-      const int K = kind == ORC_HDIV1 || kind == ORC_HCURL1 ? 1 : 2, nin = (K + 1) * (K - 1);
+      const int K = bdm_order(kind), nin = (K + 1) * (K - 1);
       nd = (K + 1) * (K + 2);
       ndof = m.ne * (K + 1) + m.nt * nin;
       dofs.resize((size_t)m.nt * nd);
@@ -442,17 +454,24 @@ static void eval_trace(const Mesh& m, const Space& sp, int ev, int e, double xi,
       S[a][0] = dubiner(sp.kind - ORC_L2P1 + 1, a, xi, eta, sp.sign[3 * e], sp.sign[3 * e + 1]);
     return;
   }
-  if (sp.kind == ORC_HDIV1 || sp.kind == ORC_HDIV2 || sp.kind == ORC_HCURL1 || sp.kind == ORC_HCURL2) {
+  if (bdm_order(sp.kind) > 0) {
     // HDivSurface of order K (DiffOpMaxwellNew on NGSolve's HDivSurface element, restated for
     // a hierarchical BDM_K basis of our own): reference fields v on the triangle with vertices
     // (1,0), (0,1), (0,0), Piola-mapped J v / |J|, surface divergence (div v) / |J|.  Per local
     // edge k (vertices i = k, j = k+1; orientation s): m = 0 the RT0 shape s (xhat - vhat_o);
-    // m = 1 the curl (d/deta, -d/dxi) of l_i l_j; m = 2 that of s l_i l_j (l_j - l_i).
-    // Interior (K = 2): l_j l_k curl(l_i).  HCurl of order K: phi = n x those shapes, traces as
-    // on the lowest-order HCurl below (ID phi, ROTATED_TRACE n x phi, MAXWELL_CURL
+    // m >= 1 the curl (d/deta, -d/dxi) of s^(m-1) l_i l_j (l_j - l_i)^(m-1).  Interior: for
+    // i = 0, 1, 2 and the monomials xi^p eta^q (p + q <= K - 2, p outer; only p = 0 for i = 2),
+    // l_j l_k xi^p eta^q curl(l_i).  HCurl of order K: phi = n x those shapes, traces as on the
+    // lowest-order HCurl below (ID phi, ROTATED_TRACE n x phi, MAXWELL_CURL
     // [n x phi; the divergence of the HDiv shape]).
-    const int K = sp.kind == ORC_HDIV1 || sp.kind == ORC_HCURL1 ? 1 : 2;
-    const bool hcurl = sp.kind == ORC_HCURL1 || sp.kind == ORC_HCURL2;
+    const int K = bdm_order(sp.kind);
+    const bool hcurl = bdm_curl(sp.kind);
+    // the interior functions' (i, p, q)
+    std::vector<std::array<int, 3>> inner;
+    for (int i = 0; i < 3; ++i)
+      for (int p = 0; p <= K - 2; ++p)
+        for (int q = 0; p + q <= K - 2; ++q)
+          if (i < 2 || p == 0) inner.push_back({i, p, q});
     const double lam[3] = {xi, eta, 1.0 - xi - eta};
     const double dxi[3] = {1.0, 0.0, -1.0}, deta[3] = {0.0, 1.0, -1.0};  // d lambda / d(xi, eta)
     const double vh[3][2] = {{1.0, 0.0}, {0.0, 1.0}, {0.0, 0.0}};
@@ -467,13 +486,11 @@ static void eval_trace(const Mesh& m, const Space& sp, int ev, int e, double xi,
           dv = 2.0 * sg;
         } else {
           double d[3] = {0.0, 0.0, 0.0};  // d phi / d lambda
-          if (mm == 1) {
-            d[i] = lam[j];
-            d[j] = lam[i];
-          } else {
-            d[i] = sg * (lam[j] * lam[j] - 2.0 * lam[i] * lam[j]);
-            d[j] = sg * (2.0 * lam[i] * lam[j] - lam[i] * lam[i]);
-          }
+          const int ex = mm - 1;
+          const double sd = lam[j] - lam[i], o = (ex % 2) ? sg : 1.0;
+          const double pw = std::pow(sd, ex), pw1 = ex > 0 ? ex * std::pow(sd, ex - 1) : 0.0;
+          d[i] = o * (lam[j] * pw - lam[i] * lam[j] * pw1);
+          d[j] = o * (lam[i] * pw + lam[i] * lam[j] * pw1);
           double px = 0.0, py = 0.0;  // d phi / d xi, d phi / d eta
           for (int t = 0; t < 3; ++t) { px += d[t] * dxi[t]; py += d[t] * deta[t]; }
           vx = py;
@@ -481,13 +498,17 @@ static void eval_trace(const Mesh& m, const Space& sp, int ev, int e, double xi,
           dv = 0.0;
         }
       } else {
-        const int i = a - 3 * (K + 1), j = (i + 1) % 3, k = (i + 2) % 3;
-        const double f = lam[j] * lam[k];
+        const auto& ipq = inner[a - 3 * (K + 1)];
+        const int i = ipq[0], j = (i + 1) % 3, k = (i + 2) % 3, p = ipq[1], q = ipq[2];
+        const double mon = std::pow(xi, p) * std::pow(eta, q);
+        const double mx = p > 0 ? p * std::pow(xi, p - 1) * std::pow(eta, q) : 0.0;
+        const double my = q > 0 ? q * std::pow(xi, p) * std::pow(eta, q - 1) : 0.0;
+        const double b = lam[j] * lam[k];
+        const double bx = lam[k] * dxi[j] + lam[j] * dxi[k], by = lam[k] * deta[j] + lam[j] * deta[k];
         const double cx = deta[i], cy = -dxi[i];  // curl lambda_i
-        vx = f * cx;
-        vy = f * cy;
-        const double fx = lam[k] * dxi[j] + lam[j] * dxi[k], fy = lam[k] * deta[j] + lam[j] * deta[k];
-        dv = fx * cx + fy * cy;
+        vx = b * mon * cx;
+        vy = b * mon * cy;
+        dv = (bx * mon + b * mx) * cx + (by * mon + b * my) * cy;
       }
       double psi[3];
       for (int c = 0; c < 3; ++c) psi[c] = (g.J0[c] * vx + g.J1[c] * vy) / g.detJ;

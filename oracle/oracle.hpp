@@ -47,8 +47,10 @@ enum {
 // ORC_HDIV1, ORC_HDIV2: HDivSurface of order K = 1, 2 (BDM_K): per local edge K + 1 dofs (the
 // edge id, then ne + edge K + m - 1), then (K + 1)(K - 1) per element after all edge dofs
 // ORC_HCURL1, ORC_HCURL2: HCurl of order K = 1, 2: n x the HDIV shapes, the same dofs
+// ORC_HDIV3, ORC_HDIV4, ORC_HCURL3, ORC_HCURL4: the same of order 3, 4
 enum { ORC_P0 = 0, ORC_P1 = 1, ORC_RT0 = 2, ORC_HCURL = 3, ORC_L2P1 = 4, ORC_L2P2 = 5, ORC_L2P3 = 6,
-       ORC_H1P2 = 7, ORC_H1P3 = 8, ORC_HDIV1 = 9, ORC_HDIV2 = 10, ORC_HCURL1 = 11, ORC_HCURL2 = 12 };
+       ORC_H1P2 = 7, ORC_H1P3 = 8, ORC_HDIV1 = 9, ORC_HDIV2 = 10, ORC_HCURL1 = 11, ORC_HCURL2 = 12,
+       ORC_HDIV3 = 13, ORC_HDIV4 = 14, ORC_HCURL3 = 15, ORC_HCURL4 = 16 };
 // trace evaluators; on ORC_HCURL: ID the tangential trace, ROTATED_TRACE DiffOpRotatedTrace,
 // MAXWELL_CURL DiffOpMaxwell
 enum { ORC_EV_ID = 0, ORC_EV_ROT = 1, ORC_EV_HELM = 2, ORC_EV_MAXWELL = 3,
@@ -77,7 +79,7 @@ int orc_set_geometry(int order, int nt, const double* nodes);
 // Trace values of the local dofs of element e at (xi, eta) (for known-answer tests):
 // out[4 a + c] component c of local dof a, dofs[a] its global dof; returns the dofs per element.
 int orc_eval_trace(int nv, const double* xyz, int nt, const int* tri, int kind, int ev, int e, double xi,
-                   double eta, double* out /*48*/, int* dofs /*12*/);
+                   double eta, double* out /*120*/, int* dofs /*30*/);
 
 // Quadrature tables (for known-answer tests).
 int orc_trig_rule(int order, double* xi, double* eta, double* w);            // returns npts

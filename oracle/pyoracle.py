@@ -18,7 +18,8 @@ KERNELS = {"laplace_sl": 0, "laplace_dl": 1, "laplace_hs": 2, "helmholtz_sl": 3,
            "helmholtz_dl": 4, "helmholtz_hs": 5, "helmholtz_cf": 6, "maxwell_sl": 7,
            "helmholtz_sl_dkappa": 8, "maxwell_dl": 9}
 KINDS = {"P0": 0, "P1": 1, "RT0": 2, "HCURL": 3, "L2P1": 4, "L2P2": 5, "L2P3": 6, "H1P2": 7, "H1P3": 8,
-         "HDIV1": 9, "HDIV2": 10, "HCURL1": 11, "HCURL2": 12}
+         "HDIV1": 9, "HDIV2": 10, "HCURL1": 11, "HCURL2": 12, "HDIV3": 13, "HDIV4": 14, "HCURL3": 15,
+         "HCURL4": 16}
 EVALS = {"id": 0, "rot": 1, "helm": 2, "maxwell": 3, "rotatedtrace": 4, "maxwellcurl": 5}
 
 
@@ -120,11 +121,11 @@ def eval_trace(mesh, kind, ev, e, xi, eta):
     _geometry(mesh)
     X = np.ascontiguousarray(mesh.vertices, dtype=np.float64)
     T = np.ascontiguousarray(mesh.triangles, dtype=np.int32)
-    out = np.zeros(48)
-    dofs = np.zeros(12, dtype=np.int32)
+    out = np.zeros(120)
+    dofs = np.zeros(30, dtype=np.int32)
     nd = lib().orc_eval_trace(mesh.nv, _dp(X), mesh.nt, _ip(T), KINDS[kind], EVALS[ev], int(e), float(xi),
                               float(eta), _dp(out), _ip(dofs))
-    return out.reshape(12, 4)[:nd], dofs[:nd]
+    return out.reshape(30, 4)[:nd], dofs[:nd]
 
 
 def ndof(mesh, kind):
@@ -139,7 +140,7 @@ def ndof(mesh, kind):
     if kind.startswith("H1P"):
         p = int(kind[3:])
         return mesh.nv + ne * (p - 1) + mesh.nt * (p - 1) * (p - 2) // 2
-    if kind.startswith("HDIV") or kind in ("HCURL1", "HCURL2"):
+    if kind.startswith("HDIV") or (kind.startswith("HCURL") and kind != "HCURL"):
         k = int(kind[-1])
         return ne * (k + 1) + mesh.nt * (k + 1) * (k - 1)
     return ne

@@ -1,4 +1,4 @@
-"""HDivSurface and HCurl of order 1 and 2 on the GPU against the FP64 oracle (the reference's
+"""HDivSurface and HCurl of order 1 to 4 on the GPU against the FP64 oracle (the reference's
 Maxwell tests use higher orders: tests/test_Maxwell_Mie.py:24, tests/test_Maxwell_Box.py:19-21).
 
 * The Maxwell single layer (DiffOpMaxwellNew traces, src/diffops.hpp:263-338): dense FP64
@@ -11,6 +11,9 @@ Maxwell tests use higher orders: tests/test_Maxwell_Mie.py:24, tests/test_Maxwel
   or HCurl) against the oracle, with their lowest-order blocks the order-0 operators; and the
   Calderon identity of the reference's Maxwell test, V j = (-1/2 M + K) m, on the exact traces
   of a dipole field, whose residual falls with the order.
+* Orders 3 and 4 (the reference's Maxwell tests): the single layer on HDivSurface of order 3, 4,
+  the double layer from HCurl to HDivSurface of order 3 (dense, H-matrix, mixed, potential,
+  mass), and the Calderon identity at order 3.
 """
 import numpy as np
 import pytest
@@ -178,3 +181,76 @@ def test_calderon_identity_higher_order(oracle):
 
         res.append(calderon_residual(mv(V.mat, jh), mv(Kop.mat, mh), mv(M, mh)))
     assert res[1] < 0.8 * res[0] and res[2] < 0.1 * res[1], res
+
+
+@pytest.mark.parametrize("g", [1, 3])
+@pytest.mark.parametrize("K", [3, 4])
+def test_order_3_4_single_layer(oracle, K, g):
+    """The Maxwell single layer on HDivSurface of order 3 and 4 (the orders of the reference's
+    Maxwell tests; 20 and 30 dofs per element) against the oracle, dense, with its lowest-order
+    block the RT0 operator."""
+    m = icosphere(1).Curve(g)
+    sp = nb.HDivSurface(m, order=K, complex=True)
+    D = _op(sp, "dense", intorder_singular=4, intorder_regular=3).mat.to_dense()
+    Do = oracle.dense_matrix("maxwell_sl", m, f"HDIV{K}", kappa=KAPPA, trial_eval="maxwell", intorder_singular=4,
+                             intorder_regular=3)
+    assert rel(D, Do) < 1e-10
+    rt = nb.HDivSurface(m, order=0, complex=True)
+    R = _op(rt, "dense", intorder_singular=4, intorder_regular=3).mat.to_dense()
+    assert rel(D[: rt.ndof, : rt.ndof], R) < 1e-12
+
+
+def test_order_3_double_layer_hmatrix_potential_mass(oracle):
+    m = icosphere(2).Curve(3)
+    HC, HD = nb.HCurl(m, order=3, complex=True), nb.HDivSurface(m, order=3, complex=True)
+    kw = dict(intorder=3, leafsize=40, eps=1e-8)
+    K3 = nb.MaxwellDoubleLayerPotentialOperator(HC, HD, KAPPA, **kw)
+    H = oracle.OracleOperator("maxwell_dl", m, "HCURL3", "HDIV3", kappa=KAPPA, trial_eval="rotatedtrace",
+                              test_eval="id", intorder=3, leafsize=40, eta=2.0, eps=1e-8)
+    b, ob = K3.mat.blocks(), H.blocks()
+    for k in ("rowcl", "colcl", "near"):
+        assert np.array_equal(b[k], ob[k])
+    rng = np.random.default_rng(43)
+    x = rng.standard_normal(HC.ndof) + 1j * rng.standard_normal(HC.ndof)
+    xd = torch.from_numpy(x).cuda()
+    y = (K3.mat * xd).cpu().numpy()
+    assert rel(y, H.mult(x)) < 1e-7
+    y32 = (nb.MaxwellDoubleLayerPotentialOperator(HC, HD, KAPPA, precision="mixed", **kw).mat * xd).cpu().numpy()
+    assert rel(y32, y) < 1e-6
+    pts = np.array([[2.0, 0.3, -0.1], [-1.5, 1.0, 0.5]])
+    val = K3.GetPotential(xd)(pts).cpu().numpy().reshape(len(pts), -1)
+    ref = oracle.potential("maxwell_dl", m, "HCURL3", x, pts, kappa=KAPPA, trial_eval="rotatedtrace", intorder=3)
+    assert rel(val, ref.reshape(len(pts), -1)) < 1e-11
+    M = nb.MassOperator(HC, HD, complex=True)
+    assert rel((M * xd).cpu().numpy(), oracle.mass_matrix(m, "HCURL3", "HDIV3", order=6) @ x) < 1e-12
+
+
+def test_calderon_identity_order_3(oracle):
+    """The identity of the reference's Maxwell test (tests/test_Maxwell_Box.py uses order 3) on
+    the curved sphere: the residual at order 3 is below order 2's."""
+    from _maxwell_fields import calderon_residual, curl, field
+    from ngbem_gb300.forms import load_vector
+    m = icosphere(2).Curve(3)
+    kappa = 1.0
+    res = []
+    for K in (2, 3):
+        HC, HD = nb.HCurl(m, order=K, complex=True), nb.HDivSurface(m, order=K, complex=True)
+
+        def mex(x, n):
+            return -np.cross(np.cross(n, field(x, kappa)), n)
+
+        def jex(x, n):
+            return np.cross(n, curl(x, kappa) / kappa)
+
+        mh = np.linalg.solve(oracle.mass_matrix(m, HC.kind, HC.kind, order=10), load_vector(HC, mex, order=12))
+        jh = np.linalg.solve(oracle.mass_matrix(m, HD.kind, HD.kind, order=10), load_vector(HD, jex, order=12))
+        kw = dict(intorder=7, leafsize=40, eps=1e-11)
+        V = nb.MaxwellSingleLayerPotentialOperator(HD, kappa, **kw)
+        Kop = nb.MaxwellDoubleLayerPotentialOperator(HC, HD, kappa, **kw)
+        M = nb.MassOperator(HC, HD, complex=True)
+
+        def mv(A, v):
+            return (A * torch.from_numpy(np.ascontiguousarray(v)).cuda()).cpu().numpy()
+
+        res.append(calderon_residual(mv(V.mat, jh), mv(Kop.mat, mh), mv(M, mh)))
+    assert res[1] < 0.5 * res[0], res

@@ -1,4 +1,4 @@
-"""HDivSurface and HCurl of order 1 and 2 on the CPU (the reference's Maxwell tests use higher-order
+"""HDivSurface and HCurl of order 1 to 4 on the CPU (the reference's Maxwell tests use higher-order
 HDivSurface: tests/test_Maxwell_Mie.py:24).  The oracle's basis against the properties that
 define the space, and the library's spaces against the oracle's:
 
@@ -11,7 +11,7 @@ define the space, and the library's spaces against the oracle's:
   polynomials of degree K;
 * the lowest-order dofs are the RT0 functions with RT0's numbering;
 * dof tables, cluster trees and partitions of the library equal the oracle's, bit for bit;
-* HCurl of order 1, 2 (n x those shapes): tangential continuity, the order-0 HCurl functions as
+* HCurl of order 1..4 (n x those shapes): tangential continuity, the order-0 HCurl functions as
   its lowest-order part, the library's space and load vectors against the oracle.
 """
 import numpy as np
@@ -42,7 +42,7 @@ def _conormal(X, tri, k):
     return nu
 
 
-@pytest.mark.parametrize("K", [1, 2])
+@pytest.mark.parametrize("K", [1, 2, 3, 4])
 def test_normal_continuity(oracle, K):
     m = ellipsoid(1)
     kind = f"HDIV{K}"
@@ -72,7 +72,7 @@ def test_normal_continuity(oracle, K):
     assert checked == len(seen) > 0  # a closed surface: every edge is shared
 
 
-@pytest.mark.parametrize("K", [1, 2])
+@pytest.mark.parametrize("K", [1, 2, 3, 4])
 def test_divergence_theorem(oracle, K):
     m = icosphere(1)
     kind = f"HDIV{K}"
@@ -93,7 +93,7 @@ def test_divergence_theorem(oracle, K):
         assert np.abs(lhs - rhs).max() < 1e-12 * np.abs(rhs).max()
 
 
-@pytest.mark.parametrize("K", [1, 2])
+@pytest.mark.parametrize("K", [1, 2, 3, 4])
 def test_span(oracle, K):
     """On a flat triangle, every tangential field (a(x) t1 + b(x) t2) with a, b of degree K is a
     combination of the element's functions."""
@@ -116,7 +116,7 @@ def test_span(oracle, K):
                 assert np.abs(A @ c - target.ravel()).max() < 1e-12
 
 
-@pytest.mark.parametrize("K", [1, 2])
+@pytest.mark.parametrize("K", [1, 2, 3, 4])
 def test_lowest_order_dofs_are_rt0(oracle, K):
     m = icosphere(1)
     for e in (0, 30):
@@ -127,7 +127,7 @@ def test_lowest_order_dofs_are_rt0(oracle, K):
             assert np.abs(S[k * (K + 1)] - R[k]).max() < 1e-15
 
 
-@pytest.mark.parametrize("K", [1, 2])
+@pytest.mark.parametrize("K", [1, 2, 3, 4])
 def test_library_space_matches_the_oracle(oracle, K):
     m = ellipsoid(3).Curve(2)
     kind = f"HDIV{K}"
@@ -149,7 +149,7 @@ def test_library_space_matches_the_oracle(oracle, K):
         assert np.array_equal(part[k], ob[k])
 
 
-@pytest.mark.parametrize("K", [1, 2])
+@pytest.mark.parametrize("K", [1, 2, 3, 4])
 def test_hcurl_tangential_continuity_and_lowest_order(oracle, K):
     """HCurl of order K (n x the HDivSurface shapes): the tangential component along every edge
     is the same from both sides, and the lowest-order dofs are the order-0 HCurl functions."""
@@ -182,7 +182,7 @@ def test_hcurl_tangential_continuity_and_lowest_order(oracle, K):
             assert np.abs(S[k * (K + 1)] - R[k]).max() < 1e-15
 
 
-@pytest.mark.parametrize("K", [1, 2])
+@pytest.mark.parametrize("K", [1, 2, 3, 4])
 def test_hcurl_library_space_and_load_vector(oracle, K):
     from ngbem_gb300.forms import _geometry, load_vector
     m = icosphere(2).Curve(3)
