@@ -58,4 +58,4 @@ def test_factory_argument_checks():
     with pytest.raises(TypeError):
         nb.MaxwellSingleLayerPotentialOperatorCurl(RT, 1.0)
     with pytest.raises(NotImplementedError):
-        nb.HCurl(m, order=3)
+        nb.HCurl(m, order=5)
