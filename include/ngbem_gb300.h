@@ -128,7 +128,7 @@ int bem_mesh_num_edges(bem_mesh_t mesh, int* ne);
 int bem_mesh_destroy(bem_mesh_t mesh);
 /* Curved geometry (NGSolve's Mesh.Curve(order), which the reference's tests call before
  * assembly, e.g. tests/test_aca.py:7; the operators then integrate through the curved element
- * maps, mesh->GetTrafo in src/ngbem.cpp:501-737).  order 1: flat triangles; order 2, 3:
+ * maps, mesh->GetTrafo in src/ngbem.cpp:501-737).  order 1: flat triangles; order 2..4:
  * isoparametric Lagrange triangles with nodes[nt][(order+1)(order+2)/2][3]: node (i, j, k),
  * i + j + k = order, at barycentric (i, j, k) / order of the triangle's vertices
  * (v0, v1, v2), listed for i = order..0, j = order-i..0; the corner nodes must equal the

@@ -290,7 +290,7 @@ __host__ __device__ inline void piola_offsets(const double* J0, const double* J1
 __host__ __device__ inline void curved_map(int g, const double* P, double xi, double eta, double* x, double* J0,
                                            double* J1) {
   const double l[3] = {xi, eta, 1.0 - xi - eta};
-  double L[3][4], D[3][4];
+  double L[3][5], D[3][5];
   for (int s = 0; s < 3; ++s)
     for (int i = 0; i <= g; ++i) {
       double v = 1.0, d = 0.0;

@@ -88,7 +88,7 @@ void MeshH::build(int nv_, const double* xyz, int nt_, const int* tri) {
 
 void MeshH::set_geometry(int order, const double* nodes) {
   std::lock_guard<std::mutex> lk(mu);
-  if (order < 1 || order > 3) throw Error(BEM_ERR_ARG, "geometry order must be 1, 2 or 3");
+  if (order < 1 || order > 4) throw Error(BEM_ERR_ARG, "geometry order must be 1 to 4");
   if (order > 1 && !nodes) throw Error(BEM_ERR_ARG, "curved geometry needs its nodes");
   if (dev_ready || !tables.empty())
     throw Error(BEM_ERR_STATE, "the mesh is in use: curve it before creating operators on it");

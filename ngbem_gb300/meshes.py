@@ -11,7 +11,7 @@ generators below build deterministic, consistently outward-oriented meshes:
 * ``perturbed_icosphere(level, sigma, seed)``: vertices moved radially by sigma*N(0,1).
 
 ``mesh.Curve(order)`` (NGSolve's ``Mesh.Curve``) makes the triangles isoparametric Lagrange
-elements of order 2 or 3 whose nodes lie on the exact surface (the generators above carry
+elements of order 2 to 4 whose nodes lie on the exact surface (the generators above carry
 their surface's projection; other meshes pass ``project``).
 
 Consistent orientation matters: the common-edge Sauter-Schwab permutation assumes that
@@ -80,7 +80,7 @@ class Mesh:
     def Curve(self, order: int, project=None) -> "Mesh":
         """Curve the triangles (NGSolve's ``Mesh.Curve(order)``, in place; returns the mesh).
 
-        Order 1 keeps flat triangles.  Order 2 or 3 makes each triangle an isoparametric
+        Order 1 keeps flat triangles.  Order 2, 3 or 4 makes each triangle an isoparametric
         Lagrange element: node (i, j, k), i + j + k = order, at barycentric (i, j, k) / order
         of the triangle's vertices (v0, v1, v2), listed for i = order..0, j = order-i..0, is
         moved to the surface by ``project`` (points (n, 3) -> points on the surface; default:
@@ -91,8 +91,8 @@ class Mesh:
         if order == 1:
             self.curve_order, self.curve_nodes = 1, None
             return self
-        if order not in (2, 3):
-            raise ValueError("curved geometry of order 2 or 3")
+        if order not in (2, 3, 4):
+            raise ValueError("curved geometry of order 2 to 4")
         proj = project if project is not None else self.project
         if proj is None:
             raise ValueError("a mesh without a surface projection needs project=")

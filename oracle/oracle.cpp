@@ -258,7 +258,7 @@ struct Mesh {
   void curved(int e, double xi, double eta, double* x, double* J0, double* J1) const {
     const int g = gorder, nn = (g + 1) * (g + 2) / 2;
     const double l[3] = {xi, eta, 1.0 - xi - eta};
-    double L[3][4], D[3][4];
+    double L[3][5], D[3][5];
     for (int s = 0; s < 3; ++s)
       for (int i = 0; i <= g; ++i) lagrange_1d(g, i, l[s], L[s][i], D[s][i]);
     for (int c = 0; c < 3; ++c) x[c] = J0[c] = J1[c] = 0.0;
@@ -1613,7 +1613,7 @@ int orc_potential(int kernel, double kappa, int nv, const double* xyz, int nt, c
 }
 
 int orc_set_geometry(int order, int nt, const double* nodes) {
-  if (order < 1 || order > 3 || nt < 0 || (order > 1 && !nodes)) return -1;
+  if (order < 1 || order > 4 || nt < 0 || (order > 1 && !nodes)) return -1;
   g_geo_order = order;
   g_geo_nt = nt;
   if (order == 1) g_geo_nodes.clear();

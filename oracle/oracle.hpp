@@ -70,7 +70,7 @@ typedef struct {
 int orc_mesh_edges(int nv, int nt, const int* tri, int* edges /*2*3nt*/, int* tri_edges /*3nt*/);
 
 // Geometry of the meshes that the following calls build (a setting of the library, kept until
-// the next call): order 1 flat triangles; order 2, 3 isoparametric Lagrange triangles with
+// the next call): order 1 flat triangles; order 2..4 isoparametric Lagrange triangles with
 // nodes[nt][(order+1)(order+2)/2][3], node (i, j, k) (i + j + k = order) at barycentric
 // (i, j, k) / order of the element's vertices, listed for i = order..0, j = order-i..0.  A
 // mesh with another element count is built flat.  Returns 0, or -1 for a bad order.

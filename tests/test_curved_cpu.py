@@ -24,13 +24,15 @@ from ngbem_gb300.meshes import Mesh, ellipsoid, icosphere
 
 def test_area_converges_with_the_geometry_order(oracle):
     err = {}
-    for g in (1, 2, 3):
-        err[g] = [abs(oracle.mass_matrix(icosphere(lev).Curve(g), "P0", "P0", order=10).sum() - 4 * np.pi)
+    for g in (1, 2, 3, 4):
+        err[g] = [abs(oracle.mass_matrix(icosphere(lev).Curve(g), "P0", "P0", order=12).sum() - 4 * np.pi)
                   for lev in (1, 2)]
     assert 3.5 < err[1][0] / err[1][1] < 4.5          # h^2
     for g in (2, 3):
         assert err[g][0] / err[g][1] > 12.0            # h^4
         assert err[g][1] < 0.01 * err[1][1]
+    assert err[4][0] / err[4][1] > 48.0                # h^6
+    assert err[4][1] < 0.02 * err[3][1]
 
 
 def test_single_layer_of_one_on_the_curved_sphere(oracle):
@@ -45,7 +47,7 @@ def test_single_layer_of_one_on_the_curved_sphere(oracle):
     assert dev[3] < 0.02 * dev[1]
 
 
-@pytest.mark.parametrize("g", [2, 3])
+@pytest.mark.parametrize("g", [2, 3, 4])
 def test_curve_nodes(g):
     m = ellipsoid(2, (1.0, 0.7, 0.5)).Curve(g)
     G = m.curve_nodes
@@ -70,7 +72,7 @@ def test_curve_nodes(g):
     assert m.Curve(1).curve_order == 1 and m.curve_nodes is None
 
 
-@pytest.mark.parametrize("g", [2, 3])
+@pytest.mark.parametrize("g", [2, 3, 4])
 @pytest.mark.parametrize("kind", ["P0", "P1", "L2P2", "H1P3"])
 def test_cluster_trees_match_the_oracle(oracle, g, kind):
     m = ellipsoid(3).Curve(g)

@@ -64,7 +64,7 @@ def _op(kernel, kappa, mesh, tr, te, ev_tr, ev_te, method="aca", precision="fp64
     return op, s_tr, s_te
 
 
-@pytest.mark.parametrize("g", [2, 3])
+@pytest.mark.parametrize("g", [2, 3, 4])
 @pytest.mark.parametrize("kernel,kappa,tr,te,ev_tr,ev_te", COMBOS, ids=IDS)
 def test_dense_parity(oracle, kernel, kappa, tr, te, ev_tr, ev_te, g):
     m = icosphere(1).Curve(g)
