@@ -11,6 +11,8 @@ define the space, and the library's spaces against the oracle's:
   polynomials of degree K;
 * the lowest-order dofs are the RT0 functions with RT0's numbering;
 * dof tables, cluster trees and partitions of the library equal the oracle's, bit for bit;
+* the reference's Mie test at order 4 with the oracle's operator: the current against the Mie
+  series within the reference's bar;
 * HCurl of order 1..4 (n x those shapes): tangential continuity, the order-0 HCurl functions as
   its lowest-order part, the library's space and load vectors against the oracle.
 """
@@ -207,3 +209,34 @@ def test_hcurl_library_space_and_load_vector(oracle, K):
             S, d = oracle.eval_trace(m, kind, "id", e, xi[q], eta[q])
             ref[d] += w[q] * detj[e, q] * (S[:, :3] @ fv[e, q])
     assert np.abs(b - ref).max() < 1e-13 * np.abs(ref).max()
+
+
+def test_mie_current_at_order_4(oracle):
+    """The reference's Mie test (tests/test_Maxwell_Mie.py: a conducting sphere of radius 0.25,
+    kappa 5, HDivSurface of order 4 on a mesh curved to order 4, intorder 16; L2 error of the
+    current below 0.0015) with the oracle's dense Maxwell single layer at intorder 12 and a
+    direct solve: the current against the Mie series (tests/_mie.py)."""
+    import sys, os
+    sys.path.insert(0, os.path.dirname(__file__))
+    from _mie import mie_current
+    from ngbem_gb300.forms import _geometry, _lagrange, hdiv_fields, load_vector
+    a, kappa = 0.25, 5.0
+    m = icosphere(1, radius=a).Curve(4)
+    sp = nb.HDivSurface(m, order=4, complex=True)
+    V = oracle.dense_matrix("maxwell_sl", m, "HDIV4", kappa=kappa, trial_eval="maxwell", intorder=12)
+    b = load_vector(sp, lambda x, n: 1j * np.stack([np.exp(1j * kappa * x[..., 2]), 0 * x[..., 2],
+                                                   0 * x[..., 2]], -1), order=14)
+    J = np.linalg.solve(V, b)
+    x, n, detj, lam, w = _geometry(m, 12)
+    xi, eta, _ = triangle_rule(12)
+    _, Dxi, Deta = _lagrange(4, xi, eta)
+    J0 = np.einsum("qn,tnc->tqc", Dxi, m.curve_nodes)
+    J1 = np.einsum("qn,tnc->tqc", Deta, m.curve_nodes)
+    fields, _ = hdiv_fields(4, lam, sp.element_dofs()[1])
+    psi = (J0[:, :, None, :] * fields[..., 0, None] + J1[:, :, None, :] * fields[..., 1, None]) / detj[:, :, None, None]
+    Jh = np.einsum("tqac,ta->tqc", psi, J[sp.dof_table()])
+    Jm = mie_current(x.reshape(-1, 3), a, kappa).reshape(x.shape)
+    W = w[None, :] * detj
+    err = np.sqrt(np.einsum("tq,tqc->", W, np.abs(Jh - Jm) ** 2))
+    assert err < 0.0015
+    assert err / np.sqrt(np.einsum("tq,tqc->", W, np.abs(Jm) ** 2)) < 5e-4
