@@ -7,7 +7,8 @@
 // rebuilds the cluster trees from the spaces (deterministic), checks them against the saved
 // permutations and the dofs' elements / vertices / edges, uploads the blocks into fresh device
 // pools and builds the work lists, so the loaded operator applies exactly like the saved one.
-// Little-endian binary, version 1.
+// The mesh's geometry order and a hash of its curved nodes are recorded too, so that an operator
+// is not loaded onto the same triangles with another geometry.  Little-endian binary, version 2.
 #include <climits>
 #include <cstdio>
 #include <cstring>
@@ -19,7 +20,19 @@ namespace bem {
 
 namespace {
 
-const char kMagic[8] = {'N', 'G', 'B', 'E', 'M', 'H', 'M', '1'};
+const char kMagic[8] = {'N', 'G', 'B', 'E', 'M', 'H', 'M', '2'};
+
+// FNV-1a over the bytes of the curved nodes (0 for flat meshes)
+unsigned long long geometry_hash(const MeshH& m) {
+  if (!m.curved()) return 0ull;
+  unsigned long long h = 1469598103934665603ull;
+  const unsigned char* p = reinterpret_cast<const unsigned char*>(m.G.data());
+  for (size_t k = 0; k < m.G.size() * sizeof(double); ++k) {
+    h ^= p[k];
+    h *= 1099511628211ull;
+  }
+  return h;
+}
 
 struct File {
   FILE* f = nullptr;
@@ -150,6 +163,8 @@ void save_operator(const HOperator& op, const char* path) {
   put(f, ts, sizeof(ts));
   put_v<int>(f, op.trial->mesh->nv);
   put_v<int>(f, op.trial->mesh->nt);
+  put_v<int>(f, op.trial->mesh->gorder);
+  put_v<unsigned long long>(f, geometry_hash(*op.trial->mesh));
   put_vec(f, op.ttrial->perm);
   put_vec(f, op.ttest->perm);
   put_vec(f, op.trial->global_dof);  // which elements / vertices / edges the dofs are
@@ -192,6 +207,8 @@ std::unique_ptr<HOperator> load_operator(const char* path, SpaceH* trial, SpaceH
   int ts[6];
   get(f, ts, sizeof(ts));
   const int nv = get_v<int>(f), nt = get_v<int>(f);
+  const int gorder = get_v<int>(f);
+  const unsigned long long ghash = get_v<unsigned long long>(f);
   if (ts[0] != trial->kind || ts[1] != trial->ndof || ts[2] != trial->dual || ts[3] != test->kind ||
       ts[4] != test->ndof || ts[5] != test->dual)
     throw Error(BEM_ERR_ARG, "the spaces do not match the saved operator");
@@ -202,6 +219,8 @@ std::unique_ptr<HOperator> load_operator(const char* path, SpaceH* trial, SpaceH
   test = op->test;
   if (nv != trial->mesh->nv || nt != trial->mesh->nt)
     throw Error(BEM_ERR_ARG, "the spaces do not match the saved operator");
+  if (gorder != trial->mesh->gorder || ghash != geometry_hash(*trial->mesh))
+    throw Error(BEM_ERR_ARG, "the mesh's geometry (flat or curved) differs from the saved operator's");
   op->trt = trace_kind(trial->kind, op->trial_ev);
   op->tet = trace_kind(test->kind, op->test_ev);
   op->cplx = kernel_complex(op->kid);

@@ -72,7 +72,7 @@ def _dense_descriptor_offset(raw, op):
     def count(o):
         return int(np.frombuffer(raw[o:o + 8], dtype=np.int64)[0])
 
-    o = 8 + 4 + 8 + 4 + 4 + 4 + C.sizeof(_lib.Params) + 6 * 4 + 4 + 4
+    o = 8 + 4 + 8 + 4 + 4 + 4 + C.sizeof(_lib.Params) + 6 * 4 + 4 + 4 + 4 + 8  # ... nv, nt, geometry
     for _ in range(4):  # the two permutations and the two dof maps (int32)
         o += 8 + 4 * count(o)
     nb_ = count(o)
@@ -112,3 +112,21 @@ def test_load_refuses_corrupt_files(tmp_path):
         assert e.value.code == 1, name  # BEM_ERR_ARG
     # the intact file still loads
     assert bem.HMatrix.load(str(path), nb.SurfaceL2(m)).info["nblocks"] == V.mat.info["nblocks"]
+
+
+def test_load_refuses_another_geometry(tmp_path):
+    """An operator assembled on a curved mesh does not load onto the flat mesh of the same
+    triangles (nor onto another curving), and loads onto its own."""
+    from ngbem_gb300._lib import BemError
+    mc = icosphere(2).Curve(3)
+    V = nb.SingleLayerPotentialOperator(nb.SurfaceL2(mc), intorder=3, leafsize=20, eps=1e-8)
+    path = tmp_path / "curved.bin"
+    V.mat.save(str(path))
+    for other in (icosphere(2), icosphere(2).Curve(2)):
+        with pytest.raises(BemError) as e:
+            bem.HMatrix.load(str(path), nb.SurfaceL2(other))
+        assert e.value.code == 1
+    W = bem.HMatrix.load(str(path), nb.SurfaceL2(mc))
+    x = torch.from_numpy(np.random.default_rng(2).standard_normal(W.width)).cuda()
+    y, z = W * x, V.mat * x
+    assert (torch.linalg.vector_norm(y - z) / torch.linalg.vector_norm(z)).item() < 1e-12
