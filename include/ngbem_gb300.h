@@ -347,9 +347,10 @@ int bem_operator_tensor_cores(bem_operator_t op, int* state, long long* bytes, i
 int bem_operator_autotune_tc(bem_operator_t op, int reps, int* nstages, double* ms);
 
 /* An assembled H-matrix to a file and back (no counterpart in the reference, which reassembles
- * each session).  The file holds the partition, ranks, dense blocks and factors; loading needs
- * the same trial and test spaces (checked through their cluster trees) and applies exactly
- * like the saved operator.  test may be NULL (= trial). */
+ * each session).  The file holds the partition, ranks, dense blocks and factors, and the mesh's
+ * geometry order with a hash of its curved nodes; loading needs the same trial and test spaces
+ * on the same geometry (checked through their cluster trees and that record) and applies
+ * exactly like the saved operator.  test may be NULL (= trial). */
 int bem_operator_save(bem_operator_t op, const char* path);
 int bem_operator_load(const char* path, bem_space_t trial, bem_space_t test, bem_operator_t* out);
 
