@@ -133,8 +133,8 @@ int bem_mesh_destroy(bem_mesh_t mesh);
  * i + j + k = order, at barycentric (i, j, k) / order of the triangle's vertices
  * (v0, v1, v2), listed for i = order..0, j = order-i..0; the corner nodes must equal the
  * vertices.  Every space lives on curved meshes (RT0 and HCurl through the Piola map of the
- * curved element at each point).  Call before the first operator on the mesh is created
- * (BEM_ERR_STATE after). */
+ * curved element at each point).  Call before the first space on the mesh is created
+ * (BEM_ERR_STATE after: spaces cache cluster trees of the mesh's geometry). */
 int bem_mesh_set_geometry(bem_mesh_t mesh, int order, const double* nodes);
 
 /* Trace space on a mesh (replaces the NGSolve FESpace argument of the factories,

@@ -90,8 +90,8 @@ void MeshH::set_geometry(int order, const double* nodes) {
   std::lock_guard<std::mutex> lk(mu);
   if (order < 1 || order > 4) throw Error(BEM_ERR_ARG, "geometry order must be 1 to 4");
   if (order > 1 && !nodes) throw Error(BEM_ERR_ARG, "curved geometry needs its nodes");
-  if (dev_ready || !tables.empty())
-    throw Error(BEM_ERR_STATE, "the mesh is in use: curve it before creating operators on it");
+  if (dev_ready || !tables.empty() || nspaces.load() > 0)
+    throw Error(BEM_ERR_STATE, "the mesh is in use: curve it before creating spaces on it");
   gorder = order;
   G.clear();
   if (order == 1) return;
@@ -285,6 +285,7 @@ MeshH::RuleTables& MeshH::rule_tables(int order) {
 // ------------------------------------------------------------------------------------------
 void SpaceH::build(MeshH* m, int kind_, int dual_, const unsigned char* mask) {
   mesh = m;
+  m->nspaces.fetch_add(1);
   kind = kind_;
   dual = dual_ ? 1 : 0;
   elems.clear();

@@ -7,6 +7,7 @@
 #include <array>
 #include <climits>
 #include <cstdint>
+#include <atomic>
 #include <map>
 #include <memory>
 #include <mutex>
@@ -91,6 +92,7 @@ struct MeshH {
   // device tables, built on first use
   std::mutex mu;
   bool dev_ready = false;
+  std::atomic<int> nspaces{0};  // spaces built on the mesh (their trees read the geometry)
   DevBuf d_tri, d_rec64, d_gnodes;
   struct RuleTables {
     int nq = 0;

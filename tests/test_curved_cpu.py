@@ -127,6 +127,11 @@ def test_c_abi_rejects_bad_geometry():
         assert _lib.lib.bem_mesh_set_geometry(h, 2, bad.ctypes.data_as(_lib._dp)) == _lib.BEM_ERR_ARG
         assert _lib.lib.bem_mesh_set_geometry(h, 2, G.ctypes.data_as(_lib._dp)) == 0
         assert _lib.lib.bem_mesh_set_geometry(h, 1, None) == 0
+        # once a space lives on the mesh, its geometry is fixed
+        sp = C.c_void_p()
+        assert _lib.lib.bem_space_create(h, 0, 0, C.byref(sp)) == 0
+        assert _lib.lib.bem_mesh_set_geometry(h, 2, G.ctypes.data_as(_lib._dp)) == _lib.BEM_ERR_STATE
+        _lib.lib.bem_space_destroy(sp)
     finally:
         _lib.lib.bem_mesh_destroy(h)
 
