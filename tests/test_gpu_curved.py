@@ -197,3 +197,32 @@ def test_a_mesh_in_use_cannot_be_curved():
     G = np.ascontiguousarray(icosphere(1).Curve(2).curve_nodes)
     rc = _lib.lib.bem_mesh_set_geometry(_MeshHandle.of(m).h, 2, G.ctypes.data_as(_lib._dp))
     assert rc == _lib.BEM_ERR_STATE
+
+
+@pytest.mark.parametrize("b_curved", [True, False], ids=["both-curved", "curved-and-flat"])
+def test_trial_and_test_on_two_curved_meshes(oracle, b_curved):
+    """Trial space on one mesh, test space on another, at least one of them curved: the library
+    joins them into one mesh of the higher geometry order (a flat mesh takes nodes on its flat
+    triangles); the operator equals the block of the oracle's operator on that union."""
+    from ngbem_gb300.meshes import Mesh
+    a = icosphere(2).Curve(3)
+    c = np.array([1.6, 0.3, -0.2])
+    b0 = icosphere(1)
+
+    def proj(x):
+        d = np.asarray(x) - c
+        return c + 0.4 * d / np.linalg.norm(d, axis=-1, keepdims=True)
+
+    b = Mesh(0.4 * b0.vertices + c, b0.triangles, project=proj)
+    bn = Mesh(b.vertices, b.triangles, project=proj if b_curved else (lambda x: np.asarray(x))).Curve(3).curve_nodes
+    if b_curved:
+        b.Curve(3)
+    union = Mesh(np.vstack([a.vertices, b.vertices]), np.vstack([a.triangles, b.triangles + a.nv]))
+    union.curve_order, union.curve_nodes = 3, np.ascontiguousarray(np.vstack([a.curve_nodes, bn]))
+    for k, tr, te, e1, e2, kap in (("laplace_dl", "P1", "P0", "id", "id", 0.0),
+                                   ("maxwell_sl", "RT0", "RT0", "maxwell", "maxwell", 2.0)):
+        trs, tes = nb.TraceSpace(b, tr, complex=kap != 0), nb.TraceSpace(a, te, complex=kap != 0)
+        D = bem.IntegralOperator(k, kap, trs, tes, e1, e2, 3, 10, 2.0, 1e-8, "dense", False).mat.to_dense()
+        Do = oracle.dense_matrix(k, union, tr, te, kappa=kap, trial_eval=e1, test_eval=e2, intorder=3)
+        Db = Do[np.ix_(np.arange(tes.ndof), oracle.ndof(a, tr) + np.arange(trs.ndof))]
+        assert D.shape == Db.shape and rel(D, Db) < 1e-10
