@@ -276,7 +276,8 @@ int bem_operator_status(bem_operator_t op, int* flags, int reset);
  * fault or a hang.  (0, 0) restores normal operation. */
 int bem_operator_test_waits(bem_operator_t op, long long limit, int extra_arrivals);
 
-/* Dense height x width matrix of the operator (row-major, host), for small cases. */
+/* Dense height x width matrix of the operator (row-major, host, in the operator's vector
+ * type), for small cases; mass matrices too (their real entries). */
 int bem_operator_to_dense(bem_operator_t op, void* out);
 
 int bem_operator_destroy(bem_operator_t op);

@@ -546,13 +546,72 @@ class HMatrix(_NativeMatrix):
 class MassMatrix(_NativeMatrix):
     """Sparse Galerkin mass matrix <u, v> of identity traces (rows = test dofs)."""
 
-    def Inverse(self, freedofs=None, tol=1e-14, maxiter=2000):
+    def to_dense(self) -> np.ndarray:
+        """The matrix as a dense (height, width) array (real entries)."""
+        dt = np.complex128 if self.is_complex else np.float64
+        out = np.zeros((self.height, self.width), dtype=dt)
+        check(lib.bem_operator_to_dense(self.h, C.c_void_p(out.ctypes.data)))
+        return out.real.copy() if self.is_complex else out
+
+    def Inverse(self, freedofs=None, tol=1e-14, maxiter=2000, direct_max=12000):
         """The inverse (the role of ``BilinearForm(...).Assemble().mat.Inverse(freedofs=...)`` as
-        the reference's tests use it for GMRes preconditioners): conjugate gradients on the
-        GPU with this matrix's products, to tol relative; dofs outside freedofs map to 0."""
+        the reference's tests use it for GMRes preconditioners); dofs outside freedofs map to 0.
+        Up to direct_max free dofs: a Cholesky factorisation on the GPU, once; above: conjugate
+        gradients with this matrix's products, to tol relative."""
         if self.height != self.width:
             raise ValueError("only square mass matrices have an inverse")
+        nfree = self.height if freedofs is None else int(np.count_nonzero(freedofs))
+        if nfree <= direct_max:
+            return _MassCholesky(self, freedofs)
         return _MassInverse(self, freedofs, tol, maxiter)
+
+
+class _MassCholesky(BaseMatrix):
+    """M^-1 of a symmetric positive definite mass matrix through its Cholesky factor on the GPU,
+    computed once (real M; it applies to real and complex vectors alike)."""
+    any_field = True
+
+    def __init__(self, M, freedofs):
+        torch = _torch()
+        self.height = self.width = M.height
+        self.is_complex = M.is_complex
+        D = M.to_dense()
+        self.free = None if freedofs is None else np.flatnonzero(np.asarray(freedofs, dtype=bool))
+        if self.free is not None:
+            D = D[np.ix_(self.free, self.free)]
+        self.L = torch.linalg.cholesky(torch.from_numpy(np.ascontiguousarray(D)).cuda())
+        self.idx = None if self.free is None else torch.from_numpy(self.free).cuda()
+
+    def _solve(self, x):
+        torch = _torch()
+        b = x if self.idx is None else x[self.idx]
+        if torch.is_complex(b):
+            Lc = self.L.to(b.dtype)
+            z = torch.cholesky_solve(b.reshape(len(b), -1), Lc).reshape(b.shape)
+        else:
+            z = torch.cholesky_solve(b.reshape(len(b), -1), self.L).reshape(b.shape)
+        if self.idx is None:
+            return z
+        out = torch.zeros_like(x)
+        out[self.idx] = z
+        return out
+
+    def _apply(self, trans, alpha, x, beta, y):
+        z = self._solve(x)
+        torch = _torch()
+        z = z.to(y.dtype) if torch.is_complex(y) else z.real
+        if beta == 0.0:
+            y.copy_(alpha * z)
+        else:
+            y.mul_(beta).add_(alpha * z)
+
+    def __mul__(self, x):
+        torch = _torch()
+        if isinstance(x, np.ndarray):
+            return (self * torch.from_numpy(np.ascontiguousarray(x)).cuda()).cpu().numpy()
+        y = torch.zeros(self.height, dtype=x.dtype if x.is_complex() else torch.float64, device=x.device)
+        self._apply(False, 1.0, x, 0.0, y)
+        return y
 
 
 class _MassInverse(BaseMatrix):

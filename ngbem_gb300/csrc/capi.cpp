@@ -1,6 +1,7 @@
 // extern "C" entry points of libngbem_gb300 (declared in include/ngbem_gb300.h).
 // Every call catches C++ exceptions and converts them to an int status plus a
 // thread-local message (bem_last_error).
+#include <algorithm>
 #include <cstring>
 
 #include "host.hpp"
@@ -410,6 +411,17 @@ int bem_operator_test_waits(bem_operator_t op, long long limit, int extra_arriva
 int bem_operator_to_dense(bem_operator_t op, void* out) {
   return guarded([&] {
     REQUIRE(op && out, "null argument");
+    if (auto* m = dynamic_cast<MassOperator*>(op->op.get())) {
+      // the sparse mass matrix (real entries) as a dense row-major array of its vector type
+      const size_t n = (size_t)m->nrows * m->ncols;
+      double* o = (double*)out;
+      const int w = m->cplx ? 2 : 1;
+      std::fill(o, o + n * w, 0.0);
+      for (int i = 0; i < m->nrows; ++i)
+        for (int k = m->h_rowptr[i]; k < m->h_rowptr[i + 1]; ++k)
+          o[((size_t)i * m->ncols + m->h_col[k]) * w] += m->h_val[k];
+      return;
+    }
     auto* h = dynamic_cast<HOperator*>(op->op.get());
     if (!h) throw Error(BEM_ERR_STATE, "not an H-matrix operator");
     h->to_dense(out);
